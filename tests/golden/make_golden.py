@@ -1,0 +1,272 @@
+"""Generate the committed golden fixtures for the space-charge kick.
+
+Run in a container that holds the Ocelot reference checkout (it is not needed
+anywhere else):
+
+    python tests/golden/make_golden.py [--reference /root/reference] [--skip-track]
+
+What it writes (all under tests/golden/):
+
+* ``ref_<case>.npz`` -- seeded beams kicked by the reference's own
+  ``SpaceCharge.apply`` (ocelot/cpbd/sc.py:208-251).  The reference's
+  intermediates are captured by wrapping its public methods ``el_field``,
+  ``potential`` and ``sym_kernel`` on the instance: the charge grid, the
+  potential, the IGF octant, the mesh steps and the field at the particles.
+* ``ref_track_kicks.npz`` -- input/output pairs of selected kicks of the
+  reference's regression scenario ``test_track_with_sp``
+  (unit_tests/ebeam_test/space_charge/space_charge_test.py:54-67, beam and
+  lattice of space_charge_conf.py), captured while the reference tracks.
+* ``track_pin.json`` -- the pin of the oracle against the reference's golden
+  vectors: the same scenario tracked by the reference's ``track()`` with the
+  kick replaced by ``oracle.sc_oracle.sc_apply``, compared particle by
+  particle with ref_results/test_track_with_sp.json at the reference test's
+  own tolerance (1e-12 absolute).
+
+The reference's import of ``pandas`` (not installed here, unused by the kick)
+is satisfied by an empty stub module written to a temporary directory.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle import sc_oracle  # noqa: E402
+
+
+def import_reference(ref_root: str):
+    stub = tempfile.mkdtemp(prefix="pandas_stub_")
+    os.makedirs(os.path.join(stub, "pandas"))
+    with open(os.path.join(stub, "pandas", "__init__.py"), "w") as f:
+        f.write("class DataFrame:\n    pass\n\n\nclass Series:\n    pass\n")
+    sys.path.insert(0, stub)
+    sys.path.insert(0, ref_root)
+    import logging
+    logging.disable(logging.INFO)
+    import ocelot  # noqa: F401
+    return ocelot
+
+
+# name: (n, nmesh, E_GeV, charge, dz, kicks, seed, random_mesh, beam overrides)
+CASES = {
+    "gauss_15": (3000, [15, 15, 15], 0.130, 250e-12, 0.1, 1, 101, False, {}),
+    "aniso_low_energy": (5000, [13, 20, 33], 0.0065, 500e-12, 0.05, 1, 202, False,
+                         dict(sigma_x=200e-6, sigma_y=200e-6, sigma_tau=700e-6)),
+    "random_mesh": (2000, [15, 15, 15], 0.130, 250e-12, 0.1, 2, 303, True, {}),
+    "multi_kick_31": (4000, [31, 31, 31], 0.130, 250e-12, 0.1, 3, 404, False, {}),
+    "even_16": (2500, [16, 16, 16], 0.130, 1e-9, 0.1, 1, 505, False, {}),
+}
+
+
+def run_cases(ref_root: str):
+    import_reference(ref_root)
+    from ocelot.cpbd.sc import SpaceCharge
+    from ocelot.cpbd.beam import ParticleArray
+
+    for name, (n, nmesh, E, charge, dz, kicks, seed, rmesh, over) in CASES.items():
+        rp, q = sc_oracle.gaussian_beam(n, seed, charge=charge, **over)
+        pa = ParticleArray(n)
+        pa.rparticles[:] = rp
+        pa.q_array = q.copy()
+        pa.E = E
+        sc = SpaceCharge(step=1, nmesh_xyz=list(nmesh), random_mesh=rmesh)
+        sc.prepare(None)  # seeds the global numpy RNG with 10 (sc.py:104-107)
+        rec: dict = {}
+        el_field = sc.el_field
+        pot = sc.potential
+        symk = sc.sym_kernel
+
+        def el_field_rec(X, Q, gamma, nxyz):
+            rec.setdefault("xyz_rot", []).append(np.array(X, copy=True))
+            rec.setdefault("gamma0", []).append(gamma)
+            out = el_field(X, Q, gamma, nxyz)
+            rec.setdefault("Exyz", []).append(out.copy())
+            return out
+
+        def pot_rec(qg, steps):
+            rec.setdefault("qgrid", []).append(qg.copy())
+            rec.setdefault("steps", []).append(np.array(steps, copy=True))
+            out = pot(qg, steps)
+            rec.setdefault("phi", []).append(out.copy())
+            return out
+
+        def symk_rec(ijk2, hxyz):
+            out = symk(ijk2, hxyz)
+            rec.setdefault("igf", []).append(out.copy())
+            return out
+
+        sc.el_field, sc.potential, sc.sym_kernel = el_field_rec, pot_rec, symk_rec
+        outs = []
+        draws = []
+        for _ in range(kicks):
+            if rmesh:
+                st = np.random.get_state()
+                draws.append((np.random.uniform(low=1, high=1.1), np.random.uniform(low=-0.5, high=0.5)))
+                np.random.set_state(st)
+            sc.apply(pa, dz)
+            outs.append(pa.rparticles.copy())
+        data = dict(rp_in=rp, q=q, E=E, dz=dz, nmesh=np.array(nmesh), kicks=kicks,
+                    random_mesh=rmesh, rp_out=np.stack(outs),
+                    mesh_draws=np.array(draws) if draws else np.zeros((0, 2)))
+        for k, v in rec.items():
+            data[k] = np.stack([np.asarray(a) for a in v])
+        path = os.path.join(HERE, f"ref_{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
+
+
+def build_track_scenario(ref_root: str):
+    """Lattice and beam of the reference's SC regression test.
+
+    Restates the fixtures of unit_tests/ebeam_test/space_charge/space_charge_conf.py
+    (lattice ``cell`` with SecondTM, beam ``p_array`` seeded with 11 and matched
+    by BeamTransform) so the scenario can be rebuilt outside pytest.
+    """
+    sys.path.insert(0, os.path.join(ref_root, "unit_tests", "ebeam_test", "space_charge"))
+    import space_charge_conf as conf
+    from ocelot import (MagneticLattice, Marker, SecondTM, ParticleArray, Twiss, BeamTransform)
+
+    cell = (Marker(), conf.D_14, conf.C_A1_1_1_I1, conf.D_15, conf.C_A1_1_2_I1, conf.D_15,
+            conf.C_A1_1_3_I1, conf.D_15, conf.C_A1_1_4_I1, conf.D_15, conf.C_A1_1_5_I1, conf.D_15,
+            conf.C_A1_1_6_I1, conf.D_15, conf.C_A1_1_7_I1, conf.D_15, conf.C_A1_1_8_I1, conf.D_22,
+            conf.Q_37_I1, conf.D_23, conf.Q_38_I1)
+    lattice = MagneticLattice(cell, method={'global': SecondTM})
+
+    np.random.seed(11)
+    n = 10000
+    x = np.random.randn(n) * 0.000231507245956
+    px = np.random.randn(n) * 0.000204206874319
+    y = np.random.randn(n) * 0.000231583942392
+    py = np.random.randn(n) * 0.000204272734636
+    cov_t_p = [[6.89508231e-07, -2.98688604e-07], [-2.98688604e-07, 1.87434257e-07]]
+    long_dist = np.random.multivariate_normal((0, 0), cov_t_p, n)
+    p_array = ParticleArray(n=n)
+    p_array.E = 0.0065
+    p_array.rparticles[0] = x
+    p_array.rparticles[1] = px
+    p_array.rparticles[2] = y
+    p_array.rparticles[3] = py
+    p_array.rparticles[4] = long_dist[:, 0]
+    p_array.rparticles[5] = long_dist[:, 1]
+    p_array.q_array = np.ones(n) * 5e-10 / n
+    tws = Twiss()
+    tws.beta_x = 1.59966676201
+    tws.beta_y = 1.60018325757
+    tws.alpha_x = -0.995487979563
+    tws.alpha_y = -0.996116091572
+    tws.mux = 0.0
+    tws.muy = 0.0
+    BeamTransform(tws=tws).apply(p_array, dz=0.0)
+    return lattice, p_array, conf
+
+
+def track_scenario(ref_root: str, proc_factory):
+    from ocelot import Navigator, track
+    lattice, p_array, conf = build_track_scenario(ref_root)
+    sc1 = proc_factory(1)
+    sc5 = proc_factory(5)
+    navi = Navigator(lattice)
+    navi.add_physics_proc(sc1, lattice.sequence[0], conf.C_A1_1_2_I1)
+    navi.add_physics_proc(sc5, conf.C_A1_1_2_I1, lattice.sequence[-1])
+    navi.unit_step = 0.02
+    _, p = track(lattice, p_array, navi, print_progress=False)
+    return p
+
+
+def run_track(ref_root: str, keep=(0, 120)):
+    import_reference(ref_root)
+    from ocelot.cpbd.sc import SpaceCharge
+    from ocelot.cpbd.physics_proc import PhysProc
+
+    golden = json.load(open(os.path.join(
+        ref_root, "unit_tests/ebeam_test/space_charge/ref_results/test_track_with_sp.json")))["p_array"]
+    gold = np.array([[d[k] for k in ("x", "px", "y", "py", "tau", "p")] for d in golden]).T
+
+    kicks = []
+    counter = [0]
+    base_apply = SpaceCharge.apply
+
+    def recording_apply(self, p_array, zstep):
+        i = counter[0]
+        counter[0] += 1
+        rin = p_array.rparticles.copy()
+        base_apply(self, p_array, zstep)
+        if i in keep:
+            kicks.append(dict(index=i, E=p_array.E, dz=zstep, rp_in=rin, rp_out=p_array.rparticles.copy(),
+                              q=p_array.q_array.copy()))
+
+    def make_ref(step):
+        sc = SpaceCharge(step=step)
+        sc.nmesh_xyz = [63, 63, 63]
+        return sc
+
+    SpaceCharge.apply = recording_apply
+    t0 = time.time()
+    p_ref = track_scenario(ref_root, make_ref)
+    t_ref = time.time() - t0
+    SpaceCharge.apply = base_apply
+    n_kicks = counter[0]
+
+    class OracleSC(PhysProc):
+        def __init__(self, step):
+            PhysProc.__init__(self, step)
+            self.nmesh_xyz = [63, 63, 63]
+
+        def prepare(self, lat):
+            self.check_step()
+            np.random.seed(10)
+
+        def apply(self, p_array, zstep):
+            sc_oracle.sc_apply(p_array.rparticles, p_array.q_array, p_array.E, zstep, self.nmesh_xyz)
+
+    t0 = time.time()
+    p_orc = track_scenario(ref_root, OracleSC)
+    t_orc = time.time() - t0
+
+    names = ("x", "px", "y", "py", "tau", "p")
+    summary = {
+        "scenario": "unit_tests/ebeam_test/space_charge/space_charge_test.py::test_track_with_sp",
+        "golden": "unit_tests/ebeam_test/space_charge/ref_results/test_track_with_sp.json",
+        "tolerance_abs": 1e-12,
+        "n_particles": int(gold.shape[1]),
+        "n_kicks": n_kicks,
+        "reference_vs_golden_max_abs": {k: float(np.abs(p_ref.rparticles[i] - gold[i]).max()) for i, k in enumerate(names)},
+        "oracle_vs_golden_max_abs": {k: float(np.abs(p_orc.rparticles[i] - gold[i]).max()) for i, k in enumerate(names)},
+        "oracle_vs_reference_max_abs": {k: float(np.abs(p_orc.rparticles[i] - p_ref.rparticles[i]).max()) for i, k in enumerate(names)},
+        "oracle_bit_identical_to_reference": bool(np.array_equal(p_orc.rparticles, p_ref.rparticles)),
+        "seconds_reference": round(t_ref, 1),
+        "seconds_oracle": round(t_orc, 1),
+    }
+    summary["oracle_pinned"] = all(v <= 1e-12 for v in summary["oracle_vs_golden_max_abs"].values())
+    with open(os.path.join(HERE, "track_pin.json"), "w") as f:
+        json.dump(summary, f, indent=1)
+    print(json.dumps(summary, indent=1))
+    data = {}
+    for j, kk in enumerate(kicks):
+        for k, v in kk.items():
+            data[f"k{j}_{k}"] = v
+    data["n_kept"] = len(kicks)
+    path = os.path.join(HERE, "ref_track_kicks.npz")
+    np.savez_compressed(path, **data)
+    print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--skip-track", action="store_true")
+    ap.add_argument("--only-track", action="store_true")
+    a = ap.parse_args()
+    if not a.only_track:
+        run_cases(a.reference)
+    if not a.skip_track:
+        run_track(a.reference)
