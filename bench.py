@@ -1,0 +1,332 @@
+"""Benchmark of the GB300 3D space-charge kick (Ocelot SpaceCharge.apply).
+
+Workload: the 2M-particle / 64^3 precision-form configuration -- a seeded
+uncorrelated 6D Gaussian beam (sigma_x = sigma_y = 50 um, sigma_x' = sigma_y'
+= 1e-5, sigma_tau = 100 um, sigma_delta = 1e-4), 130 MeV, 1 nC split equally,
+one kick of dz = 0.1 m per step.  Synthetic data, no dataset involved.
+
+A step is one kick.  ``value`` is particle-kicks/s of the FP32 form (the
+headline) with the particles resident in HBM, timed with CUDA events around
+each kick; L2 (129 MB, larger than the 112 MB of particles and charges) is
+flushed by writing a 256 MB buffer between timed kicks.  The FP64 form is
+timed the same way and reported beside it.  ``e2e`` is the same metric through
+``SpaceCharge.apply`` on a host ``ParticleArray`` in pinned memory: the
+host->device copy of rparticles and q_array and the device->host copy of
+rparticles are inside the timed region of every step.
+
+--impl reference times the CPU restatement of the reference's algorithm
+(oracle/sc_oracle.py: numpy, scipy.ndimage and scipy.fft on all host cores)
+on the same workload; the reference itself is pure Python and does not run
+on the GPU machine.
+
+N > 1 (torchrun): replicas only -- each rank kicks its own beam, no
+collective on the data path; value = all ranks' particle-kicks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "particle-kicks/s, 2M p/64^3 grid: FP32 vs FP64 form at <=1e-5 rel err; p99 latency"
+N_PART = 2_000_000
+MESH = [64, 64, 64]
+E_GEV = 0.130
+CHARGE = 1e-9
+DZ = 0.1
+SEED = 2024
+
+# algorithmic HBM bytes: rparticles read + write (2 x 48 B) + q read (8 B) per particle,
+# plus the charge grid written and the potential read once (2 x w x N_g)
+B_PER_PARTICLE = 104
+B_KICK_KERNEL_PER_PARTICLE = 96  # gather+kick: rparticles read + write
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def beam(n, seed=SEED):
+    from oracle.sc_oracle import gaussian_beam  # seeded synthetic input generator (numpy)
+    return gaussian_beam(n, seed, charge=CHARGE)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_{os.getpid()}.csv") if os.path.isdir(
+            os.path.join(REPO, "gpurun_out")) else f"/tmp/clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        d = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def time_form(precision, n, steps, warmup, dev, flush):
+    """Device-resident kicks; per-kick CUDA events; per-stage events from the library."""
+    import torch
+    from ocelot_gb300 import SpaceCharge
+    rp, q = beam(n)
+    d_rp = torch.from_numpy(rp).to(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    sc = SpaceCharge(nmesh_xyz=MESH, precision=precision, device=dev)
+    eng = sc.engine()
+    eng.ensure(n)
+    eng.profile(True)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        sc.apply_device(d_rp, d_q, E_GEV, DZ)
+    sc.check()
+    kick_ms, stages, launches = [], {}, 0
+    for _ in range(steps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        sc.apply_device(d_rp, d_q, E_GEV, DZ)
+        b.record(stream)
+        b.synchronize()
+        kick_ms.append(a.elapsed_time(b))
+        st, nl = eng.profile_read()
+        launches += nl
+        for k, v in st.items():
+            stages.setdefault(k, []).append(v)
+    sc.check()
+    eng.profile(False)
+    return kick_ms, {k: sum(v) / len(v) for k, v in stages.items()}, launches
+
+
+def time_e2e(precision, n, steps, warmup, dev):
+    """Through SpaceCharge.apply with host (pinned) buffers; copies inside the timed region."""
+    import numpy as np
+    import torch
+    from ocelot_gb300 import ParticleArray, SpaceCharge
+    rp, q = beam(n)
+    h_rp = torch.empty((6, n), dtype=torch.float64).pin_memory()
+    h_q = torch.empty(n, dtype=torch.float64).pin_memory()
+    h_rp.numpy()[:] = rp
+    h_q.numpy()[:] = q
+    pa = ParticleArray(0)
+    pa.rparticles = h_rp.numpy()
+    pa.q_array = h_q.numpy()
+    pa.E = E_GEV
+    sc = SpaceCharge(nmesh_xyz=MESH, precision=precision, device=dev)
+    for _ in range(warmup):
+        sc.apply(pa, DZ)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sc.apply(pa, DZ)  # H2D, kick, status check, D2H: synchronous per step
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    assert np.isfinite(pa.rparticles).all()
+    return dt, 6 * n * 8 + n * 8, 6 * n * 8
+
+
+def cpu_port(n, kicks_max, budget_s, threads):
+    """The oracle (numpy/scipy restatement of the reference) on the host cores."""
+    from oracle import sc_oracle
+    rp, q = beam(n)
+    sc_oracle.sc_apply(rp, q, E_GEV, DZ, MESH, fft_workers=threads)  # warm-up
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < kicks_max and (time.perf_counter() - t_start < budget_s or len(times) < 1):
+        t0 = time.perf_counter()
+        sc_oracle.sc_apply(rp, q, E_GEV, DZ, MESH, fft_workers=threads)
+        times.append(time.perf_counter() - t0)
+    return n * len(times) / sum(times), len(times)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    per_step = (args.steps + args.warmup)
+    n = N_PART if per_step <= 20 else max(100_000, int(N_PART * 20 / per_step))
+    from oracle import sc_oracle
+    rp, q = beam(n)
+    for _ in range(args.warmup):
+        sc_oracle.sc_apply(rp, q, E_GEV, DZ, MESH, fft_workers=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sc_oracle.sc_apply(rp, q, E_GEV, DZ, MESH, fft_workers=threads)
+    dt = time.perf_counter() - t0
+    value = n * args.steps / dt
+    sample = (f"{n} particles of the 2M/64^3 workload per step, {args.steps} kicks; oracle/sc_oracle.py "
+              f"(numpy + scipy.ndimage, scipy.fft with {threads} workers)")
+    out = {"metric": METRIC, "value": value, "unit": "particle-kicks/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic seeded 6D Gaussian beam",
+           "config": {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step",
+                      "sample_particles": n},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "particle-kicks/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "particle-kicks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_PART)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip timing the FP64 form")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = args.n
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    barrier()
+    with ClockSampler(local) as clk:
+        kick32, stages32, launches32 = time_form("fp32", n, args.steps, args.warmup, dev, flush)
+        barrier()
+    kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
+    e2e_dt, h2d, d2h = time_e2e("fp32", n, args.steps, args.warmup, dev)
+    barrier()
+
+    t32 = sum(kick32) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t32, e2e_dt], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t32, e2e_dt = float(tt[0]), float(tt[1])
+    value = ws * n * args.steps / t32
+    e2e_value = ws * n * args.steps / e2e_dt
+
+    peak, peak_kind = peaks()
+    # dominant kernel: the stage with the largest share of the FP32 kick
+    top = max(stages32, key=stages32.get)
+    kick_ms = stages32["kick"]
+    achieved_kick = B_KICK_KERNEL_PER_PARTICLE * n / (kick_ms * 1e-3) / 1e9
+    whole_ms = statistics.mean(kick32)
+    achieved_whole = (B_PER_PARTICLE * n + 2 * 4 * math.prod(MESH)) / (whole_ms * 1e-3) / 1e9
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            threads = os.cpu_count() or 1
+            v, k = cpu_port(N_PART, 5, 10.0, threads)
+            cpu = {"value": v, "unit": "particle-kicks/s", "cores": threads, "kind": "port",
+                   "sample": f"2M particles, 64^3, {k} kicks of oracle/sc_oracle.py (numpy + scipy.ndimage, "
+                             f"scipy.fft with {threads} workers; the rest single-threaded)"}
+        out = {
+            "metric": METRIC, "value": value, "unit": "particle-kicks/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(kick32),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic seeded 6D Gaussian beam (no dataset)",
+            "config": {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step (FP32 form)",
+                       "n_particles": n, "mesh": MESH, "form": "fp32", "l2": "flushed (256 MB write) between kicks",
+                       "parallelism": f"replicas x{ws}"},
+            "fp64_form": ({"value": n * args.steps / (sum(kick64) / 1e3), "ms_per_step": statistics.mean(kick64),
+                           "stages_ms": stages64} if kick64 else None),
+            "fp32_over_fp64": (statistics.mean(kick64) / statistics.mean(kick32)) if kick64 else None,
+            "stages_ms": stages32,
+            "roofline": {"bound": "hbm", "kernel": "k_kick32 (gather+kick+FP64 accumulate)",
+                         "achieved": achieved_kick, "peak": peak, "unit": "GB/s", "frac": achieved_kick / peak,
+                         "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": B_KICK_KERNEL_PER_PARTICLE * n,
+                         "top_stage": top, "top_stage_ms": stages32[top]},
+            "kick_roofline": {"achieved": achieved_whole, "frac": achieved_whole / peak, "unit": "GB/s",
+                              "algorithmic_bytes_per_kick": B_PER_PARTICLE * n + 2 * 4 * math.prod(MESH)},
+            "e2e": {"value": e2e_value, "unit": "particle-kicks/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches32,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

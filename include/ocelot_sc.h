@@ -1,0 +1,152 @@
+/*
+ * ocelot_sc.h -- C ABI of the GB300 (sm_103a) 3D space-charge kick.
+ *
+ * This library replaces the numerical body of Ocelot's space-charge physics
+ * process, class SpaceCharge in ocelot/cpbd/sc.py.  Every entry point below
+ * names the reference function whose behaviour it reproduces.  Arguments are
+ * plain pointers and sizes: device pointers unless stated otherwise, streams
+ * as cudaStream_t passed through a void*.  No entry point allocates device
+ * memory: the caller owns every buffer, including the workspace sized by
+ * sc_workspace_bytes().  All calls are asynchronous on the given stream
+ * unless stated otherwise; errors in arguments are reported synchronously by
+ * the return code, errors found on the device are latched in the workspace
+ * and read with sc_read_status().
+ *
+ * Return codes: SC_OK or one of the SC_ERR_* values; sc_last_error() gives a
+ * message for the calling thread's last failure.
+ */
+#ifndef OCELOT_SC_H
+#define OCELOT_SC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SC_ABI_VERSION 1
+
+/* precision of a plan */
+#define SC_FP64 0 /* plain form: FP64 end to end, matches sc.py to 1e-10 */
+#define SC_FP32 1 /* precision form: FP32 grid/gather, FP64 IGF and FP64 accumulation */
+
+/* status codes */
+#define SC_OK 0
+#define SC_ERR_ARG 1         /* invalid argument (checked on the host) */
+#define SC_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define SC_ERR_WORKSPACE 3   /* workspace missing, too small or not initialised */
+#define SC_ERR_DEGENERATE 4  /* zero or non-finite beam extent / charge (device) */
+#define SC_ERR_NONFINITE 5   /* non-finite particle coordinate or momentum (device) */
+#define SC_ERR_UNSUPPORTED 6 /* grid too large for the FFT plan */
+
+typedef struct sc_plan sc_plan; /* opaque, host-side only */
+
+/* ---- plan / workspace ------------------------------------------------- */
+
+/* Plan for a mesh of nx*ny*nz cells (SpaceCharge.nmesh_xyz, sc.py:94) in the
+ * given precision.  Each n must be >= 4 (the reference divides the extent by
+ * n-3, sc.py:179).  Host-only object: holds sizes, FFT radix plans and launch
+ * shapes, no device memory. */
+int sc_plan_create(sc_plan** plan, int nx, int ny, int nz, int precision);
+void sc_plan_destroy(sc_plan* plan);
+/* padded FFT lengths chosen for the linear convolution (each >= 2n-1) */
+int sc_plan_fft_shape(const sc_plan* plan, int* mx, int* my, int* mz);
+
+/* Bytes of device workspace for kicks of up to n_max particles. */
+int64_t sc_workspace_bytes(const sc_plan* plan, int64_t n_max);
+/* Prepare a freshly allocated workspace (twiddle tables, empty Green's-function
+ * cache, cleared status).  Required once after allocation. */
+int sc_workspace_init(const sc_plan* plan, void* ws, size_t ws_bytes, void* stream);
+/* Synchronous: waits for the stream, returns the status latched on the
+ * device by the last call using this workspace (SC_OK when none). */
+int sc_read_status(const sc_plan* plan, void* ws, void* stream);
+
+/* Where an intermediate of the last call lives in the workspace, for
+ * inspection: the NGP charge grid of el_field (sc.py:193), the potential
+ * (sc.py:168), the field grids Ex/Ey/Ez (sc.py:195-200), all [nx][ny][nz];
+ * the cell keys (sc.py:192) as uint32[n].  Grids are double for an SC_FP64
+ * plan and float for SC_FP32.  Offsets do not depend on n except for keys. */
+#define SC_REGION_QGRID 0
+#define SC_REGION_PHI 1
+#define SC_REGION_EX 2
+#define SC_REGION_EY 3
+#define SC_REGION_EZ 4
+#define SC_REGION_KEYS 5
+int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t* offset, int64_t* bytes);
+
+/* ---- the kick ---------------------------------------------------------- */
+
+/* SpaceCharge.apply(p_array, zstep)  -- sc.py:208-251.
+ *   rparticles: device, float64, row r of particle i at rparticles[r*ld + i]
+ *               (the 6xN MAD coordinates x, x', y, y', tau, delta),
+ *               rewritten in place like xp_2_xxstg_mad (coord_transform.py:16-54);
+ *   q:          device, float64[n] macro-particle charges (ParticleArray.q_array);
+ *   energy_gev: reference energy (ParticleArray.E);
+ *   zstep:      kick length in metres; 0 returns immediately (sc.py:210-212);
+ *   mesh_scale / mesh_shift: the two draws of random_mesh (sc.py:174-175,
+ *               184-185), or NaN when random_mesh is off.
+ * On a device-side error the particles are left unchanged. */
+int sc_kick(sc_plan* plan, void* ws, size_t ws_bytes, double* rparticles, int64_t ld,
+            const double* q, int64_t n, double energy_gev, double zstep,
+            double mesh_scale, double mesh_shift, void* stream);
+
+/* ---- stages, mirroring SpaceCharge's public methods ------------------- */
+
+/* SpaceCharge.el_field(X, Q, gamma, nxyz) -- sc.py:170-205.
+ *   X: device float64 [n][3] rotated positions; modified in place as the
+ *      reference modifies it (z scaled by gamma);  exyz: device float64 [n][3]. */
+int sc_el_field(sc_plan* plan, void* ws, size_t ws_bytes, double* X, const double* q, int64_t n,
+                double gamma, double mesh_scale, double mesh_shift, double* exyz, void* stream);
+
+/* SpaceCharge.potential(q, steps) -- sc.py:135-168.
+ *   qgrid, phi: device float64 [nx][ny][nz]. */
+int sc_potential(sc_plan* plan, void* ws, size_t ws_bytes, const double* qgrid,
+                 double hx, double hy, double hz, double* phi, void* stream);
+
+/* SpaceCharge.sym_kernel(q.shape, steps) -- sc.py:109-133, always FP64.
+ *   kern: device float64 [nx][ny][nz]. */
+int sc_sym_kernel(sc_plan* plan, void* ws, size_t ws_bytes, double hx, double hy, double hz,
+                  double* kern, void* stream);
+
+/* Stable LSD radix sort of 32-bit cell keys with their particle indices: the
+ * summation order of the deposit, equal to numpy.argsort(keys, kind='stable')
+ * -- it replaces the sequential np.bincount of sc.py:193.
+ *   keys_in: device uint32[n], each < 2^key_bits; keys_out, perm_out: device uint32[n]. */
+int64_t sc_sort_workspace_bytes(int64_t n, int key_bits);
+int sc_sort_keys(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* keys_out,
+                 uint32_t* perm_out, void* ws, size_t ws_bytes, void* stream);
+
+/* ---- transport between kicks ------------------------------------------ */
+
+/* TransferMap.mul_p_array -- transformations/transfer_map.py:40-50:
+ * rparticles <- R . rparticles + B for a first-order map.
+ *   R: host float64[36] row-major (already tilt-rotated, first_order_params.py:26-28);
+ *   B: host float64[6]. */
+int sc_tmap_apply(const double* R, const double* B, double* rparticles, int64_t ld, int64_t n,
+                  void* stream);
+
+/* ---- stage timing (benchmarking) --------------------------------------- */
+
+/* Stages of sc_kick, in launch order: MAD->lab frame (coord_transform.py:57-96,
+ * sc.py:224-239), mesh extent (sc.py:171-186), NGP keys (sc.py:187-192),
+ * radix sort and deposit (sc.py:193), IGF table (sc.py:109-133), Green
+ * spectrum (sc.py:142-149,164), convolution (sc.py:150-168), field grids
+ * (sc.py:195-200), gather + kick + back-transform (sc.py:201-251). */
+#define SC_NSTAGES 10
+/* When enabled, sc_kick records a CUDA event on its stream before the first
+ * stage and after each stage.  Host call; creates or destroys the events. */
+int sc_profile_enable(sc_plan* plan, int enable);
+/* Synchronous (waits for the last event): milliseconds of each stage of the
+ * last profiled sc_kick, and the number of kernels that call launched. */
+int sc_profile_read(sc_plan* plan, float* ms /* [SC_NSTAGES] */, int* n_launches);
+const char* sc_profile_stage_name(int stage);
+
+/* ---- misc -------------------------------------------------------------- */
+const char* sc_last_error(void);
+int sc_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCELOT_SC_H */

@@ -1,0 +1,497 @@
+// C ABI of libocelot_sc: plans, workspace layout, argument checking and the
+// launch sequence of each entry point (see include/ocelot_sc.h).
+#include <math.h>
+#include <stdarg.h>
+#include <stddef.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+#include <string>
+
+#include "sc_common.cuh"
+
+namespace ocsc {
+
+cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_out, double hx, double hy,
+                         double hz, cudaStream_t s);
+cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const KickParams& kp, double hx, double hy,
+                            double hz, cudaStream_t s);
+
+PhysConst phys_const() {
+    // ocelot/common/globals.py:13-24
+    PhysConst c;
+    c.pi = 3.141592653589793;
+    const double speed_of_light = 299792458.0;
+    const double q_e = 1.6021766208e-19;
+    const double m_e_kg = 9.10938215e-31;
+    c.m_e_eV = m_e_kg * pow(speed_of_light, 2.0) / q_e;
+    c.m_e_GeV = c.m_e_eV / 1e+9;
+    const double mu_0 = 4 * c.pi * 1e-7;
+    c.epsilon_0 = 1 / mu_0 / pow(speed_of_light, 2.0);
+    return c;
+}
+
+int choose_fft_length(int n) {
+    const int need = 2 * n - 1;
+    for (int L = 8; L <= 512; L *= 2)
+        if (L >= need) return L;
+    return 0;
+}
+
+bool make_radix_plan(int L, RadixPlan* p) {
+    p->L = L;
+    p->nst = 0;
+    int rem = L;
+    while (rem % 8 == 0 && rem > 1) {
+        if (p->nst >= MAX_STAGES) return false;
+        p->r[p->nst++] = 8;
+        rem /= 8;
+    }
+    while (rem % 4 == 0 && rem > 1) {
+        p->r[p->nst++] = 4;
+        rem /= 4;
+    }
+    while (rem % 2 == 0 && rem > 1) {
+        p->r[p->nst++] = 2;
+        rem /= 2;
+    }
+    return rem == 1;
+}
+
+Layout make_layout(const Plan& p, int64_t n) {
+    Layout L;
+    const size_t rs = p.prec == SC_FP64 ? 8 : 4, cs = 2 * rs;
+    const size_t ncell = (size_t)p.nx * p.ny * p.nz;
+    const size_t Kx = p.Mx / 2 + 1, Ky = p.My / 2 + 1, Kz = p.Mz / 2 + 1;
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t r = o; o += align_up(bytes ? bytes : 1); return r; };
+    L.state = take(sizeof(ScState));
+    L.tw_x = take(cs * p.Mx);
+    L.tw_y = take(cs * p.My);
+    L.tw_z = take(cs * p.Mz);
+    L.part_frame = take(8 * 3 * (size_t)p.part_blocks);
+    L.part_ext = take(8 * 10 * (size_t)p.part_blocks);
+    // n-independent regions first: the Green's-function cache keeps its
+    // offset when the same workspace serves kicks of different n
+    L.qgrid = take(rs * ncell);
+    L.phi = take(rs * ncell);
+    L.ex = take(rs * ncell);
+    L.ey = take(rs * ncell);
+    L.ez = take(rs * ncell);
+    L.igf_ig = take(8 * (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1));
+    L.igf_k1 = take(8 * ncell);
+    L.green_s1 = take(rs * (size_t)p.nx * p.ny * Kz);
+    L.green_s2 = take(rs * (size_t)p.nx * Ky * Kz);
+    L.green = take(rs * Kx * Ky * Kz);
+    L.W = take(cs * (size_t)p.nx * p.My * Kz);
+    L.xp = take(p.prec == SC_FP64 ? 8 * 6 * (size_t)n : 0);
+    L.X = take(rs * 3 * (size_t)n);
+    L.keys = take(4 * (size_t)n);
+    L.sort_keys = take(4 * (size_t)n);
+    L.sort_perm = take(4 * (size_t)n);
+    L.sort_tmp_k = take(4 * (size_t)n);
+    L.sort_tmp_v = take(4 * (size_t)n);
+    const size_t sb = (size_t)((n + 4095) / 4096);
+    L.sort_hist = take(4 * 256 * (sb ? sb : 1));
+    L.sort_tot = take(4 * 256);
+    L.total = o;
+    return L;
+}
+
+template <typename R>
+__global__ void k_init_ws(ScState* st, Cx<R>* tx, int Mx, Cx<R>* ty, int My, Cx<R>* tz, int Mz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        memset(st, 0, sizeof(ScState));
+        st->igf_h[0] = st->igf_h[1] = st->igf_h[2] = NAN;
+        st->ws_magic = WS_MAGIC;
+    }
+    double s, c;
+    if (i < Mx) { sincospi(2.0 * i / Mx, &s, &c); tx[i] = cx<R>((R)c, (R)-s); }
+    if (i < My) { sincospi(2.0 * i / My, &s, &c); ty[i] = cx<R>((R)c, (R)-s); }
+    if (i < Mz) { sincospi(2.0 * i / Mz, &s, &c); tz[i] = cx<R>((R)c, (R)-s); }
+}
+
+cudaError_t launch_init_workspace(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
+    int m = p.Mx > p.My ? p.Mx : p.My;
+    m = m > p.Mz ? m : p.Mz;
+    ScState* st = reinterpret_cast<ScState*>(ws + L.state);
+    if (p.prec == SC_FP64)
+        k_init_ws<double><<<(m + 255) / 256, 256, 0, s>>>(st, (double2*)(ws + L.tw_x), p.Mx, (double2*)(ws + L.tw_y),
+                                                          p.My, (double2*)(ws + L.tw_z), p.Mz);
+    else
+        k_init_ws<float><<<(m + 255) / 256, 256, 0, s>>>(st, (float2*)(ws + L.tw_x), p.Mx, (float2*)(ws + L.tw_y),
+                                                         p.My, (float2*)(ws + L.tw_z), p.Mz);
+    return cudaGetLastError();
+}
+
+template <typename A, typename B>
+__global__ void k_convert(const A* __restrict__ a, B* __restrict__ b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (B)a[i];
+}
+
+}  // namespace ocsc
+
+using namespace ocsc;
+
+struct sc_plan {
+    Plan p;
+    const void* ws_ready;  // workspace initialised by sc_workspace_init for this plan
+    size_t ws_ready_bytes;
+    cudaEvent_t ev[SC_NSTAGES + 1];
+    bool profiling;
+    int last_launches;
+};
+
+static const char* kStageNames[SC_NSTAGES] = {"frame", "extent", "keys", "sort", "deposit",
+                                              "igf", "green", "convolve", "field", "kick"};
+
+static inline void mark(sc_plan* plan, int i, cudaStream_t s) {
+    if (plan->profiling) cudaEventRecord(plan->ev[i], s);
+}
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+static int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* where) {
+    return fail(SC_ERR_CUDA, "%s: %s (%s)", where, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define SC_CUDA(call, where)                          \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+    } while (0)
+
+static int check_ws(const sc_plan* plan, const void* ws, size_t ws_bytes, int64_t n) {
+    if (!ws) return fail(SC_ERR_WORKSPACE, "workspace is NULL");
+    const Layout L = make_layout(plan->p, n);
+    if (ws_bytes < L.total)
+        return fail(SC_ERR_WORKSPACE, "workspace of %zu bytes is smaller than the %zu needed for n=%lld", ws_bytes,
+                    L.total, (long long)n);
+    if (plan->ws_ready != ws || plan->ws_ready_bytes != ws_bytes)
+        return fail(SC_ERR_WORKSPACE, "workspace was not initialised for this plan (call sc_workspace_init)");
+    return SC_OK;
+}
+
+static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energy_gev, double zstep,
+                              double mesh_scale, double mesh_shift) {
+    const PhysConst c = phys_const();
+    KickParams kp;
+    memset(&kp, 0, sizeof kp);
+    kp.n = n;
+    kp.ld = ld;
+    kp.nx = p.nx; kp.ny = p.ny; kp.nz = p.nz;
+    kp.Mx = p.Mx; kp.My = p.My; kp.Mz = p.Mz;
+    // sc.py:214-216 and coord_transform.py:19-20,61
+    kp.gamref = energy_gev / c.m_e_GeV;
+    kp.betaref = sqrt(1 - pow(kp.gamref, -2.0));
+    kp.pref = c.m_e_eV * sqrt(pow(kp.gamref, 2.0) - 1);
+    kp.grbr = kp.gamref * kp.betaref;
+    kp.cdT = zstep / kp.betaref;
+    kp.mesh_scale = mesh_scale;
+    kp.mesh_shift = mesh_shift;
+    kp.m_e_eV = c.m_e_eV;
+    kp.m2 = pow(c.m_e_eV, 2.0);
+    kp.four_pi_eps0 = 4 * c.pi * c.epsilon_0;
+    return kp;
+}
+
+extern "C" {
+
+int sc_abi_version(void) { return SC_ABI_VERSION; }
+
+const char* sc_last_error(void) { return g_err.c_str(); }
+
+int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int precision) {
+    if (!out) return fail(SC_ERR_ARG, "plan pointer is NULL");
+    *out = nullptr;
+    if (nx < 4 || ny < 4 || nz < 4)
+        return fail(SC_ERR_ARG, "nmesh_xyz=[%d,%d,%d]: every mesh dimension must be >= 4", nx, ny, nz);
+    if (precision != SC_FP64 && precision != SC_FP32) return fail(SC_ERR_ARG, "unknown precision %d", precision);
+    Plan p;
+    memset(&p, 0, sizeof p);
+    p.nx = nx; p.ny = ny; p.nz = nz;
+    p.prec = precision;
+    p.Mx = choose_fft_length(nx);
+    p.My = choose_fft_length(ny);
+    p.Mz = choose_fft_length(nz);
+    if (!p.Mx || !p.My || !p.Mz)
+        return fail(SC_ERR_UNSUPPORTED, "nmesh_xyz=[%d,%d,%d]: each dimension must be <= 256", nx, ny, nz);
+    if (!make_radix_plan(p.Mx, &p.rx) || !make_radix_plan(p.My, &p.ry) || !make_radix_plan(p.Mz, &p.rz))
+        return fail(SC_ERR_UNSUPPORTED, "no radix plan");
+    const uint64_t ncell = (uint64_t)nx * ny * nz;
+    int bits = 0;
+    while ((1ull << bits) < ncell) ++bits;
+    p.key_bits = bits;
+    int dev = 0;
+    SC_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    SC_CUDA(cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    p.part_blocks = p.sm_count * 4;
+    sc_plan* h = new (std::nothrow) sc_plan;
+    if (!h) return fail(SC_ERR_ARG, "out of host memory");
+    h->p = p;
+    h->ws_ready = nullptr;
+    h->ws_ready_bytes = 0;
+    h->profiling = false;
+    h->last_launches = 0;
+    for (int i = 0; i <= SC_NSTAGES; ++i) h->ev[i] = nullptr;
+    *out = h;
+    return SC_OK;
+}
+
+void sc_plan_destroy(sc_plan* plan) {
+    if (!plan) return;
+    if (plan->profiling)
+        for (int i = 0; i <= SC_NSTAGES; ++i) cudaEventDestroy(plan->ev[i]);
+    delete plan;
+}
+
+int sc_profile_enable(sc_plan* plan, int enable) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (enable && !plan->profiling) {
+        for (int i = 0; i <= SC_NSTAGES; ++i) SC_CUDA(cudaEventCreate(&plan->ev[i]), "cudaEventCreate");
+        plan->profiling = true;
+    } else if (!enable && plan->profiling) {
+        for (int i = 0; i <= SC_NSTAGES; ++i) cudaEventDestroy(plan->ev[i]);
+        plan->profiling = false;
+    }
+    return SC_OK;
+}
+
+int sc_profile_read(sc_plan* plan, float* ms, int* n_launches) {
+    if (!plan || !ms) return fail(SC_ERR_ARG, "bad arguments");
+    if (!plan->profiling) return fail(SC_ERR_ARG, "profiling is not enabled");
+    SC_CUDA(cudaEventSynchronize(plan->ev[SC_NSTAGES]), "cudaEventSynchronize");
+    for (int i = 0; i < SC_NSTAGES; ++i) SC_CUDA(cudaEventElapsedTime(&ms[i], plan->ev[i], plan->ev[i + 1]), "cudaEventElapsedTime");
+    if (n_launches) *n_launches = plan->last_launches;
+    return SC_OK;
+}
+
+const char* sc_profile_stage_name(int stage) {
+    return (stage >= 0 && stage < SC_NSTAGES) ? kStageNames[stage] : "";
+}
+
+int sc_plan_fft_shape(const sc_plan* plan, int* mx, int* my, int* mz) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (mx) *mx = plan->p.Mx;
+    if (my) *my = plan->p.My;
+    if (mz) *mz = plan->p.Mz;
+    return SC_OK;
+}
+
+int64_t sc_workspace_bytes(const sc_plan* plan, int64_t n_max) {
+    if (!plan || n_max < 0) return -1;
+    return (int64_t)make_layout(plan->p, n_max).total;
+}
+
+int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t* offset, int64_t* bytes) {
+    if (!plan || !offset || !bytes || n_max < 0) return fail(SC_ERR_ARG, "bad arguments");
+    const Layout L = make_layout(plan->p, n_max);
+    const size_t rs = plan->p.prec == SC_FP64 ? 8 : 4;
+    const size_t ncell = (size_t)plan->p.nx * plan->p.ny * plan->p.nz;
+    switch (region) {
+        case SC_REGION_QGRID: *offset = (int64_t)L.qgrid; *bytes = (int64_t)(rs * ncell); break;
+        case SC_REGION_PHI: *offset = (int64_t)L.phi; *bytes = (int64_t)(rs * ncell); break;
+        case SC_REGION_EX: *offset = (int64_t)L.ex; *bytes = (int64_t)(rs * ncell); break;
+        case SC_REGION_EY: *offset = (int64_t)L.ey; *bytes = (int64_t)(rs * ncell); break;
+        case SC_REGION_EZ: *offset = (int64_t)L.ez; *bytes = (int64_t)(rs * ncell); break;
+        case SC_REGION_KEYS: *offset = (int64_t)L.keys; *bytes = (int64_t)(4 * (size_t)n_max); break;
+        default: return fail(SC_ERR_ARG, "unknown region %d", region);
+    }
+    return SC_OK;
+}
+
+int sc_workspace_init(const sc_plan* plan_c, void* ws, size_t ws_bytes, void* stream) {
+    sc_plan* plan = const_cast<sc_plan*>(plan_c);
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (!ws) return fail(SC_ERR_WORKSPACE, "workspace is NULL");
+    const Layout L = make_layout(plan->p, 0);
+    if (ws_bytes < L.total) return fail(SC_ERR_WORKSPACE, "workspace smaller than the fixed part (%zu bytes)", L.total);
+    SC_CUDA(launch_init_workspace(plan->p, L, static_cast<char*>(ws), (cudaStream_t)stream), "init workspace");
+    plan->ws_ready = ws;
+    plan->ws_ready_bytes = ws_bytes;
+    return SC_OK;
+}
+
+int sc_read_status(const sc_plan* plan, void* ws, void* stream) {
+    if (!plan || !ws) return fail(SC_ERR_ARG, "plan or workspace is NULL");
+    const Layout L = make_layout(plan->p, 0);
+    SC_CUDA(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+    int status = 0;
+    SC_CUDA(cudaMemcpy(&status, static_cast<char*>(ws) + L.state + offsetof(ScState, status), sizeof(int),
+                       cudaMemcpyDeviceToHost),
+            "read status");
+    if (status == SC_ERR_DEGENERATE)
+        return fail(status, "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)");
+    if (status == SC_ERR_NONFINITE)
+        return fail(status, "non-finite particle coordinates or momenta (or a particle outside the mesh)");
+    if (status) return fail(status, "device status %d", status);
+    return SC_OK;
+}
+
+int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, const double* q, int64_t n,
+            double energy_gev, double zstep, double mesh_scale, double mesh_shift, void* stream) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (zstep == 0) return SC_OK;  // sc.py:210-212
+    if (n < 1) return fail(SC_ERR_ARG, "n=%lld: the kick needs at least one particle", (long long)n);
+    if (n > 0x7fffffffLL) return fail(SC_ERR_ARG, "n=%lld exceeds 2^31-1", (long long)n);
+    if (!rp || !q) return fail(SC_ERR_ARG, "rparticles or q is NULL");
+    if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
+    if (!(energy_gev > 0) || !isfinite(energy_gev) || !isfinite(zstep))
+        return fail(SC_ERR_ARG, "energy %g GeV / zstep %g invalid", energy_gev, zstep);
+    const PhysConst c = phys_const();
+    if (!(energy_gev / c.m_e_GeV > 1.0)) return fail(SC_ERR_ARG, "energy %g GeV is below the rest mass", energy_gev);
+    int r = check_ws(plan, ws_v, ws_bytes, n);
+    if (r) return r;
+    const Plan& p = plan->p;
+    const Layout L = make_layout(p, n);
+    char* ws = static_cast<char*>(ws_v);
+    cudaStream_t s = (cudaStream_t)stream;
+    const KickParams kp = make_params(p, n, ld, energy_gev, zstep, mesh_scale, mesh_shift);
+    const int passes = (p.key_bits + 7) / 8;
+    mark(plan, 0, s);
+    SC_CUDA(launch_frame(p, L, ws, kp, rp, s), "frame");
+    mark(plan, 1, s);
+    SC_CUDA(launch_extent(p, L, ws, kp, rp, q, s), "extent");
+    mark(plan, 2, s);
+    SC_CUDA(launch_keys(p, L, ws, kp, s), "keys");
+    mark(plan, 3, s);
+    SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),
+                        reinterpret_cast<uint32_t*>(ws + L.sort_perm), reinterpret_cast<uint32_t*>(ws + L.sort_tmp_k),
+                        reinterpret_cast<uint32_t*>(ws + L.sort_tmp_v), reinterpret_cast<uint32_t*>(ws + L.sort_hist),
+                        reinterpret_cast<uint32_t*>(ws + L.sort_tot), s),
+            "sort");
+    mark(plan, 4, s);
+    SC_CUDA(launch_deposit(p, L, ws, q, n, s), "deposit");
+    mark(plan, 5, s);
+    SC_CUDA(launch_igf(p, L, ws, nullptr, false, s), "igf");
+    mark(plan, 6, s);
+    SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
+    mark(plan, 7, s);
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s), "convolve");
+    mark(plan, 8, s);
+    SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
+    mark(plan, 9, s);
+    SC_CUDA(launch_gather_kick(p, L, ws, kp, rp, s), "gather/kick");
+    mark(plan, 10, s);
+    // frame 2, extent 2, keys 1, sort 3 per pass, deposit 1, igf 2, green 3, convolve 5, field 1, kick 1
+    plan->last_launches = 2 + 2 + 1 + 3 * passes + 1 + 2 + 3 + 5 + 1 + 1;
+    return SC_OK;
+}
+
+int sc_el_field(sc_plan* plan, void* ws_v, size_t ws_bytes, double* X, const double* q, int64_t n, double gamma,
+                double mesh_scale, double mesh_shift, double* exyz, void* stream) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (n < 1) return fail(SC_ERR_ARG, "n=%lld: el_field needs at least one particle", (long long)n);
+    if (!X || !q || !exyz) return fail(SC_ERR_ARG, "NULL buffer");
+    if (!(gamma >= 1.0)) return fail(SC_ERR_ARG, "gamma %g < 1", gamma);
+    int r = check_ws(plan, ws_v, ws_bytes, n);
+    if (r) return r;
+    const Plan& p = plan->p;
+    const Layout L = make_layout(p, n);
+    char* ws = static_cast<char*>(ws_v);
+    cudaStream_t s = (cudaStream_t)stream;
+    const KickParams kp = make_params(p, n, n, 1.0, 1.0, mesh_scale, mesh_shift);
+    SC_CUDA(launch_extent_xyz(p, L, ws, kp, X, q, gamma, s), "extent");
+    SC_CUDA(launch_keys(p, L, ws, kp, s), "keys");
+    SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),
+                        reinterpret_cast<uint32_t*>(ws + L.sort_perm), reinterpret_cast<uint32_t*>(ws + L.sort_tmp_k),
+                        reinterpret_cast<uint32_t*>(ws + L.sort_tmp_v), reinterpret_cast<uint32_t*>(ws + L.sort_hist),
+                        reinterpret_cast<uint32_t*>(ws + L.sort_tot), s),
+            "sort");
+    SC_CUDA(launch_deposit(p, L, ws, q, n, s), "deposit");
+    SC_CUDA(launch_igf(p, L, ws, nullptr, false, s), "igf");
+    SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s), "convolve");
+    SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
+    SC_CUDA(launch_gather_xyz(p, L, ws, kp, exyz, s), "gather");
+    return SC_OK;
+}
+
+int sc_potential(sc_plan* plan, void* ws_v, size_t ws_bytes, const double* qgrid, double hx, double hy, double hz,
+                 double* phi, void* stream) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (!qgrid || !phi) return fail(SC_ERR_ARG, "NULL buffer");
+    if (!(hx > 0 && hy > 0 && hz > 0) || !isfinite(hx * hy * hz)) return fail(SC_ERR_ARG, "mesh steps must be > 0");
+    int r = check_ws(plan, ws_v, ws_bytes, 0);
+    if (r) return r;
+    const Plan& p = plan->p;
+    const Layout L = make_layout(p, 0);
+    char* ws = static_cast<char*>(ws_v);
+    cudaStream_t s = (cudaStream_t)stream;
+    const KickParams kp = make_params(p, 0, 0, 1.0, 1.0, NAN, NAN);
+    SC_CUDA(launch_set_mesh(p, L, ws, kp, hx, hy, hz, s), "set mesh");
+    SC_CUDA(launch_igf(p, L, ws, nullptr, false, s), "igf");
+    SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
+    if (p.prec == SC_FP64) {
+        SC_CUDA(launch_convolve(p, L, ws, qgrid, phi, s), "convolve");
+    } else {
+        const size_t ncell = (size_t)p.nx * p.ny * p.nz;
+        k_convert<double, float><<<p.sm_count * 4, 256, 0, s>>>(qgrid, reinterpret_cast<float*>(ws + L.qgrid), ncell);
+        SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s), "convolve");
+        k_convert<float, double><<<p.sm_count * 4, 256, 0, s>>>(reinterpret_cast<float*>(ws + L.phi), phi, ncell);
+        SC_CUDA(cudaGetLastError(), "convert");
+    }
+    return SC_OK;
+}
+
+int sc_sym_kernel(sc_plan* plan, void* ws_v, size_t ws_bytes, double hx, double hy, double hz, double* kern,
+                  void* stream) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (!kern) return fail(SC_ERR_ARG, "NULL buffer");
+    int r = check_ws(plan, ws_v, ws_bytes, 0);
+    if (r) return r;
+    const Layout L = make_layout(plan->p, 0);
+    SC_CUDA(launch_igf_h(plan->p, L, static_cast<char*>(ws_v), kern, hx, hy, hz, (cudaStream_t)stream), "igf");
+    return SC_OK;
+}
+
+int64_t sc_sort_workspace_bytes(int64_t n, int key_bits) {
+    if (n < 0 || key_bits < 0 || key_bits > 32) return -1;
+    return (int64_t)sort_scratch_bytes(n, key_bits);
+}
+
+int sc_sort_keys(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* keys_out, uint32_t* perm_out, void* ws,
+                 size_t ws_bytes, void* stream) {
+    if (n < 0 || n > 0x7fffffffLL) return fail(SC_ERR_ARG, "n=%lld out of range", (long long)n);
+    if (key_bits < 1 || key_bits > 32) return fail(SC_ERR_ARG, "key_bits=%d not in [1,32]", key_bits);
+    if (n == 0) return SC_OK;
+    if (!keys_in || !keys_out || !perm_out) return fail(SC_ERR_ARG, "NULL buffer");
+    if (keys_in == keys_out) return fail(SC_ERR_ARG, "keys_in must not alias keys_out");
+    const size_t need = sort_scratch_bytes(n, key_bits);
+    if (!ws || ws_bytes < need) return fail(SC_ERR_WORKSPACE, "sort workspace needs %zu bytes", need);
+    char* w = static_cast<char*>(ws);
+    const size_t a = align_up(4 * (size_t)n);
+    const size_t nb = (size_t)((n + 4095) / 4096);
+    uint32_t* tk = reinterpret_cast<uint32_t*>(w);
+    uint32_t* tv = reinterpret_cast<uint32_t*>(w + a);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(w + 2 * a);
+    uint32_t* tot = reinterpret_cast<uint32_t*>(w + 2 * a + align_up(256 * nb * 4));
+    SC_CUDA(launch_sort(keys_in, n, key_bits, keys_out, perm_out, tk, tv, hist, tot, (cudaStream_t)stream), "sort");
+    return SC_OK;
+}
+
+int sc_tmap_apply(const double* R, const double* B, double* rp, int64_t ld, int64_t n, void* stream) {
+    if (!R || !B) return fail(SC_ERR_ARG, "R or B is NULL");
+    if (n < 0) return fail(SC_ERR_ARG, "n < 0");
+    if (n == 0) return SC_OK;
+    if (!rp) return fail(SC_ERR_ARG, "rparticles is NULL");
+    if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
+    SC_CUDA(launch_tmap(R, B, rp, ld, n, (cudaStream_t)stream), "tmap");
+    return SC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+// Internal declarations shared by the translation units of libocelot_sc.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/ocelot_sc.h"
+
+namespace ocsc {
+
+// ---------------------------------------------------------------------------
+// complex helpers (float2 / double2)
+// ---------------------------------------------------------------------------
+template <typename R> struct CT;
+template <> struct CT<float> { using T = float2; };
+template <> struct CT<double> { using T = double2; };
+template <typename R> using Cx = typename CT<R>::T;
+
+template <typename R> __host__ __device__ __forceinline__ Cx<R> cx(R a, R b) { Cx<R> c; c.x = a; c.y = b; return c; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    C c; c.x = a.x * b.x - a.y * b.y; c.y = a.x * b.y + a.y * b.x; return c;
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+// multiply by -i (forward) or +i (inverse)
+template <typename C> __device__ __forceinline__ C cmul_mi(C a) { C c; c.x = a.y; c.y = -a.x; return c; }
+template <typename C> __device__ __forceinline__ C cmul_pi(C a) { C c; c.x = -a.y; c.y = a.x; return c; }
+
+// ---------------------------------------------------------------------------
+// constants: the expressions of ocelot/common/globals.py:13-24 evaluated in
+// IEEE double on the host, so they are bit-identical to the reference's.
+// ---------------------------------------------------------------------------
+struct PhysConst {
+    double pi, m_e_eV, m_e_GeV, epsilon_0;
+};
+PhysConst phys_const();
+
+// ---------------------------------------------------------------------------
+// device-resident state of one workspace (first bytes of the workspace)
+// ---------------------------------------------------------------------------
+struct ScState {
+    // velocity frame (sc.py:224-239); T[i][j] = component i of basis vector j
+    double T[3][3];
+    double Pav, gamma0, beta0;
+    double kxy, kz;              // cdT*(1-beta0^2) and cdT (sc.py:244-248)
+    // mesh (sc.py:171-186)
+    double steps[3];
+    double xoff[3];
+    double phi_denom;            // 4*pi*eps0*hx*hy*hz (sc.py:167)
+    double phi_norm;             // 1/(Mx*My*Mz) of the inverse FFT
+    // Green's-function cache: spacing of the spectrum held in the workspace
+    double igf_h[3];
+    int igf_rebuild;             // 1 when the current call rebuilds it
+    int status;                  // SC_OK or a device-side SC_ERR_*
+    int ws_magic;                // set by sc_workspace_init
+    int pad;
+};
+constexpr int WS_MAGIC = 0x5c6b0e11;
+
+// host-computed scalars of one kick
+struct KickParams {
+    int64_t n, ld;
+    int nx, ny, nz;
+    int Mx, My, Mz;
+    double gamref, betaref, pref, grbr;  // grbr = gamref*betaref
+    double cdT;                          // zstep / betref
+    double mesh_scale, mesh_shift;       // NaN when unused
+    double m_e_eV, m2;                   // m_e_eV and m_e_eV**2
+    double four_pi_eps0;                 // 4*pi*epsilon_0
+};
+
+// ---------------------------------------------------------------------------
+// FFT geometry and radix plans
+// ---------------------------------------------------------------------------
+constexpr int MAX_STAGES = 8;
+struct RadixPlan {
+    int L;
+    int nst;
+    int r[MAX_STAGES];
+};
+bool make_radix_plan(int L, RadixPlan* p);
+int choose_fft_length(int n);  // smallest supported length >= 2n-1, 0 if none
+
+// ---------------------------------------------------------------------------
+// workspace layout (offsets in bytes from the workspace base)
+// ---------------------------------------------------------------------------
+struct Layout {
+    size_t state, tw_x, tw_y, tw_z;              // twiddles (Cx<R>[M])
+    size_t part_frame, part_ext;                 // per-block partial sums (double)
+    size_t xp;                                   // FP64: 6 x n lab coordinates
+    size_t X;                                    // 3 x n grid coordinates (R)
+    size_t keys, sort_keys, sort_perm, sort_tmp_k, sort_tmp_v, sort_hist, sort_tot;
+    size_t qgrid, phi, ex, ey, ez;               // [nx][ny][nz] (R)
+    size_t igf_ig;                               // (nx+1)(ny+1)(nz+1) double
+    size_t igf_k1;                               // nx*ny*nz double
+    size_t green_s1, green_s2, green;            // spectrum passes (R)
+    size_t W;                                    // complex work grid nx*My*Kz
+    size_t total;
+};
+
+struct Plan {
+    int nx, ny, nz, prec;
+    int Mx, My, Mz;
+    RadixPlan rx, ry, rz;
+    int key_bits;
+    int sm_count;
+    int part_blocks;   // blocks of the per-particle reduction kernels
+};
+
+Layout make_layout(const Plan& p, int64_t n);
+
+// ---------------------------------------------------------------------------
+// launchers (each returns cudaError_t of the launch)
+// ---------------------------------------------------------------------------
+cudaError_t launch_init_workspace(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
+
+// per-particle stages (sc_particles.cu)
+cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
+                         const double* rp, cudaStream_t s);
+cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
+                          const double* rp, const double* q, cudaStream_t s);
+cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, cudaStream_t s);
+cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
+                               double* rp, cudaStream_t s);
+// el_field entry: extent over a given X[n][3] with a given gamma, and gather to exyz
+cudaError_t launch_extent_xyz(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
+                              double* X, const double* q, double gamma, cudaStream_t s);
+cudaError_t launch_gather_xyz(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
+                              double* exyz, cudaStream_t s);
+
+// sort + deposit (sc_sort.cu)
+size_t sort_scratch_bytes(int64_t n, int key_bits);
+cudaError_t launch_sort(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* keys_out,
+                        uint32_t* perm_out, uint32_t* tmp_k, uint32_t* tmp_v, uint32_t* hist,
+                        uint32_t* tot, cudaStream_t s);
+cudaError_t launch_deposit(const Plan& p, const Layout& L, char* ws, const double* q, int64_t n,
+                           cudaStream_t s);
+
+// Green's function (sc_green.cu)
+cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, double* kern_out, bool force,
+                       cudaStream_t s);
+cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
+
+// convolution + field grids (sc_fft.cu)
+cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in,
+                            void* phi_out, cudaStream_t s);
+cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
+
+// first-order map (sc_tmap.cu)
+cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n,
+                        cudaStream_t s);
+
+inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+
+}  // namespace ocsc

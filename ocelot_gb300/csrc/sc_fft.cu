@@ -1,0 +1,283 @@
+// Free-space potential by zero-padded FFT convolution with the integrated
+// Green's function, and the forward-difference field grids.
+//
+// Restates SpaceCharge.potential (ocelot/cpbd/sc.py:135-168) and the field
+// grids of el_field (sc.py:195-200).  The reference convolves on a
+// (2N-1)^3 complex grid; the linear convolution is the same on any padded
+// length M >= 2N-1, so each axis is padded to a length with a 2/4/8 radix
+// plan.  Only the N^3 octant of the charge is non-zero and only the N^3
+// octant of the result is kept, so the passes skip the zero planes:
+//
+//   F1  z: real-to-complex of the nx*ny charge lines (two lines per complex FFT)
+//   F2  y: forward FFT of the nx*Kz columns, zero-padded from ny to My
+//   F3  x: forward FFT, multiply by the real Green spectrum, inverse FFT,
+//          keep x < nx (the only pass that sees all Mx planes, in shared memory)
+//   B2  y: inverse FFT, keep y < ny
+//   B1  z: complex-to-real of the nx*ny lines, keep z < nz, scale by
+//          1/(Mx*My*Mz) and 1/(4*pi*eps0*hx*hy*hz)
+//
+// The complex work grid W[x][y][kz] (x < nx, y < My, kz <= Mz/2) stays in
+// HBM/L2 between passes; each pass stages whole lines in shared memory.
+#include "sc_common.cuh"
+#include "sc_fft_dev.cuh"
+
+namespace ocsc {
+
+constexpr int FFT_THREADS = 256;
+
+static inline int z_lines_per_block(int Mz) {
+    int nc = 2048 / Mz;
+    return nc < 1 ? 1 : (nc > 16 ? 16 : nc);
+}
+// columns per block in the strided passes: 16, fewer when two line buffers
+// of 16 columns would not fit in shared memory (FP64 at M = 512)
+template <typename R>
+static inline int strided_cols(int M) {
+    int tk = 16;
+    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + 2 * tk * (M + 1)) > 200 * 1024) tk /= 2;
+    return tk;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_zfwd(const R* __restrict__ q, Cx<R>* __restrict__ W,
+                                                      int ny, int nz, int My, int Kz, RadixPlan rz,
+                                                      const Cx<R>* __restrict__ twg, int NC,
+                                                      const ScState* st) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if (st->status) return;
+    const int Mz = rz.L;
+    Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
+    Cx<R>* a = tw + Mz;
+    Cx<R>* b = a + NC * Mz;
+    load_twiddles<R>(tw, twg, Mz);
+    const int x = blockIdx.y;
+    const int y0 = blockIdx.x * 2 * NC;
+    for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
+        const int c = idx / Mz, z = idx - c * Mz;
+        const int ya = y0 + 2 * c, yb = ya + 1;
+        R re = 0, im = 0;
+        if (z < nz) {
+            if (ya < ny) re = q[((size_t)x * ny + ya) * nz + z];
+            if (yb < ny) im = q[((size_t)x * ny + yb) * nz + z];
+        }
+        a[idx] = cx<R>(re, im);
+    }
+    __syncthreads();
+    Cx<R>* res = fft_lines<R, false>(a, b, Mz, NC, rz, tw);
+    for (int idx = threadIdx.x; idx < NC * Kz; idx += blockDim.x) {
+        const int c = idx / Kz, k = idx - c * Kz;
+        const int ya = y0 + 2 * c, yb = ya + 1;
+        const Cx<R> Z = res[c * Mz + k];
+        const Cx<R> Zm = res[c * Mz + (k == 0 ? 0 : Mz - k)];
+        const R h = (R)0.5;
+        if (ya < ny) W[((size_t)x * My + ya) * Kz + k] = cx<R>((Z.x + Zm.x) * h, (Z.y - Zm.y) * h);
+        if (yb < ny) W[((size_t)x * My + yb) * Kz + k] = cx<R>((Z.y + Zm.y) * h, (Zm.x - Z.x) * h);
+    }
+}
+
+// strided pass along y: forward (rows < ny in, all My out) or inverse (all in, rows < ny out)
+template <typename R, bool INV>
+__global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int ny, int My, int Kz,
+                                                       RadixPlan ry, const Cx<R>* __restrict__ twg,
+                                                       int TK, const ScState* st) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if (st->status) return;
+    const int ls = My + 1;
+    Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
+    Cx<R>* a = tw + My;
+    Cx<R>* b = a + TK * ls;
+    load_twiddles<R>(tw, twg, My);
+    const int x = blockIdx.y;
+    const int k0 = blockIdx.x * TK;
+    const int nin = INV ? My : ny;
+    for (int idx = threadIdx.x; idx < My * TK; idx += blockDim.x) {
+        const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
+        Cx<R> v = cx<R>(0, 0);
+        if (y < nin && k < Kz) v = W[((size_t)x * My + y) * Kz + k];
+        a[kk * ls + y] = v;
+    }
+    __syncthreads();
+    Cx<R>* res = fft_lines<R, INV>(a, b, ls, TK, ry, tw);
+    const int nout = INV ? ny : My;
+    for (int idx = threadIdx.x; idx < nout * TK; idx += blockDim.x) {
+        const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
+        if (k < Kz) W[((size_t)x * My + y) * Kz + k] = res[kk * ls + y];
+    }
+}
+
+// x pass: forward FFT of the nx non-zero planes, Green multiply, inverse FFT, keep x < nx
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, const R* __restrict__ G,
+                                                       int nx, int My, int Kz, int Ky, RadixPlan rx,
+                                                       const Cx<R>* __restrict__ twg, int TK, const ScState* st) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if (st->status) return;
+    const int Mx = rx.L;
+    const int ls = Mx + 1;
+    Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
+    Cx<R>* a = tw + Mx;
+    Cx<R>* b = a + TK * ls;
+    load_twiddles<R>(tw, twg, Mx);
+    const int ky = blockIdx.y;
+    const int gy = ky <= My - ky ? ky : My - ky;
+    const int k0 = blockIdx.x * TK;
+    for (int idx = threadIdx.x; idx < Mx * TK; idx += blockDim.x) {
+        const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
+        Cx<R> v = cx<R>(0, 0);
+        if (x < nx && k < Kz) v = W[((size_t)x * My + ky) * Kz + k];
+        a[kk * ls + x] = v;
+    }
+    __syncthreads();
+    Cx<R>* res = fft_lines<R, false>(a, b, ls, TK, rx, tw);
+    for (int idx = threadIdx.x; idx < Mx * TK; idx += blockDim.x) {
+        const int kx = idx / TK, kk = idx - kx * TK, k = k0 + kk;
+        const int gx = kx <= Mx - kx ? kx : Mx - kx;
+        const R g = k < Kz ? G[((size_t)gx * Ky + gy) * Kz + k] : (R)0;
+        Cx<R> v = res[kk * ls + kx];
+        v.x *= g;
+        v.y *= g;
+        res[kk * ls + kx] = v;
+    }
+    __syncthreads();
+    Cx<R>* res2 = fft_lines<R, true>(res, res == a ? b : a, ls, TK, rx, tw);
+    for (int idx = threadIdx.x; idx < nx * TK; idx += blockDim.x) {
+        const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
+        if (k < Kz) W[((size_t)x * My + ky) * Kz + k] = res2[kk * ls + x];
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ W, R* __restrict__ phi,
+                                                      int ny, int nz, int My, int Kz, RadixPlan rz,
+                                                      const Cx<R>* __restrict__ twg, int NC,
+                                                      const ScState* st) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if (st->status) return;
+    const int Mz = rz.L;
+    Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
+    Cx<R>* a = tw + Mz;
+    Cx<R>* b = a + NC * Mz;
+    load_twiddles<R>(tw, twg, Mz);
+    const int x = blockIdx.y;
+    const int y0 = blockIdx.x * 2 * NC;
+    for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
+        const int c = idx / Mz, k = idx - c * Mz;
+        const int ya = y0 + 2 * c, yb = ya + 1;
+        const bool lo = k < Kz;
+        const int kk = lo ? k : Mz - k;
+        Cx<R> A = cx<R>(0, 0), B = cx<R>(0, 0);
+        if (ya < ny) A = W[((size_t)x * My + ya) * Kz + kk];
+        if (yb < ny) B = W[((size_t)x * My + yb) * Kz + kk];
+        // Z = A + iB, Hermitian-extended above Mz/2
+        a[idx] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
+    }
+    __syncthreads();
+    Cx<R>* res = fft_lines<R, true>(a, b, Mz, NC, rz, tw);
+    const double norm = st->phi_norm, denom = st->phi_denom;
+    const R fscale = (R)(norm / denom);
+    for (int idx = threadIdx.x; idx < NC * nz; idx += blockDim.x) {
+        const int c = idx / nz, z = idx - c * nz;
+        const int ya = y0 + 2 * c, yb = ya + 1;
+        const Cx<R> v = res[c * Mz + z];
+        if (sizeof(R) == 8) {
+            // out/(4*pi*eps0*hx*hy*hz) after the 1/M normalisation of ifftn (sc.py:164-167)
+            if (ya < ny) phi[((size_t)x * ny + ya) * nz + z] = (R)(((double)v.x * norm) / denom);
+            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = (R)(((double)v.y * norm) / denom);
+        } else {
+            if (ya < ny) phi[((size_t)x * ny + ya) * nz + z] = v.x * fscale;
+            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = v.y * fscale;
+        }
+    }
+}
+
+// Ex,Ey,Ez = forward differences / h, zero on the last plane (sc.py:195-200)
+template <typename R>
+__global__ void k_field_grids(const R* __restrict__ phi, R* __restrict__ ex, R* __restrict__ ey,
+                              R* __restrict__ ez, int nx, int ny, int nz, const ScState* st) {
+    if (st->status) return;
+    const size_t ncell = (size_t)nx * ny * nz;
+    const double hx = st->steps[0], hy = st->steps[1], hz = st->steps[2];
+    const R ihx = (R)(1.0 / hx), ihy = (R)(1.0 / hy), ihz = (R)(1.0 / hz);
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(c % nz);
+        const int j = (int)((c / nz) % ny);
+        const int i = (int)(c / ((size_t)nz * ny));
+        const R p = phi[c];
+        R vx = 0, vy = 0, vz = 0;
+        if (sizeof(R) == 8) {
+            if (i < nx - 1) vx = (R)(((double)p - (double)phi[c + (size_t)ny * nz]) / hx);
+            if (j < ny - 1) vy = (R)(((double)p - (double)phi[c + nz]) / hy);
+            if (k < nz - 1) vz = (R)(((double)p - (double)phi[c + 1]) / hz);
+        } else {
+            if (i < nx - 1) vx = (p - phi[c + (size_t)ny * nz]) * ihx;
+            if (j < ny - 1) vy = (p - phi[c + nz]) * ihy;
+            if (k < nz - 1) vz = (p - phi[c + 1]) * ihz;
+        }
+        ex[c] = vx;
+        ey[c] = vy;
+        ez[c] = vz;
+    }
+}
+
+template <typename K>
+static cudaError_t set_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename R>
+static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, const R* qgrid, R* phi,
+                              cudaStream_t s) {
+    const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
+    const int Kz = p.Mz / 2 + 1, Ky = p.My / 2 + 1;
+    Cx<R>* W = reinterpret_cast<Cx<R>*>(ws + L.W);
+    const R* G = reinterpret_cast<const R*>(ws + L.green);
+    const Cx<R>* twx = reinterpret_cast<const Cx<R>*>(ws + L.tw_x);
+    const Cx<R>* twy = reinterpret_cast<const Cx<R>*>(ws + L.tw_y);
+    const Cx<R>* twz = reinterpret_cast<const Cx<R>*>(ws + L.tw_z);
+    cudaError_t e;
+    const int NC = z_lines_per_block(p.Mz);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
+    if ((e = set_smem(k_zfwd<R>, smz))) return e;
+    k_zfwd<R><<<gz, FFT_THREADS, smz, s>>>(qgrid, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
+    dim3 gy((Kz + tky - 1) / tky, p.nx);
+    if ((e = set_smem(k_ypass<R, false>, smy))) return e;
+    k_ypass<R, false><<<gy, FFT_THREADS, smy, s>>>(W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    dim3 gx((Kz + tkx - 1) / tkx, p.My);
+    if ((e = set_smem(k_xconv<R>, smx))) return e;
+    k_xconv<R><<<gx, FFT_THREADS, smx, s>>>(W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st);
+    if ((e = set_smem(k_ypass<R, true>, smy))) return e;
+    k_ypass<R, true><<<gy, FFT_THREADS, smy, s>>>(W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+    if ((e = set_smem(k_zinv<R>, smz))) return e;
+    k_zinv<R><<<gz, FFT_THREADS, smz, s>>>(W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in, void* phi_out,
+                            cudaStream_t s) {
+    if (p.prec == SC_FP64)
+        return convolve_t<double>(p, L, ws, static_cast<const double*>(qgrid_in), static_cast<double*>(phi_out), s);
+    return convolve_t<float>(p, L, ws, static_cast<const float*>(qgrid_in), static_cast<float*>(phi_out), s);
+}
+
+template <typename R>
+static cudaError_t field_t(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
+    const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
+    const size_t ncell = (size_t)p.nx * p.ny * p.nz;
+    int blocks = (int)((ncell + 255) / 256);
+    if (blocks > p.sm_count * 8) blocks = p.sm_count * 8;
+    k_field_grids<R><<<blocks, 256, 0, s>>>(reinterpret_cast<const R*>(ws + L.phi), reinterpret_cast<R*>(ws + L.ex),
+                                            reinterpret_cast<R*>(ws + L.ey), reinterpret_cast<R*>(ws + L.ez),
+                                            p.nx, p.ny, p.nz, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
+    return p.prec == SC_FP64 ? field_t<double>(p, L, ws, s) : field_t<float>(p, L, ws, s);
+}
+
+}  // namespace ocsc

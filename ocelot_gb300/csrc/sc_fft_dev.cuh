@@ -1,0 +1,111 @@
+// Batched mixed-radix (2/4/8) Stockham FFT of lines held in shared memory.
+//
+// The lines of one thread block live in shared memory, line l at a + l*ls,
+// elements contiguous.  Each stage reads radix-r butterfly inputs with stride
+// L/r, applies the twiddles w^(t*k), does the r-point DFT in registers and
+// writes the outputs in autosorted (Stockham) order into the other buffer, so
+// no bit reversal is needed.  Twiddles come from a per-block copy of
+// tw[m] = exp(-2*pi*i*m/L) in shared memory; the inverse uses their
+// conjugates and leaves the 1/L normalisation to the caller.
+#pragma once
+#include "sc_common.cuh"
+
+namespace ocsc {
+
+template <typename C, bool INV>
+__device__ __forceinline__ void dft2(C& a, C& b) {
+    C t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <typename C, bool INV>
+__device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3) {
+    C t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = csub(a1, a3);
+    t3 = INV ? cmul_pi(t3) : cmul_mi(t3);
+    a0 = cadd(t0, t2);
+    a2 = csub(t0, t2);
+    a1 = cadd(t1, t3);
+    a3 = csub(t1, t3);
+}
+
+template <typename R, bool INV>
+__device__ __forceinline__ void dft8(Cx<R>* v) {
+    Cx<R> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    Cx<R> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<Cx<R>, INV>(e0, e1, e2, e3);
+    dft4<Cx<R>, INV>(o0, o1, o2, o3);
+    const R h = (R)0.70710678118654752440;
+    if (!INV) {  // w = exp(-i*pi/4)
+        o1 = cx<R>((o1.x + o1.y) * h, (o1.y - o1.x) * h);
+        o2 = cmul_mi(o2);
+        o3 = cx<R>((o3.y - o3.x) * h, (-o3.x - o3.y) * h);
+    } else {     // w = exp(+i*pi/4)
+        o1 = cx<R>((o1.x - o1.y) * h, (o1.x + o1.y) * h);
+        o2 = cmul_pi(o2);
+        o3 = cx<R>((-o3.x - o3.y) * h, (o3.x - o3.y) * h);
+    }
+    v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+}
+
+template <typename R, bool INV, int RAD>
+__device__ __forceinline__ void stockham_stage(const Cx<R>* __restrict__ a, Cx<R>* __restrict__ b,
+                                               int L, int ls, int nl, int Ns, const Cx<R>* tw) {
+    const int nb = L / RAD;
+    const int step = L / (Ns * RAD);
+    const int total = nb * nl;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int line = idx / nb;
+        const int j = idx - line * nb;
+        const Cx<R>* src = a + line * ls;
+        Cx<R>* dst = b + line * ls;
+        const int k = j % Ns;
+        Cx<R> v[RAD];
+#pragma unroll
+        for (int t = 0; t < RAD; ++t) v[t] = src[j + t * nb];
+        if (Ns > 1) {
+#pragma unroll
+            for (int t = 1; t < RAD; ++t) {
+                Cx<R> w = tw[t * k * step];
+                if (INV) w.y = -w.y;
+                v[t] = cmul(v[t], w);
+            }
+        }
+        if (RAD == 2) dft2<Cx<R>, INV>(v[0], v[1]);
+        else if (RAD == 4) dft4<Cx<R>, INV>(v[0], v[1], v[2], v[3]);
+        else dft8<R, INV>(v);
+        const int out = (j - k) * RAD + k;
+#pragma unroll
+        for (int t = 0; t < RAD; ++t) dst[out + t * Ns] = v[t];
+    }
+}
+
+// FFT of nl lines of length rp.L; a holds the input, b is scratch of the
+// same shape.  Returns the buffer that holds the result.  Must be called by
+// every thread of the block; ends with a barrier.
+template <typename R, bool INV>
+__device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan& rp, const Cx<R>* tw) {
+    int Ns = 1;
+    for (int s = 0; s < rp.nst; ++s) {
+        const int r = rp.r[s];
+        if (r == 8) stockham_stage<R, INV, 8>(a, b, rp.L, ls, nl, Ns, tw);
+        else if (r == 4) stockham_stage<R, INV, 4>(a, b, rp.L, ls, nl, Ns, tw);
+        else stockham_stage<R, INV, 2>(a, b, rp.L, ls, nl, Ns, tw);
+        __syncthreads();
+        Cx<R>* t = a;
+        a = b;
+        b = t;
+        Ns *= r;
+    }
+    return a;
+}
+
+template <typename R>
+__device__ __forceinline__ void load_twiddles(Cx<R>* dst, const Cx<R>* src, int L) {
+    for (int i = threadIdx.x; i < L; i += blockDim.x) dst[i] = src[i];
+}
+
+}  // namespace ocsc

@@ -1,0 +1,47 @@
+// First-order transport between kicks: X <- R.X + B over the 6 rows of
+// rparticles, in place.  Restates TransferMap.mul_p_array
+// (ocelot/cpbd/transformations/transfer_map.py:40-50), whose np.dot(R, X)
+// is a BLAS product; each output is accumulated as an FMA chain over the six
+// inputs in index order and then offset by B.  One thread per particle reads
+// its six coordinates (coalesced along each row) and writes six: 96 bytes of
+// HBM traffic per particle, nothing else.
+#include "sc_common.cuh"
+
+namespace ocsc {
+
+struct Map6 {
+    double R[36];
+    double B[6];
+};
+
+__global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, int64_t ld, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            double acc = __dmul_rn(m.R[r * 6], x[0]);
+#pragma unroll
+            for (int k = 1; k < 6; ++k) acc = __fma_rn(m.R[r * 6 + k], x[k], acc);
+            rp[r * ld + i] = __dadd_rn(acc, m.B[r]);
+        }
+    }
+}
+
+cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    Map6 m;
+    for (int i = 0; i < 36; ++i) m.R[i] = R[i];
+    for (int i = 0; i < 6; ++i) m.B[i] = B[i];
+    int dev = 0, sm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    int64_t b = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm * 8;
+    if (b > cap) b = cap;
+    k_tmap<<<(int)b, 256, 0, s>>>(m, rp, ld, n);
+    return cudaGetLastError();
+}
+
+}  // namespace ocsc

@@ -1,0 +1,264 @@
+"""GPU parity: the sm_103a path against the oracle and the reference's fixtures.
+
+Tolerances (FP64 form): integer/index work (sort, keys) bit-exact; the charge
+grid bit-exact (same sequential sums as np.bincount); IGF, potential and
+fields to 1e-12 relative in norm (rounding of FP64 transcendentals and FFTs);
+rparticles to 1e-10 relative per row in norm (the plain form's target), and
+to 1e-12 absolute on the reference's own regression kicks (the tolerance of
+unit_tests/ebeam_test/space_charge/space_charge_test.py:65).
+FP32 form: relative RMS error of the momentum kick <= 1e-5.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, has_gpu
+from oracle import sc_oracle
+
+pytestmark = pytest.mark.gpu
+
+if not has_gpu():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import torch  # noqa: E402
+
+from ocelot_gb300 import DeviceParticleArray, ParticleArray, SpaceCharge  # noqa: E402
+from ocelot_gb300.sorting import stable_sort_keys  # noqa: E402
+from ocelot_gb300.transfer import tmap_apply  # noqa: E402
+
+DEV = torch.device("cuda", 0)
+CASES = [c for c in sorted(glob.glob(os.path.join(GOLDEN, "ref_*.npz"))) if not c.endswith("track_kicks.npz")]
+
+
+def rel_rows(a, b):
+    return max(np.linalg.norm(a[r] - b[r]) / np.linalg.norm(b[r]) for r in range(a.shape[0]))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def make_pa(rp, q, E):
+    pa = ParticleArray(rp.shape[1])
+    pa.rparticles[:] = rp
+    pa.q_array = np.array(q, dtype=np.float64)
+    pa.E = E
+    return pa
+
+
+# ---------------------------------------------------------------------------
+# integer / index work: bit-exact
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("n,bits,kind", [
+    (1, 18, "rand"), (7, 6, "rand"), (4096, 18, "rand"), (4097, 18, "rand"), (100_003, 18, "rand"),
+    (250_000, 22, "rand"), (50_000, 18, "equal"), (50_000, 18, "sorted"), (50_000, 18, "reversed"),
+    (300_000, 12, "gauss"), (70_000, 32, "rand"), (20_000, 9, "rand"),
+])
+def test_sort_is_numpy_stable_argsort(n, bits, kind):
+    rng = np.random.default_rng(n + bits)
+    hi = 1 << bits
+    if kind == "rand":
+        k = rng.integers(0, hi, n, dtype=np.uint64)
+    elif kind == "equal":
+        k = np.full(n, hi // 3, dtype=np.uint64)
+    elif kind == "sorted":
+        k = np.sort(rng.integers(0, hi, n, dtype=np.uint64))
+    elif kind == "reversed":
+        k = np.sort(rng.integers(0, hi, n, dtype=np.uint64))[::-1].copy()
+    else:  # clustered, like cells of a Gaussian beam
+        k = np.clip(rng.normal(hi / 2, hi / 50, n), 0, hi - 1).astype(np.uint64)
+    keys = torch.from_numpy(k.astype(np.uint32).view(np.int32)).to(DEV)
+    sk, perm = stable_sort_keys(keys, bits)
+    order = np.argsort(k, kind="stable")
+    assert np.array_equal(perm.cpu().numpy(), order)
+    assert np.array_equal(sk.cpu().numpy().astype(np.uint64), k[order])
+
+
+# ---------------------------------------------------------------------------
+# stages against the reference's own intermediates
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c)[4:-4] for c in CASES])
+def test_stages_match_reference_intermediates(path):
+    d = dict(np.load(path))
+    nmesh = [int(v) for v in d["nmesh"]]
+    sc = SpaceCharge(nmesh_xyz=nmesh)
+    steps = d["steps"][0]
+    k = sc.sym_kernel(nmesh, steps)
+    assert rel(k, d["igf"][0]) < 1e-12
+    phi = sc.potential(d["qgrid"][0], steps)
+    assert rel(phi, d["phi"][0]) < 1e-12
+    # el_field from the reference's rotated positions (no random mesh draws here)
+    if not bool(d["random_mesh"]):
+        X = d["xyz_rot"][0].copy()
+        E = sc.el_field(X, d["q"], float(d["gamma0"][0]), nmesh)
+        for c in range(3):
+            assert rel(E[:, c], d["Exyz"][0][:, c]) < 1e-11, c
+        Xr = d["xyz_rot"][0].copy()
+        Xr[:, 2] *= float(d["gamma0"][0])
+        assert np.array_equal(X, Xr)
+
+
+def test_charge_grid_bit_identical_to_bincount():
+    """The deposit sums each cell in particle order, exactly like np.bincount."""
+    for name in ("ref_multi_kick_31.npz", "ref_aniso_low_energy.npz", "ref_even_16.npz"):
+        d = dict(np.load(os.path.join(GOLDEN, name)))
+        nmesh = [int(v) for v in d["nmesh"]]
+        sc = SpaceCharge(nmesh_xyz=nmesh)
+        X = d["xyz_rot"][0].copy()
+        sc.el_field(X, d["q"], float(d["gamma0"][0]), nmesh)
+        eng = sc.engine()
+        assert np.array_equal(eng.region("qgrid").cpu().numpy(), d["qgrid"][0]), name
+        keys = eng.region("keys")[: X.shape[0]].cpu().numpy().astype(np.int64)
+        Xo = d["xyz_rot"][0].copy()
+        rec = {}
+        sc_oracle.el_field(Xo, d["q"], float(d["gamma0"][0]), nmesh, record=rec)
+        assert np.array_equal(keys, rec["keys"]), name
+
+
+# ---------------------------------------------------------------------------
+# the full kick
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c)[4:-4] for c in CASES])
+def test_kick_matches_reference_fixtures(path):
+    d = dict(np.load(path))
+    nmesh = [int(v) for v in d["nmesh"]]
+    pa = make_pa(d["rp_in"], d["q"], float(d["E"]))
+    sc = SpaceCharge(nmesh_xyz=nmesh, random_mesh=bool(d["random_mesh"]))
+    sc.prepare(None)
+    for k in range(int(d["kicks"])):
+        sc.apply(pa, float(d["dz"]))
+        assert rel_rows(pa.rparticles, d["rp_out"][k]) < 1e-10, k
+
+
+def test_reference_regression_kicks_at_reference_tolerance():
+    """Kicks recorded inside the reference's test_track_with_sp (63^3, 10k particles)."""
+    d = dict(np.load(os.path.join(GOLDEN, "ref_track_kicks.npz")))
+    for j in range(int(d["n_kept"])):
+        pa = make_pa(d[f"k{j}_rp_in"], d[f"k{j}_q"], float(d[f"k{j}_E"]))
+        sc = SpaceCharge(nmesh_xyz=[63, 63, 63])
+        sc.apply(pa, float(d[f"k{j}_dz"]))
+        assert np.abs(pa.rparticles - d[f"k{j}_rp_out"]).max() <= 1e-12
+
+
+def test_config1_ten_kicks_vs_oracle():
+    """200k particles, 63^3, 130 MeV, 250 pC, 10 kicks of 0.1 m: <= 1e-10 per row."""
+    rp, q = sc_oracle.gaussian_beam(200_000, 11, charge=250e-12)
+    ref = rp.copy()
+    pa = make_pa(rp, q, 0.130)
+    sc = SpaceCharge(nmesh_xyz=[63, 63, 63])
+    for _ in range(10):
+        sc_oracle.sc_apply(ref, q, 0.130, 0.1, [63, 63, 63])
+        sc.apply(pa, 0.1)
+    assert rel_rows(pa.rparticles, ref) < 1e-10
+
+
+def test_fp32_form_kick_error():
+    """FP32 form: relative RMS momentum-kick error vs the FP64 oracle <= 1e-5."""
+    rp, q = sc_oracle.gaussian_beam(200_000, 12, charge=1e-9)
+    ref = rp.copy()
+    sc_oracle.sc_apply(ref, q, 0.130, 0.1, [64, 64, 64])
+    pa = make_pa(rp, q, 0.130)
+    SpaceCharge(nmesh_xyz=[64, 64, 64], precision="fp32").apply(pa, 0.1)
+    for r in (1, 3, 5):
+        dk = ref[r] - rp[r]
+        err = np.sqrt(np.mean(((pa.rparticles[r] - rp[r]) - dk) ** 2)) / np.sqrt(np.mean(dk ** 2))
+        assert err < 1e-5, (r, err)
+    for r in (0, 2, 4):  # positions move by the re-projection; their change is also small
+        dk = ref[r] - rp[r]
+        err = np.sqrt(np.mean(((pa.rparticles[r] - rp[r]) - dk) ** 2)) / np.sqrt(np.mean(dk ** 2))
+        assert err < 1e-4, (r, err)
+
+
+# ---------------------------------------------------------------------------
+# properties and edge cases
+# ---------------------------------------------------------------------------
+def test_bit_reproducible_and_cache_consistent():
+    rp, q = sc_oracle.gaussian_beam(50_000, 13)
+    outs = []
+    sc = SpaceCharge(nmesh_xyz=[31, 31, 31])
+    for _ in range(3):  # the 2nd and 3rd calls hit the Green's-function cache
+        pa = make_pa(rp, q, 0.130)
+        sc.apply(pa, 0.1)
+        outs.append(pa.rparticles.copy())
+    fresh = make_pa(rp, q, 0.130)
+    SpaceCharge(nmesh_xyz=[31, 31, 31]).apply(fresh, 0.1)
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
+    assert np.array_equal(outs[0], fresh.rparticles)
+
+
+def test_workspace_reuse_across_particle_counts():
+    sc = SpaceCharge(nmesh_xyz=[15, 15, 15])
+    for n, seed in ((5000, 1), (20_000, 2), (3000, 3)):
+        rp, q = sc_oracle.gaussian_beam(n, seed)
+        ref = rp.copy()
+        sc_oracle.sc_apply(ref, q, 0.130, 0.1, [15, 15, 15])
+        pa = make_pa(rp, q, 0.130)
+        sc.apply(pa, 0.1)
+        assert rel_rows(pa.rparticles, ref) < 1e-10
+
+
+def test_noncontiguous_rparticles_view():
+    rp, q = sc_oracle.gaussian_beam(20_000, 4)
+    big = np.zeros((6, 30_000))
+    big[:, :20_000] = rp
+    view = big[:, :20_000]
+    pa = make_pa(rp, q, 0.130)
+    pa.rparticles = view
+    ref = rp.copy()
+    sc_oracle.sc_apply(ref, q, 0.130, 0.1, [15, 15, 15])
+    SpaceCharge(nmesh_xyz=[15, 15, 15]).apply(pa, 0.1)
+    assert rel_rows(big[:, :20_000], ref) < 1e-10
+    assert np.all(big[:, 20_000:] == 0)
+
+
+def test_device_resident_path_matches_host_path():
+    rp, q = sc_oracle.gaussian_beam(30_000, 5)
+    host = make_pa(rp, q, 0.130)
+    SpaceCharge(nmesh_xyz=[31, 31, 31]).apply(host, 0.1)
+    dpa = DeviceParticleArray.from_host(make_pa(rp, q, 0.130), DEV)
+    sc = SpaceCharge(nmesh_xyz=[31, 31, 31])
+    sc.apply(dpa, 0.1)
+    sc.check()
+    assert np.array_equal(dpa.rparticles.cpu().numpy(), host.rparticles)
+
+
+@pytest.mark.parametrize("n", [1, 2])
+def test_degenerate_beam_raises_and_leaves_particles(n):
+    rp = np.zeros((6, n))
+    pa = make_pa(rp, np.full(n, 1e-12), 0.130)
+    with pytest.raises(ValueError):
+        SpaceCharge(nmesh_xyz=[15, 15, 15]).apply(pa, 0.1)
+    assert np.all(pa.rparticles == 0)
+
+
+def test_nonfinite_particle_raises():
+    rp, q = sc_oracle.gaussian_beam(1000, 6)
+    rp[0, 17] = np.nan
+    pa = make_pa(rp, q, 0.130)
+    with pytest.raises(ValueError):
+        SpaceCharge(nmesh_xyz=[15, 15, 15]).apply(pa, 0.1)
+    assert np.array_equal(pa.rparticles[:, :17], rp[:, :17])
+
+
+def test_small_and_odd_meshes():
+    for mesh in ([4, 4, 4], [5, 9, 17], [33, 8, 20]):
+        rp, q = sc_oracle.gaussian_beam(3000, sum(mesh))
+        ref = rp.copy()
+        sc_oracle.sc_apply(ref, q, 0.130, 0.1, mesh)
+        pa = make_pa(rp, q, 0.130)
+        SpaceCharge(nmesh_xyz=mesh).apply(pa, 0.1)
+        assert rel_rows(pa.rparticles, ref) < 1e-10, mesh
+
+
+def test_tmap_matches_oracle():
+    rng = np.random.default_rng(9)
+    rp = rng.standard_normal((6, 100_001)) * 1e-4
+    R = np.eye(6) + rng.standard_normal((6, 6)) * 0.1
+    B = rng.standard_normal((6, 1)) * 1e-6
+    ref = rp.copy()
+    sc_oracle.tmap_apply(ref, R, B)
+    d = torch.from_numpy(rp).to(DEV)
+    tmap_apply(R, B, d)
+    assert np.abs(d.cpu().numpy() - ref).max() <= 1e-15 * np.abs(ref).max()
