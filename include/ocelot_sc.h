@@ -27,9 +27,14 @@ extern "C" {
 
 #define SC_ABI_VERSION 1
 
-/* precision of a plan */
+/* mode of a plan: a precision, optionally OR-ed with FP32-form options */
 #define SC_FP64 0 /* plain form: FP64 end to end, matches sc.py to 1e-10 */
-#define SC_FP32 1 /* precision form: FP32 grid/gather, FP64 IGF and FP64 accumulation */
+#define SC_FP32 1 /* precision form: FP32 deposit/FFT/gather, FP64 accumulation into
+                     rparticles; by default the charge is accumulated exactly in
+                     64-bit fixed point and the Green's function far from the
+                     origin uses a cancellation-free 4th-order multipole form */
+#define SC_FP32_SORTED_DEPOSIT 0x10 /* FP32 form: radix sort + Kahan segment sums */
+#define SC_FP32_EXACT_IGF 0x20      /* FP32 form: FP64 8-corner IGF on every cell */
 
 /* status codes */
 #define SC_OK 0
@@ -45,10 +50,10 @@ typedef struct sc_plan sc_plan; /* opaque, host-side only */
 /* ---- plan / workspace ------------------------------------------------- */
 
 /* Plan for a mesh of nx*ny*nz cells (SpaceCharge.nmesh_xyz, sc.py:94) in the
- * given precision.  Each n must be >= 4 (the reference divides the extent by
+ * given mode (SC_FP64, or SC_FP32 with options).  Each n must be >= 4 (the reference divides the extent by
  * n-3, sc.py:179).  Host-only object: holds sizes, FFT radix plans and launch
  * shapes, no device memory. */
-int sc_plan_create(sc_plan** plan, int nx, int ny, int nz, int precision);
+int sc_plan_create(sc_plan** plan, int nx, int ny, int nz, int mode);
 void sc_plan_destroy(sc_plan* plan);
 /* padded FFT lengths chosen for the linear convolution (each >= 2n-1) */
 int sc_plan_fft_shape(const sc_plan* plan, int* mx, int* my, int* mz);
@@ -128,12 +133,13 @@ int sc_tmap_apply(const double* R, const double* B, double* rparticles, int64_t 
 
 /* ---- stage timing (benchmarking) --------------------------------------- */
 
-/* Stages of sc_kick, in launch order: MAD->lab frame (coord_transform.py:57-96,
+/* Stages of sc_kick: MAD->lab frame (coord_transform.py:57-96,
  * sc.py:224-239), mesh extent (sc.py:171-186), NGP keys (sc.py:187-192),
- * radix sort and deposit (sc.py:193), IGF table (sc.py:109-133), Green
- * spectrum (sc.py:142-149,164), convolution (sc.py:150-168), field grids
- * (sc.py:195-200), gather + kick + back-transform (sc.py:201-251). */
-#define SC_NSTAGES 10
+ * radix sort, deposit (sc.py:193), IGF table (sc.py:109-133) and Green
+ * spectrum (sc.py:142-149,164) -- these two on a second stream, beside keys,
+ * sort and deposit --, the wait for them, convolution (sc.py:150-168), field
+ * grids (sc.py:195-200), gather + kick + back-transform (sc.py:201-251). */
+#define SC_NSTAGES 11
 /* When enabled, sc_kick records a CUDA event on its stream before the first
  * stage and after each stage.  Host call; creates or destroys the events. */
 int sc_profile_enable(sc_plan* plan, int enable);

@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(_PKG, "lib", "libocelot_sc.so")
 
 SC_FP64 = 0
 SC_FP32 = 1
+SC_FP32_SORTED_DEPOSIT = 0x10
+SC_FP32_EXACT_IGF = 0x20
 
 SC_OK = 0
 SC_ERR_ARG = 1
@@ -23,7 +25,7 @@ SC_ERR_DEGENERATE = 4
 SC_ERR_NONFINITE = 5
 SC_ERR_UNSUPPORTED = 6
 
-SC_NSTAGES = 10
+SC_NSTAGES = 11
 
 REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5}
 

@@ -25,6 +25,9 @@ SOURCES = ["sc_api.cu", "sc_particles.cu", "sc_sort.cu", "sc_green.cu", "sc_fft.
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include")]
+if os.environ.get("OCELOT_SC_CHECKED") == "1":
+    # index checks that record the first bad index in the device state
+    FLAGS += ["-DSC_CHECKED"]
 
 
 def nvcc() -> str:

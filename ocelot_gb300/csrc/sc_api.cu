@@ -71,7 +71,7 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.tw_y = take(cs * p.My);
     L.tw_z = take(cs * p.Mz);
     L.part_frame = take(8 * 3 * (size_t)p.part_blocks);
-    L.part_ext = take(8 * 10 * (size_t)p.part_blocks);
+    L.part_ext = take(8 * 11 * (size_t)p.part_blocks);
     // n-independent regions first: the Green's-function cache keeps its
     // offset when the same workspace serves kicks of different n
     L.qgrid = take(rs * ncell);
@@ -79,8 +79,11 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.ex = take(rs * ncell);
     L.ey = take(rs * ncell);
     L.ez = take(rs * ncell);
+    L.cell_start = take(4 * ncell);
+    L.cell_end = take(4 * ncell);
+    L.qfix = take(8 * ncell);
     L.igf_ig = take(8 * (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1));
-    L.igf_k1 = take(8 * ncell);
+    L.igf_k1 = take(8 * ncell);  // R-typed; sized for double
     L.green_s1 = take(rs * (size_t)p.nx * p.ny * Kz);
     L.green_s2 = take(rs * (size_t)p.nx * Ky * Kz);
     L.green = take(rs * Kx * Ky * Kz);
@@ -90,11 +93,12 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.keys = take(4 * (size_t)n);
     L.sort_keys = take(4 * (size_t)n);
     L.sort_perm = take(4 * (size_t)n);
+    L.sort_q = take(rs * (size_t)n);
     L.sort_tmp_k = take(4 * (size_t)n);
     L.sort_tmp_v = take(4 * (size_t)n);
     const size_t sb = (size_t)((n + 4095) / 4096);
-    L.sort_hist = take(4 * 256 * (sb ? sb : 1));
-    L.sort_tot = take(4 * 256);
+    L.sort_hist = take(4 * 512 * (sb ? sb : 1));
+    L.sort_tot = take(4 * 512);
     L.total = o;
     return L;
 }
@@ -136,17 +140,24 @@ __global__ void k_convert(const A* __restrict__ a, B* __restrict__ b, size_t n) 
 
 using namespace ocsc;
 
+// events: main stream 0..9 (before frame, after frame, extent, keys, sort,
+// deposit, join, convolve, field, kick); side stream 10..12 (start, after
+// igf, after green)
+constexpr int NEV = 13;
+
 struct sc_plan {
     Plan p;
     const void* ws_ready;  // workspace initialised by sc_workspace_init for this plan
     size_t ws_ready_bytes;
-    cudaEvent_t ev[SC_NSTAGES + 1];
+    cudaEvent_t ev[NEV];
     bool profiling;
     int last_launches;
+    cudaStream_t side;     // the Green's-function build runs here, beside the deposit
+    cudaEvent_t fork, join;
 };
 
 static const char* kStageNames[SC_NSTAGES] = {"frame", "extent", "keys", "sort", "deposit",
-                                              "igf", "green", "convolve", "field", "kick"};
+                                              "igf", "green", "join_wait", "convolve", "field", "kick"};
 
 static inline void mark(sc_plan* plan, int i, cudaStream_t s) {
     if (plan->profiling) cudaEventRecord(plan->ev[i], s);
@@ -206,6 +217,13 @@ static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energ
     kp.m_e_eV = c.m_e_eV;
     kp.m2 = pow(c.m_e_eV, 2.0);
     kp.four_pi_eps0 = 4 * c.pi * c.epsilon_0;
+    kp.gamref_f = (float)kp.gamref;
+    kp.betaref_f = (float)kp.betaref;
+    kp.grbr_f = (float)kp.grbr;
+    kp.pref_f = (float)kp.pref;
+    kp.ipref_f = (float)(1.0 / kp.pref);
+    kp.m_f = (float)kp.m_e_eV;
+    kp.m2_f = kp.m_f * kp.m_f;
     return kp;
 }
 
@@ -215,16 +233,20 @@ int sc_abi_version(void) { return SC_ABI_VERSION; }
 
 const char* sc_last_error(void) { return g_err.c_str(); }
 
-int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int precision) {
+int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
+    const int precision = mode & 0x0f;
     if (!out) return fail(SC_ERR_ARG, "plan pointer is NULL");
     *out = nullptr;
     if (nx < 4 || ny < 4 || nz < 4)
         return fail(SC_ERR_ARG, "nmesh_xyz=[%d,%d,%d]: every mesh dimension must be >= 4", nx, ny, nz);
     if (precision != SC_FP64 && precision != SC_FP32) return fail(SC_ERR_ARG, "unknown precision %d", precision);
+    if (mode & ~(0x0f | SC_FP32_SORTED_DEPOSIT | SC_FP32_EXACT_IGF)) return fail(SC_ERR_ARG, "unknown mode bits 0x%x", mode);
     Plan p;
     memset(&p, 0, sizeof p);
     p.nx = nx; p.ny = ny; p.nz = nz;
     p.prec = precision;
+    p.sorted_deposit = precision == SC_FP64 || (mode & SC_FP32_SORTED_DEPOSIT);
+    p.exact_igf = precision == SC_FP64 || (mode & SC_FP32_EXACT_IGF);
     p.Mx = choose_fft_length(nx);
     p.My = choose_fft_length(ny);
     p.Mz = choose_fft_length(nz);
@@ -247,7 +269,9 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int precision) {
     h->ws_ready_bytes = 0;
     h->profiling = false;
     h->last_launches = 0;
-    for (int i = 0; i <= SC_NSTAGES; ++i) h->ev[i] = nullptr;
+    for (int i = 0; i < NEV; ++i) h->ev[i] = nullptr;
+    h->side = nullptr;
+    h->fork = h->join = nullptr;
     *out = h;
     return SC_OK;
 }
@@ -255,17 +279,23 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int precision) {
 void sc_plan_destroy(sc_plan* plan) {
     if (!plan) return;
     if (plan->profiling)
-        for (int i = 0; i <= SC_NSTAGES; ++i) cudaEventDestroy(plan->ev[i]);
+        for (int i = 0; i < NEV; ++i) cudaEventDestroy(plan->ev[i]);
+    if (plan->side) {
+        cudaStreamSynchronize(plan->side);
+        cudaStreamDestroy(plan->side);
+        cudaEventDestroy(plan->fork);
+        cudaEventDestroy(plan->join);
+    }
     delete plan;
 }
 
 int sc_profile_enable(sc_plan* plan, int enable) {
     if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
     if (enable && !plan->profiling) {
-        for (int i = 0; i <= SC_NSTAGES; ++i) SC_CUDA(cudaEventCreate(&plan->ev[i]), "cudaEventCreate");
+        for (int i = 0; i < NEV; ++i) SC_CUDA(cudaEventCreate(&plan->ev[i]), "cudaEventCreate");
         plan->profiling = true;
     } else if (!enable && plan->profiling) {
-        for (int i = 0; i <= SC_NSTAGES; ++i) cudaEventDestroy(plan->ev[i]);
+        for (int i = 0; i < NEV; ++i) cudaEventDestroy(plan->ev[i]);
         plan->profiling = false;
     }
     return SC_OK;
@@ -274,8 +304,11 @@ int sc_profile_enable(sc_plan* plan, int enable) {
 int sc_profile_read(sc_plan* plan, float* ms, int* n_launches) {
     if (!plan || !ms) return fail(SC_ERR_ARG, "bad arguments");
     if (!plan->profiling) return fail(SC_ERR_ARG, "profiling is not enabled");
-    SC_CUDA(cudaEventSynchronize(plan->ev[SC_NSTAGES]), "cudaEventSynchronize");
-    for (int i = 0; i < SC_NSTAGES; ++i) SC_CUDA(cudaEventElapsedTime(&ms[i], plan->ev[i], plan->ev[i + 1]), "cudaEventElapsedTime");
+    SC_CUDA(cudaEventSynchronize(plan->ev[9]), "cudaEventSynchronize");
+    // main-stream stages, then the two side-stream stages
+    static const int a[SC_NSTAGES] = {0, 1, 2, 3, 4, 10, 11, 5, 6, 7, 8};
+    static const int b[SC_NSTAGES] = {1, 2, 3, 4, 5, 11, 12, 6, 7, 8, 9};
+    for (int i = 0; i < SC_NSTAGES; ++i) SC_CUDA(cudaEventElapsedTime(&ms[i], plan->ev[a[i]], plan->ev[b[i]]), "cudaEventElapsedTime");
     if (n_launches) *n_launches = plan->last_launches;
     return SC_OK;
 }
@@ -361,34 +394,55 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     char* ws = static_cast<char*>(ws_v);
     cudaStream_t s = (cudaStream_t)stream;
     const KickParams kp = make_params(p, n, ld, energy_gev, zstep, mesh_scale, mesh_shift);
-    const int passes = (p.key_bits + 7) / 8;
+    const int passes = sort_passes(p.key_bits);
+    if (!plan->side) {
+        SC_CUDA(cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking), "cudaStreamCreate");
+        SC_CUDA(cudaEventCreateWithFlags(&plan->fork, cudaEventDisableTiming), "cudaEventCreate");
+        SC_CUDA(cudaEventCreateWithFlags(&plan->join, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    cudaStream_t side = plan->side;
     mark(plan, 0, s);
     SC_CUDA(launch_frame(p, L, ws, kp, rp, s), "frame");
     mark(plan, 1, s);
     SC_CUDA(launch_extent(p, L, ws, kp, rp, q, s), "extent");
     mark(plan, 2, s);
-    SC_CUDA(launch_keys(p, L, ws, kp, s), "keys");
+    // fork: the FP64 Green's-function table and its spectrum (they need only
+    // the mesh step) run on the side stream while the deposit runs here
+    SC_CUDA(cudaEventRecord(plan->fork, s), "cudaEventRecord");
+    SC_CUDA(cudaStreamWaitEvent(side, plan->fork, 0), "cudaStreamWaitEvent");
+    mark(plan, 10, side);
+    SC_CUDA(launch_igf(p, L, ws, side), "igf");
+    mark(plan, 11, side);
+    SC_CUDA(launch_green_spectrum(p, L, ws, side), "green spectrum");
+    mark(plan, 12, side);
+    SC_CUDA(cudaEventRecord(plan->join, side), "cudaEventRecord");
+    // keys; in the FP32 form the exact fixed-point deposit rides along
+    SC_CUDA(launch_keys(p, L, ws, kp, rp, p.sorted_deposit ? nullptr : q, s), "keys");
     mark(plan, 3, s);
-    SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),
-                        reinterpret_cast<uint32_t*>(ws + L.sort_perm), reinterpret_cast<uint32_t*>(ws + L.sort_tmp_k),
-                        reinterpret_cast<uint32_t*>(ws + L.sort_tmp_v), reinterpret_cast<uint32_t*>(ws + L.sort_hist),
-                        reinterpret_cast<uint32_t*>(ws + L.sort_tot), s),
-            "sort");
-    mark(plan, 4, s);
-    SC_CUDA(launch_deposit(p, L, ws, q, n, s), "deposit");
+    if (p.sorted_deposit) {
+        SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),
+                            reinterpret_cast<uint32_t*>(ws + L.sort_perm), reinterpret_cast<uint32_t*>(ws + L.sort_tmp_k),
+                            reinterpret_cast<uint32_t*>(ws + L.sort_tmp_v), reinterpret_cast<uint32_t*>(ws + L.sort_hist),
+                            reinterpret_cast<uint32_t*>(ws + L.sort_tot), s, q, ws + L.sort_q, p.prec == SC_FP32),
+                "sort");
+        mark(plan, 4, s);
+        SC_CUDA(launch_deposit(p, L, ws, q, n, s), "deposit");
+    } else {
+        mark(plan, 4, s);
+    }
     mark(plan, 5, s);
-    SC_CUDA(launch_igf(p, L, ws, nullptr, false, s), "igf");
+    SC_CUDA(cudaStreamWaitEvent(s, plan->join, 0), "cudaStreamWaitEvent");  // join
     mark(plan, 6, s);
-    SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s,
+                            p.sorted_deposit ? nullptr : reinterpret_cast<const long long*>(ws + L.qfix)),
+            "convolve");
     mark(plan, 7, s);
-    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s), "convolve");
-    mark(plan, 8, s);
     SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
-    mark(plan, 9, s);
+    mark(plan, 8, s);
     SC_CUDA(launch_gather_kick(p, L, ws, kp, rp, s), "gather/kick");
-    mark(plan, 10, s);
-    // frame 2, extent 2, keys 1, sort 3 per pass, deposit 1, igf 2, green 3, convolve 5, field 1, kick 1
-    plan->last_launches = 2 + 2 + 1 + 3 * passes + 1 + 2 + 3 + 5 + 1 + 1;
+    mark(plan, 9, s);
+    // frame 1, extent 1, keys 1, [sort 3 per pass, deposit 2], igf 2, green 3, convolve 5, field 1, kick 1
+    plan->last_launches = 1 + 1 + 1 + (p.sorted_deposit ? 3 * passes + 2 : 0) + 2 + 3 + 5 + 1 + 1;
     return SC_OK;
 }
 
@@ -406,16 +460,20 @@ int sc_el_field(sc_plan* plan, void* ws_v, size_t ws_bytes, double* X, const dou
     cudaStream_t s = (cudaStream_t)stream;
     const KickParams kp = make_params(p, n, n, 1.0, 1.0, mesh_scale, mesh_shift);
     SC_CUDA(launch_extent_xyz(p, L, ws, kp, X, q, gamma, s), "extent");
-    SC_CUDA(launch_keys(p, L, ws, kp, s), "keys");
-    SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),
-                        reinterpret_cast<uint32_t*>(ws + L.sort_perm), reinterpret_cast<uint32_t*>(ws + L.sort_tmp_k),
-                        reinterpret_cast<uint32_t*>(ws + L.sort_tmp_v), reinterpret_cast<uint32_t*>(ws + L.sort_hist),
-                        reinterpret_cast<uint32_t*>(ws + L.sort_tot), s),
-            "sort");
-    SC_CUDA(launch_deposit(p, L, ws, q, n, s), "deposit");
-    SC_CUDA(launch_igf(p, L, ws, nullptr, false, s), "igf");
+    SC_CUDA(launch_keys(p, L, ws, kp, nullptr, p.sorted_deposit ? nullptr : q, s), "keys");
+    if (p.sorted_deposit) {
+        SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),
+                            reinterpret_cast<uint32_t*>(ws + L.sort_perm), reinterpret_cast<uint32_t*>(ws + L.sort_tmp_k),
+                            reinterpret_cast<uint32_t*>(ws + L.sort_tmp_v), reinterpret_cast<uint32_t*>(ws + L.sort_hist),
+                            reinterpret_cast<uint32_t*>(ws + L.sort_tot), s, q, ws + L.sort_q, p.prec == SC_FP32),
+                "sort");
+        SC_CUDA(launch_deposit(p, L, ws, q, n, s), "deposit");
+    }
+    SC_CUDA(launch_igf(p, L, ws, s), "igf");
     SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
-    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s), "convolve");
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s,
+                            p.sorted_deposit ? nullptr : reinterpret_cast<const long long*>(ws + L.qfix)),
+            "convolve");
     SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
     SC_CUDA(launch_gather_xyz(p, L, ws, kp, exyz, s), "gather");
     return SC_OK;
@@ -434,7 +492,7 @@ int sc_potential(sc_plan* plan, void* ws_v, size_t ws_bytes, const double* qgrid
     cudaStream_t s = (cudaStream_t)stream;
     const KickParams kp = make_params(p, 0, 0, 1.0, 1.0, NAN, NAN);
     SC_CUDA(launch_set_mesh(p, L, ws, kp, hx, hy, hz, s), "set mesh");
-    SC_CUDA(launch_igf(p, L, ws, nullptr, false, s), "igf");
+    SC_CUDA(launch_igf(p, L, ws, s), "igf");
     SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
     if (p.prec == SC_FP64) {
         SC_CUDA(launch_convolve(p, L, ws, qgrid, phi, s), "convolve");
@@ -479,7 +537,7 @@ int sc_sort_keys(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* key
     uint32_t* tk = reinterpret_cast<uint32_t*>(w);
     uint32_t* tv = reinterpret_cast<uint32_t*>(w + a);
     uint32_t* hist = reinterpret_cast<uint32_t*>(w + 2 * a);
-    uint32_t* tot = reinterpret_cast<uint32_t*>(w + 2 * a + align_up(256 * nb * 4));
+    uint32_t* tot = reinterpret_cast<uint32_t*>(w + 2 * a + align_up(512 * nb * 4));
     SC_CUDA(launch_sort(keys_in, n, key_bits, keys_out, perm_out, tk, tv, hist, tot, (cudaStream_t)stream), "sort");
     return SC_OK;
 }

@@ -47,14 +47,29 @@ struct ScState {
     // mesh (sc.py:171-186)
     double steps[3];
     double xoff[3];
+    double isteps[3];            // 1/steps
     double phi_denom;            // 4*pi*eps0*hx*hy*hz (sc.py:167)
     double phi_norm;             // 1/(Mx*My*Mz) of the inverse FFT
     // Green's-function cache: spacing of the spectrum held in the workspace
     double igf_h[3];
+    // FP32 copies of the per-kick constants, written once by the finalizes
+    float Tf[3][3];
+    float g0f, ig0f, kxyf, kzf;
+    float stepsf[3], istepsf[3], xofff[3];
     int igf_rebuild;             // 1 when the current call rebuilds it
     int status;                  // SC_OK or a device-side SC_ERR_*
     int ws_magic;                // set by sc_workspace_init
-    int pad;
+    // exact fixed-point deposit of the FP32 form: charge units of 2^-qfix_shift
+    double qfix_scale;           // 2^qfix_shift
+    float qfix_inv;              // 2^-qfix_shift
+    int qfix_shift;
+    // near box of the hybrid Green's function (cells with all indices below
+    // it use the FP64 8-corner formula)
+    int igf_box[3];
+    unsigned int done_frame;     // blocks finished, for the last-block reductions
+    unsigned int done_extent;
+    int check_code;              // checked builds: first failed index check (kernel code)
+    long long check_index;       // ... and the offending index
 };
 constexpr int WS_MAGIC = 0x5c6b0e11;
 
@@ -68,6 +83,8 @@ struct KickParams {
     double mesh_scale, mesh_shift;       // NaN when unused
     double m_e_eV, m2;                   // m_e_eV and m_e_eV**2
     double four_pi_eps0;                 // 4*pi*epsilon_0
+    // FP32 copies for the FP32 form
+    float gamref_f, betaref_f, grbr_f, pref_f, ipref_f, m_f, m2_f;
 };
 
 // ---------------------------------------------------------------------------
@@ -90,10 +107,12 @@ struct Layout {
     size_t part_frame, part_ext;                 // per-block partial sums (double)
     size_t xp;                                   // FP64: 6 x n lab coordinates
     size_t X;                                    // 3 x n grid coordinates (R)
-    size_t keys, sort_keys, sort_perm, sort_tmp_k, sort_tmp_v, sort_hist, sort_tot;
+    size_t keys, sort_keys, sort_perm, sort_q, sort_tmp_k, sort_tmp_v, sort_hist, sort_tot;
     size_t qgrid, phi, ex, ey, ez;               // [nx][ny][nz] (R)
+    size_t cell_start, cell_end;                 // [nx*ny*nz] uint32 run bounds (adjacent)
+    size_t qfix;                                 // [nx*ny*nz] int64 fixed-point charge (FP32 form)
     size_t igf_ig;                               // (nx+1)(ny+1)(nz+1) double
-    size_t igf_k1;                               // nx*ny*nz double
+    size_t igf_k1;                               // nx*ny*nz (R; double storage size)
     size_t green_s1, green_s2, green;            // spectrum passes (R)
     size_t W;                                    // complex work grid nx*My*Kz
     size_t total;
@@ -101,6 +120,8 @@ struct Layout {
 
 struct Plan {
     int nx, ny, nz, prec;
+    bool sorted_deposit;  // FP64 always; FP32 with SC_FP32_SORTED_DEPOSIT
+    bool exact_igf;       // FP64 always; FP32 with SC_FP32_EXACT_IGF
     int Mx, My, Mz;
     RadixPlan rx, ry, rz;
     int key_bits;
@@ -120,7 +141,11 @@ cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickPar
                          const double* rp, cudaStream_t s);
 cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
                           const double* rp, const double* q, cudaStream_t s);
-cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, cudaStream_t s);
+// rp: the particles (exact recomputation of near-face keys in the FP32 form), or nullptr
+// FP32 form without the sorted deposit: also accumulates q into the
+// fixed-point grid (the deposit)
+cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, const double* rp,
+                        const double* q, cudaStream_t s);
 cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
                                double* rp, cudaStream_t s);
 // el_field entry: extent over a given X[n][3] with a given gamma, and gather to exyz
@@ -131,20 +156,29 @@ cudaError_t launch_gather_xyz(const Plan& p, const Layout& L, char* ws, const Ki
 
 // sort + deposit (sc_sort.cu)
 size_t sort_scratch_bytes(int64_t n, int key_bits);
+int sort_passes(int key_bits);
+// With q_src set, the last pass writes q_src[index] (as double or float) into
+// q_out instead of the permutation.
 cudaError_t launch_sort(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* keys_out,
                         uint32_t* perm_out, uint32_t* tmp_k, uint32_t* tmp_v, uint32_t* hist,
-                        uint32_t* tot, cudaStream_t s);
+                        uint32_t* tot, cudaStream_t s, const double* q_src = nullptr, void* q_out = nullptr,
+                        bool q_float = false);
 cudaError_t launch_deposit(const Plan& p, const Layout& L, char* ws, const double* q, int64_t n,
                            cudaStream_t s);
 
 // Green's function (sc_green.cu)
-cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, double* kern_out, bool force,
-                       cudaStream_t s);
+cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
+cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_out, double hx, double hy,
+                         double hz, cudaStream_t s);
+cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const KickParams& kp, double hx, double hy,
+                            double hz, cudaStream_t s);
 cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
 
 // convolution + field grids (sc_fft.cu)
+// qfix: the fixed-point charge grid of the FP32 form's exact deposit (then
+// qgrid_in receives the scaled grid), or nullptr
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in,
-                            void* phi_out, cudaStream_t s);
+                            void* phi_out, cudaStream_t s, const long long* qfix = nullptr);
 cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
 
 // first-order map (sc_tmap.cu)
@@ -152,5 +186,18 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
                         cudaStream_t s);
 
 inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+
+// Index checks of checked builds (-DSC_CHECKED): a failed check records the
+// kernel code and the index in the state and the access is skipped.
+#ifdef SC_CHECKED
+#define SC_IDX_OK(st, code, idx, size)                                                          \
+    ((long long)(idx) >= 0 && (long long)(idx) < (long long)(size)                            \
+         ? true                                                                                 \
+         : (atomicCAS(&const_cast<ScState*>(st)->check_code, 0, (code)) == 0                   \
+                ? ((const_cast<ScState*>(st)->check_index = (long long)(idx)), false)           \
+                : false))
+#else
+#define SC_IDX_OK(st, code, idx, size) true
+#endif
 
 }  // namespace ocsc

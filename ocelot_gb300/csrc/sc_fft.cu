@@ -38,10 +38,13 @@ static inline int strided_cols(int M) {
     return tk;
 }
 
+// qfix != nullptr: the charge arrives as the 64-bit fixed-point grid of the
+// FP32 form's exact deposit; it is scaled to R here and also stored in q
+// (the charge grid an inspection reads back)
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) k_zfwd(const R* __restrict__ q, Cx<R>* __restrict__ W,
-                                                      int ny, int nz, int My, int Kz, RadixPlan rz,
-                                                      const Cx<R>* __restrict__ twg, int NC,
+__global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const long long* __restrict__ qfix,
+                                                      Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
+                                                      RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
                                                       const ScState* st) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
@@ -57,8 +60,17 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(const R* __restrict__ q, C
         const int ya = y0 + 2 * c, yb = ya + 1;
         R re = 0, im = 0;
         if (z < nz) {
-            if (ya < ny) re = q[((size_t)x * ny + ya) * nz + z];
-            if (yb < ny) im = q[((size_t)x * ny + yb) * nz + z];
+            const size_t ia = ((size_t)x * ny + ya) * nz + z, ib = ia + nz;
+            const long long ncell = (long long)gridDim.y * ny * nz;
+            if ((ya < ny && !SC_IDX_OK(st, 21, ia, ncell)) || (yb < ny && !SC_IDX_OK(st, 22, ib, ncell))) continue;
+            if (qfix) {
+                const float u = st->qfix_inv;
+                if (ya < ny) { re = (R)(__ll2float_rn(qfix[ia]) * u); q[ia] = re; }
+                if (yb < ny) { im = (R)(__ll2float_rn(qfix[ib]) * u); q[ib] = im; }
+            } else {
+                if (ya < ny) re = q[ia];
+                if (yb < ny) im = q[ib];
+            }
         }
         a[idx] = cx<R>(re, im);
     }
@@ -70,6 +82,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(const R* __restrict__ q, C
         const Cx<R> Z = res[c * Mz + k];
         const Cx<R> Zm = res[c * Mz + (k == 0 ? 0 : Mz - k)];
         const R h = (R)0.5;
+        if (!SC_IDX_OK(st, 24, ((long long)x * My + (yb < ny ? yb : ya)) * Kz + k, (long long)gridDim.y * My * Kz)) continue;
         if (ya < ny) W[((size_t)x * My + ya) * Kz + k] = cx<R>((Z.x + Zm.x) * h, (Z.y - Zm.y) * h);
         if (yb < ny) W[((size_t)x * My + yb) * Kz + k] = cx<R>((Z.y + Zm.y) * h, (Zm.x - Z.x) * h);
     }
@@ -132,7 +145,8 @@ __global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, co
     for (int idx = threadIdx.x; idx < Mx * TK; idx += blockDim.x) {
         const int kx = idx / TK, kk = idx - kx * TK, k = k0 + kk;
         const int gx = kx <= Mx - kx ? kx : Mx - kx;
-        const R g = k < Kz ? G[((size_t)gx * Ky + gy) * Kz + k] : (R)0;
+        const long long gi = ((long long)gx * Ky + gy) * Kz + k;
+        const R g = (k < Kz && SC_IDX_OK(st, 23, gi, (long long)(rx.L / 2 + 1) * Ky * Kz)) ? G[gi] : (R)0;
         Cx<R> v = res[kk * ls + kx];
         v.x *= g;
         v.y *= g;
@@ -226,7 +240,7 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
 }
 
 template <typename R>
-static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, const R* qgrid, R* phi,
+static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid, R* phi, const long long* qfix,
                               cudaStream_t s) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int Kz = p.Mz / 2 + 1, Ky = p.My / 2 + 1;
@@ -240,7 +254,7 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, const R*
     const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
     dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
     if ((e = set_smem(k_zfwd<R>, smz))) return e;
-    k_zfwd<R><<<gz, FFT_THREADS, smz, s>>>(qgrid, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+    k_zfwd<R><<<gz, FFT_THREADS, smz, s>>>(qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
     const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
     dim3 gy((Kz + tky - 1) / tky, p.nx);
@@ -258,10 +272,12 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, const R*
 }
 
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in, void* phi_out,
-                            cudaStream_t s) {
+                            cudaStream_t s, const long long* qfix) {
     if (p.prec == SC_FP64)
-        return convolve_t<double>(p, L, ws, static_cast<const double*>(qgrid_in), static_cast<double*>(phi_out), s);
-    return convolve_t<float>(p, L, ws, static_cast<const float*>(qgrid_in), static_cast<float*>(phi_out), s);
+        return convolve_t<double>(p, L, ws, static_cast<double*>(const_cast<void*>(qgrid_in)),
+                                  static_cast<double*>(phi_out), nullptr, s);
+    return convolve_t<float>(p, L, ws, static_cast<float*>(const_cast<void*>(qgrid_in)), static_cast<float*>(phi_out),
+                             qfix, s);
 }
 
 template <typename R>

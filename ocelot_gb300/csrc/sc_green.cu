@@ -29,11 +29,33 @@ struct IgfArgs {
     double hx, hy, hz;
     int use_state;  // take the spacing from ScState::steps
     int force;      // build even if the cache is valid
+    int hybrid;     // FP32 form: 8-corner formula only inside the near box
 };
 
 __device__ __forceinline__ bool igf_skip(const ScState* st, const IgfArgs& a) {
     if (a.force) return false;
     return st->status != SC_OK || !st->igf_rebuild;
+}
+
+__device__ __forceinline__ void igf_spacing(const ScState* st, const IgfArgs& a, double& hx, double& hy, double& hz) {
+    hx = a.hx; hy = a.hy; hz = a.hz;
+    if (a.use_state) { hx = st->steps[0]; hy = st->steps[1]; hz = st->steps[2]; }
+}
+
+// Near box of the hybrid table: along each axis the cells with index below
+// ceil(5 hmax / h) + 1.  Every cell outside it is at least 5 hmax from the
+// origin, where the 4th-order multipole form of the cell integral is within
+// 5e-8 of the exact integral (checked against an extended-precision IGF).
+__device__ __forceinline__ void igf_box(double hx, double hy, double hz, int nx, int ny, int nz, int hybrid, int b[3]) {
+    if (!hybrid) { b[0] = nx; b[1] = ny; b[2] = nz; return; }
+    const double hm = fmax(hx, fmax(hy, hz));
+    const double h[3] = {hx, hy, hz};
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+        const double v = 5.0 * hm / h[a];
+        b[a] = v >= (double)n[a] ? n[a] : (int)ceil(v) + 1;
+        if (b[a] > n[a]) b[a] = n[a];
+    }
 }
 
 __device__ __forceinline__ double igf_point(double x, double y, double z) {
@@ -47,11 +69,15 @@ __device__ __forceinline__ double igf_point(double x, double y, double z) {
     return __dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(t1, t2), t3), t4), t5), t6);
 }
 
+// IG on the corners of the near box (the whole octant when not hybrid),
+// stored with the box's corner strides
 __global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, IgfArgs a, const ScState* st) {
     if (igf_skip(st, a)) return;
-    double hx = a.hx, hy = a.hy, hz = a.hz;
-    if (a.use_state) { hx = st->steps[0]; hy = st->steps[1]; hz = st->steps[2]; }
-    const int cx1 = nx + 1, cy1 = ny + 1, cz1 = nz + 1;
+    double hx, hy, hz;
+    igf_spacing(st, a, hx, hy, hz);
+    int b[3];
+    igf_box(hx, hy, hz, nx, ny, nz, a.hybrid, b);
+    const int cx1 = b[0] + 1, cy1 = b[1] + 1, cz1 = b[2] + 1;
     const size_t total = (size_t)cx1 * cy1 * cz1;
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
         const int k = (int)(c % cz1);
@@ -60,28 +86,67 @@ __global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, I
         const double x = __dsub_rn(__dmul_rn(hx, (double)i), __dmul_rn(hx, 0.5));
         const double y = __dsub_rn(__dmul_rn(hy, (double)j), __dmul_rn(hy, 0.5));
         const double z = __dsub_rn(__dmul_rn(hz, (double)k), __dmul_rn(hz, 0.5));
+        if (!SC_IDX_OK(st, 31, c, (long long)(nx + 1) * (ny + 1) * (nz + 1))) continue;
         ig[c] = igf_point(x, y, z);
     }
 }
 
-__global__ void k_igf_diff(const double* __restrict__ ig, double* __restrict__ k1, int nx, int ny, int nz,
-                           IgfArgs a, const ScState* st) {
+// 4th-order multipole form of the integral of 1/r over the cell centred at
+// (X,Y,Z) with half-widths (a,b,c), in FP32:
+//   V/R [1 + (a^2(3x^2-1) + b^2(3y^2-1) + c^2(3z^2-1)) / (6 R^2)
+//        + (sum a^4 F4(x^2)/120 + sum a^2 b^2 F22(x^2,y^2)/36) / R^4],
+//   x = X/R, ..., F4(u) = 3(35u^2 - 30u + 3), F22(u,v) = 3(35uv - 5(u+v) + 1)
+// (the Taylor expansion of 1/|R+s| averaged over the box; odd orders vanish)
+__device__ __forceinline__ float cell_multipole(float X, float Y, float Z, float a2, float b2, float c2, float V) {
+    const float R2 = X * X + Y * Y + Z * Z;
+    const float iR2 = 1.0f / R2, iR = rsqrtf(R2);
+    const float x2 = X * X * iR2, y2 = Y * Y * iR2, z2 = Z * Z * iR2;
+    const float A = a2 * iR2, B = b2 * iR2, Cc = c2 * iR2;
+    const float t2 = (A * (3.f * x2 - 1.f) + B * (3.f * y2 - 1.f) + Cc * (3.f * z2 - 1.f)) * (1.0f / 6.0f);
+    const float f4x = 3.f * (35.f * x2 * x2 - 30.f * x2 + 3.f);
+    const float f4y = 3.f * (35.f * y2 * y2 - 30.f * y2 + 3.f);
+    const float f4z = 3.f * (35.f * z2 * z2 - 30.f * z2 + 3.f);
+    const float fxy = 3.f * (35.f * x2 * y2 - 5.f * (x2 + y2) + 1.f);
+    const float fxz = 3.f * (35.f * x2 * z2 - 5.f * (x2 + z2) + 1.f);
+    const float fyz = 3.f * (35.f * y2 * z2 - 5.f * (y2 + z2) + 1.f);
+    const float t4 = (A * A * f4x + B * B * f4y + Cc * Cc * f4z) * (1.0f / 120.0f) +
+                     (A * B * fxy + A * Cc * fxz + B * Cc * fyz) * (1.0f / 36.0f);
+    return V * iR * (1.0f + t2 + t4);
+}
+
+// cell integrals: the 8-corner difference of IG inside the near box (FP64),
+// the multipole form outside it (FP32 form only); written as R
+template <typename R>
+__global__ void k_igf_diff(const double* __restrict__ ig, R* __restrict__ k1, int nx, int ny, int nz, IgfArgs a,
+                           const ScState* st) {
     if (igf_skip(st, a)) return;
+    double hx, hy, hz;
+    igf_spacing(st, a, hx, hy, hz);
+    int bx[3];
+    igf_box(hx, hy, hz, nx, ny, nz, a.hybrid, bx);
+    const float hxf = (float)hx, hyf = (float)hy, hzf = (float)hz;
+    const float a2 = 0.25f * hxf * hxf, b2 = 0.25f * hyf * hyf, c2 = 0.25f * hzf * hzf, V = hxf * hyf * hzf;
     const size_t total = (size_t)nx * ny * nz;
-    const size_t sy = nz + 1, sx = (size_t)(ny + 1) * (nz + 1);
+    const size_t sy = bx[2] + 1, sx = (size_t)(bx[1] + 1) * (bx[2] + 1);
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
         const int k = (int)(c % nz);
         const int j = (int)((c / nz) % ny);
         const int i = (int)(c / ((size_t)nz * ny));
-        const size_t o = i * sx + j * sy + k;
-        double v = __dsub_rn(ig[o + sx + sy + 1], ig[o + sy + 1]);
-        v = __dsub_rn(v, ig[o + sx + 1]);
-        v = __dadd_rn(v, ig[o + 1]);
-        v = __dsub_rn(v, ig[o + sx + sy]);
-        v = __dadd_rn(v, ig[o + sy]);
-        v = __dadd_rn(v, ig[o + sx]);
-        v = __dsub_rn(v, ig[o]);
-        k1[c] = v;
+        if (i < bx[0] && j < bx[1] && k < bx[2]) {
+            const size_t o = i * sx + j * sy + k;
+            if (!SC_IDX_OK(st, 32, o + sx + sy + 1, (long long)(nx + 1) * (ny + 1) * (nz + 1))) continue;
+            double v = __dsub_rn(ig[o + sx + sy + 1], ig[o + sy + 1]);
+            v = __dsub_rn(v, ig[o + sx + 1]);
+            v = __dadd_rn(v, ig[o + 1]);
+            v = __dsub_rn(v, ig[o + sx + sy]);
+            v = __dadd_rn(v, ig[o + sy]);
+            v = __dadd_rn(v, ig[o + sx]);
+            v = __dsub_rn(v, ig[o]);
+            k1[c] = (R)v;
+        } else {
+            if (!SC_IDX_OK(st, 34, c, total)) continue;
+            k1[c] = (R)cell_multipole((float)i * hxf, (float)j * hyf, (float)k * hzf, a2, b2, c2, V);
+        }
     }
 }
 
@@ -104,7 +169,7 @@ static inline int green_cols(int M) {
 
 // S1: along z; rows (x, y) of K1 -> S1[x][y][kz], kz <= Mz/2
 template <typename R>
-__global__ void __launch_bounds__(GT) k_green_z(const double* __restrict__ k1, R* __restrict__ s1, int ny, int nz,
+__global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __restrict__ s1, int ny, int nz,
                                                 int Kz, RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
                                                 IgfArgs a, const ScState* st) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -120,9 +185,9 @@ __global__ void __launch_bounds__(GT) k_green_z(const double* __restrict__ k1, R
         const int ya = y0 + 2 * c, yb = ya + 1;
         const int zs = even_src(z, nz, Mz);
         R re = 0, im = 0;
-        if (zs >= 0) {
-            if (ya < ny) re = (R)k1[((size_t)x * ny + ya) * nz + zs];
-            if (yb < ny) im = (R)k1[((size_t)x * ny + yb) * nz + zs];
+        if (zs >= 0 && SC_IDX_OK(st, 33, ((long long)x * ny + (ya < ny ? ya : 0)) * nz + zs, (long long)gridDim.y * ny * nz)) {
+            if (ya < ny) re = k1[((size_t)x * ny + ya) * nz + zs];
+            if (yb < ny) im = k1[((size_t)x * ny + yb) * nz + zs];
         }
         A[idx] = cx<R>(re, im);
     }
@@ -132,6 +197,7 @@ __global__ void __launch_bounds__(GT) k_green_z(const double* __restrict__ k1, R
         const int c = idx / Kz, k = idx - c * Kz;
         const int ya = y0 + 2 * c, yb = ya + 1;
         const Cx<R> v = res[c * Mz + k];
+        if (!SC_IDX_OK(st, 35, ((long long)x * ny + (yb < ny ? yb : ya)) * Kz + k, (long long)gridDim.y * ny * Kz)) continue;
         if (ya < ny) s1[((size_t)x * ny + ya) * Kz + k] = v.x;
         if (yb < ny) s1[((size_t)x * ny + yb) * Kz + k] = v.y;
     }
@@ -190,14 +256,6 @@ static int grid_for(size_t work, int sm) {
     return (int)(b < cap ? (b ? b : 1) : cap);
 }
 
-static IgfArgs state_args(bool force) {
-    IgfArgs a;
-    a.hx = a.hy = a.hz = 0;
-    a.use_state = 1;
-    a.force = force ? 1 : 0;
-    return a;
-}
-
 cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_out, double hx, double hy,
                          double hz, cudaStream_t s) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
@@ -205,32 +263,49 @@ cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_
     a.hx = hx; a.hy = hy; a.hz = hz;
     a.use_state = 0;
     a.force = 1;
+    a.hybrid = 0;
     double* ig = reinterpret_cast<double*>(ws + L.igf_ig);
     const size_t nc = (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1);
     k_igf_corners<<<grid_for(nc, p.sm_count), 256, 0, s>>>(ig, p.nx, p.ny, p.nz, a, st);
     const size_t nk = (size_t)p.nx * p.ny * p.nz;
-    k_igf_diff<<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, kern_out, p.nx, p.ny, p.nz, a, st);
+    k_igf_diff<double><<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, kern_out, p.nx, p.ny, p.nz, a, st);
     return cudaGetLastError();
 }
 
-cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, double* kern_out, bool force, cudaStream_t s) {
+cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
-    IgfArgs a = state_args(force);
+    IgfArgs a;
+    a.hx = a.hy = a.hz = 0;
+    a.use_state = 1;
+    a.force = 0;
+    a.hybrid = p.exact_igf ? 0 : 1;
     double* ig = reinterpret_cast<double*>(ws + L.igf_ig);
-    double* k1 = kern_out ? kern_out : reinterpret_cast<double*>(ws + L.igf_k1);
     const size_t nc = (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1);
-    k_igf_corners<<<grid_for(nc, p.sm_count), 256, 0, s>>>(ig, p.nx, p.ny, p.nz, a, st);
+    // one block per SM: eight warps keep an SM's FP64 pipe busy, and the
+    // registers left over hold the blocks of the concurrent particle kernels
+    size_t gb = (nc + 255) / 256;
+    if (gb > (size_t)p.sm_count) gb = (size_t)p.sm_count;
+    k_igf_corners<<<(int)gb, 256, 0, s>>>(ig, p.nx, p.ny, p.nz, a, st);
     const size_t nk = (size_t)p.nx * p.ny * p.nz;
-    k_igf_diff<<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, k1, p.nx, p.ny, p.nz, a, st);
+    if (p.prec == SC_FP64)
+        k_igf_diff<double><<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, reinterpret_cast<double*>(ws + L.igf_k1), p.nx,
+                                                                     p.ny, p.nz, a, st);
+    else
+        k_igf_diff<float><<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, reinterpret_cast<float*>(ws + L.igf_k1), p.nx,
+                                                                    p.ny, p.nz, a, st);
     return cudaGetLastError();
 }
 
 template <typename R>
 static cudaError_t spectrum_t(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
-    IgfArgs a = state_args(false);
+    IgfArgs a;
+    a.hx = a.hy = a.hz = 0;
+    a.use_state = 1;
+    a.force = 0;
+    a.hybrid = 0;
     const int Kx = p.Mx / 2 + 1, Ky = p.My / 2 + 1, Kz = p.Mz / 2 + 1;
-    const double* k1 = reinterpret_cast<const double*>(ws + L.igf_k1);
+    const R* k1 = reinterpret_cast<const R*>(ws + L.igf_k1);
     R* s1 = reinterpret_cast<R*>(ws + L.green_s1);
     R* s2 = reinterpret_cast<R*>(ws + L.green_s2);
     R* g = reinterpret_cast<R*>(ws + L.green);

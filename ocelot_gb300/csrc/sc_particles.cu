@@ -18,7 +18,7 @@
 // added to the FP64 coordinates:
 //     dE   = (2 p.dp + |dp|^2) / (E + E')
 //     dx'  = dpx/pref, dy' = dpy/pref, ddelta = dE/pref
-//     dtau = tau (pz dE - E dpz) / (E pz')
+//     dtau = tau (pz E' - pz' E) / (E pz'), the bracket in a cancellation-free form
 //     dx   = tau (dpx E - px dE) / (E E') + (px'/E') dtau      (same for y)
 // Reductions are deterministic: a fixed grid, shuffle trees within blocks,
 // per-block partials in HBM and a one-block finalize in a fixed order.
@@ -32,8 +32,11 @@ constexpr unsigned FULL = 0xffffffffu;
 // ---------------------------------------------------------------------------
 // deterministic block reductions
 // ---------------------------------------------------------------------------
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double* sm /* NV*32 */) {
+// The shared scratch is passed as a sized array so that a scratch smaller
+// than NV*32 elements is a compile-time error.
+template <int NV, int SZ>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (&sm)[SZ]) {
+    static_assert(SZ >= NV * 32, "block_sum: shared scratch too small");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int c = 0; c < NV; ++c)
@@ -52,8 +55,9 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sm /* NV*32 *
     __syncthreads();
 }
 
-template <int NV, bool MAX>
-__device__ __forceinline__ void block_minmax(double (&v)[NV], double* sm) {
+template <int NV, bool MAX, int SZ>
+__device__ __forceinline__ void block_minmax(double (&v)[NV], double (&sm)[SZ]) {
+    static_assert(SZ >= NV * 32, "block_minmax: shared scratch too small");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int c = 0; c < NV; ++c)
@@ -77,6 +81,34 @@ __device__ __forceinline__ void block_minmax(double (&v)[NV], double* sm) {
     }
     __syncthreads();
 }
+
+template <int NV, bool MAX, int SZ>
+__device__ __forceinline__ void block_minmax_f(float (&v)[NV], float (&sm)[SZ]) {
+    static_assert(SZ >= NV * 32, "block_minmax_f: shared scratch too small");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+        for (int o = 16; o; o >>= 1) {
+            const float w = __shfl_xor_sync(FULL, v[c], o);
+            v[c] = MAX ? fmaxf(v[c], w) : fminf(v[c], w);
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sm[c * 32 + warp] = v[c];
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        float r = lane < nw ? sm[c * 32 + lane] : (MAX ? -INFINITY : INFINITY);
+        for (int o = 16; o; o >>= 1) {
+            const float w = __shfl_xor_sync(FULL, r, o);
+            r = MAX ? fmaxf(r, w) : fminf(r, w);
+        }
+        v[c] = r;  // every thread holds the block result
+    }
+    __syncthreads();
+}
+
+constexpr int PART_EXT = 11;
 
 // ---------------------------------------------------------------------------
 // FP64 transforms in the reference's operation order
@@ -123,85 +155,73 @@ __device__ __forceinline__ double dot3_blas(double a0, double a1, double a2, dou
 }
 
 // ---------------------------------------------------------------------------
-// FP32 forward quantities from the FP64 MAD coordinates
+// FP64 <-> FP32 conversions on the integer pipes.  On this GPU the hardware
+// conversions issue on the FP64 pipe, which the FP32 form keeps free for its
+// six FP64 accumulations per particle.
 // ---------------------------------------------------------------------------
-struct F32Consts {
-    float gamref, betaref, grbr, pref, m, m2;
-};
-__device__ __forceinline__ F32Consts f32c(const KickParams& kp) {
-    F32Consts c;
-    c.gamref = (float)kp.gamref;
-    c.betaref = (float)kp.betaref;
-    c.grbr = (float)kp.grbr;
-    c.pref = (float)kp.pref;
-    c.m = (float)kp.m_e_eV;
-    c.m2 = c.m * c.m;
-    return c;
+// round-half-up to the nearest float (|error| <= 2^-24 relative); magnitudes
+// below 2^-126 flush to zero, above FLT_MAX become infinity, NaN stays NaN
+__device__ __forceinline__ float d2f(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned f;
+    if (e <= 896) f = sign;
+    else if (e >= 1151) f = sign | 0x7f800000u | ((e == 2047 && ((hi & 0xfffffu) | lo)) ? 0x400000u : 0u);
+    else f = (sign | ((unsigned)(e - 896) << 23) | mant) + ((lo >> 28) & 1u);
+    return __uint_as_float(f);
 }
-// momenta (eV/c) and energy (eV) of one particle, FP32
-__device__ __forceinline__ void mom32(float xq, float yq, float d, const F32Consts& c, float& px, float& py,
+// exact widening (float subnormals, which the kick never produces, read as 0)
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned hi, lo;
+    if (e == 0) { hi = sign; lo = 0u; }
+    else if (e == 255) { hi = sign | 0x7ff00000u | (m >> 3); lo = m << 29; }
+    else { hi = sign | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// momenta (eV/c) and energy (eV) of one particle in FP32 (coord_transform.py:64-72)
+__device__ __forceinline__ void mom32(float xq, float yq, float d, const KickParams& kp, float& px, float& py,
                                       float& pz, float& E) {
-    const float gamma = c.gamref * (1.0f + c.betaref * d);
+    const float gamma = kp.gamref_f * (1.0f + kp.betaref_f * d);
     const float beta = sqrtf(1.0f - 1.0f / (gamma * gamma));
-    const float g = gamma * beta / c.grbr;
+    const float g = gamma * beta / kp.grbr_f;
     const float pz2 = sqrtf(g * g - xq * xq - yq * yq);
-    px = xq * c.pref;
-    py = yq * c.pref;
-    pz = pz2 * c.pref;
-    E = gamma * c.m;
+    px = xq * kp.pref_f;
+    py = yq * kp.pref_f;
+    pz = pz2 * kp.pref_f;
+    E = gamma * kp.m_f;
 }
 
 // ---------------------------------------------------------------------------
-// frame: sum of momenta (+ FP64: lab coordinates stored for later stages)
+// last-block reductions: every block writes its partials, the last block to
+// finish reduces all of them in block order (deterministic) and resets the
+// counter for the next launch
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(PT) k_frame64(const double* __restrict__ rp, KickParams kp,
-                                                double* __restrict__ xp, double* __restrict__ part) {
-    __shared__ double sm[3 * 32];
-    double acc[3] = {0.0, 0.0, 0.0};
-    const int64_t n = kp.n, ld = kp.ld;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double r[6], c[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i];
-        mad_to_cart64(r, kp, c);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) xp[k * n + i] = c[k];
-        acc[0] += c[3];
-        acc[1] += c[4];
-        acc[2] += c[5];
+__device__ __forceinline__ bool arrive_last(unsigned int* counter) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
-    block_sum<3>(acc, sm);
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = acc[k];
+    __syncthreads();
+    return last;
 }
 
-__global__ void __launch_bounds__(PT) k_frame32(const double* __restrict__ rp, KickParams kp,
-                                                double* __restrict__ part) {
-    __shared__ double sm[3 * 32];
-    const F32Consts c = f32c(kp);
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    const int64_t n = kp.n, ld = kp.ld;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        float px, py, pz, E;
-        mom32((float)rp[ld + i], (float)rp[3 * ld + i], (float)rp[5 * ld + i], c, px, py, pz, E);
-        a0 += px;
-        a1 += py;
-        a2 += pz;
-    }
-    double acc[3] = {a0, a1, a2};
-    block_sum<3>(acc, sm);
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = acc[k];
-}
-
-// one block: mean momentum -> basis T, gamma0, beta0 (sc.py:224-239, 243-248)
-__global__ void k_frame_finalize(const double* __restrict__ part, int nblk, KickParams kp, ScState* st) {
+// mean momentum -> basis T, gamma0, beta0 (sc.py:224-239, 243-248); called by
+// the last block of a frame kernel with all per-block momentum sums in part
+__device__ void frame_finalize(const double* part, int nblk, const KickParams& kp, ScState* st) {
     __shared__ double sm[3 * 32];
     double acc[3] = {0.0, 0.0, 0.0};
     for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-        for (int k = 0; k < 3; ++k) acc[k] += part[b * 3 + k];
+        for (int k = 0; k < 3; ++k) acc[k] += __ldcg(part + b * 3 + k);
     block_sum<3>(acc, sm);
     if (threadIdx.x != 0) return;
+    st->done_frame = 0;
     const double nn = (double)kp.n;
     double t3[3] = {__ddiv_rn(acc[0], nn), __ddiv_rn(acc[1], nn), __ddiv_rn(acc[2], nn)};
     const double Pav = __dsqrt_rn(__fma_rn(t3[2], t3[2], __fma_rn(t3[1], t3[1], __dmul_rn(t3[0], t3[0]))));
@@ -218,6 +238,9 @@ __global__ void k_frame_finalize(const double* __restrict__ part, int nblk, Kick
         st->T[i][0] = t1[i];
         st->T[i][1] = t2[i];
         st->T[i][2] = t3[i];
+        st->Tf[i][0] = (float)t1[i];
+        st->Tf[i][1] = (float)t2[i];
+        st->Tf[i][2] = (float)t3[i];
     }
     const double pm = __ddiv_rn(Pav, kp.m_e_eV);
     const double gamma0 = __dsqrt_rn(__dadd_rn(__dmul_rn(pm, pm), 1.0));
@@ -227,143 +250,43 @@ __global__ void k_frame_finalize(const double* __restrict__ part, int nblk, Kick
     st->beta0 = beta0;
     st->kxy = __dmul_rn(kp.cdT, __dsub_rn(1.0, __dmul_rn(beta0, beta0)));
     st->kz = kp.cdT;
+    st->g0f = (float)gamma0;
+    st->ig0f = (float)(1.0 / gamma0);
+    st->kxyf = (float)st->kxy;
+    st->kzf = (float)kp.cdT;
     int status = SC_OK;
     if (!(Pav > 0.0) || !isfinite(Pav) || !isfinite(gamma0) || !isfinite(t1[0]) || !isfinite(t2[1])) status = SC_ERR_NONFINITE;
     st->status = status;
 }
 
-// ---------------------------------------------------------------------------
-// extent: rotated positions (z scaled by gamma0), min/max, charge moments
-// part layout per block: min[3], max[3], sum q*x[3], sum q
-// ---------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ void extent_block_out(double (&mn)[3], double (&mx)[3], double (&qs)[4], double* sm,
-                                                 double* part) {
-    block_minmax<3, false>(mn, sm);
-    block_minmax<3, true>(mx, sm);
-    block_sum<4>(qs, sm);
-    if (threadIdx.x == 0) {
-        double* o = part + blockIdx.x * 10;
-        for (int k = 0; k < 3; ++k) {
-            o[k] = mn[k];
-            o[3 + k] = mx[k];
-            o[6 + k] = qs[k];
-        }
-        o[9] = qs[3];
-    }
-}
-
-__global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, const double* __restrict__ q,
-                                                 KickParams kp, double* __restrict__ X, double* __restrict__ part,
-                                                 const ScState* st) {
-    __shared__ double sm[4 * 32];
+// steps, X_off, potential scale, Green cache check (sc.py:172-186, 167)
+// part layout per block (PART_EXT doubles): min[3], max[3], sum q*x[3], sum q, sum |q|
+__device__ void mesh_finalize(const double* part, int nblk, const KickParams& kp, ScState* st, double gamma_override) {
+    __shared__ double sm[5 * 32];
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double qs[4] = {0.0, 0.0, 0.0, 0.0};
-    const int64_t n = kp.n;
-    const bool ok = st->status == SC_OK;
-    double T[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) T[i][j] = st->T[i][j];
-    const double g0 = st->gamma0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ok && i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double a0 = xp[i], a1 = xp[n + i], a2 = xp[2 * n + i];
-        double v[3];
-        for (int j = 0; j < 3; ++j) v[j] = dot3_blas(a0, a1, a2, T[0][j], T[1][j], T[2][j]);
-        v[2] = __dmul_rn(v[2], g0);
-        const double qi = q[i];
-        for (int j = 0; j < 3; ++j) {
-            X[j * n + i] = v[j];
-            mn[j] = fmin(mn[j], v[j]);
-            mx[j] = fmax(mx[j], v[j]);
-            qs[j] += qi * v[j];
-        }
-        qs[3] += qi;
-    }
-    extent_block_out<double>(mn, mx, qs, sm, part);
-}
-
-__global__ void __launch_bounds__(PT) k_extent32(const double* __restrict__ rp, const double* __restrict__ q,
-                                                 KickParams kp, float* __restrict__ X, double* __restrict__ part,
-                                                 const ScState* st) {
-    __shared__ double sm[4 * 32];
-    const F32Consts c = f32c(kp);
-    float mnf[3] = {INFINITY, INFINITY, INFINITY}, mxf[3] = {-INFINITY, -INFINITY, -INFINITY};
-    float qsf[4] = {0.f, 0.f, 0.f, 0.f};
-    const int64_t n = kp.n, ld = kp.ld;
-    const bool ok = st->status == SC_OK;
-    float T[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) T[i][j] = (float)st->T[i][j];
-    const float g0 = (float)st->gamma0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ok && i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float xq = (float)rp[ld + i], yq = (float)rp[3 * ld + i], d = (float)rp[5 * ld + i];
-        const float tau = (float)rp[4 * ld + i];
-        float px, py, pz, E;
-        mom32(xq, yq, d, c, px, py, pz, E);
-        const float s = tau / E;
-        const float l0 = (float)rp[i] - px * s, l1 = (float)rp[2 * ld + i] - py * s, l2 = -pz * s;
-        float v[3];
-        for (int j = 0; j < 3; ++j) v[j] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
-        v[2] *= g0;
-        const float qi = (float)q[i];
-        for (int j = 0; j < 3; ++j) {
-            X[j * n + i] = v[j];
-            mnf[j] = fminf(mnf[j], v[j]);
-            mxf[j] = fmaxf(mxf[j], v[j]);
-            qsf[j] += qi * v[j];
-        }
-        qsf[3] += qi;
-    }
-    double mn[3] = {mnf[0], mnf[1], mnf[2]}, mx[3] = {mxf[0], mxf[1], mxf[2]};
-    double qs[4] = {qsf[0], qsf[1], qsf[2], qsf[3]};
-    extent_block_out<float>(mn, mx, qs, sm, part);
-}
-
-// el_field entry: X given as [n][3] rotated positions; z scaled by gamma in place
-template <typename R>
-__global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, const double* __restrict__ q, int64_t n,
-                                                   double gamma, R* __restrict__ X, double* __restrict__ part) {
-    __shared__ double sm[4 * 32];
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double qs[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double v[3] = {Xin[3 * i], Xin[3 * i + 1], __dmul_rn(Xin[3 * i + 2], gamma)};
-        Xin[3 * i + 2] = v[2];
-        const double qi = q[i];
-        for (int j = 0; j < 3; ++j) {
-            X[j * n + i] = (R)v[j];
-            mn[j] = fmin(mn[j], v[j]);
-            mx[j] = fmax(mx[j], v[j]);
-            qs[j] += qi * v[j];
-        }
-        qs[3] += qi;
-    }
-    extent_block_out<R>(mn, mx, qs, sm, part);
-}
-
-// one block: steps, X_off, potential scale, Green cache check (sc.py:172-186, 167)
-__global__ void k_mesh_finalize(const double* __restrict__ part, int nblk, KickParams kp, ScState* st,
-                                double gamma_override) {
-    __shared__ double sm[4 * 32];
-    if (gamma_override > 0.0 && threadIdx.x == 0) st->status = SC_OK;
-    __syncthreads();
-    const bool ok = st->status == SC_OK;
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double qs[4] = {0.0, 0.0, 0.0, 0.0};
+    double qs[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-        const double* o = part + b * 10;
+        const double* o = part + b * PART_EXT;
         for (int k = 0; k < 3; ++k) {
-            mn[k] = fmin(mn[k], o[k]);
-            mx[k] = fmax(mx[k], o[3 + k]);
-            qs[k] += o[6 + k];
+            mn[k] = fmin(mn[k], __ldcg(o + k));
+            mx[k] = fmax(mx[k], __ldcg(o + 3 + k));
+            qs[k] += __ldcg(o + 6 + k);
         }
-        qs[3] += o[9];
+        qs[3] += __ldcg(o + 9);
+        qs[4] += __ldcg(o + 10);
     }
     block_minmax<3, false>(mn, sm);
     block_minmax<3, true>(mx, sm);
-    block_sum<4>(qs, sm);
-    if (threadIdx.x != 0 || !ok) return;
-    if (gamma_override > 0.0) st->gamma0 = gamma_override;
+    block_sum<5>(qs, sm);
+    if (threadIdx.x != 0) return;
+    st->done_extent = 0;
+    if (gamma_override > 0.0) {
+        st->gamma0 = gamma_override;
+        st->g0f = (float)gamma_override;
+        st->ig0f = (float)(1.0 / gamma_override);
+        st->status = SC_OK;
+    }
+    if (st->status != SC_OK) return;
     const int nm[3] = {kp.nx, kp.ny, kp.nz};
     double steps[3], xoff[3];
     bool bad = !(qs[3] != 0.0) || !isfinite(qs[3]);
@@ -384,12 +307,267 @@ __global__ void k_mesh_finalize(const double* __restrict__ part, int nblk, KickP
     for (int k = 0; k < 3; ++k) {
         st->steps[k] = steps[k];
         st->xoff[k] = xoff[k];
+        st->isteps[k] = 1.0 / steps[k];
+        st->stepsf[k] = (float)steps[k];
+        st->istepsf[k] = (float)(1.0 / steps[k]);
+        st->xofff[k] = (float)xoff[k];
     }
     st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, steps[0]), steps[1]), steps[2]);
     st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
     const bool same = steps[0] == st->igf_h[0] && steps[1] == st->igf_h[1] && steps[2] == st->igf_h[2];
     st->igf_rebuild = same ? 0 : 1;
     for (int k = 0; k < 3; ++k) st->igf_h[k] = steps[k];
+    // fixed-point unit of the exact deposit: sum |q| * 2^S < 2^62, so no cell
+    // (nor the total) can overflow a signed 64-bit accumulator
+    int e2;
+    frexp(qs[4], &e2);
+    const int S = 62 - e2;
+    st->qfix_shift = S;
+    st->qfix_scale = ldexp(1.0, S);
+    st->qfix_inv = (float)ldexp(1.0, -S);
+}
+
+// ---------------------------------------------------------------------------
+// frame: sum of momenta (+ FP64: lab coordinates stored for later stages)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PT) k_frame64(const double* __restrict__ rp, KickParams kp,
+                                                double* __restrict__ xp, double* __restrict__ part, ScState* st) {
+    __shared__ double sm[3 * 32];
+    double acc[3] = {0.0, 0.0, 0.0};
+    const int64_t n = kp.n, ld = kp.ld;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double r[6], c[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i];
+        mad_to_cart64(r, kp, c);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xp[k * n + i] = c[k];
+        acc[0] += c[3];
+        acc[1] += c[4];
+        acc[2] += c[5];
+    }
+    block_sum<3>(acc, sm);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = acc[k];
+    if (arrive_last(&st->done_frame)) frame_finalize(part, gridDim.x, kp, st);
+}
+
+__global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
+                                                   double* __restrict__ part, ScState* st) {
+    __shared__ double sm[3 * 32];
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    const int64_t n = kp.n, ld = kp.ld;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float px, py, pz, E;
+        mom32(d2f(rp[ld + i]), d2f(rp[3 * ld + i]), d2f(rp[5 * ld + i]), kp, px, py, pz, E);
+        a0 += px;
+        a1 += py;
+        a2 += pz;
+    }
+    double acc[3] = {a0, a1, a2};
+    block_sum<3>(acc, sm);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = acc[k];
+    if (arrive_last(&st->done_frame)) frame_finalize(part, gridDim.x, kp, st);
+}
+
+// ---------------------------------------------------------------------------
+// extent: rotated positions (z scaled by gamma0), min/max, charge moments
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void extent_block_out(double (&mn)[3], double (&mx)[3], double (&qs)[5],
+                                                 double (&sm)[5 * 32], double* part) {
+    block_minmax<3, false>(mn, sm);
+    block_minmax<3, true>(mx, sm);
+    block_sum<5>(qs, sm);
+    if (threadIdx.x == 0) {
+        double* o = part + blockIdx.x * PART_EXT;
+        for (int k = 0; k < 3; ++k) {
+            o[k] = mn[k];
+            o[3 + k] = mx[k];
+            o[6 + k] = qs[k];
+        }
+        o[9] = qs[3];
+        o[10] = qs[4];
+    }
+}
+
+__global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, const double* __restrict__ q,
+                                                 KickParams kp, double* __restrict__ X, double* __restrict__ part,
+                                                 ScState* st) {
+    __shared__ double sm[5 * 32];
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double qs[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const int64_t n = kp.n;
+    const bool ok = st->status == SC_OK;
+    double T[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) T[i][j] = st->T[i][j];
+    const double g0 = st->gamma0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ok && i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a0 = xp[i], a1 = xp[n + i], a2 = xp[2 * n + i];
+        double v[3];
+        for (int j = 0; j < 3; ++j) v[j] = dot3_blas(a0, a1, a2, T[0][j], T[1][j], T[2][j]);
+        v[2] = __dmul_rn(v[2], g0);
+        const double qi = q[i];
+        for (int j = 0; j < 3; ++j) {
+            X[j * n + i] = v[j];
+            mn[j] = fmin(mn[j], v[j]);
+            mx[j] = fmax(mx[j], v[j]);
+            qs[j] += qi * v[j];
+        }
+        qs[3] += qi;
+        qs[4] += fabs(qi);
+    }
+    extent_block_out(mn, mx, qs, sm, part);
+    if (arrive_last(&st->done_extent)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
+}
+
+// order-preserving map of a double onto uint64 (for integer atomics on doubles)
+__device__ __forceinline__ unsigned long long ord64(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord64(unsigned long long u) {
+    return __longlong_as_double((long long)((u >> 63) ? (u & 0x7fffffffffffffffull) : ~u));
+}
+
+// Rotated position (z scaled by gamma0) of particle i to ~1e-11 of a cell:
+// each lab coordinate is its FP64 MAD value plus a small correction computed
+// in FP32 (x - (px/E) tau, and z = -tau + tau (1 - pz/E) with
+// 1 - pz/E = (m^2 + pT^2) / ((E + pz) E), free of cancellation), rotated in
+// FP64.  No FP64 division or square root.
+__device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t ld, int64_t i, const KickParams& kp,
+                                         const double (&T)[3][3], double g0, double v[3]) {
+    const double x = rp[i], y = rp[2 * ld + i], tau = rp[4 * ld + i];
+    float px, py, pz, E;
+    mom32(d2f(rp[ld + i]), d2f(rp[3 * ld + i]), d2f(rp[5 * ld + i]), kp, px, py, pz, E);
+    const float tf = d2f(tau), iE = 1.0f / E;
+    const double l0 = x - f2d(px * iE * tf);
+    const double l1 = y - f2d(py * iE * tf);
+    const float k = (kp.m2_f + px * px + py * py) / (E + pz) * iE;
+    const double l2 = -tau + f2d(tf * k);
+    for (int j = 0; j < 3; ++j) v[j] = fma(l2, T[2][j], fma(l1, T[1][j], l0 * T[0][j]));
+    v[2] *= g0;
+}
+
+// FP32 extent.  Pass 1 computes the rotated positions in FP32, stores them and
+// reduces FP32 extremes and charge moments.  Pass 2 re-walks the block's
+// particles and evaluates to ~1e-11 of a cell (xyz_fine) every particle whose
+// FP32 coordinate lies within a rounding margin of the block's FP32 extreme:
+// the FP64 extreme of the block is among them, so the mesh step equals the
+// FP64 form's.
+__global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ rp, const double* __restrict__ q,
+                                                    KickParams kp, float* __restrict__ X, double* __restrict__ part,
+                                                    ScState* st) {
+    __shared__ double sm[5 * 32];
+    __shared__ float smf[3 * 32];
+    __shared__ float bmin[3], bmax[3];
+    __shared__ unsigned long long emin[3], emax[3];
+    float mnf[3] = {INFINITY, INFINITY, INFINITY}, mxf[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float qsf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int64_t n = kp.n, ld = kp.ld;
+    const bool ok = st->status == SC_OK;
+    float T[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) T[i][j] = st->Tf[i][j];
+    const float g0 = st->g0f;
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = i0; ok && i < n; i += stride) {
+        const float xq = d2f(rp[ld + i]), yq = d2f(rp[3 * ld + i]), d = d2f(rp[5 * ld + i]);
+        const float tau = d2f(rp[4 * ld + i]);
+        float px, py, pz, E;
+        mom32(xq, yq, d, kp, px, py, pz, E);
+        const float s = tau / E;
+        const float l0 = d2f(rp[i]) - px * s, l1 = d2f(rp[2 * ld + i]) - py * s, l2 = -pz * s;
+        float v[3];
+        for (int j = 0; j < 3; ++j) v[j] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
+        v[2] *= g0;
+        const float qi = d2f(q[i]);
+        if (!SC_IDX_OK(st, 13, 2 * n + i, 3 * n)) continue;
+        for (int j = 0; j < 3; ++j) {
+            X[j * n + i] = v[j];
+            mnf[j] = fminf(mnf[j], v[j]);
+            mxf[j] = fmaxf(mxf[j], v[j]);
+            qsf[j] += qi * v[j];
+        }
+        qsf[3] += qi;
+        qsf[4] += fabsf(qi);
+    }
+    // float extremes reduce exactly in float; the sums in double
+    block_minmax_f<3, false>(mnf, smf);
+    block_minmax_f<3, true>(mxf, smf);
+    double qs[5] = {qsf[0], qsf[1], qsf[2], qsf[3], qsf[4]};
+    block_sum<5>(qs, sm);
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 3; ++j) {
+            bmin[j] = mnf[j];
+            bmax[j] = mxf[j];
+            emin[j] = ord64(INFINITY);
+            emax[j] = ord64(-INFINITY);
+        }
+    __syncthreads();
+    float tol[3];
+    for (int j = 0; j < 3; ++j)  // 2^-18 of the coordinate scale: 64x the FP32 rounding bound of v
+        tol[j] = ldexpf(fmaxf(fabsf(bmin[j]), fabsf(bmax[j])) + (bmax[j] - bmin[j]), -18);
+    if (ok) {
+        double Td[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) Td[a][b] = st->T[a][b];
+        const double g0d = st->gamma0;
+        for (int64_t i = i0; i < n; i += stride) {
+            bool cand = false;
+            for (int j = 0; j < 3; ++j) {
+                const float v = X[j * n + i];
+                cand |= (v <= bmin[j] + tol[j]) || (v >= bmax[j] - tol[j]);
+            }
+            if (cand) {
+                double v[3];
+                xyz_fine(rp, ld, i, kp, Td, g0d, v);
+                for (int j = 0; j < 3; ++j) {
+                    if (X[j * n + i] <= bmin[j] + tol[j]) atomicMin(&emin[j], ord64(v[j]));
+                    if (X[j * n + i] >= bmax[j] - tol[j]) atomicMax(&emax[j], ord64(v[j]));
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && SC_IDX_OK(st, 12, blockIdx.x, kp.n > 0 ? gridDim.x : 0)) {
+        double* o = part + blockIdx.x * PART_EXT;
+        for (int k = 0; k < 3; ++k) {
+            o[k] = unord64(emin[k]);
+            o[3 + k] = unord64(emax[k]);
+            o[6 + k] = qs[k];
+        }
+        o[9] = qs[3];
+        o[10] = qs[4];
+    }
+    if (arrive_last(&st->done_extent)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
+}
+
+// el_field entry: X given as [n][3] rotated positions; z scaled by gamma in place
+template <typename R>
+__global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, const double* __restrict__ q, KickParams kp,
+                                                   double gamma, R* __restrict__ X, double* __restrict__ part,
+                                                   ScState* st) {
+    __shared__ double sm[5 * 32];
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double qs[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const int64_t n = kp.n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v[3] = {Xin[3 * i], Xin[3 * i + 1], __dmul_rn(Xin[3 * i + 2], gamma)};
+        Xin[3 * i + 2] = v[2];
+        const double qi = q[i];
+        for (int j = 0; j < 3; ++j) {
+            X[j * n + i] = (R)v[j];
+            mn[j] = fmin(mn[j], v[j]);
+            mx[j] = fmax(mx[j], v[j]);
+            qs[j] += qi * v[j];
+        }
+        qs[3] += qi;
+        qs[4] += fabs(qi);
+    }
+    extent_block_out(mn, mx, qs, sm, part);
+    if (arrive_last(&st->done_extent)) mesh_finalize(part, gridDim.x, kp, st, gamma);
 }
 
 // potential entry: explicit spacing
@@ -410,30 +588,106 @@ __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickPar
 // ---------------------------------------------------------------------------
 // keys: X = xyz/steps - X_off, key = (Xi*ny + Yi)*nz + Zi with Xi = floor(X)+1
 // ---------------------------------------------------------------------------
-template <typename R>
-__global__ void __launch_bounds__(PT) k_keys(R* __restrict__ X, uint32_t* __restrict__ keys, KickParams kp,
-                                             ScState* st) {
+__device__ __forceinline__ bool key_of(double fx, double fy, double fz, const KickParams& kp, uint32_t& key) {
+    const bool in = fx >= 0 && fy >= 0 && fz >= 0 && fx < kp.nx && fy < kp.ny && fz < kp.nz;
+    key = in ? ((uint32_t)fx * (uint32_t)kp.ny + (uint32_t)fy) * (uint32_t)kp.nz + (uint32_t)fz : 0u;
+    return in;
+}
+
+__global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t* __restrict__ keys, KickParams kp,
+                                               ScState* st) {
     if (st->status) return;
     const int64_t n = kp.n;
     const double s0 = st->steps[0], s1 = st->steps[1], s2 = st->steps[2];
     const double o0 = st->xoff[0], o1 = st->xoff[1], o2 = st->xoff[2];
     bool bad = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        R g[3];
-        if (sizeof(R) == 8) {
-            g[0] = (R)__dsub_rn(__ddiv_rn((double)X[i], s0), o0);
-            g[1] = (R)__dsub_rn(__ddiv_rn((double)X[n + i], s1), o1);
-            g[2] = (R)__dsub_rn(__ddiv_rn((double)X[2 * n + i], s2), o2);
-        } else {
-            g[0] = (R)((float)X[i] / (float)s0 - (float)o0);
-            g[1] = (R)((float)X[n + i] / (float)s1 - (float)o1);
-            g[2] = (R)((float)X[2 * n + i] / (float)s2 - (float)o2);
+        const double g0 = __dsub_rn(__ddiv_rn(X[i], s0), o0);
+        const double g1 = __dsub_rn(__ddiv_rn(X[n + i], s1), o1);
+        const double g2 = __dsub_rn(__ddiv_rn(X[2 * n + i], s2), o2);
+        uint32_t key;
+        bad |= !key_of(floor(g0) + 1, floor(g1) + 1, floor(g2) + 1, kp, key);
+        keys[i] = key;
+        X[i] = g0;
+        X[n + i] = g1;
+        X[2 * n + i] = g2;
+    }
+    if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
+}
+
+__device__ __forceinline__ bool key_of_f(float fx, float fy, float fz, const KickParams& kp, uint32_t& key) {
+    const bool in = fx >= 0.f && fy >= 0.f && fz >= 0.f && fx < (float)kp.nx && fy < (float)kp.ny && fz < (float)kp.nz;
+    key = in ? ((uint32_t)fx * (uint32_t)kp.ny + (uint32_t)fy) * (uint32_t)kp.nz + (uint32_t)fz : 0u;
+    return in;
+}
+
+// q * 2^S rounded to an integer, on the integer pipes (|q| 2^S < 2^62)
+__device__ __forceinline__ long long to_fixed(double q, int S) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e == 0) return 0;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    const int sh = e - 1075 + S;
+    unsigned long long v;
+    if (sh >= 0) v = sh > 10 ? 0x3fffffffffffffffull : (m << sh);
+    else if (sh < -63) v = 0;
+    else v = (m + (1ull << (-sh - 1))) >> (-sh);
+    return (b >> 63) ? -(long long)v : (long long)v;
+}
+
+// FP32 grid coordinates with an explicit rounding margin; a particle whose
+// coordinate lies within the margin of a cell face is recomputed to ~1e-11 of
+// a cell (xyz_fine), so its key equals the FP64 form's key unless it lies
+// within ~1e-11 of the face.
+// rp == nullptr (el_field entry) keeps the FP32 result.
+// qfix != nullptr: the deposit -- each charge, in units of 2^-S, is added to
+// its cell with a 64-bit integer atomic.  Integer addition is exact and
+// associative, so the charge grid does not depend on the order of the
+// atomics: deterministic, the same alone and in a batch.
+__global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
+                                                  const double* __restrict__ rp, const double* __restrict__ q,
+                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
+    if (st->status) return;
+    const int64_t n = kp.n, ld = kp.ld;
+    float sf[3], of[3], is[3];
+    for (int j = 0; j < 3; ++j) {
+        sf[j] = st->stepsf[j];
+        of[j] = st->xofff[j];
+        is[j] = st->istepsf[j];
+    }
+    const float ig0 = st->ig0f;
+    const int S = st->qfix_shift;
+    bool bad = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v0 = X[i], v1 = X[n + i], v2 = X[2 * n + i];
+        const float nrm = sqrtf(v0 * v0 + v1 * v1 + (v2 * ig0) * (v2 * ig0));  // |lab position|
+        float g[3] = {v0 / sf[0] - of[0], v1 / sf[1] - of[1], v2 / sf[2] - of[2]};
+        bool amb = false;
+        for (int j = 0; j < 3; ++j) {
+            const float scale = (j == 2 ? nrm / ig0 : nrm) * is[j] + fabsf(of[j]) + 1.0f;
+            const float tol = ldexpf(scale, -19);  // >= 4x the FP32 rounding bound of g
+            const float f = g[j] - floorf(g[j]);
+            amb |= !(f >= tol && f <= 1.0f - tol);
         }
-        const R fx = floor(g[0]) + 1, fy = floor(g[1]) + 1, fz = floor(g[2]) + 1;
-        const bool in = fx >= 0 && fy >= 0 && fz >= 0 && fx < kp.nx && fy < kp.ny && fz < kp.nz;
-        uint32_t key = 0;
-        if (in) key = ((uint32_t)fx * (uint32_t)kp.ny + (uint32_t)fy) * (uint32_t)kp.nz + (uint32_t)fz;
-        else bad = true;
+        uint32_t key;
+        if (amb && rp) {
+            double T[3][3];
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
+            double v[3];
+            xyz_fine(rp, ld, i, kp, T, st->gamma0, v);
+            double e[3];
+            for (int j = 0; j < 3; ++j) {
+                e[j] = fma(v[j], st->isteps[j], -st->xoff[j]);
+                g[j] = (float)e[j];
+            }
+            bad |= !key_of(floor(e[0]) + 1, floor(e[1]) + 1, floor(e[2]) + 1, kp, key);
+        } else {
+            bad |= !key_of_f(floorf(g[0]) + 1.f, floorf(g[1]) + 1.f, floorf(g[2]) + 1.f, kp, key);
+        }
+        if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
+            atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
+        if (!SC_IDX_OK(st, 14, 2 * n + i, 3 * n)) continue;
         keys[i] = key;
         X[i] = g[0];
         X[n + i] = g[1];
@@ -512,17 +766,16 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
     }
 }
 
-__global__ void __launch_bounds__(PT) k_kick32(double* __restrict__ rp, const float* __restrict__ X,
-                                               const float* __restrict__ ex, const float* __restrict__ ey,
-                                               const float* __restrict__ ez, KickParams kp, const ScState* st) {
+__global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const float* __restrict__ X,
+                                                  const float* __restrict__ ex, const float* __restrict__ ey,
+                                                  const float* __restrict__ ez, KickParams kp, const ScState* st) {
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld;
-    const F32Consts c = f32c(kp);
     float T[3][3];
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) T[i][j] = (float)st->T[i][j];
-    const float g0 = (float)st->gamma0, kxy = (float)st->kxy, kz = (float)st->kz;
-    const float ipref = 1.0f / c.pref;
+        for (int j = 0; j < 3; ++j) T[i][j] = st->Tf[i][j];
+    const float g0 = st->g0f, kxy = st->kxyf, kz = st->kzf;
+    const float ipref = kp.ipref_f, m2 = kp.m2_f;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float e0, e1, e2;
         gather3<float>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[n + i], X[2 * n + i], e0, e1, e2);
@@ -530,23 +783,31 @@ __global__ void __launch_bounds__(PT) k_kick32(double* __restrict__ rp, const fl
         const float dpx = T[0][0] * d0 + T[0][1] * d1 + T[0][2] * d2;
         const float dpy = T[1][0] * d0 + T[1][1] * d1 + T[1][2] * d2;
         const float dpz = T[2][0] * d0 + T[2][1] * d1 + T[2][2] * d2;
-        const double r1 = rp[ld + i], r3 = rp[3 * ld + i], r4 = rp[4 * ld + i], r5 = rp[5 * ld + i];
+        const double r0 = rp[i], r1 = rp[ld + i], r2 = rp[2 * ld + i];
+        const double r3 = rp[3 * ld + i], r4 = rp[4 * ld + i], r5 = rp[5 * ld + i];
         float px, py, pz, E;
-        mom32((float)r1, (float)r3, (float)r5, c, px, py, pz, E);
+        mom32(d2f(r1), d2f(r3), d2f(r5), kp, px, py, pz, E);
         const float pxn = px + dpx, pyn = py + dpy, pzn = pz + dpz;
-        const float En = sqrtf(pxn * pxn + pyn * pyn + pzn * pzn + c.m2);
+        const float En = sqrtf(pxn * pxn + pyn * pyn + pzn * pzn + m2);
         const float dE = (2.0f * (px * dpx + py * dpy + pz * dpz) + (dpx * dpx + dpy * dpy + dpz * dpz)) / (E + En);
-        const float tau = (float)r4;
-        const float dtau = tau * (pz * dE - E * dpz) / (E * pzn);
+        const float tau = d2f(r4);
+        // pz E' - pz' E without cancellation (it is suppressed by 1/gamma^2):
+        //   = [pz^2 dT - dpz (pz + pz') (m^2 + pT^2)] / (pz E' + pz' E),
+        //   dT = |pT'|^2 - |pT|^2
+        const float pT2 = px * px + py * py;
+        const float dT = 2.0f * (px * dpx + py * dpy) + dpx * dpx + dpy * dpy;
+        const float fz = (pz * pz * dT - dpz * (pz + pzn) * (m2 + pT2)) / (pz * En + pzn * E);
+        const float dtau = tau * fz / (E * pzn);
         const float iEE = 1.0f / (E * En);
         const float dx = tau * (dpx * E - px * dE) * iEE + (pxn / En) * dtau;
         const float dy = tau * (dpy * E - py * dE) * iEE + (pyn / En) * dtau;
-        rp[i] = rp[i] + (double)dx;
-        rp[ld + i] = r1 + (double)(dpx * ipref);
-        rp[2 * ld + i] = rp[2 * ld + i] + (double)dy;
-        rp[3 * ld + i] = r3 + (double)(dpy * ipref);
-        rp[4 * ld + i] = r4 + (double)dtau;
-        rp[5 * ld + i] = r5 + (double)(dE * ipref);
+        // the only FP64 arithmetic: six additions into the float64 coordinates
+        rp[i] = r0 + f2d(dx);
+        rp[ld + i] = r1 + f2d(dpx * ipref);
+        rp[2 * ld + i] = r2 + f2d(dy);
+        rp[3 * ld + i] = r3 + f2d(dpy * ipref);
+        rp[4 * ld + i] = r4 + f2d(dtau);
+        rp[5 * ld + i] = r5 + f2d(dE * ipref);
     }
 }
 
@@ -581,10 +842,9 @@ cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickPar
     double* part = reinterpret_cast<double*>(ws + L.part_frame);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_frame64<<<nb, PT, 0, s>>>(rp, kp, reinterpret_cast<double*>(ws + L.xp), part);
+        k_frame64<<<nb, PT, 0, s>>>(rp, kp, reinterpret_cast<double*>(ws + L.xp), part, st);
     else
-        k_frame32<<<nb, PT, 0, s>>>(rp, kp, part);
-    k_frame_finalize<<<1, PT, 0, s>>>(part, nb, kp, st);
+        k_frame32<<<nb, PT, 0, s>>>(rp, kp, part, st);
     return cudaGetLastError();
 }
 
@@ -598,7 +858,6 @@ cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickPa
                                      reinterpret_cast<double*>(ws + L.X), part, st);
     else
         k_extent32<<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
-    k_mesh_finalize<<<1, PT, 0, s>>>(part, nb, kp, st, -1.0);
     return cudaGetLastError();
 }
 
@@ -608,10 +867,9 @@ cudaError_t launch_extent_xyz(const Plan& p, const Layout& L, char* ws, const Ki
     double* part = reinterpret_cast<double*>(ws + L.part_ext);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_extent_xyz<double><<<nb, PT, 0, s>>>(X, q, kp.n, gamma, reinterpret_cast<double*>(ws + L.X), part);
+        k_extent_xyz<double><<<nb, PT, 0, s>>>(X, q, kp, gamma, reinterpret_cast<double*>(ws + L.X), part, st);
     else
-        k_extent_xyz<float><<<nb, PT, 0, s>>>(X, q, kp.n, gamma, reinterpret_cast<float*>(ws + L.X), part);
-    k_mesh_finalize<<<1, PT, 0, s>>>(part, nb, kp, st, gamma);
+        k_extent_xyz<float><<<nb, PT, 0, s>>>(X, q, kp, gamma, reinterpret_cast<float*>(ws + L.X), part, st);
     return cudaGetLastError();
 }
 
@@ -622,14 +880,23 @@ cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const Kick
     return cudaGetLastError();
 }
 
-cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, cudaStream_t s) {
+cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, const double* rp,
+                        const double* q, cudaStream_t s) {
     ScState* st = reinterpret_cast<ScState*>(ws + L.state);
     const int nb = particle_blocks(p, kp.n);
     uint32_t* keys = reinterpret_cast<uint32_t*>(ws + L.keys);
     if (p.prec == SC_FP64)
-        k_keys<double><<<nb, PT, 0, s>>>(reinterpret_cast<double*>(ws + L.X), keys, kp, st);
+        k_keys64<<<nb, PT, 0, s>>>(reinterpret_cast<double*>(ws + L.X), keys, kp, st);
     else
-        k_keys<float><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, kp, st);
+    {
+        unsigned long long* qfix = nullptr;
+        if (q && !p.sorted_deposit) {
+            qfix = reinterpret_cast<unsigned long long*>(ws + L.qfix);
+            cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
+            if (e) return e;
+        }
+        k_keys32<<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+    }
     return cudaGetLastError();
 }
 

@@ -32,6 +32,23 @@ from .physics_proc import PhysProc
 _PREC = {"fp64": N.SC_FP64, "fp32": N.SC_FP32}
 
 
+def plan_mode(precision: str, deposit: str = "fixed", igf: str = "hybrid") -> int:
+    """Mode bits of a plan (include/ocelot_sc.h): the FP32 form's options."""
+    if precision not in _PREC:
+        raise ValueError(f"precision must be one of {sorted(_PREC)}, not {precision!r}")
+    if deposit not in ("fixed", "sorted"):
+        raise ValueError(f"deposit must be 'fixed' or 'sorted', not {deposit!r}")
+    if igf not in ("hybrid", "exact"):
+        raise ValueError(f"igf must be 'hybrid' or 'exact', not {igf!r}")
+    mode = _PREC[precision]
+    if precision == "fp32":
+        if deposit == "sorted":
+            mode |= N.SC_FP32_SORTED_DEPOSIT
+        if igf == "exact":
+            mode |= N.SC_FP32_EXACT_IGF
+    return mode
+
+
 def _torch():
     import torch
     return torch
@@ -49,7 +66,7 @@ def _stream(device) -> C.c_void_p:
 class Engine:
     """A plan (mesh shape, precision) and its device workspace on one GPU."""
 
-    def __init__(self, shape, precision: str, device=None):
+    def __init__(self, shape, precision: str, device=None, mode=None):
         torch = _torch()
         if not torch.cuda.is_available():
             raise N.NativeLibraryError("ocelot_gb300 needs a CUDA device; there is no CPU fallback")
@@ -57,9 +74,10 @@ class Engine:
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.shape = tuple(int(v) for v in shape)
         self.precision = precision
+        self.mode = plan_mode(precision) if mode is None else int(mode)
         plan = C.c_void_p()
         with torch.cuda.device(self.device):
-            N.check(self.lib.sc_plan_create(C.byref(plan), *self.shape, _PREC[precision]))
+            N.check(self.lib.sc_plan_create(C.byref(plan), *self.shape, self.mode))
         self.plan = plan
         self.ws = None
         self.cap = -1
@@ -149,7 +167,11 @@ class SpaceCharge(PhysProc):
     Attributes as in the reference: ``step`` (in Navigator unit steps),
     ``nmesh_xyz`` (default [63, 63, 63]), ``low_order_kick`` (stored, unused,
     as in the reference), ``random_mesh``, ``random_seed`` (10), ``debug``,
-    ``start_elem``/``end_elem``.  Additions: ``precision`` ("fp64" | "fp32")
+    ``start_elem``/``end_elem``.  Additions: ``precision`` ("fp64" | "fp32"),
+    for the FP32 form ``deposit`` ("fixed": exact 64-bit fixed-point
+    accumulation, default; "sorted": radix sort + Kahan segment sums) and
+    ``igf`` ("hybrid": FP64 8-corner IGF near the origin, multipole form
+    beyond 5 cell widths, default; "exact": FP64 8-corner IGF everywhere),
     and ``device``.
     """
 
@@ -164,8 +186,9 @@ class SpaceCharge(PhysProc):
         self.random_mesh = kwargs.get("random_mesh", False)
         self.random_seed = 10
         self.precision = kwargs.get("precision", "fp64")
-        if self.precision not in _PREC:
-            raise ValueError(f"precision must be one of {sorted(_PREC)}, not {self.precision!r}")
+        self.deposit = kwargs.get("deposit", "fixed")
+        self.igf = kwargs.get("igf", "hybrid")
+        plan_mode(self.precision, self.deposit, self.igf)  # validates
         self.device = kwargs.get("device", None)
         self._engines = {}
 
@@ -178,10 +201,11 @@ class SpaceCharge(PhysProc):
 
     def engine(self, shape=None) -> Engine:
         shape = tuple(int(v) for v in (self.nmesh_xyz if shape is None else shape))
-        key = (shape, self.precision, str(self.device))
+        mode = plan_mode(self.precision, self.deposit, self.igf)
+        key = (shape, mode, str(self.device))
         eng = self._engines.get(key)
         if eng is None:
-            eng = Engine(shape, self.precision, self.device)
+            eng = Engine(shape, self.precision, self.device, mode)
             self._engines[key] = eng
         return eng
 
