@@ -114,6 +114,24 @@ int sc_potential(sc_plan* plan, void* ws, size_t ws_bytes, const double* qgrid,
 int sc_sym_kernel(sc_plan* plan, void* ws, size_t ws_bytes, double hx, double hy, double hz,
                   double* kern, void* stream);
 
+/* The table of sc_sym_kernel computed without any workspace or device
+ * allocation.  No counterpart in the reference: it serves callers that cannot
+ * allocate device memory where they need the table -- processes whose device
+ * memory is reserved up front by another allocator or a fixed budget, and
+ * latency-critical loops that must not call cudaMalloc/cudaFree (which can
+ * synchronise the device).  The scratch is one static device array of
+ * SC_SYM_KERNEL_STATIC_MAX_CORNERS doubles (4 MiB), held by every GPU that
+ * loads the library until the process exits; meshes need
+ * (nx+1)(ny+1)(nz+1) <= SC_SYM_KERNEL_STATIC_MAX_CORNERS (64^3 fits), larger
+ * ones are rejected with SC_ERR_UNSUPPORTED.  The first call on a device
+ * looks up the array's device address, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams or
+ * host threads) race -- keep them on one stream.
+ *   kern: device float64 [nx][ny][nz]. */
+#define SC_SYM_KERNEL_STATIC_MAX_CORNERS 524288
+int sc_sym_kernel_static(int nx, int ny, int nz, double hx, double hy, double hz, double* kern,
+                         void* stream);
+
 /* Stable LSD radix sort of 32-bit cell keys with their particle indices: the
  * summation order of the deposit, equal to numpy.argsort(keys, kind='stable')
  * -- it replaces the sequential np.bincount of sc.py:193.

@@ -46,6 +46,7 @@ SIGNATURES = {
     "sc_el_field": (C.c_int, [vp, vp, C.c_size_t, vp, vp, i64, dbl, dbl, dbl, vp, vp]),
     "sc_potential": (C.c_int, [vp, vp, C.c_size_t, vp, dbl, dbl, dbl, vp, vp]),
     "sc_sym_kernel": (C.c_int, [vp, vp, C.c_size_t, dbl, dbl, dbl, vp, vp]),
+    "sc_sym_kernel_static": (C.c_int, [C.c_int, C.c_int, C.c_int, dbl, dbl, dbl, vp, vp]),
     "sc_sort_workspace_bytes": (i64, [i64, C.c_int]),
     "sc_sort_keys": (C.c_int, [vp, i64, C.c_int, vp, vp, vp, C.c_size_t, vp]),
     "sc_tmap_apply": (C.c_int, [C.POINTER(dbl), C.POINTER(dbl), vp, i64, i64, vp]),

@@ -176,6 +176,18 @@ static int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+namespace ocsc {
+int sc_report(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+}  // namespace ocsc
+
 static int cuda_fail(cudaError_t e, const char* where) {
     return fail(SC_ERR_CUDA, "%s: %s (%s)", where, cudaGetErrorString(e), cudaGetErrorName(e));
 }

@@ -187,6 +187,9 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
 
 inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
 
+// records the calling thread's error message (sc_last_error) and returns code
+int sc_report(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+
 // Index checks of checked builds (-DSC_CHECKED): a failed check records the
 // kernel code and the index in the state and the access is skipped.
 #ifdef SC_CHECKED

@@ -20,6 +20,8 @@
 // All kernels here return immediately unless ScState::igf_rebuild is set
 // (the mesh spacing changed since the table in the workspace was built) or
 // the caller forces a build.
+#include <mutex>
+
 #include "sc_common.cuh"
 #include "sc_fft_dev.cuh"
 
@@ -336,4 +338,88 @@ cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cuda
     return p.prec == SC_FP64 ? spectrum_t<double>(p, L, ws, s) : spectrum_t<float>(p, L, ws, s);
 }
 
+// ---------------------------------------------------------------------------
+// Workspace-free IGF table (sc_sym_kernel_static)
+//
+// Some callers cannot allocate device memory at the point where they need the
+// table: a process whose device memory is reserved up front by another
+// allocator (a framework's memory pool, an online control application with a
+// fixed memory budget), or code on a latency-critical path that must not call
+// cudaMalloc/cudaFree, which can synchronise the device.  For them the corner
+// table lives in one file-scope device array, allocated by the driver when
+// the library's module is loaded and kept by every GPU that loads the
+// library until the process exits.  The first kScratchState bytes of it hold
+// a zeroed stand-in for the workspace state that the kernels are handed.
+// ---------------------------------------------------------------------------
+constexpr long long kStaticMaxCorners = SC_SYM_KERNEL_STATIC_MAX_CORNERS;
+constexpr long long kScratchState = 64;  // doubles (512 bytes >= sizeof(ScState))
+static __device__ __align__(256) double g_igf_scratch[kScratchState + kStaticMaxCorners];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_ptr[kMaxDevices] = {};  // device address of g_igf_scratch, per device
+int g_scratch_sms[kMaxDevices] = {};
+}  // namespace
+
+// Once per device, with that device current: the device address of the
+// scratch array (host code may not use the symbol itself as a pointer) and
+// the SM count for the launch shape.
+static cudaError_t static_scratch(int dev, double** ptr, int* sms) {
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_igf_scratch);
+        if (e != cudaSuccess) return e;
+        int sm = 0;
+        e = cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        g_scratch_sms[dev] = sm;
+        g_scratch_ptr[dev] = static_cast<double*>(p);
+    }
+    *ptr = g_scratch_ptr[dev];
+    *sms = g_scratch_sms[dev];
+    return cudaSuccess;
+}
+
 }  // namespace ocsc
+
+extern "C" int sc_sym_kernel_static(int nx, int ny, int nz, double hx, double hy, double hz, double* kern,
+                                    void* stream) {
+    using namespace ocsc;
+    if (nx < 1 || ny < 1 || nz < 1) return sc_report(SC_ERR_ARG, "sc_sym_kernel_static: mesh dimensions must be >= 1");
+    const long long corners = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+    if (corners > kStaticMaxCorners)
+        return sc_report(SC_ERR_UNSUPPORTED,
+                         "sc_sym_kernel_static: (nx+1)(ny+1)(nz+1) = %lld corners exceeds the static table of %lld "
+                         "(use sc_sym_kernel with a workspace for this mesh)",
+                         corners, kStaticMaxCorners);
+    if (!kern) return sc_report(SC_ERR_ARG, "sc_sym_kernel_static: kern is NULL");
+    if (!(hx > 0 && hy > 0 && hz > 0) || !isfinite(hx * hy * hz))
+        return sc_report(SC_ERR_ARG, "sc_sym_kernel_static: mesh steps must be > 0");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return sc_report(SC_ERR_CUDA, "sc_sym_kernel_static: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return sc_report(SC_ERR_UNSUPPORTED, "sc_sym_kernel_static: device %d", dev);
+    double* base = nullptr;
+    int sms = 0;
+    e = static_scratch(dev, &base, &sms);
+    if (e != cudaSuccess)
+        return sc_report(SC_ERR_CUDA, "sc_sym_kernel_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    cudaStream_t s = (cudaStream_t)stream;
+    ScState* st = reinterpret_cast<ScState*>(base);
+    double* ig = base + kScratchState;
+    // the state stand-in starts at zero (only its check fields are ever written)
+    e = cudaMemsetAsync(st, 0, sizeof(ScState), s);
+    if (e != cudaSuccess) return sc_report(SC_ERR_CUDA, "sc_sym_kernel_static: %s", cudaGetErrorString(e));
+    IgfArgs a;
+    a.hx = hx; a.hy = hy; a.hz = hz;
+    a.use_state = 0;
+    a.force = 1;
+    a.hybrid = 0;
+    k_igf_corners<<<grid_for((size_t)corners, sms), 256, 0, s>>>(ig, nx, ny, nz, a, st);
+    k_igf_diff<double><<<grid_for((size_t)nx * ny * nz, sms), 256, 0, s>>>(ig, kern, nx, ny, nz, a, st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return sc_report(SC_ERR_CUDA, "sc_sym_kernel_static: %s", cudaGetErrorString(e));
+    return SC_OK;
+}
