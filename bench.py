@@ -154,6 +154,29 @@ def time_form(precision, n, steps, warmup, dev, flush):
     return kick_ms, {k: sum(v) / len(v) for k, v in stages.items()}, launches
 
 
+def fp32_kick_error(n, dev):
+    """Relative RMS error of the FP32 form's kicks (Δx', Δy', Δδ) against the FP64
+    form on the same beam, one kick, computed on the device."""
+    import torch
+    from ocelot_gb300 import SpaceCharge
+    rp, q = beam(n, seed=SEED + 1)
+    r0 = torch.from_numpy(rp).to(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        d = r0.clone()
+        sc = SpaceCharge(nmesh_xyz=MESH, precision=prec, device=dev)
+        sc.apply_device(d, d_q, E_GEV, DZ)
+        sc.check()
+        out[prec] = d
+    err = {}
+    for r, name in ((1, "dxp"), (3, "dyp"), (5, "ddelta")):
+        k64 = out["fp64"][r] - r0[r]
+        k32 = out["fp32"][r] - r0[r]
+        err[name] = float(torch.sqrt(torch.mean((k32 - k64) ** 2)) / torch.sqrt(torch.mean(k64 ** 2)))
+    return err
+
+
 def time_e2e(precision, n, steps, warmup, dev):
     """Through SpaceCharge.apply with host (pinned) buffers; copies inside the timed region."""
     import numpy as np
@@ -271,6 +294,7 @@ def main():
         barrier()
     kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
     e2e_dt, h2d, d2h = time_e2e("fp32", n, args.steps, args.warmup, dev)
+    kick_err = fp32_kick_error(n, dev)
     barrier()
 
     t32 = sum(kick32) / 1e3
@@ -309,6 +333,7 @@ def main():
             "fp64_form": ({"value": n * args.steps / (sum(kick64) / 1e3), "ms_per_step": statistics.mean(kick64),
                            "stages_ms": stages64} if kick64 else None),
             "fp32_over_fp64": (statistics.mean(kick64) / statistics.mean(kick32)) if kick64 else None,
+            "fp32_kick_rel_rms_err_vs_fp64": kick_err,
             "stages_ms": stages32,
             "roofline": {"bound": "hbm", "kernel": "k_kick32 (gather+kick+FP64 accumulate)",
                          "achieved": achieved_kick, "peak": peak, "unit": "GB/s", "frac": achieved_kick / peak,

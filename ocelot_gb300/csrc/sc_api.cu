@@ -79,6 +79,9 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.ex = take(rs * ncell);
     L.ey = take(rs * ncell);
     L.ez = take(rs * ncell);
+    L.exq = take(p.prec == SC_FP32 ? 16 * ncell : 0);
+    L.eyq = take(p.prec == SC_FP32 ? 16 * ncell : 0);
+    L.ezq = take(p.prec == SC_FP32 ? 16 * ncell : 0);
     L.cell_start = take(4 * ncell);
     L.cell_end = take(4 * ncell);
     L.qfix = take(8 * ncell);
@@ -89,7 +92,7 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.green = take(rs * Kx * Ky * Kz);
     L.W = take(cs * (size_t)p.nx * p.My * Kz);
     L.xp = take(p.prec == SC_FP64 ? 8 * 6 * (size_t)n : 0);
-    L.X = take(rs * 3 * (size_t)n);
+    L.X = take(rs * 3 * (size_t)((n + 3) / 4 * 4));
     L.keys = take(4 * (size_t)n);
     L.sort_keys = take(4 * (size_t)n);
     L.sort_perm = take(4 * (size_t)n);
@@ -216,6 +219,7 @@ static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energ
     memset(&kp, 0, sizeof kp);
     kp.n = n;
     kp.ld = ld;
+    kp.nX = (n + 3) / 4 * 4;
     kp.nx = p.nx; kp.ny = p.ny; kp.nz = p.nz;
     kp.Mx = p.Mx; kp.My = p.My; kp.Mz = p.Mz;
     // sc.py:214-216 and coord_transform.py:19-20,61

@@ -76,6 +76,7 @@ constexpr int WS_MAGIC = 0x5c6b0e11;
 // host-computed scalars of one kick
 struct KickParams {
     int64_t n, ld;
+    int64_t nX;                          // row stride of the 3-row grid-coordinate array (n rounded up to 4)
     int nx, ny, nz;
     int Mx, My, Mz;
     double gamref, betaref, pref, grbr;  // grbr = gamref*betaref
@@ -109,6 +110,7 @@ struct Layout {
     size_t X;                                    // 3 x n grid coordinates (R)
     size_t keys, sort_keys, sort_perm, sort_q, sort_tmp_k, sort_tmp_v, sort_hist, sort_tot;
     size_t qgrid, phi, ex, ey, ez;               // [nx][ny][nz] (R)
+    size_t exq, eyq, ezq;                        // FP32 form: [nx][ny][nz] float4 gather quads
     size_t cell_start, cell_end;                 // [nx*ny*nz] uint32 run bounds (adjacent)
     size_t qfix;                                 // [nx*ny*nz] int64 fixed-point charge (FP32 form)
     size_t igf_ig;                               // (nx+1)(ny+1)(nz+1) double

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const l
         R re = 0, im = 0;
         if (z < nz) {
             const size_t ia = ((size_t)x * ny + ya) * nz + z, ib = ia + nz;
-            const long long ncell = (long long)gridDim.y * ny * nz;
+            [[maybe_unused]] const long long ncell = (long long)gridDim.y * ny * nz;
             if ((ya < ny && !SC_IDX_OK(st, 21, ia, ncell)) || (yb < ny && !SC_IDX_OK(st, 22, ib, ncell))) continue;
             if (qfix) {
                 const float u = st->qfix_inv;
@@ -204,32 +204,57 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ 
     }
 }
 
-// Ex,Ey,Ez = forward differences / h, zero on the last plane (sc.py:195-200)
+// Ex,Ey,Ez = forward differences / h, zero on the last plane (sc.py:195-200).
+// One block per (x, y) line of cells, one thread per z: no index division.
 template <typename R>
 __global__ void k_field_grids(const R* __restrict__ phi, R* __restrict__ ex, R* __restrict__ ey,
                               R* __restrict__ ez, int nx, int ny, int nz, const ScState* st) {
     if (st->status) return;
-    const size_t ncell = (size_t)nx * ny * nz;
+    const int j = blockIdx.x, i = blockIdx.y;
     const double hx = st->steps[0], hy = st->steps[1], hz = st->steps[2];
-    const R ihx = (R)(1.0 / hx), ihy = (R)(1.0 / hy), ihz = (R)(1.0 / hz);
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
-        const int k = (int)(c % nz);
-        const int j = (int)((c / nz) % ny);
-        const int i = (int)(c / ((size_t)nz * ny));
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        const int c = (i * ny + j) * nz + k;
         const R p = phi[c];
         R vx = 0, vy = 0, vz = 0;
-        if (sizeof(R) == 8) {
-            if (i < nx - 1) vx = (R)(((double)p - (double)phi[c + (size_t)ny * nz]) / hx);
-            if (j < ny - 1) vy = (R)(((double)p - (double)phi[c + nz]) / hy);
-            if (k < nz - 1) vz = (R)(((double)p - (double)phi[c + 1]) / hz);
-        } else {
-            if (i < nx - 1) vx = (p - phi[c + (size_t)ny * nz]) * ihx;
-            if (j < ny - 1) vy = (p - phi[c + nz]) * ihy;
-            if (k < nz - 1) vz = (p - phi[c + 1]) * ihz;
-        }
+        if (i < nx - 1) vx = (R)(((double)p - (double)phi[c + ny * nz]) / hx);
+        if (j < ny - 1) vy = (R)(((double)p - (double)phi[c + nz]) / hy);
+        if (k < nz - 1) vz = (R)(((double)p - (double)phi[c + 1]) / hz);
         ex[c] = vx;
         ey[c] = vy;
         ez[c] = vz;
+    }
+}
+
+// FP32 form: the field grids as "quads" for the gather -- for each cell
+// (i,j,k) and each component F, float4 (F[i][j][k], F[i][j][k+1],
+// F[i][j+1][k], F[i][j+1][k+1]); a trilinear sample then reads two float4
+// (x planes i and i+1) instead of eight scalars.  Entries that the gather
+// never uses (j = ny-1 or k = nz-1 as a base) are written but not read.
+__device__ __forceinline__ float fd(const float* __restrict__ phi, int i, int j, int k, int di, int dj, int dk,
+                                    int nx, int ny, int nz, float ih) {
+    // forward difference along (di,dj,dk), zero on the last plane and outside the grid
+    if (i >= nx || j >= ny || k >= nz) return 0.f;
+    if (i + di >= nx || j + dj >= ny || k + dk >= nz) return 0.f;
+    const int c = (i * ny + j) * nz + k;
+    return (phi[c] - phi[c + (di * ny + dj) * nz + dk]) * ih;
+}
+
+__global__ void k_field_quads(const float* __restrict__ phi, float4* __restrict__ qx, float4* __restrict__ qy,
+                              float4* __restrict__ qz, int nx, int ny, int nz, const ScState* st) {
+    if (st->status) return;
+    const int j = blockIdx.x, i = blockIdx.y;
+    const float ihx = st->istepsf[0], ihy = st->istepsf[1], ihz = st->istepsf[2];
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        const int c = (i * ny + j) * nz + k;
+        qx[c] = make_float4(fd(phi, i, j, k, 1, 0, 0, nx, ny, nz, ihx), fd(phi, i, j, k + 1, 1, 0, 0, nx, ny, nz, ihx),
+                            fd(phi, i, j + 1, k, 1, 0, 0, nx, ny, nz, ihx),
+                            fd(phi, i, j + 1, k + 1, 1, 0, 0, nx, ny, nz, ihx));
+        qy[c] = make_float4(fd(phi, i, j, k, 0, 1, 0, nx, ny, nz, ihy), fd(phi, i, j, k + 1, 0, 1, 0, nx, ny, nz, ihy),
+                            fd(phi, i, j + 1, k, 0, 1, 0, nx, ny, nz, ihy),
+                            fd(phi, i, j + 1, k + 1, 0, 1, 0, nx, ny, nz, ihy));
+        qz[c] = make_float4(fd(phi, i, j, k, 0, 0, 1, nx, ny, nz, ihz), fd(phi, i, j, k + 1, 0, 0, 1, nx, ny, nz, ihz),
+                            fd(phi, i, j + 1, k, 0, 0, 1, nx, ny, nz, ihz),
+                            fd(phi, i, j + 1, k + 1, 0, 0, 1, nx, ny, nz, ihz));
     }
 }
 
@@ -283,12 +308,16 @@ cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void
 template <typename R>
 static cudaError_t field_t(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
-    const size_t ncell = (size_t)p.nx * p.ny * p.nz;
-    int blocks = (int)((ncell + 255) / 256);
-    if (blocks > p.sm_count * 8) blocks = p.sm_count * 8;
-    k_field_grids<R><<<blocks, 256, 0, s>>>(reinterpret_cast<const R*>(ws + L.phi), reinterpret_cast<R*>(ws + L.ex),
-                                            reinterpret_cast<R*>(ws + L.ey), reinterpret_cast<R*>(ws + L.ez),
-                                            p.nx, p.ny, p.nz, st);
+    const int bt = p.nz < 256 ? ((p.nz + 31) / 32) * 32 : 256;
+    const dim3 grid(p.ny, p.nx);
+    if (sizeof(R) == 4)
+        k_field_quads<<<grid, bt, 0, s>>>(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float4*>(ws + L.exq),
+                                          reinterpret_cast<float4*>(ws + L.eyq), reinterpret_cast<float4*>(ws + L.ezq),
+                                          p.nx, p.ny, p.nz, st);
+    else
+        k_field_grids<R><<<grid, bt, 0, s>>>(reinterpret_cast<const R*>(ws + L.phi), reinterpret_cast<R*>(ws + L.ex),
+                                             reinterpret_cast<R*>(ws + L.ey), reinterpret_cast<R*>(ws + L.ez),
+                                             p.nx, p.ny, p.nz, st);
     return cudaGetLastError();
 }
 

@@ -352,18 +352,67 @@ __global__ void __launch_bounds__(PT) k_frame64(const double* __restrict__ rp, K
     if (arrive_last(&st->done_frame)) frame_finalize(part, gridDim.x, kp, st);
 }
 
+// Pair-wise particle loop of the FP32 kernels: with VEC each thread takes two
+// adjacent particles and moves every row with one 16-byte access (rows
+// 16-byte aligned, even row stride); an odd last particle is taken alone.
+#define PAIR_LOOP_BEGIN(n)                                                                        \
+    const int64_t npair_ = VEC ? (n) / 2 : (n);                                                   \
+    const int64_t ntot_ = npair_ + ((VEC && ((n) & 1)) ? 1 : 0);                                  \
+    for (int64_t p_ = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p_ < ntot_;                 \
+         p_ += (int64_t)gridDim.x * blockDim.x) {                                                 \
+        const bool pair_ = VEC && p_ < npair_;                                                    \
+        const int64_t i0_ = pair_ ? 2 * p_ : (VEC ? (n) - 1 : p_);                                \
+        const int W_ = pair_ ? 2 : 1;
+#define PAIR_LOOP_END }
+
+__device__ __forceinline__ void ld_row(const double* __restrict__ row, int64_t i, bool pair, double& a, double& b) {
+    if (pair) {
+        const double2 v = __ldg(reinterpret_cast<const double2*>(row + i));
+        a = v.x;
+        b = v.y;
+    } else {
+        a = row[i];
+        b = 0.0;
+    }
+}
+__device__ __forceinline__ void st_row(double* __restrict__ row, int64_t i, bool pair, double a, double b) {
+    if (pair) *reinterpret_cast<double2*>(row + i) = make_double2(a, b);
+    else row[i] = a;
+}
+__device__ __forceinline__ void ld_rowf(const float* __restrict__ row, int64_t i, bool pair, float& a, float& b) {
+    if (pair) {
+        const float2 v = *reinterpret_cast<const float2*>(row + i);
+        a = v.x;
+        b = v.y;
+    } else {
+        a = row[i];
+        b = 0.f;
+    }
+}
+__device__ __forceinline__ void st_rowf(float* __restrict__ row, int64_t i, bool pair, float a, float b) {
+    if (pair) *reinterpret_cast<float2*>(row + i) = make_float2(a, b);
+    else row[i] = a;
+}
+
+template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
                                                    double* __restrict__ part, ScState* st) {
     __shared__ double sm[3 * 32];
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
     const int64_t n = kp.n, ld = kp.ld;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    PAIR_LOOP_BEGIN(n)
+    double xq[2], yq[2], d[2];
+    ld_row(rp + ld, i0_, pair_, xq[0], xq[1]);
+    ld_row(rp + 3 * ld, i0_, pair_, yq[0], yq[1]);
+    ld_row(rp + 5 * ld, i0_, pair_, d[0], d[1]);
+    for (int w = 0; w < W_; ++w) {
         float px, py, pz, E;
-        mom32(d2f(rp[ld + i]), d2f(rp[3 * ld + i]), d2f(rp[5 * ld + i]), kp, px, py, pz, E);
+        mom32(d2f(xq[w]), d2f(yq[w]), d2f(d[w]), kp, px, py, pz, E);
         a0 += px;
         a1 += py;
         a2 += pz;
     }
+    PAIR_LOOP_END
     double acc[3] = {a0, a1, a2};
     block_sum<3>(acc, sm);
     if (threadIdx.x == 0)
@@ -410,7 +459,7 @@ __global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, 
         v[2] = __dmul_rn(v[2], g0);
         const double qi = q[i];
         for (int j = 0; j < 3; ++j) {
-            X[j * n + i] = v[j];
+            X[j * kp.nX + i] = v[j];
             mn[j] = fmin(mn[j], v[j]);
             mx[j] = fmax(mx[j], v[j]);
             qs[j] += qi * v[j];
@@ -456,6 +505,7 @@ __device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t 
 // FP32 coordinate lies within a rounding margin of the block's FP32 extreme:
 // the FP64 extreme of the block is among them, so the mesh step equals the
 // FP64 form's.
+template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ rp, const double* __restrict__ q,
                                                     KickParams kp, float* __restrict__ X, double* __restrict__ part,
                                                     ScState* st) {
@@ -465,33 +515,46 @@ __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ r
     __shared__ unsigned long long emin[3], emax[3];
     float mnf[3] = {INFINITY, INFINITY, INFINITY}, mxf[3] = {-INFINITY, -INFINITY, -INFINITY};
     float qsf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    const int64_t n = kp.n, ld = kp.ld;
+    const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     const bool ok = st->status == SC_OK;
     float T[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) T[i][j] = st->Tf[i][j];
     const float g0 = st->g0f;
-    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = i0; ok && i < n; i += stride) {
-        const float xq = d2f(rp[ld + i]), yq = d2f(rp[3 * ld + i]), d = d2f(rp[5 * ld + i]);
-        const float tau = d2f(rp[4 * ld + i]);
-        float px, py, pz, E;
-        mom32(xq, yq, d, kp, px, py, pz, E);
-        const float s = tau / E;
-        const float l0 = d2f(rp[i]) - px * s, l1 = d2f(rp[2 * ld + i]) - py * s, l2 = -pz * s;
-        float v[3];
-        for (int j = 0; j < 3; ++j) v[j] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
-        v[2] *= g0;
-        const float qi = d2f(q[i]);
-        if (!SC_IDX_OK(st, 13, 2 * n + i, 3 * n)) continue;
-        for (int j = 0; j < 3; ++j) {
-            X[j * n + i] = v[j];
-            mnf[j] = fminf(mnf[j], v[j]);
-            mxf[j] = fmaxf(mxf[j], v[j]);
-            qsf[j] += qi * v[j];
+    if (ok) {
+        PAIR_LOOP_BEGIN(n)
+        float r[6][2], qq[2];
+        for (int k = 0; k < 6; ++k) {
+            double a, b;
+            ld_row(rp + k * ld, i0_, pair_, a, b);
+            r[k][0] = d2f(a);
+            r[k][1] = d2f(b);
         }
-        qsf[3] += qi;
-        qsf[4] += fabsf(qi);
+        {
+            double a, b;
+            ld_row(q, i0_, pair_, a, b);
+            qq[0] = d2f(a);
+            qq[1] = d2f(b);
+        }
+        float v[3][2];
+        for (int w = 0; w < W_; ++w) {
+            float px, py, pz, E;
+            mom32(r[1][w], r[3][w], r[5][w], kp, px, py, pz, E);
+            const float s = r[4][w] / E;
+            const float l0 = r[0][w] - px * s, l1 = r[2][w] - py * s, l2 = -pz * s;
+            for (int j = 0; j < 3; ++j) v[j][w] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
+            v[2][w] *= g0;
+            const float qi = qq[w];
+            for (int j = 0; j < 3; ++j) {
+                mnf[j] = fminf(mnf[j], v[j][w]);
+                mxf[j] = fmaxf(mxf[j], v[j][w]);
+                qsf[j] += qi * v[j][w];
+            }
+            qsf[3] += qi;
+            qsf[4] += fabsf(qi);
+        }
+        for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, v[j][0], v[j][1]);
+        PAIR_LOOP_END
     }
     // float extremes reduce exactly in float; the sums in double
     block_minmax_f<3, false>(mnf, smf);
@@ -514,21 +577,26 @@ __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ r
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) Td[a][b] = st->T[a][b];
         const double g0d = st->gamma0;
-        for (int64_t i = i0; i < n; i += stride) {
+        // the same particles as pass 1 (same pair mapping), so the block's FP32
+        // extremes bound them
+        PAIR_LOOP_BEGIN(n)
+        for (int w = 0; w < W_; ++w) {
+            const int64_t i = i0_ + w;
             bool cand = false;
             for (int j = 0; j < 3; ++j) {
-                const float v = X[j * n + i];
+                const float v = X[j * nX + i];
                 cand |= (v <= bmin[j] + tol[j]) || (v >= bmax[j] - tol[j]);
             }
             if (cand) {
                 double v[3];
                 xyz_fine(rp, ld, i, kp, Td, g0d, v);
                 for (int j = 0; j < 3; ++j) {
-                    if (X[j * n + i] <= bmin[j] + tol[j]) atomicMin(&emin[j], ord64(v[j]));
-                    if (X[j * n + i] >= bmax[j] - tol[j]) atomicMax(&emax[j], ord64(v[j]));
+                    if (X[j * nX + i] <= bmin[j] + tol[j]) atomicMin(&emin[j], ord64(v[j]));
+                    if (X[j * nX + i] >= bmax[j] - tol[j]) atomicMax(&emax[j], ord64(v[j]));
                 }
             }
         }
+        PAIR_LOOP_END
     }
     __syncthreads();
     if (threadIdx.x == 0 && SC_IDX_OK(st, 12, blockIdx.x, kp.n > 0 ? gridDim.x : 0)) {
@@ -558,7 +626,7 @@ __global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, con
         Xin[3 * i + 2] = v[2];
         const double qi = q[i];
         for (int j = 0; j < 3; ++j) {
-            X[j * n + i] = (R)v[j];
+            X[j * kp.nX + i] = (R)v[j];
             mn[j] = fmin(mn[j], v[j]);
             mx[j] = fmax(mx[j], v[j]);
             qs[j] += qi * v[j];
@@ -602,15 +670,16 @@ __global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t*
     const double o0 = st->xoff[0], o1 = st->xoff[1], o2 = st->xoff[2];
     bool bad = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t nX = kp.nX;
         const double g0 = __dsub_rn(__ddiv_rn(X[i], s0), o0);
-        const double g1 = __dsub_rn(__ddiv_rn(X[n + i], s1), o1);
-        const double g2 = __dsub_rn(__ddiv_rn(X[2 * n + i], s2), o2);
+        const double g1 = __dsub_rn(__ddiv_rn(X[nX + i], s1), o1);
+        const double g2 = __dsub_rn(__ddiv_rn(X[2 * nX + i], s2), o2);
         uint32_t key;
         bad |= !key_of(floor(g0) + 1, floor(g1) + 1, floor(g2) + 1, kp, key);
         keys[i] = key;
         X[i] = g0;
-        X[n + i] = g1;
-        X[2 * n + i] = g2;
+        X[nX + i] = g1;
+        X[2 * nX + i] = g2;
     }
     if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
 }
@@ -644,11 +713,12 @@ __device__ __forceinline__ long long to_fixed(double q, int S) {
 // its cell with a 64-bit integer atomic.  Integer addition is exact and
 // associative, so the charge grid does not depend on the order of the
 // atomics: deterministic, the same alone and in a batch.
+template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
                                                   const double* __restrict__ rp, const double* __restrict__ q,
                                                   unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
     if (st->status) return;
-    const int64_t n = kp.n, ld = kp.ld;
+    const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     float sf[3], of[3], is[3];
     for (int j = 0; j < 3; ++j) {
         sf[j] = st->stepsf[j];
@@ -658,8 +728,16 @@ __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_
     const float ig0 = st->ig0f;
     const int S = st->qfix_shift;
     bool bad = false;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float v0 = X[i], v1 = X[n + i], v2 = X[2 * n + i];
+    PAIR_LOOP_BEGIN(n)
+    float v[3][2];
+    for (int j = 0; j < 3; ++j) ld_rowf(X + j * nX, i0_, pair_, v[j][0], v[j][1]);
+    double qq[2] = {0.0, 0.0};
+    if (qfix) ld_row(q, i0_, pair_, qq[0], qq[1]);
+    uint32_t key2[2] = {0u, 0u};
+    float g2[3][2];
+    for (int w = 0; w < W_; ++w) {
+        const int64_t i = i0_ + w;
+        const float v0 = v[0][w], v1 = v[1][w], v2 = v[2][w];
         const float nrm = sqrtf(v0 * v0 + v1 * v1 + (v2 * ig0) * (v2 * ig0));  // |lab position|
         float g[3] = {v0 / sf[0] - of[0], v1 / sf[1] - of[1], v2 / sf[2] - of[2]};
         bool amb = false;
@@ -674,11 +752,11 @@ __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_
             double T[3][3];
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
-            double v[3];
-            xyz_fine(rp, ld, i, kp, T, st->gamma0, v);
+            double xv[3];
+            xyz_fine(rp, ld, i, kp, T, st->gamma0, xv);
             double e[3];
             for (int j = 0; j < 3; ++j) {
-                e[j] = fma(v[j], st->isteps[j], -st->xoff[j]);
+                e[j] = fma(xv[j], st->isteps[j], -st->xoff[j]);
                 g[j] = (float)e[j];
             }
             bad |= !key_of(floor(e[0]) + 1, floor(e[1]) + 1, floor(e[2]) + 1, kp, key);
@@ -686,13 +764,14 @@ __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_
             bad |= !key_of_f(floorf(g[0]) + 1.f, floorf(g[1]) + 1.f, floorf(g[2]) + 1.f, kp, key);
         }
         if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
-            atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
-        if (!SC_IDX_OK(st, 14, 2 * n + i, 3 * n)) continue;
-        keys[i] = key;
-        X[i] = g[0];
-        X[n + i] = g[1];
-        X[2 * n + i] = g[2];
+            atomicAdd(qfix + key, (unsigned long long)to_fixed(qq[w], S));
+        key2[w] = key;
+        for (int j = 0; j < 3; ++j) g2[j][w] = g[j];
     }
+    if (pair_) *reinterpret_cast<uint2*>(keys + i0_) = make_uint2(key2[0], key2[1]);
+    else keys[i0_] = key2[0];
+    for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
+    PAIR_LOOP_END
     if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
 }
 
@@ -735,6 +814,31 @@ __device__ __forceinline__ void gather3(const R* ex, const R* ey, const R* ez, i
     e2 = trilerp<R>(ez, nx, ny, nz, X0 + h, X1 + h, X2);
 }
 
+// trilinear sample from the FP32 gather quads (two float4 loads)
+__device__ __forceinline__ float trilerp_q(const float4* __restrict__ Q, int nx, int ny, int nz, float c0, float c1,
+                                           float c2) {
+    if (!(c0 >= 0.f) || !(c1 >= 0.f) || !(c2 >= 0.f) || c0 > (float)(nx - 1) || c1 > (float)(ny - 1) ||
+        c2 > (float)(nz - 1))
+        return 0.f;
+    int i = (int)c0, j = (int)c1, k = (int)c2;
+    if (i > nx - 2) i = nx - 2;
+    if (j > ny - 2) j = ny - 2;
+    if (k > nz - 2) k = nz - 2;
+    const float tx = c0 - (float)i, ty = c1 - (float)j, tz = c2 - (float)k;
+    const int c = (i * ny + j) * nz + k;
+    const float4 a = __ldg(Q + c), b = __ldg(Q + c + ny * nz);
+    const float ya = (1.f - ty) * ((1.f - tz) * a.x + tz * a.y) + ty * ((1.f - tz) * a.z + tz * a.w);
+    const float yb = (1.f - ty) * ((1.f - tz) * b.x + tz * b.y) + ty * ((1.f - tz) * b.z + tz * b.w);
+    return (1.f - tx) * ya + tx * yb;
+}
+
+__device__ __forceinline__ void gather3q(const float4* qx, const float4* qy, const float4* qz, int nx, int ny, int nz,
+                                         float X0, float X1, float X2, float& e0, float& e1, float& e2) {
+    e0 = trilerp_q(qx, nx, ny, nz, X0, X1 + 0.5f, X2 + 0.5f);
+    e1 = trilerp_q(qy, nx, ny, nz, X0 + 0.5f, X1, X2 + 0.5f);
+    e2 = trilerp_q(qz, nx, ny, nz, X0 + 0.5f, X1 + 0.5f, X2);
+}
+
 __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const double* __restrict__ xp,
                                                const double* __restrict__ X, const double* __restrict__ ex,
                                                const double* __restrict__ ey, const double* __restrict__ ez,
@@ -747,7 +851,7 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
     const double g0 = st->gamma0, kxy = st->kxy, kz = st->kz;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double e0, e1, e2;
-        gather3<double>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[n + i], X[2 * n + i], e0, e1, e2);
+        gather3<double>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[kp.nX + i], X[2 * kp.nX + i], e0, e1, e2);
         e0 = __dmul_rn(e0, g0);
         e1 = __dmul_rn(e1, g0);
         const double p0 = xp[3 * n + i], p1 = xp[4 * n + i], p2 = xp[5 * n + i];
@@ -766,31 +870,36 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
     }
 }
 
+template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const float* __restrict__ X,
-                                                  const float* __restrict__ ex, const float* __restrict__ ey,
-                                                  const float* __restrict__ ez, KickParams kp, const ScState* st) {
+                                                  const float4* __restrict__ qx, const float4* __restrict__ qy,
+                                                  const float4* __restrict__ qz, KickParams kp, const ScState* st) {
     if (st->status) return;
-    const int64_t n = kp.n, ld = kp.ld;
+    const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     float T[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) T[i][j] = st->Tf[i][j];
     const float g0 = st->g0f, kxy = st->kxyf, kz = st->kzf;
     const float ipref = kp.ipref_f, m2 = kp.m2_f;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    PAIR_LOOP_BEGIN(n)
+    double r[6][2];
+    for (int k = 0; k < 6; ++k) ld_row(rp + k * ld, i0_, pair_, r[k][0], r[k][1]);
+    float xg[3][2];
+    for (int j = 0; j < 3; ++j) ld_rowf(X + j * nX, i0_, pair_, xg[j][0], xg[j][1]);
+    float o[6][2];
+    for (int w = 0; w < W_; ++w) {
         float e0, e1, e2;
-        gather3<float>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[n + i], X[2 * n + i], e0, e1, e2);
+        gather3q(qx, qy, qz, kp.nx, kp.ny, kp.nz, xg[0][w], xg[1][w], xg[2][w], e0, e1, e2);
         const float d0 = kxy * e0 * g0, d1 = kxy * e1 * g0, d2 = kz * e2;  // kick in the beam frame
         const float dpx = T[0][0] * d0 + T[0][1] * d1 + T[0][2] * d2;
         const float dpy = T[1][0] * d0 + T[1][1] * d1 + T[1][2] * d2;
         const float dpz = T[2][0] * d0 + T[2][1] * d1 + T[2][2] * d2;
-        const double r0 = rp[i], r1 = rp[ld + i], r2 = rp[2 * ld + i];
-        const double r3 = rp[3 * ld + i], r4 = rp[4 * ld + i], r5 = rp[5 * ld + i];
         float px, py, pz, E;
-        mom32(d2f(r1), d2f(r3), d2f(r5), kp, px, py, pz, E);
+        mom32(d2f(r[1][w]), d2f(r[3][w]), d2f(r[5][w]), kp, px, py, pz, E);
         const float pxn = px + dpx, pyn = py + dpy, pzn = pz + dpz;
         const float En = sqrtf(pxn * pxn + pyn * pyn + pzn * pzn + m2);
         const float dE = (2.0f * (px * dpx + py * dpy + pz * dpz) + (dpx * dpx + dpy * dpy + dpz * dpz)) / (E + En);
-        const float tau = d2f(r4);
+        const float tau = d2f(r[4][w]);
         // pz E' - pz' E without cancellation (it is suppressed by 1/gamma^2):
         //   = [pz^2 dT - dpz (pz + pz') (m^2 + pT^2)] / (pz E' + pz' E),
         //   dT = |pT'|^2 - |pT|^2
@@ -801,14 +910,16 @@ __global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const
         const float iEE = 1.0f / (E * En);
         const float dx = tau * (dpx * E - px * dE) * iEE + (pxn / En) * dtau;
         const float dy = tau * (dpy * E - py * dE) * iEE + (pyn / En) * dtau;
-        // the only FP64 arithmetic: six additions into the float64 coordinates
-        rp[i] = r0 + f2d(dx);
-        rp[ld + i] = r1 + f2d(dpx * ipref);
-        rp[2 * ld + i] = r2 + f2d(dy);
-        rp[3 * ld + i] = r3 + f2d(dpy * ipref);
-        rp[4 * ld + i] = r4 + f2d(dtau);
-        rp[5 * ld + i] = r5 + f2d(dE * ipref);
+        o[0][w] = dx;
+        o[1][w] = dpx * ipref;
+        o[2][w] = dy;
+        o[3][w] = dpy * ipref;
+        o[4][w] = dtau;
+        o[5][w] = dE * ipref;
     }
+    // the only FP64 arithmetic: six additions into the float64 coordinates
+    for (int k = 0; k < 6; ++k) st_row(rp + k * ld, i0_, pair_, r[k][0] + f2d(o[k][0]), r[k][1] + f2d(o[k][1]));
+    PAIR_LOOP_END
 }
 
 template <typename R>
@@ -816,11 +927,17 @@ __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, cons
                                                    const R* __restrict__ ey, const R* __restrict__ ez,
                                                    double* __restrict__ out, KickParams kp, const ScState* st) {
     if (st->status) return;
-    const int64_t n = kp.n;
+    const int64_t n = kp.n, nX = kp.nX;
     const double g0 = st->gamma0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         R e0, e1, e2;
-        gather3<R>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[n + i], X[2 * n + i], e0, e1, e2);
+        if (sizeof(R) == 4)
+            gather3q(reinterpret_cast<const float4*>(ex), reinterpret_cast<const float4*>(ey),
+                     reinterpret_cast<const float4*>(ez), kp.nx, kp.ny, kp.nz, (float)X[i], (float)X[nX + i],
+                     (float)X[2 * nX + i], *reinterpret_cast<float*>(&e0), *reinterpret_cast<float*>(&e1),
+                     *reinterpret_cast<float*>(&e2));
+        else
+            gather3<R>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[nX + i], X[2 * nX + i], e0, e1, e2);
         out[3 * i] = __dmul_rn((double)e0, g0);
         out[3 * i + 1] = __dmul_rn((double)e1, g0);
         out[3 * i + 2] = (double)e2;
@@ -830,6 +947,11 @@ __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, cons
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+// 16-byte row accesses need 16-byte aligned rows and an even row stride
+static bool vec_ok(const double* rp, int64_t ld, const double* q) {
+    return ((uintptr_t)rp % 16 == 0) && (ld % 2 == 0) && (q == nullptr || (uintptr_t)q % 16 == 0);
+}
+
 static int particle_blocks(const Plan& p, int64_t n) {
     int64_t b = (n + PT - 1) / PT;
     if (b > p.part_blocks) b = p.part_blocks;
@@ -844,7 +966,8 @@ cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickPar
     if (p.prec == SC_FP64)
         k_frame64<<<nb, PT, 0, s>>>(rp, kp, reinterpret_cast<double*>(ws + L.xp), part, st);
     else
-        k_frame32<<<nb, PT, 0, s>>>(rp, kp, part, st);
+        vec_ok(rp, kp.ld, nullptr) ? k_frame32<true><<<nb, PT, 0, s>>>(rp, kp, part, st)
+                                   : k_frame32<false><<<nb, PT, 0, s>>>(rp, kp, part, st);
     return cudaGetLastError();
 }
 
@@ -857,7 +980,8 @@ cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickPa
         k_extent64<<<nb, PT, 0, s>>>(reinterpret_cast<const double*>(ws + L.xp), q, kp,
                                      reinterpret_cast<double*>(ws + L.X), part, st);
     else
-        k_extent32<<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
+        vec_ok(rp, kp.ld, q) ? k_extent32<true><<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st)
+                             : k_extent32<false><<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
     return cudaGetLastError();
 }
 
@@ -895,7 +1019,10 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
             cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
             if (e) return e;
         }
-        k_keys32<<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+        if (vec_ok(rp ? rp : reinterpret_cast<const double*>(ws), rp ? kp.ld : 0, q))
+            k_keys32<true><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+        else
+            k_keys32<false><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
     }
     return cudaGetLastError();
 }
@@ -910,9 +1037,14 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
                                    reinterpret_cast<const double*>(ws + L.ey), reinterpret_cast<const double*>(ws + L.ez),
                                    kp, st);
     else
-        k_kick32<<<nb, PT, 0, s>>>(rp, reinterpret_cast<const float*>(ws + L.X), reinterpret_cast<const float*>(ws + L.ex),
-                                   reinterpret_cast<const float*>(ws + L.ey), reinterpret_cast<const float*>(ws + L.ez),
-                                   kp, st);
+    {
+        const float* X = reinterpret_cast<const float*>(ws + L.X);
+        const float4* qx = reinterpret_cast<const float4*>(ws + L.exq);
+        const float4* qy = reinterpret_cast<const float4*>(ws + L.eyq);
+        const float4* qz = reinterpret_cast<const float4*>(ws + L.ezq);
+        if (vec_ok(rp, kp.ld, nullptr)) k_kick32<true><<<nb, PT, 0, s>>>(rp, X, qx, qy, qz, kp, st);
+        else k_kick32<false><<<nb, PT, 0, s>>>(rp, X, qx, qy, qz, kp, st);
+    }
     return cudaGetLastError();
 }
 
@@ -927,9 +1059,9 @@ cudaError_t launch_gather_xyz(const Plan& p, const Layout& L, char* ws, const Ki
                                                reinterpret_cast<const double*>(ws + L.ez), exyz, kp, st);
     else
         k_gather_xyz<float><<<nb, PT, 0, s>>>(reinterpret_cast<const float*>(ws + L.X),
-                                              reinterpret_cast<const float*>(ws + L.ex),
-                                              reinterpret_cast<const float*>(ws + L.ey),
-                                              reinterpret_cast<const float*>(ws + L.ez), exyz, kp, st);
+                                              reinterpret_cast<const float*>(ws + L.exq),
+                                              reinterpret_cast<const float*>(ws + L.eyq),
+                                              reinterpret_cast<const float*>(ws + L.ezq), exyz, kp, st);
     return cudaGetLastError();
 }
 

@@ -113,7 +113,8 @@ class Engine:
     def staging(self, n: int):
         torch = _torch()
         if self._rp is None or self._rp.shape[1] < n:
-            self._rp = torch.empty((6, n), dtype=torch.float64, device=self.device)
+            # even row stride: the kernels then move rows with 16-byte accesses
+            self._rp = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=self.device)
             self._q = torch.empty(n, dtype=torch.float64, device=self.device)
         return self._rp[:, :n], self._q[:n]
 

@@ -18,7 +18,7 @@ Parity is pinned in two ways (both committed under tests/golden/):
   * the reference's own regression vectors of ``test_track_with_sp``
     (unit_tests/ebeam_test/space_charge/ref_results/test_track_with_sp.json),
     reproduced by running the reference's ``track()`` with this oracle swapped
-    in for its kick (tests/golden/pin_track_golden.py).
+    in for its kick (tests/golden/make_golden.py, recorded in tests/golden/track_pin.json).
 """
 from __future__ import annotations
 
@@ -279,5 +279,23 @@ def gaussian_beam(n: int, seed: int, sigma_x=50e-6, sigma_px=1e-5, sigma_y=50e-6
     rp = np.empty((6, n))
     for row, s in enumerate((sigma_x, sigma_px, sigma_y, sigma_py, sigma_tau, sigma_p)):
         rp[row] = rng.standard_normal(n) * s
+    q = np.full(n, charge / n)
+    return rp, q
+
+
+def flat_top_beam(n: int, seed: int, length=2e-3, edge=100e-6, chirp=-10.0, sigma_xy=200e-6, tilt=1e-3,
+                  sigma_pxy=1e-5, sigma_p=1e-4, charge=500e-12):
+    """Low-energy stress shape: tau uniform over `length` convolved with a
+    Gaussian edge of `edge` (a flat top with Gaussian edges), delta chirped by
+    `chirp`*tau, transverse Gaussian with an x-tau tilt of `tilt`."""
+    rng = np.random.default_rng(seed)
+    rp = np.empty((6, n))
+    tau = rng.uniform(-length / 2, length / 2, n) + rng.standard_normal(n) * edge
+    rp[4] = tau
+    rp[5] = rng.standard_normal(n) * sigma_p + chirp * tau
+    rp[0] = rng.standard_normal(n) * sigma_xy + tilt * tau
+    rp[2] = rng.standard_normal(n) * sigma_xy
+    rp[1] = rng.standard_normal(n) * sigma_pxy
+    rp[3] = rng.standard_normal(n) * sigma_pxy
     q = np.full(n, charge / n)
     return rp, q

@@ -234,6 +234,56 @@ def test_fp32_form_deterministic():
     assert np.array_equal(outs[0], outs[1])
 
 
+def kick_rms_error(rp0, out, ref, rows=(1, 3, 5)):
+    return max(np.sqrt(np.mean(((out[r] - rp0[r]) - (ref[r] - rp0[r])) ** 2))
+               / np.sqrt(np.mean((ref[r] - rp0[r]) ** 2)) for r in rows)
+
+
+def test_flat_top_low_energy_shape_vs_oracle():
+    """6.5 MeV flat-top with chirp and tilt (the stress shape), 200k particles on a
+    32x32x64 mesh of the same aspect: FP64 form 1e-10, FP32 form 1e-5."""
+    rp, q = sc_oracle.flat_top_beam(200_000, 31)
+    ref = rp.copy()
+    sc_oracle.sc_apply(ref, q, 0.0065, 0.05, [32, 32, 64])
+    pa = make_pa(rp, q, 0.0065)
+    SpaceCharge(nmesh_xyz=[32, 32, 64]).apply(pa, 0.05)
+    assert rel_rows(pa.rparticles, ref) < 1e-10
+    pa32 = make_pa(rp, q, 0.0065)
+    SpaceCharge(nmesh_xyz=[32, 32, 64], precision="fp32").apply(pa32, 0.05)
+    assert kick_rms_error(rp, pa32.rparticles, ref) < 1e-5
+
+
+@pytest.mark.parametrize("n,mesh,beam,E,dz,tol", [
+    (2_000_000, [64, 64, 64], "gauss", 0.130, 0.1, 1e-5),        # the benchmark workload: <= 1e-5
+    (10_000_000, [128, 128, 256], "flat", 0.0065, 0.05, 2e-5),   # low-energy stress: error stated, ~1.1e-5
+])
+def test_fp32_form_at_full_size_vs_fp64_form(n, mesh, beam, E, dz, tol):
+    """Full-size property: the FP32 form against the FP64 form (itself checked against
+    the oracle at smaller sizes) on the same beam -- relative RMS error of the momentum
+    kicks within tol, same NGP cells.  The transverse fields are differences of FP32
+    potentials a few hundred times larger than the differences, which sets the ~1e-5."""
+    if beam == "gauss":
+        rp, q = sc_oracle.gaussian_beam(n, 41, charge=1e-9)
+    else:
+        rp, q = sc_oracle.flat_top_beam(n, 42)
+    d64 = DeviceParticleArray.from_host(make_pa(rp, q, E), DEV)
+    d32 = DeviceParticleArray.from_host(make_pa(rp, q, E), DEV)
+    s64 = SpaceCharge(nmesh_xyz=mesh)
+    s32 = SpaceCharge(nmesh_xyz=mesh, precision="fp32")
+    s64.apply(d64, dz)
+    s32.apply(d32, dz)
+    s64.check()
+    s32.check()
+    k64 = s64.engine().region("keys")[:n].cpu().numpy()
+    k32 = s32.engine().region("keys")[:n].cpu().numpy()
+    assert np.count_nonzero(k64 != k32) <= 2
+    out64 = d64.rparticles.cpu().numpy()
+    out32 = d32.rparticles.cpu().numpy()
+    assert kick_rms_error(rp, out32, out64) < tol
+    del d64, d32, s64, s32
+    torch.cuda.empty_cache()
+
+
 # ---------------------------------------------------------------------------
 # properties and edge cases
 # ---------------------------------------------------------------------------
