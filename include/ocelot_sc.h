@@ -51,8 +51,10 @@ typedef struct sc_plan sc_plan; /* opaque, host-side only */
 
 /* Plan for a mesh of nx*ny*nz cells (SpaceCharge.nmesh_xyz, sc.py:94) in the
  * given mode (SC_FP64, or SC_FP32 with options).  Each n must be >= 4 (the reference divides the extent by
- * n-3, sc.py:179).  Host-only object: holds sizes, FFT radix plans and launch
- * shapes, no device memory. */
+ * n-3, sc.py:179).  Holds sizes, FFT radix plans, launch shapes and the stream
+ * and events of the Green's-function branch -- no device memory; everything a
+ * kick needs besides stream operations is set up here, so kicks can be
+ * recorded in a CUDA graph. */
 int sc_plan_create(sc_plan** plan, int nx, int ny, int nz, int mode);
 void sc_plan_destroy(sc_plan* plan);
 /* padded FFT lengths chosen for the linear convolution (each >= 2n-1) */
@@ -148,6 +150,17 @@ int sc_sort_keys(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* key
  *   B: host float64[6]. */
 int sc_tmap_apply(const double* R, const double* B, double* rparticles, int64_t ld, int64_t n,
                   void* stream);
+
+/* The transport steps of a tracking loop kept on the device: the same map as
+ * sc_tmap_apply, taken from a device table of maps -- map i is
+ * table[i*42 .. i*42+35] (R, row-major) and table[i*42+36 .. i*42+41] (B) --
+ * at i = *counter (a device int; out of range: no transport), after which
+ * *counter is incremented, in stream order.  The maps are the element slices
+ * Navigator.get_map builds between two kicks (ocelot/cpbd/navi.py:406-434),
+ * composed, applied as TransferMap.apply does; with the index on the device,
+ * one recorded step (this call, then sc_kick) replays for every step. */
+int sc_tmap_apply_indexed(const double* table, int* counter, int nmaps, double* rparticles,
+                          int64_t ld, int64_t n, void* stream);
 
 /* ---- stage timing (benchmarking) --------------------------------------- */
 

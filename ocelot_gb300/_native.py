@@ -50,6 +50,7 @@ SIGNATURES = {
     "sc_sort_workspace_bytes": (i64, [i64, C.c_int]),
     "sc_sort_keys": (C.c_int, [vp, i64, C.c_int, vp, vp, vp, C.c_size_t, vp]),
     "sc_tmap_apply": (C.c_int, [C.POINTER(dbl), C.POINTER(dbl), vp, i64, i64, vp]),
+    "sc_tmap_apply_indexed": (C.c_int, [vp, vp, C.c_int, vp, i64, i64, vp]),
     "sc_profile_enable": (C.c_int, [vp, C.c_int]),
     "sc_profile_read": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     "sc_profile_stage_name": (C.c_char_p, [C.c_int]),

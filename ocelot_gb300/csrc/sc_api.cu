@@ -6,8 +6,10 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 
 #include "sc_common.cuh"
 
@@ -17,6 +19,22 @@ cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_
                          double hz, cudaStream_t s);
 cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const KickParams& kp, double hx, double hy,
                             double hz, cudaStream_t s);
+
+cudaError_t smem_opt_in(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, size_t> opted;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = opted.find(kernel);
+    if (it != opted.end() && it->second >= bytes) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev))) return e;
+    if (bytes > (size_t)optin) return cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
+    opted[kernel] = (size_t)optin;
+    return cudaSuccess;
+}
 
 PhysConst phys_const() {
     // ocelot/common/globals.py:13-24
@@ -278,6 +296,15 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     SC_CUDA(cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     p.part_blocks = p.sm_count * 4;
+    // everything that is not a stream operation happens here, so that kicks
+    // can be recorded in a CUDA graph
+    SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
+    SC_CUDA(prepare_green_kernels(p), "kernel attributes");
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    SC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
+    SC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+    SC_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
     sc_plan* h = new (std::nothrow) sc_plan;
     if (!h) return fail(SC_ERR_ARG, "out of host memory");
     h->p = p;
@@ -286,8 +313,9 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     h->profiling = false;
     h->last_launches = 0;
     for (int i = 0; i < NEV; ++i) h->ev[i] = nullptr;
-    h->side = nullptr;
-    h->fork = h->join = nullptr;
+    h->side = side;
+    h->fork = fork;
+    h->join = join;
     *out = h;
     return SC_OK;
 }
@@ -411,11 +439,6 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     cudaStream_t s = (cudaStream_t)stream;
     const KickParams kp = make_params(p, n, ld, energy_gev, zstep, mesh_scale, mesh_shift);
     const int passes = sort_passes(p.key_bits);
-    if (!plan->side) {
-        SC_CUDA(cudaStreamCreateWithFlags(&plan->side, cudaStreamNonBlocking), "cudaStreamCreate");
-        SC_CUDA(cudaEventCreateWithFlags(&plan->fork, cudaEventDisableTiming), "cudaEventCreate");
-        SC_CUDA(cudaEventCreateWithFlags(&plan->join, cudaEventDisableTiming), "cudaEventCreate");
-    }
     cudaStream_t side = plan->side;
     mark(plan, 0, s);
     SC_CUDA(launch_frame(p, L, ws, kp, rp, s), "frame");
@@ -565,6 +588,17 @@ int sc_tmap_apply(const double* R, const double* B, double* rp, int64_t ld, int6
     if (!rp) return fail(SC_ERR_ARG, "rparticles is NULL");
     if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
     SC_CUDA(launch_tmap(R, B, rp, ld, n, (cudaStream_t)stream), "tmap");
+    return SC_OK;
+}
+
+int sc_tmap_apply_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld, int64_t n,
+                          void* stream) {
+    if (!table || !counter) return fail(SC_ERR_ARG, "table or counter is NULL");
+    if (nmaps < 1 || n < 0) return fail(SC_ERR_ARG, "nmaps < 1 or n < 0");
+    if (n == 0) return SC_OK;
+    if (!rp) return fail(SC_ERR_ARG, "rparticles is NULL");
+    if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
+    SC_CUDA(launch_tmap_indexed(table, counter, nmaps, rp, ld, n, (cudaStream_t)stream), "tmap");
     return SC_OK;
 }
 

@@ -186,8 +186,24 @@ cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStr
 // first-order map (sc_tmap.cu)
 cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n,
                         cudaStream_t s);
+cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld,
+                                int64_t n, cudaStream_t s);
 
 inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+
+// Opt a kernel in to the device's largest dynamic shared memory, once per
+// kernel (a registry keyed by the kernel's address), so that launches made
+// later -- including those recorded in a CUDA graph capture -- issue no
+// attribute calls.
+cudaError_t smem_opt_in(const void* kernel, size_t bytes);
+template <typename K>
+inline cudaError_t set_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return smem_opt_in(reinterpret_cast<const void*>(kernel), bytes);
+}
+// opts every kernel of a plan in (called when the plan is created)
+cudaError_t prepare_fft_kernels(const Plan& p);
+cudaError_t prepare_green_kernels(const Plan& p);
 
 // records the calling thread's error message (sc_last_error) and returns code
 int sc_report(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));

@@ -258,11 +258,6 @@ __global__ void k_field_quads(const float* __restrict__ phi, float4* __restrict_
     }
 }
 
-template <typename K>
-static cudaError_t set_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
 
 template <typename R>
 static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid, R* phi, const long long* qfix,
@@ -294,6 +289,25 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     if ((e = set_smem(k_zinv<R>, smz))) return e;
     k_zinv<R><<<gz, FFT_THREADS, smz, s>>>(W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
     return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t prepare_fft_t(const Plan& p) {
+    cudaError_t e;
+    const int NC = z_lines_per_block(p.Mz);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    if ((e = set_smem(k_zfwd<R>, smz))) return e;
+    if ((e = set_smem(k_ypass<R, false>, smy))) return e;
+    if ((e = set_smem(k_xconv<R>, smx))) return e;
+    if ((e = set_smem(k_ypass<R, true>, smy))) return e;
+    return set_smem(k_zinv<R>, smz);
+}
+
+cudaError_t prepare_fft_kernels(const Plan& p) {
+    return p.prec == SC_FP64 ? prepare_fft_t<double>(p) : prepare_fft_t<float>(p);
 }
 
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in, void* phi_out,

@@ -246,11 +246,6 @@ __global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, 
     }
 }
 
-template <typename K>
-static cudaError_t set_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
 
 static int grid_for(size_t work, int sm) {
     size_t b = (work + 255) / 256;
@@ -332,6 +327,23 @@ static cudaError_t spectrum_t(const Plan& p, const Layout& L, char* ws, cudaStre
     dim3 gx((Kz + 2 * tkx - 1) / (2 * tkx), Ky);
     k_green_strided<R><<<gx, GT, smx, s>>>(s2, g, p.nx, Ky * Kz, Kx, Kz, Kz, Kz, p.rx, twx, tkx, a, st);
     return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t prepare_green_t(const Plan& p) {
+    cudaError_t e;
+    int NC = 2048 / p.Mz;
+    NC = NC < 1 ? 1 : (NC > 16 ? 16 : NC);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    const int tky = green_cols<R>(p.My), tkx = green_cols<R>(p.Mx);
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    if ((e = set_smem(k_green_z<R>, smz))) return e;
+    return set_smem(k_green_strided<R>, smx > smy ? smx : smy);
+}
+
+cudaError_t prepare_green_kernels(const Plan& p) {
+    return p.prec == SC_FP64 ? prepare_green_t<double>(p) : prepare_green_t<float>(p);
 }
 
 cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {

@@ -29,6 +29,50 @@ __global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, i
     }
 }
 
+// Map i = *counter of a device table of maps (row-major R[36] then B[6] per
+// map): the transport step of a device-resident tracking loop whose launches
+// are recorded once (a CUDA graph) and replayed step after step.  Every block
+// reads the counter before k_advance (the next launch on the stream) moves it.
+__global__ void __launch_bounds__(256) k_tmap_indexed(const double* __restrict__ table, const int* __restrict__ counter,
+                                                      int nmaps, double* __restrict__ rp, int64_t ld, int64_t n) {
+    __shared__ double m[42];
+    const int idx = *counter;
+    if (idx < 0 || idx >= nmaps) return;
+    if (threadIdx.x < 42) m[threadIdx.x] = table[(size_t)idx * 42 + threadIdx.x];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            double acc = __dmul_rn(m[r * 6], x[0]);
+#pragma unroll
+            for (int k = 1; k < 6; ++k) acc = __fma_rn(m[r * 6 + k], x[k], acc);
+            rp[r * ld + i] = __dadd_rn(acc, m[36 + r]);
+        }
+    }
+}
+
+__global__ void k_advance(int* counter, int delta) { *counter += delta; }
+
+cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld, int64_t n,
+                                cudaStream_t s) {
+    if (n <= 0) {
+        k_advance<<<1, 1, 0, s>>>(counter, 1);
+        return cudaGetLastError();
+    }
+    int dev = 0, sm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    int64_t b = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm * 8;
+    if (b > cap) b = cap;
+    k_tmap_indexed<<<(int)b, 256, 0, s>>>(table, counter, nmaps, rp, ld, n);
+    k_advance<<<1, 1, 0, s>>>(counter, 1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     Map6 m;

@@ -269,6 +269,120 @@ def tmap_apply(rparticles: np.ndarray, R: np.ndarray, B: np.ndarray) -> None:
     rparticles[:] = a[:]
 
 
+def uni_matrix(z: float, k1: float, energy: float) -> np.ndarray:
+    """6x6 first-order matrix of a drift (k1 = 0) or quadrupole of length z
+    with no bend and no tilt: ocelot/cpbd/r_matrix.py:41-91 at hx = 0 and
+    sum_tilts = 0, the call made by Element/Magnet.create_first_order_main_params
+    (ocelot/cpbd/elements/element.py:83-96, magnet.py:106-117).  The same
+    operations as the reference, complex square roots included."""
+    hx = 0.0
+    gamma = energy / m_e_GeV
+    kx2 = k1 + hx * hx
+    ky2 = -k1
+    kx = np.sqrt(kx2 + 0.j)
+    ky = np.sqrt(ky2 + 0.j)
+    cx = np.cos(z * kx).real
+    cy = np.cos(z * ky).real
+    sy = (np.sin(ky * z) / ky).real if ky != 0 else z
+    igamma2 = 1. / (gamma * gamma) if gamma != 0 else 0.
+    beta = np.sqrt(1. - igamma2)
+    if kx != 0:
+        sx = (np.sin(kx * z) / kx).real
+        dx = hx / kx2 * (1. - cx)
+        r56 = hx * hx * (z - sx) / kx2 / beta ** 2
+    else:
+        sx = z
+        dx = z * z * hx / 2.
+        r56 = hx * hx * z ** 3 / 6. / beta ** 2
+    r56 -= z / (beta * beta) * igamma2
+    return np.array([[cx, sx, 0., 0., 0., dx / beta],
+                     [-kx2 * sx, cx, 0., 0., 0., sx * hx / beta],
+                     [0., 0., cy, sy, 0., 0.],
+                     [0., 0., -ky2 * sy, cy, 0., 0.],
+                     [hx * sx / beta, dx / beta, 0., 0., 1., r56],
+                     [0., 0., 0., 0., 0., 1.]])
+
+
+def _section_length(total_length: float, start_l: float, delta_l: float) -> float:
+    if start_l < 1e-10 and np.isclose(delta_l, total_length):
+        return total_length
+    if start_l + delta_l > total_length or np.isclose(start_l + delta_l, total_length):
+        return total_length - start_l
+    return delta_l
+
+
+def navigator_schedule(lengths, unit_step: float, step: int = 1):
+    """The kicks of one space-charge process attached from the first to the
+    last element, as Ocelot's Navigator steps them: a list of
+    (slices, zstep, z0) where slices = [(element index, slice length)] are the
+    element sections transported before the kick of length zstep taken at z0
+    (track() passes phys_steps, ocelot/cpbd/track.py:474-476).  The slice
+    length is the one OpticElement.get_section_tms builds its map for
+    (ocelot/cpbd/elements/optic_element.py:376-403): the whole element when a
+    slice from its start spans it, the rest of the element when a slice
+    reaches its end, the requested length otherwise.
+
+    Restates Navigator.get_next_step / get_next / check_overjump / get_map
+    (ocelot/cpbd/navi.py:343-352, 354-371, 219-237, 406-434) for that single
+    process, with the lattice length of MagneticLattice.totalLen
+    (ocelot/cpbd/magnetic_lattice.py:226-227) and the stop position of
+    add_physics_proc (navi.py:76-77).  The floating-point operations are the
+    reference's, so z0 and dz are identical to its values.
+    """
+    lengths = [float(v) for v in lengths]
+    nel = len(lengths)
+    total = sum(lengths)
+    l_stop = np.sum(np.array(lengths[:nel - 1]))
+    z0, n_elem, sum_lengths = 0.0, 0, 0.0
+    out = []
+    while np.abs(z0 - total) > 1e-10:
+        phys = np.array([step]) * unit_step
+        dz = float(phys.min())
+        phys_red = phys - dz
+        if z0 + dz > l_stop:
+            dz = l_stop - z0
+        zstep = float((phys_red + dz)[0])
+        if z0 + dz > total:
+            dz = total - z0
+        slices = []
+        i = n_elem
+        z1 = z0 + dz
+        rem = dz
+        L = sum_lengths + lengths[i]
+        while z1 + 1e-10 > L:
+            dl = L - z0
+            slices.append((i, _section_length(lengths[i], z0 + lengths[i] - L, dl)))
+            z0 = L
+            rem -= dl
+            if i >= nel - 1:
+                break
+            i += 1
+            L += lengths[i]
+        if abs(rem) > 1e-10:
+            slices.append((i, _section_length(lengths[i], z0 + lengths[i] - L, rem)))
+        z0 += rem
+        sum_lengths = L - lengths[i]
+        n_elem = i
+        out.append((slices, zstep, float(z0)))
+    return out
+
+
+def track_first_order(rparticles: np.ndarray, q_array: np.ndarray, E_GeV: float, elements, unit_step: float,
+                      nmesh, step: int = 1) -> list:
+    """Track through drifts and quadrupoles ``elements`` = [(length, k1)] with
+    first-order maps and a space-charge kick every ``step`` unit steps, as
+    Ocelot's track() does (ocelot/cpbd/track.py:470-480: the maps of a step,
+    then the kick).  Returns the (z0, dz) of each kick."""
+    kicks = []
+    for slices, dz, z0 in navigator_schedule([l for l, _ in elements], unit_step, step):
+        for i, dl in slices:
+            if dl != 0.0:
+                tmap_apply(rparticles, uni_matrix(dl, elements[i][1], E_GeV), np.zeros((6, 1)))
+        sc_apply(rparticles, q_array, E_GeV, dz, nmesh)
+        kicks.append((z0, dz))
+    return kicks
+
+
 # --------------------------------------------------------------------------
 # Seeded synthetic beams (shapes of the benchmark configurations)
 # --------------------------------------------------------------------------

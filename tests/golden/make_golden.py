@@ -16,6 +16,11 @@ What it writes (all under tests/golden/):
   reference's regression scenario ``test_track_with_sp``
   (unit_tests/ebeam_test/space_charge/space_charge_test.py:54-67, beam and
   lattice of space_charge_conf.py), captured while the reference tracks.
+* ``ref_uni_matrix.npz`` -- first-order drift/quadrupole matrices of the
+  reference's ``uni_matrix`` (ocelot/cpbd/r_matrix.py:41-91).
+* ``ref_fodo_track.npz`` -- the reference's ``track()`` of a beam with
+  ``SpaceCharge`` through FODO cells with first-order maps, with the kick
+  positions and lengths its Navigator chose.
 * ``track_pin.json`` -- the pin of the oracle against the reference's golden
   vectors: the same scenario tracked by the reference's ``track()`` with the
   kick replaced by ``oracle.sc_oracle.sc_apply``, compared particle by
@@ -260,13 +265,82 @@ def run_track(ref_root: str, keep=(0, 120)):
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
 
 
+def run_matrices(ref_root: str):
+    """First-order matrices of drifts and quadrupoles from the reference's
+    uni_matrix (ocelot/cpbd/r_matrix.py:41-91), for the transport between kicks."""
+    import_reference(ref_root)
+    from ocelot.cpbd.r_matrix import uni_matrix
+    params = [(0.25, 0.0, 0.130), (1.0, 0.0, 0.130), (0.2, 1.2, 0.130), (0.2, -1.2, 0.130), (0.05, 1.2, 0.130),
+              (0.15, -1.2, 0.0065), (0.3, -1.537886, 0.0065), (0.3, 1.435078, 2.0), (0.0, 1.2, 0.13)]
+    R = np.stack([uni_matrix(z, k1, 0.0, 0.0, E) for z, k1, E in params])
+    # a tilted, offset quadrupole section through the element's own first-order
+    # parameters (elements/magnet.py:106-117, tm_params/first_order_params.py:26-28)
+    from ocelot import Quadrupole
+    quad = Quadrupole(l=0.2, k1=-1.2, tilt=0.3)
+    quad.dx, quad.dy = 1e-3, -2e-3
+    fp = quad.element.create_first_order_main_params(0.130, 0.15)
+    path = os.path.join(HERE, "ref_uni_matrix.npz")
+    np.savez_compressed(path, params=np.array(params), R=R, tilted_params=np.array([0.15, -1.2, 0.130, 0.3, 1e-3, -2e-3]),
+                        tilted_R=fp.get_rotated_R(), tilted_B=np.asarray(fp.B).reshape(6))
+    print(f"wrote {path}")
+
+
+def run_fodo(ref_root: str, cells=2, n=4000, mesh=(15, 15, 15)):
+    """The reference tracking a beam with SpaceCharge through FODO cells
+    (quadrupoles of 0.2 m at k1 = +-1.2 m^-2, drifts of 1 m) with first-order
+    maps, a kick every 0.25 m (Navigator unit_step 0.25, process step 1),
+    through its own Navigator/track() (ocelot/cpbd/navi.py, track.py:431).
+    The kick lengths and positions it used are recorded with the result."""
+    import_reference(ref_root)
+    from ocelot import Drift, Marker, Quadrupole, MagneticLattice, TransferMap, Navigator, track
+    from ocelot.cpbd.sc import SpaceCharge
+    from ocelot.cpbd.beam import ParticleArray
+    seq = []
+    for _ in range(cells):
+        seq += [Quadrupole(l=0.2, k1=1.2), Drift(l=1.0), Quadrupole(l=0.2, k1=-1.2), Drift(l=1.0)]
+    seq.append(Marker())
+    lat = MagneticLattice(seq, method={"global": TransferMap})
+    rp, q = sc_oracle.gaussian_beam(n, 606, sigma_x=200e-6, sigma_y=200e-6, sigma_px=2e-5, sigma_py=2e-5,
+                                    charge=500e-12)
+    pa = ParticleArray(n)
+    pa.rparticles[:] = rp
+    pa.q_array = q.copy()
+    pa.E = 0.130
+    sc = SpaceCharge(step=1, nmesh_xyz=list(mesh))
+    kicks = []
+    base_apply = SpaceCharge.apply
+
+    def rec_apply(self, p_array, zstep):
+        kicks.append((self.z0, zstep))
+        base_apply(self, p_array, zstep)
+
+    SpaceCharge.apply = rec_apply
+    navi = Navigator(lat)
+    navi.add_physics_proc(sc, lat.sequence[0], lat.sequence[-1])
+    navi.unit_step = 0.25
+    _, p = track(lat, pa, navi, print_progress=False, calc_tws=False)
+    SpaceCharge.apply = base_apply
+    path = os.path.join(HERE, "ref_fodo_track.npz")
+    np.savez_compressed(path, rp_in=rp, q=q, E=0.130, cells=cells, nmesh=np.array(mesh),
+                        kicks=np.array(kicks), rp_out=p.rparticles.copy())
+    print(f"wrote {path} ({len(kicks)} kicks)")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--skip-track", action="store_true")
     ap.add_argument("--only-track", action="store_true")
+    ap.add_argument("--only-matrices", action="store_true")
     a = ap.parse_args()
+    if a.only_matrices:
+        run_matrices(a.reference)
+        if not os.path.exists(os.path.join(HERE, "ref_fodo_track.npz")):
+            run_fodo(a.reference)
+        sys.exit(0)
     if not a.only_track:
         run_cases(a.reference)
+        run_matrices(a.reference)
+        run_fodo(a.reference)
     if not a.skip_track:
         run_track(a.reference)

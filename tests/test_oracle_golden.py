@@ -16,7 +16,8 @@ from oracle import sc_oracle
 from conftest import GOLDEN
 
 CASES = sorted(glob.glob(os.path.join(GOLDEN, "ref_*.npz")))
-CASES = [c for c in CASES if not c.endswith("ref_track_kicks.npz")]
+CASES = [c for c in CASES if os.path.basename(c) not in ("ref_track_kicks.npz", "ref_uni_matrix.npz",
+                                                          "ref_fodo_track.npz")]
 
 
 def _load(path):
