@@ -218,6 +218,96 @@ def cpu_port(n, kicks_max, budget_s, threads):
     return n * len(times) / sum(times), len(times)
 
 
+# batched workload: 96 seeded Gaussian beams, N log-uniform in [1e4, 4e6], mesh
+# drawn from these five, E uniform 5-500 MeV, charge uniform 20-500 pC,
+# sigma_x (= sigma_y) and sigma_tau each log-uniform in 20-500 um
+BATCH_MESHES = [(32, 32, 32), (48, 48, 48), (64, 64, 64), (96, 96, 96), (32, 32, 128)]
+
+
+def batch_specs(nbeams=96, seed=SEED + 4):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lg = lambda a, b: float(10 ** rng.uniform(math.log10(a), math.log10(b)))  # noqa: E731
+    out = []
+    for i in range(nbeams):
+        out.append({"n": int(round(lg(1e4, 4e6))), "mesh": BATCH_MESHES[int(rng.integers(len(BATCH_MESHES)))],
+                    "E": float(rng.uniform(0.005, 0.5)), "Q": float(rng.uniform(20e-12, 500e-12)),
+                    "sx": lg(20e-6, 500e-6), "st": lg(20e-6, 500e-6), "seed": seed * 1000 + i})
+    return out
+
+
+def device_beam(spec, dev):
+    """Seeded Gaussian beam generated on the device (rows padded to an even stride)."""
+    import torch
+    n = spec["n"]
+    g = torch.Generator(device=dev)
+    g.manual_seed(spec["seed"])
+    buf = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=dev)
+    for row, sig in enumerate((spec["sx"], 1e-5, spec["sx"], 1e-5, spec["st"], 1e-4)):
+        buf[row].normal_(0.0, sig, generator=g)
+    q = torch.full((n,), spec["Q"] / n, dtype=torch.float64, device=dev)
+    return buf[:, :n], q
+
+
+def time_batched(steps, warmup, dev):
+    """The 96-beam workload kicked by sc_kick_batched (one launch per stage,
+    recorded once as a CUDA graph and replayed), against the same beams
+    kicked one sc_kick after another on one stream."""
+    import torch
+    from ocelot_gb300.batch import BeamBatch
+    specs = batch_specs()
+    batch = BeamBatch(dev)
+    beams = []
+    for sp in specs:
+        rp, q = device_beam(sp, dev)
+        batch.add(rp, q, sp["E"], sp["mesh"], DZ)
+        beams.append((rp, q, sp))
+    batch.commit()
+    g = batch.graph()
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        g.replay()
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        g.replay()
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    batch.check()
+    # the same beams, one plain kick each, on one stream (same plans and workspaces)
+    seq_ms = []
+    for it in range(warmup + steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for (eng, rp, q, E, dz) in batch.beams:
+            eng.kick(rp, q, int(rp.shape[1]), E, dz)
+        b.record(stream)
+        b.synchronize()
+        if it >= warmup:
+            seq_ms.append(a.elapsed_time(b))
+    batch.check()
+    ntot = sum(sp["n"] for sp in specs)
+    cells = sum(math.prod(sp["mesh"]) for sp in specs)
+    t = statistics.mean(ms)
+    ts = statistics.mean(seq_ms)
+    alg = B_PER_PARTICLE * ntot + 2 * 4 * cells
+    return {
+        "workload": "96 seeded Gaussian beams, N log-uniform 1e4-4e6, meshes from 32^3/48^3/64^3/96^3/32x32x128, "
+                    "E 5-500 MeV, Q 20-500 pC, sigma_x and sigma_tau log-uniform 20-500 um; one 0.1 m kick "
+                    "per beam per step (FP32 form); 15 launches per step recorded as one CUDA graph",
+        "beams": len(specs), "particles": ntot, "value": ntot / (t * 1e-3), "unit": "particle-kicks/s",
+        "ms_per_step": t, "launches_per_step": 15,
+        "sequential": {"value": ntot / (ts * 1e-3), "ms_per_step": ts, "launches_per_step": 15 * len(specs),
+                       "how": "one sc_kick per beam, one stream, same plans and workspaces"},
+        "batched_over_sequential": ts / t,
+        "hbm": {"algorithmic_bytes_per_step": alg, "achieved_gbs": alg / (t * 1e-3) / 1e9},
+        "l2": "not flushed: the 96 beams' particles (several GB) exceed L2",
+    }
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -265,6 +355,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_PART)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip timing the FP64 form")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 96-beam batched leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -294,6 +385,7 @@ def main():
         barrier()
     kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
     e2e_dt, h2d, d2h = time_e2e("fp32", n, args.steps, args.warmup, dev)
+    batched = None if args.no_batch else time_batched(args.steps, args.warmup, dev)
     kick_err = fp32_kick_error(n, dev)
     barrier()
 
@@ -345,6 +437,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "particle-kicks/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches32,
+            "batched": batched,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }

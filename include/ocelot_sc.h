@@ -98,6 +98,53 @@ int sc_kick(sc_plan* plan, void* ws, size_t ws_bytes, double* rparticles, int64_
             const double* q, int64_t n, double energy_gev, double zstep,
             double mesh_scale, double mesh_shift, void* stream);
 
+/* ---- many beams at once ------------------------------------------------ */
+
+/* One kick for each of many beams, each with its own plan (mesh), workspace
+ * and particles, in ONE launch per stage: every stage kernel runs over a
+ * device work table whose prefix rows map each block to a beam and to its
+ * block within that beam's grid.  A beam keeps the grids, reductions and
+ * arithmetic of a single sc_kick, so its result is bit-identical to
+ * sc_kick's alone; the number of launches per batched kick (15) does not
+ * depend on the number of beams.  No counterpart in the reference, whose
+ * track() kicks one beam at a time (ocelot/cpbd/track.py:476-478): this is
+ * the multi-beam entry of the same SpaceCharge.apply (sc.py:208-251).
+ *
+ * Requirements: every plan is SC_FP32 without SC_FP32_SORTED_DEPOSIT (the
+ * exact fixed-point deposit), each beam has its own plan and initialised
+ * workspace, and no two beams share a workspace or particles.  Beams with
+ * zstep == 0 are left out (sc.py:210-212). */
+typedef struct sc_batch sc_batch;
+typedef struct sc_beam {
+    sc_plan* plan;
+    void* ws;
+    size_t ws_bytes;
+    double* rparticles;     /* device float64 [6][ld] */
+    int64_t ld;
+    const double* q;        /* device float64 [n] */
+    int64_t n;
+    double energy_gev;
+    double zstep;
+    double mesh_scale;      /* NAN unless random_mesh */
+    double mesh_shift;
+} sc_beam;
+
+/* A batch of up to max_beams beams.  Allocates its work table (device and
+ * pinned host, about 1 KB per beam) and a second stream with two events. */
+int sc_batch_create(sc_batch** out, int max_beams);
+void sc_batch_destroy(sc_batch* batch);
+/* Validates the beams and uploads the work table with an asynchronous copy
+ * on `stream`.  Waits (on the host) only for the copy of the previous call.
+ * Not allowed during stream capture. */
+int sc_batch_set(sc_batch* batch, const sc_beam* beams, int nbeams, void* stream);
+/* Kicks every beam of the table currently set (stream-ordered after the
+ * upload).  Capturable in a CUDA graph; a replay kicks the beams of the
+ * table resident at replay time.  Device errors latch in each beam's
+ * workspace (sc_read_status). */
+int sc_kick_batched(sc_batch* batch, void* stream);
+/* Kernels launched by the last sc_kick_batched (0 before the first). */
+int sc_batch_launches(const sc_batch* batch);
+
 /* ---- stages, mirroring SpaceCharge's public methods ------------------- */
 
 /* SpaceCharge.el_field(X, Q, gamma, nxyz) -- sc.py:170-205.

@@ -33,6 +33,12 @@ vp = C.c_void_p
 i64 = C.c_int64
 dbl = C.c_double
 
+class ScBeam(C.Structure):
+    """struct sc_beam of include/ocelot_sc.h."""
+    _fields_ = [("plan", vp), ("ws", vp), ("ws_bytes", C.c_size_t), ("rparticles", vp), ("ld", i64), ("q", vp),
+                ("n", i64), ("energy_gev", dbl), ("zstep", dbl), ("mesh_scale", dbl), ("mesh_shift", dbl)]
+
+
 # name -> (restype, argtypes); the same list as include/ocelot_sc.h
 SIGNATURES = {
     "sc_plan_create": (C.c_int, [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_int]),
@@ -51,6 +57,11 @@ SIGNATURES = {
     "sc_sort_keys": (C.c_int, [vp, i64, C.c_int, vp, vp, vp, C.c_size_t, vp]),
     "sc_tmap_apply": (C.c_int, [C.POINTER(dbl), C.POINTER(dbl), vp, i64, i64, vp]),
     "sc_tmap_apply_indexed": (C.c_int, [vp, vp, C.c_int, vp, i64, i64, vp]),
+    "sc_batch_create": (C.c_int, [C.POINTER(vp), C.c_int]),
+    "sc_batch_destroy": (None, [vp]),
+    "sc_batch_set": (C.c_int, [vp, C.POINTER(ScBeam), C.c_int, vp]),
+    "sc_kick_batched": (C.c_int, [vp, vp]),
+    "sc_batch_launches": (C.c_int, [vp]),
     "sc_profile_enable": (C.c_int, [vp, C.c_int]),
     "sc_profile_read": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     "sc_profile_stage_name": (C.c_char_p, [C.c_int]),

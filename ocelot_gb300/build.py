@@ -23,7 +23,12 @@ LIB = os.path.join(LIBDIR, "libocelot_sc.so")
 
 SOURCES = ["sc_api.cu", "sc_particles.cu", "sc_sort.cu", "sc_green.cu", "sc_fft.cu", "sc_tmap.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+# -fmad=false: no implicit contraction of a*b+c into FMAs.  Every kernel body
+# is inlined into a plain and a batched kernel, and a + b*c + d*e can be
+# contracted either way; without implicit contraction each body rounds the
+# same in both, so a beam's result does not depend on how it was launched.
+# The FMAs the kernels want are written out (fma, __fma_rn).
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include")]
 if os.environ.get("OCELOT_SC_CHECKED") == "1":
     # index checks that record the first bad index in the device state

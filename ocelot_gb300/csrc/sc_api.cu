@@ -112,14 +112,16 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.xp = take(p.prec == SC_FP64 ? 8 * 6 * (size_t)n : 0);
     L.X = take(rs * 3 * (size_t)((n + 3) / 4 * 4));
     L.keys = take(4 * (size_t)n);
-    L.sort_keys = take(4 * (size_t)n);
-    L.sort_perm = take(4 * (size_t)n);
-    L.sort_q = take(rs * (size_t)n);
-    L.sort_tmp_k = take(4 * (size_t)n);
-    L.sort_tmp_v = take(4 * (size_t)n);
-    const size_t sb = (size_t)((n + 4095) / 4096);
-    L.sort_hist = take(4 * 512 * (sb ? sb : 1));
-    L.sort_tot = take(4 * 512);
+    // the radix sort's buffers: only the sorted deposit uses them
+    const size_t ns = p.sorted_deposit ? (size_t)n : 0;
+    L.sort_keys = take(4 * ns);
+    L.sort_perm = take(4 * ns);
+    L.sort_q = take(rs * ns);
+    L.sort_tmp_k = take(4 * ns);
+    L.sort_tmp_v = take(4 * ns);
+    const size_t sb = (ns + 4095) / 4096;
+    L.sort_hist = take(p.sorted_deposit ? 4 * 512 * (sb ? sb : 1) : 0);
+    L.sort_tot = take(p.sorted_deposit ? 4 * 512 : 0);
     L.total = o;
     return L;
 }
@@ -590,6 +592,179 @@ int sc_tmap_apply(const double* R, const double* B, double* rp, int64_t ld, int6
     SC_CUDA(launch_tmap(R, B, rp, ld, n, (cudaStream_t)stream), "tmap");
     return SC_OK;
 }
+
+struct sc_batch {
+    int max_beams;
+    char* h_buf;             // pinned: BatchBeam[max_beams], then int start[BS_COUNT][max_beams + 1]
+    char* d_buf;             // device copy
+    size_t beams_bytes, start_bytes;
+    cudaEvent_t uploaded;    // the last upload's copy has read h_buf
+    bool upload_pending;
+    int nb;
+    int blocks[BS_COUNT];
+    size_t fft_smem[3], green_smem[3];
+    cudaStream_t side;
+    cudaEvent_t fork, join;
+    int last_launches;
+};
+
+int sc_batch_create(sc_batch** out, int max_beams) {
+    if (!out) return fail(SC_ERR_ARG, "batch pointer is NULL");
+    *out = nullptr;
+    if (max_beams < 1 || max_beams > (1 << 20)) return fail(SC_ERR_ARG, "max_beams=%d out of range", max_beams);
+    SC_CUDA(prepare_batch_fft(), "kernel attributes");
+    SC_CUDA(prepare_batch_green(), "kernel attributes");
+    sc_batch* b = new (std::nothrow) sc_batch;
+    if (!b) return fail(SC_ERR_ARG, "out of host memory");
+    memset(b, 0, sizeof *b);
+    b->max_beams = max_beams;
+    b->beams_bytes = align_up(sizeof(BatchBeam) * (size_t)max_beams);
+    b->start_bytes = sizeof(int) * (size_t)BS_COUNT * (max_beams + 1);
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&b->h_buf), b->beams_bytes + b->start_bytes);
+    if (!e) e = cudaMalloc(reinterpret_cast<void**>(&b->d_buf), b->beams_bytes + b->start_bytes);
+    if (!e) e = cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming);
+    if (!e) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (!e) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    if (e) {
+        sc_batch_destroy(b);
+        return fail(SC_ERR_CUDA, "sc_batch_create: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return SC_OK;
+}
+
+void sc_batch_destroy(sc_batch* b) {
+    if (!b) return;
+    if (b->side) {
+        cudaStreamSynchronize(b->side);
+        cudaStreamDestroy(b->side);
+    }
+    if (b->uploaded) cudaEventSynchronize(b->uploaded), cudaEventDestroy(b->uploaded);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->d_buf) cudaFree(b->d_buf);
+    if (b->h_buf) cudaFreeHost(b->h_buf);
+    delete b;
+}
+
+int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
+    if (!b) return fail(SC_ERR_ARG, "batch is NULL");
+    if (nbeams < 0 || nbeams > b->max_beams)
+        return fail(SC_ERR_ARG, "nbeams=%d outside [0, %d]", nbeams, b->max_beams);
+    if (nbeams && !beams) return fail(SC_ERR_ARG, "beams is NULL");
+    const PhysConst c = phys_const();
+    // validate everything before touching the table
+    std::unordered_map<const void*, int> seen;
+    for (int i = 0; i < nbeams; ++i) {
+        const sc_beam& m = beams[i];
+        if (!m.plan) return fail(SC_ERR_ARG, "beam %d: plan is NULL", i);
+        if (m.plan->p.prec != SC_FP32 || m.plan->p.sorted_deposit)
+            return fail(SC_ERR_UNSUPPORTED, "beam %d: batched kicks need SC_FP32 plans with the fixed-point deposit", i);
+        if (m.zstep == 0) continue;
+        if (m.n < 1 || m.n > 0x7fffffffLL) return fail(SC_ERR_ARG, "beam %d: n=%lld", i, (long long)m.n);
+        if (!m.rparticles || !m.q) return fail(SC_ERR_ARG, "beam %d: rparticles or q is NULL", i);
+        if (m.ld < m.n) return fail(SC_ERR_ARG, "beam %d: ld=%lld < n=%lld", i, (long long)m.ld, (long long)m.n);
+        if (!(m.energy_gev > 0) || !isfinite(m.energy_gev) || !isfinite(m.zstep) ||
+            !(m.energy_gev / c.m_e_GeV > 1.0))
+            return fail(SC_ERR_ARG, "beam %d: energy %g GeV / zstep %g invalid", i, m.energy_gev, m.zstep);
+        int r = check_ws(m.plan, m.ws, m.ws_bytes, m.n);
+        if (r) return fail(r, "beam %d: %s", i, g_err.c_str());
+        for (const void* ptr : {(const void*)m.ws, (const void*)m.rparticles}) {
+            if (!seen.emplace(ptr, i).second)
+                return fail(SC_ERR_ARG, "beam %d shares a workspace or particle array with beam %d", i, seen[ptr]);
+        }
+    }
+    if (b->upload_pending) SC_CUDA(cudaEventSynchronize(b->uploaded), "cudaEventSynchronize");
+    BatchBeam* hb = reinterpret_cast<BatchBeam*>(b->h_buf);
+    int* hs = reinterpret_cast<int*>(b->h_buf + b->beams_bytes);
+    const int stride = b->max_beams + 1;
+    int nb = 0;
+    for (int k = 0; k < 3; ++k) b->fft_smem[k] = b->green_smem[k] = 0;
+    for (int i = 0; i < nbeams; ++i) {
+        const sc_beam& m = beams[i];
+        if (m.zstep == 0) continue;
+        BatchBeam& B = hb[nb];
+        memset(&B, 0, sizeof B);
+        const Plan& p = m.plan->p;
+        B.ws = static_cast<char*>(m.ws);
+        B.rp = m.rparticles;
+        B.q = m.q;
+        B.kp = make_params(p, m.n, m.ld, m.energy_gev, m.zstep, m.mesh_scale, m.mesh_shift);
+        B.L = make_layout(p, m.n);
+        B.p = p;
+        const bool rp_ok = ((uintptr_t)m.rparticles % 16 == 0) && (m.ld % 2 == 0);
+        B.vec_rp = rp_ok;
+        B.vec_rpq = rp_ok && ((uintptr_t)m.q % 16 == 0);
+        size_t fs[3], gs[3];
+        batch_fft_tiling(B, fs);
+        batch_green_tiling(B, gs);
+        for (int k = 0; k < 3; ++k) {
+            b->fft_smem[k] = fs[k] > b->fft_smem[k] ? fs[k] : b->fft_smem[k];
+            b->green_smem[k] = gs[k] > b->green_smem[k] ? gs[k] : b->green_smem[k];
+        }
+        B.gx[BS_PART] = batch_particle_blocks(p, m.n);
+        B.gy[BS_PART] = 1;
+        ++nb;
+    }
+    for (int st = 0; st < BS_COUNT; ++st) {
+        int64_t acc = 0;
+        hs[st * stride] = 0;
+        for (int i = 0; i < nb; ++i) {
+            acc += (int64_t)hb[i].gx[st] * hb[i].gy[st];
+            if (acc > 0x7fffffffLL) return fail(SC_ERR_UNSUPPORTED, "batch needs more than 2^31 blocks in a stage");
+            hs[st * stride + i + 1] = (int)acc;
+        }
+        b->blocks[st] = (int)acc;
+    }
+    b->nb = nb;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nb) {
+        SC_CUDA(cudaMemcpyAsync(b->d_buf, b->h_buf, sizeof(BatchBeam) * nb, cudaMemcpyHostToDevice, s), "upload");
+        SC_CUDA(cudaMemcpyAsync(b->d_buf + b->beams_bytes, b->h_buf + b->beams_bytes, b->start_bytes,
+                                cudaMemcpyHostToDevice, s),
+                "upload");
+        SC_CUDA(cudaEventRecord(b->uploaded, s), "cudaEventRecord");
+        b->upload_pending = true;
+    }
+    return SC_OK;
+}
+
+int sc_kick_batched(sc_batch* b, void* stream) {
+    if (!b) return fail(SC_ERR_ARG, "batch is NULL");
+    b->last_launches = 0;
+    if (b->nb == 0) return SC_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const BatchBeam* beams = reinterpret_cast<const BatchBeam*>(b->d_buf);
+    const int* start = reinterpret_cast<const int*>(b->d_buf + b->beams_bytes);
+    const int stride = b->max_beams + 1;
+    auto row = [&](int st) { return start + st * stride; };
+    const int nb = b->nb;
+    SC_CUDA(launch_batch_particles(BP_FRAME, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched frame");
+    SC_CUDA(launch_batch_particles(BP_EXTENT, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched extent");
+    SC_CUDA(cudaEventRecord(b->fork, s), "cudaEventRecord");
+    SC_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "cudaStreamWaitEvent");
+    SC_CUDA(launch_batch_igf(beams, row(BS_IGF_C), row(BS_IGF_D), nb, b->blocks[BS_IGF_C], b->blocks[BS_IGF_D],
+                             b->side),
+            "batched igf");
+    const int gb[3] = {b->blocks[BS_GREEN_Z], b->blocks[BS_GREEN_Y], b->blocks[BS_GREEN_X]};
+    SC_CUDA(launch_batch_green(beams, row(BS_GREEN_Z), row(BS_GREEN_Y), row(BS_GREEN_X), nb, gb, b->green_smem,
+                               b->side),
+            "batched green spectrum");
+    SC_CUDA(cudaEventRecord(b->join, b->side), "cudaEventRecord");
+    SC_CUDA(launch_batch_particles(BP_KEYS, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched keys");
+    SC_CUDA(cudaStreamWaitEvent(s, b->join, 0), "cudaStreamWaitEvent");
+    const int fb[3] = {b->blocks[BS_FFT_Z], b->blocks[BS_FFT_Y], b->blocks[BS_FFT_X]};
+    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), nb, fb, b->fft_smem, s),
+            "batched convolve");
+    SC_CUDA(launch_batch_field(beams, row(BS_FIELD), nb, b->blocks[BS_FIELD], s), "batched field");
+    SC_CUDA(launch_batch_particles(BP_KICK, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched kick");
+    // frame, extent, igf 2, green 3, keys, convolve 5, field, kick
+    b->last_launches = 1 + 1 + 2 + 3 + 1 + 5 + 1 + 1;
+    return SC_OK;
+}
+
+int sc_batch_launches(const sc_batch* b) { return b ? b->last_launches : 0; }
 
 int sc_tmap_apply_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld, int64_t n,
                           void* stream) {

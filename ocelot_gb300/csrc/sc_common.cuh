@@ -189,6 +189,86 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
 cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld,
                                 int64_t n, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Batched kicks (sc_kick_batched): one launch per stage over many beams.
+//
+// Every kernel body takes the coordinates of its block within its beam's
+// grid (VBlk).  A plain launch passes the hardware's; a batched launch runs
+// one 1D grid that is the concatenation of every beam's grid for that stage,
+// and each block finds its beam in a prefix table of block counts.  The
+// per-beam grids are the ones the plain launches use, so a beam's arithmetic
+// -- reduction trees included -- is the same in a batch as alone.
+// ---------------------------------------------------------------------------
+struct VBlk {
+    int x, y, nx, ny;
+};
+__device__ __forceinline__ VBlk hw_vblk() {
+    return VBlk{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y};
+}
+
+enum BatchStage {
+    BS_PART = 0,   // frame, extent, keys, kick (one block per PT particles, capped)
+    BS_IGF_C,      // IGF corners
+    BS_IGF_D,      // IGF cell differences
+    BS_GREEN_Z,    // spectrum S1
+    BS_GREEN_Y,    // spectrum S2
+    BS_GREEN_X,    // spectrum S3
+    BS_FFT_Z,      // F1 and B1
+    BS_FFT_Y,      // F2 and B2
+    BS_FFT_X,      // F3 (x forward, Green multiply, x inverse)
+    BS_FIELD,      // field quads
+    BS_COUNT
+};
+
+struct BatchBeam {
+    char* ws;
+    double* rp;
+    const double* q;
+    KickParams kp;
+    Layout L;
+    Plan p;
+    int vec_rp, vec_rpq;              // 16-byte row accesses allowed: rparticles / rparticles and q
+    int fft_nc, fft_tky, fft_tkx;     // convolution tiling
+    int green_nc, green_tky, green_tkx;
+    int gx[BS_COUNT], gy[BS_COUNT];   // this beam's grid per stage
+};
+
+// beam of this block: the last b with start[b] <= blockIdx.x (start[nb] = total)
+__device__ __forceinline__ int batch_beam(const int* __restrict__ start, int nb) {
+    const int bid = (int)blockIdx.x;
+    int lo = 0, hi = nb;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(start + mid) <= bid) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+__device__ __forceinline__ VBlk batch_vblk(const int* __restrict__ start, int b, int gx, int gy) {
+    const int local = (int)blockIdx.x - __ldg(start + b);
+    return VBlk{local % gx, local / gx, gx, gy};
+}
+
+// batched stage launchers; start = the stage's prefix row (nb + 1 entries)
+enum BatchPartKernel { BP_FRAME, BP_EXTENT, BP_KEYS, BP_KICK };
+cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, const int* start, int nb, int blocks,
+                                   cudaStream_t s);
+cudaError_t launch_batch_igf(const BatchBeam* beams, const int* start_c, const int* start_d, int nb, int blocks_c,
+                             int blocks_d, cudaStream_t s);
+cudaError_t launch_batch_green(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
+                               const int blocks[3], const size_t smem[3], cudaStream_t s);
+cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
+                                  const int blocks[3], const size_t smem[3], cudaStream_t s);
+cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
+// host-side tiling of one beam (sets the tiling fields and grids of B)
+void batch_fft_tiling(BatchBeam& B, size_t smem[3]);
+void batch_green_tiling(BatchBeam& B, size_t smem[3]);
+int batch_particle_blocks(const Plan& p, int64_t n);
+int batch_igf_blocks(const Plan& p, int diff);
+// opt the batched kernels in to the device's largest dynamic shared memory
+cudaError_t prepare_batch_fft();
+cudaError_t prepare_batch_green();
+
 inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
 
 // Opt a kernel in to the device's largest dynamic shared memory, once per

@@ -42,10 +42,10 @@ static inline int strided_cols(int M) {
 // FP32 form's exact deposit; it is scaled to R here and also stored in q
 // (the charge grid an inspection reads back)
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const long long* __restrict__ qfix,
-                                                      Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
-                                                      RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
-                                                      const ScState* st) {
+__device__ __forceinline__ void zfwd_body(R* __restrict__ q, const long long* __restrict__ qfix,
+                                          Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
+                                          const RadixPlan& rz, const Cx<R>* __restrict__ twg, int NC,
+                                          const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mz = rz.L;
@@ -53,15 +53,15 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const l
     Cx<R>* a = tw + Mz;
     Cx<R>* b = a + NC * Mz;
     load_twiddles<R>(tw, twg, Mz);
-    const int x = blockIdx.y;
-    const int y0 = blockIdx.x * 2 * NC;
+    const int x = vb.y;
+    const int y0 = vb.x * 2 * NC;
     for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
         const int c = idx / Mz, z = idx - c * Mz;
         const int ya = y0 + 2 * c, yb = ya + 1;
         R re = 0, im = 0;
         if (z < nz) {
             const size_t ia = ((size_t)x * ny + ya) * nz + z, ib = ia + nz;
-            [[maybe_unused]] const long long ncell = (long long)gridDim.y * ny * nz;
+            [[maybe_unused]] const long long ncell = (long long)vb.ny * ny * nz;
             if ((ya < ny && !SC_IDX_OK(st, 21, ia, ncell)) || (yb < ny && !SC_IDX_OK(st, 22, ib, ncell))) continue;
             if (qfix) {
                 const float u = st->qfix_inv;
@@ -82,17 +82,24 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const l
         const Cx<R> Z = res[c * Mz + k];
         const Cx<R> Zm = res[c * Mz + (k == 0 ? 0 : Mz - k)];
         const R h = (R)0.5;
-        if (!SC_IDX_OK(st, 24, ((long long)x * My + (yb < ny ? yb : ya)) * Kz + k, (long long)gridDim.y * My * Kz)) continue;
+        if (!SC_IDX_OK(st, 24, ((long long)x * My + (yb < ny ? yb : ya)) * Kz + k, (long long)vb.ny * My * Kz)) continue;
         if (ya < ny) W[((size_t)x * My + ya) * Kz + k] = cx<R>((Z.x + Zm.x) * h, (Z.y - Zm.y) * h);
         if (yb < ny) W[((size_t)x * My + yb) * Kz + k] = cx<R>((Z.y + Zm.y) * h, (Zm.x - Z.x) * h);
     }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const long long* __restrict__ qfix,
+                                                      Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
+                                                      RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
+                                                      const ScState* st) {
+    zfwd_body<R>(q, qfix, W, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk());
+}
+
 // strided pass along y: forward (rows < ny in, all My out) or inverse (all in, rows < ny out)
 template <typename R, bool INV>
-__global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int ny, int My, int Kz,
-                                                       RadixPlan ry, const Cx<R>* __restrict__ twg,
-                                                       int TK, const ScState* st) {
+__device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My, int Kz, const RadixPlan& ry,
+                                           const Cx<R>* __restrict__ twg, int TK, const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int ls = My + 1;
@@ -100,8 +107,8 @@ __global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, in
     Cx<R>* a = tw + My;
     Cx<R>* b = a + TK * ls;
     load_twiddles<R>(tw, twg, My);
-    const int x = blockIdx.y;
-    const int k0 = blockIdx.x * TK;
+    const int x = vb.y;
+    const int k0 = vb.x * TK;
     const int nin = INV ? My : ny;
     for (int idx = threadIdx.x; idx < My * TK; idx += blockDim.x) {
         const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
@@ -118,11 +125,18 @@ __global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, in
     }
 }
 
+template <typename R, bool INV>
+__global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int ny, int My, int Kz,
+                                                       RadixPlan ry, const Cx<R>* __restrict__ twg,
+                                                       int TK, const ScState* st) {
+    ypass_body<R, INV>(W, ny, My, Kz, ry, twg, TK, st, hw_vblk());
+}
+
 // x pass: forward FFT of the nx non-zero planes, Green multiply, inverse FFT, keep x < nx
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, const R* __restrict__ G,
-                                                       int nx, int My, int Kz, int Ky, RadixPlan rx,
-                                                       const Cx<R>* __restrict__ twg, int TK, const ScState* st) {
+__device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __restrict__ G, int nx, int My, int Kz,
+                                           int Ky, const RadixPlan& rx, const Cx<R>* __restrict__ twg, int TK,
+                                           const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mx = rx.L;
@@ -131,9 +145,9 @@ __global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, co
     Cx<R>* a = tw + Mx;
     Cx<R>* b = a + TK * ls;
     load_twiddles<R>(tw, twg, Mx);
-    const int ky = blockIdx.y;
+    const int ky = vb.y;
     const int gy = ky <= My - ky ? ky : My - ky;
-    const int k0 = blockIdx.x * TK;
+    const int k0 = vb.x * TK;
     for (int idx = threadIdx.x; idx < Mx * TK; idx += blockDim.x) {
         const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
         Cx<R> v = cx<R>(0, 0);
@@ -161,10 +175,16 @@ __global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, co
 }
 
 template <typename R>
-__global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ W, R* __restrict__ phi,
-                                                      int ny, int nz, int My, int Kz, RadixPlan rz,
-                                                      const Cx<R>* __restrict__ twg, int NC,
-                                                      const ScState* st) {
+__global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, const R* __restrict__ G,
+                                                       int nx, int My, int Kz, int Ky, RadixPlan rx,
+                                                       const Cx<R>* __restrict__ twg, int TK, const ScState* st) {
+    xconv_body<R>(W, G, nx, My, Kz, Ky, rx, twg, TK, st, hw_vblk());
+}
+
+template <typename R>
+__device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __restrict__ phi, int ny, int nz, int My,
+                                          int Kz, const RadixPlan& rz, const Cx<R>* __restrict__ twg, int NC,
+                                          const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mz = rz.L;
@@ -172,8 +192,8 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ 
     Cx<R>* a = tw + Mz;
     Cx<R>* b = a + NC * Mz;
     load_twiddles<R>(tw, twg, Mz);
-    const int x = blockIdx.y;
-    const int y0 = blockIdx.x * 2 * NC;
+    const int x = vb.y;
+    const int y0 = vb.x * 2 * NC;
     for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
         const int c = idx / Mz, k = idx - c * Mz;
         const int ya = y0 + 2 * c, yb = ya + 1;
@@ -202,6 +222,14 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ 
             if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = v.y * fscale;
         }
     }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ W, R* __restrict__ phi,
+                                                      int ny, int nz, int My, int Kz, RadixPlan rz,
+                                                      const Cx<R>* __restrict__ twg, int NC,
+                                                      const ScState* st) {
+    zinv_body<R>(W, phi, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk());
 }
 
 // Ex,Ey,Ez = forward differences / h, zero on the last plane (sc.py:195-200).
@@ -239,10 +267,11 @@ __device__ __forceinline__ float fd(const float* __restrict__ phi, int i, int j,
     return (phi[c] - phi[c + (di * ny + dj) * nz + dk]) * ih;
 }
 
-__global__ void k_field_quads(const float* __restrict__ phi, float4* __restrict__ qx, float4* __restrict__ qy,
-                              float4* __restrict__ qz, int nx, int ny, int nz, const ScState* st) {
+__device__ __forceinline__ void field_quads_body(const float* __restrict__ phi, float4* __restrict__ qx,
+                                                 float4* __restrict__ qy, float4* __restrict__ qz, int nx, int ny,
+                                                 int nz, const ScState* st, VBlk vb) {
     if (st->status) return;
-    const int j = blockIdx.x, i = blockIdx.y;
+    const int j = vb.x, i = vb.y;
     const float ihx = st->istepsf[0], ihy = st->istepsf[1], ihz = st->istepsf[2];
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
         const int c = (i * ny + j) * nz + k;
@@ -256,6 +285,11 @@ __global__ void k_field_quads(const float* __restrict__ phi, float4* __restrict_
                             fd(phi, i, j + 1, k, 0, 0, 1, nx, ny, nz, ihz),
                             fd(phi, i, j + 1, k + 1, 0, 0, 1, nx, ny, nz, ihz));
     }
+}
+
+__global__ void k_field_quads(const float* __restrict__ phi, float4* __restrict__ qx, float4* __restrict__ qy,
+                              float4* __restrict__ qz, int nx, int ny, int nz, const ScState* st) {
+    field_quads_body(phi, qx, qy, qz, nx, ny, nz, st, hw_vblk());
 }
 
 
@@ -337,6 +371,104 @@ static cudaError_t field_t(const Plan& p, const Layout& L, char* ws, cudaStream_
 
 cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
     return p.prec == SC_FP64 ? field_t<double>(p, L, ws, s) : field_t<float>(p, L, ws, s);
+}
+
+// ---------------------------------------------------------------------------
+// batched convolution and field (FP32 form): one launch per pass over every
+// beam of a batch, each beam with the tiling of its plain launch
+// ---------------------------------------------------------------------------
+#define BATCH_BEAM(stage)                                                       \
+    const int b = batch_beam(start, nb);                                        \
+    const BatchBeam& B = beams[b];                                              \
+    const VBlk vb = batch_vblk(start, b, B.gx[stage], B.gy[stage]);             \
+    char* ws = B.ws;                                                            \
+    const Layout& L = B.L;                                                      \
+    const Plan& p = B.p;                                                        \
+    const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
+
+__global__ void __launch_bounds__(FFT_THREADS) kb_zfwd(const BatchBeam* __restrict__ beams,
+                                                       const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_FFT_Z)
+    zfwd_body<float>(reinterpret_cast<float*>(ws + L.qgrid), reinterpret_cast<const long long*>(ws + L.qfix),
+                     reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.nz, p.My, p.Mz / 2 + 1, p.rz,
+                     reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.fft_nc, st, vb);
+}
+
+template <bool INV>
+__global__ void __launch_bounds__(FFT_THREADS) kb_ypass(const BatchBeam* __restrict__ beams,
+                                                        const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_FFT_Y)
+    ypass_body<float, INV>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry,
+                           reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.fft_tky, st, vb);
+}
+
+__global__ void __launch_bounds__(FFT_THREADS) kb_xconv(const BatchBeam* __restrict__ beams,
+                                                        const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_FFT_X)
+    xconv_body<float>(reinterpret_cast<Cx<float>*>(ws + L.W), reinterpret_cast<const float*>(ws + L.green), p.nx,
+                      p.My, p.Mz / 2 + 1, p.My / 2 + 1, p.rx, reinterpret_cast<const Cx<float>*>(ws + L.tw_x),
+                      B.fft_tkx, st, vb);
+}
+
+__global__ void __launch_bounds__(FFT_THREADS) kb_zinv(const BatchBeam* __restrict__ beams,
+                                                       const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_FFT_Z)
+    zinv_body<float>(reinterpret_cast<const Cx<float>*>(ws + L.W), reinterpret_cast<float*>(ws + L.phi), p.ny, p.nz,
+                     p.My, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.fft_nc, st, vb);
+}
+
+__global__ void kb_field_quads(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_FIELD)
+    field_quads_body(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float4*>(ws + L.exq),
+                     reinterpret_cast<float4*>(ws + L.eyq), reinterpret_cast<float4*>(ws + L.ezq), p.nx, p.ny, p.nz,
+                     st, vb);
+}
+#undef BATCH_BEAM
+
+void batch_fft_tiling(BatchBeam& B, size_t smem[3]) {
+    const Plan& p = B.p;
+    const int Kz = p.Mz / 2 + 1;
+    B.fft_nc = z_lines_per_block(p.Mz);
+    B.fft_tky = strided_cols<float>(p.My);
+    B.fft_tkx = strided_cols<float>(p.Mx);
+    B.gx[BS_FFT_Z] = (p.ny + 2 * B.fft_nc - 1) / (2 * B.fft_nc);
+    B.gy[BS_FFT_Z] = p.nx;
+    B.gx[BS_FFT_Y] = (Kz + B.fft_tky - 1) / B.fft_tky;
+    B.gy[BS_FFT_Y] = p.nx;
+    B.gx[BS_FFT_X] = (Kz + B.fft_tkx - 1) / B.fft_tkx;
+    B.gy[BS_FFT_X] = p.My;
+    B.gx[BS_FIELD] = p.ny;
+    B.gy[BS_FIELD] = p.nx;
+    smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.fft_nc * p.Mz);
+    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.fft_tky * (p.My + 1));
+    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.fft_tkx * (p.Mx + 1));
+}
+
+cudaError_t prepare_batch_fft() {
+    cudaError_t e;
+    const size_t big = 48 * 1024 + 1;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_zfwd), big))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_ypass<false>), big))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_ypass<true>), big))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_xconv), big))) return e;
+    return smem_opt_in(reinterpret_cast<const void*>(kb_zinv), big);
+}
+
+cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
+                                  const int blocks[3], const size_t smem[3], cudaStream_t s) {
+    if (nb <= 0) return cudaSuccess;
+    kb_zfwd<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
+    kb_ypass<false><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
+    kb_xconv<<<blocks[2], FFT_THREADS, smem[2], s>>>(beams, sx, nb);
+    kb_ypass<true><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
+    kb_zinv<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s) {
+    if (nb <= 0) return cudaSuccess;
+    kb_field_quads<<<blocks, 128, 0, s>>>(beams, start, nb);
+    return cudaGetLastError();
 }
 
 }  // namespace ocsc

@@ -73,7 +73,8 @@ __device__ __forceinline__ double igf_point(double x, double y, double z) {
 
 // IG on the corners of the near box (the whole octant when not hybrid),
 // stored with the box's corner strides
-__global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, IgfArgs a, const ScState* st) {
+__device__ __forceinline__ void igf_corners_body(double* __restrict__ ig, int nx, int ny, int nz, const IgfArgs& a,
+                                                 const ScState* st, VBlk vb) {
     if (igf_skip(st, a)) return;
     double hx, hy, hz;
     igf_spacing(st, a, hx, hy, hz);
@@ -81,7 +82,7 @@ __global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, I
     igf_box(hx, hy, hz, nx, ny, nz, a.hybrid, b);
     const int cx1 = b[0] + 1, cy1 = b[1] + 1, cz1 = b[2] + 1;
     const size_t total = (size_t)cx1 * cy1 * cz1;
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
+    for (size_t c = vb.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)vb.nx * blockDim.x) {
         const int k = (int)(c % cz1);
         const int j = (int)((c / cz1) % cy1);
         const int i = (int)(c / ((size_t)cz1 * cy1));
@@ -91,6 +92,10 @@ __global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, I
         if (!SC_IDX_OK(st, 31, c, (long long)(nx + 1) * (ny + 1) * (nz + 1))) continue;
         ig[c] = igf_point(x, y, z);
     }
+}
+
+__global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, IgfArgs a, const ScState* st) {
+    igf_corners_body(ig, nx, ny, nz, a, st, hw_vblk());
 }
 
 // 4th-order multipole form of the integral of 1/r over the cell centred at
@@ -119,8 +124,8 @@ __device__ __forceinline__ float cell_multipole(float X, float Y, float Z, float
 // cell integrals: the 8-corner difference of IG inside the near box (FP64),
 // the multipole form outside it (FP32 form only); written as R
 template <typename R>
-__global__ void k_igf_diff(const double* __restrict__ ig, R* __restrict__ k1, int nx, int ny, int nz, IgfArgs a,
-                           const ScState* st) {
+__device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* __restrict__ k1, int nx, int ny,
+                                              int nz, const IgfArgs& a, const ScState* st, VBlk vb) {
     if (igf_skip(st, a)) return;
     double hx, hy, hz;
     igf_spacing(st, a, hx, hy, hz);
@@ -130,7 +135,7 @@ __global__ void k_igf_diff(const double* __restrict__ ig, R* __restrict__ k1, in
     const float a2 = 0.25f * hxf * hxf, b2 = 0.25f * hyf * hyf, c2 = 0.25f * hzf * hzf, V = hxf * hyf * hzf;
     const size_t total = (size_t)nx * ny * nz;
     const size_t sy = bx[2] + 1, sx = (size_t)(bx[1] + 1) * (bx[2] + 1);
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
+    for (size_t c = vb.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)vb.nx * blockDim.x) {
         const int k = (int)(c % nz);
         const int j = (int)((c / nz) % ny);
         const int i = (int)(c / ((size_t)nz * ny));
@@ -152,6 +157,12 @@ __global__ void k_igf_diff(const double* __restrict__ ig, R* __restrict__ k1, in
     }
 }
 
+template <typename R>
+__global__ void k_igf_diff(const double* __restrict__ ig, R* __restrict__ k1, int nx, int ny, int nz, IgfArgs a,
+                           const ScState* st) {
+    igf_diff_body<R>(ig, k1, nx, ny, nz, a, st, hw_vblk());
+}
+
 // index of the even extension of a length-n octant to a period M (-1: zero)
 __device__ __forceinline__ int even_src(int z, int n, int M) {
     if (z < n) return z;
@@ -171,9 +182,9 @@ static inline int green_cols(int M) {
 
 // S1: along z; rows (x, y) of K1 -> S1[x][y][kz], kz <= Mz/2
 template <typename R>
-__global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __restrict__ s1, int ny, int nz,
-                                                int Kz, RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
-                                                IgfArgs a, const ScState* st) {
+__device__ __forceinline__ void green_z_body(const R* __restrict__ k1, R* __restrict__ s1, int ny, int nz, int Kz,
+                                             const RadixPlan& rz, const Cx<R>* __restrict__ twg, int NC,
+                                             const IgfArgs& a, const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (igf_skip(st, a)) return;
     const int Mz = rz.L;
@@ -181,13 +192,13 @@ __global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __r
     Cx<R>* A = tw + Mz;
     Cx<R>* B = A + NC * Mz;
     load_twiddles<R>(tw, twg, Mz);
-    const int x = blockIdx.y, y0 = blockIdx.x * 2 * NC;
+    const int x = vb.y, y0 = vb.x * 2 * NC;
     for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
         const int c = idx / Mz, z = idx - c * Mz;
         const int ya = y0 + 2 * c, yb = ya + 1;
         const int zs = even_src(z, nz, Mz);
         R re = 0, im = 0;
-        if (zs >= 0 && SC_IDX_OK(st, 33, ((long long)x * ny + (ya < ny ? ya : 0)) * nz + zs, (long long)gridDim.y * ny * nz)) {
+        if (zs >= 0 && SC_IDX_OK(st, 33, ((long long)x * ny + (ya < ny ? ya : 0)) * nz + zs, (long long)vb.ny * ny * nz)) {
             if (ya < ny) re = k1[((size_t)x * ny + ya) * nz + zs];
             if (yb < ny) im = k1[((size_t)x * ny + yb) * nz + zs];
         }
@@ -199,20 +210,27 @@ __global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __r
         const int c = idx / Kz, k = idx - c * Kz;
         const int ya = y0 + 2 * c, yb = ya + 1;
         const Cx<R> v = res[c * Mz + k];
-        if (!SC_IDX_OK(st, 35, ((long long)x * ny + (yb < ny ? yb : ya)) * Kz + k, (long long)gridDim.y * ny * Kz)) continue;
+        if (!SC_IDX_OK(st, 35, ((long long)x * ny + (yb < ny ? yb : ya)) * Kz + k, (long long)vb.ny * ny * Kz)) continue;
         if (ya < ny) s1[((size_t)x * ny + ya) * Kz + k] = v.x;
         if (yb < ny) s1[((size_t)x * ny + yb) * Kz + k] = v.y;
     }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __restrict__ s1, int ny, int nz,
+                                                int Kz, RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
+                                                IgfArgs a, const ScState* st) {
+    green_z_body<R>(k1, s1, ny, nz, Kz, rz, twg, NC, a, st, hw_vblk());
+}
+
 // S2/S3: strided passes over columns kz (paired), line axis of length n -> M,
 // input rows in[(o*nin + l)*Kz + kz], output rows out[(o*nout + kl)*Kz + kz]
 template <typename R>
-__global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, R* __restrict__ out, int n,
-                                                      int nin_stride, int nout, int Kz, int outer_in_stride,
-                                                      int outer_out_stride, RadixPlan rp,
-                                                      const Cx<R>* __restrict__ twg, int GTK, IgfArgs a,
-                                                      const ScState* st) {
+__device__ __forceinline__ void green_strided_body(const R* __restrict__ in, R* __restrict__ out, int n,
+                                                   int nin_stride, int nout, int Kz, int outer_in_stride,
+                                                   int outer_out_stride, const RadixPlan& rp,
+                                                   const Cx<R>* __restrict__ twg, int GTK, const IgfArgs& a,
+                                                   const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (igf_skip(st, a)) return;
     const int M = rp.L, ls = M + 1;
@@ -220,8 +238,8 @@ __global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, 
     Cx<R>* A = tw + M;
     Cx<R>* B = A + GTK * ls;
     load_twiddles<R>(tw, twg, M);
-    const int o = blockIdx.y;
-    const int k0 = blockIdx.x * 2 * GTK;
+    const int o = vb.y;
+    const int k0 = vb.x * 2 * GTK;
     const R* src = in + (size_t)o * outer_in_stride;
     R* dst = out + (size_t)o * outer_out_stride;
     for (int idx = threadIdx.x; idx < M * GTK; idx += blockDim.x) {
@@ -244,6 +262,16 @@ __global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, 
         if (ka < Kz) dst[(size_t)l * nin_stride + ka] = v.x;
         if (kb < Kz) dst[(size_t)l * nin_stride + kb] = v.y;
     }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, R* __restrict__ out, int n,
+                                                      int nin_stride, int nout, int Kz, int outer_in_stride,
+                                                      int outer_out_stride, RadixPlan rp,
+                                                      const Cx<R>* __restrict__ twg, int GTK, IgfArgs a,
+                                                      const ScState* st) {
+    green_strided_body<R>(in, out, n, nin_stride, nout, Kz, outer_in_stride, outer_out_stride, rp, twg, GTK, a, st,
+                          hw_vblk());
 }
 
 
@@ -348,6 +376,123 @@ cudaError_t prepare_green_kernels(const Plan& p) {
 
 cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
     return p.prec == SC_FP64 ? spectrum_t<double>(p, L, ws, s) : spectrum_t<float>(p, L, ws, s);
+}
+
+// ---------------------------------------------------------------------------
+// batched IGF table and spectrum (FP32 form): one launch per pass over every
+// beam of a batch; each beam decides on the device whether its table needs a
+// rebuild, as in the plain launches
+// ---------------------------------------------------------------------------
+#define BATCH_BEAM(stage)                                                       \
+    const int b = batch_beam(start, nb);                                        \
+    const BatchBeam& B = beams[b];                                              \
+    const VBlk vb = batch_vblk(start, b, B.gx[stage], B.gy[stage]);             \
+    char* ws = B.ws;                                                            \
+    const Layout& L = B.L;                                                      \
+    const Plan& p = B.p;                                                        \
+    const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
+
+__device__ __forceinline__ IgfArgs batch_igf_args(const Plan& p, int hybrid_allowed) {
+    IgfArgs a;
+    a.hx = a.hy = a.hz = 0;
+    a.use_state = 1;
+    a.force = 0;
+    a.hybrid = (hybrid_allowed && !p.exact_igf) ? 1 : 0;
+    return a;
+}
+
+__global__ void __launch_bounds__(256) kb_igf_corners(const BatchBeam* __restrict__ beams,
+                                                      const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_IGF_C)
+    igf_corners_body(reinterpret_cast<double*>(ws + L.igf_ig), p.nx, p.ny, p.nz, batch_igf_args(p, 1), st, vb);
+}
+
+__global__ void __launch_bounds__(256) kb_igf_diff(const BatchBeam* __restrict__ beams,
+                                                   const int* __restrict__ start, int nb) {
+    BATCH_BEAM(BS_IGF_D)
+    igf_diff_body<float>(reinterpret_cast<const double*>(ws + L.igf_ig), reinterpret_cast<float*>(ws + L.igf_k1),
+                         p.nx, p.ny, p.nz, batch_igf_args(p, 1), st, vb);
+}
+
+__global__ void __launch_bounds__(GT) kb_green_z(const BatchBeam* __restrict__ beams, const int* __restrict__ start,
+                                                 int nb) {
+    BATCH_BEAM(BS_GREEN_Z)
+    green_z_body<float>(reinterpret_cast<const float*>(ws + L.igf_k1), reinterpret_cast<float*>(ws + L.green_s1),
+                        p.ny, p.nz, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.green_nc,
+                        batch_igf_args(p, 0), st, vb);
+}
+
+// AXIS 1: S2 along y (S1 -> S2); AXIS 0: S3 along x (S2 -> G)
+template <int AXIS>
+__global__ void __launch_bounds__(GT) kb_green_strided(const BatchBeam* __restrict__ beams,
+                                                       const int* __restrict__ start, int nb) {
+    BATCH_BEAM(AXIS == 1 ? BS_GREEN_Y : BS_GREEN_X)
+    const int Kx = p.Mx / 2 + 1, Ky = p.My / 2 + 1, Kz = p.Mz / 2 + 1;
+    if (AXIS == 1)
+        green_strided_body<float>(reinterpret_cast<const float*>(ws + L.green_s1),
+                                  reinterpret_cast<float*>(ws + L.green_s2), p.ny, Kz, Ky, Kz, p.ny * Kz, Ky * Kz,
+                                  p.ry, reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.green_tky,
+                                  batch_igf_args(p, 0), st, vb);
+    else
+        green_strided_body<float>(reinterpret_cast<const float*>(ws + L.green_s2),
+                                  reinterpret_cast<float*>(ws + L.green), p.nx, Ky * Kz, Kx, Kz, Kz, Kz, p.rx,
+                                  reinterpret_cast<const Cx<float>*>(ws + L.tw_x), B.green_tkx, batch_igf_args(p, 0),
+                                  st, vb);
+}
+#undef BATCH_BEAM
+
+int batch_igf_blocks(const Plan& p, int diff) {
+    const size_t work = diff ? (size_t)p.nx * p.ny * p.nz : (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1);
+    const size_t cap = diff ? 64 : 32;
+    size_t b = (work + 255) / 256;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+void batch_green_tiling(BatchBeam& B, size_t smem[3]) {
+    const Plan& p = B.p;
+    const int Ky = p.My / 2 + 1, Kz = p.Mz / 2 + 1;
+    int NC = 2048 / p.Mz;
+    B.green_nc = NC < 1 ? 1 : (NC > 16 ? 16 : NC);
+    B.green_tky = green_cols<float>(p.My);
+    B.green_tkx = green_cols<float>(p.Mx);
+    B.gx[BS_IGF_C] = batch_igf_blocks(p, 0);
+    B.gy[BS_IGF_C] = 1;
+    B.gx[BS_IGF_D] = batch_igf_blocks(p, 1);
+    B.gy[BS_IGF_D] = 1;
+    B.gx[BS_GREEN_Z] = (p.ny + 2 * B.green_nc - 1) / (2 * B.green_nc);
+    B.gy[BS_GREEN_Z] = p.nx;
+    B.gx[BS_GREEN_Y] = (Kz + 2 * B.green_tky - 1) / (2 * B.green_tky);
+    B.gy[BS_GREEN_Y] = p.nx;
+    B.gx[BS_GREEN_X] = (Kz + 2 * B.green_tkx - 1) / (2 * B.green_tkx);
+    B.gy[BS_GREEN_X] = Ky;
+    smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.green_nc * p.Mz);
+    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.green_tky * (p.My + 1));
+    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.green_tkx * (p.Mx + 1));
+}
+
+cudaError_t prepare_batch_green() {
+    cudaError_t e;
+    const size_t big = 48 * 1024 + 1;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_green_z), big))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_green_strided<1>), big))) return e;
+    return smem_opt_in(reinterpret_cast<const void*>(kb_green_strided<0>), big);
+}
+
+cudaError_t launch_batch_igf(const BatchBeam* beams, const int* start_c, const int* start_d, int nb, int blocks_c,
+                             int blocks_d, cudaStream_t s) {
+    if (nb <= 0) return cudaSuccess;
+    kb_igf_corners<<<blocks_c, 256, 0, s>>>(beams, start_c, nb);
+    kb_igf_diff<<<blocks_d, 256, 0, s>>>(beams, start_d, nb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_green(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
+                               const int blocks[3], const size_t smem[3], cudaStream_t s) {
+    if (nb <= 0) return cudaSuccess;
+    kb_green_z<<<blocks[0], GT, smem[0], s>>>(beams, sz, nb);
+    kb_green_strided<1><<<blocks[1], GT, smem[1], s>>>(beams, sy, nb);
+    kb_green_strided<0><<<blocks[2], GT, smem[2], s>>>(beams, sx, nb);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

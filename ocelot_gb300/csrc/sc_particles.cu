@@ -201,12 +201,12 @@ __device__ __forceinline__ void mom32(float xq, float yq, float d, const KickPar
 // finish reduces all of them in block order (deterministic) and resets the
 // counter for the next launch
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool arrive_last(unsigned int* counter) {
+__device__ __forceinline__ bool arrive_last(unsigned int* counter, int nblk) {
     __shared__ bool last;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+        last = atomicAdd(counter, 1u) == (unsigned)nblk - 1u;
     }
     __syncthreads();
     return last;
@@ -349,17 +349,18 @@ __global__ void __launch_bounds__(PT) k_frame64(const double* __restrict__ rp, K
     block_sum<3>(acc, sm);
     if (threadIdx.x == 0)
         for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = acc[k];
-    if (arrive_last(&st->done_frame)) frame_finalize(part, gridDim.x, kp, st);
+    if (arrive_last(&st->done_frame, gridDim.x)) frame_finalize(part, gridDim.x, kp, st);
 }
 
 // Pair-wise particle loop of the FP32 kernels: with VEC each thread takes two
 // adjacent particles and moves every row with one 16-byte access (rows
 // 16-byte aligned, even row stride); an odd last particle is taken alone.
+// The loop strides over the blocks of the beam (vb), not of the launch.
 #define PAIR_LOOP_BEGIN(n)                                                                        \
     const int64_t npair_ = VEC ? (n) / 2 : (n);                                                   \
     const int64_t ntot_ = npair_ + ((VEC && ((n) & 1)) ? 1 : 0);                                  \
-    for (int64_t p_ = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p_ < ntot_;                 \
-         p_ += (int64_t)gridDim.x * blockDim.x) {                                                 \
+    for (int64_t p_ = vb.x * (int64_t)blockDim.x + threadIdx.x; p_ < ntot_;                       \
+         p_ += (int64_t)vb.nx * blockDim.x) {                                                     \
         const bool pair_ = VEC && p_ < npair_;                                                    \
         const int64_t i0_ = pair_ ? 2 * p_ : (VEC ? (n) - 1 : p_);                                \
         const int W_ = pair_ ? 2 : 1;
@@ -394,10 +395,16 @@ __device__ __forceinline__ void st_rowf(float* __restrict__ row, int64_t i, bool
     else row[i] = a;
 }
 
+// qzero != nullptr (batched kicks): the beam's blocks also clear its
+// fixed-point charge grid of nzero cells for the deposit of this kick
 template <bool VEC>
-__global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
-                                                   double* __restrict__ part, ScState* st) {
+__device__ __forceinline__ void frame32_body(const double* __restrict__ rp, const KickParams& kp,
+                                             double* __restrict__ part, ScState* st,
+                                             unsigned long long* __restrict__ qzero, int64_t nzero, VBlk vb) {
     __shared__ double sm[3 * 32];
+    if (qzero)
+        for (int64_t i = vb.x * (int64_t)blockDim.x + threadIdx.x; i < nzero; i += (int64_t)vb.nx * blockDim.x)
+            qzero[i] = 0ull;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
     const int64_t n = kp.n, ld = kp.ld;
     PAIR_LOOP_BEGIN(n)
@@ -416,20 +423,26 @@ __global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp
     double acc[3] = {a0, a1, a2};
     block_sum<3>(acc, sm);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) part[blockIdx.x * 3 + k] = acc[k];
-    if (arrive_last(&st->done_frame)) frame_finalize(part, gridDim.x, kp, st);
+        for (int k = 0; k < 3; ++k) part[vb.x * 3 + k] = acc[k];
+    if (arrive_last(&st->done_frame, vb.nx)) frame_finalize(part, vb.nx, kp, st);
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
+                                                   double* __restrict__ part, ScState* st) {
+    frame32_body<VEC>(rp, kp, part, st, nullptr, 0, hw_vblk());
 }
 
 // ---------------------------------------------------------------------------
 // extent: rotated positions (z scaled by gamma0), min/max, charge moments
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void extent_block_out(double (&mn)[3], double (&mx)[3], double (&qs)[5],
-                                                 double (&sm)[5 * 32], double* part) {
+                                                 double (&sm)[5 * 32], double* part, int bx) {
     block_minmax<3, false>(mn, sm);
     block_minmax<3, true>(mx, sm);
     block_sum<5>(qs, sm);
     if (threadIdx.x == 0) {
-        double* o = part + blockIdx.x * PART_EXT;
+        double* o = part + bx * PART_EXT;
         for (int k = 0; k < 3; ++k) {
             o[k] = mn[k];
             o[3 + k] = mx[k];
@@ -467,8 +480,8 @@ __global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, 
         qs[3] += qi;
         qs[4] += fabs(qi);
     }
-    extent_block_out(mn, mx, qs, sm, part);
-    if (arrive_last(&st->done_extent)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
+    extent_block_out(mn, mx, qs, sm, part, blockIdx.x);
+    if (arrive_last(&st->done_extent, gridDim.x)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
 }
 
 // order-preserving map of a double onto uint64 (for integer atomics on doubles)
@@ -506,9 +519,9 @@ __device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t 
 // the FP64 extreme of the block is among them, so the mesh step equals the
 // FP64 form's.
 template <bool VEC>
-__global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ rp, const double* __restrict__ q,
-                                                    KickParams kp, float* __restrict__ X, double* __restrict__ part,
-                                                    ScState* st) {
+__device__ __forceinline__ void extent32_body(const double* __restrict__ rp, const double* __restrict__ q,
+                                              const KickParams& kp, float* __restrict__ X, double* __restrict__ part,
+                                              ScState* st, VBlk vb) {
     __shared__ double sm[5 * 32];
     __shared__ float smf[3 * 32];
     __shared__ float bmin[3], bmax[3];
@@ -599,8 +612,8 @@ __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ r
         PAIR_LOOP_END
     }
     __syncthreads();
-    if (threadIdx.x == 0 && SC_IDX_OK(st, 12, blockIdx.x, kp.n > 0 ? gridDim.x : 0)) {
-        double* o = part + blockIdx.x * PART_EXT;
+    if (threadIdx.x == 0 && SC_IDX_OK(st, 12, vb.x, kp.n > 0 ? vb.nx : 0)) {
+        double* o = part + vb.x * PART_EXT;
         for (int k = 0; k < 3; ++k) {
             o[k] = unord64(emin[k]);
             o[3 + k] = unord64(emax[k]);
@@ -609,7 +622,14 @@ __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ r
         o[9] = qs[3];
         o[10] = qs[4];
     }
-    if (arrive_last(&st->done_extent)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
+    if (arrive_last(&st->done_extent, vb.nx)) mesh_finalize(part, vb.nx, kp, st, -1.0);
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ rp, const double* __restrict__ q,
+                                                    KickParams kp, float* __restrict__ X, double* __restrict__ part,
+                                                    ScState* st) {
+    extent32_body<VEC>(rp, q, kp, X, part, st, hw_vblk());
 }
 
 // el_field entry: X given as [n][3] rotated positions; z scaled by gamma in place
@@ -634,8 +654,8 @@ __global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, con
         qs[3] += qi;
         qs[4] += fabs(qi);
     }
-    extent_block_out(mn, mx, qs, sm, part);
-    if (arrive_last(&st->done_extent)) mesh_finalize(part, gridDim.x, kp, st, gamma);
+    extent_block_out(mn, mx, qs, sm, part, blockIdx.x);
+    if (arrive_last(&st->done_extent, gridDim.x)) mesh_finalize(part, gridDim.x, kp, st, gamma);
 }
 
 // potential entry: explicit spacing
@@ -714,9 +734,10 @@ __device__ __forceinline__ long long to_fixed(double q, int S) {
 // associative, so the charge grid does not depend on the order of the
 // atomics: deterministic, the same alone and in a batch.
 template <bool VEC>
-__global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
-                                                  const double* __restrict__ rp, const double* __restrict__ q,
-                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
+__device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __restrict__ keys,
+                                            const double* __restrict__ rp, const double* __restrict__ q,
+                                            unsigned long long* __restrict__ qfix, const KickParams& kp, ScState* st,
+                                            VBlk vb) {
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     float sf[3], of[3], is[3];
@@ -773,6 +794,13 @@ __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_
     for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
     PAIR_LOOP_END
     if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
+                                                  const double* __restrict__ rp, const double* __restrict__ q,
+                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
+    keys32_body<VEC>(X, keys, rp, q, qfix, kp, st, hw_vblk());
 }
 
 // ---------------------------------------------------------------------------
@@ -871,9 +899,10 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
 }
 
 template <bool VEC>
-__global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const float* __restrict__ X,
-                                                  const float4* __restrict__ qx, const float4* __restrict__ qy,
-                                                  const float4* __restrict__ qz, KickParams kp, const ScState* st) {
+__device__ __forceinline__ void kick32_body(double* __restrict__ rp, const float* __restrict__ X,
+                                            const float4* __restrict__ qx, const float4* __restrict__ qy,
+                                            const float4* __restrict__ qz, const KickParams& kp, const ScState* st,
+                                            VBlk vb) {
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     float T[3][3];
@@ -922,6 +951,13 @@ __global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const
     PAIR_LOOP_END
 }
 
+template <bool VEC>
+__global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const float* __restrict__ X,
+                                                  const float4* __restrict__ qx, const float4* __restrict__ qy,
+                                                  const float4* __restrict__ qz, KickParams kp, const ScState* st) {
+    kick32_body<VEC>(rp, X, qx, qy, qz, kp, st, hw_vblk());
+}
+
 template <typename R>
 __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, const R* __restrict__ ex,
                                                    const R* __restrict__ ey, const R* __restrict__ ez,
@@ -945,6 +981,73 @@ __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, cons
 }
 
 // ---------------------------------------------------------------------------
+// batched particle stages: one launch over every beam of a batch
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PT, 4) kb_frame32(const BatchBeam* __restrict__ beams,
+                                                    const int* __restrict__ start, int nb) {
+    const int b = batch_beam(start, nb);
+    const BatchBeam& B = beams[b];
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    ScState* st = reinterpret_cast<ScState*>(B.ws + B.L.state);
+    double* part = reinterpret_cast<double*>(B.ws + B.L.part_frame);
+    unsigned long long* qz = reinterpret_cast<unsigned long long*>(B.ws + B.L.qfix);
+    const int64_t nc = (int64_t)B.p.nx * B.p.ny * B.p.nz;
+    if (B.vec_rp) frame32_body<true>(B.rp, B.kp, part, st, qz, nc, vb);
+    else frame32_body<false>(B.rp, B.kp, part, st, qz, nc, vb);
+}
+
+__global__ void __launch_bounds__(PT, 4) kb_extent32(const BatchBeam* __restrict__ beams,
+                                                     const int* __restrict__ start, int nb) {
+    const int b = batch_beam(start, nb);
+    const BatchBeam& B = beams[b];
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    ScState* st = reinterpret_cast<ScState*>(B.ws + B.L.state);
+    float* X = reinterpret_cast<float*>(B.ws + B.L.X);
+    double* part = reinterpret_cast<double*>(B.ws + B.L.part_ext);
+    if (B.vec_rpq) extent32_body<true>(B.rp, B.q, B.kp, X, part, st, vb);
+    else extent32_body<false>(B.rp, B.q, B.kp, X, part, st, vb);
+}
+
+__global__ void __launch_bounds__(PT, 4) kb_keys32(const BatchBeam* __restrict__ beams,
+                                                   const int* __restrict__ start, int nb) {
+    const int b = batch_beam(start, nb);
+    const BatchBeam& B = beams[b];
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    ScState* st = reinterpret_cast<ScState*>(B.ws + B.L.state);
+    float* X = reinterpret_cast<float*>(B.ws + B.L.X);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(B.ws + B.L.keys);
+    unsigned long long* qfix = reinterpret_cast<unsigned long long*>(B.ws + B.L.qfix);
+    if (B.vec_rpq) keys32_body<true>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
+    else keys32_body<false>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
+}
+
+__global__ void __launch_bounds__(PT, 4) kb_kick32(const BatchBeam* __restrict__ beams,
+                                                   const int* __restrict__ start, int nb) {
+    const int b = batch_beam(start, nb);
+    const BatchBeam& B = beams[b];
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    const ScState* st = reinterpret_cast<const ScState*>(B.ws + B.L.state);
+    const float* X = reinterpret_cast<const float*>(B.ws + B.L.X);
+    const float4* qx = reinterpret_cast<const float4*>(B.ws + B.L.exq);
+    const float4* qy = reinterpret_cast<const float4*>(B.ws + B.L.eyq);
+    const float4* qz = reinterpret_cast<const float4*>(B.ws + B.L.ezq);
+    if (B.vec_rp) kick32_body<true>(B.rp, X, qx, qy, qz, B.kp, st, vb);
+    else kick32_body<false>(B.rp, X, qx, qy, qz, B.kp, st, vb);
+}
+
+cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, const int* start, int nb, int blocks,
+                                   cudaStream_t s) {
+    if (blocks <= 0) return cudaSuccess;
+    switch (k) {
+        case BP_FRAME: kb_frame32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
+        case BP_EXTENT: kb_extent32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
+        case BP_KEYS: kb_keys32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
+        case BP_KICK: kb_kick32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 // 16-byte row accesses need 16-byte aligned rows and an even row stride
@@ -957,6 +1060,8 @@ static int particle_blocks(const Plan& p, int64_t n) {
     if (b > p.part_blocks) b = p.part_blocks;
     return (int)(b > 0 ? b : 1);
 }
+
+int batch_particle_blocks(const Plan& p, int64_t n) { return particle_blocks(p, n); }
 
 cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickParams& kp, const double* rp,
                          cudaStream_t s) {
