@@ -282,7 +282,7 @@ def time_batched(steps, warmup, dev):
     for it in range(warmup + steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for (eng, rp, q, E, dz) in batch.beams:
+        for (eng, rp, q, E, dz, _) in batch.beams:
             eng.kick(rp, q, int(rp.shape[1]), E, dz)
         b.record(stream)
         b.synchronize()
@@ -306,6 +306,53 @@ def time_batched(steps, warmup, dev):
         "hbm": {"algorithmic_bytes_per_step": alg, "achieved_gbs": alg / (t * 1e-3) / 1e9},
         "l2": "not flushed: the 96 beams' particles (several GB) exceed L2",
     }
+
+
+# serving workload: Poisson-arriving tracking jobs, each a seeded Gaussian beam
+# (sigma_x = sigma_y = 200 um, sigma_x' = sigma_y' = 2e-5, sigma_tau = 100 um,
+# sigma_delta = 1e-4, 130 MeV, 250 pC) with N log-uniform in [5e4, 5e6] on a
+# mesh of 32^3, 48^3, 64^3 or 96^3, tracked through 10 FODO cells with a kick
+# every 0.25 m (96 kicks) and first-order transport between kicks
+SERVE_MESHES = [(32, 32, 32), (48, 48, 48), (64, 64, 64), (96, 96, 96)]
+SERVE_RATES = [4.0, 12.0, 24.0, 36.0, 48.0]
+SERVE_JOBS = 30
+
+
+def serve_requests(count, seed):
+    import numpy as np
+    from ocelot_gb300 import serve as S
+    rng = np.random.default_rng(seed)
+    lattice = S.fodo(10)
+    out = []
+    for i in range(count):
+        n = int(round(10 ** rng.uniform(math.log10(5e4), math.log10(5e6))))
+        mesh = SERVE_MESHES[int(rng.integers(len(SERVE_MESHES)))]
+        out.append(S.Request(S.BeamSpec(n=n, seed=seed * 1000 + i), lattice, mesh, 0.25, 1))
+    return out
+
+
+def time_serving(dev, rates=SERVE_RATES, jobs=SERVE_JOBS):
+    import numpy as np
+    from ocelot_gb300 import serve as S
+    srv = S.Server(dev, max_active=64)
+    S.poisson_run(srv, serve_requests(4, SEED + 50), rate_hz=100.0, seed=0)   # warm-up
+    results = []
+    for k, rate in enumerate(rates):
+        reqs = serve_requests(jobs, SEED + 60 + k)
+        ticks0 = srv.ticks
+        lat, wall, kicks, _ = S.poisson_run(srv, reqs, rate_hz=rate, seed=k + 1)
+        results.append({"rate_hz": rate, "jobs": len(reqs), "p50_s": float(np.percentile(lat, 50)),
+                        "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+                        "max_s": float(lat.max()), "throughput": kicks / wall, "unit": "particle-kicks/s",
+                        "wall_s": wall, "ticks": srv.ticks - ticks0,
+                        "offered_particle_kicks_per_s": rate * float(np.mean([r.beam.n for r in reqs])) * 96})
+    sustained = [r for r in results if r["throughput"] >= 0.9 * r["offered_particle_kicks_per_s"]]
+    return {"workload": "Poisson-arriving FODO tracking jobs (10 cells, kick every 0.25 m = 96 kicks, first-order "
+                        "transport between kicks), N log-uniform 5e4-5e6, mesh 32^3/48^3/64^3/96^3, FP32 form; "
+                        "latency = arrival to tracked particles in pinned host memory",
+            "rates": results, "peak_hbm_bytes": srv.peak_used,
+            "sustained_rate_hz": max((r["rate_hz"] for r in sustained), default=None),
+            "p99_at_sustained_s": (max(sustained, key=lambda r: r["rate_hz"])["p99_s"] if sustained else None)}
 
 
 def dist_env():
@@ -356,6 +403,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip timing the FP64 form")
     ap.add_argument("--no-batch", action="store_true", help="skip the 96-beam batched leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -386,6 +434,7 @@ def main():
     kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
     e2e_dt, h2d, d2h = time_e2e("fp32", n, args.steps, args.warmup, dev)
     batched = None if args.no_batch else time_batched(args.steps, args.warmup, dev)
+    serving = None if args.no_serve else time_serving(dev)
     kick_err = fp32_kick_error(n, dev)
     barrier()
 
@@ -438,6 +487,7 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches32,
             "batched": batched,
+            "serving": serving,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }

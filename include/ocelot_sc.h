@@ -73,13 +73,19 @@ int sc_read_status(const sc_plan* plan, void* ws, void* stream);
  * inspection: the NGP charge grid of el_field (sc.py:193), the potential
  * (sc.py:168), the field grids Ex/Ey/Ez (sc.py:195-200), all [nx][ny][nz];
  * the cell keys (sc.py:192) as uint32[n].  Grids are double for an SC_FP64
- * plan and float for SC_FP32.  Offsets do not depend on n except for keys. */
+ * plan and float for SC_FP32.  Offsets do not depend on n except for keys.
+ * SC_REGION_STATUS is the int that sc_read_status returns (the last kick's
+ * status) and SC_REGION_FIRST_ERROR an int holding the first non-OK status of
+ * any earlier kick since sc_workspace_init: a device-resident loop of many
+ * kicks copies the two asynchronously instead of synchronising per kick. */
 #define SC_REGION_QGRID 0
 #define SC_REGION_PHI 1
 #define SC_REGION_EX 2
 #define SC_REGION_EY 3
 #define SC_REGION_EZ 4
 #define SC_REGION_KEYS 5
+#define SC_REGION_STATUS 6
+#define SC_REGION_FIRST_ERROR 7
 int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t* offset, int64_t* bytes);
 
 /* ---- the kick ---------------------------------------------------------- */
@@ -113,7 +119,7 @@ int sc_kick(sc_plan* plan, void* ws, size_t ws_bytes, double* rparticles, int64_
  * Requirements: every plan is SC_FP32 without SC_FP32_SORTED_DEPOSIT (the
  * exact fixed-point deposit), each beam has its own plan and initialised
  * workspace, and no two beams share a workspace or particles.  Beams with
- * zstep == 0 are left out (sc.py:210-212). */
+ * zstep == 0 are left out (sc.py:210-212), their transport map included. */
 typedef struct sc_batch sc_batch;
 typedef struct sc_beam {
     sc_plan* plan;
@@ -127,6 +133,7 @@ typedef struct sc_beam {
     double zstep;
     double mesh_scale;      /* NAN unless random_mesh */
     double mesh_shift;
+    const double* tmap;     /* host float64[42]: R (row-major) then B, for sc_tmap_batched; or NULL */
 } sc_beam;
 
 /* A batch of up to max_beams beams.  Allocates its work table (device and
@@ -144,6 +151,11 @@ int sc_batch_set(sc_batch* batch, const sc_beam* beams, int nbeams, void* stream
 int sc_kick_batched(sc_batch* batch, void* stream);
 /* Kernels launched by the last sc_kick_batched (0 before the first). */
 int sc_batch_launches(const sc_batch* batch);
+/* rparticles <- R . rparticles + B for every beam of the table that was set
+ * with a map (sc_beam.tmap), in one launch: the transport before the kick of
+ * a tracking step (TransferMap.mul_p_array, transfer_map.py:40-50), with the
+ * arithmetic of sc_tmap_apply.  Capturable like sc_kick_batched. */
+int sc_tmap_batched(sc_batch* batch, void* stream);
 
 /* ---- stages, mirroring SpaceCharge's public methods ------------------- */
 

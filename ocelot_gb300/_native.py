@@ -27,7 +27,12 @@ SC_ERR_UNSUPPORTED = 6
 
 SC_NSTAGES = 11
 
-REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5}
+REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7}
+
+ERROR_TEXT = {
+    SC_ERR_DEGENERATE: "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)",
+    SC_ERR_NONFINITE: "non-finite particle coordinates or momenta (or a particle outside the mesh)",
+}
 
 vp = C.c_void_p
 i64 = C.c_int64
@@ -36,7 +41,8 @@ dbl = C.c_double
 class ScBeam(C.Structure):
     """struct sc_beam of include/ocelot_sc.h."""
     _fields_ = [("plan", vp), ("ws", vp), ("ws_bytes", C.c_size_t), ("rparticles", vp), ("ld", i64), ("q", vp),
-                ("n", i64), ("energy_gev", dbl), ("zstep", dbl), ("mesh_scale", dbl), ("mesh_shift", dbl)]
+                ("n", i64), ("energy_gev", dbl), ("zstep", dbl), ("mesh_scale", dbl), ("mesh_shift", dbl),
+                ("tmap", C.POINTER(dbl))]
 
 
 # name -> (restype, argtypes); the same list as include/ocelot_sc.h
@@ -62,6 +68,7 @@ SIGNATURES = {
     "sc_batch_set": (C.c_int, [vp, C.POINTER(ScBeam), C.c_int, vp]),
     "sc_kick_batched": (C.c_int, [vp, vp]),
     "sc_batch_launches": (C.c_int, [vp]),
+    "sc_tmap_batched": (C.c_int, [vp, vp]),
     "sc_profile_enable": (C.c_int, [vp, C.c_int]),
     "sc_profile_read": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     "sc_profile_stage_name": (C.c_char_p, [C.c_int]),

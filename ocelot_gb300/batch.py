@@ -44,8 +44,9 @@ class BeamBatch:
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_batch_create(C.byref(h), self.max_beams))
         self.handle = h
-        self.beams = []      # (engine, rp, q, E, zstep)
+        self.beams = []      # (engine, rp, q, E, zstep, tmap or None)
         self._table = None
+        self._maps = None
 
     def __del__(self):
         try:
@@ -57,10 +58,12 @@ class BeamBatch:
     def __len__(self):
         return len(self.beams)
 
-    def add(self, rparticles, q_array, energy_gev: float, nmesh_xyz, zstep: float, engine: Engine | None = None):
+    def add(self, rparticles, q_array, energy_gev: float, nmesh_xyz, zstep: float, engine: Engine | None = None,
+            tmap=None):
         """Register a beam; returns its index.  A new plan and workspace are
         made for it unless ``engine`` (an FP32 Engine of the same mesh, not
-        used by another beam) is given."""
+        used by another beam) is given.  ``tmap`` = (R [6x6], B [6]): the
+        transport ``transport()`` applies before the kick, or None."""
         if len(self.beams) >= self.max_beams:
             raise ValueError(f"batch is full ({self.max_beams} beams)")
         if rparticles.dim() != 2 or rparticles.shape[0] != 6 or rparticles.stride(1) != 1:
@@ -71,26 +74,40 @@ class BeamBatch:
         if engine is None:
             engine = Engine(tuple(int(v) for v in nmesh_xyz), "fp32", self.device, self.mode)
         engine.ensure(n)
-        self.beams.append((engine, rparticles, q_array, float(energy_gev), float(zstep)))
+        self.beams.append((engine, rparticles, q_array, float(energy_gev), float(zstep), tmap))
         self._table = None
         return len(self.beams) - 1
 
-    def set_zstep(self, index: int, zstep: float):
-        e, rp, q, E, _ = self.beams[index]
-        self.beams[index] = (e, rp, q, E, float(zstep))
+    def set_step(self, index: int, zstep: float, tmap=None):
+        """Kick length and transport map of beam ``index`` for the next step."""
+        e, rp, q, E, _, _ = self.beams[index]
+        self.beams[index] = (e, rp, q, E, float(zstep), tmap)
+        self._table = None
+
+    def clear(self):
+        """Forget every beam (their engines are not touched)."""
+        self.beams = []
         self._table = None
 
     def commit(self):
         """Upload the work table (asynchronous copy on the current stream)."""
         import torch
+        import numpy as np
         arr = (N.ScBeam * max(1, len(self.beams)))()
-        for i, (e, rp, q, E, dz) in enumerate(self.beams):
+        maps = []
+        for i, (e, rp, q, E, dz, tm) in enumerate(self.beams):
+            mp = None
+            if tm is not None:
+                m = np.ascontiguousarray(np.concatenate([np.asarray(tm[0], dtype=np.float64).reshape(36),
+                                                         np.asarray(tm[1], dtype=np.float64).reshape(6)]))
+                maps.append(m)
+                mp = m.ctypes.data_as(C.POINTER(C.c_double))
             arr[i] = N.ScBeam(e.plan.value, e.ws.data_ptr(), e.ws.numel(), rp.data_ptr(), rp.stride(0),
-                              q.data_ptr(), int(rp.shape[1]), E, dz, math.nan, math.nan)
+                              q.data_ptr(), int(rp.shape[1]), E, dz, math.nan, math.nan, mp)
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_batch_set(self.handle, arr, len(self.beams),
                                           C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
-        self._table = arr   # the host structs stay alive with the batch
+        self._table, self._maps = arr, maps   # copied by sc_batch_set; kept for inspection
 
     def kick(self):
         """Kick every beam once (asynchronous on the current stream)."""
@@ -99,6 +116,15 @@ class BeamBatch:
             self.commit()
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_kick_batched(self.handle,
+                                             C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
+
+    def transport(self):
+        """Apply every beam's transport map (one launch, current stream)."""
+        import torch
+        if self._table is None:
+            self.commit()
+        with torch.cuda.device(self.device):
+            N.check(self.lib.sc_tmap_batched(self.handle,
                                              C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
 
     @property

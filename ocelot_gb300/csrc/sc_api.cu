@@ -388,6 +388,14 @@ int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t*
         case SC_REGION_EY: *offset = (int64_t)L.ey; *bytes = (int64_t)(rs * ncell); break;
         case SC_REGION_EZ: *offset = (int64_t)L.ez; *bytes = (int64_t)(rs * ncell); break;
         case SC_REGION_KEYS: *offset = (int64_t)L.keys; *bytes = (int64_t)(4 * (size_t)n_max); break;
+        case SC_REGION_STATUS:
+            *offset = (int64_t)(L.state + offsetof(ScState, status));
+            *bytes = (int64_t)sizeof(int);
+            break;
+        case SC_REGION_FIRST_ERROR:
+            *offset = (int64_t)(L.state + offsetof(ScState, first_error));
+            *bytes = (int64_t)sizeof(int);
+            break;
         default: return fail(SC_ERR_ARG, "unknown region %d", region);
     }
     return SC_OK;
@@ -705,6 +713,10 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
         }
         B.gx[BS_PART] = batch_particle_blocks(p, m.n);
         B.gy[BS_PART] = 1;
+        if (m.tmap) {
+            B.has_tm = 1;
+            for (int k = 0; k < 42; ++k) B.tm[k] = m.tmap[k];
+        }
         ++nb;
     }
     for (int st = 0; st < BS_COUNT; ++st) {
@@ -765,6 +777,17 @@ int sc_kick_batched(sc_batch* b, void* stream) {
 }
 
 int sc_batch_launches(const sc_batch* b) { return b ? b->last_launches : 0; }
+
+int sc_tmap_batched(sc_batch* b, void* stream) {
+    if (!b) return fail(SC_ERR_ARG, "batch is NULL");
+    if (b->nb == 0) return SC_OK;
+    const BatchBeam* beams = reinterpret_cast<const BatchBeam*>(b->d_buf);
+    const int* start = reinterpret_cast<const int*>(b->d_buf + b->beams_bytes);
+    SC_CUDA(launch_batch_tmap(beams, start + BS_PART * (b->max_beams + 1), b->nb, b->blocks[BS_PART],
+                              (cudaStream_t)stream),
+            "batched transfer map");
+    return SC_OK;
+}
 
 int sc_tmap_apply_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld, int64_t n,
                           void* stream) {

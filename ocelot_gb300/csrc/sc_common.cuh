@@ -69,7 +69,8 @@ struct ScState {
     unsigned int done_frame;     // blocks finished, for the last-block reductions
     unsigned int done_extent;
     int check_code;              // checked builds: first failed index check (kernel code)
-    long long check_index;       // ... and the offending index
+    int first_error;             // first non-OK status of any kick since sc_workspace_init
+    long long check_index;       // ... and the offending index (checked builds)
 };
 constexpr int WS_MAGIC = 0x5c6b0e11;
 
@@ -228,6 +229,8 @@ struct BatchBeam {
     Layout L;
     Plan p;
     int vec_rp, vec_rpq;              // 16-byte row accesses allowed: rparticles / rparticles and q
+    int has_tm;                       // a transport map to apply before the kick (sc_tmap_batched)
+    double tm[42];                    // R (row-major), then B
     int fft_nc, fft_tky, fft_tkx;     // convolution tiling
     int green_nc, green_tky, green_tkx;
     int gx[BS_COUNT], gy[BS_COUNT];   // this beam's grid per stage
@@ -260,6 +263,7 @@ cudaError_t launch_batch_green(const BatchBeam* beams, const int* sz, const int*
 cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
                                   const int blocks[3], const size_t smem[3], cudaStream_t s);
 cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
+cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
 // host-side tiling of one beam (sets the tiling fields and grids of B)
 void batch_fft_tiling(BatchBeam& B, size_t smem[3]);
 void batch_green_tiling(BatchBeam& B, size_t smem[3]);

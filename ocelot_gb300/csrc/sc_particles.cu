@@ -222,6 +222,8 @@ __device__ void frame_finalize(const double* part, int nblk, const KickParams& k
     block_sum<3>(acc, sm);
     if (threadIdx.x != 0) return;
     st->done_frame = 0;
+    // the previous kick's outcome, kept before this kick resets the status
+    if (st->status != SC_OK && st->first_error == SC_OK) st->first_error = st->status;
     const double nn = (double)kp.n;
     double t3[3] = {__ddiv_rn(acc[0], nn), __ddiv_rn(acc[1], nn), __ddiv_rn(acc[2], nn)};
     const double Pav = __dsqrt_rn(__fma_rn(t3[2], t3[2], __fma_rn(t3[1], t3[1], __dmul_rn(t3[0], t3[0]))));

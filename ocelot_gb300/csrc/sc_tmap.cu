@@ -10,23 +10,48 @@
 namespace ocsc {
 
 struct Map6 {
-    double R[36];
-    double B[6];
+    double m[42];  // R (row-major), then B
 };
 
-__global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, int64_t ld, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double x[6];
+// one particle: x <- R.x + B with m = R (row-major) then B
+__device__ __forceinline__ void tmap_one(const double* __restrict__ m, double* __restrict__ rp, int64_t ld,
+                                         int64_t i) {
+    double x[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
+    for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
 #pragma unroll
-        for (int r = 0; r < 6; ++r) {
-            double acc = __dmul_rn(m.R[r * 6], x[0]);
+    for (int r = 0; r < 6; ++r) {
+        double acc = __dmul_rn(m[r * 6], x[0]);
 #pragma unroll
-            for (int k = 1; k < 6; ++k) acc = __fma_rn(m.R[r * 6 + k], x[k], acc);
-            rp[r * ld + i] = __dadd_rn(acc, m.B[r]);
-        }
+        for (int k = 1; k < 6; ++k) acc = __fma_rn(m[r * 6 + k], x[k], acc);
+        rp[r * ld + i] = __dadd_rn(acc, m[36 + r]);
     }
+}
+
+__global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, int64_t ld, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        tmap_one(m.m, rp, ld, i);
+}
+
+// batched: each beam's own map from the work table, over the beam's blocks
+__global__ void __launch_bounds__(256) kb_tmap(const BatchBeam* __restrict__ beams, const int* __restrict__ start,
+                                               int nb) {
+    __shared__ double m[42];
+    const int b = batch_beam(start, nb);
+    const BatchBeam& B = beams[b];
+    if (!B.has_tm) return;
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    if (threadIdx.x < 42) m[threadIdx.x] = B.tm[threadIdx.x];
+    __syncthreads();
+    const int64_t n = B.kp.n, ld = B.kp.ld;
+    for (int64_t i = vb.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)vb.nx * blockDim.x)
+        tmap_one(m, B.rp, ld, i);
+}
+
+cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s) {
+    if (nb <= 0 || blocks <= 0) return cudaSuccess;
+    kb_tmap<<<blocks, 256, 0, s>>>(beams, start, nb);
+    return cudaGetLastError();
 }
 
 // Map i = *counter of a device table of maps (row-major R[36] then B[6] per
@@ -40,18 +65,8 @@ __global__ void __launch_bounds__(256) k_tmap_indexed(const double* __restrict__
     if (idx < 0 || idx >= nmaps) return;
     if (threadIdx.x < 42) m[threadIdx.x] = table[(size_t)idx * 42 + threadIdx.x];
     __syncthreads();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double x[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
-#pragma unroll
-        for (int r = 0; r < 6; ++r) {
-            double acc = __dmul_rn(m[r * 6], x[0]);
-#pragma unroll
-            for (int k = 1; k < 6; ++k) acc = __fma_rn(m[r * 6 + k], x[k], acc);
-            rp[r * ld + i] = __dadd_rn(acc, m[36 + r]);
-        }
-    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        tmap_one(m, rp, ld, i);
 }
 
 __global__ void k_advance(int* counter, int delta) { *counter += delta; }
@@ -76,8 +91,8 @@ cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, do
 cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     Map6 m;
-    for (int i = 0; i < 36; ++i) m.R[i] = R[i];
-    for (int i = 0; i < 6; ++i) m.B[i] = B[i];
+    for (int i = 0; i < 36; ++i) m.m[i] = R[i];
+    for (int i = 0; i < 6; ++i) m.m[36 + i] = B[i];
     int dev = 0, sm = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);

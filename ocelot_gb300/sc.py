@@ -132,12 +132,13 @@ class Engine:
 
     def region(self, name: str):
         """A view of an intermediate of the last call (charge grid, potential,
-        field grids [nx][ny][nz]; keys [n])."""
+        field grids [nx][ny][nz]; keys [n]; the status ints "status" and
+        "first_error", one element each)."""
         torch = _torch()
         off, nb = C.c_int64(), C.c_int64()
         N.check(self.lib.sc_workspace_region(self.plan, max(self.cap, 0), N.REGIONS[name], C.byref(off), C.byref(nb)))
         raw = self.ws[off.value:off.value + nb.value]
-        if name == "keys":
+        if name in ("keys", "status", "first_error"):
             return raw.view(torch.int32)
         dt = torch.float64 if self.precision == "fp64" else torch.float32
         return raw.view(dt).view(self.shape)

@@ -322,11 +322,14 @@ class DeviceTrack:
         return self
 
     def synchronize(self):
-        """Wait for the job and raise if a kick latched an error."""
+        """Wait for the job and raise if any of its kicks latched an error."""
         import torch
         self.stream.synchronize()
         with torch.cuda.device(self.dev), torch.cuda.stream(self.stream):
             self.engine.check_status()
+            first = int(self.engine.region("first_error").item())
+        if first:
+            raise ValueError(f"[sc error {first}] {N.ERROR_TEXT.get(first, 'device error')} (in an earlier step)")
 
     def result(self, p_array=None):
         self.synchronize()
