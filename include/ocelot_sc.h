@@ -44,6 +44,7 @@ extern "C" {
 #define SC_ERR_DEGENERATE 4  /* zero or non-finite beam extent / charge (device) */
 #define SC_ERR_NONFINITE 5   /* non-finite particle coordinate or momentum (device) */
 #define SC_ERR_UNSUPPORTED 6 /* grid too large for the FFT plan */
+#define SC_ERR_TIMEOUT 7     /* a device-side wait gave up after its iteration limit */
 
 typedef struct sc_plan sc_plan; /* opaque, host-side only */
 

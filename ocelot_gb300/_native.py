@@ -24,6 +24,7 @@ SC_ERR_WORKSPACE = 3
 SC_ERR_DEGENERATE = 4
 SC_ERR_NONFINITE = 5
 SC_ERR_UNSUPPORTED = 6
+SC_ERR_TIMEOUT = 7
 
 SC_NSTAGES = 11
 
@@ -32,6 +33,7 @@ REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status":
 ERROR_TEXT = {
     SC_ERR_DEGENERATE: "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)",
     SC_ERR_NONFINITE: "non-finite particle coordinates or momenta (or a particle outside the mesh)",
+    SC_ERR_TIMEOUT: "a device-side wait for a bulk copy gave up after its iteration limit",
 }
 
 vp = C.c_void_p

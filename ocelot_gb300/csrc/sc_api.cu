@@ -30,9 +30,13 @@ cudaError_t smem_opt_in(const void* kernel, size_t bytes) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e) return e;
     if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev))) return e;
-    if (bytes > (size_t)optin) return cudaErrorInvalidValue;
-    if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
-    opted[kernel] = (size_t)optin;
+    // the dynamic limit is what the kernel's static shared memory leaves
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, kernel))) return e;
+    const size_t room = (size_t)optin > fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+    if (bytes > room) return cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room))) return e;
+    opted[kernel] = room;
     return cudaSuccess;
 }
 
@@ -97,9 +101,9 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.ex = take(rs * ncell);
     L.ey = take(rs * ncell);
     L.ez = take(rs * ncell);
-    L.exq = take(p.prec == SC_FP32 ? 16 * ncell : 0);
-    L.eyq = take(p.prec == SC_FP32 ? 16 * ncell : 0);
-    L.ezq = take(p.prec == SC_FP32 ? 16 * ncell : 0);
+    L.exq = take(p.prec == SC_FP32 ? 32 * ncell : 0);
+    L.eyq = take(p.prec == SC_FP32 ? 32 * ncell : 0);
+    L.ezq = take(p.prec == SC_FP32 ? 32 * ncell : 0);
     L.cell_start = take(4 * ncell);
     L.cell_end = take(4 * ncell);
     L.qfix = take(8 * ncell);
@@ -166,7 +170,7 @@ using namespace ocsc;
 // events: main stream 0..9 (before frame, after frame, extent, keys, sort,
 // deposit, join, convolve, field, kick); side stream 10..12 (start, after
 // igf, after green)
-constexpr int NEV = 13;
+constexpr int NEV = 14;
 
 struct sc_plan {
     Plan p;
@@ -302,6 +306,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     // can be recorded in a CUDA graph
     SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
     SC_CUDA(prepare_green_kernels(p), "kernel attributes");
+    SC_CUDA(prepare_particle_kernels(), "kernel attributes");
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     SC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -351,10 +356,15 @@ int sc_profile_read(sc_plan* plan, float* ms, int* n_launches) {
     if (!plan || !ms) return fail(SC_ERR_ARG, "bad arguments");
     if (!plan->profiling) return fail(SC_ERR_ARG, "profiling is not enabled");
     SC_CUDA(cudaEventSynchronize(plan->ev[9]), "cudaEventSynchronize");
-    // main-stream stages, then the two side-stream stages
-    static const int a[SC_NSTAGES] = {0, 1, 2, 3, 4, 10, 11, 5, 6, 7, 8};
+    // main-stream stages, then the two side-stream stages; the convolution is
+    // its forward passes (5 -> 13, before the join) plus the rest (6 -> 7),
+    // the join wait is 13 -> 6
+    static const int a[SC_NSTAGES] = {0, 1, 2, 3, 4, 10, 11, 13, 6, 7, 8};
     static const int b[SC_NSTAGES] = {1, 2, 3, 4, 5, 11, 12, 6, 7, 8, 9};
     for (int i = 0; i < SC_NSTAGES; ++i) SC_CUDA(cudaEventElapsedTime(&ms[i], plan->ev[a[i]], plan->ev[b[i]]), "cudaEventElapsedTime");
+    float fwd = 0.f;
+    SC_CUDA(cudaEventElapsedTime(&fwd, plan->ev[5], plan->ev[13]), "cudaEventElapsedTime");
+    ms[8] += fwd;
     if (n_launches) *n_launches = plan->last_launches;
     return SC_OK;
 }
@@ -425,6 +435,8 @@ int sc_read_status(const sc_plan* plan, void* ws, void* stream) {
         return fail(status, "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)");
     if (status == SC_ERR_NONFINITE)
         return fail(status, "non-finite particle coordinates or momenta (or a particle outside the mesh)");
+    if (status == SC_ERR_TIMEOUT)
+        return fail(status, "a device-side wait for a bulk copy gave up after its iteration limit");
     if (status) return fail(status, "device status %d", status);
     return SC_OK;
 }
@@ -480,11 +492,14 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
         mark(plan, 4, s);
     }
     mark(plan, 5, s);
+    // the z and y forward passes need only the charge grid: they run before
+    // the join, beside the Green's-function build
+    const long long* qfix = p.sorted_deposit ? nullptr : reinterpret_cast<const long long*>(ws + L.qfix);
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s, qfix, CONV_FORWARD), "convolve");
+    mark(plan, 13, s);
     SC_CUDA(cudaStreamWaitEvent(s, plan->join, 0), "cudaStreamWaitEvent");  // join
     mark(plan, 6, s);
-    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s,
-                            p.sorted_deposit ? nullptr : reinterpret_cast<const long long*>(ws + L.qfix)),
-            "convolve");
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s, qfix, CONV_REST), "convolve");
     mark(plan, 7, s);
     SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
     mark(plan, 8, s);
@@ -622,6 +637,7 @@ int sc_batch_create(sc_batch** out, int max_beams) {
     if (max_beams < 1 || max_beams > (1 << 20)) return fail(SC_ERR_ARG, "max_beams=%d out of range", max_beams);
     SC_CUDA(prepare_batch_fft(), "kernel attributes");
     SC_CUDA(prepare_batch_green(), "kernel attributes");
+    SC_CUDA(prepare_particle_kernels(), "kernel attributes");
     sc_batch* b = new (std::nothrow) sc_batch;
     if (!b) return fail(SC_ERR_ARG, "out of host memory");
     memset(b, 0, sizeof *b);
@@ -765,9 +781,13 @@ int sc_kick_batched(sc_batch* b, void* stream) {
             "batched green spectrum");
     SC_CUDA(cudaEventRecord(b->join, b->side), "cudaEventRecord");
     SC_CUDA(launch_batch_particles(BP_KEYS, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched keys");
-    SC_CUDA(cudaStreamWaitEvent(s, b->join, 0), "cudaStreamWaitEvent");
     const int fb[3] = {b->blocks[BS_FFT_Z], b->blocks[BS_FFT_Y], b->blocks[BS_FFT_X]};
-    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), nb, fb, b->fft_smem, s),
+    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), nb, fb, b->fft_smem, s,
+                                  CONV_FORWARD),
+            "batched convolve");
+    SC_CUDA(cudaStreamWaitEvent(s, b->join, 0), "cudaStreamWaitEvent");
+    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), nb, fb, b->fft_smem, s,
+                                  CONV_REST),
             "batched convolve");
     SC_CUDA(launch_batch_field(beams, row(BS_FIELD), nb, b->blocks[BS_FIELD], s), "batched field");
     SC_CUDA(launch_batch_particles(BP_KICK, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched kick");

@@ -68,11 +68,29 @@ struct ScState {
     int igf_box[3];
     unsigned int done_frame;     // blocks finished, for the last-block reductions
     unsigned int done_extent;
+    int frame_timeout;           // a frame block's bulk-copy wait gave up (the finalize reports it)
     int check_code;              // checked builds: first failed index check (kernel code)
     int first_error;             // first non-OK status of any kick since sc_workspace_init
     long long check_index;       // ... and the offending index (checked builds)
 };
+static_assert(sizeof(ScState) <= 512, "the state must fit the 512 bytes the static IGF scratch reserves");
 constexpr int WS_MAGIC = 0x5c6b0e11;
+
+// Near box of the hybrid Green's function: along each axis the cells with
+// index below ceil(5 hmax / h) + 1.  Every cell outside it is at least
+// 5 hmax from the origin, where the 4th-order multipole form of the cell
+// integral is within 5e-8 of the exact integral (checked against an
+// extended-precision IGF).  Written into the state once per kick by the
+// kernel that sets the mesh step.
+__device__ __forceinline__ void igf_box_of(const double (&h)[3], int nx, int ny, int nz, int (&b)[3]) {
+    const double hm = fmax(h[0], fmax(h[1], h[2]));
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+        const double v = 5.0 * hm / h[a];
+        b[a] = v >= (double)n[a] ? n[a] : (int)ceil(v) + 1;
+        if (b[a] > n[a]) b[a] = n[a];
+    }
+}
 
 // host-computed scalars of one kick
 struct KickParams {
@@ -111,7 +129,7 @@ struct Layout {
     size_t X;                                    // 3 x n grid coordinates (R)
     size_t keys, sort_keys, sort_perm, sort_q, sort_tmp_k, sort_tmp_v, sort_hist, sort_tot;
     size_t qgrid, phi, ex, ey, ez;               // [nx][ny][nz] (R)
-    size_t exq, eyq, ezq;                        // FP32 form: [nx][ny][nz] float4 gather quads
+    size_t exq, eyq, ezq;                        // FP32 form: [nx][ny][nz] gather octs (8 floats, 32-byte aligned)
     size_t cell_start, cell_end;                 // [nx*ny*nz] uint32 run bounds (adjacent)
     size_t qfix;                                 // [nx*ny*nz] int64 fixed-point charge (FP32 form)
     size_t igf_ig;                               // (nx+1)(ny+1)(nz+1) double
@@ -180,8 +198,11 @@ cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cuda
 // convolution + field grids (sc_fft.cu)
 // qfix: the fixed-point charge grid of the FP32 form's exact deposit (then
 // qgrid_in receives the scaled grid), or nullptr
+// part: CONV_ALL, or CONV_FORWARD (z and y forward passes: they need only the
+// charge grid) and then CONV_REST (the passes that need the Green spectrum)
+enum ConvPart { CONV_ALL = 0, CONV_FORWARD = 1, CONV_REST = 2 };
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in,
-                            void* phi_out, cudaStream_t s, const long long* qfix = nullptr);
+                            void* phi_out, cudaStream_t s, const long long* qfix = nullptr, int part = CONV_ALL);
 cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
 
 // first-order map (sc_tmap.cu)
@@ -261,7 +282,7 @@ cudaError_t launch_batch_igf(const BatchBeam* beams, const int* start_c, const i
 cudaError_t launch_batch_green(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
                                const int blocks[3], const size_t smem[3], cudaStream_t s);
 cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
-                                  const int blocks[3], const size_t smem[3], cudaStream_t s);
+                                  const int blocks[3], const size_t smem[3], cudaStream_t s, int part = CONV_ALL);
 cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
 cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
 // host-side tiling of one beam (sets the tiling fields and grids of B)
@@ -288,6 +309,65 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
 // opts every kernel of a plan in (called when the plan is created)
 cudaError_t prepare_fft_kernels(const Plan& p);
 cudaError_t prepare_green_kernels(const Plan& p);
+cudaError_t prepare_particle_kernels();
+
+// ---------------------------------------------------------------------------
+// bulk (TMA) copies between global and shared memory.  Loads complete on an
+// mbarrier (expect_tx / complete_tx); stores are bulk groups.  Every wait has
+// an iteration limit: a wait that gives up returns false and the caller
+// records SC_ERR_TIMEOUT instead of spinning on.
+// ---------------------------------------------------------------------------
+constexpr unsigned MBAR_WAIT_LIMIT = 1u << 20;  // tries of ~1 us at most each
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// makes the initialised barriers visible to the async proxy (then __syncthreads)
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// true once the phase with the given parity has completed; false when the
+// limit ran out first
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit = MBAR_WAIT_LIMIT) {
+    const uint32_t a = smem_u32(bar);
+    for (unsigned it = 0; it < limit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity), "r"(1000u)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+// global -> shared, bytes a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst_smem)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// shared -> global (same rules), part of the current bulk group
+__device__ __forceinline__ void bulk_store(void* dst, const void* src_smem, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src_smem)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// all but the newest N bulk groups have finished reading shared memory
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+// every bulk group has completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// orders this thread's shared-memory writes before later async-proxy reads
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // records the calling thread's error message (sc_last_error) and returns code
 int sc_report(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));

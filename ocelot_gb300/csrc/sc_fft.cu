@@ -25,9 +25,11 @@ namespace ocsc {
 
 constexpr int FFT_THREADS = 256;
 
+// complex lines (two real lines each) per block of the z passes: up to 8,
+// so that a 64^3 mesh gives 256 blocks
 static inline int z_lines_per_block(int Mz) {
-    int nc = 2048 / Mz;
-    return nc < 1 ? 1 : (nc > 16 ? 16 : nc);
+    int nc = 1024 / Mz;
+    return nc < 1 ? 1 : (nc > 8 ? 8 : nc);
 }
 // columns per block in the strided passes: 16, fewer when two line buffers
 // of 16 columns would not fit in shared memory (FP64 at M = 512)
@@ -253,11 +255,12 @@ __global__ void k_field_grids(const R* __restrict__ phi, R* __restrict__ ex, R* 
     }
 }
 
-// FP32 form: the field grids as "quads" for the gather -- for each cell
-// (i,j,k) and each component F, float4 (F[i][j][k], F[i][j][k+1],
-// F[i][j+1][k], F[i][j+1][k+1]); a trilinear sample then reads two float4
-// (x planes i and i+1) instead of eight scalars.  Entries that the gather
-// never uses (j = ny-1 or k = nz-1 as a base) are written but not read.
+// FP32 form: the field grids as "octs" for the gather -- for each cell
+// (i,j,k) and each component F, the 8 values F[i+a][j+b][k+c] (a, b, c in
+// {0,1}) at index 4a + 2b + c, 32 bytes aligned to 32; a trilinear sample
+// then reads one 32-byte sector instead of eight scalars.  Entries that the
+// gather never uses (i = nx-1, j = ny-1 or k = nz-1 as a base) are written
+// but not read.
 __device__ __forceinline__ float fd(const float* __restrict__ phi, int i, int j, int k, int di, int dj, int dk,
                                     int nx, int ny, int nz, float ih) {
     // forward difference along (di,dj,dk), zero on the last plane and outside the grid
@@ -267,35 +270,45 @@ __device__ __forceinline__ float fd(const float* __restrict__ phi, int i, int j,
     return (phi[c] - phi[c + (di * ny + dj) * nz + dk]) * ih;
 }
 
-__device__ __forceinline__ void field_quads_body(const float* __restrict__ phi, float4* __restrict__ qx,
-                                                 float4* __restrict__ qy, float4* __restrict__ qz, int nx, int ny,
-                                                 int nz, const ScState* st, VBlk vb) {
+__device__ __forceinline__ void st_oct(float* p, const float (&o)[8]) {
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(o[0]), "f"(o[1]), "f"(o[2]),
+                 "f"(o[3]), "f"(o[4]), "f"(o[5]), "f"(o[6]), "f"(o[7])
+                 : "memory");
+}
+
+__device__ __forceinline__ void field_octs_body(const float* __restrict__ phi, float* __restrict__ ox,
+                                                float* __restrict__ oy, float* __restrict__ oz, int nx, int ny,
+                                                int nz, const ScState* st, VBlk vb) {
     if (st->status) return;
     const int j = vb.x, i = vb.y;
-    const float ihx = st->istepsf[0], ihy = st->istepsf[1], ihz = st->istepsf[2];
+    const float ih[3] = {st->istepsf[0], st->istepsf[1], st->istepsf[2]};
+    float* const out[3] = {ox, oy, oz};
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        const int c = (i * ny + j) * nz + k;
-        qx[c] = make_float4(fd(phi, i, j, k, 1, 0, 0, nx, ny, nz, ihx), fd(phi, i, j, k + 1, 1, 0, 0, nx, ny, nz, ihx),
-                            fd(phi, i, j + 1, k, 1, 0, 0, nx, ny, nz, ihx),
-                            fd(phi, i, j + 1, k + 1, 1, 0, 0, nx, ny, nz, ihx));
-        qy[c] = make_float4(fd(phi, i, j, k, 0, 1, 0, nx, ny, nz, ihy), fd(phi, i, j, k + 1, 0, 1, 0, nx, ny, nz, ihy),
-                            fd(phi, i, j + 1, k, 0, 1, 0, nx, ny, nz, ihy),
-                            fd(phi, i, j + 1, k + 1, 0, 1, 0, nx, ny, nz, ihy));
-        qz[c] = make_float4(fd(phi, i, j, k, 0, 0, 1, nx, ny, nz, ihz), fd(phi, i, j, k + 1, 0, 0, 1, nx, ny, nz, ihz),
-                            fd(phi, i, j + 1, k, 0, 0, 1, nx, ny, nz, ihz),
-                            fd(phi, i, j + 1, k + 1, 0, 0, 1, nx, ny, nz, ihz));
+        const size_t c = ((size_t)i * ny + j) * nz + k;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float o[8];
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e)
+                        o[4 * a + 2 * b + e] = fd(phi, i + a, j + b, k + e, d == 0, d == 1, d == 2, nx, ny, nz, ih[d]);
+            st_oct(out[d] + 8 * c, o);
+        }
     }
 }
 
-__global__ void k_field_quads(const float* __restrict__ phi, float4* __restrict__ qx, float4* __restrict__ qy,
-                              float4* __restrict__ qz, int nx, int ny, int nz, const ScState* st) {
-    field_quads_body(phi, qx, qy, qz, nx, ny, nz, st, hw_vblk());
+__global__ void k_field_octs(const float* __restrict__ phi, float* __restrict__ ox, float* __restrict__ oy,
+                             float* __restrict__ oz, int nx, int ny, int nz, const ScState* st) {
+    field_octs_body(phi, ox, oy, oz, nx, ny, nz, st, hw_vblk());
 }
 
 
 template <typename R>
 static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid, R* phi, const long long* qfix,
-                              cudaStream_t s) {
+                              cudaStream_t s, int part) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int Kz = p.Mz / 2 + 1, Ky = p.My / 2 + 1;
     Cx<R>* W = reinterpret_cast<Cx<R>*>(ws + L.W);
@@ -307,13 +320,16 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     const int NC = z_lines_per_block(p.Mz);
     const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
     dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
-    if ((e = set_smem(k_zfwd<R>, smz))) return e;
-    k_zfwd<R><<<gz, FFT_THREADS, smz, s>>>(qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
     const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
     dim3 gy((Kz + tky - 1) / tky, p.nx);
-    if ((e = set_smem(k_ypass<R, false>, smy))) return e;
-    k_ypass<R, false><<<gy, FFT_THREADS, smy, s>>>(W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+    if (part != CONV_REST) {
+        if ((e = set_smem(k_zfwd<R>, smz))) return e;
+        k_zfwd<R><<<gz, FFT_THREADS, smz, s>>>(qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+        if ((e = set_smem(k_ypass<R, false>, smy))) return e;
+        k_ypass<R, false><<<gy, FFT_THREADS, smy, s>>>(W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+    }
+    if (part == CONV_FORWARD) return cudaGetLastError();
     const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
     dim3 gx((Kz + tkx - 1) / tkx, p.My);
     if ((e = set_smem(k_xconv<R>, smx))) return e;
@@ -345,12 +361,12 @@ cudaError_t prepare_fft_kernels(const Plan& p) {
 }
 
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in, void* phi_out,
-                            cudaStream_t s, const long long* qfix) {
+                            cudaStream_t s, const long long* qfix, int part) {
     if (p.prec == SC_FP64)
         return convolve_t<double>(p, L, ws, static_cast<double*>(const_cast<void*>(qgrid_in)),
-                                  static_cast<double*>(phi_out), nullptr, s);
+                                  static_cast<double*>(phi_out), nullptr, s, part);
     return convolve_t<float>(p, L, ws, static_cast<float*>(const_cast<void*>(qgrid_in)), static_cast<float*>(phi_out),
-                             qfix, s);
+                             qfix, s, part);
 }
 
 template <typename R>
@@ -359,9 +375,9 @@ static cudaError_t field_t(const Plan& p, const Layout& L, char* ws, cudaStream_
     const int bt = p.nz < 256 ? ((p.nz + 31) / 32) * 32 : 256;
     const dim3 grid(p.ny, p.nx);
     if (sizeof(R) == 4)
-        k_field_quads<<<grid, bt, 0, s>>>(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float4*>(ws + L.exq),
-                                          reinterpret_cast<float4*>(ws + L.eyq), reinterpret_cast<float4*>(ws + L.ezq),
-                                          p.nx, p.ny, p.nz, st);
+        k_field_octs<<<grid, bt, 0, s>>>(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
+                                         reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq),
+                                         p.nx, p.ny, p.nz, st);
     else
         k_field_grids<R><<<grid, bt, 0, s>>>(reinterpret_cast<const R*>(ws + L.phi), reinterpret_cast<R*>(ws + L.ex),
                                              reinterpret_cast<R*>(ws + L.ey), reinterpret_cast<R*>(ws + L.ez),
@@ -417,10 +433,10 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_zinv(const BatchBeam* __restri
                      p.My, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.fft_nc, st, vb);
 }
 
-__global__ void kb_field_quads(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
+__global__ void kb_field_octs(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
     BATCH_BEAM(BS_FIELD)
-    field_quads_body(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float4*>(ws + L.exq),
-                     reinterpret_cast<float4*>(ws + L.eyq), reinterpret_cast<float4*>(ws + L.ezq), p.nx, p.ny, p.nz,
+    field_octs_body(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
+                    reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq), p.nx, p.ny, p.nz,
                      st, vb);
 }
 #undef BATCH_BEAM
@@ -455,10 +471,13 @@ cudaError_t prepare_batch_fft() {
 }
 
 cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
-                                  const int blocks[3], const size_t smem[3], cudaStream_t s) {
+                                  const int blocks[3], const size_t smem[3], cudaStream_t s, int part) {
     if (nb <= 0) return cudaSuccess;
-    kb_zfwd<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
-    kb_ypass<false><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
+    if (part != CONV_REST) {
+        kb_zfwd<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
+        kb_ypass<false><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
+    }
+    if (part == CONV_FORWARD) return cudaGetLastError();
     kb_xconv<<<blocks[2], FFT_THREADS, smem[2], s>>>(beams, sx, nb);
     kb_ypass<true><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
     kb_zinv<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
@@ -467,7 +486,7 @@ cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const i
 
 cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s) {
     if (nb <= 0) return cudaSuccess;
-    kb_field_quads<<<blocks, 128, 0, s>>>(beams, start, nb);
+    kb_field_octs<<<blocks, 128, 0, s>>>(beams, start, nb);
     return cudaGetLastError();
 }
 

@@ -83,11 +83,90 @@ __device__ __forceinline__ void stockham_stage(const Cx<R>* __restrict__ a, Cx<R
     }
 }
 
+// The same stages with the line length known at compile time: the radix of
+// each stage, the butterfly count and the twiddle stride are constants, so
+// the index arithmetic reduces to shifts and masks.  The plan is the greedy
+// one of make_radix_plan (radix 8 while it divides, then 4, then 2) and the
+// arithmetic is that of stockham_stage, so results are identical.
+constexpr int plan_radix(int L, int s) {
+    int rem = L, st = 0;
+    while (rem % 8 == 0 && rem > 1) {
+        if (st == s) return 8;
+        rem /= 8;
+        ++st;
+    }
+    while (rem % 4 == 0 && rem > 1) {
+        if (st == s) return 4;
+        rem /= 4;
+        ++st;
+    }
+    while (rem % 2 == 0 && rem > 1) {
+        if (st == s) return 2;
+        rem /= 2;
+        ++st;
+    }
+    return 0;
+}
+
+template <typename R, bool INV, int RAD, int L, int NS>
+__device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx<R>* __restrict__ b, int ls,
+                                                 int nl, const Cx<R>* tw) {
+    constexpr int nb = L / RAD;
+    constexpr int step = L / (NS * RAD);
+    const int total = nb * nl;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int line = idx / nb;
+        const int j = idx - line * nb;
+        const int k = j % NS;
+        const Cx<R>* src = a + line * ls;
+        Cx<R>* dst = b + line * ls;
+        Cx<R> v[RAD];
+#pragma unroll
+        for (int t = 0; t < RAD; ++t) v[t] = src[j + t * nb];
+        if (NS > 1) {
+#pragma unroll
+            for (int t = 1; t < RAD; ++t) {
+                Cx<R> w = tw[t * k * step];
+                if (INV) w.y = -w.y;
+                v[t] = cmul(v[t], w);
+            }
+        }
+        if (RAD == 2) dft2<Cx<R>, INV>(v[0], v[1]);
+        else if (RAD == 4) dft4<Cx<R>, INV>(v[0], v[1], v[2], v[3]);
+        else dft8<R, INV>(v);
+        const int out = (j - k) * RAD + k;
+#pragma unroll
+        for (int t = 0; t < RAD; ++t) dst[out + t * NS] = v[t];
+    }
+}
+
+template <typename R, bool INV, int L, int S, int NS>
+__device__ __forceinline__ Cx<R>* fft_stages_c(Cx<R>* a, Cx<R>* b, int ls, int nl, const Cx<R>* tw) {
+    constexpr int RAD = plan_radix(L, S);
+    if constexpr (RAD == 0) {
+        return a;
+    } else {
+        stockham_stage_c<R, INV, RAD, L, NS>(a, b, ls, nl, tw);
+        __syncthreads();
+        return fft_stages_c<R, INV, L, S + 1, NS * RAD>(b, a, ls, nl, tw);
+    }
+}
+
 // FFT of nl lines of length rp.L; a holds the input, b is scratch of the
 // same shape.  Returns the buffer that holds the result.  Must be called by
 // every thread of the block; ends with a barrier.
 template <typename R, bool INV>
 __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan& rp, const Cx<R>* tw) {
+    switch (rp.L) {  // the padded lengths of meshes up to 256 per axis
+        case 8: return fft_stages_c<R, INV, 8, 0, 1>(a, b, ls, nl, tw);
+        case 16: return fft_stages_c<R, INV, 16, 0, 1>(a, b, ls, nl, tw);
+        case 32: return fft_stages_c<R, INV, 32, 0, 1>(a, b, ls, nl, tw);
+        case 64: return fft_stages_c<R, INV, 64, 0, 1>(a, b, ls, nl, tw);
+        case 128: return fft_stages_c<R, INV, 128, 0, 1>(a, b, ls, nl, tw);
+        case 256: return fft_stages_c<R, INV, 256, 0, 1>(a, b, ls, nl, tw);
+        case 512: return fft_stages_c<R, INV, 512, 0, 1>(a, b, ls, nl, tw);
+        default: break;
+    }
     int Ns = 1;
     for (int s = 0; s < rp.nst; ++s) {
         const int r = rp.r[s];

@@ -44,20 +44,14 @@ __device__ __forceinline__ void igf_spacing(const ScState* st, const IgfArgs& a,
     if (a.use_state) { hx = st->steps[0]; hy = st->steps[1]; hz = st->steps[2]; }
 }
 
-// Near box of the hybrid table: along each axis the cells with index below
-// ceil(5 hmax / h) + 1.  Every cell outside it is at least 5 hmax from the
-// origin, where the 4th-order multipole form of the cell integral is within
-// 5e-8 of the exact integral (checked against an extended-precision IGF).
-__device__ __forceinline__ void igf_box(double hx, double hy, double hz, int nx, int ny, int nz, int hybrid, int b[3]) {
+// Near box of the hybrid table (igf_box_of in sc_common.cuh): computed once
+// per kick with the mesh step and kept in the state; the full octant when
+// the table is exact
+__device__ __forceinline__ void igf_box(const ScState* st, int nx, int ny, int nz, int hybrid, int b[3]) {
     if (!hybrid) { b[0] = nx; b[1] = ny; b[2] = nz; return; }
-    const double hm = fmax(hx, fmax(hy, hz));
-    const double h[3] = {hx, hy, hz};
-    const int n[3] = {nx, ny, nz};
-    for (int a = 0; a < 3; ++a) {
-        const double v = 5.0 * hm / h[a];
-        b[a] = v >= (double)n[a] ? n[a] : (int)ceil(v) + 1;
-        if (b[a] > n[a]) b[a] = n[a];
-    }
+    b[0] = st->igf_box[0];
+    b[1] = st->igf_box[1];
+    b[2] = st->igf_box[2];
 }
 
 __device__ __forceinline__ double igf_point(double x, double y, double z) {
@@ -79,13 +73,15 @@ __device__ __forceinline__ void igf_corners_body(double* __restrict__ ig, int nx
     double hx, hy, hz;
     igf_spacing(st, a, hx, hy, hz);
     int b[3];
-    igf_box(hx, hy, hz, nx, ny, nz, a.hybrid, b);
+    igf_box(st, nx, ny, nz, a.hybrid, b);
     const int cx1 = b[0] + 1, cy1 = b[1] + 1, cz1 = b[2] + 1;
-    const size_t total = (size_t)cx1 * cy1 * cz1;
-    for (size_t c = vb.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)vb.nx * blockDim.x) {
-        const int k = (int)(c % cz1);
-        const int j = (int)((c / cz1) % cy1);
-        const int i = (int)(c / ((size_t)cz1 * cy1));
+    // 32-bit index arithmetic: a mesh has fewer than 2^31 corners
+    const unsigned total = (unsigned)cx1 * cy1 * cz1;
+    for (unsigned c = vb.x * blockDim.x + threadIdx.x; c < total; c += vb.nx * blockDim.x) {
+        const unsigned t = c / (unsigned)cz1;
+        const int k = (int)(c - t * (unsigned)cz1);
+        const int i = (int)(t / (unsigned)cy1);
+        const int j = (int)(t - (unsigned)i * cy1);
         const double x = __dsub_rn(__dmul_rn(hx, (double)i), __dmul_rn(hx, 0.5));
         const double y = __dsub_rn(__dmul_rn(hy, (double)j), __dmul_rn(hy, 0.5));
         const double z = __dsub_rn(__dmul_rn(hz, (double)k), __dmul_rn(hz, 0.5));
@@ -130,17 +126,18 @@ __device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* 
     double hx, hy, hz;
     igf_spacing(st, a, hx, hy, hz);
     int bx[3];
-    igf_box(hx, hy, hz, nx, ny, nz, a.hybrid, bx);
+    igf_box(st, nx, ny, nz, a.hybrid, bx);
     const float hxf = (float)hx, hyf = (float)hy, hzf = (float)hz;
     const float a2 = 0.25f * hxf * hxf, b2 = 0.25f * hyf * hyf, c2 = 0.25f * hzf * hzf, V = hxf * hyf * hzf;
-    const size_t total = (size_t)nx * ny * nz;
-    const size_t sy = bx[2] + 1, sx = (size_t)(bx[1] + 1) * (bx[2] + 1);
-    for (size_t c = vb.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)vb.nx * blockDim.x) {
-        const int k = (int)(c % nz);
-        const int j = (int)((c / nz) % ny);
-        const int i = (int)(c / ((size_t)nz * ny));
+    const unsigned total = (unsigned)nx * ny * nz;
+    const unsigned sy = bx[2] + 1, sx = (unsigned)(bx[1] + 1) * (bx[2] + 1);
+    for (unsigned c = vb.x * blockDim.x + threadIdx.x; c < total; c += vb.nx * blockDim.x) {
+        const unsigned t = c / (unsigned)nz;
+        const int k = (int)(c - t * (unsigned)nz);
+        const int i = (int)(t / (unsigned)ny);
+        const int j = (int)(t - (unsigned)i * ny);
         if (i < bx[0] && j < bx[1] && k < bx[2]) {
-            const size_t o = i * sx + j * sy + k;
+            const unsigned o = i * sx + j * sy + k;
             if (!SC_IDX_OK(st, 32, o + sx + sy + 1, (long long)(nx + 1) * (ny + 1) * (nz + 1))) continue;
             double v = __dsub_rn(ig[o + sx + sy + 1], ig[o + sy + 1]);
             v = __dsub_rn(v, ig[o + sx + 1]);

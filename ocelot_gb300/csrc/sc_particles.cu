@@ -196,6 +196,141 @@ __device__ __forceinline__ void mom32(float xq, float yq, float d, const KickPar
     E = gamma * kp.m_f;
 }
 
+// rotated position (z scaled by gamma0) of one particle in FP32 from its
+// FP32-rounded MAD coordinates and momenta (coord_transform.py:57-96 for the
+// lab position, sc.py:233 for the rotation), as the extent kernel stores it
+__device__ __forceinline__ void pos32(float x, float y, float tau, float px, float py, float pz, float E,
+                                      const float (&T)[3][3], float g0, float (&v)[3]) {
+    const float s = tau / E;
+    const float l0 = x - px * s, l1 = y - py * s, l2 = -pz * s;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) v[j] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
+    v[2] *= g0;
+}
+// grid coordinate X = v/steps - X_off (sc.py:182-183) in FP32
+__device__ __forceinline__ float grid32(float v, float step, float off) { return v / step - off; }
+
+// 32-byte and 16-byte row accesses of G consecutive particles; a partial
+// group (full == false) takes one element
+template <int G>
+__device__ __forceinline__ void ld_rows(const double* __restrict__ row, int64_t i, bool full, double (&a)[G]) {
+    if constexpr (G == 4) {
+        if (full) {
+            asm("ld.global.nc.L1::no_allocate.v4.f64 {%0,%1,%2,%3}, [%4];"
+                : "=d"(a[0]), "=d"(a[1]), "=d"(a[2]), "=d"(a[3])
+                : "l"(row + i));
+            return;
+        }
+    } else if constexpr (G == 2) {
+        if (full) {
+            const double2 v = __ldg(reinterpret_cast<const double2*>(row + i));
+            a[0] = v.x;
+            a[1] = v.y;
+            return;
+        }
+    }
+    a[0] = row[i];
+#pragma unroll
+    for (int w = 1; w < G; ++w) a[w] = 0.0;
+}
+template <int G>
+__device__ __forceinline__ void st_rows(double* __restrict__ row, int64_t i, bool full, const double (&a)[G]) {
+    if constexpr (G == 4) {
+        if (full) {
+            asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(row + i), "d"(a[0]), "d"(a[1]), "d"(a[2]),
+                         "d"(a[3])
+                         : "memory");
+            return;
+        }
+    } else if constexpr (G == 2) {
+        if (full) {
+            *reinterpret_cast<double2*>(row + i) = make_double2(a[0], a[1]);
+            return;
+        }
+    }
+    row[i] = a[0];
+}
+
+// Group-wise particle loop: each thread takes G consecutive particles (one
+// row access each), the last n mod G particles one per thread.  The loop
+// strides over the blocks of the beam (vb), not of the launch.
+#define GROUP_LOOP_BEGIN(n, G)                                                                    \
+    const int64_t ngrp_ = (n) / (G);                                                              \
+    const int64_t ntot_ = ngrp_ + ((n) - ngrp_ * (G));                                            \
+    for (int64_t p_ = vb.x * (int64_t)blockDim.x + threadIdx.x; p_ < ntot_;                       \
+         p_ += (int64_t)vb.nx * blockDim.x) {                                                     \
+        const bool full_ = p_ < ngrp_;                                                            \
+        const int64_t i0_ = full_ ? p_ * (G) : ngrp_ * (G) + (p_ - ngrp_);                        \
+        const int W_ = full_ ? (G) : 1;
+#define GROUP_LOOP_END }
+
+// ---------------------------------------------------------------------------
+// Bulk-copy (TMA) streaming of particle rows through shared memory, for the
+// frame, extent and keys kernels.  A block walks its tiles of PT_TILE
+// particles (local tile t is global tile vb.x + t * vb.nx); PS_STAGES tile
+// buffers rotate so that the loads of the next tiles are in flight while the
+// block works on one.  Thread t takes particles 2t and 2t+1 of a tile.  A
+// tile's copies cover a prefix whose byte length is a multiple of 16; the
+// few particles after it (the end of the beam) are read directly.
+// ---------------------------------------------------------------------------
+constexpr int PT_TILE = 2 * PT;
+constexpr int PS_STAGES = 2;
+
+struct BlockTiles {
+    int64_t n, first, stride, mine;
+    __device__ BlockTiles(int64_t n_, VBlk vb) : n(n_), first(vb.x), stride(vb.nx) {
+        const int64_t nt = (n + PT_TILE - 1) / PT_TILE;
+        mine = first < nt ? (nt - 1 - first) / stride + 1 : 0;
+    }
+    __device__ int64_t start(int64_t t) const { return (first + t * stride) * PT_TILE; }
+    __device__ int count(int64_t t) const {
+        const int64_t c = n - start(t);
+        return (int)(c < PT_TILE ? c : PT_TILE);
+    }
+};
+
+// Runs body(t, stage) for each of the block's tiles once its rows have
+// landed in tile buffer `stage`; issue(t, stage, bar) (thread 0) starts the
+// loads of local tile t.  Every thread of the block must call it; body must
+// not synchronise the block.  Returns false if a wait gave up, after
+// waiting (again with a limit) for the loads still in flight.
+template <typename Issue, typename Body>
+__device__ __forceinline__ bool stream_tiles(const BlockTiles& T, uint64_t* bar, Issue&& issue, Body&& body) {
+    const bool lead = threadIdx.x == 0;
+    if (lead) {
+        for (int s = 0; s < PS_STAGES; ++s) mbar_init(&bar[s], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    int64_t issued = T.mine < PS_STAGES ? T.mine : PS_STAGES;
+    if (lead)
+        for (int64_t t = 0; t < issued; ++t) issue(t, (int)t, &bar[t]);
+    int64_t t = 0;
+    bool failed = false;
+    for (; t < T.mine; ++t) {
+        const int s = (int)(t % PS_STAGES);
+        const bool ok = mbar_wait(&bar[s], (unsigned)((t / PS_STAGES) & 1));
+        if (ok) body(t, s);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        // every thread is done with buffer s: it takes local tile t + PS_STAGES
+        if (lead && issued < T.mine) {
+            issue(issued, s, &bar[s]);
+            ++issued;
+        }
+    }
+    if (failed && lead)
+        for (int64_t u = t; u < issued; ++u) mbar_wait(&bar[u % PS_STAGES], (unsigned)((u / PS_STAGES) & 1));
+    return !failed;
+}
+
+// shared memory of the streamed kernels: the tile buffers, then the barriers
+constexpr size_t FR_SMEM = (size_t)PS_STAGES * 3 * PT_TILE * sizeof(double) + PS_STAGES * sizeof(uint64_t);
+constexpr size_t EX_SMEM = (size_t)PS_STAGES * 7 * PT_TILE * sizeof(double) + PS_STAGES * sizeof(uint64_t);
+static_assert(3 * (EX_SMEM + 1024 + 5 * 1024) <= 228 * 1024, "three extent blocks must fit an SM");
+
 // ---------------------------------------------------------------------------
 // last-block reductions: every block writes its partials, the last block to
 // finish reduces all of them in block order (deterministic) and resets the
@@ -258,6 +393,10 @@ __device__ void frame_finalize(const double* part, int nblk, const KickParams& k
     st->kzf = (float)kp.cdT;
     int status = SC_OK;
     if (!(Pav > 0.0) || !isfinite(Pav) || !isfinite(gamma0) || !isfinite(t1[0]) || !isfinite(t2[1])) status = SC_ERR_NONFINITE;
+    if (st->frame_timeout) {
+        status = SC_ERR_TIMEOUT;
+        st->frame_timeout = 0;
+    }
     st->status = status;
 }
 
@@ -316,6 +455,7 @@ __device__ void mesh_finalize(const double* part, int nblk, const KickParams& kp
     }
     st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, steps[0]), steps[1]), steps[2]);
     st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
+    igf_box_of(steps, kp.nx, kp.ny, kp.nz, st->igf_box);
     const bool same = steps[0] == st->igf_h[0] && steps[1] == st->igf_h[1] && steps[2] == st->igf_h[2];
     st->igf_rebuild = same ? 0 : 1;
     for (int k = 0; k < 3; ++k) st->igf_h[k] = steps[k];
@@ -433,6 +573,62 @@ template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
                                                    double* __restrict__ part, ScState* st) {
     frame32_body<VEC>(rp, kp, part, st, nullptr, 0, hw_vblk());
+}
+
+// frame32_body with the rows x', y', delta streamed through shared memory
+// (rows 16-byte aligned, even stride)
+__device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, const KickParams& kp,
+                                                 double* __restrict__ part, ScState* st,
+                                                 unsigned long long* __restrict__ qzero, int64_t nzero, VBlk vb) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __shared__ double sm[3 * 32];
+    double* buf = reinterpret_cast<double*>(smraw);  // [PS_STAGES][3][PT_TILE]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + PS_STAGES * 3 * PT_TILE);
+    if (qzero)
+        for (int64_t i = vb.x * (int64_t)blockDim.x + threadIdx.x; i < nzero; i += (int64_t)vb.nx * blockDim.x)
+            qzero[i] = 0ull;
+    const int64_t n = kp.n, ld = kp.ld;
+    const BlockTiles T(n, vb);
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    auto add = [&](double xq, double yq, double d) {
+        float px, py, pz, E;
+        mom32(d2f(xq), d2f(yq), d2f(d), kp, px, py, pz, E);
+        a0 += px;
+        a1 += py;
+        a2 += pz;
+    };
+    auto issue = [&](int64_t t, int s, uint64_t* b) {
+        const int64_t i0 = T.start(t);
+        const unsigned bytes = (unsigned)(T.count(t) & ~1) * 8u;
+        mbar_arrive_expect_tx(b, 3u * bytes);
+        if (bytes)
+            for (int r = 0; r < 3; ++r) bulk_load(buf + (s * 3 + r) * PT_TILE, rp + (2 * r + 1) * ld + i0, bytes, b);
+    };
+    auto body = [&](int64_t t, int s) {
+        const int cnt = T.count(t), staged = cnt & ~1, j = 2 * threadIdx.x;
+        const double* B = buf + s * 3 * PT_TILE;
+        if (j + 1 < staged) {
+            const double2 x = *reinterpret_cast<const double2*>(B + j);
+            const double2 y = *reinterpret_cast<const double2*>(B + PT_TILE + j);
+            const double2 d = *reinterpret_cast<const double2*>(B + 2 * PT_TILE + j);
+            add(x.x, y.x, d.x);
+            add(x.y, y.y, d.y);
+        } else if (j < cnt) {
+            const int64_t i = T.start(t) + j;
+            add(rp[ld + i], rp[3 * ld + i], rp[5 * ld + i]);
+        }
+    };
+    if (!stream_tiles(T, bar, issue, body) && threadIdx.x == 0) atomicExch(&st->frame_timeout, 1);
+    double acc[3] = {a0, a1, a2};
+    block_sum<3>(acc, sm);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) part[vb.x * 3 + k] = acc[k];
+    if (arrive_last(&st->done_frame, vb.nx)) frame_finalize(part, vb.nx, kp, st);
+}
+
+__global__ void __launch_bounds__(PT, 4) k_frame32_tma(const double* __restrict__ rp, KickParams kp,
+                                                       double* __restrict__ part, ScState* st) {
+    frame32_tma_body(rp, kp, part, st, nullptr, 0, hw_vblk());
 }
 
 // ---------------------------------------------------------------------------
@@ -555,10 +751,9 @@ __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, con
         for (int w = 0; w < W_; ++w) {
             float px, py, pz, E;
             mom32(r[1][w], r[3][w], r[5][w], kp, px, py, pz, E);
-            const float s = r[4][w] / E;
-            const float l0 = r[0][w] - px * s, l1 = r[2][w] - py * s, l2 = -pz * s;
-            for (int j = 0; j < 3; ++j) v[j][w] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
-            v[2][w] *= g0;
+            float vw[3];
+            pos32(r[0][w], r[2][w], r[4][w], px, py, pz, E, T, g0, vw);
+            for (int j = 0; j < 3; ++j) v[j][w] = vw[j];
             const float qi = qq[w];
             for (int j = 0; j < 3; ++j) {
                 mnf[j] = fminf(mnf[j], v[j][w]);
@@ -634,6 +829,145 @@ __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ r
     extent32_body<VEC>(rp, q, kp, X, part, st, hw_vblk());
 }
 
+// extent32_body with the six rows and the charges streamed through shared
+// memory (rows and q 16-byte aligned, even stride).  Pass 2 is walked only
+// by the threads whose own FP32 extreme lies within the margin of the
+// block's: a particle of any other thread is farther from the block's
+// extreme than that thread's extreme, so the candidates are the same.
+__device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp, const double* __restrict__ q,
+                                                  const KickParams& kp, float* __restrict__ X,
+                                                  double* __restrict__ part, ScState* st, VBlk vb) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __shared__ double sm[5 * 32];
+    __shared__ float smf[3 * 32];
+    __shared__ float bmin[3], bmax[3];
+    __shared__ unsigned long long emin[3], emax[3];
+    double* buf = reinterpret_cast<double*>(smraw);  // [PS_STAGES][7][PT_TILE]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + PS_STAGES * 7 * PT_TILE);
+    float mnf[3] = {INFINITY, INFINITY, INFINITY}, mxf[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float qsf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
+    const bool ok = !__syncthreads_or(st->status != SC_OK);
+    float T[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) T[i][j] = st->Tf[i][j];
+    const float g0 = st->g0f;
+    const BlockTiles Tl(ok ? n : 0, vb);
+    // one particle: rotated position, extremes and charge moments; returns v
+    auto one = [&](const double (&r)[6], double qd, float (&v)[3]) {
+        float px, py, pz, E;
+        mom32(d2f(r[1]), d2f(r[3]), d2f(r[5]), kp, px, py, pz, E);
+        pos32(d2f(r[0]), d2f(r[2]), d2f(r[4]), px, py, pz, E, T, g0, v);
+        const float qi = d2f(qd);
+        for (int j = 0; j < 3; ++j) {
+            mnf[j] = fminf(mnf[j], v[j]);
+            mxf[j] = fmaxf(mxf[j], v[j]);
+            qsf[j] += qi * v[j];
+        }
+        qsf[3] += qi;
+        qsf[4] += fabsf(qi);
+    };
+    auto issue = [&](int64_t t, int s, uint64_t* b) {
+        const int64_t i0 = Tl.start(t);
+        const unsigned bytes = (unsigned)(Tl.count(t) & ~1) * 8u;
+        mbar_arrive_expect_tx(b, 7u * bytes);
+        if (bytes) {
+            for (int k = 0; k < 6; ++k) bulk_load(buf + (s * 7 + k) * PT_TILE, rp + k * ld + i0, bytes, b);
+            bulk_load(buf + (s * 7 + 6) * PT_TILE, q + i0, bytes, b);
+        }
+    };
+    auto body = [&](int64_t t, int s) {
+        const int cnt = Tl.count(t), staged = cnt & ~1, j = 2 * threadIdx.x;
+        const int64_t i0 = Tl.start(t);
+        const double* B = buf + s * 7 * PT_TILE;
+        if (j + 1 < staged) {
+            double r0[6], r1[6];
+            for (int k = 0; k < 6; ++k) {
+                const double2 v = *reinterpret_cast<const double2*>(B + k * PT_TILE + j);
+                r0[k] = v.x;
+                r1[k] = v.y;
+            }
+            const double2 qq = *reinterpret_cast<const double2*>(B + 6 * PT_TILE + j);
+            float v0[3], v1[3];
+            one(r0, qq.x, v0);
+            one(r1, qq.y, v1);
+            for (int k = 0; k < 3; ++k) *reinterpret_cast<float2*>(X + k * nX + i0 + j) = make_float2(v0[k], v1[k]);
+        } else if (j < cnt) {
+            const int64_t i = i0 + j;
+            double r[6];
+            for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i];
+            float v[3];
+            one(r, q[i], v);
+            for (int k = 0; k < 3; ++k) X[k * nX + i] = v[k];
+        }
+    };
+    const bool streamed = stream_tiles(Tl, bar, issue, body);
+    if (!streamed && threadIdx.x == 0) atomicCAS(&st->status, SC_OK, SC_ERR_TIMEOUT);
+    const float my_mn[3] = {mnf[0], mnf[1], mnf[2]}, my_mx[3] = {mxf[0], mxf[1], mxf[2]};
+    // float extremes reduce exactly in float; the sums in double
+    block_minmax_f<3, false>(mnf, smf);
+    block_minmax_f<3, true>(mxf, smf);
+    double qs[5] = {qsf[0], qsf[1], qsf[2], qsf[3], qsf[4]};
+    block_sum<5>(qs, sm);
+    if (threadIdx.x == 0)
+        for (int j = 0; j < 3; ++j) {
+            bmin[j] = mnf[j];
+            bmax[j] = mxf[j];
+            emin[j] = ord64(INFINITY);
+            emax[j] = ord64(-INFINITY);
+        }
+    __syncthreads();
+    float tol[3];
+    bool mine = false;
+    for (int j = 0; j < 3; ++j) {  // 2^-18 of the coordinate scale: 64x the FP32 rounding bound of v
+        tol[j] = ldexpf(fmaxf(fabsf(bmin[j]), fabsf(bmax[j])) + (bmax[j] - bmin[j]), -18);
+        mine |= (my_mn[j] <= bmin[j] + tol[j]) || (my_mx[j] >= bmax[j] - tol[j]);
+    }
+    if (ok && streamed && mine) {
+        double Td[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) Td[a][b] = st->T[a][b];
+        const double g0d = st->gamma0;
+        for (int64_t t = 0; t < Tl.mine; ++t)
+            for (int w = 0; w < 2; ++w) {
+                const int jj = 2 * threadIdx.x + w;
+                if (jj >= Tl.count(t)) break;
+                const int64_t i = Tl.start(t) + jj;
+                bool cand = false;
+                for (int j = 0; j < 3; ++j) {
+                    const float v = X[j * nX + i];
+                    cand |= (v <= bmin[j] + tol[j]) || (v >= bmax[j] - tol[j]);
+                }
+                if (cand) {
+                    double v[3];
+                    xyz_fine(rp, ld, i, kp, Td, g0d, v);
+                    for (int j = 0; j < 3; ++j) {
+                        if (X[j * nX + i] <= bmin[j] + tol[j]) atomicMin(&emin[j], ord64(v[j]));
+                        if (X[j * nX + i] >= bmax[j] - tol[j]) atomicMax(&emax[j], ord64(v[j]));
+                    }
+                }
+            }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && SC_IDX_OK(st, 12, vb.x, kp.n > 0 ? vb.nx : 0)) {
+        double* o = part + vb.x * PART_EXT;
+        for (int k = 0; k < 3; ++k) {
+            o[k] = unord64(emin[k]);
+            o[3 + k] = unord64(emax[k]);
+            o[6 + k] = qs[k];
+        }
+        o[9] = qs[3];
+        o[10] = qs[4];
+    }
+    if (arrive_last(&st->done_extent, vb.nx)) mesh_finalize(part, vb.nx, kp, st, -1.0);
+}
+
+__global__ void __launch_bounds__(PT, 3) k_extent32_tma(const double* __restrict__ rp, const double* __restrict__ q,
+                                                        KickParams kp, float* __restrict__ X,
+                                                        double* __restrict__ part, ScState* st) {
+    extent32_tma_body(rp, q, kp, X, part, st, hw_vblk());
+}
+
 // el_field entry: X given as [n][3] rotated positions; z scaled by gamma in place
 template <typename R>
 __global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, const double* __restrict__ q, KickParams kp,
@@ -668,6 +1002,8 @@ __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickPar
     st->steps[2] = hz;
     st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, hx), hy), hz);
     st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
+    const double h[3] = {hx, hy, hz};
+    igf_box_of(h, kp.nx, kp.ny, kp.nz, st->igf_box);
     const bool same = hx == st->igf_h[0] && hy == st->igf_h[1] && hz == st->igf_h[2];
     st->igf_rebuild = same ? 0 : 1;
     st->igf_h[0] = hx;
@@ -762,7 +1098,7 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
         const int64_t i = i0_ + w;
         const float v0 = v[0][w], v1 = v[1][w], v2 = v[2][w];
         const float nrm = sqrtf(v0 * v0 + v1 * v1 + (v2 * ig0) * (v2 * ig0));  // |lab position|
-        float g[3] = {v0 / sf[0] - of[0], v1 / sf[1] - of[1], v2 / sf[2] - of[2]};
+        float g[3] = {grid32(v0, sf[0], of[0]), grid32(v1, sf[1], of[1]), grid32(v2, sf[2], of[2])};
         bool amb = false;
         for (int j = 0; j < 3; ++j) {
             const float scale = (j == 2 ? nrm / ig0 : nrm) * is[j] + fabsf(of[j]) + 1.0f;
@@ -793,7 +1129,10 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
     }
     if (pair_) *reinterpret_cast<uint2*>(keys + i0_) = make_uint2(key2[0], key2[1]);
     else keys[i0_] = key2[0];
-    for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
+    // the el_field entry gathers at the stored grid coordinates; the kick
+    // recomputes them from rparticles
+    if (!rp)
+        for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
     PAIR_LOOP_END
     if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
 }
@@ -844,8 +1183,8 @@ __device__ __forceinline__ void gather3(const R* ex, const R* ey, const R* ez, i
     e2 = trilerp<R>(ez, nx, ny, nz, X0 + h, X1 + h, X2);
 }
 
-// trilinear sample from the FP32 gather quads (two float4 loads)
-__device__ __forceinline__ float trilerp_q(const float4* __restrict__ Q, int nx, int ny, int nz, float c0, float c1,
+// trilinear sample from the FP32 gather octs (one 32-byte load)
+__device__ __forceinline__ float trilerp_o(const float* __restrict__ O, int nx, int ny, int nz, float c0, float c1,
                                            float c2) {
     if (!(c0 >= 0.f) || !(c1 >= 0.f) || !(c2 >= 0.f) || c0 > (float)(nx - 1) || c1 > (float)(ny - 1) ||
         c2 > (float)(nz - 1))
@@ -855,18 +1194,21 @@ __device__ __forceinline__ float trilerp_q(const float4* __restrict__ Q, int nx,
     if (j > ny - 2) j = ny - 2;
     if (k > nz - 2) k = nz - 2;
     const float tx = c0 - (float)i, ty = c1 - (float)j, tz = c2 - (float)k;
-    const int c = (i * ny + j) * nz + k;
-    const float4 a = __ldg(Q + c), b = __ldg(Q + c + ny * nz);
-    const float ya = (1.f - ty) * ((1.f - tz) * a.x + tz * a.y) + ty * ((1.f - tz) * a.z + tz * a.w);
-    const float yb = (1.f - ty) * ((1.f - tz) * b.x + tz * b.y) + ty * ((1.f - tz) * b.z + tz * b.w);
+    const float* p = O + 8 * ((i * ny + j) * nz + k);  // < 2^31: meshes have at most 256^3 cells
+    float o[8];
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3]), "=f"(o[4]), "=f"(o[5]), "=f"(o[6]), "=f"(o[7])
+        : "l"(p));
+    const float ya = (1.f - ty) * ((1.f - tz) * o[0] + tz * o[1]) + ty * ((1.f - tz) * o[2] + tz * o[3]);
+    const float yb = (1.f - ty) * ((1.f - tz) * o[4] + tz * o[5]) + ty * ((1.f - tz) * o[6] + tz * o[7]);
     return (1.f - tx) * ya + tx * yb;
 }
 
-__device__ __forceinline__ void gather3q(const float4* qx, const float4* qy, const float4* qz, int nx, int ny, int nz,
+__device__ __forceinline__ void gather3o(const float* ox, const float* oy, const float* oz, int nx, int ny, int nz,
                                          float X0, float X1, float X2, float& e0, float& e1, float& e2) {
-    e0 = trilerp_q(qx, nx, ny, nz, X0, X1 + 0.5f, X2 + 0.5f);
-    e1 = trilerp_q(qy, nx, ny, nz, X0 + 0.5f, X1, X2 + 0.5f);
-    e2 = trilerp_q(qz, nx, ny, nz, X0 + 0.5f, X1 + 0.5f, X2);
+    e0 = trilerp_o(ox, nx, ny, nz, X0, X1 + 0.5f, X2 + 0.5f);
+    e1 = trilerp_o(oy, nx, ny, nz, X0 + 0.5f, X1, X2 + 0.5f);
+    e2 = trilerp_o(oz, nx, ny, nz, X0 + 0.5f, X1 + 0.5f, X2);
 }
 
 __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const double* __restrict__ xp,
@@ -900,64 +1242,300 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
     }
 }
 
-template <bool VEC>
-__device__ __forceinline__ void kick32_body(double* __restrict__ rp, const float* __restrict__ X,
-                                            const float4* __restrict__ qx, const float4* __restrict__ qy,
-                                            const float4* __restrict__ qz, const KickParams& kp, const ScState* st,
-                                            VBlk vb) {
-    if (st->status) return;
-    const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
+// per-kick constants of the FP32 gather + kick, loaded once per thread
+struct Kick32C {
     float T[3][3];
+    float kxyg, kz, ipref, m2;
+    float gamref, betaref, igrbr2, pref, m;
+    float isf[3], of[3];  // 1/steps (times gamma0 along z), X_off
+    const float *ox, *oy, *oz;
+};
+__device__ __forceinline__ Kick32C kick32_const(const ScState* st, const KickParams& kp, const float* ox,
+                                                const float* oy, const float* oz) {
+    Kick32C c;
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) T[i][j] = st->Tf[i][j];
-    const float g0 = st->g0f, kxy = st->kxyf, kz = st->kzf;
-    const float ipref = kp.ipref_f, m2 = kp.m2_f;
-    PAIR_LOOP_BEGIN(n)
-    double r[6][2];
-    for (int k = 0; k < 6; ++k) ld_row(rp + k * ld, i0_, pair_, r[k][0], r[k][1]);
-    float xg[3][2];
-    for (int j = 0; j < 3; ++j) ld_rowf(X + j * nX, i0_, pair_, xg[j][0], xg[j][1]);
-    float o[6][2];
-    for (int w = 0; w < W_; ++w) {
-        float e0, e1, e2;
-        gather3q(qx, qy, qz, kp.nx, kp.ny, kp.nz, xg[0][w], xg[1][w], xg[2][w], e0, e1, e2);
-        const float d0 = kxy * e0 * g0, d1 = kxy * e1 * g0, d2 = kz * e2;  // kick in the beam frame
-        const float dpx = T[0][0] * d0 + T[0][1] * d1 + T[0][2] * d2;
-        const float dpy = T[1][0] * d0 + T[1][1] * d1 + T[1][2] * d2;
-        const float dpz = T[2][0] * d0 + T[2][1] * d1 + T[2][2] * d2;
-        float px, py, pz, E;
-        mom32(d2f(r[1][w]), d2f(r[3][w]), d2f(r[5][w]), kp, px, py, pz, E);
-        const float pxn = px + dpx, pyn = py + dpy, pzn = pz + dpz;
-        const float En = sqrtf(pxn * pxn + pyn * pyn + pzn * pzn + m2);
-        const float dE = (2.0f * (px * dpx + py * dpy + pz * dpz) + (dpx * dpx + dpy * dpy + dpz * dpz)) / (E + En);
-        const float tau = d2f(r[4][w]);
-        // pz E' - pz' E without cancellation (it is suppressed by 1/gamma^2):
-        //   = [pz^2 dT - dpz (pz + pz') (m^2 + pT^2)] / (pz E' + pz' E),
-        //   dT = |pT'|^2 - |pT|^2
-        const float pT2 = px * px + py * py;
-        const float dT = 2.0f * (px * dpx + py * dpy) + dpx * dpx + dpy * dpy;
-        const float fz = (pz * pz * dT - dpz * (pz + pzn) * (m2 + pT2)) / (pz * En + pzn * E);
-        const float dtau = tau * fz / (E * pzn);
-        const float iEE = 1.0f / (E * En);
-        const float dx = tau * (dpx * E - px * dE) * iEE + (pxn / En) * dtau;
-        const float dy = tau * (dpy * E - py * dE) * iEE + (pyn / En) * dtau;
-        o[0][w] = dx;
-        o[1][w] = dpx * ipref;
-        o[2][w] = dy;
-        o[3][w] = dpy * ipref;
-        o[4][w] = dtau;
-        o[5][w] = dE * ipref;
+        for (int j = 0; j < 3; ++j) c.T[i][j] = st->Tf[i][j];
+    c.kxyg = st->kxyf * st->g0f;
+    c.kz = st->kzf;
+    c.ipref = kp.ipref_f;
+    c.m2 = kp.m2_f;
+    c.gamref = kp.gamref_f;
+    c.betaref = kp.betaref_f;
+    c.igrbr2 = (float)(1.0 / (kp.grbr * kp.grbr));
+    c.pref = kp.pref_f;
+    c.m = kp.m_f;
+    for (int j = 0; j < 3; ++j) {
+        c.isf[j] = st->istepsf[j];
+        c.of[j] = st->xofff[j];
     }
-    // the only FP64 arithmetic: six additions into the float64 coordinates
-    for (int k = 0; k < 6; ++k) st_row(rp + k * ld, i0_, pair_, r[k][0] + f2d(o[k][0]), r[k][1] + f2d(o[k][1]));
-    PAIR_LOOP_END
+    c.isf[2] *= st->g0f;
+    c.ox = ox;
+    c.oy = oy;
+    c.oz = oz;
+    return c;
 }
 
-template <bool VEC>
-__global__ void __launch_bounds__(PT, 4) k_kick32(double* __restrict__ rp, const float* __restrict__ X,
-                                                  const float4* __restrict__ qx, const float4* __restrict__ qy,
-                                                  const float4* __restrict__ qz, KickParams kp, const ScState* st) {
-    kick32_body<VEC>(rp, X, qx, qy, qz, kp, st, hw_vblk());
+// the hardware's approximate reciprocal and square root (relative error
+// ~1e-7, far inside the FP32 form's error budget)
+__device__ __forceinline__ float rcpf(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sqrtf_fast(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
+
+// Trilinear sample coordinate along one axis of length n (map_coordinates
+// order=1, mode='constant'): valid iff 0 <= c <= n-1; base cell min(floor c,
+// n-2) and weight c - base.
+struct AxisW {
+    int i;
+    float t;
+    bool ok;
+};
+__device__ __forceinline__ AxisW axis_w(float c, int n) {
+    AxisW a;
+    a.ok = c >= 0.f && c <= (float)(n - 1);
+    int i = (int)c;
+    a.i = i > n - 2 ? n - 2 : i;
+    a.t = c - (float)a.i;
+    return a;
+}
+// one staggered field component from its octs at (ax, ay, az)
+__device__ __forceinline__ float oct_sample(const float* __restrict__ O, const AxisW& ax, const AxisW& ay,
+                                            const AxisW& az, int ny, int nz) {
+    if (!(ax.ok && ay.ok && az.ok)) return 0.f;
+    const float* p = O + 8 * ((ax.i * ny + ay.i) * nz + az.i);  // < 2^31: meshes have at most 256^3 cells
+    float o[8];
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(o[0]), "=f"(o[1]), "=f"(o[2]), "=f"(o[3]), "=f"(o[4]), "=f"(o[5]), "=f"(o[6]), "=f"(o[7])
+        : "l"(p));
+    const float y0 = lerpf(lerpf(o[0], o[1], az.t), lerpf(o[2], o[3], az.t), ay.t);
+    const float y1 = lerpf(lerpf(o[4], o[5], az.t), lerpf(o[6], o[7], az.t), ay.t);
+    return lerpf(y0, y1, ax.t);
+}
+
+// FP32 gather + kick of one particle, r = its six float64 coordinates,
+// updated in place.  The momenta, the rotated grid coordinates and the kick
+// are recomputed from r in FP32 with fused multiply-adds and the hardware's
+// approximate reciprocal and square root, so the kick reads nothing per
+// particle but rparticles.  (The NGP keys, which must equal the FP64 form's,
+// are decided by the keys kernel alone; the gather only needs the grid
+// coordinates to FP32 accuracy.)
+__device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp) {
+    (void)kp;
+    // momenta (eV/c) and energy (eV), coord_transform.py:64-72: gamma from
+    // delta, |p|^2 = (gamma^2 - 1) m^2, pz from |p|^2 - px^2 - py^2
+    const float xq = d2f(r[1]), yq = d2f(r[3]), dl = d2f(r[5]);
+    const float gamma = C.gamref * fmaf(C.betaref, dl, 1.0f);
+    const float g2 = fmaf(gamma, gamma, -1.0f) * C.igrbr2;
+    const float pz2 = sqrtf_fast(g2 - fmaf(xq, xq, yq * yq));
+    const float px = xq * C.pref, py = yq * C.pref, pz = pz2 * C.pref, E = gamma * C.m;
+    // lab position (coord_transform.py:89-95), rotated and scaled to the grid
+    const float tau = d2f(r[4]);
+    const float iE = rcpf(E);
+    const float s = tau * iE;
+    const float l0 = fmaf(-px, s, d2f(r[0])), l1 = fmaf(-py, s, d2f(r[2])), l2 = -pz * s;
+    float X[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+        X[j] = fmaf(fmaf(l0, C.T[0][j], fmaf(l1, C.T[1][j], l2 * C.T[2][j])), C.isf[j], -C.of[j]);
+    // staggered trilinear gather (sc.py:201-204): each component is sampled
+    // at +0.5 on the two axes it is not differentiated along
+    const AxisW a0 = axis_w(X[0], kp.nx), a1 = axis_w(X[1], kp.ny), a2 = axis_w(X[2], kp.nz);
+    const AxisW b0 = axis_w(X[0] + 0.5f, kp.nx), b1 = axis_w(X[1] + 0.5f, kp.ny), b2 = axis_w(X[2] + 0.5f, kp.nz);
+    const float e0 = oct_sample(C.ox, a0, b1, b2, kp.ny, kp.nz);
+    const float e1 = oct_sample(C.oy, b0, a1, b2, kp.ny, kp.nz);
+    const float e2 = oct_sample(C.oz, b0, b1, a2, kp.ny, kp.nz);
+    // kick in the beam frame, rotated back to the lab (sc.py:244-250)
+    const float d0 = C.kxyg * e0, d1 = C.kxyg * e1, d2 = C.kz * e2;
+    const float dpx = fmaf(C.T[0][0], d0, fmaf(C.T[0][1], d1, C.T[0][2] * d2));
+    const float dpy = fmaf(C.T[1][0], d0, fmaf(C.T[1][1], d1, C.T[1][2] * d2));
+    const float dpz = fmaf(C.T[2][0], d0, fmaf(C.T[2][1], d1, C.T[2][2] * d2));
+    const float pxn = px + dpx, pyn = py + dpy, pzn = pz + dpz;
+    const float En = sqrtf_fast(fmaf(pxn, pxn, fmaf(pyn, pyn, fmaf(pzn, pzn, C.m2))));
+    const float iEn = rcpf(En);
+    const float pdp = fmaf(px, dpx, fmaf(py, dpy, pz * dpz));
+    const float dp2 = fmaf(dpx, dpx, fmaf(dpy, dpy, dpz * dpz));
+    const float dE = fmaf(2.0f, pdp, dp2) * rcpf(E + En);
+    // pz E' - pz' E without cancellation (it is suppressed by 1/gamma^2):
+    //   = [pz^2 dT - dpz (pz + pz') (m^2 + pT^2)] / (pz E' + pz' E),
+    //   dT = |pT'|^2 - |pT|^2
+    const float pT2 = fmaf(px, px, py * py);
+    const float dT = fmaf(2.0f, fmaf(px, dpx, py * dpy), fmaf(dpx, dpx, dpy * dpy));
+    const float fz = fmaf(pz * pz, dT, -dpz * (pz + pzn) * (C.m2 + pT2)) * rcpf(fmaf(pz, En, pzn * E));
+    const float dtau = tau * fz * iE * rcpf(pzn);
+    const float iEE = iE * iEn;
+    // new MAD coordinates as increments (coord_transform.py:16-54)
+    const float dx = fmaf(tau * fmaf(dpx, E, -px * dE), iEE, pxn * iEn * dtau);
+    const float dy = fmaf(tau * fmaf(dpy, E, -py * dE), iEE, pyn * iEn * dtau);
+    // the only FP64 arithmetic: six additions into the float64 coordinates
+    r[0] += f2d(dx);
+    r[1] += f2d(dpx * C.ipref);
+    r[2] += f2d(dy);
+    r[3] += f2d(dpy * C.ipref);
+    r[4] += f2d(dtau);
+    r[5] += f2d(dE * C.ipref);
+}
+
+// Gather + kick with direct row accesses: each thread takes G consecutive
+// particles with one 32-byte (G = 4) or 16-byte (G = 2) access per row.
+template <int G>
+__device__ __forceinline__ void kick32_body(double* __restrict__ rp, const float* __restrict__ ox,
+                                            const float* __restrict__ oy, const float* __restrict__ oz,
+                                            const KickParams& kp, const ScState* st, VBlk vb) {
+    if (st->status) return;
+    const int64_t n = kp.n, ld = kp.ld;
+    const Kick32C C = kick32_const(st, kp, ox, oy, oz);
+    GROUP_LOOP_BEGIN(n, G)
+    double r[6][G];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) ld_rows<G>(rp + k * ld, i0_, full_, r[k]);
+#pragma unroll
+    for (int w = 0; w < G; ++w) {
+        if (w >= W_) break;
+        double x[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) x[k] = r[k][w];
+        kick_one(x, C, kp);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) r[k][w] = x[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) st_rows<G>(rp + k * ld, i0_, full_, r[k]);
+    GROUP_LOOP_END
+}
+
+// Gather + kick with the rows staged through shared memory by bulk (TMA)
+// copies.  A block walks its tiles of KT_TILE particles (tiles vb.x,
+// vb.x + vb.nx, ...); KT_STAGES tile buffers of the six rows rotate: while
+// the block kicks one tile, the loads of the next KT_STAGES - 1 are in
+// flight, so the HBM stream does not wait for the gathers.  Each thread
+// kicks particles 2t and 2t+1 of a tile in place in shared memory, and one
+// bulk store per row writes the tile back.  Rows must be 16-byte aligned
+// with an even stride.  A tile's copies cover its first (count & ~1)
+// particles; an odd last particle of the beam is read and written directly.
+constexpr int KT_TILE = 512;
+constexpr int KT_STAGES = 3;
+constexpr size_t KT_SMEM = (size_t)KT_STAGES * 6 * KT_TILE * sizeof(double) + KT_STAGES * sizeof(uint64_t);
+
+__device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const float* __restrict__ ox,
+                                                const float* __restrict__ oy, const float* __restrict__ oz,
+                                                const KickParams& kp, ScState* st, VBlk vb) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    if (__syncthreads_or(st->status != SC_OK)) return;
+    double* buf = reinterpret_cast<double*>(smraw);  // [KT_STAGES][6][KT_TILE]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + KT_STAGES * 6 * KT_TILE);
+    const int64_t n = kp.n, ld = kp.ld;
+    const int64_t ntile = (n + KT_TILE - 1) / KT_TILE;
+    const int64_t mine = vb.x < ntile ? (ntile - 1 - vb.x) / vb.nx + 1 : 0;  // this block's tiles
+    const bool lead = threadIdx.x == 0;
+    if (lead) {
+        for (int s = 0; s < KT_STAGES; ++s) mbar_init(&bar[s], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    auto tile_start = [&](int64_t t) { return (vb.x + t * vb.nx) * (int64_t)KT_TILE; };
+    auto tile_count = [&](int64_t t) {
+        const int64_t c = n - tile_start(t);
+        return (int)(c < KT_TILE ? c : KT_TILE);
+    };
+    auto issue = [&](int64_t t) {  // lead thread: the loads of local tile t
+        const int s = (int)(t % KT_STAGES);
+        const int64_t i0 = tile_start(t);
+        const unsigned bytes = (unsigned)(tile_count(t) & ~1) * 8u;
+        mbar_arrive_expect_tx(&bar[s], 6u * bytes);
+        if (bytes)
+            for (int k = 0; k < 6; ++k) bulk_load(buf + (s * 6 + k) * KT_TILE, rp + k * ld + i0, bytes, &bar[s]);
+    };
+    int64_t issued = mine < KT_STAGES ? mine : KT_STAGES;
+    if (lead)
+        for (int64_t t = 0; t < issued; ++t) issue(t);
+    const Kick32C C = kick32_const(st, kp, ox, oy, oz);
+    int64_t t = 0;
+    bool failed = false;
+    for (; t < mine; ++t) {
+        const int s = (int)(t % KT_STAGES);
+        const int64_t i0 = tile_start(t);
+        const int cnt = tile_count(t), staged = cnt & ~1;
+        const bool ok = mbar_wait(&bar[s], (unsigned)((t / KT_STAGES) & 1));
+        double* B = buf + s * 6 * KT_TILE;
+        const int j = 2 * threadIdx.x;
+        if (j + 1 < staged) {  // both particles staged: 16-byte shared accesses
+            double r[2][6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const double2 v = *reinterpret_cast<const double2*>(B + k * KT_TILE + j);
+                r[0][k] = v.x;
+                r[1][k] = v.y;
+            }
+            kick_one(r[0], C, kp);
+            kick_one(r[1], C, kp);
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                *reinterpret_cast<double2*>(B + k * KT_TILE + j) = make_double2(r[0][k], r[1][k]);
+        } else if (j < cnt) {  // the odd last particle of the beam (j == staged): read and written directly
+            double r[6];
+            for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i0 + j];
+            kick_one(r, C, kp);
+            for (int k = 0; k < 6; ++k) rp[k * ld + i0 + j] = r[k];
+        }
+        fence_async_smem();
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        if (lead) {
+            if (staged)
+                for (int k = 0; k < 6; ++k) bulk_store(rp + k * ld + i0, B + k * KT_TILE, (unsigned)staged * 8u);
+            bulk_commit();
+            // refill the previous tile's buffer once its store has read it
+            if (t >= 1 && issued < mine) {
+                bulk_wait_read<1>();
+                issue(issued);
+                ++issued;
+            }
+        }
+    }
+    if (lead) {
+        if (failed) {
+            atomicCAS(&st->status, SC_OK, SC_ERR_TIMEOUT);
+            for (int64_t u = t; u < issued; ++u)  // loads still in flight must land before the block exits
+                mbar_wait(&bar[u % KT_STAGES], (unsigned)((u / KT_STAGES) & 1));
+        }
+        bulk_wait_all();
+    }
+}
+
+constexpr int KICK_MIN_BLOCKS = 3;  // blocks per SM the kick kernels are compiled for
+
+template <int G>
+__global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) k_kick32(double* __restrict__ rp, const float* __restrict__ ox,
+                                                                const float* __restrict__ oy,
+                                                                const float* __restrict__ oz, KickParams kp,
+                                                                const ScState* st) {
+    kick32_body<G>(rp, ox, oy, oz, kp, st, hw_vblk());
+}
+
+__global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) k_kick32_tma(double* __restrict__ rp,
+                                                                    const float* __restrict__ ox,
+                                                                    const float* __restrict__ oy,
+                                                                    const float* __restrict__ oz, KickParams kp,
+                                                                    ScState* st) {
+    kick32_tma_body(rp, ox, oy, oz, kp, st, hw_vblk());
+}
+
+// particles per row access the kick can use: 4 with 32-byte aligned rows and
+// a row stride that is a multiple of 4, 2 with 16-byte alignment and an even
+// stride, else 1
+__host__ __device__ __forceinline__ int kick_group(const double* rp, int64_t ld) {
+    if ((uintptr_t)rp % 32 == 0 && ld % 4 == 0) return 4;
+    if ((uintptr_t)rp % 16 == 0 && ld % 2 == 0) return 2;
+    return 1;
 }
 
 template <typename R>
@@ -970,8 +1548,8 @@ __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, cons
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         R e0, e1, e2;
         if (sizeof(R) == 4)
-            gather3q(reinterpret_cast<const float4*>(ex), reinterpret_cast<const float4*>(ey),
-                     reinterpret_cast<const float4*>(ez), kp.nx, kp.ny, kp.nz, (float)X[i], (float)X[nX + i],
+            gather3o(reinterpret_cast<const float*>(ex), reinterpret_cast<const float*>(ey),
+                     reinterpret_cast<const float*>(ez), kp.nx, kp.ny, kp.nz, (float)X[i], (float)X[nX + i],
                      (float)X[2 * nX + i], *reinterpret_cast<float*>(&e0), *reinterpret_cast<float*>(&e1),
                      *reinterpret_cast<float*>(&e2));
         else
@@ -994,11 +1572,11 @@ __global__ void __launch_bounds__(PT, 4) kb_frame32(const BatchBeam* __restrict_
     double* part = reinterpret_cast<double*>(B.ws + B.L.part_frame);
     unsigned long long* qz = reinterpret_cast<unsigned long long*>(B.ws + B.L.qfix);
     const int64_t nc = (int64_t)B.p.nx * B.p.ny * B.p.nz;
-    if (B.vec_rp) frame32_body<true>(B.rp, B.kp, part, st, qz, nc, vb);
+    if (B.vec_rp) frame32_tma_body(B.rp, B.kp, part, st, qz, nc, vb);
     else frame32_body<false>(B.rp, B.kp, part, st, qz, nc, vb);
 }
 
-__global__ void __launch_bounds__(PT, 4) kb_extent32(const BatchBeam* __restrict__ beams,
+__global__ void __launch_bounds__(PT, 3) kb_extent32(const BatchBeam* __restrict__ beams,
                                                      const int* __restrict__ start, int nb) {
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
@@ -1006,7 +1584,7 @@ __global__ void __launch_bounds__(PT, 4) kb_extent32(const BatchBeam* __restrict
     ScState* st = reinterpret_cast<ScState*>(B.ws + B.L.state);
     float* X = reinterpret_cast<float*>(B.ws + B.L.X);
     double* part = reinterpret_cast<double*>(B.ws + B.L.part_ext);
-    if (B.vec_rpq) extent32_body<true>(B.rp, B.q, B.kp, X, part, st, vb);
+    if (B.vec_rpq) extent32_tma_body(B.rp, B.q, B.kp, X, part, st, vb);
     else extent32_body<false>(B.rp, B.q, B.kp, X, part, st, vb);
 }
 
@@ -1019,32 +1597,31 @@ __global__ void __launch_bounds__(PT, 4) kb_keys32(const BatchBeam* __restrict__
     float* X = reinterpret_cast<float*>(B.ws + B.L.X);
     uint32_t* keys = reinterpret_cast<uint32_t*>(B.ws + B.L.keys);
     unsigned long long* qfix = reinterpret_cast<unsigned long long*>(B.ws + B.L.qfix);
-    if (B.vec_rpq) keys32_body<true>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
+    if ((uintptr_t)B.q % 16 == 0) keys32_body<true>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
     else keys32_body<false>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
 }
 
-__global__ void __launch_bounds__(PT, 4) kb_kick32(const BatchBeam* __restrict__ beams,
-                                                   const int* __restrict__ start, int nb) {
+__global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) kb_kick32(const BatchBeam* __restrict__ beams,
+                                                                 const int* __restrict__ start, int nb) {
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
     const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
-    const ScState* st = reinterpret_cast<const ScState*>(B.ws + B.L.state);
-    const float* X = reinterpret_cast<const float*>(B.ws + B.L.X);
-    const float4* qx = reinterpret_cast<const float4*>(B.ws + B.L.exq);
-    const float4* qy = reinterpret_cast<const float4*>(B.ws + B.L.eyq);
-    const float4* qz = reinterpret_cast<const float4*>(B.ws + B.L.ezq);
-    if (B.vec_rp) kick32_body<true>(B.rp, X, qx, qy, qz, B.kp, st, vb);
-    else kick32_body<false>(B.rp, X, qx, qy, qz, B.kp, st, vb);
+    ScState* st = reinterpret_cast<ScState*>(B.ws + B.L.state);
+    const float* ox = reinterpret_cast<const float*>(B.ws + B.L.exq);
+    const float* oy = reinterpret_cast<const float*>(B.ws + B.L.eyq);
+    const float* oz = reinterpret_cast<const float*>(B.ws + B.L.ezq);
+    if (kick_group(B.rp, B.kp.ld) >= 2) kick32_tma_body(B.rp, ox, oy, oz, B.kp, st, vb);
+    else kick32_body<1>(B.rp, ox, oy, oz, B.kp, st, vb);
 }
 
 cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, const int* start, int nb, int blocks,
                                    cudaStream_t s) {
     if (blocks <= 0) return cudaSuccess;
     switch (k) {
-        case BP_FRAME: kb_frame32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
-        case BP_EXTENT: kb_extent32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
+        case BP_FRAME: kb_frame32<<<blocks, PT, FR_SMEM, s>>>(beams, start, nb); break;
+        case BP_EXTENT: kb_extent32<<<blocks, PT, EX_SMEM, s>>>(beams, start, nb); break;
         case BP_KEYS: kb_keys32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
-        case BP_KICK: kb_kick32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
+        case BP_KICK: kb_kick32<<<blocks, PT, KT_SMEM, s>>>(beams, start, nb); break;
     }
     return cudaGetLastError();
 }
@@ -1052,14 +1629,28 @@ cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, co
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+cudaError_t prepare_particle_kernels() {
+    cudaError_t e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(k_kick32_tma), KT_SMEM))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_kick32), KT_SMEM))) return e;
+    if ((e = set_smem(k_frame32_tma, FR_SMEM))) return e;
+    if ((e = set_smem(kb_frame32, FR_SMEM))) return e;
+    if ((e = set_smem(k_extent32_tma, EX_SMEM))) return e;
+    return set_smem(kb_extent32, EX_SMEM);
+}
+
 // 16-byte row accesses need 16-byte aligned rows and an even row stride
 static bool vec_ok(const double* rp, int64_t ld, const double* q) {
     return ((uintptr_t)rp % 16 == 0) && (ld % 2 == 0) && (q == nullptr || (uintptr_t)q % 16 == 0);
 }
 
+// blocks of the frame, extent and keys stages: one per tile of PT_TILE
+// particles, at most three per SM (each walks its tiles with the loads of
+// the next one in flight)
 static int particle_blocks(const Plan& p, int64_t n) {
-    int64_t b = (n + PT - 1) / PT;
-    if (b > p.part_blocks) b = p.part_blocks;
+    int64_t b = (n + PT_TILE - 1) / PT_TILE;
+    const int64_t cap = 3 * (int64_t)p.sm_count;
+    if (b > cap) b = cap;
     return (int)(b > 0 ? b : 1);
 }
 
@@ -1073,7 +1664,7 @@ cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickPar
     if (p.prec == SC_FP64)
         k_frame64<<<nb, PT, 0, s>>>(rp, kp, reinterpret_cast<double*>(ws + L.xp), part, st);
     else
-        vec_ok(rp, kp.ld, nullptr) ? k_frame32<true><<<nb, PT, 0, s>>>(rp, kp, part, st)
+        vec_ok(rp, kp.ld, nullptr) ? k_frame32_tma<<<nb, PT, FR_SMEM, s>>>(rp, kp, part, st)
                                    : k_frame32<false><<<nb, PT, 0, s>>>(rp, kp, part, st);
     return cudaGetLastError();
 }
@@ -1087,8 +1678,9 @@ cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickPa
         k_extent64<<<nb, PT, 0, s>>>(reinterpret_cast<const double*>(ws + L.xp), q, kp,
                                      reinterpret_cast<double*>(ws + L.X), part, st);
     else
-        vec_ok(rp, kp.ld, q) ? k_extent32<true><<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st)
-                             : k_extent32<false><<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
+        vec_ok(rp, kp.ld, q)
+            ? k_extent32_tma<<<nb, PT, EX_SMEM, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st)
+            : k_extent32<false><<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
     return cudaGetLastError();
 }
 
@@ -1126,7 +1718,7 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
             cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
             if (e) return e;
         }
-        if (vec_ok(rp ? rp : reinterpret_cast<const double*>(ws), rp ? kp.ld : 0, q))
+        if (!qfix || (uintptr_t)q % 16 == 0)
             k_keys32<true><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
         else
             k_keys32<false><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
@@ -1145,12 +1737,17 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
                                    kp, st);
     else
     {
-        const float* X = reinterpret_cast<const float*>(ws + L.X);
-        const float4* qx = reinterpret_cast<const float4*>(ws + L.exq);
-        const float4* qy = reinterpret_cast<const float4*>(ws + L.eyq);
-        const float4* qz = reinterpret_cast<const float4*>(ws + L.ezq);
-        if (vec_ok(rp, kp.ld, nullptr)) k_kick32<true><<<nb, PT, 0, s>>>(rp, X, qx, qy, qz, kp, st);
-        else k_kick32<false><<<nb, PT, 0, s>>>(rp, X, qx, qy, qz, kp, st);
+        const float* ox = reinterpret_cast<const float*>(ws + L.exq);
+        const float* oy = reinterpret_cast<const float*>(ws + L.eyq);
+        const float* oz = reinterpret_cast<const float*>(ws + L.ezq);
+        const int g = kick_group(rp, kp.ld);
+        // one wave of resident blocks, each looping over its tiles or groups
+        const int64_t units = g >= 2 ? (kp.n + KT_TILE - 1) / KT_TILE : (kp.n + PT - 1) / PT;
+        const int64_t kb = units < (int64_t)p.sm_count * KICK_MIN_BLOCKS ? units : (int64_t)p.sm_count * KICK_MIN_BLOCKS;
+        const int nbk = (int)(kb > 0 ? kb : 1);
+        ScState* stw = reinterpret_cast<ScState*>(ws + L.state);
+        if (g >= 2) k_kick32_tma<<<nbk, PT, KT_SMEM, s>>>(rp, ox, oy, oz, kp, stw);
+        else k_kick32<1><<<nbk, PT, 0, s>>>(rp, ox, oy, oz, kp, st);
     }
     return cudaGetLastError();
 }
