@@ -238,6 +238,9 @@ int sc_profile_enable(sc_plan* plan, int enable);
  * last profiled sc_kick, and the number of kernels that call launched. */
 int sc_profile_read(sc_plan* plan, float* ms /* [SC_NSTAGES] */, int* n_launches);
 const char* sc_profile_stage_name(int stage);
+/* Number of kernels the plan's last sc_kick launched (host bookkeeping, no
+ * synchronisation). */
+int sc_kick_launches(const sc_plan* plan);
 
 /* ---- misc -------------------------------------------------------------- */
 const char* sc_last_error(void);

@@ -74,6 +74,7 @@ SIGNATURES = {
     "sc_profile_enable": (C.c_int, [vp, C.c_int]),
     "sc_profile_read": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     "sc_profile_stage_name": (C.c_char_p, [C.c_int]),
+    "sc_kick_launches": (C.c_int, [vp]),
     "sc_last_error": (C.c_char_p, []),
     "sc_abi_version": (C.c_int, []),
 }

@@ -132,6 +132,7 @@ Layout make_layout(const Plan& p, int64_t n) {
 
 template <typename R>
 __global__ void k_init_ws(ScState* st, Cx<R>* tx, int Mx, Cx<R>* ty, int My, Cx<R>* tz, int Mz) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         memset(st, 0, sizeof(ScState));
@@ -149,16 +150,17 @@ cudaError_t launch_init_workspace(const Plan& p, const Layout& L, char* ws, cuda
     m = m > p.Mz ? m : p.Mz;
     ScState* st = reinterpret_cast<ScState*>(ws + L.state);
     if (p.prec == SC_FP64)
-        k_init_ws<double><<<(m + 255) / 256, 256, 0, s>>>(st, (double2*)(ws + L.tw_x), p.Mx, (double2*)(ws + L.tw_y),
+        launch(k_init_ws<double>, (m + 255) / 256, 256, 0, s, st, (double2*)(ws + L.tw_x), p.Mx, (double2*)(ws + L.tw_y),
                                                           p.My, (double2*)(ws + L.tw_z), p.Mz);
     else
-        k_init_ws<float><<<(m + 255) / 256, 256, 0, s>>>(st, (float2*)(ws + L.tw_x), p.Mx, (float2*)(ws + L.tw_y),
+        launch(k_init_ws<float>, (m + 255) / 256, 256, 0, s, st, (float2*)(ws + L.tw_x), p.Mx, (float2*)(ws + L.tw_y),
                                                          p.My, (float2*)(ws + L.tw_z), p.Mz);
     return cudaGetLastError();
 }
 
 template <typename A, typename B>
 __global__ void k_convert(const A* __restrict__ a, B* __restrict__ b, size_t n) {
+    pdl_wait();
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         b[i] = (B)a[i];
 }
@@ -264,6 +266,7 @@ static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energ
     kp.ipref_f = (float)(1.0 / kp.pref);
     kp.m_f = (float)kp.m_e_eV;
     kp.m2_f = kp.m_f * kp.m_f;
+    kp.igrbr2_f = (float)(1.0 / (kp.grbr * kp.grbr));
     return kp;
 }
 
@@ -309,7 +312,11 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(prepare_particle_kernels(), "kernel attributes");
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
-    SC_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
+    // the Green's-function branch runs at the highest priority: its FP64
+    // blocks take their SM slots first and the keys kernel fills the rest
+    int prio_lo = 0, prio_hi = 0;
+    SC_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi), "cudaDeviceGetStreamPriorityRange");
+    SC_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio_hi), "cudaStreamCreate");
     SC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
     SC_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
     sc_plan* h = new (std::nothrow) sc_plan;
@@ -368,6 +375,8 @@ int sc_profile_read(sc_plan* plan, float* ms, int* n_launches) {
     if (n_launches) *n_launches = plan->last_launches;
     return SC_OK;
 }
+
+int sc_kick_launches(const sc_plan* plan) { return plan ? plan->last_launches : 0; }
 
 const char* sc_profile_stage_name(int stage) {
     return (stage >= 0 && stage < SC_NSTAGES) ? kStageNames[stage] : "";
@@ -562,9 +571,9 @@ int sc_potential(sc_plan* plan, void* ws_v, size_t ws_bytes, const double* qgrid
         SC_CUDA(launch_convolve(p, L, ws, qgrid, phi, s), "convolve");
     } else {
         const size_t ncell = (size_t)p.nx * p.ny * p.nz;
-        k_convert<double, float><<<p.sm_count * 4, 256, 0, s>>>(qgrid, reinterpret_cast<float*>(ws + L.qgrid), ncell);
+        launch(k_convert<double, float>, p.sm_count * 4, 256, 0, s, qgrid, reinterpret_cast<float*>(ws + L.qgrid), ncell);
         SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s), "convolve");
-        k_convert<float, double><<<p.sm_count * 4, 256, 0, s>>>(reinterpret_cast<float*>(ws + L.phi), phi, ncell);
+        launch(k_convert<float, double>, p.sm_count * 4, 256, 0, s, reinterpret_cast<float*>(ws + L.phi), phi, ncell);
         SC_CUDA(cudaGetLastError(), "convert");
     }
     return SC_OK;
@@ -647,7 +656,9 @@ int sc_batch_create(sc_batch** out, int max_beams) {
     cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&b->h_buf), b->beams_bytes + b->start_bytes);
     if (!e) e = cudaMalloc(reinterpret_cast<void**>(&b->d_buf), b->beams_bytes + b->start_bytes);
     if (!e) e = cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming);
-    if (!e) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    int prio_lo = 0, prio_hi = 0;
+    if (!e) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (!e) e = cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, prio_hi);
     if (!e) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
     if (e) {

@@ -105,6 +105,7 @@ struct KickParams {
     double four_pi_eps0;                 // 4*pi*epsilon_0
     // FP32 copies for the FP32 form
     float gamref_f, betaref_f, grbr_f, pref_f, ipref_f, m_f, m2_f;
+    float igrbr2_f;                      // 1/(gamref*betaref)^2
 };
 
 // ---------------------------------------------------------------------------
@@ -117,6 +118,11 @@ struct RadixPlan {
     int r[MAX_STAGES];
 };
 bool make_radix_plan(int L, RadixPlan* p);
+// Line stride (in complex elements) of every FFT line buffer in shared
+// memory: room for the padded layout of the intermediate Stockham stages
+// (element i at i + i/8) plus one element, so that lines start on
+// different banks
+__host__ __device__ constexpr int fft_ls(int L) { return L + L / 8 + 1; }
 int choose_fft_length(int n);  // smallest supported length >= 2n-1, 0 if none
 
 // ---------------------------------------------------------------------------
@@ -295,6 +301,29 @@ cudaError_t prepare_batch_fft();
 cudaError_t prepare_batch_green();
 
 inline size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+
+// Programmatic dependent launch: every kernel of this library is launched
+// with launch(), which lets its blocks be scheduled while the previous
+// kernel of the stream drains, and begins with pdl_wait(), which holds it
+// until that kernel has completed and its memory writes are visible.  (A
+// kernel launched without the attribute passes pdl_wait() at once.)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                          Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 // Opt a kernel in to the device's largest dynamic shared memory, once per
 // kernel (a registry keyed by the kernel's address), so that launches made

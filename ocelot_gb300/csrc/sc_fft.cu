@@ -36,7 +36,7 @@ static inline int z_lines_per_block(int Mz) {
 template <typename R>
 static inline int strided_cols(int M) {
     int tk = 16;
-    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + 2 * tk * (M + 1)) > 200 * 1024) tk /= 2;
+    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + 2 * tk * fft_ls(M)) > 200 * 1024) tk /= 2;
     return tk;
 }
 
@@ -50,10 +50,10 @@ __device__ __forceinline__ void zfwd_body(R* __restrict__ q, const long long* __
                                           const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
-    const int Mz = rz.L;
+    const int Mz = rz.L, lz = fft_ls(Mz);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* a = tw + Mz;
-    Cx<R>* b = a + NC * Mz;
+    Cx<R>* b = a + NC * lz;
     load_twiddles<R>(tw, twg, Mz);
     const int x = vb.y;
     const int y0 = vb.x * 2 * NC;
@@ -74,15 +74,15 @@ __device__ __forceinline__ void zfwd_body(R* __restrict__ q, const long long* __
                 if (yb < ny) im = q[ib];
             }
         }
-        a[idx] = cx<R>(re, im);
+        a[c * lz + z] = cx<R>(re, im);
     }
     __syncthreads();
-    Cx<R>* res = fft_lines<R, false>(a, b, Mz, NC, rz, tw);
+    Cx<R>* res = fft_lines<R, false>(a, b, lz, NC, rz, tw);
     for (int idx = threadIdx.x; idx < NC * Kz; idx += blockDim.x) {
         const int c = idx / Kz, k = idx - c * Kz;
         const int ya = y0 + 2 * c, yb = ya + 1;
-        const Cx<R> Z = res[c * Mz + k];
-        const Cx<R> Zm = res[c * Mz + (k == 0 ? 0 : Mz - k)];
+        const Cx<R> Z = res[c * lz + k];
+        const Cx<R> Zm = res[c * lz + (k == 0 ? 0 : Mz - k)];
         const R h = (R)0.5;
         if (!SC_IDX_OK(st, 24, ((long long)x * My + (yb < ny ? yb : ya)) * Kz + k, (long long)vb.ny * My * Kz)) continue;
         if (ya < ny) W[((size_t)x * My + ya) * Kz + k] = cx<R>((Z.x + Zm.x) * h, (Z.y - Zm.y) * h);
@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const l
                                                       Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
                                                       RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
                                                       const ScState* st) {
+    pdl_wait();
     zfwd_body<R>(q, qfix, W, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk());
 }
 
@@ -104,7 +105,7 @@ __device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My
                                            const Cx<R>* __restrict__ twg, int TK, const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
-    const int ls = My + 1;
+    const int ls = fft_ls(My);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* a = tw + My;
     Cx<R>* b = a + TK * ls;
@@ -131,6 +132,7 @@ template <typename R, bool INV>
 __global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int ny, int My, int Kz,
                                                        RadixPlan ry, const Cx<R>* __restrict__ twg,
                                                        int TK, const ScState* st) {
+    pdl_wait();
     ypass_body<R, INV>(W, ny, My, Kz, ry, twg, TK, st, hw_vblk());
 }
 
@@ -142,7 +144,7 @@ __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __res
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mx = rx.L;
-    const int ls = Mx + 1;
+    const int ls = fft_ls(Mx);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* a = tw + Mx;
     Cx<R>* b = a + TK * ls;
@@ -180,6 +182,7 @@ template <typename R>
 __global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, const R* __restrict__ G,
                                                        int nx, int My, int Kz, int Ky, RadixPlan rx,
                                                        const Cx<R>* __restrict__ twg, int TK, const ScState* st) {
+    pdl_wait();
     xconv_body<R>(W, G, nx, My, Kz, Ky, rx, twg, TK, st, hw_vblk());
 }
 
@@ -189,10 +192,10 @@ __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __rest
                                           const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
-    const int Mz = rz.L;
+    const int Mz = rz.L, lz = fft_ls(Mz);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* a = tw + Mz;
-    Cx<R>* b = a + NC * Mz;
+    Cx<R>* b = a + NC * lz;
     load_twiddles<R>(tw, twg, Mz);
     const int x = vb.y;
     const int y0 = vb.x * 2 * NC;
@@ -205,16 +208,16 @@ __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __rest
         if (ya < ny) A = W[((size_t)x * My + ya) * Kz + kk];
         if (yb < ny) B = W[((size_t)x * My + yb) * Kz + kk];
         // Z = A + iB, Hermitian-extended above Mz/2
-        a[idx] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
+        a[c * lz + k] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
     }
     __syncthreads();
-    Cx<R>* res = fft_lines<R, true>(a, b, Mz, NC, rz, tw);
+    Cx<R>* res = fft_lines<R, true>(a, b, lz, NC, rz, tw);
     const double norm = st->phi_norm, denom = st->phi_denom;
     const R fscale = (R)(norm / denom);
     for (int idx = threadIdx.x; idx < NC * nz; idx += blockDim.x) {
         const int c = idx / nz, z = idx - c * nz;
         const int ya = y0 + 2 * c, yb = ya + 1;
-        const Cx<R> v = res[c * Mz + z];
+        const Cx<R> v = res[c * lz + z];
         if (sizeof(R) == 8) {
             // out/(4*pi*eps0*hx*hy*hz) after the 1/M normalisation of ifftn (sc.py:164-167)
             if (ya < ny) phi[((size_t)x * ny + ya) * nz + z] = (R)(((double)v.x * norm) / denom);
@@ -231,6 +234,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ 
                                                       int ny, int nz, int My, int Kz, RadixPlan rz,
                                                       const Cx<R>* __restrict__ twg, int NC,
                                                       const ScState* st) {
+    pdl_wait();
     zinv_body<R>(W, phi, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk());
 }
 
@@ -239,6 +243,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ 
 template <typename R>
 __global__ void k_field_grids(const R* __restrict__ phi, R* __restrict__ ex, R* __restrict__ ey,
                               R* __restrict__ ez, int nx, int ny, int nz, const ScState* st) {
+    pdl_wait();
     if (st->status) return;
     const int j = blockIdx.x, i = blockIdx.y;
     const double hx = st->steps[0], hy = st->steps[1], hz = st->steps[2];
@@ -302,9 +307,171 @@ __device__ __forceinline__ void field_octs_body(const float* __restrict__ phi, f
 
 __global__ void k_field_octs(const float* __restrict__ phi, float* __restrict__ ox, float* __restrict__ oy,
                              float* __restrict__ oz, int nx, int ny, int nz, const ScState* st) {
+    pdl_wait();
     field_octs_body(phi, ox, oy, oz, nx, ny, nz, st, hw_vblk());
 }
 
+
+// ---------------------------------------------------------------------------
+// Plane-fused passes (meshes whose y-by-kz plane fits in shared memory): one
+// block per x plane does the z and y forward transforms (F1 + F2), or the y
+// and z inverse transforms (B2 + B1), keeping the plane in shared memory
+// between them.  The lines go through the same fft_lines code as the
+// separate passes, so the results are identical; the plane saves a kernel
+// launch and a round trip of the work grid per direction.
+// Shared memory: twiddles z and y, then two buffers of Kz y-lines; the z
+// lines use the second buffer (forward) or whichever buffer the y result
+// does not occupy (inverse).
+// ---------------------------------------------------------------------------
+constexpr int PLANE_THREADS = 1024;
+
+template <typename R>
+static size_t plane_smem(const Plan& p) {
+    const int Kz = p.Mz / 2 + 1;
+    return sizeof(Cx<R>) * ((size_t)p.Mz + p.My + 2 * (size_t)Kz * fft_ls(p.My));
+}
+template <typename R>
+static bool plane_fits(const Plan& p, int optin) {
+    const int Kz = p.Mz / 2 + 1, ncz = (p.ny + 1) / 2;
+    return 2 * (size_t)ncz * fft_ls(p.Mz) <= (size_t)Kz * fft_ls(p.My) && plane_smem<R>(p) <= (size_t)optin;
+}
+
+template <typename R>
+__device__ __forceinline__ void zy_fwd_body(R* __restrict__ q, const long long* __restrict__ qfix,
+                                            Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
+                                            const RadixPlan& rz, const RadixPlan& ry, const Cx<R>* __restrict__ twzg,
+                                            const Cx<R>* __restrict__ twyg, const ScState* st, int x, int nx) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if (st->status) return;
+    const int Mz = rz.L, lz = fft_ls(Mz), ly = fft_ls(My), ncz = (ny + 1) / 2;
+    Cx<R>* twz = reinterpret_cast<Cx<R>*>(smraw);
+    Cx<R>* twy = twz + Mz;
+    Cx<R>* A2 = twy + My;
+    Cx<R>* B2 = A2 + Kz * ly;
+    Cx<R>* A1 = B2;
+    Cx<R>* B1 = A1 + ncz * lz;
+    load_twiddles<R>(twz, twzg, Mz);
+    load_twiddles<R>(twy, twyg, My);
+    // F1: two charge rows per complex line (as k_zfwd)
+    for (int idx = threadIdx.x; idx < ncz * Mz; idx += blockDim.x) {
+        const int c = idx / Mz, z = idx - c * Mz;
+        const int ya = 2 * c, yb = ya + 1;
+        R re = 0, im = 0;
+        if (z < nz) {
+            const size_t ia = ((size_t)x * ny + ya) * nz + z, ib = ia + nz;
+            [[maybe_unused]] const long long ncell = (long long)nx * ny * nz;
+            if ((ya < ny && !SC_IDX_OK(st, 25, ia, ncell)) || (yb < ny && !SC_IDX_OK(st, 26, ib, ncell))) continue;
+            if (qfix) {
+                const float u = st->qfix_inv;
+                if (ya < ny) { re = (R)(__ll2float_rn(qfix[ia]) * u); q[ia] = re; }
+                if (yb < ny) { im = (R)(__ll2float_rn(qfix[ib]) * u); q[ib] = im; }
+            } else {
+                if (ya < ny) re = q[ia];
+                if (yb < ny) im = q[ib];
+            }
+        }
+        A1[c * lz + z] = cx<R>(re, im);
+    }
+    __syncthreads();
+    const Cx<R>* res1 = fft_lines<R, false>(A1, B1, lz, ncz, rz, twz);
+    // unpack the two real lines into the y lines (column kz, row y); rows
+    // ny..My-1 are the zero padding of F2
+    for (int idx = threadIdx.x; idx < ncz * Kz; idx += blockDim.x) {
+        const int c = idx / Kz, k = idx - c * Kz;
+        const int ya = 2 * c, yb = ya + 1;
+        const Cx<R> Z = res1[c * lz + k];
+        const Cx<R> Zm = res1[c * lz + (k == 0 ? 0 : Mz - k)];
+        const R h = (R)0.5;
+        A2[k * ly + ya] = cx<R>((Z.x + Zm.x) * h, (Z.y - Zm.y) * h);
+        if (yb < ny) A2[k * ly + yb] = cx<R>((Z.y + Zm.y) * h, (Zm.x - Z.x) * h);
+    }
+    for (int idx = threadIdx.x; idx < Kz * (My - ny); idx += blockDim.x) {
+        const int k = idx / (My - ny), r = idx - k * (My - ny);
+        A2[k * ly + ny + r] = cx<R>(0, 0);
+    }
+    __syncthreads();
+    const Cx<R>* res2 = fft_lines<R, false>(A2, B2, ly, Kz, ry, twy);
+    for (int idx = threadIdx.x; idx < My * Kz; idx += blockDim.x) {
+        const int ky = idx / Kz, k = idx - ky * Kz;
+        W[((size_t)x * My + ky) * Kz + k] = res2[k * ly + ky];
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(PLANE_THREADS) k_zy_fwd(R* __restrict__ q, const long long* __restrict__ qfix,
+                                                          Cx<R>* __restrict__ W, int ny, int nz, int My, int Kz,
+                                                          RadixPlan rz, RadixPlan ry, const Cx<R>* __restrict__ twz,
+                                                          const Cx<R>* __restrict__ twy, const ScState* st) {
+    pdl_wait();
+    zy_fwd_body<R>(q, qfix, W, ny, nz, My, Kz, rz, ry, twz, twy, st, (int)blockIdx.x, (int)gridDim.x);
+}
+
+template <typename R>
+__device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __restrict__ phi, int ny, int nz,
+                                            int My, int Kz, const RadixPlan& rz, const RadixPlan& ry,
+                                            const Cx<R>* __restrict__ twzg, const Cx<R>* __restrict__ twyg,
+                                            const ScState* st, int x) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    if (st->status) return;
+    const int Mz = rz.L, lz = fft_ls(Mz), ly = fft_ls(My), ncz = (ny + 1) / 2;
+    Cx<R>* twz = reinterpret_cast<Cx<R>*>(smraw);
+    Cx<R>* twy = twz + Mz;
+    Cx<R>* A2 = twy + My;
+    Cx<R>* B2 = A2 + Kz * ly;
+    load_twiddles<R>(twz, twzg, Mz);
+    load_twiddles<R>(twy, twyg, My);
+    for (int idx = threadIdx.x; idx < My * Kz; idx += blockDim.x) {
+        const int ky = idx / Kz, k = idx - ky * Kz;
+        A2[k * ly + ky] = W[((size_t)x * My + ky) * Kz + k];
+    }
+    __syncthreads();
+    // B2: inverse y; only rows y < ny are used
+    const Cx<R>* res2 = fft_lines<R, true>(A2, B2, ly, Kz, ry, twy);
+    Cx<R>* A1 = res2 == B2 ? A2 : B2;
+    Cx<R>* B1 = A1 + ncz * lz;
+    // B1: two output rows per complex line, Hermitian-extended (as k_zinv)
+    for (int idx = threadIdx.x; idx < ncz * Mz; idx += blockDim.x) {
+        const int c = idx / Mz, k = idx - c * Mz;
+        const int ya = 2 * c, yb = ya + 1;
+        const bool lo = k < Kz;
+        const int kk = lo ? k : Mz - k;
+        const Cx<R> A = res2[kk * ly + ya];
+        const Cx<R> B = yb < ny ? res2[kk * ly + yb] : cx<R>(0, 0);
+        A1[c * lz + k] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
+    }
+    __syncthreads();
+    const Cx<R>* res = fft_lines<R, true>(A1, B1, lz, ncz, rz, twz);
+    const double norm = st->phi_norm, denom = st->phi_denom;
+    const R fscale = (R)(norm / denom);
+    for (int idx = threadIdx.x; idx < ncz * nz; idx += blockDim.x) {
+        const int c = idx / nz, z = idx - c * nz;
+        const int ya = 2 * c, yb = ya + 1;
+        const Cx<R> v = res[c * lz + z];
+        if (sizeof(R) == 8) {
+            // out/(4*pi*eps0*hx*hy*hz) after the 1/M normalisation of ifftn (sc.py:164-167)
+            phi[((size_t)x * ny + ya) * nz + z] = (R)(((double)v.x * norm) / denom);
+            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = (R)(((double)v.y * norm) / denom);
+        } else {
+            phi[((size_t)x * ny + ya) * nz + z] = v.x * fscale;
+            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = v.y * fscale;
+        }
+    }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(PLANE_THREADS) k_yz_inv(const Cx<R>* __restrict__ W, R* __restrict__ phi, int ny,
+                                                          int nz, int My, int Kz, RadixPlan rz, RadixPlan ry,
+                                                          const Cx<R>* __restrict__ twz,
+                                                          const Cx<R>* __restrict__ twy, const ScState* st) {
+    pdl_wait();
+    yz_inv_body<R>(W, phi, ny, nz, My, Kz, rz, ry, twz, twy, st, (int)blockIdx.x);
+}
+
+static int optin_smem() {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) return 0;
+    return v;
+}
 
 template <typename R>
 static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid, R* phi, const long long* qfix,
@@ -318,26 +485,37 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     const Cx<R>* twz = reinterpret_cast<const Cx<R>*>(ws + L.tw_z);
     cudaError_t e;
     const int NC = z_lines_per_block(p.Mz);
-    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
     dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
     const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
-    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
     dim3 gy((Kz + tky - 1) / tky, p.nx);
-    if (part != CONV_REST) {
+    static const int optin = optin_smem();
+    const bool plane = plane_fits<R>(p, optin);
+    const size_t smp = plane_smem<R>(p);
+    if (plane && part != CONV_REST) {
+        if ((e = set_smem(k_zy_fwd<R>, smp))) return e;
+        launch(k_zy_fwd<R>, p.nx, PLANE_THREADS, smp, s, qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy, st);
+    } else if (part != CONV_REST) {
         if ((e = set_smem(k_zfwd<R>, smz))) return e;
-        k_zfwd<R><<<gz, FFT_THREADS, smz, s>>>(qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+        launch(k_zfwd<R>, gz, FFT_THREADS, smz, s, qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
         if ((e = set_smem(k_ypass<R, false>, smy))) return e;
-        k_ypass<R, false><<<gy, FFT_THREADS, smy, s>>>(W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+        launch(k_ypass<R, false>, gy, FFT_THREADS, smy, s, W, p.ny, p.My, Kz, p.ry, twy, tky, st);
     }
     if (part == CONV_FORWARD) return cudaGetLastError();
-    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
     dim3 gx((Kz + tkx - 1) / tkx, p.My);
     if ((e = set_smem(k_xconv<R>, smx))) return e;
-    k_xconv<R><<<gx, FFT_THREADS, smx, s>>>(W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st);
+    launch(k_xconv<R>, gx, FFT_THREADS, smx, s, W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st);
+    if (plane) {
+        if ((e = set_smem(k_yz_inv<R>, smp))) return e;
+        launch(k_yz_inv<R>, p.nx, PLANE_THREADS, smp, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy, st);
+        return cudaGetLastError();
+    }
     if ((e = set_smem(k_ypass<R, true>, smy))) return e;
-    k_ypass<R, true><<<gy, FFT_THREADS, smy, s>>>(W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+    launch(k_ypass<R, true>, gy, FFT_THREADS, smy, s, W, p.ny, p.My, Kz, p.ry, twy, tky, st);
     if ((e = set_smem(k_zinv<R>, smz))) return e;
-    k_zinv<R><<<gz, FFT_THREADS, smz, s>>>(W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+    launch(k_zinv<R>, gz, FFT_THREADS, smz, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
     return cudaGetLastError();
 }
 
@@ -345,15 +523,20 @@ template <typename R>
 static cudaError_t prepare_fft_t(const Plan& p) {
     cudaError_t e;
     const int NC = z_lines_per_block(p.Mz);
-    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
     const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
-    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
-    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
     if ((e = set_smem(k_zfwd<R>, smz))) return e;
     if ((e = set_smem(k_ypass<R, false>, smy))) return e;
     if ((e = set_smem(k_xconv<R>, smx))) return e;
     if ((e = set_smem(k_ypass<R, true>, smy))) return e;
-    return set_smem(k_zinv<R>, smz);
+    if ((e = set_smem(k_zinv<R>, smz))) return e;
+    if (plane_fits<R>(p, optin_smem())) {
+        if ((e = set_smem(k_zy_fwd<R>, plane_smem<R>(p)))) return e;
+        if ((e = set_smem(k_yz_inv<R>, plane_smem<R>(p)))) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t prepare_fft_kernels(const Plan& p) {
@@ -375,11 +558,11 @@ static cudaError_t field_t(const Plan& p, const Layout& L, char* ws, cudaStream_
     const int bt = p.nz < 256 ? ((p.nz + 31) / 32) * 32 : 256;
     const dim3 grid(p.ny, p.nx);
     if (sizeof(R) == 4)
-        k_field_octs<<<grid, bt, 0, s>>>(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
+        launch(k_field_octs, grid, bt, 0, s, reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
                                          reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq),
                                          p.nx, p.ny, p.nz, st);
     else
-        k_field_grids<R><<<grid, bt, 0, s>>>(reinterpret_cast<const R*>(ws + L.phi), reinterpret_cast<R*>(ws + L.ex),
+        launch(k_field_grids<R>, grid, bt, 0, s, reinterpret_cast<const R*>(ws + L.phi), reinterpret_cast<R*>(ws + L.ex),
                                              reinterpret_cast<R*>(ws + L.ey), reinterpret_cast<R*>(ws + L.ez),
                                              p.nx, p.ny, p.nz, st);
     return cudaGetLastError();
@@ -404,6 +587,7 @@ cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStr
 
 __global__ void __launch_bounds__(FFT_THREADS) kb_zfwd(const BatchBeam* __restrict__ beams,
                                                        const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_FFT_Z)
     zfwd_body<float>(reinterpret_cast<float*>(ws + L.qgrid), reinterpret_cast<const long long*>(ws + L.qfix),
                      reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.nz, p.My, p.Mz / 2 + 1, p.rz,
@@ -413,6 +597,7 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_zfwd(const BatchBeam* __restri
 template <bool INV>
 __global__ void __launch_bounds__(FFT_THREADS) kb_ypass(const BatchBeam* __restrict__ beams,
                                                         const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_FFT_Y)
     ypass_body<float, INV>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry,
                            reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.fft_tky, st, vb);
@@ -420,6 +605,7 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_ypass(const BatchBeam* __restr
 
 __global__ void __launch_bounds__(FFT_THREADS) kb_xconv(const BatchBeam* __restrict__ beams,
                                                         const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_FFT_X)
     xconv_body<float>(reinterpret_cast<Cx<float>*>(ws + L.W), reinterpret_cast<const float*>(ws + L.green), p.nx,
                       p.My, p.Mz / 2 + 1, p.My / 2 + 1, p.rx, reinterpret_cast<const Cx<float>*>(ws + L.tw_x),
@@ -428,12 +614,14 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_xconv(const BatchBeam* __restr
 
 __global__ void __launch_bounds__(FFT_THREADS) kb_zinv(const BatchBeam* __restrict__ beams,
                                                        const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_FFT_Z)
     zinv_body<float>(reinterpret_cast<const Cx<float>*>(ws + L.W), reinterpret_cast<float*>(ws + L.phi), p.ny, p.nz,
                      p.My, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.fft_nc, st, vb);
 }
 
 __global__ void kb_field_octs(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_FIELD)
     field_octs_body(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
                     reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq), p.nx, p.ny, p.nz,
@@ -455,9 +643,9 @@ void batch_fft_tiling(BatchBeam& B, size_t smem[3]) {
     B.gy[BS_FFT_X] = p.My;
     B.gx[BS_FIELD] = p.ny;
     B.gy[BS_FIELD] = p.nx;
-    smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.fft_nc * p.Mz);
-    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.fft_tky * (p.My + 1));
-    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.fft_tkx * (p.Mx + 1));
+    smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.fft_nc * fft_ls(p.Mz));
+    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.fft_tky * fft_ls(p.My));
+    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.fft_tkx * fft_ls(p.Mx));
 }
 
 cudaError_t prepare_batch_fft() {
@@ -474,19 +662,19 @@ cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const i
                                   const int blocks[3], const size_t smem[3], cudaStream_t s, int part) {
     if (nb <= 0) return cudaSuccess;
     if (part != CONV_REST) {
-        kb_zfwd<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
-        kb_ypass<false><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
+        launch(kb_zfwd, blocks[0], FFT_THREADS, smem[0], s, beams, sz, nb);
+        launch(kb_ypass<false>, blocks[1], FFT_THREADS, smem[1], s, beams, sy, nb);
     }
     if (part == CONV_FORWARD) return cudaGetLastError();
-    kb_xconv<<<blocks[2], FFT_THREADS, smem[2], s>>>(beams, sx, nb);
-    kb_ypass<true><<<blocks[1], FFT_THREADS, smem[1], s>>>(beams, sy, nb);
-    kb_zinv<<<blocks[0], FFT_THREADS, smem[0], s>>>(beams, sz, nb);
+    launch(kb_xconv, blocks[2], FFT_THREADS, smem[2], s, beams, sx, nb);
+    launch(kb_ypass<true>, blocks[1], FFT_THREADS, smem[1], s, beams, sy, nb);
+    launch(kb_zinv, blocks[0], FFT_THREADS, smem[0], s, beams, sz, nb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s) {
     if (nb <= 0) return cudaSuccess;
-    kb_field_octs<<<blocks, 128, 0, s>>>(beams, start, nb);
+    launch(kb_field_octs, blocks, 128, 0, s, beams, start, nb);
     return cudaGetLastError();
 }
 

@@ -108,7 +108,14 @@ constexpr int plan_radix(int L, int s) {
     return 0;
 }
 
-template <typename R, bool INV, int RAD, int L, int NS>
+// Intermediate stages keep element i of a line at i + i/8: the Stockham
+// output index of the early stages strides by RAD elements per thread, which
+// in the plain layout puts 8 or more threads of a warp on the same bank; with
+// one pad element per 8 the strides spread over all banks.  The first stage
+// reads and the last one writes the plain layout the kernels load and store.
+__device__ __forceinline__ int fft_pad(int i) { return i + (i >> 3); }
+
+template <typename R, bool INV, int RAD, int L, int NS, bool PIN, bool POUT>
 __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx<R>* __restrict__ b, int ls,
                                                  int nl, const Cx<R>* tw) {
     constexpr int nb = L / RAD;
@@ -122,7 +129,7 @@ __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx
         Cx<R>* dst = b + line * ls;
         Cx<R> v[RAD];
 #pragma unroll
-        for (int t = 0; t < RAD; ++t) v[t] = src[j + t * nb];
+        for (int t = 0; t < RAD; ++t) v[t] = src[PIN ? fft_pad(j + t * nb) : j + t * nb];
         if (NS > 1) {
 #pragma unroll
             for (int t = 1; t < RAD; ++t) {
@@ -136,17 +143,18 @@ __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx
         else dft8<R, INV>(v);
         const int out = (j - k) * RAD + k;
 #pragma unroll
-        for (int t = 0; t < RAD; ++t) dst[out + t * NS] = v[t];
+        for (int t = 0; t < RAD; ++t) dst[POUT ? fft_pad(out + t * NS) : out + t * NS] = v[t];
     }
 }
 
+// ls must be at least fft_ls(L)
 template <typename R, bool INV, int L, int S, int NS>
 __device__ __forceinline__ Cx<R>* fft_stages_c(Cx<R>* a, Cx<R>* b, int ls, int nl, const Cx<R>* tw) {
     constexpr int RAD = plan_radix(L, S);
     if constexpr (RAD == 0) {
         return a;
     } else {
-        stockham_stage_c<R, INV, RAD, L, NS>(a, b, ls, nl, tw);
+        stockham_stage_c<R, INV, RAD, L, NS, (S > 0), (plan_radix(L, S + 1) != 0)>(a, b, ls, nl, tw);
         __syncthreads();
         return fft_stages_c<R, INV, L, S + 1, NS * RAD>(b, a, ls, nl, tw);
     }

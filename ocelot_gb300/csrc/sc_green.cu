@@ -91,6 +91,7 @@ __device__ __forceinline__ void igf_corners_body(double* __restrict__ ig, int nx
 }
 
 __global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, IgfArgs a, const ScState* st) {
+    pdl_wait();
     igf_corners_body(ig, nx, ny, nz, a, st, hw_vblk());
 }
 
@@ -157,6 +158,7 @@ __device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* 
 template <typename R>
 __global__ void k_igf_diff(const double* __restrict__ ig, R* __restrict__ k1, int nx, int ny, int nz, IgfArgs a,
                            const ScState* st) {
+    pdl_wait();
     igf_diff_body<R>(ig, k1, nx, ny, nz, a, st, hw_vblk());
 }
 
@@ -173,7 +175,7 @@ constexpr int GT = 256;
 template <typename R>
 static inline int green_cols(int M) {
     int tk = 16;
-    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + 2 * tk * (M + 1)) > 200 * 1024) tk /= 2;
+    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + 2 * tk * fft_ls(M)) > 200 * 1024) tk /= 2;
     return tk;
 }
 
@@ -184,10 +186,10 @@ __device__ __forceinline__ void green_z_body(const R* __restrict__ k1, R* __rest
                                              const IgfArgs& a, const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (igf_skip(st, a)) return;
-    const int Mz = rz.L;
+    const int Mz = rz.L, lz = fft_ls(Mz);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* A = tw + Mz;
-    Cx<R>* B = A + NC * Mz;
+    Cx<R>* B = A + NC * lz;
     load_twiddles<R>(tw, twg, Mz);
     const int x = vb.y, y0 = vb.x * 2 * NC;
     for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
@@ -199,14 +201,14 @@ __device__ __forceinline__ void green_z_body(const R* __restrict__ k1, R* __rest
             if (ya < ny) re = k1[((size_t)x * ny + ya) * nz + zs];
             if (yb < ny) im = k1[((size_t)x * ny + yb) * nz + zs];
         }
-        A[idx] = cx<R>(re, im);
+        A[c * lz + z] = cx<R>(re, im);
     }
     __syncthreads();
-    Cx<R>* res = fft_lines<R, false>(A, B, Mz, NC, rz, tw);
+    Cx<R>* res = fft_lines<R, false>(A, B, lz, NC, rz, tw);
     for (int idx = threadIdx.x; idx < NC * Kz; idx += blockDim.x) {
         const int c = idx / Kz, k = idx - c * Kz;
         const int ya = y0 + 2 * c, yb = ya + 1;
-        const Cx<R> v = res[c * Mz + k];
+        const Cx<R> v = res[c * lz + k];
         if (!SC_IDX_OK(st, 35, ((long long)x * ny + (yb < ny ? yb : ya)) * Kz + k, (long long)vb.ny * ny * Kz)) continue;
         if (ya < ny) s1[((size_t)x * ny + ya) * Kz + k] = v.x;
         if (yb < ny) s1[((size_t)x * ny + yb) * Kz + k] = v.y;
@@ -217,6 +219,7 @@ template <typename R>
 __global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __restrict__ s1, int ny, int nz,
                                                 int Kz, RadixPlan rz, const Cx<R>* __restrict__ twg, int NC,
                                                 IgfArgs a, const ScState* st) {
+    pdl_wait();
     green_z_body<R>(k1, s1, ny, nz, Kz, rz, twg, NC, a, st, hw_vblk());
 }
 
@@ -230,7 +233,7 @@ __device__ __forceinline__ void green_strided_body(const R* __restrict__ in, R* 
                                                    const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (igf_skip(st, a)) return;
-    const int M = rp.L, ls = M + 1;
+    const int M = rp.L, ls = fft_ls(M);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* A = tw + M;
     Cx<R>* B = A + GTK * ls;
@@ -267,6 +270,7 @@ __global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, 
                                                       int outer_out_stride, RadixPlan rp,
                                                       const Cx<R>* __restrict__ twg, int GTK, IgfArgs a,
                                                       const ScState* st) {
+    pdl_wait();
     green_strided_body<R>(in, out, n, nin_stride, nout, Kz, outer_in_stride, outer_out_stride, rp, twg, GTK, a, st,
                           hw_vblk());
 }
@@ -288,9 +292,9 @@ cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_
     a.hybrid = 0;
     double* ig = reinterpret_cast<double*>(ws + L.igf_ig);
     const size_t nc = (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1);
-    k_igf_corners<<<grid_for(nc, p.sm_count), 256, 0, s>>>(ig, p.nx, p.ny, p.nz, a, st);
+    launch(k_igf_corners, grid_for(nc, p.sm_count), 256, 0, s, ig, p.nx, p.ny, p.nz, a, st);
     const size_t nk = (size_t)p.nx * p.ny * p.nz;
-    k_igf_diff<double><<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, kern_out, p.nx, p.ny, p.nz, a, st);
+    launch(k_igf_diff<double>, grid_for(nk, p.sm_count), 256, 0, s, ig, kern_out, p.nx, p.ny, p.nz, a, st);
     return cudaGetLastError();
 }
 
@@ -307,13 +311,13 @@ cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, cudaStream_t s)
     // registers left over hold the blocks of the concurrent particle kernels
     size_t gb = (nc + 255) / 256;
     if (gb > (size_t)p.sm_count) gb = (size_t)p.sm_count;
-    k_igf_corners<<<(int)gb, 256, 0, s>>>(ig, p.nx, p.ny, p.nz, a, st);
+    launch(k_igf_corners, (int)gb, 256, 0, s, ig, p.nx, p.ny, p.nz, a, st);
     const size_t nk = (size_t)p.nx * p.ny * p.nz;
     if (p.prec == SC_FP64)
-        k_igf_diff<double><<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, reinterpret_cast<double*>(ws + L.igf_k1), p.nx,
+        launch(k_igf_diff<double>, grid_for(nk, p.sm_count), 256, 0, s, ig, reinterpret_cast<double*>(ws + L.igf_k1), p.nx,
                                                                      p.ny, p.nz, a, st);
     else
-        k_igf_diff<float><<<grid_for(nk, p.sm_count), 256, 0, s>>>(ig, reinterpret_cast<float*>(ws + L.igf_k1), p.nx,
+        launch(k_igf_diff<float>, grid_for(nk, p.sm_count), 256, 0, s, ig, reinterpret_cast<float*>(ws + L.igf_k1), p.nx,
                                                                     p.ny, p.nz, a, st);
     return cudaGetLastError();
 }
@@ -337,20 +341,20 @@ static cudaError_t spectrum_t(const Plan& p, const Layout& L, char* ws, cudaStre
     cudaError_t e;
     int NC = 2048 / p.Mz;
     NC = NC < 1 ? 1 : (NC > 16 ? 16 : NC);
-    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
     if ((e = set_smem(k_green_z<R>, smz))) return e;
     dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
-    k_green_z<R><<<gz, GT, smz, s>>>(k1, s1, p.ny, p.nz, Kz, p.rz, twz, NC, a, st);
+    launch(k_green_z<R>, gz, GT, smz, s, k1, s1, p.ny, p.nz, Kz, p.rz, twz, NC, a, st);
     // S2 along y: for each x, rows y < ny of S1[x] -> rows ky < Ky of S2[x]
     const int tky = green_cols<R>(p.My), tkx = green_cols<R>(p.Mx);
-    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
-    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
     if ((e = set_smem(k_green_strided<R>, smx > smy ? smx : smy))) return e;
     dim3 gy((Kz + 2 * tky - 1) / (2 * tky), p.nx);
-    k_green_strided<R><<<gy, GT, smy, s>>>(s1, s2, p.ny, Kz, Ky, Kz, p.ny * Kz, Ky * Kz, p.ry, twy, tky, a, st);
+    launch(k_green_strided<R>, gy, GT, smy, s, s1, s2, p.ny, Kz, Ky, Kz, p.ny * Kz, Ky * Kz, p.ry, twy, tky, a, st);
     // S3 along x: for each ky, rows x < nx of S2[.][ky] -> rows kx < Kx of G[.][ky]
     dim3 gx((Kz + 2 * tkx - 1) / (2 * tkx), Ky);
-    k_green_strided<R><<<gx, GT, smx, s>>>(s2, g, p.nx, Ky * Kz, Kx, Kz, Kz, Kz, p.rx, twx, tkx, a, st);
+    launch(k_green_strided<R>, gx, GT, smx, s, s2, g, p.nx, Ky * Kz, Kx, Kz, Kz, Kz, p.rx, twx, tkx, a, st);
     return cudaGetLastError();
 }
 
@@ -359,10 +363,10 @@ static cudaError_t prepare_green_t(const Plan& p) {
     cudaError_t e;
     int NC = 2048 / p.Mz;
     NC = NC < 1 ? 1 : (NC > 16 ? 16 : NC);
-    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * p.Mz);
+    const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
     const int tky = green_cols<R>(p.My), tkx = green_cols<R>(p.Mx);
-    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * (p.My + 1));
-    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * (p.Mx + 1));
+    const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
     if ((e = set_smem(k_green_z<R>, smz))) return e;
     return set_smem(k_green_strided<R>, smx > smy ? smx : smy);
 }
@@ -400,12 +404,14 @@ __device__ __forceinline__ IgfArgs batch_igf_args(const Plan& p, int hybrid_allo
 
 __global__ void __launch_bounds__(256) kb_igf_corners(const BatchBeam* __restrict__ beams,
                                                       const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_IGF_C)
     igf_corners_body(reinterpret_cast<double*>(ws + L.igf_ig), p.nx, p.ny, p.nz, batch_igf_args(p, 1), st, vb);
 }
 
 __global__ void __launch_bounds__(256) kb_igf_diff(const BatchBeam* __restrict__ beams,
                                                    const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_IGF_D)
     igf_diff_body<float>(reinterpret_cast<const double*>(ws + L.igf_ig), reinterpret_cast<float*>(ws + L.igf_k1),
                          p.nx, p.ny, p.nz, batch_igf_args(p, 1), st, vb);
@@ -413,6 +419,7 @@ __global__ void __launch_bounds__(256) kb_igf_diff(const BatchBeam* __restrict__
 
 __global__ void __launch_bounds__(GT) kb_green_z(const BatchBeam* __restrict__ beams, const int* __restrict__ start,
                                                  int nb) {
+    pdl_wait();
     BATCH_BEAM(BS_GREEN_Z)
     green_z_body<float>(reinterpret_cast<const float*>(ws + L.igf_k1), reinterpret_cast<float*>(ws + L.green_s1),
                         p.ny, p.nz, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.green_nc,
@@ -423,6 +430,7 @@ __global__ void __launch_bounds__(GT) kb_green_z(const BatchBeam* __restrict__ b
 template <int AXIS>
 __global__ void __launch_bounds__(GT) kb_green_strided(const BatchBeam* __restrict__ beams,
                                                        const int* __restrict__ start, int nb) {
+    pdl_wait();
     BATCH_BEAM(AXIS == 1 ? BS_GREEN_Y : BS_GREEN_X)
     const int Kx = p.Mx / 2 + 1, Ky = p.My / 2 + 1, Kz = p.Mz / 2 + 1;
     if (AXIS == 1)
@@ -462,9 +470,9 @@ void batch_green_tiling(BatchBeam& B, size_t smem[3]) {
     B.gy[BS_GREEN_Y] = p.nx;
     B.gx[BS_GREEN_X] = (Kz + 2 * B.green_tkx - 1) / (2 * B.green_tkx);
     B.gy[BS_GREEN_X] = Ky;
-    smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.green_nc * p.Mz);
-    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.green_tky * (p.My + 1));
-    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.green_tkx * (p.Mx + 1));
+    smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.green_nc * fft_ls(p.Mz));
+    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.green_tky * fft_ls(p.My));
+    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.green_tkx * fft_ls(p.Mx));
 }
 
 cudaError_t prepare_batch_green() {
@@ -478,17 +486,17 @@ cudaError_t prepare_batch_green() {
 cudaError_t launch_batch_igf(const BatchBeam* beams, const int* start_c, const int* start_d, int nb, int blocks_c,
                              int blocks_d, cudaStream_t s) {
     if (nb <= 0) return cudaSuccess;
-    kb_igf_corners<<<blocks_c, 256, 0, s>>>(beams, start_c, nb);
-    kb_igf_diff<<<blocks_d, 256, 0, s>>>(beams, start_d, nb);
+    launch(kb_igf_corners, blocks_c, 256, 0, s, beams, start_c, nb);
+    launch(kb_igf_diff, blocks_d, 256, 0, s, beams, start_d, nb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_green(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
                                const int blocks[3], const size_t smem[3], cudaStream_t s) {
     if (nb <= 0) return cudaSuccess;
-    kb_green_z<<<blocks[0], GT, smem[0], s>>>(beams, sz, nb);
-    kb_green_strided<1><<<blocks[1], GT, smem[1], s>>>(beams, sy, nb);
-    kb_green_strided<0><<<blocks[2], GT, smem[2], s>>>(beams, sx, nb);
+    launch(kb_green_z, blocks[0], GT, smem[0], s, beams, sz, nb);
+    launch(kb_green_strided<1>, blocks[1], GT, smem[1], s, beams, sy, nb);
+    launch(kb_green_strided<0>, blocks[2], GT, smem[2], s, beams, sx, nb);
     return cudaGetLastError();
 }
 
@@ -571,8 +579,8 @@ extern "C" int sc_sym_kernel_static(int nx, int ny, int nz, double hx, double hy
     a.use_state = 0;
     a.force = 1;
     a.hybrid = 0;
-    k_igf_corners<<<grid_for((size_t)corners, sms), 256, 0, s>>>(ig, nx, ny, nz, a, st);
-    k_igf_diff<double><<<grid_for((size_t)nx * ny * nz, sms), 256, 0, s>>>(ig, kern, nx, ny, nz, a, st);
+    launch(k_igf_corners, grid_for((size_t)corners, sms), 256, 0, s, ig, nx, ny, nz, a, st);
+    launch(k_igf_diff<double>, grid_for((size_t)nx * ny * nz, sms), 256, 0, s, ig, kern, nx, ny, nz, a, st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return sc_report(SC_ERR_CUDA, "sc_sym_kernel_static: %s", cudaGetErrorString(e));
     return SC_OK;

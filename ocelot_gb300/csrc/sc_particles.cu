@@ -29,6 +29,16 @@ namespace ocsc {
 constexpr int PT = 256;  // threads per block of the particle kernels
 constexpr unsigned FULL = 0xffffffffu;
 
+// order-preserving map of a double onto uint64 (for integer atomics on doubles)
+__device__ __forceinline__ unsigned long long ord64(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unord64(unsigned long long u) {
+    return __longlong_as_double((long long)((u >> 63) ? (u & 0x7fffffffffffffffull) : ~u));
+}
+
+
 // ---------------------------------------------------------------------------
 // deterministic block reductions
 // ---------------------------------------------------------------------------
@@ -50,6 +60,93 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (&sm)[SZ]) {
         for (int c = 0; c < NV; ++c) {
             v[c] = lane < nw ? sm[c * 32 + lane] : 0.0;
             for (int o = 16; o; o >>= 1) v[c] += __shfl_down_sync(FULL, v[c], o);
+        }
+    }
+    __syncthreads();
+}
+
+// error-free sum of two floats: s + e == a + b exactly (Knuth's TwoSum);
+// written with _rn intrinsics so that nothing is contracted or reassociated
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi, lo) += (h2, l2) in double-float arithmetic (~48 significant bits)
+__device__ __forceinline__ void df_add(float& hi, float& lo, float h2, float l2) {
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, l2));
+    hi = __fadd_rn(s, e);
+    lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
+// Deterministic block sum of double-float pairs (hi, lo), as accurate as an
+// FP64 reduction while the shuffles and adds stay on the FP32 pipes (this
+// GPU's FP64 pipe issues a warp instruction in ~18 cycles, so FP64 block
+// reductions dominate short kernels).  Thread 0 receives the sums in hi/lo.
+template <int NV, int SZ>
+__device__ __forceinline__ void block_sum_df(float (&hi)[NV], float (&lo)[NV], float (&sm)[SZ]) {
+    static_assert(SZ >= NV * 64, "block_sum_df: shared scratch too small");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+        for (int o = 16; o; o >>= 1)
+            df_add(hi[c], lo[c], __shfl_down_sync(FULL, hi[c], o), __shfl_down_sync(FULL, lo[c], o));
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            sm[c * 32 + warp] = hi[c];
+            sm[(NV + c) * 32 + warp] = lo[c];
+        }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            hi[c] = lane < nw ? sm[c * 32 + lane] : 0.f;
+            lo[c] = lane < nw ? sm[(NV + c) * 32 + lane] : 0.f;
+            for (int o = 16; o; o >>= 1)
+                df_add(hi[c], lo[c], __shfl_down_sync(FULL, hi[c], o), __shfl_down_sync(FULL, lo[c], o));
+        }
+    }
+    __syncthreads();
+}
+// the same for plain FP32 values (each thread's lo starts at 0)
+template <int NV, int SZ>
+__device__ __forceinline__ void block_sum_f2(const float (&v)[NV], float (&hi)[NV], float (&lo)[NV],
+                                             float (&sm)[SZ]) {
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        hi[c] = v[c];
+        lo[c] = 0.f;
+    }
+    block_sum_df<NV>(hi, lo, sm);
+}
+
+// block minimum or maximum of order-preserving 64-bit keys (ord64 of
+// doubles) on the integer pipes; thread 0 receives the result
+template <int NV, bool MAX, int SZ>
+__device__ __forceinline__ void block_minmax_u64(unsigned long long (&v)[NV], unsigned long long (&sm)[SZ]) {
+    static_assert(SZ >= NV * 32, "block_minmax_u64: shared scratch too small");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+        for (int o = 16; o; o >>= 1) {
+            const unsigned long long w = __shfl_down_sync(FULL, v[c], o);
+            v[c] = MAX ? (w > v[c] ? w : v[c]) : (w < v[c] ? w : v[c]);
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sm[c * 32 + warp] = v[c];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            v[c] = lane < nw ? sm[c * 32 + lane] : (MAX ? 0ull : ~0ull);
+            for (int o = 16; o; o >>= 1) {
+                const unsigned long long w = __shfl_down_sync(FULL, v[c], o);
+                v[c] = MAX ? (w > v[c] ? w : v[c]) : (w < v[c] ? w : v[c]);
+            }
         }
     }
     __syncthreads();
@@ -183,32 +280,60 @@ __device__ __forceinline__ double f2d(float f) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
-// momenta (eV/c) and energy (eV) of one particle in FP32 (coord_transform.py:64-72)
+// the hardware's approximate reciprocal and square root (relative error
+// ~1e-7)
+__device__ __forceinline__ float rcpf(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sqrtf_fast(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Momenta (eV/c) and energy (eV) of one particle in FP32
+// (coord_transform.py:64-72): gamma from delta, |p|^2 = (gamma^2 - 1) m^2,
+// pz from |p|^2 - px^2 - py^2, with the approximate square root.  Where the
+// FP32 form needs more than ~1e-7 relative accuracy it does not use these
+// values directly: the mesh step and offset cancel a common scale of the
+// positions (gamma0 scales both), the charge-weighted mean is taken of lab
+// positions in which the momenta only enter a small correction (lab32), and
+// NGP keys near a cell face are recomputed from FP64 coordinates (xyz_fine).
 __device__ __forceinline__ void mom32(float xq, float yq, float d, const KickParams& kp, float& px, float& py,
                                       float& pz, float& E) {
-    const float gamma = kp.gamref_f * (1.0f + kp.betaref_f * d);
-    const float beta = sqrtf(1.0f - 1.0f / (gamma * gamma));
-    const float g = gamma * beta / kp.grbr_f;
-    const float pz2 = sqrtf(g * g - xq * xq - yq * yq);
+    const float gamma = kp.gamref_f * fmaf(kp.betaref_f, d, 1.0f);
+    const float g2 = fmaf(gamma, gamma, -1.0f) * kp.igrbr2_f;
+    const float pz2 = sqrtf_fast(g2 - fmaf(xq, xq, yq * yq));
     px = xq * kp.pref_f;
     py = yq * kp.pref_f;
     pz = pz2 * kp.pref_f;
     E = gamma * kp.m_f;
 }
 
-// rotated position (z scaled by gamma0) of one particle in FP32 from its
-// FP32-rounded MAD coordinates and momenta (coord_transform.py:57-96 for the
-// lab position, sc.py:233 for the rotation), as the extent kernel stores it
-__device__ __forceinline__ void pos32(float x, float y, float tau, float px, float py, float pz, float E,
-                                      const float (&T)[3][3], float g0, float (&v)[3]) {
-    const float s = tau / E;
-    const float l0 = x - px * s, l1 = y - py * s, l2 = -pz * s;
+// Lab position of one particle in FP32 (coord_transform.py:89-95): each
+// coordinate is its MAD value plus a small correction, x - (px/E) tau and
+// z = -tau + tau (1 - pz/E) with 1 - pz/E = (m^2 + pT^2) / ((E + pz) E),
+// free of cancellation; the approximate reciprocal only touches the
+// corrections.
+__device__ __forceinline__ void lab32(float x, float y, float tau, float px, float py, float pz, float E,
+                                      const KickParams& kp, float (&l)[3]) {
+    const float iE = rcpf(E);
+    const float s = tau * iE;
+    l[0] = fmaf(-px, s, x);
+    l[1] = fmaf(-py, s, y);
+    const float k = (kp.m2_f + fmaf(px, px, py * py)) * rcpf((E + pz) * E);
+    l[2] = fmaf(tau, k, -tau);
+}
+// rotated position in the beam frame, z scaled by gamma0 (sc.py:233)
+__device__ __forceinline__ void rot32(const float (&l)[3], const float (&T)[3][3], float g0, float (&v)[3]) {
 #pragma unroll
-    for (int j = 0; j < 3; ++j) v[j] = l0 * T[0][j] + l1 * T[1][j] + l2 * T[2][j];
+    for (int j = 0; j < 3; ++j) v[j] = fmaf(l[0], T[0][j], fmaf(l[1], T[1][j], l[2] * T[2][j]));
     v[2] *= g0;
 }
 // grid coordinate X = v/steps - X_off (sc.py:182-183) in FP32
-__device__ __forceinline__ float grid32(float v, float step, float off) { return v / step - off; }
+__device__ __forceinline__ float grid32(float v, float istep, float off) { return fmaf(v, istep, -off); }
 
 // 32-byte and 16-byte row accesses of G consecutive particles; a partial
 // group (full == false) takes one element
@@ -267,14 +392,15 @@ __device__ __forceinline__ void st_rows(double* __restrict__ row, int64_t i, boo
 // ---------------------------------------------------------------------------
 // Bulk-copy (TMA) streaming of particle rows through shared memory, for the
 // frame, extent and keys kernels.  A block walks its tiles of PT_TILE
-// particles (local tile t is global tile vb.x + t * vb.nx); PS_STAGES tile
+// particles (local tile t is global tile vb.x + t * vb.nx); STAGES tile
 // buffers rotate so that the loads of the next tiles are in flight while the
 // block works on one.  Thread t takes particles 2t and 2t+1 of a tile.  A
 // tile's copies cover a prefix whose byte length is a multiple of 16; the
 // few particles after it (the end of the beam) are read directly.
 // ---------------------------------------------------------------------------
 constexpr int PT_TILE = 2 * PT;
-constexpr int PS_STAGES = 2;
+constexpr int FR_STAGES = 4;  // tile buffers of the frame kernel (12 KB each)
+constexpr int EX_STAGES = 2;  // tile buffers of the extent kernel (28 KB each)
 
 struct BlockTiles {
     int64_t n, first, stride, mine;
@@ -294,41 +420,41 @@ struct BlockTiles {
 // loads of local tile t.  Every thread of the block must call it; body must
 // not synchronise the block.  Returns false if a wait gave up, after
 // waiting (again with a limit) for the loads still in flight.
-template <typename Issue, typename Body>
+template <int STAGES, typename Issue, typename Body>
 __device__ __forceinline__ bool stream_tiles(const BlockTiles& T, uint64_t* bar, Issue&& issue, Body&& body) {
     const bool lead = threadIdx.x == 0;
     if (lead) {
-        for (int s = 0; s < PS_STAGES; ++s) mbar_init(&bar[s], 1);
+        for (int s = 0; s < STAGES; ++s) mbar_init(&bar[s], 1);
         mbar_init_fence();
     }
     __syncthreads();
-    int64_t issued = T.mine < PS_STAGES ? T.mine : PS_STAGES;
+    int64_t issued = T.mine < STAGES ? T.mine : STAGES;
     if (lead)
         for (int64_t t = 0; t < issued; ++t) issue(t, (int)t, &bar[t]);
     int64_t t = 0;
     bool failed = false;
     for (; t < T.mine; ++t) {
-        const int s = (int)(t % PS_STAGES);
-        const bool ok = mbar_wait(&bar[s], (unsigned)((t / PS_STAGES) & 1));
+        const int s = (int)(t % STAGES);
+        const bool ok = mbar_wait(&bar[s], (unsigned)((t / STAGES) & 1));
         if (ok) body(t, s);
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
         }
-        // every thread is done with buffer s: it takes local tile t + PS_STAGES
+        // every thread is done with buffer s: it takes local tile t + STAGES
         if (lead && issued < T.mine) {
             issue(issued, s, &bar[s]);
             ++issued;
         }
     }
     if (failed && lead)
-        for (int64_t u = t; u < issued; ++u) mbar_wait(&bar[u % PS_STAGES], (unsigned)((u / PS_STAGES) & 1));
+        for (int64_t u = t; u < issued; ++u) mbar_wait(&bar[u % STAGES], (unsigned)((u / STAGES) & 1));
     return !failed;
 }
 
 // shared memory of the streamed kernels: the tile buffers, then the barriers
-constexpr size_t FR_SMEM = (size_t)PS_STAGES * 3 * PT_TILE * sizeof(double) + PS_STAGES * sizeof(uint64_t);
-constexpr size_t EX_SMEM = (size_t)PS_STAGES * 7 * PT_TILE * sizeof(double) + PS_STAGES * sizeof(uint64_t);
+constexpr size_t FR_SMEM = (size_t)FR_STAGES * 3 * PT_TILE * sizeof(double) + FR_STAGES * sizeof(uint64_t);
+constexpr size_t EX_SMEM = (size_t)EX_STAGES * 7 * PT_TILE * sizeof(double) + EX_STAGES * sizeof(uint64_t);
 static_assert(3 * (EX_SMEM + 1024 + 5 * 1024) <= 228 * 1024, "three extent blocks must fit an SM");
 
 // ---------------------------------------------------------------------------
@@ -349,60 +475,195 @@ __device__ __forceinline__ bool arrive_last(unsigned int* counter, int nblk) {
 
 // mean momentum -> basis T, gamma0, beta0 (sc.py:224-239, 243-248); called by
 // the last block of a frame kernel with all per-block momentum sums in part
+// Mean-velocity frame from the momentum sums (valid in thread 0); called by
+// every thread of the last block.  The FP64 operations are the serial
+// ones of sc.py:224-239, 243-248, spread over lanes: lane k of warp 0 takes
+// component k of each basis vector and warp 1 the gamma0 chain, so the
+// dependent FP64 divisions and square roots (very slow on this GPU's FP64
+// pipe) form three short chains instead of one long one.  Each value goes
+// through exactly the serial sequence of operations.
+__device__ void frame_finish(const double (&acc)[3], const KickParams& kp, ScState* st) {
+    __shared__ double s_acc[3];
+    __shared__ double s_gamma0;
+    __shared__ int s_bad1;
+    if (threadIdx.x == 0) {
+        st->done_frame = 0;
+        // the previous kick's outcome, kept before this kick resets the status
+        if (st->status != SC_OK && st->first_error == SC_OK) st->first_error = st->status;
+        for (int k = 0; k < 3; ++k) s_acc[k] = acc[k];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, k = lane < 3 ? lane : 0;
+    if (warp > 1) return;
+    const double nn = (double)kp.n;
+    double t3k = __ddiv_rn(s_acc[k], nn);
+    double t3[3] = {__shfl_sync(FULL, t3k, 0), __shfl_sync(FULL, t3k, 1), __shfl_sync(FULL, t3k, 2)};
+    const double Pav = __dsqrt_rn(__fma_rn(t3[2], t3[2], __fma_rn(t3[1], t3[1], __dmul_rn(t3[0], t3[0]))));
+    if (warp == 1) {
+        if (lane == 0) {
+            const double pm = __ddiv_rn(Pav, kp.m_e_eV);
+            const double gamma0 = __dsqrt_rn(__dadd_rn(__dmul_rn(pm, pm), 1.0));
+            const double beta0 = __dsqrt_rn(__dsub_rn(1.0, __drcp_rn(__dmul_rn(gamma0, gamma0))));
+            st->Pav = Pav;
+            st->gamma0 = gamma0;
+            st->beta0 = beta0;
+            st->kxy = __dmul_rn(kp.cdT, __dsub_rn(1.0, __dmul_rn(beta0, beta0)));
+            st->kz = kp.cdT;
+            st->g0f = (float)gamma0;
+            st->ig0f = (float)(1.0 / gamma0);
+            st->kxyf = (float)st->kxy;
+            st->kzf = (float)kp.cdT;
+            s_gamma0 = gamma0;
+            s_bad1 = !(Pav > 0.0) || !isfinite(Pav) || !isfinite(gamma0);
+        }
+        asm volatile("bar.sync 1, 64;" ::: "memory");
+        return;
+    }
+    t3k = __ddiv_rn(t3k, Pav);
+    for (int j = 0; j < 3; ++j) t3[j] = __shfl_sync(FULL, t3k, j);
+    // t1 = cross(ey, t3) = (t3z, 0, -t3x), normalised
+    const double t1r[3] = {t3[2], 0.0, -t3[0]};
+    const double n1 = __dsqrt_rn(__fma_rn(t1r[2], t1r[2], __fma_rn(t1r[1], t1r[1], __dmul_rn(t1r[0], t1r[0]))));
+    const double t1k = __ddiv_rn(t1r[k], n1);
+    const double t1[3] = {__shfl_sync(FULL, t1k, 0), __shfl_sync(FULL, t1k, 1), __shfl_sync(FULL, t1k, 2)};
+    // t2 = cross(t3, t1)
+    const double t2[3] = {__dsub_rn(__dmul_rn(t3[1], t1[2]), __dmul_rn(t3[2], t1[1])),
+                          __dsub_rn(__dmul_rn(t3[2], t1[0]), __dmul_rn(t3[0], t1[2])),
+                          __dsub_rn(__dmul_rn(t3[0], t1[1]), __dmul_rn(t3[1], t1[0]))};
+    if (lane < 3) {
+        st->T[lane][0] = t1[lane];
+        st->T[lane][1] = t2[lane];
+        st->T[lane][2] = t3[lane];
+        st->Tf[lane][0] = (float)t1[lane];
+        st->Tf[lane][1] = (float)t2[lane];
+        st->Tf[lane][2] = (float)t3[lane];
+    }
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    if (lane == 0) {
+        int status = SC_OK;
+        if (s_bad1 || !isfinite(s_gamma0) || !isfinite(t1[0]) || !isfinite(t2[1])) status = SC_ERR_NONFINITE;
+        if (st->frame_timeout) {
+            status = SC_ERR_TIMEOUT;
+            st->frame_timeout = 0;
+        }
+        st->status = status;
+    }
+}
+
 __device__ void frame_finalize(const double* part, int nblk, const KickParams& kp, ScState* st) {
     __shared__ double sm[3 * 32];
     double acc[3] = {0.0, 0.0, 0.0};
     for (int b = threadIdx.x; b < nblk; b += blockDim.x)
         for (int k = 0; k < 3; ++k) acc[k] += __ldcg(part + b * 3 + k);
     block_sum<3>(acc, sm);
-    if (threadIdx.x != 0) return;
-    st->done_frame = 0;
-    // the previous kick's outcome, kept before this kick resets the status
-    if (st->status != SC_OK && st->first_error == SC_OK) st->first_error = st->status;
-    const double nn = (double)kp.n;
-    double t3[3] = {__ddiv_rn(acc[0], nn), __ddiv_rn(acc[1], nn), __ddiv_rn(acc[2], nn)};
-    const double Pav = __dsqrt_rn(__fma_rn(t3[2], t3[2], __fma_rn(t3[1], t3[1], __dmul_rn(t3[0], t3[0]))));
-    for (int k = 0; k < 3; ++k) t3[k] = __ddiv_rn(t3[k], Pav);
-    // t1 = cross(ey, t3) = (t3z, 0, -t3x), normalised
-    double t1[3] = {t3[2], 0.0, -t3[0]};
-    const double n1 = __dsqrt_rn(__fma_rn(t1[2], t1[2], __fma_rn(t1[1], t1[1], __dmul_rn(t1[0], t1[0]))));
-    for (int k = 0; k < 3; ++k) t1[k] = __ddiv_rn(t1[k], n1);
-    // t2 = cross(t3, t1)
-    const double t2[3] = {__dsub_rn(__dmul_rn(t3[1], t1[2]), __dmul_rn(t3[2], t1[1])),
-                          __dsub_rn(__dmul_rn(t3[2], t1[0]), __dmul_rn(t3[0], t1[2])),
-                          __dsub_rn(__dmul_rn(t3[0], t1[1]), __dmul_rn(t3[1], t1[0]))};
-    for (int i = 0; i < 3; ++i) {
-        st->T[i][0] = t1[i];
-        st->T[i][1] = t2[i];
-        st->T[i][2] = t3[i];
-        st->Tf[i][0] = (float)t1[i];
-        st->Tf[i][1] = (float)t2[i];
-        st->Tf[i][2] = (float)t3[i];
-    }
-    const double pm = __ddiv_rn(Pav, kp.m_e_eV);
-    const double gamma0 = __dsqrt_rn(__dadd_rn(__dmul_rn(pm, pm), 1.0));
-    const double beta0 = __dsqrt_rn(__dsub_rn(1.0, __drcp_rn(__dmul_rn(gamma0, gamma0))));
-    st->Pav = Pav;
-    st->gamma0 = gamma0;
-    st->beta0 = beta0;
-    st->kxy = __dmul_rn(kp.cdT, __dsub_rn(1.0, __dmul_rn(beta0, beta0)));
-    st->kz = kp.cdT;
-    st->g0f = (float)gamma0;
-    st->ig0f = (float)(1.0 / gamma0);
-    st->kxyf = (float)st->kxy;
-    st->kzf = (float)kp.cdT;
-    int status = SC_OK;
-    if (!(Pav > 0.0) || !isfinite(Pav) || !isfinite(gamma0) || !isfinite(t1[0]) || !isfinite(t2[1])) status = SC_ERR_NONFINITE;
-    if (st->frame_timeout) {
-        status = SC_ERR_TIMEOUT;
-        st->frame_timeout = 0;
-    }
-    st->status = status;
+    frame_finish(acc, kp, st);
+}
+
+// FP32 form: per-block momentum sums as double-float pairs (hi[3], lo[3]),
+// reduced on the FP32 pipes
+struct FramePart32 {
+    float hi[3], lo[3];
+};
+__device__ void frame_finalize32(const FramePart32* part, int nblk, const KickParams& kp, ScState* st) {
+    __shared__ float sm[3 * 64];
+    float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+        for (int k = 0; k < 3; ++k) df_add(hi[k], lo[k], __ldcg(&part[b].hi[k]), __ldcg(&part[b].lo[k]));
+    block_sum_df<3>(hi, lo, sm);
+    const double acc[3] = {(double)hi[0] + (double)lo[0], (double)hi[1] + (double)lo[1],
+                           (double)hi[2] + (double)lo[2]};
+    frame_finish(acc, kp, st);
 }
 
 // steps, X_off, potential scale, Green cache check (sc.py:172-186, 167)
 // part layout per block (PART_EXT doubles): min[3], max[3], sum q*x[3], sum q, sum |q|
-__device__ void mesh_finalize(const double* part, int nblk, const KickParams& kp, ScState* st, double gamma_override) {
+// lab_sums: the sums q*x are of lab positions (the FP32 extent); they are
+// rotated into the beam frame and scaled by gamma0 here (a linear map, so
+// the same charge-weighted mean)
+// Mesh step, offset and derived constants from the extremes and charge
+// moments (valid in thread 0); called by every thread of the last block.
+// Lane k of warp 0 takes axis k with the serial FP64 operations of
+// sc.py:172-186, so the divisions of the three axes run side by side.
+__device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const double (&qs)[5], const KickParams& kp,
+                            ScState* st, double gamma_override, bool lab_sums) {
+    __shared__ double s_mn[3], s_mx[3], s_qs[5];
+    if (threadIdx.x == 0) {
+        st->done_extent = 0;
+        if (gamma_override > 0.0) {
+            st->gamma0 = gamma_override;
+            st->g0f = (float)gamma_override;
+            st->ig0f = (float)(1.0 / gamma_override);
+            st->status = SC_OK;
+        }
+        for (int k = 0; k < 3; ++k) {
+            s_mn[k] = mn[k];
+            s_mx[k] = mx[k];
+        }
+        for (int k = 0; k < 5; ++k) s_qs[k] = qs[k];
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    if (st->status != SC_OK) return;
+    const int lane = threadIdx.x, k = lane < 3 ? lane : 0;
+    double q3[3] = {s_qs[0], s_qs[1], s_qs[2]};
+    if (lab_sums) {
+        double r[3];
+        for (int j = 0; j < 3; ++j) r[j] = fma(q3[2], st->T[2][j], fma(q3[1], st->T[1][j], q3[0] * st->T[0][j]));
+        r[2] *= st->gamma0;
+        for (int j = 0; j < 3; ++j) q3[j] = r[j];
+    }
+    const double qsum = s_qs[3];
+    const int nm[3] = {kp.nx, kp.ny, kp.nz};
+    double XX = __dsub_rn(s_mx[k], s_mn[k]);
+    if (!isnan(kp.mesh_scale)) XX = __dmul_rn(XX, kp.mesh_scale);
+    const double stepk = __ddiv_rn(XX, (double)(nm[k] - 3));
+    const double xmin = __ddiv_rn(s_mn[k], stepk);
+    const double xmid = __ddiv_rn(__ddiv_rn(q3[k], stepk), qsum);
+    double xoffk = __dadd_rn(floor(__dsub_rn(xmin, xmid)), xmid);
+    if (!isnan(kp.mesh_shift)) xoffk = __dadd_rn(xoffk, kp.mesh_shift);
+    const bool badk = !(stepk > 0.0) || !isfinite(stepk) || !isfinite(xoffk);
+    const bool bad = __any_sync(FULL, badk) || !(qsum != 0.0) || !isfinite(qsum);
+    if (bad) {
+        if (lane == 0) st->status = SC_ERR_DEGENERATE;
+        return;
+    }
+    const double istepk = 1.0 / stepk;
+    const double steps[3] = {__shfl_sync(FULL, stepk, 0), __shfl_sync(FULL, stepk, 1), __shfl_sync(FULL, stepk, 2)};
+    // near box of the hybrid Green's function along axis k (igf_box_of)
+    const double hm = fmax(steps[0], fmax(steps[1], steps[2]));
+    const double v = 5.0 * hm / stepk;
+    int bk = v >= (double)nm[k] ? nm[k] : (int)ceil(v) + 1;
+    if (bk > nm[k]) bk = nm[k];
+    if (lane < 3) {
+        st->steps[k] = stepk;
+        st->xoff[k] = xoffk;
+        st->isteps[k] = istepk;
+        st->stepsf[k] = (float)stepk;
+        st->istepsf[k] = (float)istepk;
+        st->xofff[k] = (float)xoffk;
+        st->igf_box[k] = bk;
+    }
+    if (lane == 1) st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
+    if (lane == 2) {
+        // fixed-point unit of the exact deposit: sum |q| * 2^S < 2^62, so no
+        // cell (nor the total) can overflow a signed 64-bit accumulator
+        int e2;
+        frexp(s_qs[4], &e2);
+        const int S = 62 - e2;
+        st->qfix_shift = S;
+        st->qfix_scale = ldexp(1.0, S);
+        st->qfix_inv = (float)ldexp(1.0, -S);
+    }
+    if (lane == 0) {
+        st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, steps[0]), steps[1]), steps[2]);
+        const bool same = steps[0] == st->igf_h[0] && steps[1] == st->igf_h[1] && steps[2] == st->igf_h[2];
+        st->igf_rebuild = same ? 0 : 1;
+        for (int j = 0; j < 3; ++j) st->igf_h[j] = steps[j];
+    }
+}
+
+__device__ void mesh_finalize(const double* part, int nblk, const KickParams& kp, ScState* st, double gamma_override,
+                              bool lab_sums = false) {
     __shared__ double sm[5 * 32];
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     double qs[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -419,54 +680,37 @@ __device__ void mesh_finalize(const double* part, int nblk, const KickParams& kp
     block_minmax<3, false>(mn, sm);
     block_minmax<3, true>(mx, sm);
     block_sum<5>(qs, sm);
-    if (threadIdx.x != 0) return;
-    st->done_extent = 0;
-    if (gamma_override > 0.0) {
-        st->gamma0 = gamma_override;
-        st->g0f = (float)gamma_override;
-        st->ig0f = (float)(1.0 / gamma_override);
-        st->status = SC_OK;
+    mesh_finish(mn, mx, qs, kp, st, gamma_override, lab_sums);
+}
+
+// FP32 form: per-block extremes as ord64 keys (integer min/max) and the
+// charge moments of the lab positions as double-float pairs
+struct ExtPart32 {
+    unsigned long long mn[3], mx[3];
+    float hi[5], lo[5];
+};
+static_assert(sizeof(ExtPart32) <= PART_EXT * sizeof(double), "ExtPart32 must fit a block's partial slot");
+__device__ void mesh_finalize32(const ExtPart32* part, int nblk, const KickParams& kp, ScState* st) {
+    __shared__ unsigned long long smu[3 * 32];
+    __shared__ float smf[5 * 64];
+    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
+    float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        for (int k = 0; k < 3; ++k) {
+            const unsigned long long a = __ldcg(&part[b].mn[k]), c = __ldcg(&part[b].mx[k]);
+            mn[k] = a < mn[k] ? a : mn[k];
+            mx[k] = c > mx[k] ? c : mx[k];
+        }
+        for (int k = 0; k < 5; ++k) df_add(hi[k], lo[k], __ldcg(&part[b].hi[k]), __ldcg(&part[b].lo[k]));
     }
-    if (st->status != SC_OK) return;
-    const int nm[3] = {kp.nx, kp.ny, kp.nz};
-    double steps[3], xoff[3];
-    bool bad = !(qs[3] != 0.0) || !isfinite(qs[3]);
-    for (int k = 0; k < 3; ++k) {
-        double XX = __dsub_rn(mx[k], mn[k]);
-        if (!isnan(kp.mesh_scale)) XX = __dmul_rn(XX, kp.mesh_scale);
-        steps[k] = __ddiv_rn(XX, (double)(nm[k] - 3));
-        const double xmin = __ddiv_rn(mn[k], steps[k]);
-        const double xmid = __ddiv_rn(__ddiv_rn(qs[k], steps[k]), qs[3]);
-        xoff[k] = __dadd_rn(floor(__dsub_rn(xmin, xmid)), xmid);
-        if (!isnan(kp.mesh_shift)) xoff[k] = __dadd_rn(xoff[k], kp.mesh_shift);
-        if (!(steps[k] > 0.0) || !isfinite(steps[k]) || !isfinite(xoff[k])) bad = true;
-    }
-    if (bad) {
-        st->status = SC_ERR_DEGENERATE;
-        return;
-    }
-    for (int k = 0; k < 3; ++k) {
-        st->steps[k] = steps[k];
-        st->xoff[k] = xoff[k];
-        st->isteps[k] = 1.0 / steps[k];
-        st->stepsf[k] = (float)steps[k];
-        st->istepsf[k] = (float)(1.0 / steps[k]);
-        st->xofff[k] = (float)xoff[k];
-    }
-    st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, steps[0]), steps[1]), steps[2]);
-    st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
-    igf_box_of(steps, kp.nx, kp.ny, kp.nz, st->igf_box);
-    const bool same = steps[0] == st->igf_h[0] && steps[1] == st->igf_h[1] && steps[2] == st->igf_h[2];
-    st->igf_rebuild = same ? 0 : 1;
-    for (int k = 0; k < 3; ++k) st->igf_h[k] = steps[k];
-    // fixed-point unit of the exact deposit: sum |q| * 2^S < 2^62, so no cell
-    // (nor the total) can overflow a signed 64-bit accumulator
-    int e2;
-    frexp(qs[4], &e2);
-    const int S = 62 - e2;
-    st->qfix_shift = S;
-    st->qfix_scale = ldexp(1.0, S);
-    st->qfix_inv = (float)ldexp(1.0, -S);
+    block_minmax_u64<3, false>(mn, smu);
+    block_minmax_u64<3, true>(mx, smu);
+    block_sum_df<5>(hi, lo, smf);
+    const double dmn[3] = {unord64(mn[0]), unord64(mn[1]), unord64(mn[2])};
+    const double dmx[3] = {unord64(mx[0]), unord64(mx[1]), unord64(mx[2])};
+    double qs[5];
+    for (int k = 0; k < 5; ++k) qs[k] = (double)hi[k] + (double)lo[k];
+    mesh_finish(dmn, dmx, qs, kp, st, -1.0, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -474,6 +718,7 @@ __device__ void mesh_finalize(const double* part, int nblk, const KickParams& kp
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(PT) k_frame64(const double* __restrict__ rp, KickParams kp,
                                                 double* __restrict__ xp, double* __restrict__ part, ScState* st) {
+    pdl_wait();
     __shared__ double sm[3 * 32];
     double acc[3] = {0.0, 0.0, 0.0};
     const int64_t n = kp.n, ld = kp.ld;
@@ -543,7 +788,7 @@ template <bool VEC>
 __device__ __forceinline__ void frame32_body(const double* __restrict__ rp, const KickParams& kp,
                                              double* __restrict__ part, ScState* st,
                                              unsigned long long* __restrict__ qzero, int64_t nzero, VBlk vb) {
-    __shared__ double sm[3 * 32];
+    __shared__ float smf[3 * 64];
     if (qzero)
         for (int64_t i = vb.x * (int64_t)blockDim.x + threadIdx.x; i < nzero; i += (int64_t)vb.nx * blockDim.x)
             qzero[i] = 0ull;
@@ -562,16 +807,22 @@ __device__ __forceinline__ void frame32_body(const double* __restrict__ rp, cons
         a2 += pz;
     }
     PAIR_LOOP_END
-    double acc[3] = {a0, a1, a2};
-    block_sum<3>(acc, sm);
+    const float a[3] = {a0, a1, a2};
+    float hi[3], lo[3];
+    block_sum_f2<3>(a, hi, lo, smf);
+    FramePart32* fp = reinterpret_cast<FramePart32*>(part);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) part[vb.x * 3 + k] = acc[k];
-    if (arrive_last(&st->done_frame, vb.nx)) frame_finalize(part, vb.nx, kp, st);
+        for (int k = 0; k < 3; ++k) {
+            fp[vb.x].hi[k] = hi[k];
+            fp[vb.x].lo[k] = lo[k];
+        }
+    if (arrive_last(&st->done_frame, vb.nx)) frame_finalize32(fp, vb.nx, kp, st);
 }
 
 template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
                                                    double* __restrict__ part, ScState* st) {
+    pdl_wait();
     frame32_body<VEC>(rp, kp, part, st, nullptr, 0, hw_vblk());
 }
 
@@ -581,9 +832,9 @@ __device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, 
                                                  double* __restrict__ part, ScState* st,
                                                  unsigned long long* __restrict__ qzero, int64_t nzero, VBlk vb) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    __shared__ double sm[3 * 32];
-    double* buf = reinterpret_cast<double*>(smraw);  // [PS_STAGES][3][PT_TILE]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + PS_STAGES * 3 * PT_TILE);
+    __shared__ float smf[3 * 64];
+    double* buf = reinterpret_cast<double*>(smraw);  // [FR_STAGES][3][PT_TILE]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + FR_STAGES * 3 * PT_TILE);
     if (qzero)
         for (int64_t i = vb.x * (int64_t)blockDim.x + threadIdx.x; i < nzero; i += (int64_t)vb.nx * blockDim.x)
             qzero[i] = 0ull;
@@ -618,16 +869,22 @@ __device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, 
             add(rp[ld + i], rp[3 * ld + i], rp[5 * ld + i]);
         }
     };
-    if (!stream_tiles(T, bar, issue, body) && threadIdx.x == 0) atomicExch(&st->frame_timeout, 1);
-    double acc[3] = {a0, a1, a2};
-    block_sum<3>(acc, sm);
+    if (!stream_tiles<FR_STAGES>(T, bar, issue, body) && threadIdx.x == 0) atomicExch(&st->frame_timeout, 1);
+    const float a[3] = {a0, a1, a2};
+    float hi[3], lo[3];
+    block_sum_f2<3>(a, hi, lo, smf);
+    FramePart32* fp = reinterpret_cast<FramePart32*>(part);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 3; ++k) part[vb.x * 3 + k] = acc[k];
-    if (arrive_last(&st->done_frame, vb.nx)) frame_finalize(part, vb.nx, kp, st);
+        for (int k = 0; k < 3; ++k) {
+            fp[vb.x].hi[k] = hi[k];
+            fp[vb.x].lo[k] = lo[k];
+        }
+    if (arrive_last(&st->done_frame, vb.nx)) frame_finalize32(fp, vb.nx, kp, st);
 }
 
 __global__ void __launch_bounds__(PT, 4) k_frame32_tma(const double* __restrict__ rp, KickParams kp,
                                                        double* __restrict__ part, ScState* st) {
+    pdl_wait();
     frame32_tma_body(rp, kp, part, st, nullptr, 0, hw_vblk());
 }
 
@@ -654,6 +911,7 @@ __device__ __forceinline__ void extent_block_out(double (&mn)[3], double (&mx)[3
 __global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, const double* __restrict__ q,
                                                  KickParams kp, double* __restrict__ X, double* __restrict__ part,
                                                  ScState* st) {
+    pdl_wait();
     __shared__ double sm[5 * 32];
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     double qs[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -682,15 +940,6 @@ __global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, 
     if (arrive_last(&st->done_extent, gridDim.x)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
 }
 
-// order-preserving map of a double onto uint64 (for integer atomics on doubles)
-__device__ __forceinline__ unsigned long long ord64(double v) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double unord64(unsigned long long u) {
-    return __longlong_as_double((long long)((u >> 63) ? (u & 0x7fffffffffffffffull) : ~u));
-}
-
 // Rotated position (z scaled by gamma0) of particle i to ~1e-11 of a cell:
 // each lab coordinate is its FP64 MAD value plus a small correction computed
 // in FP32 (x - (px/E) tau, and z = -tau + tau (1 - pz/E) with
@@ -701,10 +950,10 @@ __device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t 
     const double x = rp[i], y = rp[2 * ld + i], tau = rp[4 * ld + i];
     float px, py, pz, E;
     mom32(d2f(rp[ld + i]), d2f(rp[3 * ld + i]), d2f(rp[5 * ld + i]), kp, px, py, pz, E);
-    const float tf = d2f(tau), iE = 1.0f / E;
+    const float tf = d2f(tau), iE = rcpf(E);
     const double l0 = x - f2d(px * iE * tf);
     const double l1 = y - f2d(py * iE * tf);
-    const float k = (kp.m2_f + px * px + py * py) / (E + pz) * iE;
+    const float k = (kp.m2_f + fmaf(px, px, py * py)) * rcpf((E + pz) * E);
     const double l2 = -tau + f2d(tf * k);
     for (int j = 0; j < 3; ++j) v[j] = fma(l2, T[2][j], fma(l1, T[1][j], l0 * T[0][j]));
     v[2] *= g0;
@@ -720,7 +969,7 @@ template <bool VEC>
 __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, const double* __restrict__ q,
                                               const KickParams& kp, float* __restrict__ X, double* __restrict__ part,
                                               ScState* st, VBlk vb) {
-    __shared__ double sm[5 * 32];
+    __shared__ float smq[5 * 64];
     __shared__ float smf[3 * 32];
     __shared__ float bmin[3], bmax[3];
     __shared__ unsigned long long emin[3], emax[3];
@@ -751,14 +1000,15 @@ __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, con
         for (int w = 0; w < W_; ++w) {
             float px, py, pz, E;
             mom32(r[1][w], r[3][w], r[5][w], kp, px, py, pz, E);
-            float vw[3];
-            pos32(r[0][w], r[2][w], r[4][w], px, py, pz, E, T, g0, vw);
+            float lw[3], vw[3];
+            lab32(r[0][w], r[2][w], r[4][w], px, py, pz, E, kp, lw);
+            rot32(lw, T, g0, vw);
             for (int j = 0; j < 3; ++j) v[j][w] = vw[j];
             const float qi = qq[w];
-            for (int j = 0; j < 3; ++j) {
+            for (int j = 0; j < 3; ++j) {  // charge moments of the lab positions
                 mnf[j] = fminf(mnf[j], v[j][w]);
                 mxf[j] = fmaxf(mxf[j], v[j][w]);
-                qsf[j] += qi * v[j][w];
+                qsf[j] = fmaf(qi, lw[j], qsf[j]);
             }
             qsf[3] += qi;
             qsf[4] += fabsf(qi);
@@ -769,8 +1019,8 @@ __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, con
     // float extremes reduce exactly in float; the sums in double
     block_minmax_f<3, false>(mnf, smf);
     block_minmax_f<3, true>(mxf, smf);
-    double qs[5] = {qsf[0], qsf[1], qsf[2], qsf[3], qsf[4]};
-    block_sum<5>(qs, sm);
+    float qhi[5], qlo[5];
+    block_sum_f2<5>(qsf, qhi, qlo, smq);
     if (threadIdx.x == 0)
         for (int j = 0; j < 3; ++j) {
             bmin[j] = mnf[j];
@@ -809,23 +1059,25 @@ __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, con
         PAIR_LOOP_END
     }
     __syncthreads();
+    ExtPart32* ep = reinterpret_cast<ExtPart32*>(part);
     if (threadIdx.x == 0 && SC_IDX_OK(st, 12, vb.x, kp.n > 0 ? vb.nx : 0)) {
-        double* o = part + vb.x * PART_EXT;
         for (int k = 0; k < 3; ++k) {
-            o[k] = unord64(emin[k]);
-            o[3 + k] = unord64(emax[k]);
-            o[6 + k] = qs[k];
+            ep[vb.x].mn[k] = emin[k];
+            ep[vb.x].mx[k] = emax[k];
         }
-        o[9] = qs[3];
-        o[10] = qs[4];
+        for (int k = 0; k < 5; ++k) {
+            ep[vb.x].hi[k] = qhi[k];
+            ep[vb.x].lo[k] = qlo[k];
+        }
     }
-    if (arrive_last(&st->done_extent, vb.nx)) mesh_finalize(part, vb.nx, kp, st, -1.0);
+    if (arrive_last(&st->done_extent, vb.nx)) mesh_finalize32(ep, vb.nx, kp, st);
 }
 
 template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ rp, const double* __restrict__ q,
                                                     KickParams kp, float* __restrict__ X, double* __restrict__ part,
                                                     ScState* st) {
+    pdl_wait();
     extent32_body<VEC>(rp, q, kp, X, part, st, hw_vblk());
 }
 
@@ -838,12 +1090,12 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
                                                   const KickParams& kp, float* __restrict__ X,
                                                   double* __restrict__ part, ScState* st, VBlk vb) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    __shared__ double sm[5 * 32];
+    __shared__ float smq[5 * 64];
     __shared__ float smf[3 * 32];
     __shared__ float bmin[3], bmax[3];
     __shared__ unsigned long long emin[3], emax[3];
-    double* buf = reinterpret_cast<double*>(smraw);  // [PS_STAGES][7][PT_TILE]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + PS_STAGES * 7 * PT_TILE);
+    double* buf = reinterpret_cast<double*>(smraw);  // [EX_STAGES][7][PT_TILE]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + EX_STAGES * 7 * PT_TILE);
     float mnf[3] = {INFINITY, INFINITY, INFINITY}, mxf[3] = {-INFINITY, -INFINITY, -INFINITY};
     float qsf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
@@ -857,12 +1109,14 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
     auto one = [&](const double (&r)[6], double qd, float (&v)[3]) {
         float px, py, pz, E;
         mom32(d2f(r[1]), d2f(r[3]), d2f(r[5]), kp, px, py, pz, E);
-        pos32(d2f(r[0]), d2f(r[2]), d2f(r[4]), px, py, pz, E, T, g0, v);
+        float l[3];
+        lab32(d2f(r[0]), d2f(r[2]), d2f(r[4]), px, py, pz, E, kp, l);
+        rot32(l, T, g0, v);
         const float qi = d2f(qd);
-        for (int j = 0; j < 3; ++j) {
+        for (int j = 0; j < 3; ++j) {  // charge moments of the lab positions
             mnf[j] = fminf(mnf[j], v[j]);
             mxf[j] = fmaxf(mxf[j], v[j]);
-            qsf[j] += qi * v[j];
+            qsf[j] = fmaf(qi, l[j], qsf[j]);
         }
         qsf[3] += qi;
         qsf[4] += fabsf(qi);
@@ -901,14 +1155,14 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
             for (int k = 0; k < 3; ++k) X[k * nX + i] = v[k];
         }
     };
-    const bool streamed = stream_tiles(Tl, bar, issue, body);
+    const bool streamed = stream_tiles<EX_STAGES>(Tl, bar, issue, body);
     if (!streamed && threadIdx.x == 0) atomicCAS(&st->status, SC_OK, SC_ERR_TIMEOUT);
     const float my_mn[3] = {mnf[0], mnf[1], mnf[2]}, my_mx[3] = {mxf[0], mxf[1], mxf[2]};
     // float extremes reduce exactly in float; the sums in double
     block_minmax_f<3, false>(mnf, smf);
     block_minmax_f<3, true>(mxf, smf);
-    double qs[5] = {qsf[0], qsf[1], qsf[2], qsf[3], qsf[4]};
-    block_sum<5>(qs, sm);
+    float qhi[5], qlo[5];
+    block_sum_f2<5>(qsf, qhi, qlo, smq);
     if (threadIdx.x == 0)
         for (int j = 0; j < 3; ++j) {
             bmin[j] = mnf[j];
@@ -949,22 +1203,24 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
             }
     }
     __syncthreads();
+    ExtPart32* ep = reinterpret_cast<ExtPart32*>(part);
     if (threadIdx.x == 0 && SC_IDX_OK(st, 12, vb.x, kp.n > 0 ? vb.nx : 0)) {
-        double* o = part + vb.x * PART_EXT;
         for (int k = 0; k < 3; ++k) {
-            o[k] = unord64(emin[k]);
-            o[3 + k] = unord64(emax[k]);
-            o[6 + k] = qs[k];
+            ep[vb.x].mn[k] = emin[k];
+            ep[vb.x].mx[k] = emax[k];
         }
-        o[9] = qs[3];
-        o[10] = qs[4];
+        for (int k = 0; k < 5; ++k) {
+            ep[vb.x].hi[k] = qhi[k];
+            ep[vb.x].lo[k] = qlo[k];
+        }
     }
-    if (arrive_last(&st->done_extent, vb.nx)) mesh_finalize(part, vb.nx, kp, st, -1.0);
+    if (arrive_last(&st->done_extent, vb.nx)) mesh_finalize32(ep, vb.nx, kp, st);
 }
 
 __global__ void __launch_bounds__(PT, 3) k_extent32_tma(const double* __restrict__ rp, const double* __restrict__ q,
                                                         KickParams kp, float* __restrict__ X,
                                                         double* __restrict__ part, ScState* st) {
+    pdl_wait();
     extent32_tma_body(rp, q, kp, X, part, st, hw_vblk());
 }
 
@@ -973,6 +1229,7 @@ template <typename R>
 __global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, const double* __restrict__ q, KickParams kp,
                                                    double gamma, R* __restrict__ X, double* __restrict__ part,
                                                    ScState* st) {
+    pdl_wait();
     __shared__ double sm[5 * 32];
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     double qs[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -996,6 +1253,7 @@ __global__ void __launch_bounds__(PT) k_extent_xyz(double* __restrict__ Xin, con
 
 // potential entry: explicit spacing
 __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickParams kp) {
+    pdl_wait();
     st->status = SC_OK;
     st->steps[0] = hx;
     st->steps[1] = hy;
@@ -1022,6 +1280,7 @@ __device__ __forceinline__ bool key_of(double fx, double fy, double fz, const Ki
 
 __global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t* __restrict__ keys, KickParams kp,
                                                ScState* st) {
+    pdl_wait();
     if (st->status) return;
     const int64_t n = kp.n;
     const double s0 = st->steps[0], s1 = st->steps[1], s2 = st->steps[2];
@@ -1078,13 +1337,12 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
                                             VBlk vb) {
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
-    float sf[3], of[3], is[3];
+    float of[3], is[3];
     for (int j = 0; j < 3; ++j) {
-        sf[j] = st->stepsf[j];
         of[j] = st->xofff[j];
         is[j] = st->istepsf[j];
     }
-    const float ig0 = st->ig0f;
+    const float ig0 = st->ig0f, g0 = st->g0f;
     const int S = st->qfix_shift;
     bool bad = false;
     PAIR_LOOP_BEGIN(n)
@@ -1097,12 +1355,14 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
     for (int w = 0; w < W_; ++w) {
         const int64_t i = i0_ + w;
         const float v0 = v[0][w], v1 = v[1][w], v2 = v[2][w];
-        const float nrm = sqrtf(v0 * v0 + v1 * v1 + (v2 * ig0) * (v2 * ig0));  // |lab position|
-        float g[3] = {grid32(v0, sf[0], of[0]), grid32(v1, sf[1], of[1]), grid32(v2, sf[2], of[2])};
+        const float nrm = sqrtf_fast(fmaf(v0, v0, fmaf(v1, v1, (v2 * ig0) * (v2 * ig0))));  // |lab position|
+        float g[3] = {grid32(v0, is[0], of[0]), grid32(v1, is[1], of[1]), grid32(v2, is[2], of[2])};
         bool amb = false;
         for (int j = 0; j < 3; ++j) {
-            const float scale = (j == 2 ? nrm / ig0 : nrm) * is[j] + fabsf(of[j]) + 1.0f;
-            const float tol = ldexpf(scale, -19);  // >= 4x the FP32 rounding bound of g
+            const float scale = (j == 2 ? nrm * g0 : nrm) * is[j] + fabsf(of[j]) + 1.0f;
+            // 16 units in the last place of the scale: 2x the error bound of g
+            // (FP32 position with approximate momenta, product, difference)
+            const float tol = ldexpf(scale, -19);
             const float f = g[j] - floorf(g[j]);
             amb |= !(f >= tol && f <= 1.0f - tol);
         }
@@ -1141,6 +1401,7 @@ template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
                                                   const double* __restrict__ rp, const double* __restrict__ q,
                                                   unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
+    pdl_wait();
     keys32_body<VEC>(X, keys, rp, q, qfix, kp, st, hw_vblk());
 }
 
@@ -1215,6 +1476,7 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
                                                const double* __restrict__ X, const double* __restrict__ ex,
                                                const double* __restrict__ ey, const double* __restrict__ ez,
                                                KickParams kp, const ScState* st) {
+    pdl_wait();
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld;
     double T[3][3];
@@ -1246,7 +1508,6 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
 struct Kick32C {
     float T[3][3];
     float kxyg, kz, ipref, m2;
-    float gamref, betaref, igrbr2, pref, m;
     float isf[3], of[3];  // 1/steps (times gamma0 along z), X_off
     const float *ox, *oy, *oz;
 };
@@ -1259,11 +1520,6 @@ __device__ __forceinline__ Kick32C kick32_const(const ScState* st, const KickPar
     c.kz = st->kzf;
     c.ipref = kp.ipref_f;
     c.m2 = kp.m2_f;
-    c.gamref = kp.gamref_f;
-    c.betaref = kp.betaref_f;
-    c.igrbr2 = (float)(1.0 / (kp.grbr * kp.grbr));
-    c.pref = kp.pref_f;
-    c.m = kp.m_f;
     for (int j = 0; j < 3; ++j) {
         c.isf[j] = st->istepsf[j];
         c.of[j] = st->xofff[j];
@@ -1275,18 +1531,6 @@ __device__ __forceinline__ Kick32C kick32_const(const ScState* st, const KickPar
     return c;
 }
 
-// the hardware's approximate reciprocal and square root (relative error
-// ~1e-7, far inside the FP32 form's error budget)
-__device__ __forceinline__ float rcpf(float x) {
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float sqrtf_fast(float x) {
-    float y;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
 __device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b - a, a); }
 
 // Trilinear sample coordinate along one axis of length n (map_coordinates
@@ -1327,23 +1571,17 @@ __device__ __forceinline__ float oct_sample(const float* __restrict__ O, const A
 // are decided by the keys kernel alone; the gather only needs the grid
 // coordinates to FP32 accuracy.)
 __device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp) {
-    (void)kp;
-    // momenta (eV/c) and energy (eV), coord_transform.py:64-72: gamma from
-    // delta, |p|^2 = (gamma^2 - 1) m^2, pz from |p|^2 - px^2 - py^2
-    const float xq = d2f(r[1]), yq = d2f(r[3]), dl = d2f(r[5]);
-    const float gamma = C.gamref * fmaf(C.betaref, dl, 1.0f);
-    const float g2 = fmaf(gamma, gamma, -1.0f) * C.igrbr2;
-    const float pz2 = sqrtf_fast(g2 - fmaf(xq, xq, yq * yq));
-    const float px = xq * C.pref, py = yq * C.pref, pz = pz2 * C.pref, E = gamma * C.m;
-    // lab position (coord_transform.py:89-95), rotated and scaled to the grid
+    float px, py, pz, E;
+    mom32(d2f(r[1]), d2f(r[3]), d2f(r[5]), kp, px, py, pz, E);
+    // lab position, rotated and scaled to the grid
     const float tau = d2f(r[4]);
     const float iE = rcpf(E);
-    const float s = tau * iE;
-    const float l0 = fmaf(-px, s, d2f(r[0])), l1 = fmaf(-py, s, d2f(r[2])), l2 = -pz * s;
+    float l[3];
+    lab32(d2f(r[0]), d2f(r[2]), tau, px, py, pz, E, kp, l);
     float X[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-        X[j] = fmaf(fmaf(l0, C.T[0][j], fmaf(l1, C.T[1][j], l2 * C.T[2][j])), C.isf[j], -C.of[j]);
+        X[j] = fmaf(fmaf(l[0], C.T[0][j], fmaf(l[1], C.T[1][j], l[2] * C.T[2][j])), C.isf[j], -C.of[j]);
     // staggered trilinear gather (sc.py:201-204): each component is sampled
     // at +0.5 on the two axes it is not differentiated along
     const AxisW a0 = axis_w(X[0], kp.nx), a1 = axis_w(X[1], kp.ny), a2 = axis_w(X[2], kp.nz);
@@ -1518,6 +1756,7 @@ __global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) k_kick32(double* __restri
                                                                 const float* __restrict__ oy,
                                                                 const float* __restrict__ oz, KickParams kp,
                                                                 const ScState* st) {
+    pdl_wait();
     kick32_body<G>(rp, ox, oy, oz, kp, st, hw_vblk());
 }
 
@@ -1526,6 +1765,7 @@ __global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) k_kick32_tma(double* __re
                                                                     const float* __restrict__ oy,
                                                                     const float* __restrict__ oz, KickParams kp,
                                                                     ScState* st) {
+    pdl_wait();
     kick32_tma_body(rp, ox, oy, oz, kp, st, hw_vblk());
 }
 
@@ -1542,6 +1782,7 @@ template <typename R>
 __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, const R* __restrict__ ex,
                                                    const R* __restrict__ ey, const R* __restrict__ ez,
                                                    double* __restrict__ out, KickParams kp, const ScState* st) {
+    pdl_wait();
     if (st->status) return;
     const int64_t n = kp.n, nX = kp.nX;
     const double g0 = st->gamma0;
@@ -1565,6 +1806,7 @@ __global__ void __launch_bounds__(PT) k_gather_xyz(const R* __restrict__ X, cons
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(PT, 4) kb_frame32(const BatchBeam* __restrict__ beams,
                                                     const int* __restrict__ start, int nb) {
+    pdl_wait();
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
     const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
@@ -1578,6 +1820,7 @@ __global__ void __launch_bounds__(PT, 4) kb_frame32(const BatchBeam* __restrict_
 
 __global__ void __launch_bounds__(PT, 3) kb_extent32(const BatchBeam* __restrict__ beams,
                                                      const int* __restrict__ start, int nb) {
+    pdl_wait();
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
     const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
@@ -1590,6 +1833,7 @@ __global__ void __launch_bounds__(PT, 3) kb_extent32(const BatchBeam* __restrict
 
 __global__ void __launch_bounds__(PT, 4) kb_keys32(const BatchBeam* __restrict__ beams,
                                                    const int* __restrict__ start, int nb) {
+    pdl_wait();
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
     const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
@@ -1603,6 +1847,7 @@ __global__ void __launch_bounds__(PT, 4) kb_keys32(const BatchBeam* __restrict__
 
 __global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) kb_kick32(const BatchBeam* __restrict__ beams,
                                                                  const int* __restrict__ start, int nb) {
+    pdl_wait();
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
     const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
@@ -1618,10 +1863,10 @@ cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, co
                                    cudaStream_t s) {
     if (blocks <= 0) return cudaSuccess;
     switch (k) {
-        case BP_FRAME: kb_frame32<<<blocks, PT, FR_SMEM, s>>>(beams, start, nb); break;
-        case BP_EXTENT: kb_extent32<<<blocks, PT, EX_SMEM, s>>>(beams, start, nb); break;
-        case BP_KEYS: kb_keys32<<<blocks, PT, 0, s>>>(beams, start, nb); break;
-        case BP_KICK: kb_kick32<<<blocks, PT, KT_SMEM, s>>>(beams, start, nb); break;
+        case BP_FRAME: launch(kb_frame32, blocks, PT, FR_SMEM, s, beams, start, nb); break;
+        case BP_EXTENT: launch(kb_extent32, blocks, PT, EX_SMEM, s, beams, start, nb); break;
+        case BP_KEYS: launch(kb_keys32, blocks, PT, 0, s, beams, start, nb); break;
+        case BP_KICK: launch(kb_kick32, blocks, PT, KT_SMEM, s, beams, start, nb); break;
     }
     return cudaGetLastError();
 }
@@ -1662,10 +1907,10 @@ cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickPar
     double* part = reinterpret_cast<double*>(ws + L.part_frame);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_frame64<<<nb, PT, 0, s>>>(rp, kp, reinterpret_cast<double*>(ws + L.xp), part, st);
+        launch(k_frame64, nb, PT, 0, s, rp, kp, reinterpret_cast<double*>(ws + L.xp), part, st);
     else
-        vec_ok(rp, kp.ld, nullptr) ? k_frame32_tma<<<nb, PT, FR_SMEM, s>>>(rp, kp, part, st)
-                                   : k_frame32<false><<<nb, PT, 0, s>>>(rp, kp, part, st);
+        vec_ok(rp, kp.ld, nullptr) ? launch(k_frame32_tma, nb, PT, FR_SMEM, s, rp, kp, part, st)
+                                   : launch(k_frame32<false>, nb, PT, 0, s, rp, kp, part, st);
     return cudaGetLastError();
 }
 
@@ -1675,12 +1920,12 @@ cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickPa
     double* part = reinterpret_cast<double*>(ws + L.part_ext);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_extent64<<<nb, PT, 0, s>>>(reinterpret_cast<const double*>(ws + L.xp), q, kp,
+        launch(k_extent64, nb, PT, 0, s, reinterpret_cast<const double*>(ws + L.xp), q, kp,
                                      reinterpret_cast<double*>(ws + L.X), part, st);
     else
         vec_ok(rp, kp.ld, q)
-            ? k_extent32_tma<<<nb, PT, EX_SMEM, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st)
-            : k_extent32<false><<<nb, PT, 0, s>>>(rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
+            ? launch(k_extent32_tma, nb, PT, EX_SMEM, s, rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st)
+            : launch(k_extent32<false>, nb, PT, 0, s, rp, q, kp, reinterpret_cast<float*>(ws + L.X), part, st);
     return cudaGetLastError();
 }
 
@@ -1690,16 +1935,16 @@ cudaError_t launch_extent_xyz(const Plan& p, const Layout& L, char* ws, const Ki
     double* part = reinterpret_cast<double*>(ws + L.part_ext);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_extent_xyz<double><<<nb, PT, 0, s>>>(X, q, kp, gamma, reinterpret_cast<double*>(ws + L.X), part, st);
+        launch(k_extent_xyz<double>, nb, PT, 0, s, X, q, kp, gamma, reinterpret_cast<double*>(ws + L.X), part, st);
     else
-        k_extent_xyz<float><<<nb, PT, 0, s>>>(X, q, kp, gamma, reinterpret_cast<float*>(ws + L.X), part, st);
+        launch(k_extent_xyz<float>, nb, PT, 0, s, X, q, kp, gamma, reinterpret_cast<float*>(ws + L.X), part, st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const KickParams& kp, double hx, double hy,
                             double hz, cudaStream_t s) {
     (void)p;
-    k_set_mesh<<<1, 1, 0, s>>>(reinterpret_cast<ScState*>(ws + L.state), hx, hy, hz, kp);
+    launch(k_set_mesh, 1, 1, 0, s, reinterpret_cast<ScState*>(ws + L.state), hx, hy, hz, kp);
     return cudaGetLastError();
 }
 
@@ -1709,7 +1954,7 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
     const int nb = particle_blocks(p, kp.n);
     uint32_t* keys = reinterpret_cast<uint32_t*>(ws + L.keys);
     if (p.prec == SC_FP64)
-        k_keys64<<<nb, PT, 0, s>>>(reinterpret_cast<double*>(ws + L.X), keys, kp, st);
+        launch(k_keys64, nb, PT, 0, s, reinterpret_cast<double*>(ws + L.X), keys, kp, st);
     else
     {
         unsigned long long* qfix = nullptr;
@@ -1719,9 +1964,9 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
             if (e) return e;
         }
         if (!qfix || (uintptr_t)q % 16 == 0)
-            k_keys32<true><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+            launch(k_keys32<true>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
         else
-            k_keys32<false><<<nb, PT, 0, s>>>(reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+            launch(k_keys32<false>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
     }
     return cudaGetLastError();
 }
@@ -1731,7 +1976,7 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_kick64<<<nb, PT, 0, s>>>(rp, reinterpret_cast<const double*>(ws + L.xp),
+        launch(k_kick64, nb, PT, 0, s, rp, reinterpret_cast<const double*>(ws + L.xp),
                                    reinterpret_cast<const double*>(ws + L.X), reinterpret_cast<const double*>(ws + L.ex),
                                    reinterpret_cast<const double*>(ws + L.ey), reinterpret_cast<const double*>(ws + L.ez),
                                    kp, st);
@@ -1746,8 +1991,8 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
         const int64_t kb = units < (int64_t)p.sm_count * KICK_MIN_BLOCKS ? units : (int64_t)p.sm_count * KICK_MIN_BLOCKS;
         const int nbk = (int)(kb > 0 ? kb : 1);
         ScState* stw = reinterpret_cast<ScState*>(ws + L.state);
-        if (g >= 2) k_kick32_tma<<<nbk, PT, KT_SMEM, s>>>(rp, ox, oy, oz, kp, stw);
-        else k_kick32<1><<<nbk, PT, 0, s>>>(rp, ox, oy, oz, kp, st);
+        if (g >= 2) launch(k_kick32_tma, nbk, PT, KT_SMEM, s, rp, ox, oy, oz, kp, stw);
+        else launch(k_kick32<1>, nbk, PT, 0, s, rp, ox, oy, oz, kp, st);
     }
     return cudaGetLastError();
 }
@@ -1757,12 +2002,12 @@ cudaError_t launch_gather_xyz(const Plan& p, const Layout& L, char* ws, const Ki
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
-        k_gather_xyz<double><<<nb, PT, 0, s>>>(reinterpret_cast<const double*>(ws + L.X),
+        launch(k_gather_xyz<double>, nb, PT, 0, s, reinterpret_cast<const double*>(ws + L.X),
                                                reinterpret_cast<const double*>(ws + L.ex),
                                                reinterpret_cast<const double*>(ws + L.ey),
                                                reinterpret_cast<const double*>(ws + L.ez), exyz, kp, st);
     else
-        k_gather_xyz<float><<<nb, PT, 0, s>>>(reinterpret_cast<const float*>(ws + L.X),
+        launch(k_gather_xyz<float>, nb, PT, 0, s, reinterpret_cast<const float*>(ws + L.X),
                                               reinterpret_cast<const float*>(ws + L.exq),
                                               reinterpret_cast<const float*>(ws + L.eyq),
                                               reinterpret_cast<const float*>(ws + L.ezq), exyz, kp, st);

@@ -33,6 +33,7 @@ constexpr unsigned FULLM = 0xffffffffu;
 
 __global__ void __launch_bounds__(RT) k_rhist(const uint32_t* __restrict__ keys, int64_t n, int shift, int bins,
                                               uint32_t* __restrict__ hist) {
+    pdl_wait();
     __shared__ uint32_t h[RBINS];
     for (int d = threadIdx.x; d < RBINS; d += RT) h[d] = 0;
     __syncthreads();
@@ -48,6 +49,7 @@ __global__ void __launch_bounds__(RT) k_rhist(const uint32_t* __restrict__ keys,
 }
 
 __global__ void k_rrowscan(uint32_t* __restrict__ hist, int nblk, int bins, uint32_t* __restrict__ tot) {
+    pdl_wait();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= bins) return;
@@ -73,6 +75,7 @@ __global__ void __launch_bounds__(RT) k_rscatter(const uint32_t* __restrict__ ki
                                                  const uint32_t* __restrict__ tot, uint32_t* __restrict__ kout,
                                                  uint32_t* __restrict__ vout, const double* __restrict__ qsrc,
                                                  void* __restrict__ qout, int qfloat) {
+    pdl_wait();
     __shared__ uint32_t base[RBINS];
     __shared__ uint32_t wc[RWARPS][RBINS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -164,10 +167,10 @@ cudaError_t launch_sort(const uint32_t* keys_in, int64_t n, int key_bits, uint32
         const int bins = 1 << dbits;
         uint32_t* dk = to_out ? keys_out : tmp_k;
         uint32_t* dv = to_out ? perm_out : tmp_v;
-        k_rhist<<<nb, RT, 0, s>>>(sk, n, shift, bins, hist);
-        k_rrowscan<<<(bins * 32 + 255) / 256, 256, 0, s>>>(hist, nb, bins, tot);
+        launch(k_rhist, nb, RT, 0, s, sk, n, shift, bins, hist);
+        launch(k_rrowscan, (bins * 32 + 255) / 256, 256, 0, s, hist, nb, bins, tot);
         const bool last = p == passes - 1;
-        k_rscatter<<<nb, RT, 0, s>>>(sk, sv, n, shift, bins, hist, tot, dk, dv, last ? q_src : nullptr,
+        launch(k_rscatter, nb, RT, 0, s, sk, sv, n, shift, bins, hist, tot, dk, dv, last ? q_src : nullptr,
                                      last ? q_out : nullptr, q_float ? 1 : 0);
         sk = dk;
         sv = dv;
@@ -180,6 +183,7 @@ cudaError_t launch_sort(const uint32_t* keys_in, int64_t n, int key_bits, uint32
 // empty cell, from a memset).
 __global__ void k_cell_bounds(const uint32_t* __restrict__ sk, int64_t n, uint32_t* __restrict__ start,
                               uint32_t* __restrict__ end, const ScState* st) {
+    pdl_wait();
     if (st->status) return;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t key = sk[j];
@@ -203,6 +207,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_deposit_cells(const R* __restrict__ sq, const uint32_t* __restrict__ start,
                                                        const uint32_t* __restrict__ end, int64_t ncell,
                                                        R* __restrict__ qgrid, const ScState* st) {
+    pdl_wait();
     if (st->status) return;
     const int lane = threadIdx.x & 31;
     const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -251,13 +256,13 @@ cudaError_t launch_deposit(const Plan& p, const Layout& L, char* ws, const doubl
     const uint32_t* sk = reinterpret_cast<const uint32_t*>(ws + L.sort_keys);
     uint32_t* cs = reinterpret_cast<uint32_t*>(ws + L.cell_start);
     uint32_t* ce = reinterpret_cast<uint32_t*>(ws + L.cell_end);
-    k_cell_bounds<<<(int)b, 256, 0, s>>>(sk, n, cs, ce, st);
+    launch(k_cell_bounds, (int)b, 256, 0, s, sk, n, cs, ce, st);
     const int cb = p.sm_count * 8;
     if (p.prec == SC_FP64)
-        k_deposit_cells<double><<<cb, 256, 0, s>>>(reinterpret_cast<const double*>(ws + L.sort_q), cs, ce, ncell,
+        launch(k_deposit_cells<double>, cb, 256, 0, s, reinterpret_cast<const double*>(ws + L.sort_q), cs, ce, ncell,
                                                    reinterpret_cast<double*>(ws + L.qgrid), st);
     else
-        k_deposit_cells<float><<<cb, 256, 0, s>>>(reinterpret_cast<const float*>(ws + L.sort_q), cs, ce, ncell,
+        launch(k_deposit_cells<float>, cb, 256, 0, s, reinterpret_cast<const float*>(ws + L.sort_q), cs, ce, ncell,
                                                   reinterpret_cast<float*>(ws + L.qgrid), st);
     return cudaGetLastError();
 }

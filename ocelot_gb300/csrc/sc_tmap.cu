@@ -29,6 +29,7 @@ __device__ __forceinline__ void tmap_one(const double* __restrict__ m, double* _
 }
 
 __global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, int64_t ld, int64_t n) {
+    pdl_wait();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         tmap_one(m.m, rp, ld, i);
 }
@@ -36,6 +37,7 @@ __global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, i
 // batched: each beam's own map from the work table, over the beam's blocks
 __global__ void __launch_bounds__(256) kb_tmap(const BatchBeam* __restrict__ beams, const int* __restrict__ start,
                                                int nb) {
+    pdl_wait();
     __shared__ double m[42];
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
@@ -50,7 +52,7 @@ __global__ void __launch_bounds__(256) kb_tmap(const BatchBeam* __restrict__ bea
 
 cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s) {
     if (nb <= 0 || blocks <= 0) return cudaSuccess;
-    kb_tmap<<<blocks, 256, 0, s>>>(beams, start, nb);
+    launch(kb_tmap, blocks, 256, 0, s, beams, start, nb);
     return cudaGetLastError();
 }
 
@@ -60,6 +62,7 @@ cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, 
 // reads the counter before k_advance (the next launch on the stream) moves it.
 __global__ void __launch_bounds__(256) k_tmap_indexed(const double* __restrict__ table, const int* __restrict__ counter,
                                                       int nmaps, double* __restrict__ rp, int64_t ld, int64_t n) {
+    pdl_wait();
     __shared__ double m[42];
     const int idx = *counter;
     if (idx < 0 || idx >= nmaps) return;
@@ -69,12 +72,13 @@ __global__ void __launch_bounds__(256) k_tmap_indexed(const double* __restrict__
         tmap_one(m, rp, ld, i);
 }
 
-__global__ void k_advance(int* counter, int delta) { *counter += delta; }
+__global__ void k_advance(int* counter, int delta) {
+    pdl_wait(); *counter += delta; }
 
 cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld, int64_t n,
                                 cudaStream_t s) {
     if (n <= 0) {
-        k_advance<<<1, 1, 0, s>>>(counter, 1);
+        launch(k_advance, 1, 1, 0, s, counter, 1);
         return cudaGetLastError();
     }
     int dev = 0, sm = 148;
@@ -83,8 +87,8 @@ cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, do
     int64_t b = (n + 255) / 256;
     const int64_t cap = (int64_t)sm * 8;
     if (b > cap) b = cap;
-    k_tmap_indexed<<<(int)b, 256, 0, s>>>(table, counter, nmaps, rp, ld, n);
-    k_advance<<<1, 1, 0, s>>>(counter, 1);
+    launch(k_tmap_indexed, (int)b, 256, 0, s, table, counter, nmaps, rp, ld, n);
+    launch(k_advance, 1, 1, 0, s, counter, 1);
     return cudaGetLastError();
 }
 
@@ -99,7 +103,7 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
     int64_t b = (n + 255) / 256;
     const int64_t cap = (int64_t)sm * 8;
     if (b > cap) b = cap;
-    k_tmap<<<(int)b, 256, 0, s>>>(m, rp, ld, n);
+    launch(k_tmap, (int)b, 256, 0, s, m, rp, ld, n);
     return cudaGetLastError();
 }
 

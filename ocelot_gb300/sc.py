@@ -146,6 +146,10 @@ class Engine:
     def profile(self, enable: bool = True):
         N.check(self.lib.sc_profile_enable(self.plan, 1 if enable else 0))
 
+    def launches(self) -> int:
+        """Kernels launched by the last kick (host bookkeeping)."""
+        return int(self.lib.sc_kick_launches(self.plan))
+
     def profile_read(self):
         """{stage: ms} of the last kick and the number of kernels it launched (synchronous)."""
         ms = (C.c_float * N.SC_NSTAGES)()
