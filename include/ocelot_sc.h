@@ -222,6 +222,27 @@ int sc_tmap_apply(const double* R, const double* B, double* rparticles, int64_t 
 int sc_tmap_apply_indexed(const double* table, int* counter, int nmaps, double* rparticles,
                           int64_t ld, int64_t n, void* stream);
 
+/* Second-order maps: SecondTM.t_apply of drift/quadrupole slices
+ * (ocelot/cpbd/transformations/second_order.py:31-38, SecondOrderMult.numpy_apply,
+ * ocelot/cpbd/tm_utils.py:54-55): x <- R.x + T:xx, then x <- x + B.
+ *   maps: DEVICE float64[nmaps * SC_MAP2_DOUBLES], map m at maps + m*SC_MAP2_DOUBLES:
+ *         R[36] row-major (tilt applied), B[6], then Tc[6][21], the coefficient
+ *         of x_j x_k (j <= k, pairs in lexicographic order) in output i, i.e.
+ *         T[i,j,k] + T[i,k,j] for j < k and T[i,j,j] on the diagonal.
+ * The maps are applied in order with each particle's coordinates kept in
+ * registers (second-order maps do not compose exactly, so the slices of a
+ * step are not multiplied together). */
+#define SC_MAP2_DOUBLES 168
+int sc_tmap2_apply(const double* maps, int nmaps, double* rparticles, int64_t ld, int64_t n, void* stream);
+
+/* The second-order transport of a tracking loop kept on the device: the maps
+ * [first[s], first[s+1]) of a device table at s = *counter (a device int;
+ * out of range: no transport), then *counter += 1, in stream order, so that
+ * one recorded step replays for every step (as sc_tmap_apply_indexed).
+ *   first: DEVICE int32[nsteps + 1]. */
+int sc_tmap2_apply_step(const double* maps, const int* first, int* counter, int nsteps, double* rparticles,
+                        int64_t ld, int64_t n, void* stream);
+
 /* ---- stage timing (benchmarking) --------------------------------------- */
 
 /* Stages of sc_kick: MAD->lab frame (coord_transform.py:57-96,

@@ -107,4 +107,93 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Second-order maps (SecondTM of drift/quadrupole slices,
+// ocelot/cpbd/transformations/second_order.py:31-38):
+//   y = R.x + sum_{j<=k} Tc[i][jk] x_j x_k,   x <- y + B
+// with Tc the combined coefficient T[i,j,k] + T[i,k,j] (j < k) or T[i,j,j].
+// A map is MAP2 doubles: R (row-major), B, then Tc[6][21] with the pairs
+// (j, k), j <= k, in lexicographic order.  Every thread reads the same map
+// entries, so the test that skips a zero coefficient is warp-uniform.
+// ---------------------------------------------------------------------------
+constexpr int MAP2 = 36 + 6 + 6 * 21;
+
+__device__ __forceinline__ void tmap2_one(const double* __restrict__ m, double (&x)[6]) {
+    double p[21];
+    int q = 0;
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+#pragma unroll
+        for (int k = j; k < 6; ++k) p[q++] = __dmul_rn(x[j], x[k]);
+    double y[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        double acc = __dmul_rn(__ldg(m + r * 6), x[0]);
+#pragma unroll
+        for (int k = 1; k < 6; ++k) acc = __fma_rn(__ldg(m + r * 6 + k), x[k], acc);
+#pragma unroll
+        for (int t = 0; t < 21; ++t) {
+            const double v = __ldg(m + 42 + r * 21 + t);
+            if (v != 0.0) acc = __fma_rn(v, p[t], acc);
+        }
+        y[r] = acc;
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) x[r] = __dadd_rn(y[r], __ldg(m + 36 + r));
+}
+
+// maps [first, last) of the table applied in order to every particle, its
+// coordinates kept in registers between maps
+__device__ __forceinline__ void tmap2_range(const double* __restrict__ maps, int first, int last,
+                                            double* __restrict__ rp, int64_t ld, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double x[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
+        for (int mi = first; mi < last; ++mi) tmap2_one(maps + (size_t)mi * MAP2, x);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) rp[k * ld + i] = x[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_tmap2(const double* __restrict__ maps, int nmaps, double* __restrict__ rp,
+                                               int64_t ld, int64_t n) {
+    pdl_wait();
+    tmap2_range(maps, 0, nmaps, rp, ld, n);
+}
+
+// the maps of step *counter: [first[*counter], first[*counter + 1]) (a
+// device-resident tracking loop's transport, replayed from a CUDA graph)
+__global__ void __launch_bounds__(256) k_tmap2_step(const double* __restrict__ maps, const int* __restrict__ first,
+                                                    const int* __restrict__ counter, int nsteps,
+                                                    double* __restrict__ rp, int64_t ld, int64_t n) {
+    pdl_wait();
+    const int step = *counter;
+    if (step < 0 || step >= nsteps) return;
+    tmap2_range(maps, first[step], first[step + 1], rp, ld, n);
+}
+
+static int tmap_blocks(int64_t n) {
+    int dev = 0, sm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    int64_t b = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm * 8;
+    if (b > cap) b = cap;
+    return (int)(b > 0 ? b : 1);
+}
+
+cudaError_t launch_tmap2(const double* maps, int nmaps, double* rp, int64_t ld, int64_t n, cudaStream_t s) {
+    if (n <= 0 || nmaps <= 0) return cudaSuccess;
+    launch(k_tmap2, tmap_blocks(n), 256, 0, s, maps, nmaps, rp, ld, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tmap2_step(const double* maps, const int* first, int* counter, int nsteps, double* rp, int64_t ld,
+                              int64_t n, cudaStream_t s) {
+    if (n > 0) launch(k_tmap2_step, tmap_blocks(n), 256, 0, s, maps, first, counter, nsteps, rp, ld, n);
+    launch(k_advance, 1, 1, 0, s, counter, 1);
+    return cudaGetLastError();
+}
+
 }  // namespace ocsc

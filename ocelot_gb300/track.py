@@ -18,7 +18,9 @@ Scope: drifts, quadrupoles (with tilt and offsets), markers and monitors --
 the elements whose first-order map is ``uni_matrix`` without bending
 (ocelot/cpbd/r_matrix.py:41-91); one SpaceCharge process attached from the
 first to the last element, the configuration of a space-charge transport
-line.
+line.  With ``order=2`` the transport is the reference's SecondTM instead
+(second_order.py): the slices of a step are not composed but applied one
+after the other in one pass (``sc_tmap2_apply_step``).
 """
 from __future__ import annotations
 
@@ -214,6 +216,26 @@ def step_maps(elements, energy: float, unit_step: float, step: int = 1):
     return steps
 
 
+def step_maps2(elements, energy: float, unit_step: float, step: int = 1):
+    """Second-order maps of every step: (packed slice maps [m, MAP2_DOUBLES],
+    zstep, z0), the slices in the order the reference applies them."""
+    from .second_order import MAP2_DOUBLES, element_map2, pack_map
+    lengths = [_element_params(e)[0] for e in elements]
+    steps = []
+    for slices, zstep, z0 in kick_schedule(lengths, unit_step, step):
+        maps = [pack_map(*element_map2(elements[i], dl, energy)) for i, dl in slices if dl != 0.0]
+        steps.append((np.array(maps).reshape(-1, MAP2_DOUBLES), zstep, z0))
+    return steps
+
+
+def lattice_order(lat) -> int:
+    """2 when the reference lattice tracks with SecondTM (its ``method``
+    dict), else 1."""
+    method = getattr(lat, "method", None)
+    glob = method.get("global") if isinstance(method, dict) else None
+    return 2 if glob is not None and getattr(glob, "__name__", "") == "SecondTM" else 1
+
+
 # ---------------------------------------------------------------------------
 # The device loop
 # ---------------------------------------------------------------------------
@@ -234,7 +256,7 @@ class DeviceTrack:
     DeviceParticleArray (the particles are copied once to the device).
     """
 
-    def __init__(self, elements, sc, unit_step: float, p_array, graph: bool = True, stream=None):
+    def __init__(self, elements, sc, unit_step: float, p_array, graph: bool = True, stream=None, order: int = 1):
         import torch
         from .beam import DeviceParticleArray
         from .sc import Engine, plan_mode
@@ -251,12 +273,23 @@ class DeviceTrack:
         if self.n == 0:
             raise ValueError("zero-size array: the space-charge kick needs at least one particle")
         self.E = float(self.beam.E)
-        self.steps = step_maps(seq, self.E, unit_step, int(sc.step))
-        table = np.zeros((len(self.steps), 42))
-        for k, (R, B, _, _) in enumerate(self.steps):
-            table[k, :36] = R.reshape(-1)
-            table[k, 36:] = B
-        self.table = torch.from_numpy(table).to(self.dev)
+        if order not in (1, 2):
+            raise ValueError("order must be 1 (TransferMap) or 2 (SecondTM)")
+        self.order = order
+        if order == 1:
+            self.steps = step_maps(seq, self.E, unit_step, int(sc.step))
+            table = np.zeros((len(self.steps), 42))
+            for k, (R, B, _, _) in enumerate(self.steps):
+                table[k, :36] = R.reshape(-1)
+                table[k, 36:] = B
+        else:
+            # the slice maps of all steps, and where each step's maps begin
+            steps2 = step_maps2(seq, self.E, unit_step, int(sc.step))
+            self.steps = [(None, None, zstep, z0) for _, zstep, z0 in steps2]
+            table = np.concatenate([m for m, _, _ in steps2]) if steps2 else np.zeros((0, 1))
+            first = np.cumsum([0] + [m.shape[0] for m, _, _ in steps2]).astype(np.int32)
+            self.first = torch.from_numpy(first).to(self.dev)
+        self.table = torch.from_numpy(np.ascontiguousarray(table)).to(self.dev)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.engine = Engine(tuple(int(v) for v in sc.nmesh_xyz), sc.precision, self.dev,
                              plan_mode(sc.precision, sc.deposit, sc.igf))
@@ -282,8 +315,13 @@ class DeviceTrack:
         rp, q = self.beam.rparticles, self.beam.q_array
         lib = self.engine.lib
         s = C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
-        N.check(lib.sc_tmap_apply_indexed(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.counter.data_ptr()),
-                                          len(self.steps), C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
+        if self.order == 1:
+            N.check(lib.sc_tmap_apply_indexed(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.counter.data_ptr()),
+                                              len(self.steps), C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
+        else:
+            N.check(lib.sc_tmap2_apply_step(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.first.data_ptr()),
+                                            C.c_void_p(self.counter.data_ptr()), len(self.steps),
+                                            C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
         self.engine.kick(rp, q, self.n, self.E, zstep)
 
     def _graph(self, zstep: float):
@@ -337,13 +375,15 @@ class DeviceTrack:
         return self.beam.to_host(p_array)
 
 
-def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = True):
+def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = True, order=None):
     """Device counterpart of the reference's ``track(lat, p_array, navi)``
     for a space-charge transport line: the particles go to the GPU once, all
     steps run there, and ``p_array`` is updated in place at the end.
 
     Either pass a Navigator-like ``navi`` (``unit_step`` and one SpaceCharge
     process in ``navi.process_table.proc_list``) or ``sc`` and ``unit_step``.
+    ``order``: 1 (first-order maps, TransferMap) or 2 (SecondTM); by default
+    the lattice's own ``method`` decides.
     Returns (tws, p_array) like the reference, with an empty twiss list.
     """
     if navi is not None:
@@ -363,6 +403,7 @@ def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = Tr
         unit_step = navi.unit_step if unit_step is None else unit_step
     if sc is None or unit_step is None:
         raise ValueError("pass navi, or sc and unit_step")
-    job = DeviceTrack(lattice, sc, unit_step, p_array, graph=graph).run()
+    order = lattice_order(lattice) if order is None else int(order)
+    job = DeviceTrack(lattice, sc, unit_step, p_array, graph=graph, order=order).run()
     job.result(p_array)
     return [], p_array

@@ -21,6 +21,11 @@ What it writes (all under tests/golden/):
 * ``ref_fodo_track.npz`` -- the reference's ``track()`` of a beam with
   ``SpaceCharge`` through FODO cells with first-order maps, with the kick
   positions and lengths its Navigator chose.
+* ``ref_second_order.npz``, ``ref_fodo_track2.npz`` -- second-order
+  tensors and maps (SecondTM) of drifts and quadrupoles and the reference's
+  ``track()`` through FODO cells with SecondTM and SpaceCharge.
+* ``ref_io.npz``, ``ref_beam.ast``, ``ref_beam.fmt1`` -- a seeded beam saved
+  and loaded by the reference's ASTRA and CSRtrack adaptors.
 * ``track_pin.json`` -- the pin of the oracle against the reference's golden
   vectors: the same scenario tracked by the reference's ``track()`` with the
   kick replaced by ``oracle.sc_oracle.sc_apply``, compared particle by
@@ -326,13 +331,94 @@ def run_fodo(ref_root: str, cells=2, n=4000, mesh=(15, 15, 15)):
     print(f"wrote {path} ({len(kicks)} kicks)")
 
 
+def run_second_order(ref_root: str, cells=2, n=4000, mesh=(15, 15, 15)):
+    """Second-order transport (SecondTM) of drifts and quadrupoles:
+    the reference's t_nnn tensors (ocelot/cpbd/high_order.py:456-617), the
+    offset and tilt handling of a quadrupole's SecondOrderParams, the maps
+    applied by SecondTM.map_function to a small beam, and the reference's
+    track() with SpaceCharge through FODO cells with method SecondTM."""
+    import_reference(ref_root)
+    from ocelot import Drift, Marker, Quadrupole, MagneticLattice, SecondTM, Navigator, track
+    from ocelot.cpbd.high_order import t_nnn
+    from ocelot.cpbd.sc import SpaceCharge
+    from ocelot.cpbd.beam import ParticleArray
+    params = [(0.25, 0.0, 0.130), (1.0, 0.0, 0.130), (0.2, 1.2, 0.130), (0.2, -1.2, 0.130), (0.05, 1.2, 0.130),
+              (0.15, -1.2, 0.0065), (0.3, -1.537886, 0.0065), (0.3, 1.435078, 2.0)]
+    T = np.stack([t_nnn(L, 0.0, k1, 0.0, E) for L, k1, E in params])
+    quad = Quadrupole(l=0.2, k1=-1.2, tilt=0.3)
+    quad.dx, quad.dy = 1e-3, -2e-3
+    sp = quad.element.create_second_order_main_params(0.130, 0.15)
+    # maps applied to a small beam by the reference's own SecondTM
+    rng = np.random.default_rng(77)
+    X0 = np.stack([rng.normal(0, s, 64) for s in (1e-3, 1e-4, 1e-3, 1e-4, 1e-4, 1e-3)])
+    outs = []
+    for e, dl in ((Drift(l=0.7), 0.7), (Quadrupole(l=0.2, k1=1.2), 0.2), (quad, 0.15)):
+        tm = SecondTM.from_element(e.element if hasattr(e, "element") else e, delta_l=dl)
+        outs.append(tm.map_function(X0.copy(), energy=0.130))
+    path = os.path.join(HERE, "ref_second_order.npz")
+    np.savez_compressed(path, params=np.array(params), T=T, quad=np.array([0.15, -1.2, 0.130, 0.3, 1e-3, -2e-3]),
+                        quad_R=np.asarray(sp.R), quad_B=np.asarray(sp.B).reshape(6), quad_Rrot=sp.get_rotated_R(),
+                        quad_Trot=sp.get_rotated_T(), X0=X0, X_drift=outs[0], X_quad=outs[1], X_tilted=outs[2])
+    print(f"wrote {path}")
+    seq = []
+    for _ in range(cells):
+        seq += [Quadrupole(l=0.2, k1=1.2), Drift(l=1.0), Quadrupole(l=0.2, k1=-1.2), Drift(l=1.0)]
+    seq.append(Marker())
+    lat = MagneticLattice(seq, method={"global": SecondTM})
+    rp, q = sc_oracle.gaussian_beam(n, 607, sigma_x=200e-6, sigma_y=200e-6, sigma_px=2e-5, sigma_py=2e-5,
+                                    charge=500e-12)
+    pa = ParticleArray(n)
+    pa.rparticles[:] = rp
+    pa.q_array = q.copy()
+    pa.E = 0.130
+    sc = SpaceCharge(step=1, nmesh_xyz=list(mesh))
+    navi = Navigator(lat)
+    navi.add_physics_proc(sc, lat.sequence[0], lat.sequence[-1])
+    navi.unit_step = 0.25
+    _, p = track(lat, pa, navi, print_progress=False, calc_tws=False)
+    path = os.path.join(HERE, "ref_fodo_track2.npz")
+    np.savez_compressed(path, rp_in=rp, q=q, E=0.130, cells=cells, nmesh=np.array(mesh), rp_out=p.rparticles.copy())
+    print(f"wrote {path}")
+
+
+def run_io(ref_root: str, n=64):
+    """Beam files written and read by the reference's adaptors
+    (ocelot/cpbd/io.py:223-295, ocelot/adaptors/astra2ocelot.py:150-233,
+    ocelot/adaptors/csrtrack2ocelot.py:9-87), from a seeded beam."""
+    import_reference(ref_root)
+    from ocelot.cpbd.beam import ParticleArray
+    from ocelot.cpbd.io import load_particle_array, save_particle_array
+    rp, q = sc_oracle.gaussian_beam(n, 909, sigma_x=80e-6, sigma_y=60e-6, sigma_px=3e-5, sigma_py=2e-5,
+                                    sigma_tau=50e-6, sigma_p=2e-4, charge=100e-12)
+    pa = ParticleArray(n)
+    pa.rparticles[:] = rp
+    pa.q_array = q.copy()
+    pa.E = 0.130
+    pa.s = 12.5
+    ast = os.path.join(HERE, "ref_beam.ast")
+    fmt1 = os.path.join(HERE, "ref_beam.fmt1")
+    save_particle_array(ast, pa)
+    save_particle_array(fmt1, pa)
+    a = load_particle_array(ast)
+    c = load_particle_array(fmt1)
+    path = os.path.join(HERE, "ref_io.npz")
+    np.savez_compressed(path, rp=rp, q=q, E=0.130, s=12.5, ast_rp=a.rparticles, ast_q=a.q_array, ast_E=a.E,
+                        ast_s=a.s, fmt1_rp=c.rparticles, fmt1_q=c.q_array, fmt1_E=c.E, fmt1_s=c.s)
+    print(f"wrote {path}, {ast}, {fmt1}")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--skip-track", action="store_true")
     ap.add_argument("--only-track", action="store_true")
     ap.add_argument("--only-matrices", action="store_true")
+    ap.add_argument("--only-second-order-io", action="store_true")
     a = ap.parse_args()
+    if a.only_second_order_io:
+        run_second_order(a.reference)
+        run_io(a.reference)
+        sys.exit(0)
     if a.only_matrices:
         run_matrices(a.reference)
         if not os.path.exists(os.path.join(HERE, "ref_fodo_track.npz")):
@@ -342,5 +428,7 @@ if __name__ == "__main__":
         run_cases(a.reference)
         run_matrices(a.reference)
         run_fodo(a.reference)
+        run_second_order(a.reference)
+        run_io(a.reference)
     if not a.skip_track:
         run_track(a.reference)
