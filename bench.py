@@ -50,6 +50,11 @@ SEED = 2024
 # plus the charge grid written and the potential read once (2 x w x N_g)
 B_PER_PARTICLE = 104
 B_KICK_KERNEL_PER_PARTICLE = 96  # gather+kick: rparticles read + write
+# DRAM traffic of one k_kick32_tma launch per particle, from the ncu capture
+# summarised in profiles/k_kick32_tma_4M_64cube.txt (200.62 MB read + 132.30 MB
+# written at 4M particles); traffic grows with the particles, so it is scaled
+# to the bench's n
+KICK_TRAFFIC_PER_PARTICLE = (200.62e6 + 132.30e6) / 4e6
 
 
 def log(*a):
@@ -498,9 +503,11 @@ def main():
             "fp32_over_fp64": (statistics.mean(kick64) / statistics.mean(kick32)) if kick64 else None,
             "fp32_kick_rel_rms_err_vs_fp64": kick_err,
             "stages_ms": stages32,
-            "roofline": {"bound": "hbm", "kernel": "k_kick32 (gather+kick+FP64 accumulate)",
+            "roofline": {"bound": "hbm", "kernel": "k_kick32_tma (gather+kick+FP64 accumulate)",
                          "achieved": achieved_kick, "peak": peak, "unit": "GB/s", "frac": achieved_kick / peak,
-                         "traffic": None, "peak_kind": peak_kind,
+                         "traffic": KICK_TRAFFIC_PER_PARTICLE * n, "peak_kind": peak_kind,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_kick32_tma at 4M "
+                                           "particles (profiles/k_kick32_tma_4M_64cube.txt), scaled by particles",
                          "algorithmic_bytes_per_launch": B_KICK_KERNEL_PER_PARTICLE * n,
                          "top_stage": top, "top_stage_ms": stages32[top]},
             "kick_roofline": {"achieved": achieved_whole, "frac": achieved_whole / peak, "unit": "GB/s",
