@@ -257,8 +257,11 @@ __device__ __forceinline__ double dot3_blas(double a0, double a1, double a2, dou
 // six FP64 accumulations per particle.
 // ---------------------------------------------------------------------------
 // round-half-up to the nearest float (|error| <= 2^-24 relative); magnitudes
-// below 2^-126 flush to zero, above FLT_MAX become infinity, NaN stays NaN
-__device__ __forceinline__ float d2f(double d) {
+// below 2^-126 flush to zero, above FLT_MAX become infinity, NaN stays NaN.
+// d2f_exact handles every exponent; d2f_nr only FP32's normal range, in five
+// instructions, and d2f uses it with d2f_exact out of line (d2f_edge) for the
+// rest.  All three give the same bits wherever they apply.
+__device__ __forceinline__ float d2f_exact(double d) {
     const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
     const unsigned sign = hi & 0x80000000u;
     const int e = (int)((hi >> 20) & 0x7ffu);
@@ -269,8 +272,28 @@ __device__ __forceinline__ float d2f(double d) {
     else f = (sign | ((unsigned)(e - 896) << 23) | mant) + ((lo >> 28) & 1u);
     return __uint_as_float(f);
 }
-// exact widening (float subnormals, which the kick never produces, read as 0)
-__device__ __forceinline__ double f2d(float f) {
+__device__ __noinline__ float d2f_edge(double d) { return d2f_exact(d); }
+// d2f for a biased FP64 exponent of 897..1150 (the FP32 normal range): one
+// funnel shift lines up the low eight exponent bits and 23 mantissa bits;
+// adding 2^30 rebiases the exponent (-896 = +128 mod 256) and the first
+// dropped bit rounds, its carry running into the exponent as in d2f_edge.
+// range: the running unsigned maximum of (2|hi| - 2*897*2^20), below
+// 2*254*2^20 iff every value converted so far was in range.
+__device__ __forceinline__ float d2f_nr(double d, unsigned& range) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned t = __funnelshift_l(lo, hi, 3) + 0x40000000u + ((lo >> 28) & 1u);
+    range = umax(range, hi * 2u - (897u << 21));
+    return __uint_as_float((t & 0x7fffffffu) | (hi & 0x80000000u));
+}
+__device__ __forceinline__ bool d2f_range_ok(unsigned range) { return range < (254u << 21); }
+__device__ __forceinline__ float d2f(double d) {
+    unsigned range = 0u;
+    const float f = d2f_nr(d, range);
+    return d2f_range_ok(range) ? f : d2f_edge(d);
+}
+// exact widening (float subnormals, which the kick never produces, read as
+// 0); f2d_exact, f2d_nr and f2d split the exponents as the d2f forms do
+__device__ __forceinline__ double f2d_exact(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
     unsigned hi, lo;
@@ -278,6 +301,20 @@ __device__ __forceinline__ double f2d(float f) {
     else if (e == 255) { hi = sign | 0x7ff00000u | (m >> 3); lo = m << 29; }
     else { hi = sign | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
     return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __noinline__ double f2d_edge(float f) { return f2d_exact(f); }
+// f2d for FP32 exponents 1..254 (rebiased by 896); range as in d2f_nr, below
+// 2*254*2^23 iff every value was in range
+__device__ __forceinline__ double f2d_nr(float f, unsigned& range) {
+    const unsigned u = __float_as_uint(f);
+    range = umax(range, u * 2u - (1u << 24));
+    return __hiloint2double((int)((((u & 0x7fffffffu) >> 3) + 0x38000000u) | (u & 0x80000000u)), (int)(u << 29));
+}
+__device__ __forceinline__ bool f2d_range_ok(unsigned range) { return range < (254u << 24); }
+__device__ __forceinline__ double f2d(float f) {
+    unsigned range = 0u;
+    const double d = f2d_nr(f, range);
+    return f2d_range_ok(range) ? d : f2d_edge(f);
 }
 
 // the hardware's approximate reciprocal and square root (relative error
@@ -589,6 +626,7 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
     __shared__ double s_mn[3], s_mx[3], s_qs[5];
     if (threadIdx.x == 0) {
         st->done_extent = 0;
+        st->amb_count = 0;
         if (gamma_override > 0.0) {
             st->gamma0 = gamma_override;
             st->g0f = (float)gamma_override;
@@ -841,13 +879,14 @@ __device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, 
     const int64_t n = kp.n, ld = kp.ld;
     const BlockTiles T(n, vb);
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    auto add = [&](double xq, double yq, double d) {
+    auto addf = [&](float xq, float yq, float d) {
         float px, py, pz, E;
-        mom32(d2f(xq), d2f(yq), d2f(d), kp, px, py, pz, E);
+        mom32(xq, yq, d, kp, px, py, pz, E);
         a0 += px;
         a1 += py;
         a2 += pz;
     };
+    auto add = [&](double xq, double yq, double d) { addf(d2f(xq), d2f(yq), d2f(d)); };
     auto issue = [&](int64_t t, int s, uint64_t* b) {
         const int64_t i0 = T.start(t);
         const unsigned bytes = (unsigned)(T.count(t) & ~1) * 8u;
@@ -862,8 +901,16 @@ __device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, 
             const double2 x = *reinterpret_cast<const double2*>(B + j);
             const double2 y = *reinterpret_cast<const double2*>(B + PT_TILE + j);
             const double2 d = *reinterpret_cast<const double2*>(B + 2 * PT_TILE + j);
-            add(x.x, y.x, d.x);
-            add(x.y, y.y, d.y);
+            unsigned rg = 0u;  // one range check for both particles (d2f_nr)
+            const float f[6] = {d2f_nr(x.x, rg), d2f_nr(y.x, rg), d2f_nr(d.x, rg),
+                                d2f_nr(x.y, rg), d2f_nr(y.y, rg), d2f_nr(d.y, rg)};
+            if (d2f_range_ok(rg)) {
+                addf(f[0], f[1], f[2]);
+                addf(f[3], f[4], f[5]);
+            } else {
+                add(x.x, y.x, d.x);
+                add(x.y, y.y, d.y);
+            }
         } else if (j < cnt) {
             const int64_t i = T.start(t) + j;
             add(rp[ld + i], rp[3 * ld + i], rp[5 * ld + i]);
@@ -1106,13 +1153,14 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
     const float g0 = st->g0f;
     const BlockTiles Tl(ok ? n : 0, vb);
     // one particle: rotated position, extremes and charge moments; returns v
-    auto one = [&](const double (&r)[6], double qd, float (&v)[3]) {
+    // f: the six coordinates and the charge rounded to FP32
+    auto one = [&](const float (&f)[7], float (&v)[3]) {
         float px, py, pz, E;
-        mom32(d2f(r[1]), d2f(r[3]), d2f(r[5]), kp, px, py, pz, E);
+        mom32(f[1], f[3], f[5], kp, px, py, pz, E);
         float l[3];
-        lab32(d2f(r[0]), d2f(r[2]), d2f(r[4]), px, py, pz, E, kp, l);
+        lab32(f[0], f[2], f[4], px, py, pz, E, kp, l);
         rot32(l, T, g0, v);
-        const float qi = d2f(qd);
+        const float qi = f[6];
         for (int j = 0; j < 3; ++j) {  // charge moments of the lab positions
             mnf[j] = fminf(mnf[j], v[j]);
             mxf[j] = fmaxf(mxf[j], v[j]);
@@ -1142,16 +1190,33 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
                 r1[k] = v.y;
             }
             const double2 qq = *reinterpret_cast<const double2*>(B + 6 * PT_TILE + j);
+            float f0[7], f1[7];
+            unsigned rg = 0u;  // one range check for both particles (d2f_nr)
+            for (int k = 0; k < 6; ++k) {
+                f0[k] = d2f_nr(r0[k], rg);
+                f1[k] = d2f_nr(r1[k], rg);
+            }
+            f0[6] = d2f_nr(qq.x, rg);
+            f1[6] = d2f_nr(qq.y, rg);
+            if (!d2f_range_ok(rg)) {
+                for (int k = 0; k < 6; ++k) {
+                    f0[k] = d2f_edge(r0[k]);
+                    f1[k] = d2f_edge(r1[k]);
+                }
+                f0[6] = d2f_edge(qq.x);
+                f1[6] = d2f_edge(qq.y);
+            }
             float v0[3], v1[3];
-            one(r0, qq.x, v0);
-            one(r1, qq.y, v1);
+            one(f0, v0);
+            one(f1, v1);
             for (int k = 0; k < 3; ++k) *reinterpret_cast<float2*>(X + k * nX + i0 + j) = make_float2(v0[k], v1[k]);
         } else if (j < cnt) {
             const int64_t i = i0 + j;
-            double r[6];
-            for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i];
+            float f[7];
+            for (int k = 0; k < 6; ++k) f[k] = d2f(rp[k * ld + i]);
+            f[6] = d2f(q[i]);
             float v[3];
-            one(r, q[i], v);
+            one(f, v);
             for (int k = 0; k < 3; ++k) X[k * nX + i] = v[k];
         }
     };
@@ -1334,7 +1399,7 @@ template <bool VEC>
 __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __restrict__ keys,
                                             const double* __restrict__ rp, const double* __restrict__ q,
                                             unsigned long long* __restrict__ qfix, const KickParams& kp, ScState* st,
-                                            VBlk vb) {
+                                            VBlk vb, uint32_t* __restrict__ ambl = nullptr) {
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     float of[3], is[3];
@@ -1366,8 +1431,13 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
             const float f = g[j] - floorf(g[j]);
             amb |= !(f >= tol && f <= 1.0f - tol);
         }
-        uint32_t key;
-        if (amb && rp) {
+        uint32_t key = 0u;
+        bool deferred = false;
+        if (amb && rp && ambl) {  // listed for k_keys_fix, which writes its key and deposits its charge
+            const unsigned slot = atomicAdd(&st->amb_count, 1u);
+            ambl[slot] = (uint32_t)i;  // slot < n: each particle is listed at most once
+            deferred = true;
+        } else if (amb && rp) {
             double T[3][3];
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
@@ -1382,7 +1452,7 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
         } else {
             bad |= !key_of_f(floorf(g[0]) + 1.f, floorf(g[1]) + 1.f, floorf(g[2]) + 1.f, kp, key);
         }
-        if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
+        if (qfix && !deferred && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
             atomicAdd(qfix + key, (unsigned long long)to_fixed(qq[w], S));
         key2[w] = key;
         for (int j = 0; j < 3; ++j) g2[j][w] = g[j];
@@ -1400,9 +1470,43 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
 template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
                                                   const double* __restrict__ rp, const double* __restrict__ q,
-                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
+                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st,
+                                                  uint32_t* __restrict__ ambl) {
     pdl_wait();
-    keys32_body<VEC>(X, keys, rp, q, qfix, kp, st, hw_vblk());
+    keys32_body<VEC>(X, keys, rp, q, qfix, kp, st, hw_vblk(), ambl);
+}
+
+// The particles the keys kernel listed (FP32 coordinate within the margin of
+// a cell face): key from the FP64 coordinates and, with qfix, the deposit.
+// One particle per thread, so the slow FP64 evaluations run side by side
+// instead of holding up the warps of the keys kernel.
+constexpr int FIX_THREADS = 128;
+__global__ void __launch_bounds__(FIX_THREADS) k_keys_fix(uint32_t* __restrict__ keys, const double* __restrict__ rp,
+                                                          const double* __restrict__ q,
+                                                          unsigned long long* __restrict__ qfix,
+                                                          const uint32_t* __restrict__ ambl, KickParams kp,
+                                                          ScState* st) {
+    pdl_wait();
+    if (st->status) return;
+    const unsigned cnt = st->amb_count;
+    bool bad = false;
+    for (unsigned e = blockIdx.x * FIX_THREADS + threadIdx.x; e < cnt; e += gridDim.x * FIX_THREADS) {
+        if (!SC_IDX_OK(st, 13, e, kp.n)) break;
+        const int64_t i = ambl[e];
+        double T[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
+        double xv[3];
+        xyz_fine(rp, kp.ld, i, kp, T, st->gamma0, xv);
+        double g[3];
+        for (int j = 0; j < 3; ++j) g[j] = fma(xv[j], st->isteps[j], -st->xoff[j]);
+        uint32_t key;
+        bad |= !key_of(floor(g[0]) + 1, floor(g[1]) + 1, floor(g[2]) + 1, kp, key);
+        keys[i] = key;
+        if (qfix && SC_IDX_OK(st, 14, key, (long long)kp.nx * kp.ny * kp.nz))
+            atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], st->qfix_shift));
+    }
+    if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
 }
 
 // ---------------------------------------------------------------------------
@@ -1569,15 +1673,17 @@ __device__ __forceinline__ float oct_sample(const float* __restrict__ O, const A
 // approximate reciprocal and square root, so the kick reads nothing per
 // particle but rparticles.  (The NGP keys, which must equal the FP64 form's,
 // are decided by the keys kernel alone; the gather only needs the grid
-// coordinates to FP32 accuracy.)
+// coordinates to FP32 accuracy.)  The conversions are the full-range inline
+// forms: with the range-checked forms and their out-of-line fallbacks the
+// kick kernel, at its 80-register limit, ran 15% slower.
 __device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp) {
     float px, py, pz, E;
-    mom32(d2f(r[1]), d2f(r[3]), d2f(r[5]), kp, px, py, pz, E);
+    mom32(d2f_exact(r[1]), d2f_exact(r[3]), d2f_exact(r[5]), kp, px, py, pz, E);
     // lab position, rotated and scaled to the grid
-    const float tau = d2f(r[4]);
+    const float tau = d2f_exact(r[4]);
     const float iE = rcpf(E);
     float l[3];
-    lab32(d2f(r[0]), d2f(r[2]), tau, px, py, pz, E, kp, l);
+    lab32(d2f_exact(r[0]), d2f_exact(r[2]), tau, px, py, pz, E, kp, l);
     float X[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -1612,12 +1718,12 @@ __device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const
     const float dx = fmaf(tau * fmaf(dpx, E, -px * dE), iEE, pxn * iEn * dtau);
     const float dy = fmaf(tau * fmaf(dpy, E, -py * dE), iEE, pyn * iEn * dtau);
     // the only FP64 arithmetic: six additions into the float64 coordinates
-    r[0] += f2d(dx);
-    r[1] += f2d(dpx * C.ipref);
-    r[2] += f2d(dy);
-    r[3] += f2d(dpy * C.ipref);
-    r[4] += f2d(dtau);
-    r[5] += f2d(dE * C.ipref);
+    r[0] += f2d_exact(dx);
+    r[1] += f2d_exact(dpx * C.ipref);
+    r[2] += f2d_exact(dy);
+    r[3] += f2d_exact(dpy * C.ipref);
+    r[4] += f2d_exact(dtau);
+    r[5] += f2d_exact(dE * C.ipref);
 }
 
 // Gather + kick with direct row accesses: each thread takes G consecutive
@@ -1963,10 +2069,12 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
             cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
             if (e) return e;
         }
+        uint32_t* ambl = rp ? reinterpret_cast<uint32_t*>(ws + L.amb) : nullptr;
         if (!qfix || (uintptr_t)q % 16 == 0)
-            launch(k_keys32<true>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+            launch(k_keys32<true>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st, ambl);
         else
-            launch(k_keys32<false>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
+            launch(k_keys32<false>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st, ambl);
+        if (ambl) launch(k_keys_fix, 2 * p.sm_count, FIX_THREADS, 0, s, keys, rp, q, qfix, ambl, kp, st);
     }
     return cudaGetLastError();
 }
