@@ -116,7 +116,6 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.xp = take(p.prec == SC_FP64 ? 8 * 6 * (size_t)n : 0);
     L.X = take(rs * 3 * (size_t)((n + 3) / 4 * 4));
     L.keys = take(4 * (size_t)n);
-    L.amb = take(p.prec == SC_FP32 ? 4 * (size_t)n : 0);
     // the radix sort's buffers: only the sorted deposit uses them
     const size_t ns = p.sorted_deposit ? (size_t)n : 0;
     L.sort_keys = take(4 * ns);
@@ -515,10 +514,8 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     mark(plan, 8, s);
     SC_CUDA(launch_gather_kick(p, L, ws, kp, rp, s), "gather/kick");
     mark(plan, 9, s);
-    // frame 1, extent 1, keys 1 (FP32: + the deferred keys 1), [sort 3 per pass, deposit 2], igf 2, green 3,
-    // convolve 5, field 1, kick 1
-    plan->last_launches = 1 + 1 + 1 + (p.prec == SC_FP32 ? 1 : 0) + (p.sorted_deposit ? 3 * passes + 2 : 0) + 2 + 3 +
-                          5 + 1 + 1;
+    // frame 1, extent 1, keys 1, [sort 3 per pass, deposit 2], igf 2, green 3, convolve 5, field 1, kick 1
+    plan->last_launches = 1 + 1 + 1 + (p.sorted_deposit ? 3 * passes + 2 : 0) + 2 + 3 + 5 + 1 + 1;
     return SC_OK;
 }
 

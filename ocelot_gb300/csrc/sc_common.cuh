@@ -68,7 +68,6 @@ struct ScState {
     int igf_box[3];
     unsigned int done_frame;     // blocks finished, for the last-block reductions
     unsigned int done_extent;
-    unsigned int amb_count;      // FP32 keys deferred to k_keys_fix (reset by the mesh finalize)
     int frame_timeout;           // a frame block's bulk-copy wait gave up (the finalize reports it)
     int check_code;              // checked builds: first failed index check (kernel code)
     int first_error;             // first non-OK status of any kick since sc_workspace_init
@@ -135,7 +134,6 @@ struct Layout {
     size_t xp;                                   // FP64: 6 x n lab coordinates
     size_t X;                                    // 3 x n grid coordinates (R)
     size_t keys, sort_keys, sort_perm, sort_q, sort_tmp_k, sort_tmp_v, sort_hist, sort_tot;
-    size_t amb;                                  // FP32 form: [n] uint32 particles whose key was deferred
     size_t qgrid, phi, ex, ey, ez;               // [nx][ny][nz] (R)
     size_t exq, eyq, ezq;                        // FP32 form: [nx][ny][nz] gather octs (8 floats, 32-byte aligned)
     size_t cell_start, cell_end;                 // [nx*ny*nz] uint32 run bounds (adjacent)

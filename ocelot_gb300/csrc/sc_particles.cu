@@ -626,7 +626,6 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
     __shared__ double s_mn[3], s_mx[3], s_qs[5];
     if (threadIdx.x == 0) {
         st->done_extent = 0;
-        st->amb_count = 0;
         if (gamma_override > 0.0) {
             st->gamma0 = gamma_override;
             st->g0f = (float)gamma_override;
@@ -1386,6 +1385,8 @@ __device__ __forceinline__ long long to_fixed(double q, int S) {
     return (b >> 63) ? -(long long)v : (long long)v;
 }
 
+constexpr int KEYS_FINE = 256;
+
 // FP32 grid coordinates with an explicit rounding margin; a particle whose
 // coordinate lies within the margin of a cell face is recomputed to ~1e-11 of
 // a cell (xyz_fine), so its key equals the FP64 form's key unless it lies
@@ -1399,8 +1400,13 @@ template <bool VEC>
 __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __restrict__ keys,
                                             const double* __restrict__ rp, const double* __restrict__ q,
                                             unsigned long long* __restrict__ qfix, const KickParams& kp, ScState* st,
-                                            VBlk vb, uint32_t* __restrict__ ambl = nullptr) {
-    if (st->status) return;
+                                            VBlk vb) {
+    // particles within the margin of a cell face, evaluated in FP64 after the
+    // loop, one per thread (KEYS_FINE of them per block; more go inline)
+    __shared__ uint32_t s_fine[KEYS_FINE];
+    __shared__ int s_nfine;
+    if (threadIdx.x == 0) s_nfine = 0;
+    if (__syncthreads_or(st->status != SC_OK)) return;  // the same decision in every thread of the block
     const int64_t n = kp.n, ld = kp.ld, nX = kp.nX;
     float of[3], is[3];
     for (int j = 0; j < 3; ++j) {
@@ -1433,11 +1439,14 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
         }
         uint32_t key = 0u;
         bool deferred = false;
-        if (amb && rp && ambl) {  // listed for k_keys_fix, which writes its key and deposits its charge
-            const unsigned slot = atomicAdd(&st->amb_count, 1u);
-            ambl[slot] = (uint32_t)i;  // slot < n: each particle is listed at most once
-            deferred = true;
-        } else if (amb && rp) {
+        if (amb && rp) {
+            const int slot = atomicAdd(&s_nfine, 1);
+            if (slot < KEYS_FINE) {
+                s_fine[slot] = (uint32_t)i;  // n < 2^31
+                deferred = true;
+            }
+        }
+        if (amb && rp && !deferred) {
             double T[3][3];
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
@@ -1464,49 +1473,35 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
     if (!rp)
         for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
     PAIR_LOOP_END
+    // the listed particles: key from the FP64 coordinates and the deposit;
+    // one per thread, so the block waits for one slow FP64 evaluation
+    // instead of each warp stalling on its own
+    __syncthreads();
+    const int nf = s_nfine < KEYS_FINE ? s_nfine : KEYS_FINE;
+    for (int e = threadIdx.x; e < nf; e += blockDim.x) {
+        const int64_t i = s_fine[e];
+        double T[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
+        double xv[3];
+        xyz_fine(rp, ld, i, kp, T, st->gamma0, xv);
+        double g[3];
+        for (int j = 0; j < 3; ++j) g[j] = fma(xv[j], st->isteps[j], -st->xoff[j]);
+        uint32_t key;
+        bad |= !key_of(floor(g[0]) + 1, floor(g[1]) + 1, floor(g[2]) + 1, kp, key);
+        keys[i] = key;
+        if (qfix && SC_IDX_OK(st, 13, key, (long long)kp.nx * kp.ny * kp.nz))
+            atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
+    }
     if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
 }
 
 template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_t* __restrict__ keys,
                                                   const double* __restrict__ rp, const double* __restrict__ q,
-                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st,
-                                                  uint32_t* __restrict__ ambl) {
+                                                  unsigned long long* __restrict__ qfix, KickParams kp, ScState* st) {
     pdl_wait();
-    keys32_body<VEC>(X, keys, rp, q, qfix, kp, st, hw_vblk(), ambl);
-}
-
-// The particles the keys kernel listed (FP32 coordinate within the margin of
-// a cell face): key from the FP64 coordinates and, with qfix, the deposit.
-// One particle per thread, so the slow FP64 evaluations run side by side
-// instead of holding up the warps of the keys kernel.
-constexpr int FIX_THREADS = 128;
-__global__ void __launch_bounds__(FIX_THREADS) k_keys_fix(uint32_t* __restrict__ keys, const double* __restrict__ rp,
-                                                          const double* __restrict__ q,
-                                                          unsigned long long* __restrict__ qfix,
-                                                          const uint32_t* __restrict__ ambl, KickParams kp,
-                                                          ScState* st) {
-    pdl_wait();
-    if (st->status) return;
-    const unsigned cnt = st->amb_count;
-    bool bad = false;
-    for (unsigned e = blockIdx.x * FIX_THREADS + threadIdx.x; e < cnt; e += gridDim.x * FIX_THREADS) {
-        if (!SC_IDX_OK(st, 13, e, kp.n)) break;
-        const int64_t i = ambl[e];
-        double T[3][3];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
-        double xv[3];
-        xyz_fine(rp, kp.ld, i, kp, T, st->gamma0, xv);
-        double g[3];
-        for (int j = 0; j < 3; ++j) g[j] = fma(xv[j], st->isteps[j], -st->xoff[j]);
-        uint32_t key;
-        bad |= !key_of(floor(g[0]) + 1, floor(g[1]) + 1, floor(g[2]) + 1, kp, key);
-        keys[i] = key;
-        if (qfix && SC_IDX_OK(st, 14, key, (long long)kp.nx * kp.ny * kp.nz))
-            atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], st->qfix_shift));
-    }
-    if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
+    keys32_body<VEC>(X, keys, rp, q, qfix, kp, st, hw_vblk());
 }
 
 // ---------------------------------------------------------------------------
@@ -2069,12 +2064,10 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
             cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
             if (e) return e;
         }
-        uint32_t* ambl = rp ? reinterpret_cast<uint32_t*>(ws + L.amb) : nullptr;
         if (!qfix || (uintptr_t)q % 16 == 0)
-            launch(k_keys32<true>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st, ambl);
+            launch(k_keys32<true>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
         else
-            launch(k_keys32<false>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st, ambl);
-        if (ambl) launch(k_keys_fix, 2 * p.sm_count, FIX_THREADS, 0, s, keys, rp, q, qfix, ambl, kp, st);
+            launch(k_keys32<false>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
     }
     return cudaGetLastError();
 }
