@@ -487,7 +487,7 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     mark(plan, 12, side);
     SC_CUDA(cudaEventRecord(plan->join, side), "cudaEventRecord");
     // keys; in the FP32 form the exact fixed-point deposit rides along
-    SC_CUDA(launch_keys(p, L, ws, kp, rp, p.sorted_deposit ? nullptr : q, s), "keys");
+    SC_CUDA(launch_keys(p, L, ws, kp, rp, p.sorted_deposit ? nullptr : q, s, p.prec == SC_FP32), "keys");
     mark(plan, 3, s);
     if (p.sorted_deposit) {
         SC_CUDA(launch_sort(reinterpret_cast<uint32_t*>(ws + L.keys), n, p.key_bits, reinterpret_cast<uint32_t*>(ws + L.sort_keys),

@@ -170,9 +170,10 @@ cudaError_t launch_extent(const Plan& p, const Layout& L, char* ws, const KickPa
                           const double* rp, const double* q, cudaStream_t s);
 // rp: the particles (exact recomputation of near-face keys in the FP32 form), or nullptr
 // FP32 form without the sorted deposit: also accumulates q into the
-// fixed-point grid (the deposit)
+// fixed-point grid (the deposit), zeroed first unless qfix_zeroed (the
+// FP32 frame kernel of the same kick zeroes it)
 cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, const double* rp,
-                        const double* q, cudaStream_t s);
+                        const double* q, cudaStream_t s, bool qfix_zeroed = false);
 cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const KickParams& kp,
                                double* rp, cudaStream_t s);
 // el_field entry: extent over a given X[n][3] with a given gamma, and gather to exyz

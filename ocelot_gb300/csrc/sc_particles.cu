@@ -856,11 +856,14 @@ __device__ __forceinline__ void frame32_body(const double* __restrict__ rp, cons
     if (arrive_last(&st->done_frame, vb.nx)) frame_finalize32(fp, vb.nx, kp, st);
 }
 
+// qzero != nullptr: also zeroes the nzero cells of the fixed-point charge
+// grid for this kick's deposit
 template <bool VEC>
 __global__ void __launch_bounds__(PT, 4) k_frame32(const double* __restrict__ rp, KickParams kp,
-                                                   double* __restrict__ part, ScState* st) {
+                                                   double* __restrict__ part, ScState* st,
+                                                   unsigned long long* __restrict__ qzero, int64_t nzero) {
     pdl_wait();
-    frame32_body<VEC>(rp, kp, part, st, nullptr, 0, hw_vblk());
+    frame32_body<VEC>(rp, kp, part, st, qzero, nzero, hw_vblk());
 }
 
 // frame32_body with the rows x', y', delta streamed through shared memory
@@ -929,9 +932,10 @@ __device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, 
 }
 
 __global__ void __launch_bounds__(PT, 4) k_frame32_tma(const double* __restrict__ rp, KickParams kp,
-                                                       double* __restrict__ part, ScState* st) {
+                                                       double* __restrict__ part, ScState* st,
+                                                       unsigned long long* __restrict__ qzero, int64_t nzero) {
     pdl_wait();
-    frame32_tma_body(rp, kp, part, st, nullptr, 0, hw_vblk());
+    frame32_tma_body(rp, kp, part, st, qzero, nzero, hw_vblk());
 }
 
 // ---------------------------------------------------------------------------
@@ -2009,9 +2013,14 @@ cudaError_t launch_frame(const Plan& p, const Layout& L, char* ws, const KickPar
     const int nb = particle_blocks(p, kp.n);
     if (p.prec == SC_FP64)
         launch(k_frame64, nb, PT, 0, s, rp, kp, reinterpret_cast<double*>(ws + L.xp), part, st);
-    else
-        vec_ok(rp, kp.ld, nullptr) ? launch(k_frame32_tma, nb, PT, FR_SMEM, s, rp, kp, part, st)
-                                   : launch(k_frame32<false>, nb, PT, 0, s, rp, kp, part, st);
+    else {
+        // the exact deposit's fixed-point grid is zeroed here, so the keys
+        // kernel follows the extent kernel without a memset between them
+        unsigned long long* qz = p.sorted_deposit ? nullptr : reinterpret_cast<unsigned long long*>(ws + L.qfix);
+        const int64_t nz = qz ? (int64_t)p.nx * p.ny * p.nz : 0;
+        vec_ok(rp, kp.ld, nullptr) ? launch(k_frame32_tma, nb, PT, FR_SMEM, s, rp, kp, part, st, qz, nz)
+                                   : launch(k_frame32<false>, nb, PT, 0, s, rp, kp, part, st, qz, nz);
+    }
     return cudaGetLastError();
 }
 
@@ -2050,7 +2059,7 @@ cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const Kick
 }
 
 cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, const double* rp,
-                        const double* q, cudaStream_t s) {
+                        const double* q, cudaStream_t s, bool qfix_zeroed) {
     ScState* st = reinterpret_cast<ScState*>(ws + L.state);
     const int nb = particle_blocks(p, kp.n);
     uint32_t* keys = reinterpret_cast<uint32_t*>(ws + L.keys);
@@ -2061,8 +2070,10 @@ cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickPara
         unsigned long long* qfix = nullptr;
         if (q && !p.sorted_deposit) {
             qfix = reinterpret_cast<unsigned long long*>(ws + L.qfix);
-            cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
-            if (e) return e;
+            if (!qfix_zeroed) {
+                cudaError_t e = cudaMemsetAsync(qfix, 0, 8 * (size_t)p.nx * p.ny * p.nz, s);
+                if (e) return e;
+            }
         }
         if (!qfix || (uintptr_t)q % 16 == 0)
             launch(k_keys32<true>, nb, PT, 0, s, reinterpret_cast<float*>(ws + L.X), keys, rp, q, qfix, kp, st);
