@@ -259,6 +259,7 @@ static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energ
     kp.m_e_eV = c.m_e_eV;
     kp.m2 = pow(c.m_e_eV, 2.0);
     kp.four_pi_eps0 = 4 * c.pi * c.epsilon_0;
+    kp.phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
     kp.gamref_f = (float)kp.gamref;
     kp.betaref_f = (float)kp.betaref;
     kp.grbr_f = (float)kp.grbr;

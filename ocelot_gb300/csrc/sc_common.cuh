@@ -103,6 +103,7 @@ struct KickParams {
     double mesh_scale, mesh_shift;       // NaN when unused
     double m_e_eV, m2;                   // m_e_eV and m_e_eV**2
     double four_pi_eps0;                 // 4*pi*epsilon_0
+    double phi_norm;                     // 1/(Mx*My*Mz) of the inverse FFT
     // FP32 copies for the FP32 form
     float gamref_f, betaref_f, grbr_f, pref_f, ipref_f, m_f, m2_f;
     float igrbr2_f;                      // 1/(gamref*betaref)^2

@@ -596,6 +596,8 @@ __device__ void frame_finalize(const double* part, int nblk, const KickParams& k
     frame_finish(acc, kp, st);
 }
 
+constexpr int FIN_U = 3;  // partials per thread per round of the last-block reductions
+
 // FP32 form: per-block momentum sums as double-float pairs (hi[3], lo[3]),
 // reduced on the FP32 pipes
 struct FramePart32 {
@@ -604,8 +606,24 @@ struct FramePart32 {
 __device__ void frame_finalize32(const FramePart32* part, int nblk, const KickParams& kp, ScState* st) {
     __shared__ float sm[3 * 64];
     float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
-        for (int k = 0; k < 3; ++k) df_add(hi[k], lo[k], __ldcg(&part[b].hi[k]), __ldcg(&part[b].lo[k]));
+    // loads of up to FIN_U partials per thread before any is combined (block order)
+    for (int b0 = threadIdx.x; b0 < nblk; b0 += FIN_U * blockDim.x) {
+        float ph[FIN_U][3], pl[FIN_U][3];
+#pragma unroll
+        for (int u = 0; u < FIN_U; ++u) {
+            const int b = b0 + u * blockDim.x < nblk ? b0 + u * blockDim.x : b0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                ph[u][k] = __ldcg(&part[b].hi[k]);
+                pl[u][k] = __ldcg(&part[b].lo[k]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < FIN_U; ++u) {
+            if (b0 + u * blockDim.x >= nblk) break;
+            for (int k = 0; k < 3; ++k) df_add(hi[k], lo[k], ph[u][k], pl[u][k]);
+        }
+    }
     block_sum_df<3>(hi, lo, sm);
     const double acc[3] = {(double)hi[0] + (double)lo[0], (double)hi[1] + (double)lo[1],
                            (double)hi[2] + (double)lo[2]};
@@ -651,11 +669,26 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
     }
     const double qsum = s_qs[3];
     const int nm[3] = {kp.nx, kp.ny, kp.nz};
-    double XX = __dsub_rn(s_mx[k], s_mn[k]);
+    // Every lane takes axis a = lane % 3 of the step; then group g = lane / 3
+    // (0..3; lanes 12..31 repeat group 3) divides by it: g = 0 X_min,
+    // g = 1 the charge-weighted mean (then / sum q), g = 2 1/step, g = 3 the
+    // near-box ratio 5 h_max / step.  One SIMD division serves all four, so
+    // the chain holds three dependent divisions instead of six; each value is
+    // the same operation sequence as the serial form.
+    const int a = lane % 3, g = lane < 12 ? lane / 3 : 3;
+    double XX = __dsub_rn(s_mx[a], s_mn[a]);
     if (!isnan(kp.mesh_scale)) XX = __dmul_rn(XX, kp.mesh_scale);
-    const double stepk = __ddiv_rn(XX, (double)(nm[k] - 3));
-    const double xmin = __ddiv_rn(s_mn[k], stepk);
-    const double xmid = __ddiv_rn(__ddiv_rn(q3[k], stepk), qsum);
+    const double stepa = __ddiv_rn(XX, (double)(nm[a] - 3));
+    const double steps[3] = {__shfl_sync(FULL, stepa, 0), __shfl_sync(FULL, stepa, 1), __shfl_sync(FULL, stepa, 2)};
+    const double hm = fmax(steps[0], fmax(steps[1], steps[2]));
+    const double num = g == 0 ? s_mn[a] : g == 1 ? q3[a] : g == 2 ? 1.0 : __dmul_rn(5.0, hm);
+    const double r1 = __ddiv_rn(num, stepa);
+    const double r2 = __ddiv_rn(r1, qsum);  // used by group 1
+    const double stepk = steps[k];
+    const double xmin = __shfl_sync(FULL, r1, k);
+    const double xmid = __shfl_sync(FULL, r2, 3 + k);
+    const double istepk = __shfl_sync(FULL, r1, 6 + k);
+    const double v = __shfl_sync(FULL, r1, 9 + k);
     double xoffk = __dadd_rn(floor(__dsub_rn(xmin, xmid)), xmid);
     if (!isnan(kp.mesh_shift)) xoffk = __dadd_rn(xoffk, kp.mesh_shift);
     const bool badk = !(stepk > 0.0) || !isfinite(stepk) || !isfinite(xoffk);
@@ -664,11 +697,7 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
         if (lane == 0) st->status = SC_ERR_DEGENERATE;
         return;
     }
-    const double istepk = 1.0 / stepk;
-    const double steps[3] = {__shfl_sync(FULL, stepk, 0), __shfl_sync(FULL, stepk, 1), __shfl_sync(FULL, stepk, 2)};
     // near box of the hybrid Green's function along axis k (igf_box_of)
-    const double hm = fmax(steps[0], fmax(steps[1], steps[2]));
-    const double v = 5.0 * hm / stepk;
     int bk = v >= (double)nm[k] ? nm[k] : (int)ceil(v) + 1;
     if (bk > nm[k]) bk = nm[k];
     if (lane < 3) {
@@ -680,7 +709,7 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
         st->xofff[k] = (float)xoffk;
         st->igf_box[k] = bk;
     }
-    if (lane == 1) st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
+    if (lane == 1) st->phi_norm = kp.phi_norm;
     if (lane == 2) {
         // fixed-point unit of the exact deposit: sum |q| * 2^S < 2^62, so no
         // cell (nor the total) can overflow a signed 64-bit accumulator
@@ -732,13 +761,34 @@ __device__ void mesh_finalize32(const ExtPart32* part, int nblk, const KickParam
     __shared__ float smf[5 * 64];
     unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
     float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-        for (int k = 0; k < 3; ++k) {
-            const unsigned long long a = __ldcg(&part[b].mn[k]), c = __ldcg(&part[b].mx[k]);
-            mn[k] = a < mn[k] ? a : mn[k];
-            mx[k] = c > mx[k] ? c : mx[k];
+    // the partials of up to FIN_U blocks per thread loaded before any is
+    // combined (one round trip instead of FIN_U); combined in block order
+    for (int b0 = threadIdx.x; b0 < nblk; b0 += FIN_U * blockDim.x) {
+        unsigned long long pn[FIN_U][3], px[FIN_U][3];
+        float ph[FIN_U][5], pl[FIN_U][5];
+#pragma unroll
+        for (int u = 0; u < FIN_U; ++u) {
+            const int b = b0 + u * blockDim.x < nblk ? b0 + u * blockDim.x : b0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                pn[u][k] = __ldcg(&part[b].mn[k]);
+                px[u][k] = __ldcg(&part[b].mx[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                ph[u][k] = __ldcg(&part[b].hi[k]);
+                pl[u][k] = __ldcg(&part[b].lo[k]);
+            }
         }
-        for (int k = 0; k < 5; ++k) df_add(hi[k], lo[k], __ldcg(&part[b].hi[k]), __ldcg(&part[b].lo[k]));
+#pragma unroll
+        for (int u = 0; u < FIN_U; ++u) {
+            if (b0 + u * blockDim.x >= nblk) break;
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = pn[u][k] < mn[k] ? pn[u][k] : mn[k];
+                mx[k] = px[u][k] > mx[k] ? px[u][k] : mx[k];
+            }
+            for (int k = 0; k < 5; ++k) df_add(hi[k], lo[k], ph[u][k], pl[u][k]);
+        }
     }
     block_minmax_u64<3, false>(mn, smu);
     block_minmax_u64<3, true>(mx, smu);
@@ -1131,11 +1181,15 @@ __global__ void __launch_bounds__(PT, 4) k_extent32(const double* __restrict__ r
     extent32_body<VEC>(rp, q, kp, X, part, st, hw_vblk());
 }
 
+constexpr int EX_SCAN = 4;  // tiles whose coordinates a pass-2 thread loads before checking them
+
 // extent32_body with the six rows and the charges streamed through shared
 // memory (rows and q 16-byte aligned, even stride).  Pass 2 is walked only
 // by the threads whose own FP32 extreme lies within the margin of the
 // block's: a particle of any other thread is farther from the block's
-// extreme than that thread's extreme, so the candidates are the same.
+// extreme than that thread's extreme, so the candidates are the same.  Each
+// such thread loads the coordinates of EX_SCAN tiles before it checks them,
+// one round trip per EX_SCAN tiles instead of one per tile.
 __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp, const double* __restrict__ q,
                                                   const KickParams& kp, float* __restrict__ X,
                                                   double* __restrict__ part, ScState* st, VBlk vb) {
@@ -1250,25 +1304,44 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) Td[a][b] = st->T[a][b];
         const double g0d = st->gamma0;
-        for (int64_t t = 0; t < Tl.mine; ++t)
-            for (int w = 0; w < 2; ++w) {
-                const int jj = 2 * threadIdx.x + w;
-                if (jj >= Tl.count(t)) break;
-                const int64_t i = Tl.start(t) + jj;
-                bool cand = false;
-                for (int j = 0; j < 3; ++j) {
-                    const float v = X[j * nX + i];
-                    cand |= (v <= bmin[j] + tol[j]) || (v >= bmax[j] - tol[j]);
+        for (int64_t t0 = 0; t0 < Tl.mine; t0 += EX_SCAN) {
+            float xv[EX_SCAN][2][3];
+#pragma unroll
+            for (int u = 0; u < EX_SCAN; ++u)
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    const int64_t t = t0 + u;
+                    const int jj = 2 * threadIdx.x + w;
+                    const bool valid = t < Tl.mine && jj < Tl.count(t);
+                    const int64_t i = valid ? Tl.start(t) + jj : 0;
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) xv[u][w][j] = valid ? X[j * nX + i] : NAN;
                 }
-                if (cand) {
-                    double v[3];
-                    xyz_fine(rp, ld, i, kp, Td, g0d, v);
-                    for (int j = 0; j < 3; ++j) {
-                        if (X[j * nX + i] <= bmin[j] + tol[j]) atomicMin(&emin[j], ord64(v[j]));
-                        if (X[j * nX + i] >= bmax[j] - tol[j]) atomicMax(&emax[j], ord64(v[j]));
+            // the extremes each particle may be: 6 bits per particle (min x, y, z; max x, y, z)
+            unsigned long long sides = 0;
+#pragma unroll
+            for (int u = 0; u < EX_SCAN; ++u)
+#pragma unroll
+                for (int w = 0; w < 2; ++w)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {  // NaN (no particle) is no candidate
+                        const int b = 6 * (2 * u + w);
+                        if (xv[u][w][j] <= bmin[j] + tol[j]) sides |= 1ull << (b + j);
+                        if (xv[u][w][j] >= bmax[j] - tol[j]) sides |= 8ull << (b + j);
                     }
+            while (sides) {
+                const int p = (__ffsll((long long)sides) - 1) / 6;  // first candidate: particle p of the chunk
+                const unsigned sd = (unsigned)(sides >> (6 * p)) & 63u;
+                sides &= ~(63ull << (6 * p));
+                const int64_t i = Tl.start(t0 + p / 2) + 2 * threadIdx.x + (p & 1);
+                double v[3];
+                xyz_fine(rp, ld, i, kp, Td, g0d, v);
+                for (int j = 0; j < 3; ++j) {
+                    if (sd & (1u << j)) atomicMin(&emin[j], ord64(v[j]));
+                    if (sd & (8u << j)) atomicMax(&emax[j], ord64(v[j]));
                 }
             }
+        }
     }
     __syncthreads();
     ExtPart32* ep = reinterpret_cast<ExtPart32*>(part);
@@ -1327,7 +1400,7 @@ __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickPar
     st->steps[1] = hy;
     st->steps[2] = hz;
     st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, hx), hy), hz);
-    st->phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
+    st->phi_norm = kp.phi_norm;
     const double h[3] = {hx, hy, hz};
     igf_box_of(h, kp.nx, kp.ny, kp.nz, st->igf_box);
     const bool same = hx == st->igf_h[0] && hy == st->igf_h[1] && hz == st->igf_h[2];
