@@ -50,6 +50,7 @@ struct ScState {
     double isteps[3];            // 1/steps
     double phi_denom;            // 4*pi*eps0*hx*hy*hz (sc.py:167)
     double phi_norm;             // 1/(Mx*My*Mz) of the inverse FFT
+    float phi_scalef;            // (float)(phi_norm / phi_denom): the FP32 form's potential scale
     // Green's-function cache: spacing of the spectrum held in the workspace
     double igf_h[3];
     // FP32 copies of the per-kick constants, written once by the finalizes
@@ -68,6 +69,7 @@ struct ScState {
     int igf_box[3];
     unsigned int done_frame;     // blocks finished, for the last-block reductions
     unsigned int done_extent;
+    unsigned int kick_next;      // tiles claimed by the gather + kick (reset by the frame finalize)
     int frame_timeout;           // a frame block's bulk-copy wait gave up (the finalize reports it)
     int check_code;              // checked builds: first failed index check (kernel code)
     int first_error;             // first non-OK status of any kick since sc_workspace_init

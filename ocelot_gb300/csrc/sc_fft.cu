@@ -213,7 +213,7 @@ __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __rest
     __syncthreads();
     Cx<R>* res = fft_lines<R, true>(a, b, lz, NC, rz, tw);
     const double norm = st->phi_norm, denom = st->phi_denom;
-    const R fscale = (R)(norm / denom);
+    const R fscale = (R)st->phi_scalef;  // (float)(norm / denom), computed once by the mesh finalize
     for (int idx = threadIdx.x; idx < NC * nz; idx += blockDim.x) {
         const int c = idx / nz, z = idx - c * nz;
         const int ya = y0 + 2 * c, yb = ya + 1;
@@ -442,7 +442,7 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
     __syncthreads();
     const Cx<R>* res = fft_lines<R, true>(A1, B1, lz, ncz, rz, twz);
     const double norm = st->phi_norm, denom = st->phi_denom;
-    const R fscale = (R)(norm / denom);
+    const R fscale = (R)st->phi_scalef;  // (float)(norm / denom), computed once by the mesh finalize
     for (int idx = threadIdx.x; idx < ncz * nz; idx += blockDim.x) {
         const int c = idx / nz, z = idx - c * nz;
         const int ya = 2 * c, yb = ya + 1;

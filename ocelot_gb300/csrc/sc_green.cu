@@ -128,7 +128,18 @@ __device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* 
     igf_spacing(st, a, hx, hy, hz);
     int bx[3];
     igf_box(st, nx, ny, nz, a.hybrid, bx);
-    const float hxf = (float)hx, hyf = (float)hy, hzf = (float)hz;
+    // the FP32 spacing: the copies the mesh finalize stored (conversions
+    // from FP64 issue on this GPU's slow FP64 pipe, so not once per thread)
+    float hxf, hyf, hzf;
+    if (a.use_state) {
+        hxf = st->stepsf[0];
+        hyf = st->stepsf[1];
+        hzf = st->stepsf[2];
+    } else {
+        hxf = (float)hx;
+        hyf = (float)hy;
+        hzf = (float)hz;
+    }
     const float a2 = 0.25f * hxf * hxf, b2 = 0.25f * hyf * hyf, c2 = 0.25f * hzf * hzf, V = hxf * hyf * hzf;
     const unsigned total = (unsigned)nx * ny * nz;
     const unsigned sy = bx[2] + 1, sx = (unsigned)(bx[1] + 1) * (bx[2] + 1);

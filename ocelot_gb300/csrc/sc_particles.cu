@@ -525,6 +525,7 @@ __device__ void frame_finish(const double (&acc)[3], const KickParams& kp, ScSta
     __shared__ int s_bad1;
     if (threadIdx.x == 0) {
         st->done_frame = 0;
+        st->kick_next = 0;  // the tile counter of this kick's gather + kick
         // the previous kick's outcome, kept before this kick resets the status
         if (st->status != SC_OK && st->first_error == SC_OK) st->first_error = st->status;
         for (int k = 0; k < 3; ++k) s_acc[k] = acc[k];
@@ -596,7 +597,6 @@ __device__ void frame_finalize(const double* part, int nblk, const KickParams& k
     frame_finish(acc, kp, st);
 }
 
-constexpr int FIN_U = 3;  // partials per thread per round of the last-block reductions
 
 // FP32 form: per-block momentum sums as double-float pairs (hi[3], lo[3]),
 // reduced on the FP32 pipes
@@ -606,24 +606,8 @@ struct FramePart32 {
 __device__ void frame_finalize32(const FramePart32* part, int nblk, const KickParams& kp, ScState* st) {
     __shared__ float sm[3 * 64];
     float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
-    // loads of up to FIN_U partials per thread before any is combined (block order)
-    for (int b0 = threadIdx.x; b0 < nblk; b0 += FIN_U * blockDim.x) {
-        float ph[FIN_U][3], pl[FIN_U][3];
-#pragma unroll
-        for (int u = 0; u < FIN_U; ++u) {
-            const int b = b0 + u * blockDim.x < nblk ? b0 + u * blockDim.x : b0;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                ph[u][k] = __ldcg(&part[b].hi[k]);
-                pl[u][k] = __ldcg(&part[b].lo[k]);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < FIN_U; ++u) {
-            if (b0 + u * blockDim.x >= nblk) break;
-            for (int k = 0; k < 3; ++k) df_add(hi[k], lo[k], ph[u][k], pl[u][k]);
-        }
-    }
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+        for (int k = 0; k < 3; ++k) df_add(hi[k], lo[k], __ldcg(&part[b].hi[k]), __ldcg(&part[b].lo[k]));
     block_sum_df<3>(hi, lo, sm);
     const double acc[3] = {(double)hi[0] + (double)lo[0], (double)hi[1] + (double)lo[1],
                            (double)hi[2] + (double)lo[2]};
@@ -670,12 +654,14 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
     const double qsum = s_qs[3];
     const int nm[3] = {kp.nx, kp.ny, kp.nz};
     // Every lane takes axis a = lane % 3 of the step; then group g = lane / 3
-    // (0..3; lanes 12..31 repeat group 3) divides by it: g = 0 X_min,
+    // (0..4; lanes 15..31 repeat group 3) divides by it: g = 0 X_min,
     // g = 1 the charge-weighted mean (then / sum q), g = 2 1/step, g = 3 the
-    // near-box ratio 5 h_max / step.  One SIMD division serves all four, so
-    // the chain holds three dependent divisions instead of six; each value is
-    // the same operation sequence as the serial form.
-    const int a = lane % 3, g = lane < 12 ? lane / 3 : 3;
+    // near-box ratio 5 h_max / step; in the second division group 4 forms the
+    // FP32 form's potential scale phi_norm / (4 pi eps0 hx hy hz).  One SIMD
+    // division serves all groups, so the chain holds three dependent
+    // divisions instead of seven; each value is the same operation sequence
+    // as the serial form.
+    const int a = lane % 3, g = lane < 15 ? lane / 3 : 3;
     double XX = __dsub_rn(s_mx[a], s_mn[a]);
     if (!isnan(kp.mesh_scale)) XX = __dmul_rn(XX, kp.mesh_scale);
     const double stepa = __ddiv_rn(XX, (double)(nm[a] - 3));
@@ -683,12 +669,15 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
     const double hm = fmax(steps[0], fmax(steps[1], steps[2]));
     const double num = g == 0 ? s_mn[a] : g == 1 ? q3[a] : g == 2 ? 1.0 : __dmul_rn(5.0, hm);
     const double r1 = __ddiv_rn(num, stepa);
-    const double r2 = __ddiv_rn(r1, qsum);  // used by group 1
+    const double pden = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, steps[0]), steps[1]), steps[2]);
+    const double n2 = g == 4 ? kp.phi_norm : r1, d2 = g == 4 ? pden : qsum;
+    const double r2 = __ddiv_rn(n2, d2);  // used by groups 1 and 4
     const double stepk = steps[k];
     const double xmin = __shfl_sync(FULL, r1, k);
     const double xmid = __shfl_sync(FULL, r2, 3 + k);
     const double istepk = __shfl_sync(FULL, r1, 6 + k);
     const double v = __shfl_sync(FULL, r1, 9 + k);
+    const double scale = __shfl_sync(FULL, r2, 12);
     double xoffk = __dadd_rn(floor(__dsub_rn(xmin, xmid)), xmid);
     if (!isnan(kp.mesh_shift)) xoffk = __dadd_rn(xoffk, kp.mesh_shift);
     const bool badk = !(stepk > 0.0) || !isfinite(stepk) || !isfinite(xoffk);
@@ -721,7 +710,8 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
         st->qfix_inv = (float)ldexp(1.0, -S);
     }
     if (lane == 0) {
-        st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, steps[0]), steps[1]), steps[2]);
+        st->phi_denom = pden;
+        st->phi_scalef = (float)scale;
         const bool same = steps[0] == st->igf_h[0] && steps[1] == st->igf_h[1] && steps[2] == st->igf_h[2];
         st->igf_rebuild = same ? 0 : 1;
         for (int j = 0; j < 3; ++j) st->igf_h[j] = steps[j];
@@ -761,34 +751,13 @@ __device__ void mesh_finalize32(const ExtPart32* part, int nblk, const KickParam
     __shared__ float smf[5 * 64];
     unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
     float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    // the partials of up to FIN_U blocks per thread loaded before any is
-    // combined (one round trip instead of FIN_U); combined in block order
-    for (int b0 = threadIdx.x; b0 < nblk; b0 += FIN_U * blockDim.x) {
-        unsigned long long pn[FIN_U][3], px[FIN_U][3];
-        float ph[FIN_U][5], pl[FIN_U][5];
-#pragma unroll
-        for (int u = 0; u < FIN_U; ++u) {
-            const int b = b0 + u * blockDim.x < nblk ? b0 + u * blockDim.x : b0;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                pn[u][k] = __ldcg(&part[b].mn[k]);
-                px[u][k] = __ldcg(&part[b].mx[k]);
-            }
-#pragma unroll
-            for (int k = 0; k < 5; ++k) {
-                ph[u][k] = __ldcg(&part[b].hi[k]);
-                pl[u][k] = __ldcg(&part[b].lo[k]);
-            }
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        for (int k = 0; k < 3; ++k) {
+            const unsigned long long a = __ldcg(&part[b].mn[k]), c = __ldcg(&part[b].mx[k]);
+            mn[k] = a < mn[k] ? a : mn[k];
+            mx[k] = c > mx[k] ? c : mx[k];
         }
-#pragma unroll
-        for (int u = 0; u < FIN_U; ++u) {
-            if (b0 + u * blockDim.x >= nblk) break;
-            for (int k = 0; k < 3; ++k) {
-                mn[k] = pn[u][k] < mn[k] ? pn[u][k] : mn[k];
-                mx[k] = px[u][k] > mx[k] ? px[u][k] : mx[k];
-            }
-            for (int k = 0; k < 5; ++k) df_add(hi[k], lo[k], ph[u][k], pl[u][k]);
-        }
+        for (int k = 0; k < 5; ++k) df_add(hi[k], lo[k], __ldcg(&part[b].hi[k]), __ldcg(&part[b].lo[k]));
     }
     block_minmax_u64<3, false>(mn, smu);
     block_minmax_u64<3, true>(mx, smu);
@@ -1399,7 +1368,11 @@ __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickPar
     st->steps[0] = hx;
     st->steps[1] = hy;
     st->steps[2] = hz;
+    st->stepsf[0] = (float)hx;
+    st->stepsf[1] = (float)hy;
+    st->stepsf[2] = (float)hz;
     st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, hx), hy), hz);
+    st->phi_scalef = (float)(kp.phi_norm / st->phi_denom);
     st->phi_norm = kp.phi_norm;
     const double h[3] = {hx, hy, hz};
     igf_box_of(h, kp.nx, kp.ny, kp.nz, st->igf_box);
@@ -1848,36 +1821,53 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
     uint64_t* bar = reinterpret_cast<uint64_t*>(buf + KT_STAGES * 6 * KT_TILE);
     const int64_t n = kp.n, ld = kp.ld;
     const int64_t ntile = (n + KT_TILE - 1) / KT_TILE;
-    const int64_t mine = vb.x < ntile ? (ntile - 1 - vb.x) / vb.nx + 1 : 0;  // this block's tiles
     const bool lead = threadIdx.x == 0;
+    // Tiles are handed out at run time: a block's first tile is its index,
+    // each further one is claimed from the kick's tile counter when its
+    // loads are issued, so blocks on faster SMs take more tiles and the
+    // blocks finish together.  s_tile[s] is the tile in buffer s; a tile
+    // index >= ntile marks the end.  (The tiles are independent: which block
+    // kicks a particle does not change its result.)
+    __shared__ int64_t s_tile[KT_STAGES];
     if (lead) {
         for (int s = 0; s < KT_STAGES; ++s) mbar_init(&bar[s], 1);
         mbar_init_fence();
     }
     __syncthreads();
-    auto tile_start = [&](int64_t t) { return (vb.x + t * vb.nx) * (int64_t)KT_TILE; };
-    auto tile_count = [&](int64_t t) {
-        const int64_t c = n - tile_start(t);
+    auto tile_start = [&](int64_t g) { return g * (int64_t)KT_TILE; };
+    auto tile_count = [&](int64_t g) {
+        const int64_t c = n - tile_start(g);
         return (int)(c < KT_TILE ? c : KT_TILE);
     };
-    auto issue = [&](int64_t t) {  // lead thread: the loads of local tile t
-        const int s = (int)(t % KT_STAGES);
-        const int64_t i0 = tile_start(t);
-        const unsigned bytes = (unsigned)(tile_count(t) & ~1) * 8u;
+    auto claim = [&]() { return (int64_t)vb.nx + (int64_t)atomicAdd(&st->kick_next, 1u); };
+    auto issue = [&](int64_t u, int64_t g) {  // lead thread: tile g as the block's u-th, into buffer u % KT_STAGES
+        const int s = (int)(u % KT_STAGES);
+        s_tile[s] = g;
+        if (g >= ntile) return;
+        const int64_t i0 = tile_start(g);
+        const unsigned bytes = (unsigned)(tile_count(g) & ~1) * 8u;
         mbar_arrive_expect_tx(&bar[s], 6u * bytes);
         if (bytes)
             for (int k = 0; k < 6; ++k) bulk_load(buf + (s * 6 + k) * KT_TILE, rp + k * ld + i0, bytes, &bar[s]);
     };
-    int64_t issued = mine < KT_STAGES ? mine : KT_STAGES;
+    int64_t issued = 0;  // lead: tiles issued (the end marker included)
+    bool more = true;    // lead: the last claim was a tile
     if (lead)
-        for (int64_t t = 0; t < issued; ++t) issue(t);
+        for (int u = 0; u < KT_STAGES && more; ++u) {
+            const int64_t g = u == 0 ? (int64_t)vb.x : claim();
+            issue(issued++, g);
+            more = g < ntile;
+        }
+    __syncthreads();
     const Kick32C C = kick32_const(st, kp, ox, oy, oz);
     int64_t t = 0;
     bool failed = false;
-    for (; t < mine; ++t) {
+    for (;; ++t) {
         const int s = (int)(t % KT_STAGES);
-        const int64_t i0 = tile_start(t);
-        const int cnt = tile_count(t), staged = cnt & ~1;
+        const int64_t g = s_tile[s];
+        if (g >= ntile) break;  // the same in every thread
+        const int64_t i0 = tile_start(g);
+        const int cnt = tile_count(g), staged = cnt & ~1;
         const bool ok = mbar_wait(&bar[s], (unsigned)((t / KT_STAGES) & 1));
         double* B = buf + s * 6 * KT_TILE;
         const int j = 2 * threadIdx.x;
@@ -1910,18 +1900,21 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
                 for (int k = 0; k < 6; ++k) bulk_store(rp + k * ld + i0, B + k * KT_TILE, (unsigned)staged * 8u);
             bulk_commit();
             // refill the previous tile's buffer once its store has read it
-            if (t >= 1 && issued < mine) {
+            if (t >= 1 && more) {
                 bulk_wait_read<1>();
-                issue(issued);
-                ++issued;
+                const int64_t g2 = claim();
+                issue(issued++, g2);
+                more = g2 < ntile;
             }
         }
+        // the buffer refilled here is read KT_STAGES - 1 iterations on, after
+        // the barriers of the iterations between
     }
     if (lead) {
         if (failed) {
             atomicCAS(&st->status, SC_OK, SC_ERR_TIMEOUT);
             for (int64_t u = t; u < issued; ++u)  // loads still in flight must land before the block exits
-                mbar_wait(&bar[u % KT_STAGES], (unsigned)((u / KT_STAGES) & 1));
+                if (s_tile[u % KT_STAGES] < ntile) mbar_wait(&bar[u % KT_STAGES], (unsigned)((u / KT_STAGES) & 1));
         }
         bulk_wait_all();
     }
