@@ -54,7 +54,7 @@ B_KICK_KERNEL_PER_PARTICLE = 96  # gather+kick: rparticles read + write
 # summarised in profiles/k_kick32_tma_4M_64cube.txt (200.62 MB read + 132.30 MB
 # written at 4M particles); traffic grows with the particles, so it is scaled
 # to the bench's n
-KICK_TRAFFIC_PER_PARTICLE = (200.62e6 + 132.30e6) / 4e6
+KICK_TRAFFIC_PER_PARTICLE = (200.73e6 + 131.93e6) / 4e6
 
 
 def log(*a):
