@@ -183,6 +183,7 @@ struct sc_plan {
     int last_launches;
     cudaStream_t side;     // the Green's-function build runs here, beside the deposit
     cudaEvent_t fork, join;
+    int* status_host;      // pinned: the status word is read with an asynchronous copy
 };
 
 static const char* kStageNames[SC_NSTAGES] = {"frame", "extent", "keys", "sort", "deposit",
@@ -320,8 +321,13 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio_hi), "cudaStreamCreate");
     SC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
     SC_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
+    int* status_host = nullptr;
+    SC_CUDA(cudaMallocHost(reinterpret_cast<void**>(&status_host), sizeof(int)), "cudaMallocHost");
     sc_plan* h = new (std::nothrow) sc_plan;
-    if (!h) return fail(SC_ERR_ARG, "out of host memory");
+    if (!h) {
+        cudaFreeHost(status_host);
+        return fail(SC_ERR_ARG, "out of host memory");
+    }
     h->p = p;
     h->ws_ready = nullptr;
     h->ws_ready_bytes = 0;
@@ -331,6 +337,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     h->side = side;
     h->fork = fork;
     h->join = join;
+    h->status_host = status_host;
     *out = h;
     return SC_OK;
 }
@@ -345,6 +352,7 @@ void sc_plan_destroy(sc_plan* plan) {
         cudaEventDestroy(plan->fork);
         cudaEventDestroy(plan->join);
     }
+    if (plan->status_host) cudaFreeHost(plan->status_host);
     delete plan;
 }
 
@@ -436,11 +444,13 @@ int sc_workspace_init(const sc_plan* plan_c, void* ws, size_t ws_bytes, void* st
 int sc_read_status(const sc_plan* plan, void* ws, void* stream) {
     if (!plan || !ws) return fail(SC_ERR_ARG, "plan or workspace is NULL");
     const Layout L = make_layout(plan->p, 0);
-    SC_CUDA(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
-    int status = 0;
-    SC_CUDA(cudaMemcpy(&status, static_cast<char*>(ws) + L.state + offsetof(ScState, status), sizeof(int),
-                       cudaMemcpyDeviceToHost),
+    // one wait for the stream: the status word follows the work already queued
+    // on it (copies of the results included) into pinned memory
+    SC_CUDA(cudaMemcpyAsync(plan->status_host, static_cast<char*>(ws) + L.state + offsetof(ScState, status),
+                            sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream),
             "read status");
+    SC_CUDA(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+    const int status = *plan->status_host;
     if (status == SC_ERR_DEGENERATE)
         return fail(status, "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)");
     if (status == SC_ERR_NONFINITE)

@@ -249,10 +249,14 @@ class SpaceCharge(PhysProc):
             d_rp.copy_(h_rp, non_blocking=True)
             d_q.copy_(h_q, non_blocking=True)
             eng.kick(d_rp, d_q, n, p_array.E, zstep, scale, shift)
-            eng.check_status()
             if src is rp:
-                h_rp.copy_(d_rp)
+                # queued behind the kick; check_status waits once for both.  A
+                # kick that stops on an error leaves the device copy as it was
+                # copied in, so the caller's values come back unchanged.
+                h_rp.copy_(d_rp, non_blocking=True)
+                eng.check_status()
             else:
+                eng.check_status()
                 rp[...] = d_rp.cpu().numpy()
 
     def apply_device(self, rparticles, q_array, energy_gev, zstep, mesh_draws=None):
