@@ -525,8 +525,9 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     mark(plan, 8, s);
     SC_CUDA(launch_gather_kick(p, L, ws, kp, rp, s), "gather/kick");
     mark(plan, 9, s);
-    // frame 1, extent 1, keys 1, [sort 3 per pass, deposit 2], igf 2, green 3, convolve 5, field 1, kick 1
-    plan->last_launches = 1 + 1 + 1 + (p.sorted_deposit ? 3 * passes + 2 : 0) + 2 + 3 + 5 + 1 + 1;
+    // frame 1, extent 1, keys 1, [sort 3 per pass, deposit 2], igf 2, green 3, convolve 3 (plane passes) or 5,
+    // field 1, kick 1
+    plan->last_launches = 1 + 1 + 1 + (p.sorted_deposit ? 3 * passes + 2 : 0) + 2 + 3 + convolve_launches(p) + 1 + 1;
     return SC_OK;
 }
 

@@ -214,6 +214,8 @@ enum ConvPart { CONV_ALL = 0, CONV_FORWARD = 1, CONV_REST = 2 };
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in,
                             void* phi_out, cudaStream_t s, const long long* qfix = nullptr, int part = CONV_ALL);
 cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
+// kernels launch_convolve(CONV_ALL) launches for this plan
+int convolve_launches(const Plan& p);
 
 // first-order map (sc_tmap.cu)
 cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n,

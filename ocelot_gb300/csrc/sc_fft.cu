@@ -467,6 +467,12 @@ __global__ void __launch_bounds__(PLANE_THREADS) k_yz_inv(const Cx<R>* __restric
     yz_inv_body<R>(W, phi, ny, nz, My, Kz, rz, ry, twz, twy, st, (int)blockIdx.x);
 }
 
+static int optin_smem();
+int convolve_launches(const Plan& p) {
+    const bool plane = p.prec == SC_FP64 ? plane_fits<double>(p, optin_smem()) : plane_fits<float>(p, optin_smem());
+    return plane ? 3 : 5;
+}
+
 static int optin_smem() {
     int dev = 0, v = 0;
     if (cudaGetDevice(&dev) || cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) return 0;

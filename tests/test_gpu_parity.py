@@ -340,6 +340,38 @@ def test_device_resident_path_matches_host_path():
     assert np.array_equal(dpa.rparticles.cpu().numpy(), host.rparticles)
 
 
+@pytest.mark.parametrize("n,pinned", [(3, False), (1001, False), (200_001, False), (200_001, True)])
+def test_fp32_host_path_matches_device_path(n, pinned):
+    """SpaceCharge.apply on host arrays (sc_kick_host: copies overlapped, the
+    kick in chunks copied back one by one) equals the device-resident kick."""
+    rp, q = sc_oracle.gaussian_beam(n, 11)
+    host_rp = rp.copy()
+    if pinned:
+        t = torch.empty((6, n), dtype=torch.float64).pin_memory()
+        host_rp = t.numpy()
+        host_rp[:] = rp
+    host = make_pa(host_rp, q, 0.130)
+    host.rparticles = host_rp
+    SpaceCharge(nmesh_xyz=[32, 32, 32], precision="fp32").apply(host, 0.1)
+    # the device rows with the staging buffer's even row stride: the FP32
+    # reductions (and so the last bits of the kick) depend on the row layout
+    d_rp = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=DEV)[:, :n]
+    d_rp.copy_(torch.from_numpy(rp))
+    sc = SpaceCharge(nmesh_xyz=[32, 32, 32], precision="fp32")
+    sc.apply_device(d_rp, torch.from_numpy(q).to(DEV), 0.130, 0.1)
+    sc.check()
+    assert np.array_equal(d_rp.cpu().numpy(), host.rparticles)
+
+
+def test_fp32_host_path_error_leaves_particles():
+    rp, q = sc_oracle.gaussian_beam(5000, 12)
+    rp[2, 4321] = np.inf
+    pa = make_pa(rp, q, 0.130)
+    with pytest.raises(ValueError):
+        SpaceCharge(nmesh_xyz=[15, 15, 15], precision="fp32").apply(pa, 0.1)
+    assert np.array_equal(pa.rparticles, rp, equal_nan=True)
+
+
 @pytest.mark.parametrize("n", [1, 2])
 def test_degenerate_beam_raises_and_leaves_particles(n):
     rp = np.zeros((6, n))
