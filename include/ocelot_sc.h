@@ -243,6 +243,32 @@ int sc_tmap2_apply(const double* maps, int nmaps, double* rparticles, int64_t ld
 int sc_tmap2_apply_step(const double* maps, const int* first, int* counter, int nsteps, double* rparticles,
                         int64_t ld, int64_t n, void* stream);
 
+/* Slices of a tracking step that pass RF cavities: each record of the table
+ * (SC_MAP2_DOUBLES doubles) is either a map as in sc_tmap2_apply
+ * (kinds[m] = SC_SLICE_MAP; a first-order map has Tc = 0) or a cavity slice
+ * (kinds[m] = SC_SLICE_CAVITY), CavityTM.map4cav
+ * (ocelot/cpbd/transformations/cavity.py:29-128): x <- R.x + B with the
+ * slice's first-order matrix (elements/cavity_atom.py:93-179, tilt applied),
+ * then from the coordinates before it
+ *   x5 <- x5 E beta0 / D + A (cos(-x4 beta0 k + phi) - cos(phi)),
+ *   x4 <- x4 + T566 x5^2 + T556 x4 x5 + T555 x4^2
+ * with the record's doubles 42..52: E (energy at the slice start, GeV), beta0,
+ * D = E1 beta1, A = V beta0 / D, k = 2 pi f / c, phi [rad], cos(phi), T566,
+ * T556, T555, and a flag that is 0 when the energy after the slice is not
+ * positive (then only the T566 term is applied and x5 keeps R.x + B).
+ * The host computes the scalars in the reference's order of operations.
+ *   kinds: DEVICE int32[nmaps]. */
+#define SC_SLICE_MAP 0
+#define SC_SLICE_CAVITY 1
+int sc_slices_apply(const double* maps, const int* kinds, int nmaps, double* rparticles, int64_t ld, int64_t n,
+                    void* stream);
+
+/* The slices [first[s], first[s+1]) at s = *counter, then *counter += 1, in
+ * stream order (the transport of a device-resident tracking loop through a
+ * line with cavities; as sc_tmap2_apply_step). */
+int sc_slices_apply_step(const double* maps, const int* kinds, const int* first, int* counter, int nsteps,
+                         double* rparticles, int64_t ld, int64_t n, void* stream);
+
 /* ---- stage timing (benchmarking) --------------------------------------- */
 
 /* Stages of sc_kick: MAD->lab frame (coord_transform.py:57-96,

@@ -849,7 +849,7 @@ int sc_tmap2_apply(const double* maps, int nmaps, double* rp, int64_t ld, int64_
     if (nmaps == 0 || n == 0) return SC_OK;
     if (!maps || !rp) return fail(SC_ERR_ARG, "maps or rparticles is NULL");
     if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
-    SC_CUDA(launch_tmap2(maps, nmaps, rp, ld, n, (cudaStream_t)stream), "tmap2");
+    SC_CUDA(launch_tmap2(maps, nullptr, nmaps, rp, ld, n, (cudaStream_t)stream), "tmap2");
     return SC_OK;
 }
 
@@ -859,7 +859,27 @@ int sc_tmap2_apply_step(const double* maps, const int* first, int* counter, int 
     if (nsteps < 1 || n < 0) return fail(SC_ERR_ARG, "nsteps < 1 or n < 0");
     if (n > 0 && !rp) return fail(SC_ERR_ARG, "rparticles is NULL");
     if (n > 0 && ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
-    SC_CUDA(launch_tmap2_step(maps, first, counter, nsteps, rp, ld, n, (cudaStream_t)stream), "tmap2");
+    SC_CUDA(launch_tmap2_step(maps, nullptr, first, counter, nsteps, rp, ld, n, (cudaStream_t)stream), "tmap2");
+    return SC_OK;
+}
+
+int sc_slices_apply(const double* maps, const int* kinds, int nmaps, double* rp, int64_t ld, int64_t n,
+                    void* stream) {
+    if (nmaps < 0 || n < 0) return fail(SC_ERR_ARG, "nmaps < 0 or n < 0");
+    if (nmaps == 0 || n == 0) return SC_OK;
+    if (!maps || !kinds || !rp) return fail(SC_ERR_ARG, "maps, kinds or rparticles is NULL");
+    if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
+    SC_CUDA(launch_tmap2(maps, kinds, nmaps, rp, ld, n, (cudaStream_t)stream), "slices");
+    return SC_OK;
+}
+
+int sc_slices_apply_step(const double* maps, const int* kinds, const int* first, int* counter, int nsteps,
+                         double* rp, int64_t ld, int64_t n, void* stream) {
+    if (!maps || !kinds || !first || !counter) return fail(SC_ERR_ARG, "maps, kinds, first or counter is NULL");
+    if (nsteps < 1 || n < 0) return fail(SC_ERR_ARG, "nsteps < 1 or n < 0");
+    if (n > 0 && !rp) return fail(SC_ERR_ARG, "rparticles is NULL");
+    if (n > 0 && ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
+    SC_CUDA(launch_tmap2_step(maps, kinds, first, counter, nsteps, rp, ld, n, (cudaStream_t)stream), "slices");
     return SC_OK;
 }
 

@@ -220,9 +220,10 @@ int convolve_launches(const Plan& p);
 // first-order map (sc_tmap.cu)
 cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld, int64_t n,
                         cudaStream_t s);
-cudaError_t launch_tmap2(const double* maps, int nmaps, double* rp, int64_t ld, int64_t n, cudaStream_t s);
-cudaError_t launch_tmap2_step(const double* maps, const int* first, int* counter, int nsteps, double* rp, int64_t ld,
-                              int64_t n, cudaStream_t s);
+cudaError_t launch_tmap2(const double* maps, const int* kinds, int nmaps, double* rp, int64_t ld, int64_t n,
+                         cudaStream_t s);
+cudaError_t launch_tmap2_step(const double* maps, const int* kinds, const int* first, int* counter, int nsteps,
+                              double* rp, int64_t ld, int64_t n, cudaStream_t s);
 cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld,
                                 int64_t n, cudaStream_t s);
 

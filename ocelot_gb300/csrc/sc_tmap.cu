@@ -142,35 +142,80 @@ __device__ __forceinline__ void tmap2_one(const double* __restrict__ m, double (
     for (int r = 0; r < 6; ++r) x[r] = __dadd_rn(y[r], __ldg(m + 36 + r));
 }
 
+// An RF cavity slice, CavityTM.map4cav (ocelot/cpbd/transformations/cavity.py:29-128):
+// the first-order map x <- R.x + B of the slice, then, from the coordinates
+// before it,
+//   x5 <- x5_0 E beta0 / (E1 beta1) + V beta0 / (E1 beta1) (cos(-x4_0 beta0 k + phi) - cos phi)
+//   x4 <- x4 + T566 x5_0^2 + T556 x4_0 x5_0 + T555 x4_0^2
+// with the reference's operation order (the products left to right, one
+// division).  A cavity record is MAP2 doubles: R, B, then the slice's scalars
+// at CAV_*; when the energy after the slice is not positive only the T566
+// term is applied and x5 keeps its first-order value (cavity.py:67-70).
+constexpr int CAV_E = 42, CAV_BETA0 = 43, CAV_DEN = 44, CAV_A = 45, CAV_K = 46, CAV_PHI = 47, CAV_COSPHI = 48,
+              CAV_T566 = 49, CAV_T556 = 50, CAV_T555 = 51, CAV_RF = 52;
+
+__device__ __forceinline__ void cavity_one(const double* __restrict__ m, double (&x)[6]) {
+    const double x4 = x[4], x5 = x[5];
+    double y[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        double acc = __dmul_rn(__ldg(m + r * 6), x[0]);
+#pragma unroll
+        for (int k = 1; k < 6; ++k) acc = __fma_rn(__ldg(m + r * 6 + k), x[k], acc);
+        y[r] = __dadd_rn(acc, __ldg(m + 36 + r));
+    }
+    const double t566 = __ldg(m + CAV_T566);
+    if (__ldg(m + CAV_RF) != 0.0) {
+        const double beta0 = __ldg(m + CAV_BETA0);
+        const double lin = __ddiv_rn(__dmul_rn(__dmul_rn(x5, __ldg(m + CAV_E)), beta0), __ldg(m + CAV_DEN));
+        const double arg = __dadd_rn(__dmul_rn(__dmul_rn(-x4, beta0), __ldg(m + CAV_K)), __ldg(m + CAV_PHI));
+        y[5] = __dadd_rn(lin, __dmul_rn(__ldg(m + CAV_A), __dsub_rn(cos(arg), __ldg(m + CAV_COSPHI))));
+        const double s = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(t566, x5), x5),
+                                             __dmul_rn(__dmul_rn(__ldg(m + CAV_T556), x4), x5)),
+                                   __dmul_rn(__dmul_rn(__ldg(m + CAV_T555), x4), x4));
+        y[4] = __dadd_rn(y[4], s);
+    } else {
+        y[4] = __dadd_rn(y[4], __dmul_rn(__dmul_rn(t566, x5), x5));
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) x[r] = y[r];
+}
+
 // maps [first, last) of the table applied in order to every particle, its
-// coordinates kept in registers between maps
-__device__ __forceinline__ void tmap2_range(const double* __restrict__ maps, int first, int last,
-                                            double* __restrict__ rp, int64_t ld, int64_t n) {
+// coordinates kept in registers between maps; kinds (optional) marks the
+// cavity slices (SC_SLICE_CAVITY), the others are second-order maps
+__device__ __forceinline__ void tmap2_range(const double* __restrict__ maps, const int* __restrict__ kinds, int first,
+                                            int last, double* __restrict__ rp, int64_t ld, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double x[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
-        for (int mi = first; mi < last; ++mi) tmap2_one(maps + (size_t)mi * MAP2, x);
+        for (int mi = first; mi < last; ++mi) {
+            if (kinds != nullptr && __ldg(kinds + mi) == SC_SLICE_CAVITY)
+                cavity_one(maps + (size_t)mi * MAP2, x);
+            else
+                tmap2_one(maps + (size_t)mi * MAP2, x);
+        }
 #pragma unroll
         for (int k = 0; k < 6; ++k) rp[k * ld + i] = x[k];
     }
 }
 
-__global__ void __launch_bounds__(256) k_tmap2(const double* __restrict__ maps, int nmaps, double* __restrict__ rp,
-                                               int64_t ld, int64_t n) {
+__global__ void __launch_bounds__(256) k_tmap2(const double* __restrict__ maps, const int* __restrict__ kinds,
+                                               int nmaps, double* __restrict__ rp, int64_t ld, int64_t n) {
     pdl_wait();
-    tmap2_range(maps, 0, nmaps, rp, ld, n);
+    tmap2_range(maps, kinds, 0, nmaps, rp, ld, n);
 }
 
 // the maps of step *counter: [first[*counter], first[*counter + 1]) (a
 // device-resident tracking loop's transport, replayed from a CUDA graph)
-__global__ void __launch_bounds__(256) k_tmap2_step(const double* __restrict__ maps, const int* __restrict__ first,
-                                                    const int* __restrict__ counter, int nsteps,
-                                                    double* __restrict__ rp, int64_t ld, int64_t n) {
+__global__ void __launch_bounds__(256) k_tmap2_step(const double* __restrict__ maps, const int* __restrict__ kinds,
+                                                    const int* __restrict__ first, const int* __restrict__ counter,
+                                                    int nsteps, double* __restrict__ rp, int64_t ld, int64_t n) {
     pdl_wait();
     const int step = *counter;
     if (step < 0 || step >= nsteps) return;
-    tmap2_range(maps, first[step], first[step + 1], rp, ld, n);
+    tmap2_range(maps, kinds, first[step], first[step + 1], rp, ld, n);
 }
 
 static int tmap_blocks(int64_t n) {
@@ -183,15 +228,16 @@ static int tmap_blocks(int64_t n) {
     return (int)(b > 0 ? b : 1);
 }
 
-cudaError_t launch_tmap2(const double* maps, int nmaps, double* rp, int64_t ld, int64_t n, cudaStream_t s) {
+cudaError_t launch_tmap2(const double* maps, const int* kinds, int nmaps, double* rp, int64_t ld, int64_t n,
+                         cudaStream_t s) {
     if (n <= 0 || nmaps <= 0) return cudaSuccess;
-    launch(k_tmap2, tmap_blocks(n), 256, 0, s, maps, nmaps, rp, ld, n);
+    launch(k_tmap2, tmap_blocks(n), 256, 0, s, maps, kinds, nmaps, rp, ld, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_tmap2_step(const double* maps, const int* first, int* counter, int nsteps, double* rp, int64_t ld,
-                              int64_t n, cudaStream_t s) {
-    if (n > 0) launch(k_tmap2_step, tmap_blocks(n), 256, 0, s, maps, first, counter, nsteps, rp, ld, n);
+cudaError_t launch_tmap2_step(const double* maps, const int* kinds, const int* first, int* counter, int nsteps,
+                              double* rp, int64_t ld, int64_t n, cudaStream_t s) {
+    if (n > 0) launch(k_tmap2_step, tmap_blocks(n), 256, 0, s, maps, kinds, first, counter, nsteps, rp, ld, n);
     launch(k_advance, 1, 1, 0, s, counter, 1);
     return cudaGetLastError();
 }

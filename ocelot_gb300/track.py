@@ -228,6 +228,141 @@ def step_maps2(elements, energy: float, unit_step: float, step: int = 1):
     return steps
 
 
+def navigator_steps(lengths, procs, unit_step: float):
+    """The steps of a Navigator with several processes, each attached over
+    elements [indx0, indx1) with its own step count: a list of
+    (sections, kicks, z0), sections = [(element index, start in the element,
+    length)] transported in the step, kicks = [(process index, zstep)] applied
+    after it, in the reference's order, and z0 the position after the step.
+    ``procs`` = [(indx0, indx1, step)] in the order the processes were added.
+
+    Restates Navigator.get_next_step / get_next / check_overjump /
+    check_proc_bounds / get_map (ocelot/cpbd/navi.py:343-352, 354-390,
+    219-266, 281-287, 406-434) with the positions of add_physics_proc
+    (navi.py:58-64) and MagneticLattice.totalLen; processes on a single
+    element (the Navigator's kick processes) are not supported.
+    """
+    lengths = [float(v) for v in lengths]
+    nel = len(lengths)
+    if not nel:
+        raise ValueError("empty lattice")
+    procs = [(int(a), int(b), int(st)) for a, b, st in procs]
+    for a, b, st in procs:
+        if not (0 <= a < nel and 0 <= b < nel and a <= b):
+            raise ValueError(f"process range [{a}, {b}) is not inside the lattice")
+        if a == b or (a + 1 == b and lengths[a] == 0):
+            raise NotImplementedError("a process on a single element (a kick process) is not supported")
+        if st < 1:
+            raise ValueError("process step must be >= 1")
+    total = 0.0
+    for v in lengths:
+        total += v
+    s_start = [np.sum(np.array(lengths[:a])) for a, _, _ in procs]
+    s_stop = [np.sum(np.array(lengths[:b])) for _, b, _ in procs]
+    counters = [st for _, _, st in procs]
+    z0, n_elem, sum_lengths = 0.0, 0, 0.0
+    out = []
+    while np.abs(z0 - total) > 1e-10:
+        active = [j for j, (a, b, _) in enumerate(procs) if a <= n_elem < b]
+        if active:
+            cmin = min(counters[j] for j in active)
+            chosen = [j for j in active if counters[j] == cmin]
+            phys = np.array([procs[j][2] for j in chosen]) * unit_step
+            for j in active:
+                counters[j] -= cmin
+                if counters[j] == 0:
+                    counters[j] = procs[j][2]
+            dz = np.min(phys)
+        else:
+            chosen = []
+            dz = (np.sum(np.array(lengths[:n_elem + 1])) if nel >= n_elem + 1 else total) - z0
+            phys = np.array([])
+        phys_red = phys - dz
+        if chosen:
+            l_stop = np.sum(np.array(lengths[:min(procs[j][1] for j in chosen)]))
+            if z0 + dz > l_stop:
+                dz = l_stop - z0
+            starts = sorted(s_start[j] for j in range(len(procs)) if j not in chosen and z0 < s_start[j] < z0 + dz)
+            if starts:
+                dz = starts[0] - z0
+        phys = phys_red + dz
+        for j in active:
+            if dz + z0 >= s_stop[j] and j not in chosen:
+                chosen.append(j)
+                phys = np.append(phys, dz)
+        if z0 + dz > total:
+            dz = total - z0
+        # Navigator.get_map
+        sections, i = [], n_elem
+        z1 = z0 + dz
+        L = sum_lengths + lengths[i]
+        while z1 + 1e-10 > L:
+            dl = L - z0
+            sections.append((i, z0 + lengths[i] - L, dl))
+            z0 = L
+            dz -= dl
+            if i >= nel - 1:
+                break
+            i += 1
+            L += lengths[i]
+        if abs(dz) > 1e-10:
+            sections.append((i, z0 + lengths[i] - L, dz))
+        z0 += dz
+        sum_lengths = L - lengths[i]
+        n_elem = i
+        out.append((sections, [(j, float(phys[q])) for q, j in enumerate(chosen)], float(z0)))
+        if len(out) > 10_000_000:
+            raise RuntimeError("the Navigator's schedule does not terminate")
+    return out
+
+
+def _line_lengths(seq):
+    from .cavity import is_cavity
+    return [float(e.l) if is_cavity(e) else _element_params(e)[0] for e in seq]
+
+
+def step_slices(elements, energy: float, steps, order: int = 2, s: float = 0.0):
+    """Device records of the maps of every step of ``steps`` (from
+    navigator_steps), with the reference energy carried through the cavities
+    as Transformation.apply does (p_array.E += delta_e after every map):
+    ([(records [m, MAP2_DOUBLES], kinds [m], kicks [(process, E, zstep)], z0)],
+    final energy, final position).  The position is accumulated as
+    Transformation.apply moves p_array.s: by each map's length, starting
+    from ``s``.  Drift/quadrupole slices are SecondTM maps (order 2) or
+    first-order maps with T = 0 (order 1); cavity sections are the coupler
+    kicks (left out when they are the identity, which the reference applies
+    exactly) and the cavity slice records."""
+    from . import cavity as CV
+    from .second_order import element_map2, pack_map
+    zero_t = np.zeros((6, 6, 6))
+    E = energy
+    out = []
+    for sections, kicks, z0 in steps:
+        recs, kinds = [], []
+        for i, start_l, dl in sections:
+            e = elements[i]
+            if CV.is_cavity(e):
+                r, k, E = CV.section_records(e, start_l, dl, E)
+                recs += list(r)
+                kinds += k
+                for kind, d in CV.section_tms(e, start_l, dl, True):
+                    s += (d if d is not None else e.l) if kind == "main" else 0.0
+                continue
+            length = _section_length(e.l, start_l, dl)
+            s += length
+            if length == 0.0:
+                continue
+            if order == 2:
+                recs.append(pack_map(*element_map2(e, length, E)))
+            else:
+                R, B = element_map(e, length, E)
+                recs.append(pack_map(R, zero_t, B))
+            kinds.append(CV.SLICE_MAP)
+        table = np.array(recs).reshape(-1, CV.MAP2_DOUBLES)
+        out.append((table, np.array(kinds, dtype=np.int32), [(j, E, zstep) for j, zstep in kicks], z0))
+    return out, E, s
+
+
 def lattice_order(lat) -> int:
     """2 when the reference lattice tracks with SecondTM (its ``method``
     dict), else 1."""
@@ -245,25 +380,48 @@ def _lattice_sequence(lat):
 
 class DeviceTrack:
     """One tracking job resident on the GPU: its particles, its map table,
-    the kick's plan and workspace (Green's table cache included) and its own
-    stream.  ``step()`` enqueues the next step; ``run()`` all of them.
+    the kicks' plans and workspaces (Green's table caches included) and its
+    own stream.  ``step()`` enqueues the next step; ``run()`` all of them.
 
-    ``elements``: drifts/quadrupoles/markers (a lattice object with
-    ``.sequence`` or a list); ``sc``: the SpaceCharge process (its precision,
-    mesh and deposit/IGF options are used; random_mesh is not supported,
-    its draws would have to be taken per step on the host); ``unit_step``:
-    the Navigator's unit step; ``p_array``: host ParticleArray or
-    DeviceParticleArray (the particles are copied once to the device).
+    ``elements``: drifts/quadrupoles/markers/cavities (a lattice object with
+    ``.sequence`` or a list); ``sc``: the SpaceCharge process attached from
+    the first to the last element, or ``processes`` = [(SpaceCharge, indx0,
+    indx1)], each attached over elements [indx0, indx1) as
+    Navigator.add_physics_proc does, in the order they were added (each
+    process's precision, mesh and deposit/IGF options are used; random_mesh
+    is not supported, its draws would have to be taken per step on the host);
+    ``unit_step``: the Navigator's unit step; ``p_array``: host ParticleArray
+    or DeviceParticleArray (the particles are copied once to the device).
+
+    A line of drifts and quadrupoles with one process over all of it and
+    first-order maps composes each step's slices into one map
+    (``sc_tmap_apply_indexed``).  Otherwise -- second-order maps, cavities,
+    several processes -- each step's slices are applied one after the other
+    in one pass (``sc_slices_apply_step``), the reference energy is carried
+    through the cavities on the host, and each kick gets the energy of its
+    step.  Steps whose kicks (energy, length, plan) repeat are recorded once
+    as a CUDA graph and replayed.
     """
 
-    def __init__(self, elements, sc, unit_step: float, p_array, graph: bool = True, stream=None, order: int = 1):
+    def __init__(self, elements, sc, unit_step: float, p_array, graph: bool = True, stream=None, order: int = 1,
+                 processes=None):
         import torch
         from .beam import DeviceParticleArray
-        from .sc import Engine, plan_mode
-        if sc.random_mesh:
-            raise NotImplementedError("random_mesh draws host random numbers per kick: use track() on the host")
+        from .cavity import is_cavity
         seq = _lattice_sequence(elements)
-        self.dev = torch.device(sc.device) if sc.device is not None else torch.device(
+        if processes is None:
+            if sc is None:
+                raise ValueError("pass sc or processes")
+            processes = [(sc, 0, len(seq) - 1)]
+            whole = True
+        else:
+            processes = [(p, int(a), int(b)) for p, a, b in processes]
+            whole = len(processes) == 1 and processes[0][1] == 0 and processes[0][2] == len(seq) - 1
+        for p, _, _ in processes:
+            if p.random_mesh:
+                raise NotImplementedError("random_mesh draws host random numbers per kick: use track() on the host")
+        first = processes[0][0] if processes else sc
+        self.dev = torch.device(first.device) if first is not None and first.device is not None else torch.device(
             "cuda", torch.cuda.current_device())
         if isinstance(p_array, DeviceParticleArray):
             self.beam = p_array
@@ -276,28 +434,55 @@ class DeviceTrack:
         if order not in (1, 2):
             raise ValueError("order must be 1 (TransferMap) or 2 (SecondTM)")
         self.order = order
-        if order == 1:
-            self.steps = step_maps(seq, self.E, unit_step, int(sc.step))
-            table = np.zeros((len(self.steps), 42))
-            for k, (R, B, _, _) in enumerate(self.steps):
+        lengths = _line_lengths(seq)
+        self.composed = order == 1 and whole and not any(is_cavity(e) for e in seq)
+        self.engines, eng_of = [], []
+        from .sc import Engine, plan_mode
+        keys = {}
+        for p, _, _ in processes:
+            key = (tuple(int(v) for v in p.nmesh_xyz), p.precision, plan_mode(p.precision, p.deposit, p.igf))
+            if key not in keys:
+                keys[key] = len(self.engines)
+                self.engines.append(Engine(key[0], key[1], self.dev, key[2]))
+            eng_of.append(keys[key])
+        self.engine = self.engines[0]
+        for eng in self.engines:
+            eng.ensure(self.n)
+        if self.composed:
+            self.steps = []
+            maps = step_maps(seq, self.E, unit_step, int(processes[0][0].step))
+            table = np.zeros((len(maps), 42))
+            for k, (R, B, zstep, z0) in enumerate(maps):
                 table[k, :36] = R.reshape(-1)
                 table[k, 36:] = B
+                self.steps.append((((0, self.E, zstep),), z0))
+            self.E_end = self.E
+            self.s_end = float(self.beam.s)
+            for slices, _, _ in kick_schedule(lengths, unit_step, int(processes[0][0].step)):
+                for _, dl in slices:
+                    self.s_end += dl
         else:
-            # the slice maps of all steps, and where each step's maps begin
-            steps2 = step_maps2(seq, self.E, unit_step, int(sc.step))
-            self.steps = [(None, None, zstep, z0) for _, zstep, z0 in steps2]
-            table = np.concatenate([m for m, _, _ in steps2]) if steps2 else np.zeros((0, 1))
-            first = np.cumsum([0] + [m.shape[0] for m, _, _ in steps2]).astype(np.int32)
+            sched = navigator_steps(lengths, [(a, b, p.step) for p, a, b in processes], unit_step)
+            slices, self.E_end, self.s_end = step_slices(seq, self.E, sched, order, float(self.beam.s))
+            self.steps = [(tuple((eng_of[j], float(E), float(zstep)) for j, E, zstep in kicks), z0)
+                          for _, _, kicks, z0 in slices]
+            table = np.concatenate([t for t, _, _, _ in slices]) if slices else np.zeros((0, 1))
+            if table.shape[0] == 0:
+                table = np.zeros((1, 168))
+            kinds = np.concatenate([k for _, k, _, _ in slices]) if slices else np.zeros(0, np.int32)
+            first = np.cumsum([0] + [t.shape[0] for t, _, _, _ in slices]).astype(np.int32)
             self.first = torch.from_numpy(first).to(self.dev)
+            self.kinds = torch.from_numpy(np.ascontiguousarray(np.append(kinds, 0).astype(np.int32))).to(self.dev)
         self.table = torch.from_numpy(np.ascontiguousarray(table)).to(self.dev)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        self.engine = Engine(tuple(int(v) for v in sc.nmesh_xyz), sc.precision, self.dev,
-                             plan_mode(sc.precision, sc.deposit, sc.igf))
-        self.engine.ensure(self.n)
         self.stream = stream if stream is not None else torch.cuda.Stream(self.dev)
         self.next = 0
         self.use_graph = bool(graph)
         self._graphs = {}
+        # a graph pays when its step repeats (the composed line: every step)
+        self._repeats = {}
+        for key, _ in self.steps:
+            self._repeats[key] = self._repeats.get(key, 0) + 1
         self.done = torch.cuda.Event()
         with torch.cuda.device(self.dev):
             self.stream.wait_stream(torch.cuda.current_stream(self.dev))
@@ -310,31 +495,32 @@ class DeviceTrack:
     def finished(self) -> bool:
         return self.next >= len(self.steps)
 
-    def _launch(self, zstep: float):
+    def _launch(self, kicks):
         import torch
         rp, q = self.beam.rparticles, self.beam.q_array
         lib = self.engine.lib
         s = C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
-        if self.order == 1:
+        if self.composed:
             N.check(lib.sc_tmap_apply_indexed(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.counter.data_ptr()),
                                               len(self.steps), C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
         else:
-            N.check(lib.sc_tmap2_apply_step(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.first.data_ptr()),
-                                            C.c_void_p(self.counter.data_ptr()), len(self.steps),
-                                            C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
-        self.engine.kick(rp, q, self.n, self.E, zstep)
+            N.check(lib.sc_slices_apply_step(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.kinds.data_ptr()),
+                                             C.c_void_p(self.first.data_ptr()), C.c_void_p(self.counter.data_ptr()),
+                                             len(self.steps), C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
+        for eng, E, zstep in kicks:
+            self.engines[eng].kick(rp, q, self.n, E, zstep)
 
-    def _graph(self, zstep: float):
+    def _graph(self, kicks):
         import torch
-        g = self._graphs.get(zstep)
+        g = self._graphs.get(kicks)
         if g is None:
             g = torch.cuda.CUDAGraph()
             with torch.cuda.device(self.dev):
                 self.stream.synchronize()
                 # recording does not execute: counter and particles are untouched
                 with torch.cuda.graph(g, stream=self.stream):
-                    self._launch(zstep)
-            self._graphs[zstep] = g
+                    self._launch(kicks)
+            self._graphs[kicks] = g
         return g
 
     def step(self, count: int = 1) -> int:
@@ -344,11 +530,11 @@ class DeviceTrack:
         k = 0
         with torch.cuda.device(self.dev), torch.cuda.stream(self.stream):
             while k < count and self.next < len(self.steps):
-                zstep = self.steps[self.next][2]
-                if self.use_graph:
-                    self._graph(zstep).replay()
+                kicks = self.steps[self.next][0]
+                if self.use_graph and self._repeats[kicks] > 1:
+                    self._graph(kicks).replay()
                 else:
-                    self._launch(zstep)
+                    self._launch(kicks)
                 self.next += 1
                 k += 1
             if self.next >= len(self.steps) and k:
@@ -364,46 +550,64 @@ class DeviceTrack:
         import torch
         self.stream.synchronize()
         with torch.cuda.device(self.dev), torch.cuda.stream(self.stream):
-            self.engine.check_status()
-            first = int(self.engine.region("first_error").item())
-        if first:
-            raise ValueError(f"[sc error {first}] {N.ERROR_TEXT.get(first, 'device error')} (in an earlier step)")
+            for eng in self.engines:
+                eng.check_status()
+                first = int(eng.region("first_error").item())
+                if first:
+                    raise ValueError(f"[sc error {first}] {N.ERROR_TEXT.get(first, 'device error')} "
+                                     "(in an earlier step)")
 
     def result(self, p_array=None):
         self.synchronize()
-        self.beam.s = self.steps[-1][3] if self.steps else self.beam.s
+        self.beam.s = self.s_end
+        self.beam.E = self.E_end
         return self.beam.to_host(p_array)
+
+
+def _navigator_processes(navi, lattice):
+    """[(process, indx0, indx1)] of a Navigator-like object, in the order the
+    processes were added (its process table; a process without the indices
+    add_physics_proc sets spans the lattice)."""
+    from .sc import SpaceCharge
+    procs = []
+    for table in ("process_table", "ref_process_table"):
+        for p in (getattr(getattr(navi, table, None), "proc_list", None) or []):
+            if not any(p is q for q in procs):
+                procs.append(p)
+    if not procs:
+        raise NotImplementedError("device tracking needs at least one ocelot_gb300 SpaceCharge process")
+    seq = _lattice_sequence(lattice)
+    out = []
+    for p in procs:
+        if not isinstance(p, SpaceCharge):
+            raise NotImplementedError(f"{type(p).__name__}: device tracking runs ocelot_gb300 SpaceCharge processes only")
+        i0, i1 = getattr(p, "indx0", None), getattr(p, "indx1", None)
+        out.append((p, 0 if i0 is None else int(i0), len(seq) - 1 if i1 is None else int(i1)))
+    return out
 
 
 def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = True, order=None):
     """Device counterpart of the reference's ``track(lat, p_array, navi)``
     for a space-charge transport line: the particles go to the GPU once, all
-    steps run there, and ``p_array`` is updated in place at the end.
+    steps run there, and ``p_array`` is updated in place at the end (its
+    energy and position included).
 
-    Either pass a Navigator-like ``navi`` (``unit_step`` and one SpaceCharge
-    process in ``navi.process_table.proc_list``) or ``sc`` and ``unit_step``.
-    ``order``: 1 (first-order maps, TransferMap) or 2 (SecondTM); by default
-    the lattice's own ``method`` decides.
+    Either pass a Navigator-like ``navi`` (``unit_step`` and its SpaceCharge
+    processes in ``navi.process_table.proc_list``, with the element ranges
+    add_physics_proc gave them) or ``sc`` and ``unit_step`` (one process over
+    the whole lattice).  ``order``: 1 (first-order maps, TransferMap) or 2
+    (SecondTM); by default the lattice's own ``method`` decides.  Cavities are
+    tracked with their own map (CavityTM) in either case, as in the reference.
     Returns (tws, p_array) like the reference, with an empty twiss list.
     """
+    processes = None
     if navi is not None:
-        procs = []
-        for table in ("process_table", "ref_process_table"):
-            procs += [p for p in (getattr(getattr(navi, table, None), "proc_list", None) or []) if p not in procs]
         if sc is None:
-            from .sc import SpaceCharge
-            found = [p for p in procs if isinstance(p, SpaceCharge)]
-            if len(found) != 1:
-                raise NotImplementedError("device tracking takes exactly one ocelot_gb300 SpaceCharge process")
-            sc = found[0]
-            seq = _lattice_sequence(lattice)
-            i0, i1 = getattr(sc, "indx0", None), getattr(sc, "indx1", None)
-            if (i0 is not None and i0 != 0) or (i1 is not None and i1 != len(seq) - 1):
-                raise NotImplementedError("device tracking needs the SpaceCharge process on the whole lattice")
+            processes = _navigator_processes(navi, lattice)
         unit_step = navi.unit_step if unit_step is None else unit_step
-    if sc is None or unit_step is None:
+    if (sc is None and processes is None) or unit_step is None:
         raise ValueError("pass navi, or sc and unit_step")
     order = lattice_order(lattice) if order is None else int(order)
-    job = DeviceTrack(lattice, sc, unit_step, p_array, graph=graph, order=order).run()
+    job = DeviceTrack(lattice, sc, unit_step, p_array, graph=graph, order=order, processes=processes).run()
     job.result(p_array)
     return [], p_array

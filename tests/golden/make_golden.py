@@ -26,6 +26,13 @@ What it writes (all under tests/golden/):
   ``track()`` through FODO cells with SecondTM and SpaceCharge.
 * ``ref_io.npz``, ``ref_beam.ast``, ``ref_beam.fmt1`` -- a seeded beam saved
   and loaded by the reference's ASTRA and CSRtrack adaptors.
+* ``ref_cavity.npz`` -- sections of RF cavities (CavityTM, coupler kicks,
+  tilt) applied by the reference to a seeded beam, with the energy before and
+  after (elements/cavity_atom.py, transformations/cavity.py).
+* ``ref_track_line.npz`` -- the reference's ``track()`` of the
+  ``test_track_with_sp`` scenario (16 cavities, SecondTM, two SpaceCharge
+  processes): its start beam, every kick's position, length, energy and
+  process step, and the beam at the end.
 * ``track_pin.json`` -- the pin of the oracle against the reference's golden
   vectors: the same scenario tracked by the reference's ``track()`` with the
   kick replaced by ``oracle.sc_oracle.sc_apply``, compared particle by
@@ -407,6 +414,94 @@ def run_io(ref_root: str, n=64):
     print(f"wrote {path}, {ast}, {fmt1}")
 
 
+CAVITY_CASES = [
+    # (l, v, phi, freq, couplers (vx_up, vy_up, vxx_up, vxy_up, vx_down, vy_down, vxx_down, vxy_down), tilt, E)
+    (1.0377, 18.50662e-3 / np.cos(18.7268 * np.pi / 180.0), 18.7268, 1.3e9, (0,) * 8, 0.0, 0.0065),
+    (0.346, -20.2E-3 / 8.0 / np.cos(np.pi), 180.0, 3.9e9, (0,) * 8, 0.0, 0.13),
+    (1.0377, 1e-3, 90.0, 1.3e9, (0,) * 8, 0.0, 0.05),
+    (0.8, 0.0, 10.0, 1.3e9, (0,) * 8, 0.0, 0.02),
+    (1.0377, 0.02, -30.0, 1.3e9, (1e-3 + 2e-3j, -5e-4 + 1e-4j, 2e-3 - 1e-3j, 1e-3 + 3e-3j,
+                                   -1e-3 + 5e-4j, 3e-4 - 2e-4j, -2e-3 + 1e-3j, 5e-4 - 1e-3j), 0.05, 0.01),
+]
+# (start in the element, length) of the sections taken through each cavity
+CAVITY_SECTIONS = [(0.0, 0.02), (0.0, None), (0.3, 0.02), (None, 0.02), (0.5, 0.1)]
+
+
+def run_cavity(ref_root: str, n=64):
+    """Sections of RF cavities (CavityTM with its coupler kicks) applied by
+    the reference to a seeded beam: the maps OpticElement.get_section_tms
+    builds, each applied by Transformation.apply (which also raises p_array.E)."""
+    import_reference(ref_root)
+    from ocelot import Cavity, ParticleArray
+    rng = np.random.default_rng(21)
+    data = {"n_cases": len(CAVITY_CASES), "n_sections": len(CAVITY_SECTIONS)}
+    for c, (l, v, phi, freq, cp, tilt, E) in enumerate(CAVITY_CASES):
+        cav = Cavity(l=l, v=v, phi=phi, freq=freq, vx_up=cp[0], vy_up=cp[1], vxx_up=cp[2], vxy_up=cp[3],
+                     vx_down=cp[4], vy_down=cp[5], vxx_down=cp[6], vxy_down=cp[7], eid=f"C{c}")
+        cav.tilt = tilt
+        data[f"c{c}_params"] = np.array([l, v, phi, freq, tilt, E])
+        data[f"c{c}_couplers"] = np.array(cp, dtype=np.complex128)
+        for k, (start, dl) in enumerate(CAVITY_SECTIONS):
+            start = l - dl if start is None else start
+            dl = l if dl is None else dl
+            X = np.stack([rng.normal(0, 1e-3, n), rng.normal(0, 1e-4, n), rng.normal(0, 1e-3, n),
+                          rng.normal(0, 1e-4, n), rng.normal(0, 1e-3, n), rng.normal(0, 1e-2, n)])
+            pa = ParticleArray(n=n)
+            pa.E = E
+            pa.rparticles[:] = X
+            for tm in cav.get_section_tms(start_l=start, delta_l=dl):
+                tm.apply(pa)
+            data[f"c{c}_s{k}_section"] = np.array([start, dl])
+            data[f"c{c}_s{k}_in"] = X
+            data[f"c{c}_s{k}_out"] = pa.rparticles.copy()
+            data[f"c{c}_s{k}_E"] = np.array([E, pa.E])
+    path = os.path.join(HERE, "ref_cavity.npz")
+    np.savez_compressed(path, **data)
+    print(f"wrote {path} ({os.path.getsize(path) / 1e6:.3f} MB)")
+
+
+def run_track_line(ref_root: str):
+    """The reference's test_track_with_sp scenario (16 cavities, SecondTM,
+    two SpaceCharge processes of step 1 and 5) tracked by the reference's own
+    track(): the beam it starts from, every kick's position, length, energy
+    and process, and the particles and energy at the end."""
+    import_reference(ref_root)
+    from ocelot.cpbd.sc import SpaceCharge
+    lattice, p0, conf = build_track_scenario(ref_root)
+    start = p0.rparticles.copy()
+    rec = []
+    base_apply = SpaceCharge.apply
+
+    def recording_apply(self, p_array, zstep):
+        rec.append((self.step, self.z0, zstep, p_array.E))
+        base_apply(self, p_array, zstep)
+
+    def make_ref(step):
+        sc = SpaceCharge(step=step)
+        sc.nmesh_xyz = [63, 63, 63]
+        return sc
+
+    SpaceCharge.apply = recording_apply
+    try:
+        p = track_scenario(ref_root, make_ref)
+    finally:
+        SpaceCharge.apply = base_apply
+    seq = lattice.sequence
+    data = dict(rp_start=start, q=p0.q_array.copy(), E_start=np.array(0.0065), rp_end=p.rparticles.copy(),
+                E_end=np.array(p.E), s_end=np.array(p.s),
+                kick_step=np.array([r[0] for r in rec], dtype=np.int32), kick_z0=np.array([r[1] for r in rec]),
+                kick_zstep=np.array([r[2] for r in rec]), kick_E=np.array([r[3] for r in rec]),
+                lengths=np.array([e.l for e in seq]),
+                # per element: kind (0 drift/marker, 1 quadrupole, 2 cavity), l, k1, v, phi, freq
+                elements=np.array([[2 if type(e).__name__ == "Cavity" else 1 if type(e).__name__ == "Quadrupole" else 0,
+                                    e.l, getattr(e, "k1", 0.0), getattr(e, "v", 0.0), getattr(e, "phi", 0.0),
+                                    getattr(e, "freq", 0.0)] for e in seq]),
+                indx=np.array([seq.index(conf.C_A1_1_2_I1), len(seq) - 1], dtype=np.int32))
+    path = os.path.join(HERE, "ref_track_line.npz")
+    np.savez_compressed(path, **data)
+    print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB), {len(rec)} kicks")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -414,7 +509,12 @@ if __name__ == "__main__":
     ap.add_argument("--only-track", action="store_true")
     ap.add_argument("--only-matrices", action="store_true")
     ap.add_argument("--only-second-order-io", action="store_true")
+    ap.add_argument("--only-cavity", action="store_true")
     a = ap.parse_args()
+    if a.only_cavity:
+        run_cavity(a.reference)
+        run_track_line(a.reference)
+        sys.exit(0)
     if a.only_second_order_io:
         run_second_order(a.reference)
         run_io(a.reference)
@@ -430,5 +530,7 @@ if __name__ == "__main__":
         run_fodo(a.reference)
         run_second_order(a.reference)
         run_io(a.reference)
+        run_cavity(a.reference)
     if not a.skip_track:
         run_track(a.reference)
+        run_track_line(a.reference)

@@ -1,0 +1,132 @@
+"""RF cavity sections and the Navigator's schedule with several processes, on
+the host, against the reference's own outputs (tests/golden/ref_cavity.npz,
+ref_track_line.npz; tests/golden/make_golden.py wrote them)."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from ocelot_gb300 import cavity as CV
+from ocelot_gb300 import track as T
+
+CAV = dict(np.load(os.path.join(GOLDEN, "ref_cavity.npz")))
+LINE = dict(np.load(os.path.join(GOLDEN, "ref_track_line.npz")))
+
+
+def cavity_case(c):
+    l, v, phi, freq, tilt, E = (float(x) for x in CAV[f"c{c}_params"])
+    cp = [complex(x) for x in CAV[f"c{c}_couplers"]]
+    cav = CV.Cavity(l=l, v=v, phi=phi, freq=freq, vx_up=cp[0], vy_up=cp[1], vxx_up=cp[2], vxy_up=cp[3],
+                    vx_down=cp[4], vy_down=cp[5], vxx_down=cp[6], vxy_down=cp[7], tilt=tilt)
+    return cav, E
+
+
+def sections():
+    return [(c, k) for c in range(int(CAV["n_cases"])) for k in range(int(CAV["n_sections"]))]
+
+
+def close_rows(a, b, rtol):
+    """max |a - b| per row within rtol of the row's largest |b|."""
+    return all(np.abs(a[r] - b[r]).max() <= rtol * np.abs(b[r]).max() for r in range(6))
+
+
+def line_elements():
+    seq = []
+    for kind, l, k1, v, phi, freq in LINE["elements"]:
+        if kind == 2:
+            seq.append(CV.Cavity(l=l, v=v, phi=phi, freq=freq))
+        elif kind == 1:
+            seq.append(T.Quadrupole(l=l, k1=k1))
+        elif l == 0:
+            seq.append(T.Marker())
+        else:
+            seq.append(T.Drift(l=l))
+    return seq
+
+
+def line_procs():
+    i4, i20 = (int(v) for v in LINE["indx"])
+    return [(0, i4, 1), (i4, i20, 5)]
+
+
+@pytest.mark.parametrize("c,k", sections())
+def test_cavity_section_records_match_reference(c, k):
+    cav, E = cavity_case(c)
+    start, dl = (float(v) for v in CAV[f"c{c}_s{k}_section"])
+    recs, kinds, E1 = CV.section_records(cav, start, dl, E)
+    assert E1 == CAV[f"c{c}_s{k}_E"][1]          # the energy gain, bit for bit
+    out = CV.apply_records_numpy(recs, kinds, CAV[f"c{c}_s{k}_in"])
+    assert close_rows(out, CAV[f"c{c}_s{k}_out"], 1e-13)
+
+
+def test_cavity_sections_cover_the_branches():
+    # accelerating, decelerating (180 deg), zero-crossing (90 deg: the T556/T555 limits), v = 0 (drift
+    # matrix), couplers + tilt
+    kinds_seen = set()
+    for c in range(int(CAV["n_cases"])):
+        cav, E = cavity_case(c)
+        recs, kinds, _ = CV.section_records(cav, 0.0, cav.l, E)
+        kinds_seen.add(tuple(kinds))
+        rec = recs[kinds.index(CV.SLICE_CAVITY)]
+        if c == 2:
+            assert rec[CV.CAV_T556] != 0.0 and rec[CV.CAV_T555] != 0.0
+        if c == 3:
+            assert rec[CV.CAV_T556] == 0.0 and rec[CV.CAV_T555] == 0.0
+    assert (CV.SLICE_MAP, CV.SLICE_CAVITY, CV.SLICE_MAP) in kinds_seen    # coupler kicks kept
+    assert (CV.SLICE_CAVITY,) in kinds_seen                              # identity edges left out
+
+
+def test_section_tms_edges_follow_reference_convention():
+    cav = CV.Cavity(l=1.0, v=0.01, phi=10.0, freq=1.3e9)
+    assert CV.section_tms(cav, 0.0, 1.0, True) == [("entrance", None), ("main", None), ("exit", None)]
+    assert CV.section_tms(cav, 0.0, 0.2, True) == [("entrance", None), ("main", 0.2)]
+    assert CV.section_tms(cav, 0.4, 0.2, True) == [("main", 0.2)]
+    assert CV.section_tms(cav, 0.9, 0.2, True) == [("main", 1.0 - 0.9), ("exit", None)]
+
+
+def test_navigator_steps_one_process_equals_kick_schedule():
+    seq = []
+    for _ in range(3):
+        seq += [T.Quadrupole(l=0.2, k1=1.2), T.Drift(l=1.0), T.Quadrupole(l=0.2, k1=-1.2), T.Drift(l=1.0)]
+    seq.append(T.Marker())
+    lengths = [e.l for e in seq]
+    for unit_step, step in ((0.25, 1), (0.1, 3), (0.07, 2)):
+        a = T.kick_schedule(lengths, unit_step, step)
+        b = T.navigator_steps(lengths, [(0, len(seq) - 1, step)], unit_step)
+        assert len(a) == len(b)
+        for (sl_a, zstep, z0a), (sec_b, kicks, z0b) in zip(a, b):
+            assert z0a == z0b and kicks == [(0, zstep)]
+            assert sl_a == [(i, T._section_length(lengths[i], s, d)) for i, s, d in sec_b]
+
+
+def test_line_schedule_and_energies_are_the_reference_navigators():
+    """test_track_with_sp's line: 16 cavities, SpaceCharge with step 1 up to
+    the second cavity and step 5 after it -- every kick's position, length,
+    energy and process equal to the reference's, bit for bit."""
+    seq = line_elements()
+    procs = line_procs()
+    steps = T.navigator_steps([e.l for e in seq], procs, 0.02)
+    slices, E_end, s_end = T.step_slices(seq, float(LINE["E_start"]), steps, order=2)
+    kicks = [(procs[j][2], z0, zstep, E) for (_, _, ks, z0) in slices for j, E, zstep in ks]
+    assert len(kicks) == len(LINE["kick_step"]) == 193
+    assert [k[0] for k in kicks] == list(LINE["kick_step"])
+    assert np.array_equal([k[1] for k in kicks], LINE["kick_z0"])
+    assert np.array_equal([k[2] for k in kicks], LINE["kick_zstep"])
+    assert np.array_equal([k[3] for k in kicks], LINE["kick_E"])
+    assert E_end == LINE["E_end"]
+    assert s_end == LINE["s_end"]                   # p_array.s as Transformation.apply moves it
+    assert len(slices[-1][2]) == 0                  # the last quadrupole: transport only, no process
+
+
+def test_navigator_steps_reject_kick_processes_and_bad_ranges():
+    with pytest.raises(NotImplementedError):
+        T.navigator_steps([1.0, 1.0, 1.0], [(1, 1, 1)], 0.1)
+    with pytest.raises(NotImplementedError):
+        T.navigator_steps([0.0, 1.0, 1.0], [(0, 1, 1)], 0.1)
+    with pytest.raises(ValueError):
+        T.navigator_steps([1.0, 1.0], [(0, 5, 1)], 0.1)
+    with pytest.raises(ValueError):
+        T.navigator_steps([], [(0, 0, 1)], 0.1)

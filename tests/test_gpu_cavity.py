@@ -1,0 +1,128 @@
+"""RF cavities on the device: the cavity slice records through
+``sc_slices_apply`` against the reference's sections, and the reference's
+space-charge regression line (test_track_with_sp: 16 cavities, SecondTM, two
+SpaceCharge processes) tracked end to end on the GPU against the reference's
+own track() of it (tests/golden/ref_track_line.npz)."""
+from __future__ import annotations
+
+import ctypes as C
+import types
+
+import numpy as np
+import pytest
+
+from conftest import has_gpu
+from test_cavity_host import CAV, LINE, cavity_case, close_rows, line_elements, line_procs, sections
+
+pytestmark = pytest.mark.gpu
+if not has_gpu():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+import torch  # noqa: E402
+
+from ocelot_gb300 import ParticleArray, SpaceCharge  # noqa: E402
+from ocelot_gb300 import _native as N  # noqa: E402
+from ocelot_gb300 import cavity as CV  # noqa: E402
+from ocelot_gb300 import track as T  # noqa: E402
+
+# the reference test's own tolerance on the particles (space_charge_test.py:65)
+TOL_ABS = 1e-12
+
+
+def slices_apply(recs, kinds, X):
+    dev = torch.device("cuda", 0)
+    rp = torch.from_numpy(np.ascontiguousarray(X)).to(dev)
+    maps = torch.from_numpy(np.ascontiguousarray(recs)).to(dev)
+    kd = torch.tensor(list(kinds), dtype=torch.int32, device=dev)
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    N.check(N.lib().sc_slices_apply(C.c_void_p(maps.data_ptr()), C.c_void_p(kd.data_ptr()), len(kinds),
+                                    C.c_void_p(rp.data_ptr()), rp.stride(0), rp.shape[1], s))
+    torch.cuda.synchronize()
+    return rp.cpu().numpy()
+
+
+@pytest.mark.parametrize("c,k", sections())
+def test_cavity_sections_on_device_match_reference(c, k):
+    cav, E = cavity_case(c)
+    start, dl = (float(v) for v in CAV[f"c{c}_s{k}_section"])
+    recs, kinds, _ = CV.section_records(cav, start, dl, E)
+    out = slices_apply(recs, kinds, CAV[f"c{c}_s{k}_in"])
+    assert close_rows(out, CAV[f"c{c}_s{k}_out"], 1e-13)
+
+
+def test_cavity_record_without_positive_final_energy():
+    # the branch where the energy after the slice is not positive: only the T566 term, x5 from R.x + B
+    rng = np.random.default_rng(3)
+    rec = np.zeros(CV.MAP2_DOUBLES)
+    rec[:36] = (np.eye(6) + 1e-3 * rng.standard_normal((6, 6))).reshape(-1)
+    rec[36:42] = 1e-6 * rng.standard_normal(6)
+    rec[CV.CAV_T566] = 0.7
+    X = 1e-3 * rng.standard_normal((6, 257))
+    out = slices_apply(rec[None, :], [CV.SLICE_CAVITY], X)
+    ref = CV.apply_records_numpy(rec[None, :], [CV.SLICE_CAVITY], X)
+    assert close_rows(out, ref, 1e-14)
+
+
+def _line_job(precision="fp64", graph=True):
+    pa = ParticleArray(LINE["rp_start"].shape[1])
+    pa.rparticles[:] = LINE["rp_start"]
+    pa.q_array = LINE["q"].copy()
+    pa.E = float(LINE["E_start"])
+    procs = [(SpaceCharge(step=st, nmesh_xyz=[63, 63, 63], precision=precision), a, b) for a, b, st in line_procs()]
+    job = T.DeviceTrack(line_elements(), None, 0.02, pa, graph=graph, order=2, processes=procs)
+    return job, pa
+
+
+def test_line_fp64_matches_reference_track():
+    job, pa = _line_job("fp64", graph=False)
+    assert job.nsteps == 194 and sum(len(k) for k, _ in job.steps) == 193
+    assert len(job.engines) == 1          # both processes share one plan (same mesh and form)
+    job.run()
+    job.result(pa)
+    assert pa.E == LINE["E_end"] and pa.s == LINE["s_end"]
+    err = np.abs(pa.rparticles - LINE["rp_end"]).max(axis=1)
+    assert (err <= TOL_ABS).all(), err
+
+
+def test_line_graph_replay_equals_eager():
+    job, pa = _line_job("fp64", graph=True)
+    job.run()
+    out = job.result().rparticles
+    assert 0 < len(job._graphs) < job.nsteps
+    job2, _ = _line_job("fp64", graph=False)
+    job2.run()
+    assert np.array_equal(out, job2.result().rparticles)
+
+
+def test_line_through_navigator_like_object():
+    seq = line_elements()
+    procs = []
+    for a, b, st in line_procs():
+        sc = SpaceCharge(step=st, nmesh_xyz=[63, 63, 63])
+        sc.indx0, sc.indx1 = a, b
+        procs.append(sc)
+    navi = types.SimpleNamespace(unit_step=0.02, process_table=types.SimpleNamespace(proc_list=procs))
+    pa = ParticleArray(LINE["rp_start"].shape[1])
+    pa.rparticles[:] = LINE["rp_start"]
+    pa.q_array = LINE["q"].copy()
+    pa.E = float(LINE["E_start"])
+    tws, p = T.track(seq, pa, navi, order=2)
+    assert p is pa and tws == []
+    assert (np.abs(pa.rparticles - LINE["rp_end"]).max(axis=1) <= TOL_ABS).all()
+
+
+def test_line_fp32_space_charge_part():
+    job64, _ = _line_job("fp64")
+    out64 = job64.run().result().rparticles
+    job32, _ = _line_job("fp32")
+    out32 = job32.run().result().rparticles
+    # the transport alone, from the same records on the host
+    lin = LINE["rp_start"].copy()
+    seq = line_elements()
+    steps = T.navigator_steps([e.l for e in seq], line_procs(), 0.02)
+    for recs, kinds, _, _ in T.step_slices(seq, float(LINE["E_start"]), steps, order=2)[0]:
+        lin = CV.apply_records_numpy(recs, kinds, lin)
+    for r in (0, 1, 2, 3, 5):
+        sc64, sc32 = out64[r] - lin[r], out32[r] - lin[r]
+        err = np.sqrt(np.mean((sc32 - sc64) ** 2)) / np.sqrt(np.mean(sc64 ** 2))
+        assert err < 1e-4, (r, err)
