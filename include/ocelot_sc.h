@@ -269,6 +269,21 @@ int sc_slices_apply(const double* maps, const int* kinds, int nmaps, double* rpa
 int sc_slices_apply_step(const double* maps, const int* kinds, const int* first, int* counter, int nsteps,
                          double* rparticles, int64_t ld, int64_t n, void* stream);
 
+/* Beam moments after a tracking step: get_envelope (ocelot/cpbd/beam/analysis.py:27-226) without dispersion
+ * correction, the statistics track() takes after every step (ocelot/cpbd/track.py:466-486).  Writes slot
+ * s = *counter (counter NULL: slot 0; out of [0, nslots): nothing) of a DEVICE table out[nslots][SC_MOMENTS]:
+ *   [0] particles counted, [1] mean and [2] standard deviation of tau over all particles (only with bounds),
+ *   [3..8] means of x, y, px', py', tau, p, [9..20] central moments xx, xpx, pxpx, yy, ypy, pypy, tautau,
+ *   xy, pxpy, xpy, ypx, pp, with px' = px f, py' = py f, f = 1 - p - p^2/2 + px^2/2 + py^2/2.
+ * use_bounds: only the particles with m + lo s <= tau <= m + hi s count (get_envelope's bounds, in units of
+ * the standard deviation s of tau around its mean m).  Two launches (four with bounds); the sums are
+ * deterministic.  scratch: DEVICE, sc_moments_scratch_bytes() bytes, zero-filled once before the first call,
+ * not shared by concurrent calls. */
+#define SC_MOMENTS 21
+int64_t sc_moments_scratch_bytes(void);
+int sc_moments(const double* rparticles, int64_t ld, int64_t n, const int* counter, int nslots, int use_bounds,
+               double lo, double hi, double* out, void* scratch, void* stream);
+
 /* ---- stage timing (benchmarking) --------------------------------------- */
 
 /* Stages of sc_kick: MAD->lab frame (coord_transform.py:57-96,

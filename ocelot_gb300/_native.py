@@ -68,6 +68,8 @@ SIGNATURES = {
     "sc_tmap2_apply": (C.c_int, [vp, C.c_int, vp, i64, i64, vp]),
     "sc_tmap2_apply_step": (C.c_int, [vp, vp, vp, C.c_int, vp, i64, i64, vp]),
     "sc_slices_apply": (C.c_int, [vp, vp, C.c_int, vp, i64, i64, vp]),
+    "sc_moments_scratch_bytes": (i64, []),
+    "sc_moments": (C.c_int, [vp, i64, i64, vp, C.c_int, C.c_int, dbl, dbl, vp, vp, vp]),
     "sc_slices_apply_step": (C.c_int, [vp, vp, vp, vp, C.c_int, vp, i64, i64, vp]),
     "sc_batch_create": (C.c_int, [C.POINTER(vp), C.c_int]),
     "sc_batch_destroy": (None, [vp]),

@@ -863,6 +863,20 @@ int sc_tmap2_apply_step(const double* maps, const int* first, int* counter, int 
     return SC_OK;
 }
 
+int64_t sc_moments_scratch_bytes(void) { return (int64_t)moments_scratch_bytes(); }
+
+int sc_moments(const double* rp, int64_t ld, int64_t n, const int* counter, int nslots, int use_bounds, double lo,
+               double hi, double* out, void* scratch, void* stream) {
+    if (!out || !scratch) return fail(SC_ERR_ARG, "out or scratch is NULL");
+    if (n < 1 || nslots < 1) return fail(SC_ERR_ARG, "n < 1 or nslots < 1");
+    if (!rp) return fail(SC_ERR_ARG, "rparticles is NULL");
+    if (ld < n) return fail(SC_ERR_ARG, "row stride ld=%lld < n=%lld", (long long)ld, (long long)n);
+    if (use_bounds && !(lo <= hi)) return fail(SC_ERR_ARG, "bounds: lo must be <= hi");
+    SC_CUDA(launch_moments(rp, ld, n, counter, nslots, use_bounds ? 1 : 0, lo, hi, out, scratch,
+                           (cudaStream_t)stream), "moments");
+    return SC_OK;
+}
+
 int sc_slices_apply(const double* maps, const int* kinds, int nmaps, double* rp, int64_t ld, int64_t n,
                     void* stream) {
     if (nmaps < 0 || n < 0) return fail(SC_ERR_ARG, "nmaps < 0 or n < 0");

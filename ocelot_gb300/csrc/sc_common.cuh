@@ -224,6 +224,9 @@ cudaError_t launch_tmap2(const double* maps, const int* kinds, int nmaps, double
                          cudaStream_t s);
 cudaError_t launch_tmap2_step(const double* maps, const int* kinds, const int* first, int* counter, int nsteps,
                               double* rp, int64_t ld, int64_t n, cudaStream_t s);
+cudaError_t launch_moments(const double* rp, int64_t ld, int64_t n, const int* counter, int nslots, int use_bounds,
+                           double lo, double hi, double* out, void* scratch, cudaStream_t s);
+size_t moments_scratch_bytes();
 cudaError_t launch_tmap_indexed(const double* table, int* counter, int nmaps, double* rp, int64_t ld,
                                 int64_t n, cudaStream_t s);
 

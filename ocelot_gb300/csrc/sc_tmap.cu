@@ -243,3 +243,138 @@ cudaError_t launch_tmap2_step(const double* maps, const int* kinds, const int* f
 }
 
 }  // namespace ocsc
+
+namespace ocsc {
+
+// ---------------------------------------------------------------------------
+// Beam moments of get_envelope (ocelot/cpbd/beam/analysis.py:27-226) without
+// dispersion correction: the means of x, y, px', py', tau, p and the twelve
+// central second moments, with px' = px f, py' = py f,
+// f = 1 - p - p^2/2 + px^2/2 + py^2/2, over all particles or over those with
+// tau within [m + lo s, m + hi s] (m, s: mean and standard deviation of tau).
+// Two passes over the rows (four with bounds), each one launch: every block
+// reduces its grid-stride share, writes its partial sums, and the last block
+// to finish (a ticket) adds the partials in block order -- so the sums are
+// deterministic -- and writes the slot *counter of the output table.
+// ---------------------------------------------------------------------------
+constexpr int MOM_BLOCKS = 304, MOM_THREADS = 256, MOM_K = 12;
+
+struct MomSlot {
+    double* v;  // SC_MOMENTS doubles
+};
+
+__device__ __forceinline__ double mom_factor(double px, double py, double p) {
+    return __dadd_rn(__dadd_rn(__dsub_rn(__dsub_rn(1.0, p), __dmul_rn(__dmul_rn(0.5, p), p)),
+                               __dmul_rn(__dmul_rn(0.5, px), px)),
+                     __dmul_rn(__dmul_rn(0.5, py), py));
+}
+
+__global__ void __launch_bounds__(MOM_THREADS) k_moments(const double* __restrict__ rp, int64_t ld, int64_t n,
+                                                        const int* __restrict__ counter, int nslots, int pass,
+                                                        int use_bounds, double lo, double hi, double* out,
+                                                        double* __restrict__ partial, unsigned int* ticket) {
+    pdl_wait();
+    const int slot = counter ? *counter : 0;
+    if (slot < 0 || slot >= nslots) return;
+    double* o = out + (size_t)slot * SC_MOMENTS;
+    double acc[MOM_K];
+#pragma unroll
+    for (int k = 0; k < MOM_K; ++k) acc[k] = 0.0;
+    double tlo = -INFINITY, thi = INFINITY;
+    if (pass >= 2 && use_bounds) {
+        tlo = __dadd_rn(o[1], __dmul_rn(o[2], lo));
+        thi = __dadd_rn(o[1], __dmul_rn(o[2], hi));
+    }
+    const double* X = rp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double tau = X[4 * ld + i];
+        if (pass == 0) {
+            acc[0] += tau;
+            continue;
+        }
+        if (pass == 1) {
+            const double d = __dsub_rn(tau, o[1]);
+            acc[0] += __dmul_rn(d, d);
+            continue;
+        }
+        if (!(tlo <= tau && tau <= thi)) continue;
+        const double x = X[i], y = X[2 * ld + i], p = X[5 * ld + i];
+        const double f = mom_factor(X[ld + i], X[3 * ld + i], p);
+        const double px = __dmul_rn(X[ld + i], f), py = __dmul_rn(X[3 * ld + i], f);
+        if (pass == 2) {
+            acc[0] += 1.0;
+            acc[1] += x; acc[2] += y; acc[3] += px; acc[4] += py; acc[5] += tau; acc[6] += p;
+        } else {
+            const double dx = __dsub_rn(x, o[3]), dy = __dsub_rn(y, o[4]), dpx = __dsub_rn(px, o[5]),
+                         dpy = __dsub_rn(py, o[6]), dt = __dsub_rn(tau, o[7]), dp = __dsub_rn(p, o[8]);
+            acc[0] += __dmul_rn(dx, dx);    acc[1] += __dmul_rn(dx, dpx);  acc[2] += __dmul_rn(dpx, dpx);
+            acc[3] += __dmul_rn(dy, dy);    acc[4] += __dmul_rn(dy, dpy);  acc[5] += __dmul_rn(dpy, dpy);
+            acc[6] += __dmul_rn(dt, dt);    acc[7] += __dmul_rn(dx, dy);   acc[8] += __dmul_rn(dpx, dpy);
+            acc[9] += __dmul_rn(dx, dpy);   acc[10] += __dmul_rn(dy, dpx); acc[11] += __dmul_rn(dp, dp);
+        }
+    }
+    const int nk = pass < 2 ? 1 : (pass == 2 ? 7 : MOM_K);
+    __shared__ double s_red[MOM_THREADS / 32][MOM_K];
+    __shared__ bool s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < MOM_K; ++k) {
+        if (k >= nk) break;
+        double v = acc[k];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) s_red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nk) {
+        double v = 0.0;
+        for (int w = 0; w < MOM_THREADS / 32; ++w) v += s_red[w][threadIdx.x];
+        partial[(size_t)blockIdx.x * MOM_K + threadIdx.x] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x < nk) {
+        double v = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) v += __ldcg(partial + (size_t)b * MOM_K + threadIdx.x);
+        if (pass == 0) {
+            o[1] = v / (double)n;
+        } else if (pass == 1) {
+            o[2] = sqrt(v / (double)n);
+        } else if (pass == 2) {
+            o[threadIdx.x == 0 ? 0 : 2 + threadIdx.x] = v;  // count, then the six sums (divided below)
+        } else {
+            o[9 + threadIdx.x] = v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (pass == 2) {
+            const double cnt = o[0];
+            for (int k = 3; k < 9; ++k) o[k] = o[k] / cnt;
+        } else if (pass == 3) {
+            const double cnt = o[0];
+            for (int k = 9; k < 21; ++k) o[k] = o[k] / cnt;
+        }
+        *ticket = 0u;
+    }
+}
+
+cudaError_t launch_moments(const double* rp, int64_t ld, int64_t n, const int* counter, int nslots, int use_bounds,
+                           double lo, double hi, double* out, void* scratch, cudaStream_t s) {
+    double* partial = (double*)scratch;
+    unsigned int* ticket = (unsigned int*)(partial + (size_t)MOM_BLOCKS * MOM_K);
+    int64_t b = (n + MOM_THREADS - 1) / MOM_THREADS;
+    const int blocks = (int)(b < 1 ? 1 : (b > MOM_BLOCKS ? MOM_BLOCKS : b));
+    for (int pass = use_bounds ? 0 : 2; pass < 4; ++pass)
+        launch(k_moments, blocks, MOM_THREADS, 0, s, rp, ld, n, counter, nslots, pass, use_bounds, lo, hi, out,
+               partial, ticket);
+    return cudaGetLastError();
+}
+
+size_t moments_scratch_bytes() { return (size_t)MOM_BLOCKS * MOM_K * sizeof(double) + 64; }
+
+}  // namespace ocsc

@@ -1,0 +1,121 @@
+"""Twiss parameters of a tracked beam from its moments.
+
+The reference's track() calls get_envelope after every step
+(ocelot/cpbd/track.py:466-486, ocelot/cpbd/beam/analysis.py:27-226).  On the
+device the moments are taken by ``sc_moments`` (two passes over the rows of
+rparticles, four with bounds) into a table with one slot per step; this module
+turns a slot into a ``Twiss`` with get_envelope's derived quantities:
+emittances sqrt(<xx><px px> - <x px>^2), normalised by gamma beta of the beam
+energy, beta = <xx>/emit, alpha = -<x px>/emit, and the two eigen-emittances of
+the 4D (x, y, px, py) second-moment matrix Sigma -- the moduli of the
+eigenvalues of Sigma.S, S the symplectic form, which are +-i e1 and +-i e2;
+eigemit_1 is the larger, eigemit_2 the smaller.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .globals import m_e_GeV
+
+MOMENTS = 21  # SC_MOMENTS: count, tau mean/std (bounds), 6 means, 12 central moments
+_MEANS = ("x", "y", "px", "py", "tau", "p")
+_SECOND = ("xx", "xpx", "pxpx", "yy", "ypy", "pypy", "tautau", "xy", "pxpy", "xpy", "ypx", "pp")
+_S4 = np.array([[0, 0, 1, 0], [0, 0, 0, 1], [-1, 0, 0, 0], [0, -1, 0, 0]], dtype=np.float64)
+
+
+class Twiss:
+    """The attributes get_envelope fills in the reference's Twiss
+    (ocelot/cpbd/beam/core.py:16-75); dispersion and phase advance stay 0."""
+
+    def __init__(self):
+        self.E = 0.0
+        self.q = 0.0
+        self.s = 0.0
+        self.emit_x = self.emit_y = self.emit_xn = self.emit_yn = 0.0
+        self.eigemit_1 = self.eigemit_2 = 0.0
+        self.beta_x = self.beta_y = self.alpha_x = self.alpha_y = 0.0
+        self.Dx = self.Dy = self.Dxp = self.Dyp = 0.0
+        self.mux = self.muy = 0.0
+        self.xp = self.yp = 0.0
+        for k in _MEANS + _SECOND:
+            setattr(self, k, 0.0)
+        self.id = ""
+
+    @property
+    def gamma_x(self):
+        return (1 + self.alpha_x ** 2) / self.beta_x if self.beta_x != 0 else 0
+
+    @property
+    def gamma_y(self):
+        return (1 + self.alpha_y ** 2) / self.beta_y if self.beta_y != 0 else 0
+
+    def __repr__(self):
+        return (f"Twiss(s={self.s}, E={self.E}, emit_x={self.emit_x}, emit_y={self.emit_y}, beta_x={self.beta_x}, "
+                f"beta_y={self.beta_y}, alpha_x={self.alpha_x}, alpha_y={self.alpha_y})")
+
+
+def eigen_emittances(tws) -> tuple[float, float]:
+    sigma = np.array([[tws.xx, tws.xy, tws.xpx, tws.xpy],
+                      [tws.xy, tws.yy, tws.ypx, tws.ypy],
+                      [tws.xpx, tws.ypx, tws.pxpx, tws.pxpy],
+                      [tws.xpy, tws.ypy, tws.pxpy, tws.pypy]])
+    if not np.all(np.isfinite(sigma)):
+        return float("nan"), float("nan")
+    w = np.sort(np.abs(np.linalg.eigvals(sigma @ _S4).imag))
+    # w = [e2, e2, e1, e1]
+    return float(0.5 * (w[2] + w[3])), float(0.5 * (w[0] + w[1]))
+
+
+def twiss_from_moments(m, energy: float, charge: float, s: float = 0.0) -> Twiss:
+    """A Twiss from one slot of the sc_moments table (get_envelope's steps
+    after the moments, analysis.py:83-226)."""
+    m = np.asarray(m, dtype=np.float64)
+    tws = Twiss()
+    tws.E = energy
+    tws.q = charge
+    tws.s = s
+    tws.p = float(m[8])
+    if not m[0] >= 3:
+        return tws     # fewer than 3 particles: E, q and p only, as the reference
+    for k, v in zip(_MEANS, m[3:9]):
+        setattr(tws, k, float(v))
+    for k, v in zip(_SECOND, m[9:21]):
+        setattr(tws, k, float(v))
+    tws.emit_x = float(np.sqrt(tws.xx * tws.pxpx - tws.xpx ** 2))
+    tws.emit_y = float(np.sqrt(tws.yy * tws.pypy - tws.ypy ** 2))
+    relgamma = energy / m_e_GeV
+    relbeta = np.sqrt(1 - relgamma ** -2) if relgamma != 0 else 1.
+    tws.emit_xn = float(tws.emit_x * relgamma * relbeta)
+    tws.emit_yn = float(tws.emit_y * relgamma * relbeta)
+    tws.eigemit_1, tws.eigemit_2 = eigen_emittances(tws)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        tws.beta_x = float(np.float64(tws.xx) / tws.emit_x)
+        tws.beta_y = float(np.float64(tws.yy) / tws.emit_y)
+        tws.alpha_x = float(-np.float64(tws.xpx) / tws.emit_x)
+        tws.alpha_y = float(-np.float64(tws.ypy) / tws.emit_y)
+    return tws
+
+
+def moments_numpy(rp: np.ndarray, bounds=None) -> np.ndarray:
+    """One slot of the moments table computed on the host (the same sums as
+    the device passes, in numpy; a check of the device table)."""
+    rp = np.asarray(rp, dtype=np.float64)
+    out = np.zeros(MOMENTS)
+    tau = rp[4]
+    sel = np.ones(rp.shape[1], dtype=bool)
+    if bounds is not None:
+        out[1] = np.mean(tau)
+        out[2] = np.std(tau)
+        sel = (out[1] + out[2] * bounds[0] <= tau) & (tau <= out[1] + out[2] * bounds[1])
+    x, px, y, py, t, p = (rp[r][sel] for r in range(6))
+    f = 1. - p - 0.5 * p * p + 0.5 * px * px + 0.5 * py * py
+    px, py = px * f, py * f
+    out[0] = x.size
+    cols = (x, y, px, py, t, p)
+    means = [np.mean(c) for c in cols]
+    out[3:9] = means
+    d = [c - mu for c, mu in zip(cols, means)]
+    dx, dy, dpx, dpy, dt, dp = d
+    out[9:21] = [np.mean(a * b) for a, b in ((dx, dx), (dx, dpx), (dpx, dpx), (dy, dy), (dy, dpy), (dpy, dpy),
+                                              (dt, dt), (dx, dy), (dpx, dpy), (dx, dpy), (dy, dpx), (dp, dp))]
+    return out

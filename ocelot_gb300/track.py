@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+from typing import NamedTuple
 
 import numpy as np
 
@@ -161,9 +162,9 @@ def kick_schedule(lengths, unit_step: float, step: int = 1):
     if not lengths:
         raise ValueError("empty lattice")
     nel = len(lengths)
-    total = 0.0
-    for v in lengths:
-        total += v
+    # MagneticLattice.totalLen is the built-in sum() of the lengths (compensated
+    # summation on Python 3.12+), not a running total
+    total = sum(lengths)
     stop = float(np.sum(np.array(lengths[:nel - 1]))) if nel > 1 else 0.0
     nominal = float(step) * float(unit_step)
     if not nominal > 0:
@@ -231,9 +232,11 @@ def step_maps2(elements, energy: float, unit_step: float, step: int = 1):
 def navigator_steps(lengths, procs, unit_step: float):
     """The steps of a Navigator with several processes, each attached over
     elements [indx0, indx1) with its own step count: a list of
-    (sections, kicks, z0), sections = [(element index, start in the element,
-    length)] transported in the step, kicks = [(process index, zstep)] applied
-    after it, in the reference's order, and z0 the position after the step.
+    (sections, kicks, z0, dz), sections = [(element index, start in the
+    element, length)] transported in the step, kicks = [(process index, zstep)]
+    applied after it, in the reference's order, z0 the position after the step
+    and dz the step length get_next_step yields (track() adds it to the twiss
+    position).
     ``procs`` = [(indx0, indx1, step)] in the order the processes were added.
 
     Restates Navigator.get_next_step / get_next / check_overjump /
@@ -254,9 +257,7 @@ def navigator_steps(lengths, procs, unit_step: float):
             raise NotImplementedError("a process on a single element (a kick process) is not supported")
         if st < 1:
             raise ValueError("process step must be >= 1")
-    total = 0.0
-    for v in lengths:
-        total += v
+    total = sum(lengths)      # MagneticLattice.totalLen (magnetic_lattice.py:225-227)
     s_start = [np.sum(np.array(lengths[:a])) for a, _, _ in procs]
     s_stop = [np.sum(np.array(lengths[:b])) for _, b, _ in procs]
     counters = [st for _, _, st in procs]
@@ -292,6 +293,7 @@ def navigator_steps(lengths, procs, unit_step: float):
                 phys = np.append(phys, dz)
         if z0 + dz > total:
             dz = total - z0
+        step_dz = float(dz)
         # Navigator.get_map
         sections, i = [], n_elem
         z1 = z0 + dz
@@ -310,7 +312,7 @@ def navigator_steps(lengths, procs, unit_step: float):
         z0 += dz
         sum_lengths = L - lengths[i]
         n_elem = i
-        out.append((sections, [(j, float(phys[q])) for q, j in enumerate(chosen)], float(z0)))
+        out.append((sections, [(j, float(phys[q])) for q, j in enumerate(chosen)], float(z0), step_dz))
         if len(out) > 10_000_000:
             raise RuntimeError("the Navigator's schedule does not terminate")
     return out
@@ -321,12 +323,20 @@ def _line_lengths(seq):
     return [float(e.l) if is_cavity(e) else _element_params(e)[0] for e in seq]
 
 
+class StepSlices(NamedTuple):
+    table: np.ndarray      # [m, MAP2_DOUBLES] records
+    kinds: np.ndarray      # [m] SLICE_MAP | SLICE_CAVITY
+    kicks: list            # [(process, energy, zstep)]
+    z0: float              # Navigator position after the step
+    E: float               # beam energy after the step's maps
+    dz: float              # step length
+
+
 def step_slices(elements, energy: float, steps, order: int = 2, s: float = 0.0):
     """Device records of the maps of every step of ``steps`` (from
     navigator_steps), with the reference energy carried through the cavities
     as Transformation.apply does (p_array.E += delta_e after every map):
-    ([(records [m, MAP2_DOUBLES], kinds [m], kicks [(process, E, zstep)], z0)],
-    final energy, final position).  The position is accumulated as
+    ([StepSlices], final energy, final position).  The position is accumulated as
     Transformation.apply moves p_array.s: by each map's length, starting
     from ``s``.  Drift/quadrupole slices are SecondTM maps (order 2) or
     first-order maps with T = 0 (order 1); cavity sections are the coupler
@@ -337,7 +347,7 @@ def step_slices(elements, energy: float, steps, order: int = 2, s: float = 0.0):
     zero_t = np.zeros((6, 6, 6))
     E = energy
     out = []
-    for sections, kicks, z0 in steps:
+    for sections, kicks, z0, dz in steps:
         recs, kinds = [], []
         for i, start_l, dl in sections:
             e = elements[i]
@@ -359,7 +369,8 @@ def step_slices(elements, energy: float, steps, order: int = 2, s: float = 0.0):
                 recs.append(pack_map(R, zero_t, B))
             kinds.append(CV.SLICE_MAP)
         table = np.array(recs).reshape(-1, CV.MAP2_DOUBLES)
-        out.append((table, np.array(kinds, dtype=np.int32), [(j, E, zstep) for j, zstep in kicks], z0))
+        out.append(StepSlices(table, np.array(kinds, dtype=np.int32), [(j, E, zstep) for j, zstep in kicks], z0, E,
+                              dz))
     return out, E, s
 
 
@@ -401,10 +412,15 @@ class DeviceTrack:
     through the cavities on the host, and each kick gets the energy of its
     step.  Steps whose kicks (energy, length, plan) repeat are recorded once
     as a CUDA graph and replayed.
+
+    ``twiss``: take the beam moments on the device before the first step and
+    after every step (``sc_moments``, get_envelope's statistics; ``bounds`` =
+    [lo, hi] selects the particles within lo..hi standard deviations of tau
+    around its mean); ``twiss_list()`` returns them as Twiss objects.
     """
 
     def __init__(self, elements, sc, unit_step: float, p_array, graph: bool = True, stream=None, order: int = 1,
-                 processes=None):
+                 processes=None, twiss: bool = False, bounds=None):
         import torch
         from .beam import DeviceParticleArray
         from .cavity import is_cavity
@@ -461,20 +477,35 @@ class DeviceTrack:
             for slices, _, _ in kick_schedule(lengths, unit_step, int(processes[0][0].step)):
                 for _, dl in slices:
                     self.s_end += dl
+            self._step_E = [self.E] * len(self.steps)
+            self._step_dz = [st[3] for st in navigator_steps(lengths, [(0, len(seq) - 1, int(processes[0][0].step))],
+                                                             unit_step)]
         else:
             sched = navigator_steps(lengths, [(a, b, p.step) for p, a, b in processes], unit_step)
             slices, self.E_end, self.s_end = step_slices(seq, self.E, sched, order, float(self.beam.s))
-            self.steps = [(tuple((eng_of[j], float(E), float(zstep)) for j, E, zstep in kicks), z0)
-                          for _, _, kicks, z0 in slices]
-            table = np.concatenate([t for t, _, _, _ in slices]) if slices else np.zeros((0, 1))
+            self.steps = [(tuple((eng_of[j], float(E), float(zstep)) for j, E, zstep in st.kicks), st.z0)
+                          for st in slices]
+            self._step_E = [float(st.E) for st in slices]
+            self._step_dz = [st.dz for st in slices]
+            table = np.concatenate([st.table for st in slices]) if slices else np.zeros((0, 1))
             if table.shape[0] == 0:
                 table = np.zeros((1, 168))
-            kinds = np.concatenate([k for _, k, _, _ in slices]) if slices else np.zeros(0, np.int32)
-            first = np.cumsum([0] + [t.shape[0] for t, _, _, _ in slices]).astype(np.int32)
+            kinds = np.concatenate([st.kinds for st in slices]) if slices else np.zeros(0, np.int32)
+            first = np.cumsum([0] + [st.table.shape[0] for st in slices]).astype(np.int32)
             self.first = torch.from_numpy(first).to(self.dev)
             self.kinds = torch.from_numpy(np.ascontiguousarray(np.append(kinds, 0).astype(np.int32))).to(self.dev)
         self.table = torch.from_numpy(np.ascontiguousarray(table)).to(self.dev)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.twiss = bool(twiss)
+        self.bounds = None if bounds is None else (float(bounds[0]), float(bounds[1]))
+        if self.twiss:
+            from .envelope import MOMENTS
+            q_host = p_array.q_array if not isinstance(p_array, DeviceParticleArray) else \
+                self.beam.q_array.cpu().numpy()
+            self.q_total = float(np.sum(np.asarray(q_host)))
+            self.moments = torch.zeros((len(self.steps) + 1, MOMENTS), dtype=torch.float64, device=self.dev)
+            self._mom_scratch = torch.zeros(int(self.engine.lib.sc_moments_scratch_bytes()), dtype=torch.uint8,
+                                            device=self.dev)
         self.stream = stream if stream is not None else torch.cuda.Stream(self.dev)
         self.next = 0
         self.use_graph = bool(graph)
@@ -486,6 +517,9 @@ class DeviceTrack:
         self.done = torch.cuda.Event()
         with torch.cuda.device(self.dev):
             self.stream.wait_stream(torch.cuda.current_stream(self.dev))
+            if self.twiss:
+                with torch.cuda.stream(self.stream):
+                    self._moments(None)      # slot 0: the beam before the first step
 
     @property
     def nsteps(self) -> int:
@@ -509,6 +543,37 @@ class DeviceTrack:
                                              len(self.steps), C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
         for eng, E, zstep in kicks:
             self.engines[eng].kick(rp, q, self.n, E, zstep)
+        if self.twiss:
+            self._moments(self.counter)      # slot *counter = step + 1 (advanced by the transport)
+
+    def _moments(self, counter):
+        import torch
+        rp = self.beam.rparticles
+        s = C.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+        lo, hi = self.bounds if self.bounds is not None else (0.0, 0.0)
+        N.check(self.engine.lib.sc_moments(C.c_void_p(rp.data_ptr()), rp.stride(0), self.n,
+                                           None if counter is None else C.c_void_p(counter.data_ptr()),
+                                           int(self.moments.shape[0]), 1 if self.bounds is not None else 0, lo, hi,
+                                           C.c_void_p(self.moments.data_ptr()), C.c_void_p(self._mom_scratch.data_ptr()),
+                                           s))
+
+    def twiss_list(self):
+        """Twiss of the beam before the first step and after every step, as
+        the reference's track() returns them (s = the sum of the step lengths
+        so far, E = the beam energy after the step).  Waits for the job."""
+        from .envelope import twiss_from_moments
+        if not self.twiss:
+            raise RuntimeError("the job was created with twiss=False")
+        if not self.finished:
+            raise RuntimeError("the job has steps left to run")
+        self.synchronize()
+        m = self.moments.cpu().numpy()
+        out = [twiss_from_moments(m[0], self.E, self.q_total, 0.0)]
+        L = 0.
+        for k in range(len(self.steps)):
+            L += self._step_dz[k]
+            out.append(twiss_from_moments(m[k + 1], self._step_E[k], self.q_total, 0.0 + L))
+        return out
 
     def _graph(self, kicks):
         import torch
@@ -586,7 +651,8 @@ def _navigator_processes(navi, lattice):
     return out
 
 
-def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = True, order=None):
+def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = True, order=None,
+          calc_tws: bool = True, bounds=None, slice=None):
     """Device counterpart of the reference's ``track(lat, p_array, navi)``
     for a space-charge transport line: the particles go to the GPU once, all
     steps run there, and ``p_array`` is updated in place at the end (its
@@ -598,8 +664,13 @@ def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = Tr
     the whole lattice).  ``order``: 1 (first-order maps, TransferMap) or 2
     (SecondTM); by default the lattice's own ``method`` decides.  Cavities are
     tracked with their own map (CavityTM) in either case, as in the reference.
-    Returns (tws, p_array) like the reference, with an empty twiss list.
+    ``calc_tws``, ``bounds``: as the reference's track() -- the beam's Twiss
+    before the first step and after each step, from moments taken on the
+    device (``slice`` other than None, the maximum-current reference slice,
+    is not supported).  Returns (tws, p_array) like the reference.
     """
+    if slice is not None:
+        raise NotImplementedError("slice='Imax' is not supported by device tracking; use slice=None")
     processes = None
     if navi is not None:
         if sc is None:
@@ -608,6 +679,16 @@ def track(lattice, p_array, navi=None, sc=None, unit_step=None, graph: bool = Tr
     if (sc is None and processes is None) or unit_step is None:
         raise ValueError("pass navi, or sc and unit_step")
     order = lattice_order(lattice) if order is None else int(order)
-    job = DeviceTrack(lattice, sc, unit_step, p_array, graph=graph, order=order, processes=processes).run()
+    job = DeviceTrack(lattice, sc, unit_step, p_array, graph=graph, order=order, processes=processes,
+                      twiss=calc_tws, bounds=bounds).run()
     job.result(p_array)
-    return [], p_array
+    if calc_tws:
+        return job.twiss_list(), p_array
+    from .envelope import Twiss
+    tws, L = [Twiss()], 0.
+    for dz in job._step_dz:
+        L += dz
+        tw = Twiss()
+        tw.s += L
+        tws.append(tw)
+    return tws, p_array

@@ -186,7 +186,7 @@ def build_track_scenario(ref_root: str):
     return lattice, p_array, conf
 
 
-def track_scenario(ref_root: str, proc_factory):
+def track_scenario(ref_root: str, proc_factory, with_tws=False, **kw):
     from ocelot import Navigator, track
     lattice, p_array, conf = build_track_scenario(ref_root)
     sc1 = proc_factory(1)
@@ -195,8 +195,8 @@ def track_scenario(ref_root: str, proc_factory):
     navi.add_physics_proc(sc1, lattice.sequence[0], conf.C_A1_1_2_I1)
     navi.add_physics_proc(sc5, conf.C_A1_1_2_I1, lattice.sequence[-1])
     navi.unit_step = 0.02
-    _, p = track(lattice, p_array, navi, print_progress=False)
-    return p
+    tws, p = track(lattice, p_array, navi, print_progress=False, **kw)
+    return (tws, p) if with_tws else p
 
 
 def run_track(ref_root: str, keep=(0, 120)):
@@ -460,6 +460,11 @@ def run_cavity(ref_root: str, n=64):
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.3f} MB)")
 
 
+TWISS_KEYS = ["E", "q", "s", "p", "x", "y", "px", "py", "tau", "xx", "xpx", "pxpx", "yy", "ypy", "pypy", "tautau",
+              "xy", "pxpy", "xpy", "ypx", "pp", "emit_x", "emit_y", "emit_xn", "emit_yn", "eigemit_1", "eigemit_2",
+              "beta_x", "beta_y", "alpha_x", "alpha_y"]
+
+
 def run_track_line(ref_root: str):
     """The reference's test_track_with_sp scenario (16 cavities, SecondTM,
     two SpaceCharge processes of step 1 and 5) tracked by the reference's own
@@ -481,12 +486,23 @@ def run_track_line(ref_root: str):
         sc.nmesh_xyz = [63, 63, 63]
         return sc
 
+    from ocelot.cpbd.beam.analysis import get_envelope
+    bounded = []
+
+    def both_envelopes(p_array, bounds=None, slice=None, auto_disp=False):
+        bounded.append(get_envelope(p_array, bounds=[-0.5, 0.5]))
+        return get_envelope(p_array, bounds=bounds, slice=slice, auto_disp=auto_disp)
+
     SpaceCharge.apply = recording_apply
     try:
-        p = track_scenario(ref_root, make_ref)
+        tws, p = track_scenario(ref_root, make_ref, with_tws=True, get_twiss=both_envelopes)
     finally:
         SpaceCharge.apply = base_apply
     seq = lattice.sequence
+    keys = TWISS_KEYS
+    twiss = np.array([[float(np.real(getattr(t, k))) for k in keys] for t in tws])
+    twiss_b = np.array([[float(np.real(getattr(t, k))) for k in keys] for t in bounded])
+    twiss_b[:, keys.index("s")] = twiss[:, keys.index("s")]
     data = dict(rp_start=start, q=p0.q_array.copy(), E_start=np.array(0.0065), rp_end=p.rparticles.copy(),
                 E_end=np.array(p.E), s_end=np.array(p.s),
                 kick_step=np.array([r[0] for r in rec], dtype=np.int32), kick_z0=np.array([r[1] for r in rec]),
@@ -496,7 +512,9 @@ def run_track_line(ref_root: str):
                 elements=np.array([[2 if type(e).__name__ == "Cavity" else 1 if type(e).__name__ == "Quadrupole" else 0,
                                     e.l, getattr(e, "k1", 0.0), getattr(e, "v", 0.0), getattr(e, "phi", 0.0),
                                     getattr(e, "freq", 0.0)] for e in seq]),
-                indx=np.array([seq.index(conf.C_A1_1_2_I1), len(seq) - 1], dtype=np.int32))
+                indx=np.array([seq.index(conf.C_A1_1_2_I1), len(seq) - 1], dtype=np.int32),
+                # get_envelope after every step (track()'s twiss list), and with bounds [-0.5, 0.5]
+                twiss_keys=np.array(keys), twiss=twiss, twiss_bounds=twiss_b)
     path = os.path.join(HERE, "ref_track_line.npz")
     np.savez_compressed(path, **data)
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB), {len(rec)} kicks")

@@ -97,7 +97,7 @@ def test_navigator_steps_one_process_equals_kick_schedule():
         a = T.kick_schedule(lengths, unit_step, step)
         b = T.navigator_steps(lengths, [(0, len(seq) - 1, step)], unit_step)
         assert len(a) == len(b)
-        for (sl_a, zstep, z0a), (sec_b, kicks, z0b) in zip(a, b):
+        for (sl_a, zstep, z0a), (sec_b, kicks, z0b, _) in zip(a, b):
             assert z0a == z0b and kicks == [(0, zstep)]
             assert sl_a == [(i, T._section_length(lengths[i], s, d)) for i, s, d in sec_b]
 
@@ -110,7 +110,7 @@ def test_line_schedule_and_energies_are_the_reference_navigators():
     procs = line_procs()
     steps = T.navigator_steps([e.l for e in seq], procs, 0.02)
     slices, E_end, s_end = T.step_slices(seq, float(LINE["E_start"]), steps, order=2)
-    kicks = [(procs[j][2], z0, zstep, E) for (_, _, ks, z0) in slices for j, E, zstep in ks]
+    kicks = [(procs[j][2], st.z0, zstep, E) for st in slices for j, E, zstep in st.kicks]
     assert len(kicks) == len(LINE["kick_step"]) == 193
     assert [k[0] for k in kicks] == list(LINE["kick_step"])
     assert np.array_equal([k[1] for k in kicks], LINE["kick_z0"])
@@ -118,7 +118,7 @@ def test_line_schedule_and_energies_are_the_reference_navigators():
     assert np.array_equal([k[3] for k in kicks], LINE["kick_E"])
     assert E_end == LINE["E_end"]
     assert s_end == LINE["s_end"]                   # p_array.s as Transformation.apply moves it
-    assert len(slices[-1][2]) == 0                  # the last quadrupole: transport only, no process
+    assert len(slices[-1].kicks) == 0               # the last quadrupole: transport only, no process
 
 
 def test_navigator_steps_reject_kick_processes_and_bad_ranges():
@@ -130,3 +130,68 @@ def test_navigator_steps_reject_kick_processes_and_bad_ranges():
         T.navigator_steps([1.0, 1.0], [(0, 5, 1)], 0.1)
     with pytest.raises(ValueError):
         T.navigator_steps([], [(0, 0, 1)], 0.1)
+
+
+def _twiss_row(t, keys):
+    return np.array([float(getattr(t, k)) for k in keys])
+
+
+_CROSS = {"xpx": ("xx", "pxpx"), "ypy": ("yy", "pypy"), "xy": ("xx", "yy"), "pxpy": ("pxpx", "pypy"),
+          "xpy": ("xx", "pypy"), "ypx": ("yy", "pxpx")}
+
+
+def twiss_close(ours, ref, keys, rtol=1e-9, eig_rtol=1e-7, derived_rtol=None):
+    """Twiss rows against the reference's: the means within rtol of the
+    beam size and the correlations within rtol of the product of the two rms
+    sizes (both are near zero), eigen-emittances within eig_rtol (they are
+    computed by another method here), emittances, beta and alpha within
+    derived_rtol (they amplify the moments' differences: an emittance by
+    about 1 + alpha^2), the rest within rtol."""
+    k = list(keys)
+    bad = []
+    for j, name in enumerate(k):
+        a, b = ours[j], ref[j]
+        if name in ("x", "px", "y", "py", "tau", "p"):
+            scale = np.sqrt(abs(ref[k.index({"x": "xx", "px": "pxpx", "y": "yy", "py": "pypy", "tau": "tautau",
+                                              "p": "pp"}[name])]))
+            ok = abs(a - b) <= rtol * scale
+        elif name.startswith("eigemit"):
+            ok = abs(a - b) <= eig_rtol * abs(b)
+        elif name in _CROSS:
+            # a correlation: relative to the product of the two rms sizes
+            u, v = _CROSS[name]
+            ok = abs(a - b) <= rtol * np.sqrt(abs(ref[k.index(u)] * ref[k.index(v)]))
+        elif name.startswith("alpha"):
+            ok = abs(a - b) <= (derived_rtol or rtol) * (abs(b) + 1.0)
+        elif name.startswith(("emit", "beta")):
+            ok = abs(a - b) <= (derived_rtol or rtol) * abs(b)
+        else:
+            ok = abs(a - b) <= rtol * abs(b)
+        if not ok:
+            bad.append((name, a, b))
+    return bad
+
+
+def test_envelope_of_start_and_end_beams_matches_reference():
+    from ocelot_gb300.envelope import moments_numpy, twiss_from_moments
+    keys = [str(k) for k in LINE["twiss_keys"]]
+    q = float(np.sum(LINE["q"]))
+    for rp, E, row, s in ((LINE["rp_start"], float(LINE["E_start"]), 0, 0.0),
+                          (LINE["rp_end"], float(LINE["E_end"]), -1, float(LINE["twiss"][-1][keys.index("s")]))):
+        for bounds, table in ((None, LINE["twiss"]), ([-0.5, 0.5], LINE["twiss_bounds"])):
+            t = twiss_from_moments(moments_numpy(rp, bounds), E, q, s)
+            assert not twiss_close(_twiss_row(t, keys), table[row], keys, rtol=1e-12, eig_rtol=1e-8)
+
+
+def test_twiss_positions_and_energies_are_the_reference_tracks():
+    keys = [str(k) for k in LINE["twiss_keys"]]
+    seq = line_elements()
+    steps = T.navigator_steps([e.l for e in seq], line_procs(), 0.02)
+    slices, _, _ = T.step_slices(seq, float(LINE["E_start"]), steps, order=2)
+    L, s, E = 0., [0.0], [float(LINE["E_start"])]
+    for st in slices:
+        L += st.dz
+        s.append(0.0 + L)
+        E.append(st.E)
+    assert np.array_equal(s, LINE["twiss"][:, keys.index("s")])
+    assert np.array_equal(E, LINE["twiss"][:, keys.index("E")])
