@@ -520,6 +520,63 @@ def run_track_line(ref_root: str):
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB), {len(rec)} kicks")
 
 
+def run_track_mixed(ref_root: str, n=5000, mesh=(31, 31, 31)):
+    """A short line with first-order transport (TransferMap), an RF cavity,
+    quadrupoles and two SpaceCharge processes of different step counts,
+    tracked by the reference's own track(): the start and end beams, the
+    energy and position at the end, every kick, and the twiss list."""
+    import_reference(ref_root)
+    from ocelot import (Cavity, Drift, Marker, MagneticLattice, Navigator, Quadrupole, TransferMap, track)
+    from ocelot.cpbd.sc import SpaceCharge
+    c = Cavity(l=0.5, v=0.005, phi=20.0, freq=1.3e9, eid="C")
+    q1 = Quadrupole(l=0.2, k1=2.0, eid="Q1")
+    q2 = Quadrupole(l=0.2, k1=-2.0, eid="Q2")
+    m_end = Marker(eid="END")
+    seq = [Marker(eid="START"), Drift(l=0.3), c, Drift(l=0.2), q1, Drift(l=0.5), q2, Drift(l=0.3), m_end]
+    lat = MagneticLattice(seq, method={"global": TransferMap})
+    rp, q = sc_oracle.gaussian_beam(n, seed=5, sigma_x=3e-4, sigma_px=2e-5, sigma_y=2e-4, sigma_py=3e-5,
+                                    sigma_tau=5e-4, sigma_p=1e-3, charge=300e-12)
+    from ocelot import ParticleArray
+    pa = ParticleArray(n=n)
+    pa.rparticles[:] = rp
+    pa.q_array = q.copy()
+    pa.E = 0.02
+    start = rp.copy()
+    sc_a = SpaceCharge(step=2)
+    sc_a.nmesh_xyz = list(mesh)
+    sc_b = SpaceCharge(step=3)
+    sc_b.nmesh_xyz = list(mesh)
+    navi = Navigator(lat)
+    navi.add_physics_proc(sc_a, seq[0], q1)
+    navi.add_physics_proc(sc_b, q1, m_end)
+    navi.unit_step = 0.05
+    rec = []
+    base_apply = SpaceCharge.apply
+
+    def recording_apply(self, p_array, zstep):
+        rec.append((self.step, self.z0, zstep, p_array.E))
+        base_apply(self, p_array, zstep)
+
+    SpaceCharge.apply = recording_apply
+    try:
+        tws, p = track(lat, pa, navi, print_progress=False)
+    finally:
+        SpaceCharge.apply = base_apply
+    keys = TWISS_KEYS
+    data = dict(rp_start=start, q=q, E_start=np.array(0.02), rp_end=p.rparticles.copy(), E_end=np.array(p.E),
+                s_end=np.array(p.s), nmesh=np.array(mesh), unit_step=np.array(0.05),
+                kick_step=np.array([r[0] for r in rec], dtype=np.int32), kick_z0=np.array([r[1] for r in rec]),
+                kick_zstep=np.array([r[2] for r in rec]), kick_E=np.array([r[3] for r in rec]),
+                elements=np.array([[2 if type(e).__name__ == "Cavity" else 1 if type(e).__name__ == "Quadrupole" else 0,
+                                    e.l, getattr(e, "k1", 0.0), getattr(e, "v", 0.0), getattr(e, "phi", 0.0),
+                                    getattr(e, "freq", 0.0)] for e in seq]),
+                indx=np.array([seq.index(q1), len(seq) - 1], dtype=np.int32),
+                twiss_keys=np.array(keys), twiss=np.array([[float(np.real(getattr(t, k))) for k in keys] for t in tws]))
+    path = os.path.join(HERE, "ref_track_mixed.npz")
+    np.savez_compressed(path, **data)
+    print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB), {len(rec)} kicks")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -531,6 +588,7 @@ if __name__ == "__main__":
     a = ap.parse_args()
     if a.only_cavity:
         run_cavity(a.reference)
+        run_track_mixed(a.reference)
         run_track_line(a.reference)
         sys.exit(0)
     if a.only_second_order_io:
@@ -551,4 +609,5 @@ if __name__ == "__main__":
         run_cavity(a.reference)
     if not a.skip_track:
         run_track(a.reference)
+        run_track_mixed(a.reference)
         run_track_line(a.reference)

@@ -33,9 +33,12 @@ def close_rows(a, b, rtol):
     return all(np.abs(a[r] - b[r]).max() <= rtol * np.abs(b[r]).max() for r in range(6))
 
 
-def line_elements():
+MIXED = dict(np.load(os.path.join(GOLDEN, "ref_track_mixed.npz")))
+
+
+def line_elements(fixture=None):
     seq = []
-    for kind, l, k1, v, phi, freq in LINE["elements"]:
+    for kind, l, k1, v, phi, freq in (LINE if fixture is None else fixture)["elements"]:
         if kind == 2:
             seq.append(CV.Cavity(l=l, v=v, phi=phi, freq=freq))
         elif kind == 1:
@@ -50,6 +53,11 @@ def line_elements():
 def line_procs():
     i4, i20 = (int(v) for v in LINE["indx"])
     return [(0, i4, 1), (i4, i20, 5)]
+
+
+def mixed_procs():
+    i_q1, i_end = (int(v) for v in MIXED["indx"])
+    return [(0, i_q1, 2), (i_q1, i_end, 3)]
 
 
 @pytest.mark.parametrize("c,k", sections())
@@ -195,3 +203,27 @@ def test_twiss_positions_and_energies_are_the_reference_tracks():
         E.append(st.E)
     assert np.array_equal(s, LINE["twiss"][:, keys.index("s")])
     assert np.array_equal(E, LINE["twiss"][:, keys.index("E")])
+
+
+def test_mixed_line_schedule_energies_and_positions_are_the_reference_tracks():
+    """First-order transport, a cavity and two processes (step 2 up to the
+    first quadrupole, step 3 after it): kicks, energies, s and the twiss
+    positions bit for bit."""
+    keys = [str(k) for k in MIXED["twiss_keys"]]
+    seq = line_elements(MIXED)
+    procs = mixed_procs()
+    steps = T.navigator_steps([e.l for e in seq], procs, float(MIXED["unit_step"]))
+    slices, E_end, s_end = T.step_slices(seq, float(MIXED["E_start"]), steps, order=1)
+    kicks = [(procs[j][2], st.z0, zstep, E) for st in slices for j, E, zstep in st.kicks]
+    assert [k[0] for k in kicks] == list(MIXED["kick_step"])
+    assert np.array_equal([k[1] for k in kicks], MIXED["kick_z0"])
+    assert np.array_equal([k[2] for k in kicks], MIXED["kick_zstep"])
+    assert np.array_equal([k[3] for k in kicks], MIXED["kick_E"])
+    assert E_end == MIXED["E_end"] and s_end == MIXED["s_end"]
+    L, s = 0., [0.0]
+    for st in slices:
+        L += st.dz
+        s.append(0.0 + L)
+    assert np.array_equal(s, MIXED["twiss"][:, keys.index("s")])
+    # first-order records only: the slices carry no second-order terms
+    assert all(not st.table[st.kinds == CV.SLICE_MAP][:, 42:].any() for st in slices)

@@ -12,7 +12,8 @@ import numpy as np
 import pytest
 
 from conftest import has_gpu
-from test_cavity_host import CAV, LINE, cavity_case, close_rows, line_elements, line_procs, sections
+from test_cavity_host import (CAV, LINE, MIXED, cavity_case, close_rows, line_elements, line_procs, mixed_procs,
+                              sections)
 
 pytestmark = pytest.mark.gpu
 if not has_gpu():
@@ -205,3 +206,28 @@ def test_line_twiss_graph_equals_eager():
         job.synchronize()
         runs.append(job.moments.cpu().numpy())
     assert np.array_equal(runs[0], runs[1])
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_mixed_line_first_order_matches_reference_track(graph):
+    """First-order transport through a cavity and quadrupoles with two
+    processes of different step counts (the reference's TransferMap lattice)."""
+    from test_cavity_host import _twiss_row, twiss_close
+    pa = ParticleArray(MIXED["rp_start"].shape[1])
+    pa.rparticles[:] = MIXED["rp_start"]
+    pa.q_array = MIXED["q"].copy()
+    pa.E = float(MIXED["E_start"])
+    mesh = [int(v) for v in MIXED["nmesh"]]
+    procs = [(SpaceCharge(step=st, nmesh_xyz=mesh), a, b) for a, b, st in mixed_procs()]
+    job = T.DeviceTrack(line_elements(MIXED), None, float(MIXED["unit_step"]), pa, graph=graph, order=1,
+                        processes=procs, twiss=True).run()
+    tws = job.twiss_list()
+    job.result(pa)
+    assert not job.composed and sum(len(k) for k, _ in job.steps) == len(MIXED["kick_step"])
+    assert pa.E == MIXED["E_end"] and pa.s == MIXED["s_end"]
+    err = np.abs(pa.rparticles - MIXED["rp_end"]).max(axis=1)
+    assert (err <= TOL_ABS).all(), err
+    keys = [str(k) for k in MIXED["twiss_keys"]]
+    for i, t in enumerate(tws):
+        assert not twiss_close(_twiss_row(t, keys), MIXED["twiss"][i], keys, rtol=1e-9, eig_rtol=1e-6,
+                               derived_rtol=1e-8), i
