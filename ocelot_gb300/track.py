@@ -399,8 +399,8 @@ class DeviceTrack:
     the first to the last element, or ``processes`` = [(SpaceCharge, indx0,
     indx1)], each attached over elements [indx0, indx1) as
     Navigator.add_physics_proc does, in the order they were added (each
-    process's precision, mesh and deposit/IGF options are used; random_mesh
-    is not supported, its draws would have to be taken per step on the host);
+    process's precision, mesh, deposit/IGF options and random_mesh are used;
+    the random mesh draws are taken when the job is built, in kick order);
     ``unit_step``: the Navigator's unit step; ``p_array``: host ParticleArray
     or DeviceParticleArray (the particles are copied once to the device).
 
@@ -433,9 +433,6 @@ class DeviceTrack:
         else:
             processes = [(p, int(a), int(b)) for p, a, b in processes]
             whole = len(processes) == 1 and processes[0][1] == 0 and processes[0][2] == len(seq) - 1
-        for p, _, _ in processes:
-            if p.random_mesh:
-                raise NotImplementedError("random_mesh draws host random numbers per kick: use track() on the host")
         first = processes[0][0] if processes else sc
         self.dev = torch.device(first.device) if first is not None and first.device is not None else torch.device(
             "cuda", torch.cuda.current_device())
@@ -471,7 +468,7 @@ class DeviceTrack:
             for k, (R, B, zstep, z0) in enumerate(maps):
                 table[k, :36] = R.reshape(-1)
                 table[k, 36:] = B
-                self.steps.append((((0, self.E, zstep),), z0))
+                self.steps.append((((0, self.E, zstep) + self._draws(processes[0][0], zstep),), z0))
             self.E_end = self.E
             self.s_end = float(self.beam.s)
             for slices, _, _ in kick_schedule(lengths, unit_step, int(processes[0][0].step)):
@@ -483,8 +480,8 @@ class DeviceTrack:
         else:
             sched = navigator_steps(lengths, [(a, b, p.step) for p, a, b in processes], unit_step)
             slices, self.E_end, self.s_end = step_slices(seq, self.E, sched, order, float(self.beam.s))
-            self.steps = [(tuple((eng_of[j], float(E), float(zstep)) for j, E, zstep in st.kicks), st.z0)
-                          for st in slices]
+            self.steps = [(tuple((eng_of[j], float(E), float(zstep)) + self._draws(processes[j][0], zstep)
+                                 for j, E, zstep in st.kicks), st.z0) for st in slices]
             self._step_E = [float(st.E) for st in slices]
             self._step_dz = [st.dz for st in slices]
             table = np.concatenate([st.table for st in slices]) if slices else np.zeros((0, 1))
@@ -521,6 +518,17 @@ class DeviceTrack:
                 with torch.cuda.stream(self.stream):
                     self._moments(None)      # slot 0: the beam before the first step
 
+    @staticmethod
+    def _draws(p, zstep):
+        """A random_mesh process's two draws for one kick (sc.py:174-175,
+        184-185), taken from numpy's global generator in kick order when the
+        job is built -- the order the reference's track() takes them in
+        (SpaceCharge.apply returns before drawing when zstep is 0)."""
+        if not p.random_mesh or zstep == 0:
+            return (None, None)
+        scale, shift = p._mesh_draws()
+        return (float(scale), float(shift))
+
     @property
     def nsteps(self) -> int:
         return len(self.steps)
@@ -541,8 +549,9 @@ class DeviceTrack:
             N.check(lib.sc_slices_apply_step(C.c_void_p(self.table.data_ptr()), C.c_void_p(self.kinds.data_ptr()),
                                              C.c_void_p(self.first.data_ptr()), C.c_void_p(self.counter.data_ptr()),
                                              len(self.steps), C.c_void_p(rp.data_ptr()), rp.stride(0), self.n, s))
-        for eng, E, zstep in kicks:
-            self.engines[eng].kick(rp, q, self.n, E, zstep)
+        for eng, E, zstep, scale, shift in kicks:
+            self.engines[eng].kick(rp, q, self.n, E, zstep, math.nan if scale is None else scale,
+                                   math.nan if shift is None else shift)
         if self.twiss:
             self._moments(self.counter)      # slot *counter = step + 1 (advanced by the transport)
 

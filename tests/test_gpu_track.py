@@ -139,3 +139,41 @@ def test_interleaved_jobs_equal_alone(precision):
             j.step(1)
     for j, ref in zip(jobs, alone):
         assert np.array_equal(j.result().rparticles, ref)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_random_mesh_track_equals_plugin_step_by_step(precision):
+    """random_mesh: the device loop takes the two draws per kick from numpy's
+    global generator in kick order, as SpaceCharge.apply does inside the
+    reference's track() -- so a seeded device track equals the plugin
+    applied after each step's map, bit for bit, and leaves the generator in
+    the same state."""
+    mesh = [int(v) for v in FODO["nmesh"]]
+    E = float(FODO["E"])
+    seq = _fodo(int(FODO["cells"]))
+    np.random.seed(10)
+    sc = SpaceCharge(step=1, nmesh_xyz=mesh, precision=precision, random_mesh=True)
+    job = T.DeviceTrack(seq, sc, 0.25, _pa(FODO["rp_in"], FODO["q"], E), graph=True)
+    after_job = np.random.random()
+    out = job.run().result().rparticles
+    assert len(job._graphs) == 0           # every kick has its own mesh: no step repeats
+
+    np.random.seed(10)
+    sc2 = SpaceCharge(step=1, nmesh_xyz=mesh, precision=precision, random_mesh=True)
+    dev = torch.device("cuda", 0)
+    # the job's row layout (the FP32 form is bit-reproducible for a given layout)
+    rp = torch.empty_like(job.beam.rparticles)
+    assert rp.stride() == job.beam.rparticles.stride()
+    rp.copy_(torch.from_numpy(FODO["rp_in"]))
+    q = torch.from_numpy(FODO["q"]).to(dev)
+    lib = N.lib()
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    for R, B, zstep, _ in T.step_maps(seq, E, 0.25):
+        Rc = np.ascontiguousarray(R, dtype=np.float64)
+        Bc = np.ascontiguousarray(B, dtype=np.float64)
+        N.check(lib.sc_tmap_apply(Rc.ctypes.data_as(C.POINTER(C.c_double)), Bc.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.c_void_p(rp.data_ptr()), rp.stride(0), rp.shape[1], s))
+        sc2.apply_device(rp, q, E, zstep)
+    sc2.check()
+    assert np.random.random() == after_job
+    assert np.array_equal(out, rp.cpu().numpy())
