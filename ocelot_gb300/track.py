@@ -16,11 +16,16 @@ kick length (all but the last, truncated one, in a uniform lattice).
 
 Scope: drifts, quadrupoles (with tilt and offsets), markers and monitors --
 the elements whose first-order map is ``uni_matrix`` without bending
-(ocelot/cpbd/r_matrix.py:41-91); one SpaceCharge process attached from the
-first to the last element, the configuration of a space-charge transport
-line.  With ``order=2`` the transport is the reference's SecondTM instead
-(second_order.py): the slices of a step are not composed but applied one
-after the other in one pass (``sc_tmap2_apply_step``).
+(ocelot/cpbd/r_matrix.py:41-91) -- and standing-wave RF cavities (CavityTM,
+``cavity.py``); any number of SpaceCharge processes, each over its element
+range with its own step count.  With one process over a line without
+cavities and first-order maps, each step's slice maps are composed into one.
+With ``order=2`` the transport is the reference's SecondTM instead
+(second_order.py), and in a line with cavities or several processes the
+slices of a step are not composed but applied one after the other in one
+pass (``sc_slices_apply_step``), the beam energy carried through the
+cavities.  ``track()`` also returns the twiss list (beam moments taken on
+the device after every step, ``envelope.py``).
 """
 from __future__ import annotations
 
@@ -31,6 +36,8 @@ from typing import NamedTuple
 import numpy as np
 
 from . import _native as N
+from .cavity import Cavity  # noqa: F401  (the line elements are importable from here)
+from .envelope import Twiss  # noqa: F401
 from .globals import m_e_GeV
 
 
