@@ -482,12 +482,10 @@ class DeviceTrack:
                 for _, dl in slices:
                     self.s_end += dl
             self._step_E = [self.E] * len(self.steps)
-            try:
-                self._step_dz = [st[3] for st in navigator_steps(
-                    lengths, [(0, len(seq) - 1, int(processes[0][0].step))], unit_step)]
-            except NotImplementedError:
-                # a two-element line whose first element has no length (a kick process for the Navigator)
-                self._step_dz = list(np.diff([0.0] + [z0 for _, z0 in self.steps]))
+            # (a two-element line whose first element has no length makes the process a kick process for the
+            # reference's Navigator, applied once: not supported, navigator_steps raises)
+            self._step_dz = [st[3] for st in navigator_steps(
+                lengths, [(0, len(seq) - 1, int(processes[0][0].step))], unit_step)]
         else:
             sched = navigator_steps(lengths, [(a, b, p.step) for p, a, b in processes], unit_step)
             slices, self.E_end, self.s_end = step_slices(seq, self.E, sched, order, float(self.beam.s))
