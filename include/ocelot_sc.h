@@ -260,6 +260,16 @@ int sc_tmap2_apply_step(const double* maps, const int* first, int* counter, int 
  *   kinds: DEVICE int32[nmaps]. */
 #define SC_SLICE_MAP 0
 #define SC_SLICE_CAVITY 1
+/* A map (as SC_SLICE_MAP) whose non-zero entries lie in the pattern of an untilted quadrupole or drift without
+ * offsets -- R: (0,0) (0,1) (1,0) (1,1) (2,2) (2,3) (3,2) (3,3) (4,4) (4,5) (5,5); Tc: outputs 0,1 at the pairs
+ * (0,5) (1,5), outputs 2,3 at (2,5) (3,5), output 4 at (0,0) (0,1) (1,1) (2,2) (2,3) (3,3) (5,5) -- or, for
+ * SC_SLICE_MAP_DRIFT, of a drift -- R: (0,0) (0,1) (1,1) (2,2) (2,3) (3,3) (4,4) (4,5) (5,5); Tc: output 0 at
+ * (1,5), output 2 at (3,5), output 4 at (1,1) (3,3) (5,5).  Evaluated over the pattern only, with the same result
+ * as SC_SLICE_MAP for finite coordinates; the caller guarantees the pattern. */
+#define SC_SLICE_MAP_PLANAR 2
+#define SC_SLICE_MAP_DRIFT 3
+/* A first-order map (Tc = 0) whose R lies in the SC_SLICE_MAP_PLANAR pattern. */
+#define SC_SLICE_MAP_LINEAR 4
 int sc_slices_apply(const double* maps, const int* kinds, int nmaps, double* rparticles, int64_t ld, int64_t n,
                     void* stream);
 

@@ -24,9 +24,49 @@ import numpy as np
 
 from .globals import m_e_GeV, speed_of_light
 
+MAP2_DOUBLES = 36 + 6 + 6 * 21
 SLICE_MAP = 0      # SC_SLICE_MAP
 SLICE_CAVITY = 1   # SC_SLICE_CAVITY
-MAP2_DOUBLES = 36 + 6 + 6 * 21
+SLICE_MAP_PLANAR = 2   # SC_SLICE_MAP_PLANAR
+SLICE_MAP_DRIFT = 3    # SC_SLICE_MAP_DRIFT
+SLICE_MAP_LINEAR = 4   # SC_SLICE_MAP_LINEAR
+
+
+def _pair(j, k):
+    return j * 6 - j * (j - 1) // 2 + (k - j)
+
+
+def _pattern(r_entries, t_entries):
+    mask = np.zeros(MAP2_DOUBLES, dtype=bool)
+    for r, k in r_entries:
+        mask[r * 6 + k] = True
+    mask[36:42] = True
+    for r, (j, k) in t_entries:
+        mask[42 + r * 21 + _pair(j, k)] = True
+    return mask
+
+
+# the fixed patterns of the device's straight-line map forms (the C header's SC_SLICE_MAP_PLANAR / _DRIFT)
+_PLANAR = _pattern([(0, 0), (0, 1), (1, 0), (1, 1), (2, 2), (2, 3), (3, 2), (3, 3), (4, 4), (4, 5), (5, 5)],
+                   [(0, (0, 5)), (0, (1, 5)), (1, (0, 5)), (1, (1, 5)), (2, (2, 5)), (2, (3, 5)), (3, (2, 5)),
+                    (3, (3, 5)), (4, (0, 0)), (4, (0, 1)), (4, (1, 1)), (4, (2, 2)), (4, (2, 3)), (4, (3, 3)),
+                    (4, (5, 5))])
+_DRIFT = _pattern([(0, 0), (0, 1), (1, 1), (2, 2), (2, 3), (3, 3), (4, 4), (4, 5), (5, 5)],
+                  [(0, (1, 5)), (2, (3, 5)), (4, (1, 1)), (4, (3, 3)), (4, (5, 5))])
+
+
+def map_kind(record) -> int:
+    """The device form for a map record: first-order in the quadrupole
+    pattern, the drift or quadrupole pattern when every non-zero entry lies
+    in it, the general form otherwise."""
+    nz = np.asarray(record).reshape(-1) != 0.0
+    if not np.any(nz[42:]) and not np.any(nz & ~_PLANAR):
+        return SLICE_MAP_LINEAR
+    if not np.any(nz & ~_DRIFT):
+        return SLICE_MAP_DRIFT
+    if not np.any(nz & ~_PLANAR):
+        return SLICE_MAP_PLANAR
+    return SLICE_MAP
 CAV_E, CAV_BETA0, CAV_DEN, CAV_A, CAV_K, CAV_PHI, CAV_COSPHI, CAV_T566, CAV_T556, CAV_T555, CAV_RF = range(42, 53)
 
 
@@ -272,7 +312,7 @@ def section_records(e, start_l: float, delta_l: float, energy):
             R, B = edge_map(e, E, kind == "entrance")
             if not (np.array_equal(R, np.eye(6)) and not np.any(B)):
                 recs.append(pack_map(R, np.zeros((6, 6, 6)), B))
-                kinds.append(SLICE_MAP)
+                kinds.append(map_kind(recs[-1]))
     return np.array(recs).reshape(-1, MAP2_DOUBLES), kinds, E
 
 

@@ -13,25 +13,50 @@ struct Map6 {
     double m[42];  // R (row-major), then B
 };
 
+// A map coefficient and whether it is non-zero, tested on its bit pattern:
+// on this GPU a double compare issues on the narrow FP64 pipe, an integer
+// compare does not.  Every thread reads the same coefficient, so the branch on
+// it is warp-uniform.  Skipping a zero term leaves every sum unchanged (up to
+// the sign of an exact zero, which the final "+ B" removes) for finite inputs.
+// The map may sit in global or shared memory (generic loads).
+__device__ __forceinline__ bool coef_nz(const double* m, int i, double& v) {
+    const long long b = reinterpret_cast<const long long*>(m)[i];
+    v = __longlong_as_double(b);
+    return (b << 1) != 0;
+}
+
+// y_r = sum_k R[r][k] x_k over the non-zero R[r][k], in k order (FMA chain)
+__device__ __forceinline__ void rmul_sparse(const double* m, const double (&x)[6], double (&y)[6]) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            double v;
+            if (coef_nz(m, r * 6 + k, v)) acc = __fma_rn(v, x[k], acc);
+        }
+        y[r] = acc;
+    }
+}
+
 // one particle: x <- R.x + B with m = R (row-major) then B
 __device__ __forceinline__ void tmap_one(const double* __restrict__ m, double* __restrict__ rp, int64_t ld,
                                          int64_t i) {
-    double x[6];
+    double x[6], y[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
+    rmul_sparse(m, x, y);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-        double acc = __dmul_rn(m[r * 6], x[0]);
-#pragma unroll
-        for (int k = 1; k < 6; ++k) acc = __fma_rn(m[r * 6 + k], x[k], acc);
-        rp[r * ld + i] = __dadd_rn(acc, m[36 + r]);
-    }
+    for (int r = 0; r < 6; ++r) rp[r * ld + i] = __dadd_rn(y[r], m[36 + r]);
 }
 
 __global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, int64_t ld, int64_t n) {
     pdl_wait();
+    __shared__ double sm[42];
+    if (threadIdx.x < 42) sm[threadIdx.x] = m.m[threadIdx.x];
+    __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        tmap_one(m.m, rp, ld, i);
+        tmap_one(sm, rp, ld, i);
 }
 
 // batched: each beam's own map from the work table, over the beam's blocks
@@ -119,27 +144,95 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
 constexpr int MAP2 = 36 + 6 + 6 * 21;
 
 __device__ __forceinline__ void tmap2_one(const double* __restrict__ m, double (&x)[6]) {
-    double p[21];
+    double y[6];
+    rmul_sparse(m, x, y);
+    // the second-order terms pair by pair: a product x_j x_k is formed only
+    // when some output uses it; each output still takes its terms in pair order
     int q = 0;
 #pragma unroll
-    for (int j = 0; j < 6; ++j)
+    for (int j = 0; j < 6; ++j) {
 #pragma unroll
-        for (int k = j; k < 6; ++k) p[q++] = __dmul_rn(x[j], x[k]);
-    double y[6];
+        for (int k = j; k < 6; ++k, ++q) {
+            long long any = 0;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-        double acc = __dmul_rn(__ldg(m + r * 6), x[0]);
+            for (int r = 0; r < 6; ++r) any |= reinterpret_cast<const long long*>(m)[42 + r * 21 + q] << 1;
+            if (any == 0) continue;
+            const double p = __dmul_rn(x[j], x[k]);
 #pragma unroll
-        for (int k = 1; k < 6; ++k) acc = __fma_rn(__ldg(m + r * 6 + k), x[k], acc);
-#pragma unroll
-        for (int t = 0; t < 21; ++t) {
-            const double v = __ldg(m + 42 + r * 21 + t);
-            if (v != 0.0) acc = __fma_rn(v, p[t], acc);
+            for (int r = 0; r < 6; ++r) {
+                double v;
+                if (coef_nz(m, 42 + r * 21 + q, v)) y[r] = __fma_rn(v, p, y[r]);
+            }
         }
-        y[r] = acc;
     }
 #pragma unroll
     for (int r = 0; r < 6; ++r) x[r] = __dadd_rn(y[r], __ldg(m + 36 + r));
+}
+
+// Maps of untilted drifts and quadrupoles without offsets (SC_SLICE_MAP_PLANAR,
+// SC_SLICE_MAP_DRIFT): their non-zero R and Tc entries lie in a fixed pattern
+// -- R in the 2x2 x and y blocks, R44, R45, R55; Tc in the chromatic terms of
+// x, px, y, py and the path-length terms of tau -- which the host checks
+// before it marks a record so.  The same FMAs as tmap2_one in the same order
+// per output, over the pattern only: no coefficient tests, 11 (drift: 5)
+// products instead of up to 21.
+__device__ __forceinline__ double mr(const double* __restrict__ m, int r, int k) { return __ldg(m + r * 6 + k); }
+__device__ __forceinline__ double mt(const double* __restrict__ m, int r, int q) { return __ldg(m + 42 + r * 21 + q); }
+
+__device__ __forceinline__ void add_b(const double* __restrict__ m, double (&y)[6], double (&x)[6]) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        double b;
+        x[r] = coef_nz(m, 36 + r, b) ? __dadd_rn(y[r], b) : y[r];
+    }
+}
+
+__device__ __forceinline__ void planar_one(const double* __restrict__ m, double (&x)[6]) {
+    const double p00 = __dmul_rn(x[0], x[0]), p01 = __dmul_rn(x[0], x[1]), p05 = __dmul_rn(x[0], x[5]);
+    const double p11 = __dmul_rn(x[1], x[1]), p15 = __dmul_rn(x[1], x[5]), p22 = __dmul_rn(x[2], x[2]);
+    const double p23 = __dmul_rn(x[2], x[3]), p25 = __dmul_rn(x[2], x[5]), p33 = __dmul_rn(x[3], x[3]);
+    const double p35 = __dmul_rn(x[3], x[5]), p55 = __dmul_rn(x[5], x[5]);
+    double y[6];
+    y[0] = __fma_rn(mr(m, 0, 1), x[1], __fma_rn(mr(m, 0, 0), x[0], 0.0));
+    y[0] = __fma_rn(mt(m, 0, 10), p15, __fma_rn(mt(m, 0, 5), p05, y[0]));
+    y[1] = __fma_rn(mr(m, 1, 1), x[1], __fma_rn(mr(m, 1, 0), x[0], 0.0));
+    y[1] = __fma_rn(mt(m, 1, 10), p15, __fma_rn(mt(m, 1, 5), p05, y[1]));
+    y[2] = __fma_rn(mr(m, 2, 3), x[3], __fma_rn(mr(m, 2, 2), x[2], 0.0));
+    y[2] = __fma_rn(mt(m, 2, 17), p35, __fma_rn(mt(m, 2, 14), p25, y[2]));
+    y[3] = __fma_rn(mr(m, 3, 3), x[3], __fma_rn(mr(m, 3, 2), x[2], 0.0));
+    y[3] = __fma_rn(mt(m, 3, 17), p35, __fma_rn(mt(m, 3, 14), p25, y[3]));
+    double a = __fma_rn(mr(m, 4, 5), x[5], __fma_rn(mr(m, 4, 4), x[4], 0.0));
+    a = __fma_rn(mt(m, 4, 6), p11, __fma_rn(mt(m, 4, 1), p01, __fma_rn(mt(m, 4, 0), p00, a)));
+    a = __fma_rn(mt(m, 4, 15), p33, __fma_rn(mt(m, 4, 12), p23, __fma_rn(mt(m, 4, 11), p22, a)));
+    y[4] = __fma_rn(mt(m, 4, 20), p55, a);
+    y[5] = __fma_rn(mr(m, 5, 5), x[5], 0.0);
+    add_b(m, y, x);
+}
+
+__device__ __forceinline__ void drift_one(const double* __restrict__ m, double (&x)[6]) {
+    const double p11 = __dmul_rn(x[1], x[1]), p15 = __dmul_rn(x[1], x[5]), p33 = __dmul_rn(x[3], x[3]);
+    const double p35 = __dmul_rn(x[3], x[5]), p55 = __dmul_rn(x[5], x[5]);
+    double y[6];
+    y[0] = __fma_rn(mt(m, 0, 10), p15, __fma_rn(mr(m, 0, 1), x[1], __fma_rn(mr(m, 0, 0), x[0], 0.0)));
+    y[1] = __fma_rn(mr(m, 1, 1), x[1], 0.0);
+    y[2] = __fma_rn(mt(m, 2, 17), p35, __fma_rn(mr(m, 2, 3), x[3], __fma_rn(mr(m, 2, 2), x[2], 0.0)));
+    y[3] = __fma_rn(mr(m, 3, 3), x[3], 0.0);
+    double a = __fma_rn(mr(m, 4, 5), x[5], __fma_rn(mr(m, 4, 4), x[4], 0.0));
+    y[4] = __fma_rn(mt(m, 4, 20), p55, __fma_rn(mt(m, 4, 15), p33, __fma_rn(mt(m, 4, 6), p11, a)));
+    y[5] = __fma_rn(mr(m, 5, 5), x[5], 0.0);
+    add_b(m, y, x);
+}
+
+// first-order maps (Tc = 0) in the R pattern of planar_one (SC_SLICE_MAP_LINEAR)
+__device__ __forceinline__ void linear_one(const double* __restrict__ m, double (&x)[6]) {
+    double y[6];
+    y[0] = __fma_rn(mr(m, 0, 1), x[1], __fma_rn(mr(m, 0, 0), x[0], 0.0));
+    y[1] = __fma_rn(mr(m, 1, 1), x[1], __fma_rn(mr(m, 1, 0), x[0], 0.0));
+    y[2] = __fma_rn(mr(m, 2, 3), x[3], __fma_rn(mr(m, 2, 2), x[2], 0.0));
+    y[3] = __fma_rn(mr(m, 3, 3), x[3], __fma_rn(mr(m, 3, 2), x[2], 0.0));
+    y[4] = __fma_rn(mr(m, 4, 5), x[5], __fma_rn(mr(m, 4, 4), x[4], 0.0));
+    y[5] = __fma_rn(mr(m, 5, 5), x[5], 0.0);
+    add_b(m, y, x);
 }
 
 // An RF cavity slice, CavityTM.map4cav (ocelot/cpbd/transformations/cavity.py:29-128):
@@ -157,13 +250,9 @@ constexpr int CAV_E = 42, CAV_BETA0 = 43, CAV_DEN = 44, CAV_A = 45, CAV_K = 46, 
 __device__ __forceinline__ void cavity_one(const double* __restrict__ m, double (&x)[6]) {
     const double x4 = x[4], x5 = x[5];
     double y[6];
+    rmul_sparse(m, x, y);
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-        double acc = __dmul_rn(__ldg(m + r * 6), x[0]);
-#pragma unroll
-        for (int k = 1; k < 6; ++k) acc = __fma_rn(__ldg(m + r * 6 + k), x[k], acc);
-        y[r] = __dadd_rn(acc, __ldg(m + 36 + r));
-    }
+    for (int r = 0; r < 6; ++r) y[r] = __dadd_rn(y[r], __ldg(m + 36 + r));
     const double t566 = __ldg(m + CAV_T566);
     if (__ldg(m + CAV_RF) != 0.0) {
         const double beta0 = __ldg(m + CAV_BETA0);
@@ -183,7 +272,8 @@ __device__ __forceinline__ void cavity_one(const double* __restrict__ m, double 
 
 // maps [first, last) of the table applied in order to every particle, its
 // coordinates kept in registers between maps; kinds (optional) marks the
-// cavity slices (SC_SLICE_CAVITY), the others are second-order maps
+// cavity slices and the maps of the fixed drift/quadrupole patterns, the
+// others are general second-order maps
 __device__ __forceinline__ void tmap2_range(const double* __restrict__ maps, const int* __restrict__ kinds, int first,
                                             int last, double* __restrict__ rp, int64_t ld, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -191,10 +281,18 @@ __device__ __forceinline__ void tmap2_range(const double* __restrict__ maps, con
 #pragma unroll
         for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
         for (int mi = first; mi < last; ++mi) {
-            if (kinds != nullptr && __ldg(kinds + mi) == SC_SLICE_CAVITY)
-                cavity_one(maps + (size_t)mi * MAP2, x);
+            const int kind = kinds != nullptr ? __ldg(kinds + mi) : SC_SLICE_MAP;
+            const double* m = maps + (size_t)mi * MAP2;
+            if (kind == SC_SLICE_MAP_DRIFT)
+                drift_one(m, x);
+            else if (kind == SC_SLICE_MAP_LINEAR)
+                linear_one(m, x);
+            else if (kind == SC_SLICE_MAP_PLANAR)
+                planar_one(m, x);
+            else if (kind == SC_SLICE_CAVITY)
+                cavity_one(m, x);
             else
-                tmap2_one(maps + (size_t)mi * MAP2, x);
+                tmap2_one(m, x);
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) rp[k * ld + i] = x[k];
@@ -307,10 +405,12 @@ __global__ void __launch_bounds__(MOM_THREADS) k_moments(const double* __restric
         } else {
             const double dx = __dsub_rn(x, o[3]), dy = __dsub_rn(y, o[4]), dpx = __dsub_rn(px, o[5]),
                          dpy = __dsub_rn(py, o[6]), dt = __dsub_rn(tau, o[7]), dp = __dsub_rn(p, o[8]);
-            acc[0] += __dmul_rn(dx, dx);    acc[1] += __dmul_rn(dx, dpx);  acc[2] += __dmul_rn(dpx, dpx);
-            acc[3] += __dmul_rn(dy, dy);    acc[4] += __dmul_rn(dy, dpy);  acc[5] += __dmul_rn(dpy, dpy);
-            acc[6] += __dmul_rn(dt, dt);    acc[7] += __dmul_rn(dx, dy);   acc[8] += __dmul_rn(dpx, dpy);
-            acc[9] += __dmul_rn(dx, dpy);   acc[10] += __dmul_rn(dy, dpx); acc[11] += __dmul_rn(dp, dp);
+            acc[0] = __fma_rn(dx, dx, acc[0]);    acc[1] = __fma_rn(dx, dpx, acc[1]);
+            acc[2] = __fma_rn(dpx, dpx, acc[2]);  acc[3] = __fma_rn(dy, dy, acc[3]);
+            acc[4] = __fma_rn(dy, dpy, acc[4]);   acc[5] = __fma_rn(dpy, dpy, acc[5]);
+            acc[6] = __fma_rn(dt, dt, acc[6]);    acc[7] = __fma_rn(dx, dy, acc[7]);
+            acc[8] = __fma_rn(dpx, dpy, acc[8]);  acc[9] = __fma_rn(dx, dpy, acc[9]);
+            acc[10] = __fma_rn(dy, dpx, acc[10]); acc[11] = __fma_rn(dp, dp, acc[11]);
         }
     }
     const int nk = pass < 2 ? 1 : (pass == 2 ? 7 : MOM_K);

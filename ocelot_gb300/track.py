@@ -374,7 +374,7 @@ def step_slices(elements, energy: float, steps, order: int = 2, s: float = 0.0):
             else:
                 R, B = element_map(e, length, E)
                 recs.append(pack_map(R, zero_t, B))
-            kinds.append(CV.SLICE_MAP)
+            kinds.append(CV.map_kind(recs[-1]))
         table = np.array(recs).reshape(-1, CV.MAP2_DOUBLES)
         out.append(StepSlices(table, np.array(kinds, dtype=np.int32), [(j, E, zstep) for j, zstep in kicks], z0, E,
                               dz))

@@ -226,4 +226,31 @@ def test_mixed_line_schedule_energies_and_positions_are_the_reference_tracks():
         s.append(0.0 + L)
     assert np.array_equal(s, MIXED["twiss"][:, keys.index("s")])
     # first-order records only: the slices carry no second-order terms
-    assert all(not st.table[st.kinds == CV.SLICE_MAP][:, 42:].any() for st in slices)
+    assert all(not st.table[st.kinds != CV.SLICE_CAVITY][:, 42:].any() for st in slices)
+
+
+def test_map_kinds_follow_the_element_patterns():
+    from ocelot_gb300.second_order import element_map2, pack_map
+    zero_t = np.zeros((6, 6, 6))
+    E = 0.05
+    drift = T.Drift(l=0.3)
+    quad = T.Quadrupole(l=0.2, k1=1.7)
+    dquad = T.Quadrupole(l=0.2, k1=-1.7)
+    tilted = T.Quadrupole(l=0.2, k1=1.7, tilt=0.1)
+    offset = T.Quadrupole(l=0.2, k1=1.7)
+    offset.dx = 1e-4
+    assert CV.map_kind(pack_map(*element_map2(drift, 0.3, E))) == CV.SLICE_MAP_DRIFT
+    assert CV.map_kind(pack_map(*element_map2(quad, 0.2, E))) == CV.SLICE_MAP_PLANAR
+    assert CV.map_kind(pack_map(*element_map2(dquad, 0.05, E))) == CV.SLICE_MAP_PLANAR
+    assert CV.map_kind(pack_map(*element_map2(tilted, 0.2, E))) == CV.SLICE_MAP
+    assert CV.map_kind(pack_map(*element_map2(offset, 0.2, E))) == CV.SLICE_MAP
+    R, B = T.element_map(quad, 0.2, E)
+    assert CV.map_kind(pack_map(R, zero_t, B)) == CV.SLICE_MAP_LINEAR
+    R, B = T.element_map(drift, 0.3, E)
+    assert CV.map_kind(pack_map(R, zero_t, B)) == CV.SLICE_MAP_LINEAR
+    cav = CV.Cavity(l=1.0, v=0.01, phi=10.0, freq=1.3e9, vxx_up=1e-3)
+    _, kinds, _ = CV.section_records(cav, 0.0, 1.0, E)
+    assert kinds == [CV.SLICE_MAP_LINEAR, CV.SLICE_CAVITY]   # vxx: R10 and R32, inside the pattern
+    cav = CV.Cavity(l=1.0, v=0.01, phi=10.0, freq=1.3e9, vxy_up=1e-3)
+    _, kinds, _ = CV.section_records(cav, 0.0, 1.0, E)
+    assert kinds == [CV.SLICE_MAP, CV.SLICE_CAVITY]          # vxy couples x and y

@@ -231,3 +231,25 @@ def test_mixed_line_first_order_matches_reference_track(graph):
     for i, t in enumerate(tws):
         assert not twiss_close(_twiss_row(t, keys), MIXED["twiss"][i], keys, rtol=1e-9, eig_rtol=1e-6,
                                derived_rtol=1e-8), i
+
+
+def test_pattern_map_forms_equal_the_general_form():
+    """The straight-line drift/quadrupole forms give the general form's
+    result bit for bit (same FMAs in the same order over the pattern)."""
+    from ocelot_gb300.second_order import element_map2, pack_map
+    E = 0.05
+    elems = [(T.Drift(l=0.3), 0.3), (T.Quadrupole(l=0.2, k1=1.7), 0.2), (T.Quadrupole(l=0.2, k1=-1.7), 0.05),
+             (T.Quadrupole(l=0.2, k1=1.7, tilt=0.1), 0.2), (T.Marker(), 0.0)]
+    recs = [pack_map(*element_map2(e, L, E)) for e, L in elems]
+    R, B = T.element_map(T.Quadrupole(l=0.2, k1=2.5), 0.2, E)
+    recs.append(pack_map(R, np.zeros((6, 6, 6)), B))
+    recs = np.array(recs)
+    kinds = [CV.map_kind(r) for r in recs]
+    assert kinds == [CV.SLICE_MAP_DRIFT, CV.SLICE_MAP_PLANAR, CV.SLICE_MAP_PLANAR, CV.SLICE_MAP,
+                     CV.SLICE_MAP_LINEAR, CV.SLICE_MAP_LINEAR]
+    rng = np.random.default_rng(7)
+    X = rng.standard_normal((6, 4099)) * np.array([1e-3, 1e-4, 1e-3, 1e-4, 1e-3, 1e-2])[:, None]
+    fast = slices_apply(recs, kinds, X)
+    general = slices_apply(recs, [CV.SLICE_MAP] * len(kinds), X)
+    assert np.array_equal(fast, general)
+    assert close_rows(fast, CV.apply_records_numpy(recs, kinds, X), 1e-13)
