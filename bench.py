@@ -408,6 +408,66 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def time_transport(n: int, steps: int, warmup: int):
+    """The tracking transport kernels alone on a seeded device beam of n
+    particles: one slice of each record form (sc_slices_apply) and the beam
+    moments (sc_moments), CUDA-event time per launch.  Prints one JSON line;
+    the launch order (per form: warmup, then steps launches) is fixed, so a
+    profiler can pick a form's last launch by its index."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from ocelot_gb300 import _native as N
+    from ocelot_gb300 import cavity as CV
+    from ocelot_gb300 import track as T
+    from ocelot_gb300.second_order import element_map2, pack_map
+    dev = torch.device("cuda", 0)
+    lib = N.lib()
+    g = torch.Generator(device=dev).manual_seed(1)
+    rp = torch.randn((6, n), generator=g, device=dev, dtype=torch.float64) * 1e-3
+    s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    E = 0.05
+    cav = CV.Cavity(l=1.0377, v=0.0195, phi=18.7, freq=1.3e9)
+    rec_c, kinds_c, _ = CV.section_records(cav, 0.3, 0.02, E)
+    rec_d = pack_map(*element_map2(T.Drift(l=0.02), 0.02, E))
+    rec_q = pack_map(*element_map2(T.Quadrupole(l=0.02, k1=1.5), 0.02, E))
+    R1, B1 = T.element_map(T.Quadrupole(l=0.02, k1=1.5), 0.02, E)
+    rec_1 = pack_map(R1, np.zeros((6, 6, 6)), B1)
+    forms = [("cavity", rec_c, list(kinds_c)),
+             ("drift_general", rec_d[None], [CV.SLICE_MAP]), ("quad_general", rec_q[None], [CV.SLICE_MAP]),
+             ("drift", rec_d[None], [CV.map_kind(rec_d)]), ("quad", rec_q[None], [CV.map_kind(rec_q)]),
+             ("quad_first_order", rec_1[None], [CV.map_kind(rec_1)])]
+    out = {"workload": f"tracking transport kernels, {n} particles (rows {48 * n / 1e6:.0f} MB; above L2 from 2.7M)",
+           "unit": "us per launch"}
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps * 1e3
+
+    for name, recs, kinds in forms:
+        maps = torch.from_numpy(np.ascontiguousarray(recs)).to(dev)
+        kd = torch.tensor(kinds, dtype=torch.int32, device=dev)
+        us = timed(lambda: N.check(lib.sc_slices_apply(C.c_void_p(maps.data_ptr()), C.c_void_p(kd.data_ptr()),
+                                                       len(kinds), C.c_void_p(rp.data_ptr()), rp.stride(0), n, s)))
+        out[name] = {"us": round(us, 2), "kinds": kinds, "rows_read_written_GBs": round(96 * n / (us * 1e-6) / 1e9, 1)}
+    mom = torch.zeros((1, 21), dtype=torch.float64, device=dev)
+    scr = torch.zeros(int(lib.sc_moments_scratch_bytes()), dtype=torch.uint8, device=dev)
+    for bounds in (0, 1):
+        us = timed(lambda: N.check(lib.sc_moments(C.c_void_p(rp.data_ptr()), rp.stride(0), n, None, 1, bounds,
+                                                  -0.5, 0.5, C.c_void_p(mom.data_ptr()), C.c_void_p(scr.data_ptr()),
+                                                  s)))
+        out["moments" + ("_bounds" if bounds else "")] = {"us": round(us, 2), "launches": 4 if bounds else 2}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -421,7 +481,12 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--kick-only", action="store_true",
                     help="time the FP32 kick alone (no other leg): the small case for profiling")
+    ap.add_argument("--transport", type=int, default=0, metavar="N",
+                    help="time the tracking transport kernels (slice forms, moments) on N particles and exit")
     args = ap.parse_args()
+    if args.transport:
+        time_transport(args.transport, args.steps, max(args.warmup, 3))
+        return
     if args.kick_only:
         args.no_cpu = args.no_fp64 = args.no_batch = args.no_serve = True
     args.warmup = max(args.warmup, 3)
