@@ -458,6 +458,16 @@ def time_transport(n: int, steps: int, warmup: int):
         us = timed(lambda: N.check(lib.sc_slices_apply(C.c_void_p(maps.data_ptr()), C.c_void_p(kd.data_ptr()),
                                                        len(kinds), C.c_void_p(rp.data_ptr()), rp.stride(0), n, s)))
         out[name] = {"us": round(us, 2), "kinds": kinds, "rows_read_written_GBs": round(96 * n / (us * 1e-6) / 1e9, 1)}
+    # the composed first-order map of the FODO tracking loop and the batched serving path (sc_tmap_apply)
+    for name, e in (("tmap_quad", T.Quadrupole(l=0.2, k1=1.5)), ("tmap_tilted_quad", T.Quadrupole(l=0.2, k1=1.5,
+                                                                                                 tilt=0.1))):
+        R, B = T.element_map(e, 0.2, E)
+        Rc = np.ascontiguousarray(R, dtype=np.float64)
+        Bc = np.ascontiguousarray(B, dtype=np.float64)
+        us = timed(lambda: N.check(lib.sc_tmap_apply(Rc.ctypes.data_as(C.POINTER(C.c_double)),
+                                                     Bc.ctypes.data_as(C.POINTER(C.c_double)),
+                                                     C.c_void_p(rp.data_ptr()), rp.stride(0), n, s)))
+        out[name] = {"us": round(us, 2), "rows_read_written_GBs": round(96 * n / (us * 1e-6) / 1e9, 1)}
     mom = torch.zeros((1, 21), dtype=torch.float64, device=dev)
     scr = torch.zeros(int(lib.sc_moments_scratch_bytes()), dtype=torch.uint8, device=dev)
     for bounds in (0, 1):

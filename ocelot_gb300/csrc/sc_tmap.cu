@@ -39,24 +39,55 @@ __device__ __forceinline__ void rmul_sparse(const double* m, const double (&x)[6
     }
 }
 
-// one particle: x <- R.x + B with m = R (row-major) then B
-__device__ __forceinline__ void tmap_one(const double* __restrict__ m, double* __restrict__ rp, int64_t ld,
-                                         int64_t i) {
+// R entries of an untilted drift/quadrupole map: the 2x2 x and y blocks, R44, R45, R55
+constexpr unsigned long long R_PLANAR = (1ull << 0) | (1ull << 1) | (1ull << 6) | (1ull << 7) | (1ull << 14) |
+                                        (1ull << 15) | (1ull << 20) | (1ull << 21) | (1ull << 28) | (1ull << 29) |
+                                        (1ull << 35);
+
+// whether every non-zero R entry of the map lies in R_PLANAR (one thread, once per block)
+__device__ __forceinline__ bool r_is_planar(const double* m) {
+    long long any = 0;
+    for (int i = 0; i < 36; ++i)
+        if (!((R_PLANAR >> i) & 1ull)) any |= reinterpret_cast<const long long*>(m)[i] << 1;
+    return any == 0;
+}
+
+// one particle: x <- R.x + B with m = R (row-major) then B; planar: R lies in
+// R_PLANAR, so only those entries are read (the same FMAs in the same order
+// as rmul_sparse over the non-zero entries)
+__device__ __forceinline__ void tmap_one(const double* m, double* __restrict__ rp, int64_t ld, int64_t i,
+                                         bool planar) {
     double x[6], y[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) x[k] = rp[k * ld + i];
-    rmul_sparse(m, x, y);
+    if (planar) {
+        y[0] = __fma_rn(m[1], x[1], __fma_rn(m[0], x[0], 0.0));
+        y[1] = __fma_rn(m[7], x[1], __fma_rn(m[6], x[0], 0.0));
+        y[2] = __fma_rn(m[15], x[3], __fma_rn(m[14], x[2], 0.0));
+        y[3] = __fma_rn(m[21], x[3], __fma_rn(m[20], x[2], 0.0));
+        y[4] = __fma_rn(m[29], x[5], __fma_rn(m[28], x[4], 0.0));
+        y[5] = __fma_rn(m[35], x[5], 0.0);
+    } else {
+        rmul_sparse(m, x, y);
+    }
+    // + B, skipping the zero offsets (the usual case): y + 0 is y
 #pragma unroll
-    for (int r = 0; r < 6; ++r) rp[r * ld + i] = __dadd_rn(y[r], m[36 + r]);
+    for (int r = 0; r < 6; ++r) {
+        double b;
+        rp[r * ld + i] = coef_nz(m, 36 + r, b) ? __dadd_rn(y[r], b) : y[r];
+    }
 }
 
 __global__ void __launch_bounds__(256) k_tmap(Map6 m, double* __restrict__ rp, int64_t ld, int64_t n) {
     pdl_wait();
     __shared__ double sm[42];
+    __shared__ bool planar;
     if (threadIdx.x < 42) sm[threadIdx.x] = m.m[threadIdx.x];
     __syncthreads();
+    if (threadIdx.x == 0) planar = r_is_planar(sm);
+    __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        tmap_one(sm, rp, ld, i);
+        tmap_one(sm, rp, ld, i, planar);
 }
 
 // batched: each beam's own map from the work table, over the beam's blocks
@@ -68,11 +99,14 @@ __global__ void __launch_bounds__(256) kb_tmap(const BatchBeam* __restrict__ bea
     const BatchBeam& B = beams[b];
     if (!B.has_tm) return;
     const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    __shared__ bool planar;
     if (threadIdx.x < 42) m[threadIdx.x] = B.tm[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) planar = r_is_planar(m);
     __syncthreads();
     const int64_t n = B.kp.n, ld = B.kp.ld;
     for (int64_t i = vb.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)vb.nx * blockDim.x)
-        tmap_one(m, B.rp, ld, i);
+        tmap_one(m, B.rp, ld, i, planar);
 }
 
 cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s) {
@@ -91,10 +125,13 @@ __global__ void __launch_bounds__(256) k_tmap_indexed(const double* __restrict__
     __shared__ double m[42];
     const int idx = *counter;
     if (idx < 0 || idx >= nmaps) return;
+    __shared__ bool planar;
     if (threadIdx.x < 42) m[threadIdx.x] = table[(size_t)idx * 42 + threadIdx.x];
     __syncthreads();
+    if (threadIdx.x == 0) planar = r_is_planar(m);
+    __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        tmap_one(m, rp, ld, i);
+        tmap_one(m, rp, ld, i, planar);
 }
 
 __global__ void k_advance(int* counter, int delta) {
