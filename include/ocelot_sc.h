@@ -252,11 +252,16 @@ int sc_tmap2_apply_step(const double* maps, const int* first, int* counter, int 
  * then from the coordinates before it
  *   x5 <- x5 E beta0 / D + A (cos(-x4 beta0 k + phi) - cos(phi)),
  *   x4 <- x4 + T566 x5^2 + T556 x4 x5 + T555 x4^2
- * with the record's doubles 42..52: E (energy at the slice start, GeV), beta0,
+ * with the record's doubles 42..55: E (energy at the slice start, GeV), beta0,
  * D = E1 beta1, A = V beta0 / D, k = 2 pi f / c, phi [rad], cos(phi), T566,
- * T556, T555, and a flag that is 0 when the energy after the slice is not
- * positive (then only the T566 term is applied and x5 keeps R.x + B).
- * The host computes the scalars in the reference's order of operations.
+ * T556, T555, a flag that is 0 when the energy after the slice is not
+ * positive (then only the T566 term is applied and x5 keeps R.x + B),
+ * RN(1/D), sin(phi), and a flag that is non-zero when R's non-zero entries lie
+ * in the x, y and longitudinal 2x2 blocks.  The host computes the scalars in
+ * the reference's order of operations; the device divides by D as a product
+ * with RN(1/D) and one FMA correction, and evaluates cos near phi as
+ * cos(phi) + cos(phi)(cos d - 1) - sin(phi) sin d (d = arg - phi, |d| <= 1/4;
+ * cos(arg) otherwise) -- within an ulp or two of the reference's values.
  *   kinds: DEVICE int32[nmaps]. */
 #define SC_SLICE_MAP 0
 #define SC_SLICE_CAVITY 1

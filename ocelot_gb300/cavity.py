@@ -16,7 +16,8 @@ The scalars are evaluated here with the reference's expressions and numpy
 functions, in its order of operations, so they are the reference's values;
 the device applies them per particle (``sc_slices_apply``, record layout in
 the C header: R, B, then E, beta0, E1 beta1, V beta0 / (E1 beta1), k, phi,
-cos(phi), T566, T556, T555 and the positive-energy flag).
+cos(phi), T566, T556, T555, the positive-energy flag, 1 / (E1 beta1), sin(phi)
+and whether R has the pattern of cavity_R_z).
 """
 from __future__ import annotations
 
@@ -55,6 +56,12 @@ _DRIFT = _pattern([(0, 0), (0, 1), (1, 1), (2, 2), (2, 3), (3, 3), (4, 4), (4, 5
                   [(0, (1, 5)), (2, (3, 5)), (4, (1, 1)), (4, (3, 3)), (4, (5, 5))])
 
 
+# the R pattern of cavity_R_z (x and y blocks, longitudinal 2x2 block)
+_CAV_R = np.zeros((6, 6), dtype=bool)
+for _r, _k in ((0, 0), (0, 1), (1, 0), (1, 1), (2, 2), (2, 3), (3, 2), (3, 3), (4, 4), (4, 5), (5, 4), (5, 5)):
+    _CAV_R[_r, _k] = True
+
+
 def map_kind(record) -> int:
     """The device form for a map record: first-order in the quadrupole
     pattern, the drift or quadrupole pattern when every non-zero entry lies
@@ -67,7 +74,8 @@ def map_kind(record) -> int:
     if not np.any(nz & ~_PLANAR):
         return SLICE_MAP_PLANAR
     return SLICE_MAP
-CAV_E, CAV_BETA0, CAV_DEN, CAV_A, CAV_K, CAV_PHI, CAV_COSPHI, CAV_T566, CAV_T556, CAV_T555, CAV_RF = range(42, 53)
+(CAV_E, CAV_BETA0, CAV_DEN, CAV_A, CAV_K, CAV_PHI, CAV_COSPHI, CAV_T566, CAV_T556, CAV_T555, CAV_RF, CAV_RDEN,
+ CAV_SINPHI, CAV_RPAT) = range(42, 56)
 
 
 class Cavity:
@@ -233,6 +241,7 @@ def slice_record(e, delta_length, energy) -> np.ndarray:
     out = np.zeros(MAP2_DOUBLES)
     out[:36] = R.reshape(-1)
     out[36:42] = B
+    out[CAV_RPAT] = 0.0 if np.any((R != 0.0) & ~_CAV_R) else 1.0
     out[CAV_T566] = T566
     if E1 <= 0.0:
         out[CAV_RF] = 0.0
@@ -264,6 +273,8 @@ def slice_record(e, delta_length, energy) -> np.ndarray:
     out[CAV_K] = k
     out[CAV_PHI] = phi
     out[CAV_COSPHI] = np.cos(phi)
+    out[CAV_SINPHI] = np.sin(phi)
+    out[CAV_RDEN] = 1.0 / (E1 * beta1)
     out[CAV_T566] = T566
     out[CAV_T556] = T556
     out[CAV_T555] = T555

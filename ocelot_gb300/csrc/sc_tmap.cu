@@ -282,20 +282,64 @@ __device__ __forceinline__ void linear_one(const double* __restrict__ m, double 
 // at CAV_*; when the energy after the slice is not positive only the T566
 // term is applied and x5 keeps its first-order value (cavity.py:67-70).
 constexpr int CAV_E = 42, CAV_BETA0 = 43, CAV_DEN = 44, CAV_A = 45, CAV_K = 46, CAV_PHI = 47, CAV_COSPHI = 48,
-              CAV_T566 = 49, CAV_T556 = 50, CAV_T555 = 51, CAV_RF = 52;
+              CAV_T566 = 49, CAV_T556 = 50, CAV_T555 = 51, CAV_RF = 52, CAV_RDEN = 53, CAV_SINPHI = 54,
+              CAV_RPAT = 55;
+
+// cos(arg) for arg = phi + d with |d| <= 1/4: cos(phi) + (cos(phi) (cos d - 1) - sin(phi) sin d), the two
+// series in d^2 (Taylor, to d^16 and d^15: truncation below 1e-22 of the result) by Horner's rule
+__device__ __forceinline__ double cos_near(double d, double cphi, double sphi) {
+    const double z = __dmul_rn(d, d);
+    double c = __fma_rn(z, -1.0 / 20922789888000.0, 1.0 / 87178291200.0);
+    c = __fma_rn(z, c, -1.0 / 479001600.0);
+    c = __fma_rn(z, c, 1.0 / 3628800.0);
+    c = __fma_rn(z, c, -1.0 / 40320.0);
+    c = __fma_rn(z, c, 1.0 / 720.0);
+    c = __fma_rn(z, c, -1.0 / 24.0);
+    c = __fma_rn(z, c, 0.5);
+    const double cm1 = -__dmul_rn(z, c);            // cos d - 1
+    double s = __fma_rn(z, -1.0 / 1307674368000.0, 1.0 / 6227020800.0);
+    s = __fma_rn(z, s, -1.0 / 39916800.0);
+    s = __fma_rn(z, s, 1.0 / 362880.0);
+    s = __fma_rn(z, s, -1.0 / 5040.0);
+    s = __fma_rn(z, s, 1.0 / 120.0);
+    s = __fma_rn(z, s, -1.0 / 6.0);
+    const double sd = __fma_rn(__dmul_rn(z, d), s, d);   // sin d
+    return __dadd_rn(cphi, __fma_rn(cphi, cm1, -__dmul_rn(sphi, sd)));
+}
 
 __device__ __forceinline__ void cavity_one(const double* __restrict__ m, double (&x)[6]) {
     const double x4 = x[4], x5 = x[5];
+    // R: when the host found it in the pattern of cavity_R_z (x and y blocks, longitudinal 2x2 block; untilted),
+    // those 12 entries in k order per output, else the general sparse product -- the same FMAs either way
     double y[6];
-    rmul_sparse(m, x, y);
+    if (__ldg(reinterpret_cast<const long long*>(m) + CAV_RPAT) != 0) {
+        y[0] = __fma_rn(mr(m, 0, 1), x[1], __fma_rn(mr(m, 0, 0), x[0], 0.0));
+        y[1] = __fma_rn(mr(m, 1, 1), x[1], __fma_rn(mr(m, 1, 0), x[0], 0.0));
+        y[2] = __fma_rn(mr(m, 2, 3), x[3], __fma_rn(mr(m, 2, 2), x[2], 0.0));
+        y[3] = __fma_rn(mr(m, 3, 3), x[3], __fma_rn(mr(m, 3, 2), x[2], 0.0));
+        y[4] = __fma_rn(mr(m, 4, 5), x[5], __fma_rn(mr(m, 4, 4), x[4], 0.0));
+        y[5] = __fma_rn(mr(m, 5, 5), x[5], __fma_rn(mr(m, 5, 4), x[4], 0.0));
+    } else {
+        rmul_sparse(m, x, y);
+    }
 #pragma unroll
-    for (int r = 0; r < 6; ++r) y[r] = __dadd_rn(y[r], __ldg(m + 36 + r));
+    for (int r = 0; r < 6; ++r) {
+        double b;
+        if (coef_nz(m, 36 + r, b)) y[r] = __dadd_rn(y[r], b);
+    }
     const double t566 = __ldg(m + CAV_T566);
     if (__ldg(m + CAV_RF) != 0.0) {
         const double beta0 = __ldg(m + CAV_BETA0);
-        const double lin = __ddiv_rn(__dmul_rn(__dmul_rn(x5, __ldg(m + CAV_E)), beta0), __ldg(m + CAV_DEN));
-        const double arg = __dadd_rn(__dmul_rn(__dmul_rn(-x4, beta0), __ldg(m + CAV_K)), __ldg(m + CAV_PHI));
-        y[5] = __dadd_rn(lin, __dmul_rn(__ldg(m + CAV_A), __dsub_rn(cos(arg), __ldg(m + CAV_COSPHI))));
+        // a / D by a product with y = RN(1/D) and one correction, q + (a - qD) y (Markstein's division)
+        const double a = __dmul_rn(__dmul_rn(x5, __ldg(m + CAV_E)), beta0);
+        const double den = __ldg(m + CAV_DEN), rden = __ldg(m + CAV_RDEN);
+        const double q = __dmul_rn(a, rden);
+        const double lin = __fma_rn(__fma_rn(-q, den, a), rden, q);
+        const double phi = __ldg(m + CAV_PHI), cphi = __ldg(m + CAV_COSPHI);
+        const double arg = __dadd_rn(__dmul_rn(__dmul_rn(-x4, beta0), __ldg(m + CAV_K)), phi);
+        const double d = __dsub_rn(arg, phi);
+        const double c = fabs(d) <= 0.25 ? cos_near(d, cphi, __ldg(m + CAV_SINPHI)) : cos(arg);
+        y[5] = __dadd_rn(lin, __dmul_rn(__ldg(m + CAV_A), __dsub_rn(c, cphi)));
         const double s = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(t566, x5), x5),
                                              __dmul_rn(__dmul_rn(__ldg(m + CAV_T556), x4), x5)),
                                    __dmul_rn(__dmul_rn(__ldg(m + CAV_T555), x4), x4));
