@@ -176,7 +176,7 @@ cudaError_t launch_tmap(const double* R, const double* B, double* rp, int64_t ld
 // with Tc the combined coefficient T[i,j,k] + T[i,k,j] (j < k) or T[i,j,j].
 // A map is MAP2 doubles: R (row-major), B, then Tc[6][21] with the pairs
 // (j, k), j <= k, in lexicographic order.  Every thread reads the same map
-// entries, so the test that skips a zero coefficient is warp-uniform.
+// entries, so the tests that skip a zero coefficient (coef_nz) are warp-uniform.
 // ---------------------------------------------------------------------------
 constexpr int MAP2 = 36 + 6 + 6 * 21;
 
