@@ -259,6 +259,11 @@ static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energ
     kp.mesh_shift = mesh_shift;
     kp.m_e_eV = c.m_e_eV;
     kp.m2 = pow(c.m_e_eV, 2.0);
+    kp.r_gamref = 1.0 / kp.gamref;
+    kp.r_betaref = 1.0 / kp.betaref;
+    kp.r_pref = 1.0 / kp.pref;
+    kp.r_grbr = 1.0 / kp.grbr;
+    kp.r_m2 = 1.0 / kp.m2;
     kp.four_pi_eps0 = 4 * c.pi * c.epsilon_0;
     kp.phi_norm = 1.0 / ((double)kp.Mx * (double)kp.My * (double)kp.Mz);
     kp.gamref_f = (float)kp.gamref;

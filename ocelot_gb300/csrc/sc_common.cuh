@@ -101,6 +101,8 @@ struct KickParams {
     int nx, ny, nz;
     int Mx, My, Mz;
     double gamref, betaref, pref, grbr;  // grbr = gamref*betaref
+    // RN(1/x) of the four above and of m2, for correctly rounded division by them (Markstein)
+    double r_gamref, r_betaref, r_pref, r_grbr, r_m2;
     double cdT;                          // zstep / betref
     double mesh_scale, mesh_shift;       // NaN when unused
     double m_e_eV, m2;                   // m_e_eV and m_e_eV**2

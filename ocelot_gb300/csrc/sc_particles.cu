@@ -210,17 +210,28 @@ constexpr int PART_EXT = 11;
 // ---------------------------------------------------------------------------
 // FP64 transforms in the reference's operation order
 // ---------------------------------------------------------------------------
+// a / b, correctly rounded, from rb = RN(1/b): q = RN(a rb), then
+// RN(q + (a - q b) rb) with the residual exact in one FMA (Markstein's
+// theorem: the result is RN(a/b) when rb = RN(1/b), away from overflow and
+// underflow).  Three FP64 instructions instead of a division, which this GPU
+// issues on its narrow FP64 pipe as a dozen.
+__device__ __forceinline__ double div_rb(double a, double b, double rb) {
+    const double q = __dmul_rn(a, rb);
+    return __fma_rn(__fma_rn(-q, b, a), rb, q);
+}
+
 // xxstg_2_xp_mad (coord_transform.py:57-96)
 __device__ __forceinline__ void mad_to_cart64(const double r[6], const KickParams& kp, double xp[6]) {
     const double gamma = __dmul_rn(__dadd_rn(__dmul_rn(kp.betaref, r[5]), 1.0), kp.gamref);
     const double beta = __dsqrt_rn(__dsub_rn(1.0, __drcp_rn(__dmul_rn(gamma, gamma))));
-    const double g = __ddiv_rn(__dmul_rn(gamma, beta), kp.grbr);
+    const double g = div_rb(__dmul_rn(gamma, beta), kp.grbr, kp.r_grbr);
     const double pz2pref = __dsqrt_rn(__dsub_rn(__dsub_rn(__dmul_rn(g, g), __dmul_rn(r[1], r[1])), __dmul_rn(r[3], r[3])));
-    double u0 = __ddiv_rn(r[1], pz2pref), u1 = __ddiv_rn(r[3], pz2pref);
+    const double rpz = __drcp_rn(pz2pref);
+    double u0 = div_rb(r[1], pz2pref, rpz), u1 = div_rb(r[3], pz2pref, rpz);
     const double nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(u0, u0), __dmul_rn(u1, u1)), 1.0));
-    u0 = __ddiv_rn(u0, nrm);
-    u1 = __ddiv_rn(u1, nrm);
-    const double u2 = __ddiv_rn(1.0, nrm);
+    const double u2 = __drcp_rn(nrm);  // 1.0 / nrm
+    u0 = div_rb(u0, nrm, u2);
+    u1 = div_rb(u1, nrm, u2);
     xp[0] = __dsub_rn(r[0], __dmul_rn(__dmul_rn(u0, beta), r[4]));
     xp[1] = __dsub_rn(r[2], __dmul_rn(__dmul_rn(u1, beta), r[4]));
     xp[2] = __dmul_rn(__dmul_rn(-u2, beta), r[4]);
@@ -233,17 +244,18 @@ __device__ __forceinline__ void mad_to_cart64(const double r[6], const KickParam
 __device__ __forceinline__ void cart_to_mad64(const double pos[3], const double p[3], const KickParams& kp,
                                               double r[6]) {
     const double s = __dadd_rn(__dadd_rn(__dmul_rn(p[0], p[0]), __dmul_rn(p[1], p[1])), __dmul_rn(p[2], p[2]));
-    const double gamma = __dsqrt_rn(__dadd_rn(1.0, __ddiv_rn(s, kp.m2)));
+    const double gamma = __dsqrt_rn(__dadd_rn(1.0, div_rb(s, kp.m2, kp.r_m2)));
     const double beta = __dsqrt_rn(__dsub_rn(1.0, __drcp_rn(__dmul_rn(gamma, gamma))));
     const double p0 = __dsqrt_rn(s);
-    const double u0 = __ddiv_rn(p[0], p0), u1 = __ddiv_rn(p[1], p0), u2 = __ddiv_rn(p[2], p0);
+    const double rp0 = __drcp_rn(p0);
+    const double u0 = div_rb(p[0], p0, rp0), u1 = div_rb(p[1], p0, rp0), u2 = div_rb(p[2], p0, rp0);
     const double cdt = __ddiv_rn(-pos[2], __dmul_rn(beta, u2));
     r[0] = __dadd_rn(pos[0], __dmul_rn(__dmul_rn(beta, u0), cdt));
     r[2] = __dadd_rn(pos[1], __dmul_rn(__dmul_rn(beta, u1), cdt));
-    r[5] = __ddiv_rn(__dsub_rn(__ddiv_rn(gamma, kp.gamref), 1.0), kp.betaref);
+    r[5] = div_rb(__dsub_rn(div_rb(gamma, kp.gamref, kp.r_gamref), 1.0), kp.betaref, kp.r_betaref);
     r[4] = cdt;
-    r[1] = __ddiv_rn(p[0], kp.pref);
-    r[3] = __ddiv_rn(p[1], kp.pref);
+    r[1] = div_rb(p[0], kp.pref, kp.r_pref);
+    r[3] = div_rb(p[1], kp.pref, kp.r_pref);
 }
 
 // numpy's [N,3]@[3,3] row product: fma(a2,b2, fma(a1,b1, a0*b0))
@@ -1371,6 +1383,9 @@ __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickPar
     st->stepsf[0] = (float)hx;
     st->stepsf[1] = (float)hy;
     st->stepsf[2] = (float)hz;
+    st->isteps[0] = __ddiv_rn(1.0, hx);
+    st->isteps[1] = __ddiv_rn(1.0, hy);
+    st->isteps[2] = __ddiv_rn(1.0, hz);
     st->phi_denom = __dmul_rn(__dmul_rn(__dmul_rn(kp.four_pi_eps0, hx), hy), hz);
     st->phi_scalef = (float)(kp.phi_norm / st->phi_denom);
     st->phi_norm = kp.phi_norm;
@@ -1398,13 +1413,15 @@ __global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t*
     if (st->status) return;
     const int64_t n = kp.n;
     const double s0 = st->steps[0], s1 = st->steps[1], s2 = st->steps[2];
+    // isteps = RN(1/steps): the quotients below are the correctly rounded X / steps (div_rb)
+    const double r0 = st->isteps[0], r1 = st->isteps[1], r2 = st->isteps[2];
     const double o0 = st->xoff[0], o1 = st->xoff[1], o2 = st->xoff[2];
     bool bad = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t nX = kp.nX;
-        const double g0 = __dsub_rn(__ddiv_rn(X[i], s0), o0);
-        const double g1 = __dsub_rn(__ddiv_rn(X[nX + i], s1), o1);
-        const double g2 = __dsub_rn(__ddiv_rn(X[2 * nX + i], s2), o2);
+        const double g0 = __dsub_rn(div_rb(X[i], s0, r0), o0);
+        const double g1 = __dsub_rn(div_rb(X[nX + i], s1, r1), o1);
+        const double g2 = __dsub_rn(div_rb(X[2 * nX + i], s2, r2), o2);
         uint32_t key;
         bad |= !key_of(floor(g0) + 1, floor(g1) + 1, floor(g2) + 1, kp, key);
         keys[i] = key;
