@@ -291,8 +291,8 @@ int sc_slices_apply_step(const double* maps, const int* kinds, const int* first,
  *   [3..8] means of x, y, px', py', tau, p, [9..20] central moments xx, xpx, pxpx, yy, ypy, pypy, tautau,
  *   xy, pxpy, xpy, ypx, pp, with px' = px f, py' = py f, f = 1 - p - p^2/2 + px^2/2 + py^2/2.
  * use_bounds: only the particles with m + lo s <= tau <= m + hi s count (get_envelope's bounds, in units of
- * the standard deviation s of tau around its mean m).  Two launches (four with bounds); the sums are
- * deterministic.  scratch: DEVICE, sc_moments_scratch_bytes() bytes, zero-filled once before the first call,
+ * the standard deviation s of tau around its mean m).  One launch (two with bounds): sums shifted by the
+ * first particle's values, so the central moments carry no cancellation; the sums are deterministic.  scratch: DEVICE, sc_moments_scratch_bytes() bytes, zero-filled once before the first call,
  * not shared by concurrent calls. */
 #define SC_MOMENTS 21
 int64_t sc_moments_scratch_bytes(void);

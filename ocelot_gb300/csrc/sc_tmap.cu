@@ -431,21 +431,29 @@ namespace ocsc {
 // central second moments, with px' = px f, py' = py f,
 // f = 1 - p - p^2/2 + px^2/2 + py^2/2, over all particles or over those with
 // tau within [m + lo s, m + hi s] (m, s: mean and standard deviation of tau).
-// Two passes over the rows (four with bounds), each one launch: every block
-// reduces its grid-stride share, writes its partial sums, and the last block
-// to finish (a ticket) adds the partials in block order -- so the sums are
-// deterministic -- and writes the slot *counter of the output table.
+// One pass over the rows (two with bounds: the tau statistics first): the
+// sums of d = v - v0 and of the products d_v d_w, shifted by the first
+// particle's values v0, give mean = v0 + S1/n and central moment
+// S2/n - (S1/n)(S1/n) -- the shift keeps the subtraction free of
+// cancellation for any beam offset.  Each pass is one launch: every block
+// reduces its grid-stride share and writes its partial sums, and the last
+// block to finish (a ticket) adds the partials in block order -- so the sums
+// are deterministic -- and writes the slot *counter of the output table.
 // ---------------------------------------------------------------------------
-constexpr int MOM_BLOCKS = 304, MOM_THREADS = 256, MOM_K = 12;
+constexpr int MOM_BLOCKS = 304, MOM_THREADS = 256, MOM_K = 19;
 
-struct MomSlot {
-    double* v;  // SC_MOMENTS doubles
-};
-
-__device__ __forceinline__ double mom_factor(double px, double py, double p) {
-    return __dadd_rn(__dadd_rn(__dsub_rn(__dsub_rn(1.0, p), __dmul_rn(__dmul_rn(0.5, p), p)),
-                               __dmul_rn(__dmul_rn(0.5, px), px)),
-                     __dmul_rn(__dmul_rn(0.5, py), py));
+__device__ __forceinline__ void mom_prime(const double* __restrict__ X, int64_t ld, int64_t i, double (&v)[6]) {
+    // x, y, px', py', tau, p of particle i (the factor with get_envelope's operations, as FMAs)
+    const double px = X[ld + i], py = X[3 * ld + i], p = X[5 * ld + i];
+    double f = __fma_rn(-__dmul_rn(0.5, p), p, __dsub_rn(1.0, p));
+    f = __fma_rn(__dmul_rn(0.5, px), px, f);
+    f = __fma_rn(__dmul_rn(0.5, py), py, f);
+    v[0] = X[i];
+    v[1] = X[2 * ld + i];
+    v[2] = __dmul_rn(px, f);
+    v[3] = __dmul_rn(py, f);
+    v[4] = X[4 * ld + i];
+    v[5] = p;
 }
 
 __global__ void __launch_bounds__(MOM_THREADS) k_moments(const double* __restrict__ rp, int64_t ld, int64_t n,
@@ -459,43 +467,41 @@ __global__ void __launch_bounds__(MOM_THREADS) k_moments(const double* __restric
     double acc[MOM_K];
 #pragma unroll
     for (int k = 0; k < MOM_K; ++k) acc[k] = 0.0;
+    double v0[6];
+    mom_prime(rp, ld, 0, v0);
     double tlo = -INFINITY, thi = INFINITY;
-    if (pass >= 2 && use_bounds) {
+    if (pass == 1 && use_bounds) {
         tlo = __dadd_rn(o[1], __dmul_rn(o[2], lo));
         thi = __dadd_rn(o[1], __dmul_rn(o[2], hi));
     }
-    const double* X = rp;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double tau = X[4 * ld + i];
+        const double tau = rp[4 * ld + i];
         if (pass == 0) {
-            acc[0] += tau;
-            continue;
-        }
-        if (pass == 1) {
-            const double d = __dsub_rn(tau, o[1]);
-            acc[0] += __dmul_rn(d, d);
+            const double d = __dsub_rn(tau, v0[4]);
+            acc[0] += d;
+            acc[1] = __fma_rn(d, d, acc[1]);
             continue;
         }
         if (!(tlo <= tau && tau <= thi)) continue;
-        const double x = X[i], y = X[2 * ld + i], p = X[5 * ld + i];
-        const double f = mom_factor(X[ld + i], X[3 * ld + i], p);
-        const double px = __dmul_rn(X[ld + i], f), py = __dmul_rn(X[3 * ld + i], f);
-        if (pass == 2) {
-            acc[0] += 1.0;
-            acc[1] += x; acc[2] += y; acc[3] += px; acc[4] += py; acc[5] += tau; acc[6] += p;
-        } else {
-            const double dx = __dsub_rn(x, o[3]), dy = __dsub_rn(y, o[4]), dpx = __dsub_rn(px, o[5]),
-                         dpy = __dsub_rn(py, o[6]), dt = __dsub_rn(tau, o[7]), dp = __dsub_rn(p, o[8]);
-            acc[0] = __fma_rn(dx, dx, acc[0]);    acc[1] = __fma_rn(dx, dpx, acc[1]);
-            acc[2] = __fma_rn(dpx, dpx, acc[2]);  acc[3] = __fma_rn(dy, dy, acc[3]);
-            acc[4] = __fma_rn(dy, dpy, acc[4]);   acc[5] = __fma_rn(dpy, dpy, acc[5]);
-            acc[6] = __fma_rn(dt, dt, acc[6]);    acc[7] = __fma_rn(dx, dy, acc[7]);
-            acc[8] = __fma_rn(dpx, dpy, acc[8]);  acc[9] = __fma_rn(dx, dpy, acc[9]);
-            acc[10] = __fma_rn(dy, dpx, acc[10]); acc[11] = __fma_rn(dp, dp, acc[11]);
-        }
+        double v[6];
+        mom_prime(rp, ld, i, v);
+        double d[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) d[k] = __dsub_rn(v[k], v0[k]);
+        acc[0] += 1.0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[1 + k] += d[k];
+        // xx, xpx, pxpx, yy, ypy, pypy, tautau, xy, pxpy, xpy, ypx, pp (d: x, y, px, py, tau, p)
+        acc[7] = __fma_rn(d[0], d[0], acc[7]);    acc[8] = __fma_rn(d[0], d[2], acc[8]);
+        acc[9] = __fma_rn(d[2], d[2], acc[9]);    acc[10] = __fma_rn(d[1], d[1], acc[10]);
+        acc[11] = __fma_rn(d[1], d[3], acc[11]);  acc[12] = __fma_rn(d[3], d[3], acc[12]);
+        acc[13] = __fma_rn(d[4], d[4], acc[13]);  acc[14] = __fma_rn(d[0], d[1], acc[14]);
+        acc[15] = __fma_rn(d[2], d[3], acc[15]);  acc[16] = __fma_rn(d[0], d[3], acc[16]);
+        acc[17] = __fma_rn(d[1], d[2], acc[17]);  acc[18] = __fma_rn(d[5], d[5], acc[18]);
     }
-    const int nk = pass < 2 ? 1 : (pass == 2 ? 7 : MOM_K);
+    const int nk = pass == 0 ? 2 : MOM_K;
     __shared__ double s_red[MOM_THREADS / 32][MOM_K];
+    __shared__ double s_sum[MOM_K];
     __shared__ bool s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -521,24 +527,29 @@ __global__ void __launch_bounds__(MOM_THREADS) k_moments(const double* __restric
     if (threadIdx.x < nk) {
         double v = 0.0;
         for (unsigned b = 0; b < gridDim.x; ++b) v += __ldcg(partial + (size_t)b * MOM_K + threadIdx.x);
-        if (pass == 0) {
-            o[1] = v / (double)n;
-        } else if (pass == 1) {
-            o[2] = sqrt(v / (double)n);
-        } else if (pass == 2) {
-            o[threadIdx.x == 0 ? 0 : 2 + threadIdx.x] = v;  // count, then the six sums (divided below)
-        } else {
-            o[9 + threadIdx.x] = v;
-        }
+        s_sum[threadIdx.x] = v;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        if (pass == 2) {
-            const double cnt = o[0];
-            for (int k = 3; k < 9; ++k) o[k] = o[k] / cnt;
-        } else if (pass == 3) {
-            const double cnt = o[0];
-            for (int k = 9; k < 21; ++k) o[k] = o[k] / cnt;
+        if (pass == 0) {
+            const double m1 = s_sum[0] / (double)n;
+            o[1] = __dadd_rn(v0[4], m1);
+            o[2] = sqrt(fmax(__fma_rn(-m1, m1, s_sum[1] / (double)n), 0.0));
+        } else {
+            const double cnt = s_sum[0];
+            o[0] = cnt;
+            double m1[6];
+            for (int k = 0; k < 6; ++k) {
+                m1[k] = s_sum[1 + k] / cnt;
+                o[3 + k] = __dadd_rn(v0[k], m1[k]);
+            }
+            const int a[12] = {0, 0, 2, 1, 1, 3, 4, 0, 2, 0, 1, 5};
+            const int b[12] = {0, 2, 2, 1, 3, 3, 4, 1, 3, 3, 2, 5};
+            for (int k = 0; k < 12; ++k) {
+                double c = __fma_rn(-m1[a[k]], m1[b[k]], s_sum[7 + k] / cnt);
+                if (a[k] == b[k]) c = fmax(c, 0.0);   // a variance: not below 0 by rounding
+                o[9 + k] = cnt == 1.0 ? 0.0 : c;      // one particle: no spread, exactly
+            }
         }
         *ticket = 0u;
     }
@@ -550,7 +561,7 @@ cudaError_t launch_moments(const double* rp, int64_t ld, int64_t n, const int* c
     unsigned int* ticket = (unsigned int*)(partial + (size_t)MOM_BLOCKS * MOM_K);
     int64_t b = (n + MOM_THREADS - 1) / MOM_THREADS;
     const int blocks = (int)(b < 1 ? 1 : (b > MOM_BLOCKS ? MOM_BLOCKS : b));
-    for (int pass = use_bounds ? 0 : 2; pass < 4; ++pass)
+    for (int pass = use_bounds ? 0 : 1; pass < 2; ++pass)
         launch(k_moments, blocks, MOM_THREADS, 0, s, rp, ld, n, counter, nslots, pass, use_bounds, lo, hi, out,
                partial, ticket);
     return cudaGetLastError();

@@ -2,8 +2,8 @@
 
 The reference's track() calls get_envelope after every step
 (ocelot/cpbd/track.py:466-486, ocelot/cpbd/beam/analysis.py:27-226).  On the
-device the moments are taken by ``sc_moments`` (two passes over the rows of
-rparticles, four with bounds) into a table with one slot per step; this module
+device the moments are taken by ``sc_moments`` (one pass over the rows of
+rparticles, two with bounds) into a table with one slot per step; this module
 turns a slot into a ``Twiss`` with get_envelope's derived quantities:
 emittances sqrt(<xx><px px> - <x px>^2), normalised by gamma beta of the beam
 energy, beta = <xx>/emit, alpha = -<x px>/emit, and the two eigen-emittances of
@@ -97,8 +97,9 @@ def twiss_from_moments(m, energy: float, charge: float, s: float = 0.0) -> Twiss
 
 
 def moments_numpy(rp: np.ndarray, bounds=None) -> np.ndarray:
-    """One slot of the moments table computed on the host (the same sums as
-    the device passes, in numpy; a check of the device table)."""
+    """One slot of the moments table computed on the host with get_envelope's
+    two numpy passes (means, then central moments): a check of the device
+    table, which takes shifted sums in one pass."""
     rp = np.asarray(rp, dtype=np.float64)
     out = np.zeros(MOMENTS)
     tau = rp[4]

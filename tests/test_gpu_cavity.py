@@ -167,7 +167,16 @@ def test_moments_match_host(n, bounds):
         return                  # no particle within the bounds: the means are 0/0 in both
     scale = np.sqrt(np.abs(ref[[9, 12, 9, 12, 15, 20]])) + 1e-300
     assert (np.abs(dev[3:9] - ref[3:9]) <= 1e-12 * np.abs(rp).max(axis=1)[[0, 2, 1, 3, 4, 5]] + 1e-14 * scale).all()
-    assert (np.abs(dev[9:21] - ref[9:21]) <= 1e-12 * np.abs(ref[9:21]) + 1e-300).all()
+    # second moments within 1e-12 of the product of the two rms sizes (for a variance: of itself); the
+    # correlations of an uncorrelated beam are near zero, so a purely relative bound would test rounding
+    var = {0: ref[9], 1: ref[12], 2: ref[11], 3: ref[14], 4: ref[15], 5: ref[20]}
+    pairs = [(0, 0), (0, 2), (2, 2), (1, 1), (1, 3), (3, 3), (4, 4), (0, 1), (2, 3), (0, 3), (1, 2), (5, 5)]
+    scale2 = np.array([np.sqrt(abs(var[a] * var[b])) for a, b in pairs])
+    if ref[0] < 3:
+        # get_envelope takes no moments of fewer than 3 particles; the spread of the whole beam is the scale
+        rms = rp.std(axis=1)[[0, 2, 1, 3, 4, 5]]
+        scale2 = np.array([rms[a] * rms[b] for a, b in pairs])
+    assert (np.abs(dev[9:21] - ref[9:21]) <= 1e-12 * scale2 + 1e-300).all()
     if bounds is not None:
         assert abs(dev[1] - ref[1]) <= 1e-14 * abs(ref[2]) and abs(dev[2] - ref[2]) <= 1e-13 * ref[2]
 
