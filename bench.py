@@ -76,8 +76,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_{os.getpid()}.csv") if os.path.isdir(
-            os.path.join(REPO, "gpurun_out")) else f"/tmp/clocks_{os.getpid()}.csv"
+        # the raw samples go to OCELOT_SC_CLOCKS_DIR when set (the summary is in the JSON line either way)
+        self.path = os.path.join(os.environ.get("OCELOT_SC_CLOCKS_DIR", "/tmp"), f"clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
