@@ -1575,10 +1575,37 @@ __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_
 // trilinear gather, scipy.ndimage.map_coordinates(order=1, mode='constant')
 // semantics: a sample outside [0, n-1] in any axis is 0
 // ---------------------------------------------------------------------------
+// FP64: whether 0 <= c <= hi (c = -0.0 included, NaN excluded) and floor(c)
+// for such c, both on the bit pattern: the order of non-negative doubles is
+// the order of their bits, and the integer part is the significand shifted
+// by the exponent.  Equal to the double compares and floor(), without the
+// FP64 pipe, which this GPU issues at a fraction of its integer rate.
+__device__ __forceinline__ bool in_range64(double c, double hi) {
+    const long long b = __double_as_longlong(c);
+    return (b >= 0 || b == (long long)0x8000000000000000ull) && b <= __double_as_longlong(hi);
+}
+__device__ __forceinline__ int floor_nonneg64(double c) {  // 0 <= c < 2^31
+    const long long b = __double_as_longlong(c);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e < 0) return 0;
+    const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    return (int)(m >> (52 - e));
+}
+
 template <typename R>
 __device__ __forceinline__ R trilerp(const R* __restrict__ F, int nx, int ny, int nz, R c0, R c1, R c2) {
-    if (!(c0 >= 0) || !(c1 >= 0) || !(c2 >= 0) || c0 > nx - 1 || c1 > ny - 1 || c2 > nz - 1) return 0;
-    int i = (int)floor(c0), j = (int)floor(c1), k = (int)floor(c2);
+    int i, j, k;
+    if constexpr (sizeof(R) == 8) {
+        if (!in_range64(c0, nx - 1) || !in_range64(c1, ny - 1) || !in_range64(c2, nz - 1)) return 0;
+        i = floor_nonneg64(c0);
+        j = floor_nonneg64(c1);
+        k = floor_nonneg64(c2);
+    } else {
+        if (!(c0 >= 0) || !(c1 >= 0) || !(c2 >= 0) || c0 > nx - 1 || c1 > ny - 1 || c2 > nz - 1) return 0;
+        i = (int)floor(c0);
+        j = (int)floor(c1);
+        k = (int)floor(c2);
+    }
     if (i > nx - 2) i = nx - 2;
     if (j > ny - 2) j = ny - 2;
     if (k > nz - 2) k = nz - 2;
