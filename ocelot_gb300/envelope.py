@@ -120,3 +120,44 @@ def moments_numpy(rp: np.ndarray, bounds=None) -> np.ndarray:
     out[9:21] = [np.mean(a * b) for a, b in ((dx, dx), (dx, dpx), (dpx, dpx), (dy, dy), (dy, dpy), (dpy, dpy),
                                               (dt, dt), (dx, dy), (dpx, dpy), (dx, dpy), (dy, dpx), (dp, dp))]
     return out
+
+
+def get_envelope(p_array, tws_i=None, bounds=None, slice=None, auto_disp=False):
+    """Twiss of a beam from its moments, taken on the GPU: the reference's
+    get_envelope (ocelot/cpbd/beam/analysis.py:27-226) for a ParticleArray or
+    DeviceParticleArray (host particles are copied to the device once).
+    Dispersion correction (``tws_i``, ``auto_disp``) and the maximum-current
+    reference slice (``slice``) are not supported."""
+    import ctypes as C
+
+    import torch
+
+    from . import _native as N
+    from .beam import DeviceParticleArray
+    if tws_i is not None or auto_disp or slice is not None:
+        raise NotImplementedError("get_envelope on the device: no dispersion correction and no reference slice")
+    if isinstance(p_array, DeviceParticleArray):
+        rp, q = p_array.rparticles, p_array.q_array
+        dev = rp.device
+    else:
+        if not torch.cuda.is_available():
+            raise N.NativeLibraryError("ocelot_gb300 needs a CUDA device; there is no CPU fallback")
+        dev = torch.device("cuda", torch.cuda.current_device())
+        rp = torch.from_numpy(np.ascontiguousarray(p_array.rparticles, dtype=np.float64)).to(dev)
+        q = np.asarray(p_array.q_array, dtype=np.float64)
+    n = int(rp.shape[1])
+    if n < 1:
+        raise ValueError("zero-size array")
+    if rp.dtype != torch.float64 or rp.stride(1) != 1:
+        raise ValueError("rparticles must be float64 with contiguous rows")
+    lib = N.lib()
+    out = torch.zeros((1, MOMENTS), dtype=torch.float64, device=dev)
+    scratch = torch.zeros(int(lib.sc_moments_scratch_bytes()), dtype=torch.uint8, device=dev)
+    lo, hi = (float(bounds[0]), float(bounds[1])) if bounds is not None else (0.0, 0.0)
+    with torch.cuda.device(dev):
+        s = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        N.check(lib.sc_moments(C.c_void_p(rp.data_ptr()), rp.stride(0), n, None, 1, 1 if bounds is not None else 0,
+                               lo, hi, C.c_void_p(out.data_ptr()), C.c_void_p(scratch.data_ptr()), s))
+        m = out[0].cpu().numpy()
+    charge = float(np.sum(q.cpu().numpy() if isinstance(q, torch.Tensor) else q))
+    return twiss_from_moments(m, float(p_array.E), charge, 0.0)

@@ -262,3 +262,26 @@ def test_pattern_map_forms_equal_the_general_form():
     general = slices_apply(recs, [CV.SLICE_MAP] * len(kinds), X)
     assert np.array_equal(fast, general)
     assert close_rows(fast, CV.apply_records_numpy(recs, kinds, X), 1e-13)
+
+
+@pytest.mark.parametrize("bounds", [None, [-0.5, 0.5]])
+def test_get_envelope_matches_reference(bounds):
+    """get_envelope on the device, for a host and a device beam, against the
+    reference's get_envelope of the same beam (the last row of the twiss list
+    its track() returned)."""
+    from ocelot_gb300.beam import DeviceParticleArray
+    from ocelot_gb300.envelope import get_envelope
+    from test_cavity_host import _twiss_row, twiss_close
+    keys = [str(k) for k in LINE["twiss_keys"]]
+    table = LINE["twiss"] if bounds is None else LINE["twiss_bounds"]
+    pa = ParticleArray(LINE["rp_end"].shape[1])
+    pa.rparticles[:] = LINE["rp_end"]
+    pa.q_array = LINE["q"].copy()
+    pa.E = float(LINE["E_end"])
+    ref = table[-1].copy()
+    ref[keys.index("s")] = 0.0        # get_envelope leaves s at 0; track() adds the position
+    for beam in (pa, DeviceParticleArray.from_host(pa, torch.device("cuda", 0))):
+        t = get_envelope(beam, bounds=bounds)
+        assert not twiss_close(_twiss_row(t, keys), ref, keys, rtol=1e-12, eig_rtol=1e-8, derived_rtol=1e-11)
+    with pytest.raises(NotImplementedError):
+        get_envelope(pa, auto_disp=True)
