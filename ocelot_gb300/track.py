@@ -440,8 +440,8 @@ class DeviceTrack:
         else:
             processes = [(p, int(a), int(b)) for p, a, b in processes]
             whole = len(processes) == 1 and processes[0][1] == 0 and processes[0][2] == len(seq) - 1
-        first = processes[0][0] if processes else sc
-        self.dev = torch.device(first.device) if first is not None and first.device is not None else torch.device(
+        p0 = processes[0][0]
+        self.dev = torch.device(p0.device) if p0.device is not None else torch.device(
             "cuda", torch.cuda.current_device())
         if isinstance(p_array, DeviceParticleArray):
             self.beam = p_array
