@@ -439,6 +439,8 @@ class DeviceTrack:
             whole = True
         else:
             processes = [(p, int(a), int(b)) for p, a, b in processes]
+            if not processes:
+                raise ValueError("processes is empty: device tracking needs at least one SpaceCharge process")
             whole = len(processes) == 1 and processes[0][1] == 0 and processes[0][2] == len(seq) - 1
         p0 = processes[0][0]
         self.dev = torch.device(p0.device) if p0.device is not None else torch.device(
