@@ -26,6 +26,9 @@ What it writes (all under tests/golden/):
   ``track()`` through FODO cells with SecondTM and SpaceCharge.
 * ``ref_io.npz``, ``ref_beam.ast``, ``ref_beam.fmt1`` -- a seeded beam saved
   and loaded by the reference's ASTRA and CSRtrack adaptors.
+* ``ref_navigator.npz`` -- the reference Navigator's steps (lengths,
+  positions, processes applied and their step lengths) for lines with
+  overlapping process ranges, gaps and three processes (passive processes).
 * ``ref_cavity.npz`` -- sections of RF cavities (CavityTM, coupler kicks,
   tilt) applied by the reference to a seeded beam, with the energy before and
   after (elements/cavity_atom.py, transformations/cavity.py).
@@ -577,6 +580,51 @@ def run_track_mixed(ref_root: str, n=5000, mesh=(31, 31, 31)):
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB), {len(rec)} kicks")
 
 
+NAVIGATOR_CASES = [
+    # (element lengths, [(indx0, indx1, step)], unit_step): overlapping ranges, a gap, three processes,
+    # a range ending before the lattice does
+    ([0.0, 0.5, 0.3, 1.0, 0.2, 0.7, 0.0], [(0, 3, 2), (2, 6, 3)], 0.05),
+    ([0.0, 0.4, 0.25, 0.6, 0.35, 0.5, 0.0], [(1, 3, 1), (4, 5, 2)], 0.1),
+    ([0.0, 0.3, 0.3, 0.45, 0.15, 0.9, 0.2, 0.0], [(0, 7, 1), (0, 3, 4), (2, 5, 2)], 0.07),
+    ([0.1, 0.2, 0.3, 0.4, 0.5], [(0, 3, 3)], 0.033),
+]
+
+
+def run_navigator(ref_root: str):
+    """The reference Navigator's steps (get_next_step: step length, position
+    after the step, processes applied with their step lengths) for lines with
+    several processes, with passive processes (no physics)."""
+    import_reference(ref_root)
+    from ocelot import Drift, MagneticLattice, Marker, Navigator
+    from ocelot.cpbd.physics_proc import PhysProc
+    data = {"n_cases": len(NAVIGATOR_CASES)}
+    for c, (lengths, procs, unit) in enumerate(NAVIGATOR_CASES):
+        seq = [Marker(eid=f"M{i}") if L == 0 else Drift(l=L, eid=f"D{i}") for i, L in enumerate(lengths)]
+        lat = MagneticLattice(seq)
+        navi = Navigator(lat)
+        objs = []
+        for a, b, st in procs:
+            p = PhysProc(step=st)
+            navi.add_physics_proc(p, seq[a], seq[b])
+            objs.append(p)
+        navi.unit_step = unit
+        rows = []
+        for _, dz, plist, psteps in navi.get_next_step():
+            ids = [next(k for k, o in enumerate(objs) if o is p) for p in plist]
+            rows.append((float(dz), float(navi.z0), ids, [float(v) for v in psteps]))
+        data[f"c{c}_lengths"] = np.array(lengths)
+        data[f"c{c}_procs"] = np.array(procs, dtype=np.int64)
+        data[f"c{c}_unit"] = np.array(unit)
+        data[f"c{c}_dz"] = np.array([r[0] for r in rows])
+        data[f"c{c}_z0"] = np.array([r[1] for r in rows])
+        data[f"c{c}_nkick"] = np.array([len(r[2]) for r in rows], dtype=np.int64)
+        data[f"c{c}_kick_proc"] = np.array([k for r in rows for k in r[2]], dtype=np.int64)
+        data[f"c{c}_kick_dz"] = np.array([v for r in rows for v in r[3]])
+    path = os.path.join(HERE, "ref_navigator.npz")
+    np.savez_compressed(path, **data)
+    print(f"wrote {path} ({os.path.getsize(path) / 1e3:.1f} kB)")
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -587,6 +635,7 @@ if __name__ == "__main__":
     ap.add_argument("--only-cavity", action="store_true")
     a = ap.parse_args()
     if a.only_cavity:
+        run_navigator(a.reference)
         run_cavity(a.reference)
         run_track_mixed(a.reference)
         run_track_line(a.reference)
@@ -606,6 +655,7 @@ if __name__ == "__main__":
         run_fodo(a.reference)
         run_second_order(a.reference)
         run_io(a.reference)
+        run_navigator(a.reference)
         run_cavity(a.reference)
     if not a.skip_track:
         run_track(a.reference)

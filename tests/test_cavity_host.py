@@ -254,3 +254,20 @@ def test_map_kinds_follow_the_element_patterns():
     cav = CV.Cavity(l=1.0, v=0.01, phi=10.0, freq=1.3e9, vxy_up=1e-3)
     _, kinds, _ = CV.section_records(cav, 0.0, 1.0, E)
     assert kinds == [CV.SLICE_MAP, CV.SLICE_CAVITY]          # vxy couples x and y
+
+
+def test_navigator_steps_match_the_reference_navigator_with_several_processes():
+    """Overlapping process ranges, a gap, three processes, a range that ends
+    before the lattice does: every step's length, the position after it, the
+    processes applied and their step lengths equal the reference Navigator's
+    (ref_navigator.npz, passive processes), bit for bit."""
+    nav = dict(np.load(os.path.join(GOLDEN, "ref_navigator.npz")))
+    for c in range(int(nav["n_cases"])):
+        procs = [tuple(int(v) for v in p) for p in nav[f"c{c}_procs"]]
+        steps = T.navigator_steps(list(nav[f"c{c}_lengths"]), procs, float(nav[f"c{c}_unit"]))
+        assert len(steps) == len(nav[f"c{c}_dz"]), c
+        assert np.array_equal([st[3] for st in steps], nav[f"c{c}_dz"]), c
+        assert np.array_equal([st[2] for st in steps], nav[f"c{c}_z0"]), c
+        assert [len(st[1]) for st in steps] == list(nav[f"c{c}_nkick"]), c
+        assert [j for st in steps for j, _ in st[1]] == list(nav[f"c{c}_kick_proc"]), c
+        assert np.array_equal([z for st in steps for _, z in st[1]], nav[f"c{c}_kick_dz"]), c

@@ -19,7 +19,7 @@ CASES = sorted(glob.glob(os.path.join(GOLDEN, "ref_*.npz")))
 # the kick fixtures (the others hold transport, tracking and beam-file outputs)
 NOT_KICKS = ("ref_track_kicks.npz", "ref_uni_matrix.npz", "ref_fodo_track.npz", "ref_fodo_track2.npz",
              "ref_second_order.npz", "ref_io.npz", "ref_cavity.npz", "ref_track_line.npz",
-             "ref_track_mixed.npz")
+             "ref_track_mixed.npz", "ref_navigator.npz")
 CASES = [c for c in CASES if os.path.basename(c) not in NOT_KICKS]
 
 
