@@ -81,7 +81,8 @@ def _element_params(e):
     module's classes or any object with the reference's element attributes."""
     name = type(e).__name__
     if name not in _SUPPORTED:
-        raise NotImplementedError(f"{name}: device tracking supports drifts, quadrupoles, markers and monitors")
+        raise NotImplementedError(f"{name}: device tracking supports drifts, quadrupoles, markers, monitors and "
+                                  "cavities")
     angle = float(getattr(e, "angle", 0.0) or 0.0)
     if angle != 0.0:
         raise NotImplementedError(f"{name} with angle {angle}: bends are not supported by device tracking")
