@@ -1407,6 +1407,43 @@ __device__ __forceinline__ bool key_of(double fx, double fy, double fz, const Ki
     return in;
 }
 
+// FP64: whether 0 <= c <= hi (c = -0.0 included, NaN excluded) and floor(c)
+// for such c, both on the bit pattern: the order of non-negative doubles is
+// the order of their bits, and the integer part is the significand shifted
+// by the exponent.  Equal to the double compares and floor(), without the
+// FP64 pipe, which this GPU issues at a fraction of its integer rate.
+__device__ __forceinline__ bool in_range64(double c, double hi) {
+    const long long b = __double_as_longlong(c);
+    return (b >= 0 || b == (long long)0x8000000000000000ull) && b <= __double_as_longlong(hi);
+}
+__device__ __forceinline__ int floor_nonneg64(double c) {  // 0 <= c < 2^31
+    const long long b = __double_as_longlong(c);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e < 0) return 0;
+    const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    return (int)(m >> (52 - e));
+}
+
+// c = floor(g) + 1 and whether 0 <= c < n (key_of's test), for a double grid
+// coordinate g, on its bit pattern: +-0 gives 1; 0 < g < n - 1 gives
+// floor(g) + 1; -1 <= g < 0 gives 0; anything else (NaN, infinities
+// included) is out of the mesh.
+__device__ __forceinline__ bool cell_of64(double g, int n, uint32_t& c) {
+    const long long b = __double_as_longlong(g);
+    if ((b << 1) == 0) {
+        c = 1u;
+        return n > 1;
+    }
+    if (b > 0) {
+        if (b >= __double_as_longlong((double)(n - 1))) return false;
+        c = (uint32_t)floor_nonneg64(g) + 1u;
+        return true;
+    }
+    if ((b & 0x7FFFFFFFFFFFFFFFll) > 0x3FF0000000000000ll) return false;
+    c = 0u;
+    return true;
+}
+
 __global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t* __restrict__ keys, KickParams kp,
                                                ScState* st) {
     pdl_wait();
@@ -1422,9 +1459,10 @@ __global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t*
         const double g0 = __dsub_rn(div_rb(X[i], s0, r0), o0);
         const double g1 = __dsub_rn(div_rb(X[nX + i], s1, r1), o1);
         const double g2 = __dsub_rn(div_rb(X[2 * nX + i], s2, r2), o2);
-        uint32_t key;
-        bad |= !key_of(floor(g0) + 1, floor(g1) + 1, floor(g2) + 1, kp, key);
-        keys[i] = key;
+        uint32_t c0, c1, c2;
+        const bool in = cell_of64(g0, kp.nx, c0) & cell_of64(g1, kp.ny, c1) & cell_of64(g2, kp.nz, c2);
+        bad |= !in;
+        keys[i] = in ? (c0 * (uint32_t)kp.ny + c1) * (uint32_t)kp.nz + c2 : 0u;
         X[i] = g0;
         X[nX + i] = g1;
         X[2 * nX + i] = g2;
@@ -1575,23 +1613,6 @@ __global__ void __launch_bounds__(PT, 4) k_keys32(float* __restrict__ X, uint32_
 // trilinear gather, scipy.ndimage.map_coordinates(order=1, mode='constant')
 // semantics: a sample outside [0, n-1] in any axis is 0
 // ---------------------------------------------------------------------------
-// FP64: whether 0 <= c <= hi (c = -0.0 included, NaN excluded) and floor(c)
-// for such c, both on the bit pattern: the order of non-negative doubles is
-// the order of their bits, and the integer part is the significand shifted
-// by the exponent.  Equal to the double compares and floor(), without the
-// FP64 pipe, which this GPU issues at a fraction of its integer rate.
-__device__ __forceinline__ bool in_range64(double c, double hi) {
-    const long long b = __double_as_longlong(c);
-    return (b >= 0 || b == (long long)0x8000000000000000ull) && b <= __double_as_longlong(hi);
-}
-__device__ __forceinline__ int floor_nonneg64(double c) {  // 0 <= c < 2^31
-    const long long b = __double_as_longlong(c);
-    const int e = (int)((b >> 52) & 0x7ff) - 1023;
-    if (e < 0) return 0;
-    const unsigned long long m = ((unsigned long long)b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-    return (int)(m >> (52 - e));
-}
-
 template <typename R>
 __device__ __forceinline__ R trilerp(const R* __restrict__ F, int nx, int ny, int nz, R c0, R c1, R c2) {
     int i, j, k;
