@@ -271,3 +271,22 @@ def test_navigator_steps_match_the_reference_navigator_with_several_processes():
         assert [len(st[1]) for st in steps] == list(nav[f"c{c}_nkick"]), c
         assert [j for st in steps for j, _ in st[1]] == list(nav[f"c{c}_kick_proc"]), c
         assert np.array_equal([z for st in steps for _, z in st[1]], nav[f"c{c}_kick_dz"]), c
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_navigator_steps_random_lines_equal_the_oracle(seed):
+    """One process over random lines (zero-length elements included, the
+    last a marker) and random unit steps: the Navigator restatement of the
+    device loop equals the oracle's, position by position."""
+    from oracle import sc_oracle
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 12))
+    lengths = [0.0 if rng.random() < 0.2 else float(rng.uniform(0.01, 1.5)) for _ in range(n)] + [0.0]
+    unit = float(rng.uniform(0.01, 0.4))
+    step = int(rng.integers(1, 4))
+    ref = sc_oracle.navigator_schedule(lengths, unit, step)
+    got = T.navigator_steps(lengths, [(0, len(lengths) - 1, step)], unit)
+    assert len(got) == len(ref)
+    for (slices, zstep, z0), (sections, kicks, z0b, _) in zip(ref, got):
+        assert z0 == z0b and kicks == [(0, zstep)]
+        assert slices == [(i, T._section_length(lengths[i], s, d)) for i, s, d in sections]
