@@ -119,8 +119,10 @@ int sc_kick(sc_plan* plan, void* ws, size_t ws_bytes, double* rparticles, int64_
  *
  * Requirements: every plan is SC_FP32 without SC_FP32_SORTED_DEPOSIT (the
  * exact fixed-point deposit), each beam has its own plan and initialised
- * workspace, and no two beams share a workspace or particles.  Beams with
- * zstep == 0 are left out (sc.py:210-212), their transport map included. */
+ * workspace, and no two beams share a workspace or particles.  A beam with
+ * zstep == 0 is not kicked (sc.py:210-212); if it carries a transport map it
+ * stays in the table for sc_tmap_batched alone (its workspace and energy are
+ * then not used), otherwise it is left out. */
 typedef struct sc_batch sc_batch;
 typedef struct sc_beam {
     sc_plan* plan;
@@ -187,6 +189,8 @@ int sc_sym_kernel(sc_plan* plan, void* ws, size_t ws_bytes, double hx, double hy
  * (nx+1)(ny+1)(nz+1) <= SC_SYM_KERNEL_STATIC_MAX_CORNERS (64^3 fits), larger
  * ones are rejected with SC_ERR_UNSUPPORTED.  The first call on a device
  * looks up the array's device address, so make it before any stream capture.
+ * That address is kept for the life of the process: after cudaDeviceReset on
+ * a device it is stale, so do not call this entry point on that device again.
  * All calls share the array: calls that overlap on the GPU (other streams or
  * host threads) race -- keep them on one stream.
  *   kern: device float64 [nx][ny][nz]. */

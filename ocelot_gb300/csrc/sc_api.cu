@@ -317,32 +317,31 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
     SC_CUDA(prepare_green_kernels(p), "kernel attributes");
     SC_CUDA(prepare_particle_kernels(), "kernel attributes");
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-    // the Green's-function branch runs at the highest priority: its FP64
-    // blocks take their SM slots first and the keys kernel fills the rest
-    int prio_lo = 0, prio_hi = 0;
-    SC_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi), "cudaDeviceGetStreamPriorityRange");
-    SC_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio_hi), "cudaStreamCreate");
-    SC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
-    SC_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "cudaEventCreate");
-    int* status_host = nullptr;
-    SC_CUDA(cudaMallocHost(reinterpret_cast<void**>(&status_host), sizeof(int)), "cudaMallocHost");
     sc_plan* h = new (std::nothrow) sc_plan;
-    if (!h) {
-        cudaFreeHost(status_host);
-        return fail(SC_ERR_ARG, "out of host memory");
-    }
+    if (!h) return fail(SC_ERR_ARG, "out of host memory");
     h->p = p;
     h->ws_ready = nullptr;
     h->ws_ready_bytes = 0;
     h->profiling = false;
     h->last_launches = 0;
     for (int i = 0; i < NEV; ++i) h->ev[i] = nullptr;
-    h->side = side;
-    h->fork = fork;
-    h->join = join;
-    h->status_host = status_host;
+    h->side = nullptr;
+    h->fork = h->join = nullptr;
+    h->status_host = nullptr;
+    // the Green's-function branch runs at the highest priority: its FP64
+    // blocks take their SM slots first and the keys kernel fills the rest.
+    // On any failure sc_plan_destroy releases what was created so far.
+    int prio_lo = 0, prio_hi = 0;
+    const char* where = "cudaDeviceGetStreamPriorityRange";
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (!e) where = "cudaStreamCreate", e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_hi);
+    if (!e) where = "cudaEventCreate", e = cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+    if (!e) where = "cudaEventCreate", e = cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming);
+    if (!e) where = "cudaMallocHost", e = cudaMallocHost(reinterpret_cast<void**>(&h->status_host), sizeof(int));
+    if (e) {
+        sc_plan_destroy(h);
+        return cuda_fail(e, where);
+    }
     *out = h;
     return SC_OK;
 }
@@ -354,9 +353,9 @@ void sc_plan_destroy(sc_plan* plan) {
     if (plan->side) {
         cudaStreamSynchronize(plan->side);
         cudaStreamDestroy(plan->side);
-        cudaEventDestroy(plan->fork);
-        cudaEventDestroy(plan->join);
     }
+    if (plan->fork) cudaEventDestroy(plan->fork);
+    if (plan->join) cudaEventDestroy(plan->join);
     if (plan->status_host) cudaFreeHost(plan->status_host);
     delete plan;
 }
@@ -364,7 +363,14 @@ void sc_plan_destroy(sc_plan* plan) {
 int sc_profile_enable(sc_plan* plan, int enable) {
     if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
     if (enable && !plan->profiling) {
-        for (int i = 0; i < NEV; ++i) SC_CUDA(cudaEventCreate(&plan->ev[i]), "cudaEventCreate");
+        for (int i = 0; i < NEV; ++i) {
+            const cudaError_t e = cudaEventCreate(&plan->ev[i]);
+            if (e) {
+                for (int j = 0; j < i; ++j) cudaEventDestroy(plan->ev[j]);
+                for (int j = 0; j < NEV; ++j) plan->ev[j] = nullptr;
+                return cuda_fail(e, "cudaEventCreate");
+            }
+        }
         plan->profiling = true;
     } else if (!enable && plan->profiling) {
         for (int i = 0; i < NEV; ++i) cudaEventDestroy(plan->ev[i]);
@@ -713,10 +719,15 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
         if (!m.plan) return fail(SC_ERR_ARG, "beam %d: plan is NULL", i);
         if (m.plan->p.prec != SC_FP32 || m.plan->p.sorted_deposit)
             return fail(SC_ERR_UNSUPPORTED, "beam %d: batched kicks need SC_FP32 plans with the fixed-point deposit", i);
-        if (m.zstep == 0) continue;
+        if (m.zstep == 0 && !m.tmap) continue;  // nothing to do for this beam
         if (m.n < 1 || m.n > 0x7fffffffLL) return fail(SC_ERR_ARG, "beam %d: n=%lld", i, (long long)m.n);
         if (!m.rparticles || !m.q) return fail(SC_ERR_ARG, "beam %d: rparticles or q is NULL", i);
         if (m.ld < m.n) return fail(SC_ERR_ARG, "beam %d: ld=%lld < n=%lld", i, (long long)m.ld, (long long)m.n);
+        if (m.zstep == 0) {  // transport only: no kick, so no workspace or energy is used
+            if (!seen.emplace((const void*)m.rparticles, i).second)
+                return fail(SC_ERR_ARG, "beam %d shares a particle array with beam %d", i, seen[m.rparticles]);
+            continue;
+        }
         if (!(m.energy_gev > 0) || !isfinite(m.energy_gev) || !isfinite(m.zstep) ||
             !(m.energy_gev / c.m_e_GeV > 1.0))
             return fail(SC_ERR_ARG, "beam %d: energy %g GeV / zstep %g invalid", i, m.energy_gev, m.zstep);
@@ -735,16 +746,31 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
     for (int k = 0; k < 3; ++k) b->fft_smem[k] = b->green_smem[k] = 0;
     for (int i = 0; i < nbeams; ++i) {
         const sc_beam& m = beams[i];
-        if (m.zstep == 0) continue;
+        if (m.zstep == 0 && !m.tmap) continue;
         BatchBeam& B = hb[nb];
         memset(&B, 0, sizeof B);
         const Plan& p = m.plan->p;
-        B.ws = static_cast<char*>(m.ws);
         B.rp = m.rparticles;
         B.q = m.q;
+        B.p = p;
+        B.gx[BS_TMAP] = batch_particle_blocks(p, m.n);
+        B.gy[BS_TMAP] = 1;
+        B.has_tm = 1;
+        for (int k = 0; k < 42 && m.tmap; ++k) B.tm[k] = m.tmap[k];
+        if (m.zstep == 0) {
+            // the reference applies the transport of a step whose kick has
+            // zero length and skips only the kick (sc.py:210-212): the beam
+            // takes part in the transport stage alone, with no blocks in the
+            // kick stages
+            B.kp.n = m.n;
+            B.kp.ld = m.ld;
+            ++nb;
+            continue;
+        }
+        B.has_tm = m.tmap != nullptr;
+        B.ws = static_cast<char*>(m.ws);
         B.kp = make_params(p, m.n, m.ld, m.energy_gev, m.zstep, m.mesh_scale, m.mesh_shift);
         B.L = make_layout(p, m.n);
-        B.p = p;
         const bool rp_ok = ((uintptr_t)m.rparticles % 16 == 0) && (m.ld % 2 == 0);
         B.vec_rp = rp_ok;
         B.vec_rpq = rp_ok && ((uintptr_t)m.q % 16 == 0);
@@ -757,10 +783,6 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
         }
         B.gx[BS_PART] = batch_particle_blocks(p, m.n);
         B.gy[BS_PART] = 1;
-        if (m.tmap) {
-            B.has_tm = 1;
-            for (int k = 0; k < 42; ++k) B.tm[k] = m.tmap[k];
-        }
         ++nb;
     }
     for (int st = 0; st < BS_COUNT; ++st) {
@@ -831,7 +853,7 @@ int sc_tmap_batched(sc_batch* b, void* stream) {
     if (b->nb == 0) return SC_OK;
     const BatchBeam* beams = reinterpret_cast<const BatchBeam*>(b->d_buf);
     const int* start = reinterpret_cast<const int*>(b->d_buf + b->beams_bytes);
-    SC_CUDA(launch_batch_tmap(beams, start + BS_PART * (b->max_beams + 1), b->nb, b->blocks[BS_PART],
+    SC_CUDA(launch_batch_tmap(beams, start + BS_TMAP * (b->max_beams + 1), b->nb, b->blocks[BS_TMAP],
                               (cudaStream_t)stream),
             "batched transfer map");
     return SC_OK;

@@ -260,6 +260,7 @@ enum BatchStage {
     BS_FFT_Y,      // F2 and B2
     BS_FFT_X,      // F3 (x forward, Green multiply, x inverse)
     BS_FIELD,      // field quads
+    BS_TMAP,       // transport map (sc_tmap_batched): also the beams without a kick this step
     BS_COUNT
 };
 

@@ -561,7 +561,7 @@ extern "C" int sc_sym_kernel_static(int nx, int ny, int nz, double hx, double hy
                                     void* stream) {
     using namespace ocsc;
     if (nx < 1 || ny < 1 || nz < 1) return sc_report(SC_ERR_ARG, "sc_sym_kernel_static: mesh dimensions must be >= 1");
-    const long long corners = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+    const long long corners = ((long long)nx + 1) * ((long long)ny + 1) * ((long long)nz + 1);
     if (corners > kStaticMaxCorners)
         return sc_report(SC_ERR_UNSUPPORTED,
                          "sc_sym_kernel_static: (nx+1)(ny+1)(nz+1) = %lld corners exceeds the static table of %lld "

@@ -210,14 +210,39 @@ constexpr int PART_EXT = 11;
 // ---------------------------------------------------------------------------
 // FP64 transforms in the reference's operation order
 // ---------------------------------------------------------------------------
-// a / b, correctly rounded, from rb = RN(1/b): q = RN(a rb), then
-// RN(q + (a - q b) rb) with the residual exact in one FMA (Markstein's
-// theorem: the result is RN(a/b) when rb = RN(1/b), away from overflow and
-// underflow).  Three FP64 instructions instead of a division, which this GPU
-// issues on its narrow FP64 pipe as a dozen.
+// a / b from rb = RN(1/b): q = RN(a rb), then RN(q + (a - q b) rb) with the
+// residual exact in one FMA (Markstein's correction).  Markstein's theorem
+// gives RN(a/b) when the first q is within one ulp of a/b; from RN(1/b) it is
+// within 1.5 ulp in the worst case, so the result is correctly rounded in
+// every case tested (hundreds of millions, divisor significands near 1 and 2
+// included) but not proven for all (a, b).  Three FP64 instructions instead of
+// a division, which this GPU issues on its narrow FP64 pipe as a dozen; where
+// a floor() follows the quotient, div_checked proves each result.
 __device__ __forceinline__ double div_rb(double a, double b, double rb) {
     const double q = __dmul_rn(a, rb);
     return __fma_rn(__fma_rn(-q, b, a), rb, q);
+}
+
+// RN(a / b) for certain: div_rb's quotient q, kept only when the exact
+// residual r = a - q b (one FMA) proves it, |r| < |b| ulp(q) / 2 -- then a/b
+// lies within half an ulp of q.  The bound is |b| scaled by a power of two,
+// built on the bit patterns and compared as integers (both non-negative).  A
+// q that is a power of two (the spacing below it is half its ulp), zero, or
+// near the ends of the exponent range goes to the IEEE division, and so does
+// any q the test does not prove.  Used where floor() follows the quotient
+// (the NGP keys), since a one-ulp change there can move a particle to the next
+// cell.
+__device__ __forceinline__ double div_checked(double a, double b, double rb) {
+    const double q = div_rb(a, b, rb);
+    const double r = __fma_rn(-q, b, a);
+    const long long qb = __double_as_longlong(q);
+    const long long bb = __double_as_longlong(b) & 0x7fffffffffffffffll;
+    const int eq = (int)((qb >> 52) & 0x7ff), eb = (int)(bb >> 52);
+    const int et = eb + eq - 1076;  // biased exponent of |b| 2^(eq - 1023 - 53)
+    const long long thr = (bb & 0xfffffffffffffll) | ((long long)et << 52);
+    const bool ok = (qb & 0xfffffffffffffll) != 0 && eq > 0 && eq < 2047 && eb > 0 && eb < 2047 && et > 0 &&
+                    et < 2047 && (__double_as_longlong(r) & 0x7fffffffffffffffll) < thr;
+    return ok ? q : __ddiv_rn(a, b);
 }
 
 // xxstg_2_xp_mad (coord_transform.py:57-96)
@@ -1450,15 +1475,15 @@ __global__ void __launch_bounds__(PT) k_keys64(double* __restrict__ X, uint32_t*
     if (st->status) return;
     const int64_t n = kp.n;
     const double s0 = st->steps[0], s1 = st->steps[1], s2 = st->steps[2];
-    // isteps = RN(1/steps): the quotients below are the correctly rounded X / steps (div_rb)
+    // isteps = RN(1/steps): the quotients below are the correctly rounded X / steps (div_checked)
     const double r0 = st->isteps[0], r1 = st->isteps[1], r2 = st->isteps[2];
     const double o0 = st->xoff[0], o1 = st->xoff[1], o2 = st->xoff[2];
     bool bad = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t nX = kp.nX;
-        const double g0 = __dsub_rn(div_rb(X[i], s0, r0), o0);
-        const double g1 = __dsub_rn(div_rb(X[nX + i], s1, r1), o1);
-        const double g2 = __dsub_rn(div_rb(X[2 * nX + i], s2, r2), o2);
+        const double g0 = __dsub_rn(div_checked(X[i], s0, r0), o0);
+        const double g1 = __dsub_rn(div_checked(X[nX + i], s1, r1), o1);
+        const double g2 = __dsub_rn(div_checked(X[2 * nX + i], s2, r2), o2);
         uint32_t c0, c1, c2;
         const bool in = cell_of64(g0, kp.nx, c0) & cell_of64(g1, kp.ny, c1) & cell_of64(g2, kp.nz, c2);
         bad |= !in;

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(256) kb_tmap(const BatchBeam* __restrict__ bea
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
     if (!B.has_tm) return;
-    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_TMAP], 1);
     __shared__ bool planar;
     if (threadIdx.x < 42) m[threadIdx.x] = B.tm[threadIdx.x];
     __syncthreads();

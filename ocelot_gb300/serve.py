@@ -91,6 +91,7 @@ class _Job:
         self.t_arrive = t_arrive
         self.t_admit = self.t_done = None
         self.next = 0
+        self.steps = None
         self.engine = self.rp = self.q = self.host = self.status = None
         self.tick_event = self.copy_event = self.result = self.error = None
         self.bytes = 0
@@ -141,9 +142,19 @@ class Server:
             raise ValueError("zero-size array: the space-charge kick needs at least one particle")
         if len(request.nmesh) != 3 or min(int(v) for v in request.nmesh) < 4:
             raise ValueError(f"nmesh {request.nmesh}: three dimensions >= 4 needed")
+        # the step list (transport map and kick length of every step) depends
+        # only on the line and the beam energy: built here, so that a line
+        # without steps (a zero-length section) is refused instead of being
+        # admitted as a job that never finishes
+        E = float(b.energy_gev) if isinstance(b, BeamSpec) else float(b.E)
+        steps = step_maps(_lattice_sequence(request.elements), E, request.unit_step, int(request.sc_step))
+        if not steps:
+            raise ValueError("the lattice section has no tracking steps (zero length): nothing to track")
         jid = self._next_id
         self._next_id += 1
-        self.pending.append(_Job(jid, request, time.perf_counter() if t_arrive is None else t_arrive))
+        job = _Job(jid, request, time.perf_counter() if t_arrive is None else t_arrive)
+        job.steps = steps
+        self.pending.append(job)
         return jid
 
     def busy(self) -> bool:
@@ -197,7 +208,6 @@ class Server:
                     job.q = torch.from_numpy(np.ascontiguousarray(pa.q_array, dtype=np.float64)).pin_memory().to(
                         self.device, non_blocking=True)
                     job.E = float(pa.E)
-            job.steps = step_maps(_lattice_sequence(req.elements), job.E, req.unit_step, int(req.sc_step))
             self.used += need
             self.peak_used = max(self.peak_used, self.used)
             self.active.append(job)

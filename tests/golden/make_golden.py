@@ -3,7 +3,9 @@
 Run in a container that holds the Ocelot reference checkout (it is not needed
 anywhere else):
 
-    python tests/golden/make_golden.py [--reference /root/reference] [--skip-track]
+    python tests/golden/make_golden.py --reference <ocelot checkout> [--skip-track]
+
+(or set OCELOT_REFERENCE to the checkout instead of passing --reference)
 
 What it writes (all under tests/golden/):
 
@@ -627,13 +629,16 @@ def run_navigator(ref_root: str):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("OCELOT_REFERENCE"),
+                    help="the Ocelot checkout to import (default: $OCELOT_REFERENCE)")
     ap.add_argument("--skip-track", action="store_true")
     ap.add_argument("--only-track", action="store_true")
     ap.add_argument("--only-matrices", action="store_true")
     ap.add_argument("--only-second-order-io", action="store_true")
     ap.add_argument("--only-cavity", action="store_true")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("--reference (or OCELOT_REFERENCE) must name the Ocelot checkout")
     if a.only_cavity:
         run_navigator(a.reference)
         run_cavity(a.reference)

@@ -153,3 +153,36 @@ def test_batch_of_many_small_beams():
     assert b.launches == 15
     for (rp, q, spec), out in list(zip(beams, outs))[::7]:
         assert np.array_equal(out, _alone(rp, q, spec))
+
+
+def test_zero_step_beam_with_a_map_is_transported():
+    """A step whose kick has zero length still applies its transport map (the
+    reference returns early from apply only, sc.py:210-212): the beam stays in
+    the table for sc_tmap_batched alone, beside a beam that is also kicked."""
+    R = np.eye(6)
+    R[0, 1] = R[2, 3] = 0.7      # a drift of 0.7 m (first order)
+    B = np.zeros(6)
+    good = (*_beam(1, SPECS[1]), SPECS[1])
+    still = (*_beam(2, SPECS[2]), SPECS[2])
+    b = BeamBatch(DEV)
+    d0, q0 = _dev(good[0], good[1])
+    d1, q1 = _dev(still[0], still[1])
+    b.add(d0, q0, good[2][2], good[2][1], good[2][6], tmap=(R, B))
+    b.add(d1, q1, still[2][2], still[2][1], 0.0, tmap=(R, B))
+    b.commit()
+    b.transport()
+    b.kick()
+    torch.cuda.synchronize()
+    b.beams[0][0].check_status()
+    # the same maps and kick, one beam at a time through the plain entry points
+    from ocelot_gb300.transfer import tmap_apply
+    e1, _ = _dev(still[0], still[1])
+    tmap_apply(R, B, e1)
+    assert np.array_equal(d1.cpu().numpy(), e1.cpu().numpy())
+    assert not np.array_equal(d1.cpu().numpy(), still[0])
+    e0, eq0 = _dev(good[0], good[1])
+    tmap_apply(R, B, e0)
+    sc = SpaceCharge(nmesh_xyz=good[2][1], precision="fp32")
+    sc.apply_device(e0, eq0, good[2][2], good[2][6])
+    sc.check()
+    assert np.array_equal(d0.cpu().numpy(), e0.cpu().numpy())

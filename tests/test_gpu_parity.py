@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, has_gpu
+from conftest import GOLDEN, has_gpu, igf_extended
 from oracle import sc_oracle
 
 pytestmark = pytest.mark.gpu
@@ -83,25 +83,6 @@ def test_sort_is_numpy_stable_argsort(n, bits, kind):
 # ---------------------------------------------------------------------------
 # stages against the reference's own intermediates
 # ---------------------------------------------------------------------------
-def igf_extended(shape, h):
-    """sym_kernel's formula (sc.py:109-133) in np.longdouble: the 8-corner
-    difference cancels catastrophically, so FP64 results (the reference's and
-    ours) carry ~1e-12..1e-10 relative noise; this is the yardstick."""
-    L = np.longdouble
-    i2, j2, k2 = (int(v) for v in shape)
-    hx, hy, hz = (L(float(v)) for v in h)
-    x = hx * np.arange(i2 + 1, dtype=L) - hx / 2
-    y = hy * np.arange(j2 + 1, dtype=L) - hy / 2
-    z = hz * np.arange(k2 + 1, dtype=L) - hz / 2
-    x, y, z = np.ix_(x, y, z)
-    r = np.sqrt(x * x + y * y + z * z)
-    IG = (-x * x * L(0.5) * np.arctan(y * z / (x * r)) + y * z * np.log(x + r)
-          - y * y * L(0.5) * np.arctan(z * x / (y * r)) + z * x * np.log(y + r)
-          - z * z * L(0.5) * np.arctan(x * y / (z * r)) + x * y * np.log(z + r))
-    return (IG[1:, 1:, 1:] - IG[:-1, 1:, 1:] - IG[1:, :-1, 1:] + IG[:-1, :-1, 1:]
-            - IG[1:, 1:, :-1] + IG[:-1, 1:, :-1] + IG[1:, :-1, :-1] - IG[:-1, :-1, :-1])
-
-
 @pytest.mark.parametrize("path", CASES, ids=[os.path.basename(c)[4:-4] for c in CASES])
 def test_stages_match_reference_intermediates(path):
     d = dict(np.load(path))
@@ -343,8 +324,8 @@ def test_device_resident_path_matches_host_path():
 
 @pytest.mark.parametrize("n,pinned", [(3, False), (1001, False), (200_001, False), (200_001, True)])
 def test_fp32_host_path_matches_device_path(n, pinned):
-    """SpaceCharge.apply on host arrays (sc_kick_host: copies overlapped, the
-    kick in chunks copied back one by one) equals the device-resident kick."""
+    """SpaceCharge.apply on host arrays (copied to the plan's device staging
+    rows, kicked there and copied back) equals the device-resident kick."""
     rp, q = sc_oracle.gaussian_beam(n, 11)
     host_rp = rp.copy()
     if pinned:

@@ -119,3 +119,15 @@ def test_poisson_run_serves_everything():
     assert kicks == sum((2000 + 500 * i) * 10 for i in range(8))   # 10 kicks of 0.25 m per 2.4 m cell
     for jid, r in zip(ids, reqs):
         assert srv.result(jid).shape == (6, r.beam.n)
+
+
+def test_line_without_steps_is_refused():
+    # a zero-length section (only a Marker) gives no tracking step: the server
+    # refuses it at submit instead of admitting a job that never finishes
+    srv = S.Server(DEV)
+    with pytest.raises(ValueError, match="no tracking steps"):
+        srv.submit(S.Request(S.BeamSpec(n=1000, seed=1), S.fodo(0), (15, 15, 15), 0.25, 1))
+    assert not srv.busy()
+    jid = srv.submit(_req(*JOBS[0], cells=1))
+    srv.drain(timeout_s=60.0)
+    assert srv.result(jid).shape == (6, JOBS[0][0])
