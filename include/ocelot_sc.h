@@ -323,6 +323,25 @@ const char* sc_profile_stage_name(int stage);
  * synchronisation). */
 int sc_kick_launches(const sc_plan* plan);
 
+/* Failure detection of the bulk-copy waits.  The frame, extent and kick
+ * kernels of the FP32 form stream particle rows through shared memory with
+ * bulk copies and wait for each on an mbarrier with an iteration limit
+ * (2^20 tries of about 1 us); a wait that runs out latches SC_ERR_TIMEOUT in
+ * the workspace state, waits once more (full limit) for its copies still in
+ * flight and returns, so the context stays usable and sc_read_status reports
+ * the error.  This sets the limit of one kernel (SC_WAIT_FRAME, _EXTENT,
+ * _KICK) or of all three (-1) for this plan's later kicks; tries < 0 restores
+ * the default, larger values are clamped to it.  Tries = 0 makes the first
+ * wait give up at once -- the way the tests exercise the timeout path without
+ * a fault or a hang.  A timeout in the frame or extent leaves the particles
+ * unchanged; in the kick, tiles whose wait gave up are not written (tiles of
+ * other blocks may be).  No counterpart in the reference (it has no device
+ * waits). */
+#define SC_WAIT_FRAME 0
+#define SC_WAIT_EXTENT 1
+#define SC_WAIT_KICK 2
+int sc_plan_set_wait_limit(sc_plan* plan, int kernel, long long tries);
+
 /* ---- misc -------------------------------------------------------------- */
 const char* sc_last_error(void);
 int sc_abi_version(void);

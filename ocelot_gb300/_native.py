@@ -28,6 +28,11 @@ SC_ERR_TIMEOUT = 7
 
 SC_NSTAGES = 11
 
+# the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
+SC_WAIT_FRAME = 0
+SC_WAIT_EXTENT = 1
+SC_WAIT_KICK = 2
+
 REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7}
 
 ERROR_TEXT = {
@@ -81,6 +86,7 @@ SIGNATURES = {
     "sc_profile_read": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
     "sc_profile_stage_name": (C.c_char_p, [C.c_int]),
     "sc_kick_launches": (C.c_int, [vp]),
+    "sc_plan_set_wait_limit": (C.c_int, [vp, C.c_int, C.c_longlong]),
     "sc_last_error": (C.c_char_p, []),
     "sc_abi_version": (C.c_int, []),
 }

@@ -274,6 +274,7 @@ static KickParams make_params(const Plan& p, int64_t n, int64_t ld, double energ
     kp.m_f = (float)kp.m_e_eV;
     kp.m2_f = kp.m_f * kp.m_f;
     kp.igrbr2_f = (float)(1.0 / (kp.grbr * kp.grbr));
+    for (int k = 0; k < 3; ++k) kp.wait_limit[k] = p.wait_limit[k];
     return kp;
 }
 
@@ -312,6 +313,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     SC_CUDA(cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     p.part_blocks = p.sm_count * 4;
+    for (int k = 0; k < 3; ++k) p.wait_limit[k] = MBAR_WAIT_LIMIT;
     // everything that is not a stream operation happens here, so that kicks
     // can be recorded in a CUDA graph
     SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
@@ -397,6 +399,16 @@ int sc_profile_read(sc_plan* plan, float* ms, int* n_launches) {
 }
 
 int sc_kick_launches(const sc_plan* plan) { return plan ? plan->last_launches : 0; }
+
+int sc_plan_set_wait_limit(sc_plan* plan, int kernel, long long tries) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    if (kernel < -1 || kernel > 2) return fail(SC_ERR_ARG, "kernel %d: SC_WAIT_FRAME, _EXTENT, _KICK or -1", kernel);
+    const unsigned lim = tries < 0 ? MBAR_WAIT_LIMIT : (tries > (long long)MBAR_WAIT_LIMIT ? MBAR_WAIT_LIMIT
+                                                                                        : (unsigned)tries);
+    for (int k = 0; k < 3; ++k)
+        if (kernel < 0 || kernel == k) plan->p.wait_limit[k] = lim;
+    return SC_OK;
+}
 
 const char* sc_profile_stage_name(int stage) {
     return (stage >= 0 && stage < SC_NSTAGES) ? kStageNames[stage] : "";

@@ -111,6 +111,9 @@ struct KickParams {
     // FP32 copies for the FP32 form
     float gamref_f, betaref_f, grbr_f, pref_f, ipref_f, m_f, m2_f;
     float igrbr2_f;                      // 1/(gamref*betaref)^2
+    // iteration limits of the bulk-copy waits of the frame, extent and kick
+    // kernels (MBAR_WAIT_LIMIT unless a test lowers them, sc_plan_set_wait_limit)
+    unsigned wait_limit[3];
 };
 
 // ---------------------------------------------------------------------------
@@ -159,6 +162,7 @@ struct Plan {
     int key_bits;
     int sm_count;
     int part_blocks;   // blocks of the per-particle reduction kernels
+    unsigned wait_limit[3];  // KickParams::wait_limit of this plan's kicks
 };
 
 Layout make_layout(const Plan& p, int64_t n);

@@ -492,10 +492,11 @@ struct BlockTiles {
 // Runs body(t, stage) for each of the block's tiles once its rows have
 // landed in tile buffer `stage`; issue(t, stage, bar) (thread 0) starts the
 // loads of local tile t.  Every thread of the block must call it; body must
-// not synchronise the block.  Returns false if a wait gave up, after
-// waiting (again with a limit) for the loads still in flight.
+// not synchronise the block.  Returns false if a wait gave up after `limit`
+// tries, after waiting (with the full limit) for the loads still in flight.
 template <int STAGES, typename Issue, typename Body>
-__device__ __forceinline__ bool stream_tiles(const BlockTiles& T, uint64_t* bar, Issue&& issue, Body&& body) {
+__device__ __forceinline__ bool stream_tiles(const BlockTiles& T, uint64_t* bar, unsigned limit, Issue&& issue,
+                                             Body&& body) {
     const bool lead = threadIdx.x == 0;
     if (lead) {
         for (int s = 0; s < STAGES; ++s) mbar_init(&bar[s], 1);
@@ -509,7 +510,7 @@ __device__ __forceinline__ bool stream_tiles(const BlockTiles& T, uint64_t* bar,
     bool failed = false;
     for (; t < T.mine; ++t) {
         const int s = (int)(t % STAGES);
-        const bool ok = mbar_wait(&bar[s], (unsigned)((t / STAGES) & 1));
+        const bool ok = mbar_wait(&bar[s], (unsigned)((t / STAGES) & 1), limit);
         if (ok) body(t, s);
         if (__syncthreads_or(!ok)) {
             failed = true;
@@ -974,7 +975,8 @@ __device__ __forceinline__ void frame32_tma_body(const double* __restrict__ rp, 
             add(rp[ld + i], rp[3 * ld + i], rp[5 * ld + i]);
         }
     };
-    if (!stream_tiles<FR_STAGES>(T, bar, issue, body) && threadIdx.x == 0) atomicExch(&st->frame_timeout, 1);
+    if (!stream_tiles<FR_STAGES>(T, bar, kp.wait_limit[0], issue, body) && threadIdx.x == 0)
+        atomicExch(&st->frame_timeout, 1);
     const float a[3] = {a0, a1, a2};
     float hi[3], lo[3];
     block_sum_f2<3>(a, hi, lo, smf);
@@ -1283,7 +1285,7 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
             for (int k = 0; k < 3; ++k) X[k * nX + i] = v[k];
         }
     };
-    const bool streamed = stream_tiles<EX_STAGES>(Tl, bar, issue, body);
+    const bool streamed = stream_tiles<EX_STAGES>(Tl, bar, kp.wait_limit[1], issue, body);
     if (!streamed && threadIdx.x == 0) atomicCAS(&st->status, SC_OK, SC_ERR_TIMEOUT);
     const float my_mn[3] = {mnf[0], mnf[1], mnf[2]}, my_mx[3] = {mxf[0], mxf[1], mxf[2]};
     // float extremes reduce exactly in float; the sums in double
@@ -1958,7 +1960,7 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
         if (g >= ntile) break;  // the same in every thread
         const int64_t i0 = tile_start(g);
         const int cnt = tile_count(g), staged = cnt & ~1;
-        const bool ok = mbar_wait(&bar[s], (unsigned)((t / KT_STAGES) & 1));
+        const bool ok = mbar_wait(&bar[s], (unsigned)((t / KT_STAGES) & 1), kp.wait_limit[2]);
         double* B = buf + s * 6 * KT_TILE;
         const int j = 2 * threadIdx.x;
         if (j + 1 < staged) {  // both particles staged: 16-byte shared accesses
@@ -1974,7 +1976,7 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
 #pragma unroll
             for (int k = 0; k < 6; ++k)
                 *reinterpret_cast<double2*>(B + k * KT_TILE + j) = make_double2(r[0][k], r[1][k]);
-        } else if (j < cnt) {  // the odd last particle of the beam (j == staged): read and written directly
+        } else if (j < cnt && ok) {  // the odd last particle of the beam (j == staged): read and written directly
             double r[6];
             for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i0 + j];
             kick_one(r, C, kp);

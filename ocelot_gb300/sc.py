@@ -158,6 +158,13 @@ class Engine:
         names = [self.lib.sc_profile_stage_name(i).decode() for i in range(N.SC_NSTAGES)]
         return dict(zip(names, [float(v) for v in ms])), nl.value
 
+    def set_wait_limit(self, kernel: int = -1, tries: int = -1):
+        """Iteration limit of the bulk-copy waits of one FP32 kernel
+        (N.SC_WAIT_FRAME, _EXTENT, _KICK) or of all three (-1) for later
+        kicks; tries < 0 restores the default.  A wait that runs out latches
+        SC_ERR_TIMEOUT (raised by ``check_status``) instead of spinning on."""
+        N.check(self.lib.sc_plan_set_wait_limit(self.plan, int(kernel), int(tries)))
+
     def check_status(self):
         """Wait for the stream and raise if the last call latched an error."""
         torch = _torch()
