@@ -169,42 +169,26 @@ def time_form(precision, n, steps, warmup, dev, flush):
     return kick_ms, {k: sum(v) / len(v) for k, v in stages.items()}, launches
 
 
-def fp32_kick_error(n, dev):
-    """Relative RMS error of the FP32 form's kicks (Δx', Δy', Δδ) against the FP64
-    form on the same beam, one kick, computed on the device."""
-    import torch
-    from ocelot_gb300 import SpaceCharge
-    rp, q = beam(n, seed=SEED + 1)
-    r0 = torch.from_numpy(rp).to(dev)
-    d_q = torch.from_numpy(q).to(dev)
-    out = {}
-    for prec in ("fp64", "fp32"):
-        d = r0.clone()
-        sc = SpaceCharge(nmesh_xyz=MESH, precision=prec, device=dev)
-        sc.apply_device(d, d_q, E_GEV, DZ)
-        sc.check()
-        out[prec] = d
-    err = {}
-    for r, name in ((1, "dxp"), (3, "dyp"), (5, "ddelta")):
-        k64 = out["fp64"][r] - r0[r]
-        k32 = out["fp32"][r] - r0[r]
-        err[name] = float(torch.sqrt(torch.mean((k32 - k64) ** 2)) / torch.sqrt(torch.mean(k64 ** 2)))
-    return err
-
-
-def time_e2e(precision, n, steps, warmup, dev):
-    """Through SpaceCharge.apply with host (pinned) buffers; copies inside the timed region."""
+def time_e2e(precision, n, steps, warmup, dev, pinned=True):
+    """Through SpaceCharge.apply on a host ParticleArray; the host->device copy
+    of rparticles and q_array and the device->host copy of rparticles are
+    inside the timed region.  pinned=False: plain numpy arrays (pageable), as
+    Ocelot's track() hands them to SpaceCharge.apply (track.py:476-478)."""
     import numpy as np
     import torch
     from ocelot_gb300 import ParticleArray, SpaceCharge
     rp, q = beam(n)
-    h_rp = torch.empty((6, n), dtype=torch.float64).pin_memory()
-    h_q = torch.empty(n, dtype=torch.float64).pin_memory()
-    h_rp.numpy()[:] = rp
-    h_q.numpy()[:] = q
     pa = ParticleArray(0)
-    pa.rparticles = h_rp.numpy()
-    pa.q_array = h_q.numpy()
+    if pinned:
+        h_rp = torch.empty((6, n), dtype=torch.float64).pin_memory()
+        h_q = torch.empty(n, dtype=torch.float64).pin_memory()
+        h_rp.numpy()[:] = rp
+        h_q.numpy()[:] = q
+        pa.rparticles = h_rp.numpy()
+        pa.q_array = h_q.numpy()
+    else:
+        pa.rparticles = rp
+        pa.q_array = q
     pa.E = E_GEV
     sc = SpaceCharge(nmesh_xyz=MESH, precision=precision, device=dev)
     for _ in range(warmup):
@@ -217,6 +201,185 @@ def time_e2e(precision, n, steps, warmup, dev):
     dt = time.perf_counter() - t0
     assert np.isfinite(pa.rparticles).all()
     return dt, 6 * n * 8 + n * 8, 6 * n * 8
+
+
+def host_link(dev, h2d_bytes, d2h_bytes):
+    """Pinned host<->device copy bandwidth (GB/s, best of 5 CUDA-event timed
+    copies of the e2e step's own sizes) -- the bound of an end-to-end step."""
+    import torch
+    hi = torch.empty(h2d_bytes, dtype=torch.uint8).pin_memory()
+    ho = torch.empty(d2h_bytes, dtype=torch.uint8).pin_memory()
+    di = torch.empty(h2d_bytes, dtype=torch.uint8, device=dev)
+    do = torch.empty(d2h_bytes, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    best = [math.inf, math.inf]
+    for _ in range(5):
+        for k, (dst, src) in enumerate(((di, hi), (ho, do))):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            dst.copy_(src, non_blocking=True)
+            b.record(stream)
+            b.synchronize()
+            best[k] = min(best[k], a.elapsed_time(b) * 1e-3)
+    return h2d_bytes / best[0] / 1e9, d2h_bytes / best[1] / 1e9
+
+
+# Configurations of the metric timed beside the headline (each a sequence of
+# kicks on a seeded synthetic beam; a step is the whole sequence)
+CONFIG1 = {"key": "config1", "form": "fp64", "n": 200_000, "mesh": [63, 63, 63], "E": 0.130, "charge": 250e-12,
+           "dz": 0.1, "kicks": 10, "beam": "gauss",
+           "workload": "plain FP64 form: 200k particles, 6D Gaussian (sigma_x = sigma_y = 50 um, sigma_x' = "
+                       "sigma_y' = 1e-5, sigma_tau = 100 um, sigma_delta = 1e-4), 130 MeV, 250 pC, 63^3 mesh, "
+                       "10 kicks of 0.1 m"}
+CONFIG3 = {"key": "config3", "form": "fp32", "n": 10_000_000, "mesh": [128, 128, 256], "E": 0.0065,
+           "charge": 500e-12, "dz": 0.05, "kicks": 20, "beam": "flat",
+           "workload": "low-energy stress case, FP32 form: 10M particles at 6.5 MeV, 500 pC, flat-top tau of "
+                       "2 mm with 100 um Gaussian edges, chirp delta += -10 tau, transverse Gaussian 200 um with "
+                       "a 1 mrad x-tau tilt, 128x128x256 mesh, 20 kicks of 0.05 m"}
+
+
+def config_beam(cfg, seed=SEED):
+    from oracle.sc_oracle import flat_top_beam, gaussian_beam  # seeded synthetic input generators (numpy)
+    if cfg["beam"] == "gauss":
+        return gaussian_beam(cfg["n"], seed, charge=cfg["charge"])
+    return flat_top_beam(cfg["n"], seed, charge=cfg["charge"])
+
+
+def rest_frame_positions(rp, energy_gev):
+    """Positions of the particles in the mean-velocity frame and gamma0, the
+    input of SpaceCharge.el_field (sc.py:218-240, coord_transform.py:57-96),
+    in numpy: the same particles for both forms' fields."""
+    import numpy as np
+    m = 9.10938215e-31 * 299792458.0 ** 2 / 1.6021766208e-19   # m_e_eV (ocelot/common/globals.py:13-18)
+    gamref = energy_gev * 1e9 / m
+    betaref = np.sqrt(1 - gamref ** -2)
+    gamma = (betaref * rp[5] + 1) * gamref
+    beta = np.sqrt(1 - gamma ** -2)
+    pz = np.sqrt(((gamma * beta) / (gamref * betaref)) ** 2 - rp[1] ** 2 - rp[3] ** 2)
+    u = np.stack([rp[1] / pz, rp[3] / pz, np.ones(rp.shape[1])])
+    u /= np.sqrt((u * u).sum(axis=0))
+    pos = np.stack([rp[0] - u[0] * beta * rp[4], rp[2] - u[1] * beta * rp[4], -u[2] * beta * rp[4]])
+    mom = u * (gamma * beta * m)
+    t3 = mom.mean(axis=1)
+    pav = np.linalg.norm(t3)
+    t3 = t3 / pav
+    t1 = np.cross([0.0, 1.0, 0.0], t3)
+    t1 /= np.linalg.norm(t1)
+    t2 = np.cross(t3, t1)
+    T = np.c_[t1, t2, t3]
+    return np.ascontiguousarray(pos.T @ T), float(np.sqrt((pav / m) ** 2 + 1))
+
+
+def form_errors(cfg, dev, seed=SEED + 1):
+    """The FP32 form against the FP64 form on one kick of the same beam --
+    relative RMS errors of the grid potential, of E at the particles (the
+    rest-frame field, both forms' el_field on the same positions) and of the
+    momentum kicks (x', y', delta).  The FP64 form is itself within 1e-10 of
+    the oracle (tests); so these are the FP32 form's errors against FP64."""
+    import numpy as np
+    import torch
+    from ocelot_gb300 import SpaceCharge
+    rp, q = config_beam(cfg, seed)
+    n, mesh = rp.shape[1], cfg["mesh"]
+    r0 = torch.from_numpy(rp).to(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    out, phi = {}, {}
+    for prec in ("fp64", "fp32"):
+        d = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=dev)[:, :n]
+        d.copy_(r0)
+        sc = SpaceCharge(nmesh_xyz=mesh, precision=prec, device=dev)
+        sc.apply_device(d, d_q, cfg["E"], cfg["dz"])
+        sc.check()
+        out[prec] = d
+        phi[prec] = sc.engine().region("phi").to(torch.float64)
+        del sc
+    rel = lambda a, b: float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))  # noqa: E731
+    dp = {}
+    for r, name in ((1, "dxp"), (3, "dyp"), (5, "ddelta")):
+        k64 = out["fp64"][r] - r0[r]
+        k32 = out["fp32"][r] - r0[r]
+        dp[name] = float(torch.sqrt(torch.mean((k32 - k64) ** 2)) / torch.sqrt(torch.mean(k64 ** 2)))
+    del out
+    torch.cuda.empty_cache()
+    xyz, g0 = rest_frame_positions(rp, cfg["E"])
+    E = {}
+    for prec in ("fp64", "fp32"):
+        E[prec] = SpaceCharge(nmesh_xyz=mesh, precision=prec, device=dev).el_field(xyz.copy(), q, g0, mesh)
+    e_at = [float(np.linalg.norm(E["fp32"][:, c] - E["fp64"][:, c]) / np.linalg.norm(E["fp64"][:, c]))
+            for c in range(3)]
+    torch.cuda.empty_cache()
+    return {"phi": rel(phi["fp32"], phi["fp64"]), "E_at_particles": dict(zip(("Ex", "Ey", "Ez"), e_at)),
+            "kick": dp, "vs": "FP64 form (itself within 1e-10 of the oracle), one kick, same beam",
+            "beam_seed": seed}
+
+
+def time_config(cfg, steps, warmup, dev, flush, cpu_threads=None):
+    """A configuration's kick sequence, device-resident: every step restores
+    the initial beam (outside the timed region), flushes L2 and times the
+    whole sequence with CUDA events on the launching stream."""
+    import torch
+    from ocelot_gb300 import SpaceCharge
+    rp, q = config_beam(cfg)
+    n, mesh = cfg["n"], cfg["mesh"]
+    r0 = torch.from_numpy(rp).to(dev)
+    d_rp = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=dev)[:, :n]
+    d_q = torch.from_numpy(q).to(dev)
+    sc = SpaceCharge(nmesh_xyz=mesh, precision=cfg["form"], device=dev)
+    eng = sc.engine()
+    eng.ensure(n)
+    stream = torch.cuda.current_stream(dev)
+    ms, launches = [], 0
+    for it in range(warmup + steps):
+        d_rp.copy_(r0)
+        flush()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(cfg["kicks"]):
+            sc.apply_device(d_rp, d_q, cfg["E"], cfg["dz"])
+            if it >= warmup:
+                launches += eng.launches()
+        b.record(stream)
+        b.synchronize()
+        if it >= warmup:
+            ms.append(a.elapsed_time(b))
+    sc.check()
+    eng.profile(True)
+    d_rp.copy_(r0)
+    flush()
+    sc.apply_device(d_rp, d_q, cfg["E"], cfg["dz"])
+    stages, _ = eng.profile_read()
+    eng.profile(False)
+    sc.check()
+    del sc, eng, d_rp, r0
+    torch.cuda.empty_cache()
+    t = statistics.mean(ms) * 1e-3
+    w = 8 if cfg["form"] == "fp64" else 4
+    ncell = math.prod(mesh)
+    b_kick = B_PER_PARTICLE * n + 2 * w * ncell
+    peak, kind = peaks()
+    achieved = b_kick * cfg["kicks"] / t / 1e9
+    out = {"workload": cfg["workload"], "form": cfg["form"], "n_particles": n, "mesh": mesh,
+           "kicks_per_step": cfg["kicks"], "steps": steps, "warmup": warmup,
+           "value": n * cfg["kicks"] / t, "unit": "particle-kicks/s", "ms_per_step": t * 1e3,
+           "ms_per_kick": t * 1e3 / cfg["kicks"], "gpu_launches": launches, "stages_ms_one_kick": stages,
+           "l2": "flushed before each step; the kicks of a step run back to back",
+           "roofline": {"bound": "hbm" if cfg["form"] == "fp32" else "fp64 pipe (see DESIGN)",
+                        "algorithmic_bytes_per_kick": b_kick, "achieved": achieved, "unit": "GB/s",
+                        "peak": peak, "frac": achieved / peak, "peak_kind": peak_kind_text(kind)}}
+    if cpu_threads:
+        from oracle import sc_oracle
+        rp_c, q_c = config_beam(cfg)
+        t0 = time.perf_counter()
+        sc_oracle.sc_apply(rp_c, q_c, cfg["E"], cfg["dz"], mesh, fft_workers=cpu_threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "particle-kicks/s", "cores": cpu_threads, "kind": "port",
+                               "sample": f"1 kick of the same {n}-particle beam and mesh, oracle/sc_oracle.py "
+                                         f"(numpy + scipy.ndimage, scipy.fft with {cpu_threads} workers)"}
+    return out
+
+
+def peak_kind_text(kind):
+    return "of measured (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured" else "of fallback"
 
 
 def cpu_port(n, kicks_max, budget_s, threads):
@@ -370,6 +533,13 @@ def time_serving(dev, rates=SERVE_RATES, jobs=SERVE_JOBS):
             "p99_at_sustained_s": (max(sustained, key=lambda r: r["rate_hz"])["p99_s"] if sustained else None)}
 
 
+def headline_config(n, ws):
+    """The workload of the headline line (the same dict in both arms)."""
+    return {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step (FP32 form)",
+            "n_particles": n, "mesh": MESH, "form": "fp32",
+            "l2": "flushed between kicks (256 MB write, then 256 MB read)", "parallelism": f"replicas x{ws}"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -382,8 +552,7 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    per_step = (args.steps + args.warmup)
-    n = N_PART if per_step <= 20 else max(100_000, int(N_PART * 20 / per_step))
+    n = N_PART
     from oracle import sc_oracle
     rp, q = beam(n)
     for _ in range(args.warmup):
@@ -399,8 +568,8 @@ def run_reference(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic seeded 6D Gaussian beam",
-           "config": {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step",
-                      "sample_particles": n},
+           "config": headline_config(n, ws),
+           "reference_arithmetic": "FP64 (the reference's own; it has no FP32 form)",
            "impl": "reference",
            "cpu_baseline": {"value": value, "unit": "particle-kicks/s", "cores": threads, "kind": "port",
                             "sample": sample},
@@ -489,6 +658,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip timing the FP64 form")
     ap.add_argument("--no-batch", action="store_true", help="skip the 96-beam batched leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the config 1 and config 3 legs")
     ap.add_argument("--kick-only", action="store_true",
                     help="time the FP32 kick alone (no other leg): the small case for profiling")
     ap.add_argument("--transport", type=int, default=0, metavar="N",
@@ -498,7 +668,7 @@ def main():
         time_transport(args.transport, args.steps, max(args.warmup, 3))
         return
     if args.kick_only:
-        args.no_cpu = args.no_fp64 = args.no_batch = args.no_serve = True
+        args.no_cpu = args.no_fp64 = args.no_batch = args.no_serve = args.no_configs = True
     args.warmup = max(args.warmup, 3)
 
     if args.impl == "reference":
@@ -535,9 +705,20 @@ def main():
         barrier()
     kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
     e2e_dt, h2d, d2h = (math.nan, 0, 0) if args.kick_only else time_e2e("fp32", n, args.steps, args.warmup, dev)
+    e2e_page_dt = math.nan if args.kick_only else time_e2e("fp32", n, args.steps, args.warmup, dev, pinned=False)[0]
+    e2e64_dt = math.nan if (args.kick_only or args.no_fp64) else time_e2e("fp64", n, args.steps, args.warmup, dev)[0]
+    link = None if args.kick_only else host_link(dev, h2d, d2h)
+    threads = os.cpu_count() or 1
+    cpu_threads = None if (args.no_cpu or rank != 0) else threads
+    configs = {}
+    if not args.no_configs:
+        for cfg in (CONFIG1, CONFIG3):
+            configs[cfg["key"]] = time_config(cfg, 3, 1, dev, flush, cpu_threads)
+        configs["config3"]["fp32_errors_vs_fp64"] = form_errors(CONFIG3, dev)
     batched = None if args.no_batch else time_batched(args.steps, args.warmup, dev)
     serving = None if args.no_serve else time_serving(dev)
-    kick_err = None if args.kick_only else fp32_kick_error(n, dev)
+    errors = None if args.kick_only else form_errors(
+        {"n": n, "mesh": MESH, "E": E_GEV, "dz": DZ, "charge": CHARGE, "beam": "gauss"}, dev)
     barrier()
 
     t32 = sum(kick32) / 1e3
@@ -560,27 +741,31 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu:
-            threads = os.cpu_count() or 1
             v, k = cpu_port(N_PART, 5, 10.0, threads)
             cpu = {"value": v, "unit": "particle-kicks/s", "cores": threads, "kind": "port",
                    "sample": f"2M particles, 64^3, {k} kicks of oracle/sc_oracle.py (numpy + scipy.ndimage, "
                              f"scipy.fft with {threads} workers; the rest single-threaded)"}
+        e2e_step_ms = e2e_dt / args.steps * 1e3
+        link_ms = (h2d / (link[0] * 1e9) + d2h / (link[1] * 1e9)) * 1e3 if link else math.nan
         out = {
             "metric": METRIC, "value": value, "unit": "particle-kicks/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(kick32),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic seeded 6D Gaussian beam (no dataset)",
-            "config": {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step (FP32 form)",
-                       "n_particles": n, "mesh": MESH, "form": "fp32", "l2": "flushed between kicks (256 MB write, then 256 MB read)",
-                       "parallelism": f"replicas x{ws}"},
+            "config": headline_config(n, ws),
             "fp64_form": ({"value": n * args.steps / (sum(kick64) / 1e3), "ms_per_step": statistics.mean(kick64),
-                           "stages_ms": stages64} if kick64 else None),
+                           "stages_ms": stages64,
+                           "e2e": ({"value": n * args.steps / e2e64_dt, "unit": "particle-kicks/s",
+                                    "ms_per_step": e2e64_dt / args.steps * 1e3, "h2d_bytes_per_step": h2d,
+                                    "d2h_bytes_per_step": d2h, "host_memory": "pinned"}
+                                   if e2e64_dt == e2e64_dt else None)} if kick64 else None),
             "fp32_over_fp64": (statistics.mean(kick64) / statistics.mean(kick32)) if kick64 else None,
-            "fp32_kick_rel_rms_err_vs_fp64": kick_err,
+            "fp32_kick_rel_rms_err_vs_fp64": errors["kick"] if errors else None,
+            "fp32_errors_vs_fp64": errors,
             "stages_ms": stages32,
             "roofline": {"bound": "hbm", "kernel": "k_kick32_tma (gather+kick+FP64 accumulate)",
                          "achieved": achieved_kick, "peak": peak, "unit": "GB/s", "frac": achieved_kick / peak,
-                         "traffic": KICK_TRAFFIC_PER_PARTICLE * n, "peak_kind": peak_kind,
+                         "traffic": KICK_TRAFFIC_PER_PARTICLE * n, "peak_kind": peak_kind_text(peak_kind),
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_kick32_tma at 4M "
                                            "particles (profiles/k_kick32_tma_4M_64cube.txt), scaled by particles",
                          "algorithmic_bytes_per_launch": B_KICK_KERNEL_PER_PARTICLE * n,
@@ -589,8 +774,21 @@ def main():
                               "algorithmic_bytes_per_kick": B_PER_PARTICLE * n + 2 * 4 * math.prod(MESH)},
             "e2e": (None if args.kick_only else
                     {"value": e2e_value, "unit": "particle-kicks/s", "h2d_bytes_per_step": h2d,
-                     "d2h_bytes_per_step": d2h}),
+                     "d2h_bytes_per_step": d2h, "host_memory": "pinned", "ms_per_step": e2e_step_ms}),
+            "e2e_pageable": (None if args.kick_only else
+                             {"value": n * args.steps / e2e_page_dt, "unit": "particle-kicks/s",
+                              "ms_per_step": e2e_page_dt / args.steps * 1e3, "h2d_bytes_per_step": h2d,
+                              "d2h_bytes_per_step": d2h,
+                              "host_memory": "pageable numpy arrays, as track() passes them"}),
+            "e2e_roofline": (None if not link else
+                             {"bound": "host link", "h2d_gbs": link[0], "d2h_gbs": link[1], "link_ms": link_ms,
+                              "e2e_ms": e2e_step_ms, "frac": link_ms / e2e_step_ms,
+                              "how": "the step's copies at the measured pinned copy bandwidth (best of 5, CUDA "
+                                     "events) over the measured pinned e2e step"}),
+            "e2e_link_frac": (link_ms / e2e_step_ms) if link else None,
             "gpu_launches": launches32,
+            "config1": configs.get("config1"),
+            "config3": configs.get("config3"),
             "batched": batched,
             "serving": serving,
             "clocks": clk.summary(),
