@@ -245,72 +245,44 @@ def config_beam(cfg, seed=SEED):
     return flat_top_beam(cfg["n"], seed, charge=cfg["charge"])
 
 
-def rest_frame_positions(rp, energy_gev):
-    """Positions of the particles in the mean-velocity frame and gamma0, the
-    input of SpaceCharge.el_field (sc.py:218-240, coord_transform.py:57-96),
-    in numpy: the same particles for both forms' fields."""
-    import numpy as np
-    m = 9.10938215e-31 * 299792458.0 ** 2 / 1.6021766208e-19   # m_e_eV (ocelot/common/globals.py:13-18)
-    gamref = energy_gev * 1e9 / m
-    betaref = np.sqrt(1 - gamref ** -2)
-    gamma = (betaref * rp[5] + 1) * gamref
-    beta = np.sqrt(1 - gamma ** -2)
-    pz = np.sqrt(((gamma * beta) / (gamref * betaref)) ** 2 - rp[1] ** 2 - rp[3] ** 2)
-    u = np.stack([rp[1] / pz, rp[3] / pz, np.ones(rp.shape[1])])
-    u /= np.sqrt((u * u).sum(axis=0))
-    pos = np.stack([rp[0] - u[0] * beta * rp[4], rp[2] - u[1] * beta * rp[4], -u[2] * beta * rp[4]])
-    mom = u * (gamma * beta * m)
-    t3 = mom.mean(axis=1)
-    pav = np.linalg.norm(t3)
-    t3 = t3 / pav
-    t1 = np.cross([0.0, 1.0, 0.0], t3)
-    t1 /= np.linalg.norm(t1)
-    t2 = np.cross(t3, t1)
-    T = np.c_[t1, t2, t3]
-    return np.ascontiguousarray(pos.T @ T), float(np.sqrt((pav / m) ** 2 + 1))
-
-
-def form_errors(cfg, dev, seed=SEED + 1):
+def form_errors(cfg, dev, seed=SEED + 1, fp32_mode=None):
     """The FP32 form against the FP64 form on one kick of the same beam --
-    relative RMS errors of the grid potential, of E at the particles (the
-    rest-frame field, both forms' el_field on the same positions) and of the
-    momentum kicks (x', y', delta).  The FP64 form is itself within 1e-10 of
-    the oracle (tests); so these are the FP32 form's errors against FP64."""
-    import numpy as np
+    relative RMS errors of the grid potential, of the field at the particles
+    as the kick used it (both forms record it, SC_PARAM_RECORD_FIELD) and of
+    the momentum kicks (x', y', delta).  The FP64 form is itself within 1e-10
+    of the oracle (tests), so these are the FP32 form's errors."""
     import torch
-    from ocelot_gb300 import SpaceCharge
+    from ocelot_gb300 import SpaceCharge, _native as N
     rp, q = config_beam(cfg, seed)
     n, mesh = rp.shape[1], cfg["mesh"]
     r0 = torch.from_numpy(rp).to(dev)
     d_q = torch.from_numpy(q).to(dev)
-    out, phi = {}, {}
+    out, phi, field = {}, {}, {}
     for prec in ("fp64", "fp32"):
         d = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=dev)[:, :n]
         d.copy_(r0)
-        sc = SpaceCharge(nmesh_xyz=mesh, precision=prec, device=dev)
+        kw = {} if (prec == "fp64" or not fp32_mode) else fp32_mode
+        sc = SpaceCharge(nmesh_xyz=mesh, precision=prec, device=dev, **kw)
+        eng = sc.engine()
+        eng.set_param(N.SC_PARAM_RECORD_FIELD, 1)
         sc.apply_device(d, d_q, cfg["E"], cfg["dz"])
         sc.check()
         out[prec] = d
-        phi[prec] = sc.engine().region("phi").to(torch.float64)
-        del sc
+        phi[prec] = eng.region("phi").to(torch.float64)
+        field[prec] = eng.region("field", n).to(torch.float64)
+        del sc, eng
     rel = lambda a, b: float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))  # noqa: E731
     dp = {}
     for r, name in ((1, "dxp"), (3, "dyp"), (5, "ddelta")):
         k64 = out["fp64"][r] - r0[r]
         k32 = out["fp32"][r] - r0[r]
         dp[name] = float(torch.sqrt(torch.mean((k32 - k64) ** 2)) / torch.sqrt(torch.mean(k64 ** 2)))
-    del out
+    e_at = {c: rel(field["fp32"][k], field["fp64"][k]) for k, c in enumerate(("Ex", "Ey", "Ez"))}
+    res = {"phi": rel(phi["fp32"], phi["fp64"]), "E_at_particles": e_at, "kick": dp,
+           "vs": "FP64 form (itself within 1e-10 of the oracle), one kick, same beam", "beam_seed": seed}
+    del out, phi, field
     torch.cuda.empty_cache()
-    xyz, g0 = rest_frame_positions(rp, cfg["E"])
-    E = {}
-    for prec in ("fp64", "fp32"):
-        E[prec] = SpaceCharge(nmesh_xyz=mesh, precision=prec, device=dev).el_field(xyz.copy(), q, g0, mesh)
-    e_at = [float(np.linalg.norm(E["fp32"][:, c] - E["fp64"][:, c]) / np.linalg.norm(E["fp64"][:, c]))
-            for c in range(3)]
-    torch.cuda.empty_cache()
-    return {"phi": rel(phi["fp32"], phi["fp64"]), "E_at_particles": dict(zip(("Ex", "Ey", "Ez"), e_at)),
-            "kick": dp, "vs": "FP64 form (itself within 1e-10 of the oracle), one kick, same beam",
-            "beam_seed": seed}
+    return res
 
 
 def time_config(cfg, steps, warmup, dev, flush, cpu_threads=None):
@@ -663,7 +635,19 @@ def main():
                     help="time the FP32 kick alone (no other leg): the small case for profiling")
     ap.add_argument("--transport", type=int, default=0, metavar="N",
                     help="time the tracking transport kernels (slice forms, moments) on N particles and exit")
+    ap.add_argument("--tune", action="store_true",
+                    help="autotune the launch shapes on the benchmark meshes and particle counts, print the "
+                         "timings (and store them in the tuning table with --tune-save) and exit")
+    ap.add_argument("--tune-save", action="store_true")
     args = ap.parse_args()
+    if args.tune:
+        from ocelot_gb300 import tuning
+        cases = [((64, 64, 64), 2_000_000), ((64, 64, 64), 200_000), ((63, 63, 63), 200_000),
+                 ((128, 128, 256), 10_000_000), ((32, 32, 32), 100_000), ((96, 96, 96), 4_000_000),
+                 ((48, 48, 48), 1_000_000), ((32, 32, 128), 500_000)]
+        for shape, n in cases:
+            print(json.dumps(tuning.tune(shape, n, "fp32", save=args.tune_save)), flush=True)
+        return
     if args.transport:
         time_transport(args.transport, args.steps, max(args.warmup, 3))
         return

@@ -87,6 +87,11 @@ int sc_read_status(const sc_plan* plan, void* ws, void* stream);
 #define SC_REGION_KEYS 5
 #define SC_REGION_STATUS 6
 #define SC_REGION_FIRST_ERROR 7
+/* With SC_PARAM_RECORD_FIELD set: the field each particle of the last kick
+ * was kicked with -- the trilinear samples of Ex, Ey, Ez at the particle
+ * before the gamma0 factor (sc.py:201-204) -- as 3 rows of nX = n rounded up
+ * to a multiple of 4 (double for SC_FP64, float for SC_FP32). */
+#define SC_REGION_FIELD 8
 int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t* offset, int64_t* bytes);
 
 /* ---- the kick ---------------------------------------------------------- */
@@ -322,6 +327,25 @@ const char* sc_profile_stage_name(int stage);
 /* Number of kernels the plan's last sc_kick launched (host bookkeeping, no
  * synchronisation). */
 int sc_kick_launches(const sc_plan* plan);
+
+/* Launch shapes a plan may choose without changing any result (the
+ * autotuner's knobs, ocelot_gb300/tuning.py).  No counterpart in the
+ * reference, whose only knob is the FFT thread count (sc.py:152-160).
+ *   SC_PARAM_KICK_VARIANT: tiling of the FP32 gather + kick, 0 (default) ..
+ *     SC_KICK_NVARIANTS - 1, described by sc_kick_variant; every tiling runs
+ *     the same per-particle arithmetic, so the kick is bit-identical.
+ * Set between kicks (not during a stream capture that uses the plan). */
+#define SC_PARAM_KICK_VARIANT 0
+/*   SC_PARAM_RECORD_FIELD: 1 makes every kick also store the field at each
+ *     particle (SC_REGION_FIELD), for error measurements; the FP32 form then
+ *     runs its direct-access kick loop (same arithmetic, same particles). */
+#define SC_PARAM_RECORD_FIELD 1
+#define SC_KICK_NVARIANTS 6
+int sc_plan_set_param(sc_plan* plan, int param, int value);
+int sc_plan_get_param(const sc_plan* plan, int param, int* value);
+/* Tile (particles), tile buffers, particles per thread and blocks per SM of a
+ * kick variant. */
+int sc_kick_variant(int variant, int* tile, int* stages, int* particles_per_thread, int* blocks_per_sm);
 
 /* Failure detection of the bulk-copy waits.  The frame, extent and kick
  * kernels of the FP32 form stream particle rows through shared memory with

@@ -28,12 +28,17 @@ SC_ERR_TIMEOUT = 7
 
 SC_NSTAGES = 11
 
+# launch-shape parameters of a plan (sc_plan_set_param)
+SC_PARAM_KICK_VARIANT = 0
+SC_PARAM_RECORD_FIELD = 1
+SC_KICK_NVARIANTS = 6
+
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
 SC_WAIT_FRAME = 0
 SC_WAIT_EXTENT = 1
 SC_WAIT_KICK = 2
 
-REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7}
+REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7, "field": 8}
 
 ERROR_TEXT = {
     SC_ERR_DEGENERATE: "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)",
@@ -87,6 +92,10 @@ SIGNATURES = {
     "sc_profile_stage_name": (C.c_char_p, [C.c_int]),
     "sc_kick_launches": (C.c_int, [vp]),
     "sc_plan_set_wait_limit": (C.c_int, [vp, C.c_int, C.c_longlong]),
+    "sc_plan_set_param": (C.c_int, [vp, C.c_int, C.c_int]),
+    "sc_plan_get_param": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
+    "sc_kick_variant": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)]),
     "sc_last_error": (C.c_char_p, []),
     "sc_abi_version": (C.c_int, []),
 }

@@ -400,6 +400,42 @@ int sc_profile_read(sc_plan* plan, float* ms, int* n_launches) {
 
 int sc_kick_launches(const sc_plan* plan) { return plan ? plan->last_launches : 0; }
 
+int sc_plan_set_param(sc_plan* plan, int param, int value) {
+    if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
+    switch (param) {
+        case SC_PARAM_KICK_VARIANT:
+            if (value < 0 || value >= SC_KICK_NVARIANTS)
+                return fail(SC_ERR_ARG, "kick variant %d not in [0, %d)", value, SC_KICK_NVARIANTS);
+            plan->p.kick_variant = value;
+            return SC_OK;
+        case SC_PARAM_RECORD_FIELD:
+            if (value != 0 && value != 1) return fail(SC_ERR_ARG, "record field must be 0 or 1");
+            plan->p.record_field = value;
+            return SC_OK;
+        default: return fail(SC_ERR_ARG, "unknown plan parameter %d", param);
+    }
+}
+
+int sc_plan_get_param(const sc_plan* plan, int param, int* value) {
+    if (!plan || !value) return fail(SC_ERR_ARG, "plan or value is NULL");
+    switch (param) {
+        case SC_PARAM_KICK_VARIANT: *value = plan->p.kick_variant; return SC_OK;
+        case SC_PARAM_RECORD_FIELD: *value = plan->p.record_field; return SC_OK;
+        default: return fail(SC_ERR_ARG, "unknown plan parameter %d", param);
+    }
+}
+
+int sc_kick_variant(int variant, int* tile, int* stages, int* particles_per_thread, int* blocks_per_sm) {
+    int t = 0, st = 0, ppt = 0, mb = 0;
+    if (!kick_variant_info(variant, &t, &st, &ppt, &mb))
+        return fail(SC_ERR_ARG, "kick variant %d not in [0, %d)", variant, SC_KICK_NVARIANTS);
+    if (tile) *tile = t;
+    if (stages) *stages = st;
+    if (particles_per_thread) *particles_per_thread = ppt;
+    if (blocks_per_sm) *blocks_per_sm = mb;
+    return SC_OK;
+}
+
 int sc_plan_set_wait_limit(sc_plan* plan, int kernel, long long tries) {
     if (!plan) return fail(SC_ERR_ARG, "plan is NULL");
     if (kernel < -1 || kernel > 2) return fail(SC_ERR_ARG, "kernel %d: SC_WAIT_FRAME, _EXTENT, _KICK or -1", kernel);
@@ -439,6 +475,10 @@ int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t*
         case SC_REGION_EY: *offset = (int64_t)L.ey; *bytes = (int64_t)(rs * ncell); break;
         case SC_REGION_EZ: *offset = (int64_t)L.ez; *bytes = (int64_t)(rs * ncell); break;
         case SC_REGION_KEYS: *offset = (int64_t)L.keys; *bytes = (int64_t)(4 * (size_t)n_max); break;
+        case SC_REGION_FIELD:
+            *offset = (int64_t)L.X;
+            *bytes = (int64_t)(rs * 3 * (size_t)((n_max + 3) / 4 * 4));
+            break;
         case SC_REGION_STATUS:
             *offset = (int64_t)(L.state + offsetof(ScState, status));
             *bytes = (int64_t)sizeof(int);

@@ -163,7 +163,11 @@ struct Plan {
     int sm_count;
     int part_blocks;   // blocks of the per-particle reduction kernels
     unsigned wait_limit[3];  // KickParams::wait_limit of this plan's kicks
+    int kick_variant;        // tiling of the FP32 gather + kick (sc_particles.cu, SC_KICK_VARIANTS)
+    int record_field;        // the kick also stores the field at each particle (SC_REGION_FIELD)
 };
+// tile, tile buffers, particles per thread and blocks per SM of kick variant v (0 if v is out of range)
+int kick_variant_info(int v, int* tile, int* stages, int* ppt, int* minb);
 
 Layout make_layout(const Plan& p, int64_t n);
 

@@ -323,6 +323,17 @@ __device__ __forceinline__ float d2f_nr(double d, unsigned& range) {
     return __uint_as_float((t & 0x7fffffffu) | (hi & 0x80000000u));
 }
 __device__ __forceinline__ bool d2f_range_ok(unsigned range) { return range < (254u << 21); }
+// d2f_exact without its branches, for the kick: FP32's normal range as
+// d2f_nr; magnitudes below it give +-0 and above it +-infinity (NaN too --
+// the kick never sees either: the frame and extent latch non-finite and
+// out-of-range data first).  Same bits as d2f_exact for every finite double.
+__device__ __forceinline__ float d2f_kick(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned sign = hi & 0x80000000u, mag = hi & 0x7fffffffu;
+    const unsigned t = (__funnelshift_l(lo, hi, 3) + 0x40000000u + ((lo >> 28) & 1u)) & 0x7fffffffu;
+    const unsigned f = mag < (897u << 20) ? 0u : (mag >= (1151u << 20) ? 0x7f800000u : t);
+    return __uint_as_float(f | sign);
+}
 __device__ __forceinline__ float d2f(double d) {
     unsigned range = 0u;
     const float f = d2f_nr(d, range);
@@ -1713,10 +1724,13 @@ __device__ __forceinline__ void gather3o(const float* ox, const float* oy, const
     e2 = trilerp_o(oz, nx, ny, nz, X0 + 0.5f, X1 + 0.5f, X2);
 }
 
+// rec != nullptr (the record-field mode): the field samples before the gamma0
+// factor go to rec[i], rec[nX + i], rec[2 nX + i] (rec may be X itself: each
+// thread writes only the entries it has read)
 __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const double* __restrict__ xp,
-                                               const double* __restrict__ X, const double* __restrict__ ex,
+                                               const double* X, const double* __restrict__ ex,
                                                const double* __restrict__ ey, const double* __restrict__ ez,
-                                               KickParams kp, const ScState* st) {
+                                               KickParams kp, const ScState* st, double* rec) {
     pdl_wait();
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld;
@@ -1727,6 +1741,11 @@ __global__ void __launch_bounds__(PT) k_kick64(double* __restrict__ rp, const do
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double e0, e1, e2;
         gather3<double>(ex, ey, ez, kp.nx, kp.ny, kp.nz, X[i], X[kp.nX + i], X[2 * kp.nX + i], e0, e1, e2);
+        if (rec) {
+            rec[i] = e0;
+            rec[kp.nX + i] = e1;
+            rec[2 * kp.nX + i] = e2;
+        }
         e0 = __dmul_rn(e0, g0);
         e1 = __dmul_rn(e1, g0);
         const double p0 = xp[3 * n + i], p1 = xp[4 * n + i], p2 = xp[5 * n + i];
@@ -1810,17 +1829,21 @@ __device__ __forceinline__ float oct_sample(const float* __restrict__ O, const A
 // approximate reciprocal and square root, so the kick reads nothing per
 // particle but rparticles.  (The NGP keys, which must equal the FP64 form's,
 // are decided by the keys kernel alone; the gather only needs the grid
-// coordinates to FP32 accuracy.)  The conversions are the full-range inline
-// forms: with the range-checked forms and their out-of-line fallbacks the
-// kick kernel, at its 80-register limit, ran 15% slower.
-__device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp) {
+// coordinates to FP32 accuracy.)  The conversions are branch-free inline
+// forms (d2f_kick, f2d_exact): with range-checked forms and out-of-line
+// fallbacks the kick kernel, at its 80-register limit, ran 15% slower.
+// rec != nullptr (the record-field mode): the three field samples, the
+// trilinear gathers of Ex, Ey, Ez at the particle before the gamma0 factor
+// (sc.py:201-204), are stored at rec[0], rec[nX], rec[2 nX].
+__device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp,
+                                         float* rec = nullptr) {
     float px, py, pz, E;
-    mom32(d2f_exact(r[1]), d2f_exact(r[3]), d2f_exact(r[5]), kp, px, py, pz, E);
+    mom32(d2f_kick(r[1]), d2f_kick(r[3]), d2f_kick(r[5]), kp, px, py, pz, E);
     // lab position, rotated and scaled to the grid
-    const float tau = d2f_exact(r[4]);
+    const float tau = d2f_kick(r[4]);
     const float iE = rcpf(E);
     float l[3];
-    lab32(d2f_exact(r[0]), d2f_exact(r[2]), tau, px, py, pz, E, kp, l);
+    lab32(d2f_kick(r[0]), d2f_kick(r[2]), tau, px, py, pz, E, kp, l);
     float X[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -1832,6 +1855,11 @@ __device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const
     const float e0 = oct_sample(C.ox, a0, b1, b2, kp.ny, kp.nz);
     const float e1 = oct_sample(C.oy, b0, a1, b2, kp.ny, kp.nz);
     const float e2 = oct_sample(C.oz, b0, b1, a2, kp.ny, kp.nz);
+    if (rec) {
+        rec[0] = e0;
+        rec[kp.nX] = e1;
+        rec[2 * kp.nX] = e2;
+    }
     // kick in the beam frame, rotated back to the lab (sc.py:244-250)
     const float d0 = C.kxyg * e0, d1 = C.kxyg * e1, d2 = C.kz * e2;
     const float dpx = fmaf(C.T[0][0], d0, fmaf(C.T[0][1], d1, C.T[0][2] * d2));
@@ -1865,10 +1893,11 @@ __device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const
 
 // Gather + kick with direct row accesses: each thread takes G consecutive
 // particles with one 32-byte (G = 4) or 16-byte (G = 2) access per row.
-template <int G>
+template <int G, bool REC = false>
 __device__ __forceinline__ void kick32_body(double* __restrict__ rp, const float* __restrict__ ox,
                                             const float* __restrict__ oy, const float* __restrict__ oz,
-                                            const KickParams& kp, const ScState* st, VBlk vb) {
+                                            const KickParams& kp, const ScState* st, VBlk vb,
+                                            float* __restrict__ rec = nullptr) {
     if (st->status) return;
     const int64_t n = kp.n, ld = kp.ld;
     const Kick32C C = kick32_const(st, kp, ox, oy, oz);
@@ -1882,7 +1911,7 @@ __device__ __forceinline__ void kick32_body(double* __restrict__ rp, const float
         double x[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) x[k] = r[k][w];
-        kick_one(x, C, kp);
+        kick_one(x, C, kp, REC ? rec + i0_ + w : nullptr);
 #pragma unroll
         for (int k = 0; k < 6; ++k) r[k][w] = x[k];
     }
@@ -1892,27 +1921,33 @@ __device__ __forceinline__ void kick32_body(double* __restrict__ rp, const float
 }
 
 // Gather + kick with the rows staged through shared memory by bulk (TMA)
-// copies.  A block walks its tiles of KT_TILE particles (tiles vb.x,
-// vb.x + vb.nx, ...); KT_STAGES tile buffers of the six rows rotate: while
-// the block kicks one tile, the loads of the next KT_STAGES - 1 are in
-// flight, so the HBM stream does not wait for the gathers.  Each thread
-// kicks particles 2t and 2t+1 of a tile in place in shared memory, and one
-// bulk store per row writes the tile back.  Rows must be 16-byte aligned
-// with an even stride.  A tile's copies cover its first (count & ~1)
-// particles; an odd last particle of the beam is read and written directly.
-constexpr int KT_TILE = 512;
-constexpr int KT_STAGES = 3;
-constexpr size_t KT_SMEM = (size_t)KT_STAGES * 6 * KT_TILE * sizeof(double) + KT_STAGES * sizeof(uint64_t);
+// copies.  A block walks its tiles of TILE particles (its first tile is its
+// block index, every further one is claimed at run time); STAGES tile
+// buffers of the six rows rotate: while the block kicks one tile, the loads
+// of the next STAGES - 1 are in flight, so the HBM stream does not wait for
+// the gathers.  Each of the TILE / PPT threads kicks PPT adjacent particles of
+// a tile in place in shared memory, and one bulk store per row writes the
+// tile back.  Rows must be 16-byte aligned with an even stride.  A tile's
+// copies cover its first (count & ~1) particles; an odd last particle of the
+// beam is read and written directly.  Every particle's arithmetic is
+// kick_one whatever the tiling, so all tilings give the same bits.
+template <int TILE, int STAGES, int PPT>
+struct KickTiling {
+    static_assert(PPT == 1 || PPT == 2, "one or two particles per thread");
+    static constexpr int threads = TILE / PPT;
+    static constexpr size_t smem = (size_t)STAGES * 6 * TILE * sizeof(double) + STAGES * sizeof(uint64_t);
+};
 
+template <int TILE, int STAGES, int PPT>
 __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const float* __restrict__ ox,
                                                 const float* __restrict__ oy, const float* __restrict__ oz,
                                                 const KickParams& kp, ScState* st, VBlk vb) {
     extern __shared__ __align__(128) unsigned char smraw[];
     if (__syncthreads_or(st->status != SC_OK)) return;
-    double* buf = reinterpret_cast<double*>(smraw);  // [KT_STAGES][6][KT_TILE]
-    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + KT_STAGES * 6 * KT_TILE);
+    double* buf = reinterpret_cast<double*>(smraw);  // [STAGES][6][TILE]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + STAGES * 6 * TILE);
     const int64_t n = kp.n, ld = kp.ld;
-    const int64_t ntile = (n + KT_TILE - 1) / KT_TILE;
+    const int64_t ntile = (n + TILE - 1) / TILE;
     const bool lead = threadIdx.x == 0;
     // Tiles are handed out at run time: a block's first tile is its index,
     // each further one is claimed from the kick's tile counter when its
@@ -1920,32 +1955,32 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
     // blocks finish together.  s_tile[s] is the tile in buffer s; a tile
     // index >= ntile marks the end.  (The tiles are independent: which block
     // kicks a particle does not change its result.)
-    __shared__ int64_t s_tile[KT_STAGES];
+    __shared__ int64_t s_tile[STAGES];
     if (lead) {
-        for (int s = 0; s < KT_STAGES; ++s) mbar_init(&bar[s], 1);
+        for (int s = 0; s < STAGES; ++s) mbar_init(&bar[s], 1);
         mbar_init_fence();
     }
     __syncthreads();
-    auto tile_start = [&](int64_t g) { return g * (int64_t)KT_TILE; };
+    auto tile_start = [&](int64_t g) { return g * (int64_t)TILE; };
     auto tile_count = [&](int64_t g) {
         const int64_t c = n - tile_start(g);
-        return (int)(c < KT_TILE ? c : KT_TILE);
+        return (int)(c < TILE ? c : TILE);
     };
     auto claim = [&]() { return (int64_t)vb.nx + (int64_t)atomicAdd(&st->kick_next, 1u); };
-    auto issue = [&](int64_t u, int64_t g) {  // lead thread: tile g as the block's u-th, into buffer u % KT_STAGES
-        const int s = (int)(u % KT_STAGES);
+    auto issue = [&](int64_t u, int64_t g) {  // lead thread: tile g as the block's u-th, into buffer u % STAGES
+        const int s = (int)(u % STAGES);
         s_tile[s] = g;
         if (g >= ntile) return;
         const int64_t i0 = tile_start(g);
         const unsigned bytes = (unsigned)(tile_count(g) & ~1) * 8u;
         mbar_arrive_expect_tx(&bar[s], 6u * bytes);
         if (bytes)
-            for (int k = 0; k < 6; ++k) bulk_load(buf + (s * 6 + k) * KT_TILE, rp + k * ld + i0, bytes, &bar[s]);
+            for (int k = 0; k < 6; ++k) bulk_load(buf + (s * 6 + k) * TILE, rp + k * ld + i0, bytes, &bar[s]);
     };
     int64_t issued = 0;  // lead: tiles issued (the end marker included)
     bool more = true;    // lead: the last claim was a tile
     if (lead)
-        for (int u = 0; u < KT_STAGES && more; ++u) {
+        for (int u = 0; u < STAGES && more; ++u) {
             const int64_t g = u == 0 ? (int64_t)vb.x : claim();
             issue(issued++, g);
             more = g < ntile;
@@ -1955,19 +1990,19 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
     int64_t t = 0;
     bool failed = false;
     for (;; ++t) {
-        const int s = (int)(t % KT_STAGES);
+        const int s = (int)(t % STAGES);
         const int64_t g = s_tile[s];
         if (g >= ntile) break;  // the same in every thread
         const int64_t i0 = tile_start(g);
         const int cnt = tile_count(g), staged = cnt & ~1;
-        const bool ok = mbar_wait(&bar[s], (unsigned)((t / KT_STAGES) & 1), kp.wait_limit[2]);
-        double* B = buf + s * 6 * KT_TILE;
-        const int j = 2 * threadIdx.x;
-        if (j + 1 < staged) {  // both particles staged: 16-byte shared accesses
+        const bool ok = mbar_wait(&bar[s], (unsigned)((t / STAGES) & 1), kp.wait_limit[2]);
+        double* B = buf + s * 6 * TILE;
+        const int j = PPT * threadIdx.x;
+        if (PPT == 2 && j + 1 < staged) {  // both particles staged: 16-byte shared accesses
             double r[2][6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
-                const double2 v = *reinterpret_cast<const double2*>(B + k * KT_TILE + j);
+                const double2 v = *reinterpret_cast<const double2*>(B + k * TILE + j);
                 r[0][k] = v.x;
                 r[1][k] = v.y;
             }
@@ -1975,7 +2010,14 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
             kick_one(r[1], C, kp);
 #pragma unroll
             for (int k = 0; k < 6; ++k)
-                *reinterpret_cast<double2*>(B + k * KT_TILE + j) = make_double2(r[0][k], r[1][k]);
+                *reinterpret_cast<double2*>(B + k * TILE + j) = make_double2(r[0][k], r[1][k]);
+        } else if (PPT == 1 && j < staged) {
+            double r[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) r[k] = B[k * TILE + j];
+            kick_one(r, C, kp);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) B[k * TILE + j] = r[k];
         } else if (j < cnt && ok) {  // the odd last particle of the beam (j == staged): read and written directly
             double r[6];
             for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i0 + j];
@@ -1989,7 +2031,7 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
         }
         if (lead) {
             if (staged)
-                for (int k = 0; k < 6; ++k) bulk_store(rp + k * ld + i0, B + k * KT_TILE, (unsigned)staged * 8u);
+                for (int k = 0; k < 6; ++k) bulk_store(rp + k * ld + i0, B + k * TILE, (unsigned)staged * 8u);
             bulk_commit();
             // refill the previous tile's buffer once its store has read it
             if (t >= 1 && more) {
@@ -1999,37 +2041,48 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
                 more = g2 < ntile;
             }
         }
-        // the buffer refilled here is read KT_STAGES - 1 iterations on, after
+        // the buffer refilled here is read STAGES - 1 iterations on, after
         // the barriers of the iterations between
     }
     if (lead) {
         if (failed) {
             atomicCAS(&st->status, SC_OK, SC_ERR_TIMEOUT);
             for (int64_t u = t; u < issued; ++u)  // loads still in flight must land before the block exits
-                if (s_tile[u % KT_STAGES] < ntile) mbar_wait(&bar[u % KT_STAGES], (unsigned)((u / KT_STAGES) & 1));
+                if (s_tile[u % STAGES] < ntile) mbar_wait(&bar[u % STAGES], (unsigned)((u / STAGES) & 1));
         }
         bulk_wait_all();
     }
 }
 
-constexpr int KICK_MIN_BLOCKS = 3;  // blocks per SM the kick kernels are compiled for
+// The kick's tilings: (tile, tile buffers, particles per thread, blocks per
+// SM the kernel is compiled for).  Variant 0 is the default; a plan's
+// kick_variant selects another (autotuned per mesh and particle count).
+#define SC_KICK_VARIANTS(X)  \
+    X(0, 512, 3, 2, 3)       \
+    X(1, 512, 2, 2, 4)       \
+    X(2, 256, 3, 1, 4)       \
+    X(3, 256, 2, 1, 5)       \
+    X(4, 128, 4, 1, 8)       \
+    X(5, 256, 4, 1, 3)
 
-template <int G>
+template <int TILE, int STAGES, int PPT, int MINB>
+__global__ void __launch_bounds__(KickTiling<TILE, STAGES, PPT>::threads, MINB)
+    k_kick32_tma(double* __restrict__ rp, const float* __restrict__ ox, const float* __restrict__ oy,
+                 const float* __restrict__ oz, KickParams kp, ScState* st) {
+    pdl_wait();
+    kick32_tma_body<TILE, STAGES, PPT>(rp, ox, oy, oz, kp, st, hw_vblk());
+}
+
+constexpr int KICK_MIN_BLOCKS = 3;  // blocks per SM of the direct-access kick kernels
+
+// rec != nullptr only in the record-field mode (REC)
+template <int G, bool REC = false>
 __global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) k_kick32(double* __restrict__ rp, const float* __restrict__ ox,
                                                                 const float* __restrict__ oy,
                                                                 const float* __restrict__ oz, KickParams kp,
-                                                                const ScState* st) {
+                                                                const ScState* st, float* __restrict__ rec) {
     pdl_wait();
-    kick32_body<G>(rp, ox, oy, oz, kp, st, hw_vblk());
-}
-
-__global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) k_kick32_tma(double* __restrict__ rp,
-                                                                    const float* __restrict__ ox,
-                                                                    const float* __restrict__ oy,
-                                                                    const float* __restrict__ oz, KickParams kp,
-                                                                    ScState* st) {
-    pdl_wait();
-    kick32_tma_body(rp, ox, oy, oz, kp, st, hw_vblk());
+    kick32_body<G, REC>(rp, ox, oy, oz, kp, st, hw_vblk(), rec);
 }
 
 // particles per row access the kick can use: 4 with 32-byte aligned rows and
@@ -2108,8 +2161,9 @@ __global__ void __launch_bounds__(PT, 4) kb_keys32(const BatchBeam* __restrict__
     else keys32_body<false>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
 }
 
-__global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) kb_kick32(const BatchBeam* __restrict__ beams,
-                                                                 const int* __restrict__ start, int nb) {
+template <int TILE, int STAGES, int PPT, int MINB>
+__global__ void __launch_bounds__(KickTiling<TILE, STAGES, PPT>::threads, MINB)
+    kb_kick32(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
     pdl_wait();
     const int b = batch_beam(start, nb);
     const BatchBeam& B = beams[b];
@@ -2118,8 +2172,36 @@ __global__ void __launch_bounds__(PT, KICK_MIN_BLOCKS) kb_kick32(const BatchBeam
     const float* ox = reinterpret_cast<const float*>(B.ws + B.L.exq);
     const float* oy = reinterpret_cast<const float*>(B.ws + B.L.eyq);
     const float* oz = reinterpret_cast<const float*>(B.ws + B.L.ezq);
-    if (kick_group(B.rp, B.kp.ld) >= 2) kick32_tma_body(B.rp, ox, oy, oz, B.kp, st, vb);
-    else kick32_body<1>(B.rp, ox, oy, oz, B.kp, st, vb);
+    if (kick_group(B.rp, B.kp.ld) >= 2) kick32_tma_body<TILE, STAGES, PPT>(B.rp, ox, oy, oz, B.kp, st, vb);
+    else if (PPT == 2) kick32_body<1>(B.rp, ox, oy, oz, B.kp, st, vb);  // 256 threads: the direct-access loop
+}
+
+// the compiled kick tilings, indexed by a plan's kick_variant
+using KickFn = void (*)(double*, const float*, const float*, const float*, KickParams, ScState*);
+using KickBatchFn = void (*)(const BatchBeam*, const int*, int);
+struct KickVariant {
+    KickFn fn;
+    KickBatchFn batch_fn;
+    int tile, stages, ppt, minb, threads;
+    size_t smem;
+};
+static const KickVariant kKickVariants[] = {
+#define SC_KV(i, T, S, P, M) \
+    {k_kick32_tma<T, S, P, M>, kb_kick32<T, S, P, M>, T, S, P, M, KickTiling<T, S, P>::threads, KickTiling<T, S, P>::smem},
+    SC_KICK_VARIANTS(SC_KV)
+#undef SC_KV
+};
+constexpr int kNumKickVariants = (int)(sizeof(kKickVariants) / sizeof(kKickVariants[0]));
+static_assert(kNumKickVariants == SC_KICK_NVARIANTS, "SC_KICK_NVARIANTS must count SC_KICK_VARIANTS");
+
+int kick_variant_info(int v, int* tile, int* stages, int* ppt, int* minb) {
+    if (v < 0 || v >= kNumKickVariants) return 0;
+    const KickVariant& k = kKickVariants[v];
+    *tile = k.tile;
+    *stages = k.stages;
+    *ppt = k.ppt;
+    *minb = k.minb;
+    return 1;
 }
 
 cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, const int* start, int nb, int blocks,
@@ -2129,7 +2211,12 @@ cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, co
         case BP_FRAME: launch(kb_frame32, blocks, PT, FR_SMEM, s, beams, start, nb); break;
         case BP_EXTENT: launch(kb_extent32, blocks, PT, EX_SMEM, s, beams, start, nb); break;
         case BP_KEYS: launch(kb_keys32, blocks, PT, 0, s, beams, start, nb); break;
-        case BP_KICK: launch(kb_kick32, blocks, PT, KT_SMEM, s, beams, start, nb); break;
+        case BP_KICK: {
+            // the batch's particle blocks are sized for 256 threads (BS_PART): the tilings of 256 threads
+            const KickVariant& v = kKickVariants[0];
+            launch(v.batch_fn, blocks, v.threads, v.smem, s, beams, start, nb);
+            break;
+        }
     }
     return cudaGetLastError();
 }
@@ -2139,8 +2226,10 @@ cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, co
 // ---------------------------------------------------------------------------
 cudaError_t prepare_particle_kernels() {
     cudaError_t e;
-    if ((e = smem_opt_in(reinterpret_cast<const void*>(k_kick32_tma), KT_SMEM))) return e;
-    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_kick32), KT_SMEM))) return e;
+    for (int v = 0; v < kNumKickVariants; ++v) {
+        if ((e = set_smem(kKickVariants[v].fn, kKickVariants[v].smem))) return e;
+        if ((e = set_smem(kKickVariants[v].batch_fn, kKickVariants[v].smem))) return e;
+    }
     if ((e = set_smem(k_frame32_tma, FR_SMEM))) return e;
     if ((e = set_smem(kb_frame32, FR_SMEM))) return e;
     if ((e = set_smem(k_extent32_tma, EX_SMEM))) return e;
@@ -2249,7 +2338,7 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
         launch(k_kick64, nb, PT, 0, s, rp, reinterpret_cast<const double*>(ws + L.xp),
                                    reinterpret_cast<const double*>(ws + L.X), reinterpret_cast<const double*>(ws + L.ex),
                                    reinterpret_cast<const double*>(ws + L.ey), reinterpret_cast<const double*>(ws + L.ez),
-                                   kp, st);
+                                   kp, st, p.record_field ? reinterpret_cast<double*>(ws + L.X) : nullptr);
     else
     {
         const float* ox = reinterpret_cast<const float*>(ws + L.exq);
@@ -2257,12 +2346,16 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
         const float* oz = reinterpret_cast<const float*>(ws + L.ezq);
         const int g = kick_group(rp, kp.ld);
         // one wave of resident blocks, each looping over its tiles or groups
-        const int64_t units = g >= 2 ? (kp.n + KT_TILE - 1) / KT_TILE : (kp.n + PT - 1) / PT;
-        const int64_t kb = units < (int64_t)p.sm_count * KICK_MIN_BLOCKS ? units : (int64_t)p.sm_count * KICK_MIN_BLOCKS;
+        const KickVariant& v = kKickVariants[p.kick_variant >= 0 && p.kick_variant < kNumKickVariants ? p.kick_variant : 0];
+        const int minb = g >= 2 ? v.minb : KICK_MIN_BLOCKS;
+        const int64_t units = g >= 2 ? (kp.n + v.tile - 1) / v.tile : (kp.n + PT - 1) / PT;
+        const int64_t kb = units < (int64_t)p.sm_count * minb ? units : (int64_t)p.sm_count * minb;
         const int nbk = (int)(kb > 0 ? kb : 1);
         ScState* stw = reinterpret_cast<ScState*>(ws + L.state);
-        if (g >= 2) launch(k_kick32_tma, nbk, PT, KT_SMEM, s, rp, ox, oy, oz, kp, stw);
-        else launch(k_kick32<1>, nbk, PT, 0, s, rp, ox, oy, oz, kp, st);
+        if (p.record_field)  // the direct-access loop, storing the field samples in the X rows
+            launch(k_kick32<1, true>, nbk, PT, 0, s, rp, ox, oy, oz, kp, st, reinterpret_cast<float*>(ws + L.X));
+        else if (g >= 2) launch(v.fn, nbk, v.threads, v.smem, s, rp, ox, oy, oz, kp, stw);
+        else launch(k_kick32<1, false>, nbk, PT, 0, s, rp, ox, oy, oz, kp, st, nullptr);
     }
     return cudaGetLastError();
 }

@@ -66,7 +66,7 @@ def _stream(device) -> C.c_void_p:
 class Engine:
     """A plan (mesh shape, precision) and its device workspace on one GPU."""
 
-    def __init__(self, shape, precision: str, device=None, mode=None):
+    def __init__(self, shape, precision: str, device=None, mode=None, tuned: bool = True):
         torch = _torch()
         if not torch.cuda.is_available():
             raise N.NativeLibraryError("ocelot_gb300 needs a CUDA device; there is no CPU fallback")
@@ -81,6 +81,10 @@ class Engine:
         self.plan = plan
         self.ws = None
         self.cap = -1
+        # launch shapes from the autotuner's table (ocelot_gb300/tuning.py),
+        # applied per particle count; tuned=False keeps the plan's defaults
+        self.tuned = bool(tuned)
+        self._tuned_n = None
         self._rp = None
         self._q = None
 
@@ -122,6 +126,11 @@ class Engine:
         """Launch one kick on the current stream (asynchronous)."""
         torch = _torch()
         self.ensure(n)
+        if self.tuned and self._tuned_n != n:
+            from . import tuning
+            for param, value in tuning.lookup(self.precision, self.shape, n).items():
+                self.set_param(param, value)
+            self._tuned_n = n
         ld = rp.stride(0)
         if rp.stride(1) != 1:
             raise ValueError("rparticles rows must be contiguous")
@@ -130,10 +139,11 @@ class Engine:
                                      float(energy_gev), float(zstep), float(mesh_scale), float(mesh_shift),
                                      _stream(self.device)))
 
-    def region(self, name: str):
+    def region(self, name: str, n: int | None = None):
         """A view of an intermediate of the last call (charge grid, potential,
         field grids [nx][ny][nz]; keys [n]; the status ints "status" and
-        "first_error", one element each)."""
+        "first_error", one element each; "field" [3, nX], the field at each
+        particle of the last kick when SC_PARAM_RECORD_FIELD is set)."""
         torch = _torch()
         off, nb = C.c_int64(), C.c_int64()
         N.check(self.lib.sc_workspace_region(self.plan, max(self.cap, 0), N.REGIONS[name], C.byref(off), C.byref(nb)))
@@ -141,6 +151,11 @@ class Engine:
         if name in ("keys", "status", "first_error"):
             return raw.view(torch.int32)
         dt = torch.float64 if self.precision == "fp64" else torch.float32
+        if name == "field":
+            # rows of nX = n rounded up to 4, n the particle count of the last kick
+            n = self.cap if n is None else int(n)
+            nX = (n + 3) // 4 * 4
+            return raw.view(dt)[:3 * nX].view(3, nX)[:, :n]
         return raw.view(dt).view(self.shape)
 
     def profile(self, enable: bool = True):
@@ -157,6 +172,15 @@ class Engine:
         N.check(self.lib.sc_profile_read(self.plan, ms, C.byref(nl)))
         names = [self.lib.sc_profile_stage_name(i).decode() for i in range(N.SC_NSTAGES)]
         return dict(zip(names, [float(v) for v in ms])), nl.value
+
+    def set_param(self, param: int, value: int):
+        """A launch-shape parameter of the plan (N.SC_PARAM_*); results do not change."""
+        N.check(self.lib.sc_plan_set_param(self.plan, int(param), int(value)))
+
+    def get_param(self, param: int) -> int:
+        v = C.c_int()
+        N.check(self.lib.sc_plan_get_param(self.plan, int(param), C.byref(v)))
+        return v.value
 
     def set_wait_limit(self, kernel: int = -1, tries: int = -1):
         """Iteration limit of the bulk-copy waits of one FP32 kernel
