@@ -127,14 +127,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def time_form(precision, n, steps, warmup, dev, flush):
+def time_form(precision, n, steps, warmup, dev, flush, fields="difference"):
     """Device-resident kicks; per-kick CUDA events; per-stage events from the library."""
     import torch
     from ocelot_gb300 import SpaceCharge
     rp, q = beam(n)
     d_rp = torch.from_numpy(rp).to(dev)
     d_q = torch.from_numpy(q).to(dev)
-    sc = SpaceCharge(nmesh_xyz=MESH, precision=precision, device=dev)
+    sc = SpaceCharge(nmesh_xyz=MESH, precision=precision, device=dev, fields=fields)
     eng = sc.engine()
     eng.ensure(n)
     stream = torch.cuda.current_stream(dev)
@@ -231,11 +231,11 @@ CONFIG1 = {"key": "config1", "form": "fp64", "n": 200_000, "mesh": [63, 63, 63],
            "workload": "plain FP64 form: 200k particles, 6D Gaussian (sigma_x = sigma_y = 50 um, sigma_x' = "
                        "sigma_y' = 1e-5, sigma_tau = 100 um, sigma_delta = 1e-4), 130 MeV, 250 pC, 63^3 mesh, "
                        "10 kicks of 0.1 m"}
-CONFIG3 = {"key": "config3", "form": "fp32", "n": 10_000_000, "mesh": [128, 128, 256], "E": 0.0065,
-           "charge": 500e-12, "dz": 0.05, "kicks": 20, "beam": "flat",
-           "workload": "low-energy stress case, FP32 form: 10M particles at 6.5 MeV, 500 pC, flat-top tau of "
-                       "2 mm with 100 um Gaussian edges, chirp delta += -10 tau, transverse Gaussian 200 um with "
-                       "a 1 mrad x-tau tilt, 128x128x256 mesh, 20 kicks of 0.05 m"}
+CONFIG3 = {"key": "config3", "form": "fp32", "fields": "spectral", "n": 10_000_000, "mesh": [128, 128, 256],
+           "E": 0.0065, "charge": 500e-12, "dz": 0.05, "kicks": 20, "beam": "flat",
+           "workload": "low-energy stress case, FP32 form with spectral fields: 10M particles at 6.5 MeV, 500 pC, "
+                       "flat-top tau of 2 mm with 100 um Gaussian edges, chirp delta += -10 tau, transverse "
+                       "Gaussian 200 um with a 1 mrad x-tau tilt, 128x128x256 mesh, 20 kicks of 0.05 m"}
 
 
 def config_beam(cfg, seed=SEED):
@@ -296,7 +296,7 @@ def time_config(cfg, steps, warmup, dev, flush, cpu_threads=None):
     r0 = torch.from_numpy(rp).to(dev)
     d_rp = torch.empty((6, n + (n & 1)), dtype=torch.float64, device=dev)[:, :n]
     d_q = torch.from_numpy(q).to(dev)
-    sc = SpaceCharge(nmesh_xyz=mesh, precision=cfg["form"], device=dev)
+    sc = SpaceCharge(nmesh_xyz=mesh, precision=cfg["form"], device=dev, fields=cfg.get("fields", "difference"))
     eng = sc.engine()
     eng.ensure(n)
     stream = torch.cuda.current_stream(dev)
@@ -330,7 +330,8 @@ def time_config(cfg, steps, warmup, dev, flush, cpu_threads=None):
     b_kick = B_PER_PARTICLE * n + 2 * w * ncell
     peak, kind = peaks()
     achieved = b_kick * cfg["kicks"] / t / 1e9
-    out = {"workload": cfg["workload"], "form": cfg["form"], "n_particles": n, "mesh": mesh,
+    out = {"workload": cfg["workload"], "form": cfg["form"], "fields": cfg.get("fields", "difference"),
+           "n_particles": n, "mesh": mesh,
            "kicks_per_step": cfg["kicks"], "steps": steps, "warmup": warmup,
            "value": n * cfg["kicks"] / t, "unit": "particle-kicks/s", "ms_per_step": t * 1e3,
            "ms_per_kick": t * 1e3 / cfg["kicks"], "gpu_launches": launches, "stages_ms_one_kick": stages,
@@ -688,6 +689,8 @@ def main():
         kick32, stages32, launches32 = time_form("fp32", n, args.steps, args.warmup, dev, flush)
         barrier()
     kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
+    kicksp, stagessp, _ = ([], {}, 0) if args.kick_only else time_form("fp32", n, args.steps, 3, dev, flush,
+                                                                     fields="spectral")
     e2e_dt, h2d, d2h = (math.nan, 0, 0) if args.kick_only else time_e2e("fp32", n, args.steps, args.warmup, dev)
     e2e_page_dt = math.nan if args.kick_only else time_e2e("fp32", n, args.steps, args.warmup, dev, pinned=False)[0]
     e2e64_dt = math.nan if (args.kick_only or args.no_fp64) else time_e2e("fp64", n, args.steps, args.warmup, dev)[0]
@@ -698,11 +701,13 @@ def main():
     if not args.no_configs:
         for cfg in (CONFIG1, CONFIG3):
             configs[cfg["key"]] = time_config(cfg, 3, 1, dev, flush, cpu_threads)
-        configs["config3"]["fp32_errors_vs_fp64"] = form_errors(CONFIG3, dev)
+        configs["config3"]["fp32_errors_vs_fp64"] = form_errors(CONFIG3, dev, fp32_mode={"fields": "spectral"})
+        configs["config3"]["fp32_difference_fields_errors_vs_fp64"] = form_errors(CONFIG3, dev)
     batched = None if args.no_batch else time_batched(args.steps, args.warmup, dev)
     serving = None if args.no_serve else time_serving(dev)
-    errors = None if args.kick_only else form_errors(
-        {"n": n, "mesh": MESH, "E": E_GEV, "dz": DZ, "charge": CHARGE, "beam": "gauss"}, dev)
+    head_cfg = {"n": n, "mesh": MESH, "E": E_GEV, "dz": DZ, "charge": CHARGE, "beam": "gauss"}
+    errors = None if args.kick_only else form_errors(head_cfg, dev)
+    errors_sp = None if args.kick_only else form_errors(head_cfg, dev, fp32_mode={"fields": "spectral"})
     barrier()
 
     t32 = sum(kick32) / 1e3
@@ -744,6 +749,12 @@ def main():
                                     "d2h_bytes_per_step": d2h, "host_memory": "pinned"}
                                    if e2e64_dt == e2e64_dt else None)} if kick64 else None),
             "fp32_over_fp64": (statistics.mean(kick64) / statistics.mean(kick32)) if kick64 else None,
+            "fp32_spectral_form": ({"value": n * args.steps / (sum(kicksp) / 1e3),
+                                    "ms_per_step": statistics.mean(kicksp), "stages_ms": stagessp,
+                                    "errors_vs_fp64": errors_sp,
+                                    "over_fp64": (statistics.mean(kick64) / statistics.mean(kicksp)) if kick64 else None,
+                                    "what": "the FP32 form with the field differences taken in Fourier space "
+                                            "(fields='spectral')"} if kicksp else None),
             "fp32_kick_rel_rms_err_vs_fp64": errors["kick"] if errors else None,
             "fp32_errors_vs_fp64": errors,
             "stages_ms": stages32,

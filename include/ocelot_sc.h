@@ -35,6 +35,7 @@ extern "C" {
                      origin uses a cancellation-free 4th-order multipole form */
 #define SC_FP32_SORTED_DEPOSIT 0x10 /* FP32 form: radix sort + Kahan segment sums */
 #define SC_FP32_EXACT_IGF 0x20      /* FP32 form: FP64 8-corner IGF on every cell */
+#define SC_FP32_SPECTRAL_FIELDS 0x40 /* FP32 form: forward-difference fields taken in Fourier space */
 
 /* status codes */
 #define SC_OK 0
@@ -331,16 +332,17 @@ int sc_kick_launches(const sc_plan* plan);
 /* Launch shapes a plan may choose without changing any result (the
  * autotuner's knobs, ocelot_gb300/tuning.py).  No counterpart in the
  * reference, whose only knob is the FFT thread count (sc.py:152-160).
- *   SC_PARAM_KICK_VARIANT: tiling of the FP32 gather + kick, 0 (default) ..
+ *   SC_PARAM_KICK_VARIANT: tiling of the FP32 gather + kick, 0 ..
  *     SC_KICK_NVARIANTS - 1, described by sc_kick_variant; every tiling runs
- *     the same per-particle arithmetic, so the kick is bit-identical.
+ *     the same per-particle arithmetic, so the kick is bit-identical.  A new
+ *     plan starts with the tiling measured fastest on large beams. 
  * Set between kicks (not during a stream capture that uses the plan). */
 #define SC_PARAM_KICK_VARIANT 0
 /*   SC_PARAM_RECORD_FIELD: 1 makes every kick also store the field at each
  *     particle (SC_REGION_FIELD), for error measurements; the FP32 form then
  *     runs its direct-access kick loop (same arithmetic, same particles). */
 #define SC_PARAM_RECORD_FIELD 1
-#define SC_KICK_NVARIANTS 6
+#define SC_KICK_NVARIANTS 9
 int sc_plan_set_param(sc_plan* plan, int param, int value);
 int sc_plan_get_param(const sc_plan* plan, int param, int* value);
 /* Tile (particles), tile buffers, particles per thread and blocks per SM of a

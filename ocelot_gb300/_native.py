@@ -16,6 +16,7 @@ SC_FP64 = 0
 SC_FP32 = 1
 SC_FP32_SORTED_DEPOSIT = 0x10
 SC_FP32_EXACT_IGF = 0x20
+SC_FP32_SPECTRAL_FIELDS = 0x40
 
 SC_OK = 0
 SC_ERR_ARG = 1
@@ -31,7 +32,7 @@ SC_NSTAGES = 11
 # launch-shape parameters of a plan (sc_plan_set_param)
 SC_PARAM_KICK_VARIANT = 0
 SC_PARAM_RECORD_FIELD = 1
-SC_KICK_NVARIANTS = 6
+SC_KICK_NVARIANTS = 9
 
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
 SC_WAIT_FRAME = 0

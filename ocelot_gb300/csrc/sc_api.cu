@@ -113,6 +113,11 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.green_s2 = take(rs * (size_t)p.nx * Ky * Kz);
     L.green = take(rs * Kx * Ky * Kz);
     L.W = take(cs * (size_t)p.nx * p.My * Kz);
+    L.dt_x = take(p.spectral ? cs * p.Mx : 0);
+    L.dt_y = take(p.spectral ? cs * p.My : 0);
+    L.dt_z = take(p.spectral ? cs * p.Mz : 0);
+    L.W2 = take(p.spectral ? cs * (size_t)p.nx * p.My * Kz : 0);
+    L.W3 = take(p.spectral ? cs * (size_t)p.nx * p.My * Kz : 0);
     L.xp = take(p.prec == SC_FP64 ? 8 * 6 * (size_t)n : 0);
     L.X = take(rs * 3 * (size_t)((n + 3) / 4 * 4));
     L.keys = take(4 * (size_t)n);
@@ -130,8 +135,21 @@ Layout make_layout(const Plan& p, int64_t n) {
     return L;
 }
 
+// the forward difference f[i] - f[i+1] in Fourier space (the transforms'
+// convention X[k] = sum x[n] exp(-2 pi i k n / M)): the factor
+// 1 - exp(2 pi i k / M) = 2 sin^2(pi k / M) - i sin(2 pi k / M), in the
+// half-angle form that keeps its relative accuracy at small k
 template <typename R>
-__global__ void k_init_ws(ScState* st, Cx<R>* tx, int Mx, Cx<R>* ty, int My, Cx<R>* tz, int Mz) {
+__device__ __forceinline__ Cx<R> diff_factor(int k, int M) {
+    double s, c, s2;
+    sincospi((double)k / M, &s, &c);
+    s2 = sinpi(2.0 * k / M);
+    return cx<R>((R)(2.0 * s * s), (R)(-s2));
+}
+
+template <typename R>
+__global__ void k_init_ws(ScState* st, Cx<R>* tx, int Mx, Cx<R>* ty, int My, Cx<R>* tz, int Mz, Cx<R>* dx,
+                          Cx<R>* dy, Cx<R>* dz) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
@@ -143,6 +161,11 @@ __global__ void k_init_ws(ScState* st, Cx<R>* tx, int Mx, Cx<R>* ty, int My, Cx<
     if (i < Mx) { sincospi(2.0 * i / Mx, &s, &c); tx[i] = cx<R>((R)c, (R)-s); }
     if (i < My) { sincospi(2.0 * i / My, &s, &c); ty[i] = cx<R>((R)c, (R)-s); }
     if (i < Mz) { sincospi(2.0 * i / Mz, &s, &c); tz[i] = cx<R>((R)c, (R)-s); }
+    if (dx) {
+        if (i < Mx) dx[i] = diff_factor<R>(i, Mx);
+        if (i < My) dy[i] = diff_factor<R>(i, My);
+        if (i < Mz) dz[i] = diff_factor<R>(i, Mz);
+    }
 }
 
 cudaError_t launch_init_workspace(const Plan& p, const Layout& L, char* ws, cudaStream_t s) {
@@ -151,10 +174,13 @@ cudaError_t launch_init_workspace(const Plan& p, const Layout& L, char* ws, cuda
     ScState* st = reinterpret_cast<ScState*>(ws + L.state);
     if (p.prec == SC_FP64)
         launch(k_init_ws<double>, (m + 255) / 256, 256, 0, s, st, (double2*)(ws + L.tw_x), p.Mx, (double2*)(ws + L.tw_y),
-                                                          p.My, (double2*)(ws + L.tw_z), p.Mz);
+                                                          p.My, (double2*)(ws + L.tw_z), p.Mz, (double2*)nullptr,
+                                                          (double2*)nullptr, (double2*)nullptr);
     else
         launch(k_init_ws<float>, (m + 255) / 256, 256, 0, s, st, (float2*)(ws + L.tw_x), p.Mx, (float2*)(ws + L.tw_y),
-                                                         p.My, (float2*)(ws + L.tw_z), p.Mz);
+                                                         p.My, (float2*)(ws + L.tw_z), p.Mz,
+                                                         p.spectral ? (float2*)(ws + L.dt_x) : (float2*)nullptr,
+                                                         (float2*)(ws + L.dt_y), (float2*)(ws + L.dt_z));
     return cudaGetLastError();
 }
 
@@ -291,13 +317,15 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     if (nx < 4 || ny < 4 || nz < 4)
         return fail(SC_ERR_ARG, "nmesh_xyz=[%d,%d,%d]: every mesh dimension must be >= 4", nx, ny, nz);
     if (precision != SC_FP64 && precision != SC_FP32) return fail(SC_ERR_ARG, "unknown precision %d", precision);
-    if (mode & ~(0x0f | SC_FP32_SORTED_DEPOSIT | SC_FP32_EXACT_IGF)) return fail(SC_ERR_ARG, "unknown mode bits 0x%x", mode);
+    if (mode & ~(0x0f | SC_FP32_SORTED_DEPOSIT | SC_FP32_EXACT_IGF | SC_FP32_SPECTRAL_FIELDS))
+        return fail(SC_ERR_ARG, "unknown mode bits 0x%x", mode);
     Plan p;
     memset(&p, 0, sizeof p);
     p.nx = nx; p.ny = ny; p.nz = nz;
     p.prec = precision;
     p.sorted_deposit = precision == SC_FP64 || (mode & SC_FP32_SORTED_DEPOSIT);
     p.exact_igf = precision == SC_FP64 || (mode & SC_FP32_EXACT_IGF);
+    p.spectral = precision == SC_FP32 && (mode & SC_FP32_SPECTRAL_FIELDS);
     p.Mx = choose_fft_length(nx);
     p.My = choose_fft_length(ny);
     p.Mz = choose_fft_length(nz);
@@ -314,6 +342,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(cudaDeviceGetAttribute(&p.sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     p.part_blocks = p.sm_count * 4;
     for (int k = 0; k < 3; ++k) p.wait_limit[k] = MBAR_WAIT_LIMIT;
+    p.kick_variant = default_kick_variant();
     // everything that is not a stream operation happens here, so that kicks
     // can be recorded in a CUDA graph
     SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
@@ -582,7 +611,7 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     mark(plan, 13, s);
     SC_CUDA(cudaStreamWaitEvent(s, plan->join, 0), "cudaStreamWaitEvent");  // join
     mark(plan, 6, s);
-    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s, qfix, CONV_REST), "convolve");
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s, qfix, CONV_REST, true), "convolve");
     mark(plan, 7, s);
     SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
     mark(plan, 8, s);
@@ -620,7 +649,7 @@ int sc_el_field(sc_plan* plan, void* ws_v, size_t ws_bytes, double* X, const dou
     SC_CUDA(launch_igf(p, L, ws, s), "igf");
     SC_CUDA(launch_green_spectrum(p, L, ws, s), "green spectrum");
     SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s,
-                            p.sorted_deposit ? nullptr : reinterpret_cast<const long long*>(ws + L.qfix)),
+                            p.sorted_deposit ? nullptr : reinterpret_cast<const long long*>(ws + L.qfix), CONV_ALL, true),
             "convolve");
     SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
     SC_CUDA(launch_gather_xyz(p, L, ws, kp, exyz, s), "gather");
@@ -769,8 +798,9 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
     for (int i = 0; i < nbeams; ++i) {
         const sc_beam& m = beams[i];
         if (!m.plan) return fail(SC_ERR_ARG, "beam %d: plan is NULL", i);
-        if (m.plan->p.prec != SC_FP32 || m.plan->p.sorted_deposit)
-            return fail(SC_ERR_UNSUPPORTED, "beam %d: batched kicks need SC_FP32 plans with the fixed-point deposit", i);
+        if (m.plan->p.prec != SC_FP32 || m.plan->p.sorted_deposit || m.plan->p.spectral)
+            return fail(SC_ERR_UNSUPPORTED,
+                        "beam %d: batched kicks need SC_FP32 plans with the fixed-point deposit and difference fields", i);
         if (m.zstep == 0 && !m.tmap) continue;  // nothing to do for this beam
         if (m.n < 1 || m.n > 0x7fffffffLL) return fail(SC_ERR_ARG, "beam %d: n=%lld", i, (long long)m.n);
         if (!m.rparticles || !m.q) return fail(SC_ERR_ARG, "beam %d: rparticles or q is NULL", i);

@@ -150,6 +150,9 @@ struct Layout {
     size_t igf_k1;                               // nx*ny*nz (R; double storage size)
     size_t green_s1, green_s2, green;            // spectrum passes (R)
     size_t W;                                    // complex work grid nx*My*Kz
+    // spectral fields (FP32 with SC_FP32_SPECTRAL_FIELDS): the forward-difference
+    // factors 1 - exp(2 pi i k / M) per axis (Cx<R>[M]) and two more work grids
+    size_t dt_x, dt_y, dt_z, W2, W3;
     size_t total;
 };
 
@@ -157,6 +160,7 @@ struct Plan {
     int nx, ny, nz, prec;
     bool sorted_deposit;  // FP64 always; FP32 with SC_FP32_SORTED_DEPOSIT
     bool exact_igf;       // FP64 always; FP32 with SC_FP32_EXACT_IGF
+    bool spectral;        // FP32 with SC_FP32_SPECTRAL_FIELDS
     int Mx, My, Mz;
     RadixPlan rx, ry, rz;
     int key_bits;
@@ -168,6 +172,7 @@ struct Plan {
 };
 // tile, tile buffers, particles per thread and blocks per SM of kick variant v (0 if v is out of range)
 int kick_variant_info(int v, int* tile, int* stages, int* ppt, int* minb);
+int default_kick_variant();
 
 Layout make_layout(const Plan& p, int64_t n);
 
@@ -222,7 +227,8 @@ cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cuda
 // charge grid) and then CONV_REST (the passes that need the Green spectrum)
 enum ConvPart { CONV_ALL = 0, CONV_FORWARD = 1, CONV_REST = 2 };
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in,
-                            void* phi_out, cudaStream_t s, const long long* qfix = nullptr, int part = CONV_ALL);
+                            void* phi_out, cudaStream_t s, const long long* qfix = nullptr, int part = CONV_ALL,
+                            bool fields = false);
 cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
 // kernels launch_convolve(CONV_ALL) launches for this plan
 int convolve_launches(const Plan& p);

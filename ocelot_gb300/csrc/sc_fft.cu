@@ -34,10 +34,38 @@ static inline int z_lines_per_block(int Mz) {
 // columns per block in the strided passes: 16, fewer when two line buffers
 // of 16 columns would not fit in shared memory (FP64 at M = 512)
 template <typename R>
-static inline int strided_cols(int M) {
+static inline int strided_cols(int M, int nbuf = 2) {
     int tk = 16;
-    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + 2 * tk * fft_ls(M)) > 200 * 1024) tk /= 2;
+    while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + nbuf * tk * fft_ls(M)) > 200 * 1024) tk /= 2;
     return tk;
+}
+
+// Spectral fields (FP32 with SC_FP32_SPECTRAL_FIELDS).  The field grids are
+// forward differences of the potential, Ex[i] = (phi[i] - phi[i+1]) / hx
+// (sc.py:195-200); on the padded grid that difference is the product of the
+// spectrum with D(k) = 1 - exp(2 pi i k / M), exact for every cell the
+// reference keeps.  Taking it in Fourier space before the inverse transforms
+// makes the rounding of each field relative to the field itself instead of
+// to the potential, which is hundreds of times larger than the differences
+// of neighbouring cells.
+//   Ex: x inverse of (spectrum x D(kx)) into W2, then y and z inverses
+//   Ey: y inverse of (W x D(ky)) into W3 (W after the x inverse), then z
+//   Ez: z inverse of (y-inverted W) x D(kz)
+// The potential itself is kept (z inverse of the y-inverted W).
+template <typename R>
+struct Spec {
+    Cx<R>* W2;                       // the x-differenced grid (Ex); nullptr: no spectral fields
+    Cx<R>* W3;                       // the y-differenced grid (Ey), separate passes only
+    const Cx<R>* dx;                 // D(k) per axis
+    const Cx<R>* dy;
+    const Cx<R>* dz;
+    R* ex;                           // field grids [nx][ny][nz], zero on their last plane
+    R* ey;
+    R* ez;
+};
+template <typename R>
+__device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
+    return cx<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
 // qfix != nullptr: the charge arrives as the 64-bit fixed-point grid of the
@@ -99,16 +127,20 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const l
     zfwd_body<R>(q, qfix, W, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk());
 }
 
-// strided pass along y: forward (rows < ny in, all My out) or inverse (all in, rows < ny out)
+// strided pass along y: forward (rows < ny in, all My out) or inverse (all in, rows < ny out),
+// in place on W.  W3 != nullptr (inverse, spectral fields): the block also
+// transforms its columns of W multiplied by D(ky) into W3 (a third line buffer)
 template <typename R, bool INV>
 __device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My, int Kz, const RadixPlan& ry,
-                                           const Cx<R>* __restrict__ twg, int TK, const ScState* st, VBlk vb) {
+                                           const Cx<R>* __restrict__ twg, int TK, const ScState* st, VBlk vb,
+                                           Cx<R>* __restrict__ W3 = nullptr, const Cx<R>* __restrict__ dy = nullptr) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int ls = fft_ls(My);
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* a = tw + My;
     Cx<R>* b = a + TK * ls;
+    Cx<R>* c = b + TK * ls;
     load_twiddles<R>(tw, twg, My);
     const int x = vb.y;
     const int k0 = vb.x * TK;
@@ -118,6 +150,7 @@ __device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My
         Cx<R> v = cx<R>(0, 0);
         if (y < nin && k < Kz) v = W[((size_t)x * My + y) * Kz + k];
         a[kk * ls + y] = v;
+        if (W3) c[kk * ls + y] = cmul(v, dy[y]);
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, INV>(a, b, ls, TK, ry, tw);
@@ -126,21 +159,35 @@ __device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My
         const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
         if (k < Kz) W[((size_t)x * My + y) * Kz + k] = res[kk * ls + y];
     }
+    if (W3) {
+        __syncthreads();  // a and b are free
+        Cx<R>* res3 = fft_lines<R, INV>(c, a, ls, TK, ry, tw);
+        for (int idx = threadIdx.x; idx < nout * TK; idx += blockDim.x) {
+            const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
+            if (k < Kz) W3[((size_t)x * My + y) * Kz + k] = res3[kk * ls + y];
+        }
+    }
 }
 
+// blockIdx.z = 0: W (and, with spectral fields, W x D(ky) into W3);
+// blockIdx.z = 1 (inverse, spectral fields): the x-differenced grid W2 in place
 template <typename R, bool INV>
 __global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int ny, int My, int Kz,
                                                        RadixPlan ry, const Cx<R>* __restrict__ twg,
-                                                       int TK, const ScState* st) {
+                                                       int TK, const ScState* st, Spec<R> sp) {
     pdl_wait();
-    ypass_body<R, INV>(W, ny, My, Kz, ry, twg, TK, st, hw_vblk());
+    if (blockIdx.z == 0) ypass_body<R, INV>(W, ny, My, Kz, ry, twg, TK, st, hw_vblk(), sp.W3, sp.dy);
+    else ypass_body<R, INV>(sp.W2, ny, My, Kz, ry, twg, TK, st, hw_vblk());
 }
 
 // x pass: forward FFT of the nx non-zero planes, Green multiply, inverse FFT, keep x < nx
+// W2 != nullptr (spectral fields): the product times D(kx) goes through its
+// own inverse transform (a third line buffer) into W2
 template <typename R>
 __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __restrict__ G, int nx, int My, int Kz,
                                            int Ky, const RadixPlan& rx, const Cx<R>* __restrict__ twg, int TK,
-                                           const ScState* st, VBlk vb) {
+                                           const ScState* st, VBlk vb, Cx<R>* __restrict__ W2 = nullptr,
+                                           const Cx<R>* __restrict__ dx = nullptr) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mx = rx.L;
@@ -148,6 +195,7 @@ __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __res
     Cx<R>* tw = reinterpret_cast<Cx<R>*>(smraw);
     Cx<R>* a = tw + Mx;
     Cx<R>* b = a + TK * ls;
+    Cx<R>* c = b + TK * ls;
     load_twiddles<R>(tw, twg, Mx);
     const int ky = vb.y;
     const int gy = ky <= My - ky ? ky : My - ky;
@@ -169,6 +217,7 @@ __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __res
         v.x *= g;
         v.y *= g;
         res[kk * ls + kx] = v;
+        if (W2) c[kk * ls + kx] = cmul(v, dx[kx]);
     }
     __syncthreads();
     Cx<R>* res2 = fft_lines<R, true>(res, res == a ? b : a, ls, TK, rx, tw);
@@ -176,20 +225,49 @@ __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __res
         const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
         if (k < Kz) W[((size_t)x * My + ky) * Kz + k] = res2[kk * ls + x];
     }
+    if (W2) {
+        __syncthreads();  // a and b are free
+        Cx<R>* res3 = fft_lines<R, true>(c, a, ls, TK, rx, tw);
+        for (int idx = threadIdx.x; idx < nx * TK; idx += blockDim.x) {
+            const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
+            if (k < Kz) W2[((size_t)x * My + ky) * Kz + k] = res3[kk * ls + x];
+        }
+    }
 }
 
 template <typename R>
 __global__ void __launch_bounds__(FFT_THREADS) k_xconv(Cx<R>* __restrict__ W, const R* __restrict__ G,
                                                        int nx, int My, int Kz, int Ky, RadixPlan rx,
-                                                       const Cx<R>* __restrict__ twg, int TK, const ScState* st) {
+                                                       const Cx<R>* __restrict__ twg, int TK, const ScState* st,
+                                                       Spec<R> sp) {
     pdl_wait();
-    xconv_body<R>(W, G, nx, My, Kz, Ky, rx, twg, TK, st, hw_vblk());
+    xconv_body<R>(W, G, nx, My, Kz, Ky, rx, twg, TK, st, hw_vblk(), sp.W2, sp.dx);
 }
 
+// Field outputs of the inverse passes (spectral fields, FP32): the grid a
+// block writes, D(kz) applied before the z inverse or not, the factor 1/h of
+// the difference and the plane left at zero (sc.py:196-198).
+struct InvOut {
+    int field;   // 0 potential, 1 Ex, 2 Ey, 3 Ez
+    int nx;
+};
+template <typename R>
+__device__ __forceinline__ void inv_out(const Spec<R>& sp, const ScState* st, int f, const Cx<R>* W, R* phi,
+                                        const Cx<R>*& src, R*& out, const Cx<R>*& dz, R& mul) {
+    src = f == 1 ? sp.W2 : (f == 2 && sp.W3 ? sp.W3 : W);
+    out = f == 0 ? phi : (f == 1 ? sp.ex : (f == 2 ? sp.ey : sp.ez));
+    dz = f == 3 ? sp.dz : nullptr;
+    mul = f == 0 ? (R)1 : (R)st->istepsf[f - 1];
+}
+
+// dz != nullptr: the z spectrum is multiplied by D(kz) first; mul scales the
+// output; zero_axis (0, 1, 2) leaves the last plane along that axis at zero
+// (x = nx - 1, y = ny - 1 or z = nz - 1), -1 none
 template <typename R>
 __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __restrict__ phi, int ny, int nz, int My,
                                           int Kz, const RadixPlan& rz, const Cx<R>* __restrict__ twg, int NC,
-                                          const ScState* st, VBlk vb) {
+                                          const ScState* st, VBlk vb, const Cx<R>* __restrict__ dz = nullptr,
+                                          R mul = (R)1, int zero_axis = -1, int nx = 0) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mz = rz.L, lz = fft_ls(Mz);
@@ -207,13 +285,17 @@ __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __rest
         Cx<R> A = cx<R>(0, 0), B = cx<R>(0, 0);
         if (ya < ny) A = W[((size_t)x * My + ya) * Kz + kk];
         if (yb < ny) B = W[((size_t)x * My + yb) * Kz + kk];
+        if (dz) {
+            A = cmul(A, dz[kk]);
+            B = cmul(B, dz[kk]);
+        }
         // Z = A + iB, Hermitian-extended above Mz/2
         a[c * lz + k] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, true>(a, b, lz, NC, rz, tw);
     const double norm = st->phi_norm, denom = st->phi_denom;
-    const R fscale = (R)st->phi_scalef;  // (float)(norm / denom), computed once by the mesh finalize
+    const R fscale = (R)st->phi_scalef * mul;  // (float)(norm / denom), computed once by the mesh finalize
     for (int idx = threadIdx.x; idx < NC * nz; idx += blockDim.x) {
         const int c = idx / nz, z = idx - c * nz;
         const int ya = y0 + 2 * c, yb = ya + 1;
@@ -223,19 +305,29 @@ __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __rest
             if (ya < ny) phi[((size_t)x * ny + ya) * nz + z] = (R)(((double)v.x * norm) / denom);
             if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = (R)(((double)v.y * norm) / denom);
         } else {
-            if (ya < ny) phi[((size_t)x * ny + ya) * nz + z] = v.x * fscale;
-            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = v.y * fscale;
+            const bool zx = zero_axis == 0 && x == nx - 1, zz = zero_axis == 2 && z == nz - 1;
+            const bool za = zx || zz || (zero_axis == 1 && ya == ny - 1);
+            const bool zb = zx || zz || (zero_axis == 1 && yb == ny - 1);
+            if (ya < ny) phi[((size_t)x * ny + ya) * nz + z] = za ? (R)0 : v.x * fscale;
+            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = zb ? (R)0 : v.y * fscale;
         }
     }
 }
 
+// blockIdx.z: the output (0 the potential; with spectral fields 1 Ex, 2 Ey, 3 Ez)
 template <typename R>
 __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ W, R* __restrict__ phi,
                                                       int ny, int nz, int My, int Kz, RadixPlan rz,
                                                       const Cx<R>* __restrict__ twg, int NC,
-                                                      const ScState* st) {
+                                                      const ScState* st, Spec<R> sp) {
     pdl_wait();
-    zinv_body<R>(W, phi, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk());
+    const int f = (int)blockIdx.z;
+    const Cx<R>* src;
+    R* out;
+    const Cx<R>* dz;
+    R mul;
+    inv_out<R>(sp, st, f, W, phi, src, out, dz, mul);
+    zinv_body<R>(src, out, ny, nz, My, Kz, rz, twg, NC, st, hw_vblk(), dz, mul, f - 1, (int)gridDim.y);
 }
 
 // Ex,Ey,Ez = forward differences / h, zero on the last plane (sc.py:195-200).
@@ -309,6 +401,35 @@ __global__ void k_field_octs(const float* __restrict__ phi, float* __restrict__ 
                              float* __restrict__ oz, int nx, int ny, int nz, const ScState* st) {
     pdl_wait();
     field_octs_body(phi, ox, oy, oz, nx, ny, nz, st, hw_vblk());
+}
+
+// the octs of field grids computed in Fourier space (spectral fields): the 8
+// neighbouring values themselves, zero outside the grid
+__device__ __forceinline__ float at_or0(const float* __restrict__ F, int i, int j, int k, int nx, int ny, int nz) {
+    return (i < nx && j < ny && k < nz) ? F[((size_t)i * ny + j) * nz + k] : 0.f;
+}
+__global__ void k_field_octs_spectral(const float* __restrict__ ex, const float* __restrict__ ey,
+                                      const float* __restrict__ ez, float* __restrict__ ox, float* __restrict__ oy,
+                                      float* __restrict__ oz, int nx, int ny, int nz, const ScState* st) {
+    pdl_wait();
+    if (st->status) return;
+    const int j = blockIdx.x, i = blockIdx.y;
+    const float* const in[3] = {ex, ey, ez};
+    float* const out[3] = {ox, oy, oz};
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        const size_t c = ((size_t)i * ny + j) * nz + k;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float o[8];
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) o[4 * a + 2 * b + e] = at_or0(in[d], i + a, j + b, k + e, nx, ny, nz);
+            st_oct(out[d] + 8 * c, o);
+        }
+    }
 }
 
 
@@ -406,11 +527,16 @@ __global__ void __launch_bounds__(PLANE_THREADS) k_zy_fwd(R* __restrict__ q, con
     zy_fwd_body<R>(q, qfix, W, ny, nz, My, Kz, rz, ry, twz, twy, st, (int)blockIdx.x, (int)gridDim.x);
 }
 
+// dy / dz != nullptr (spectral fields): the plane is multiplied by D(ky)
+// before the y inverse / by D(kz) before the z inverse; mul and zero_axis as
+// in zinv_body
 template <typename R>
 __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __restrict__ phi, int ny, int nz,
                                             int My, int Kz, const RadixPlan& rz, const RadixPlan& ry,
                                             const Cx<R>* __restrict__ twzg, const Cx<R>* __restrict__ twyg,
-                                            const ScState* st, int x) {
+                                            const ScState* st, int x, const Cx<R>* __restrict__ dy = nullptr,
+                                            const Cx<R>* __restrict__ dz = nullptr, R mul = (R)1,
+                                            int zero_axis = -1, int nx = 0) {
     extern __shared__ __align__(16) unsigned char smraw[];
     if (st->status) return;
     const int Mz = rz.L, lz = fft_ls(Mz), ly = fft_ls(My), ncz = (ny + 1) / 2;
@@ -422,7 +548,8 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
     load_twiddles<R>(twy, twyg, My);
     for (int idx = threadIdx.x; idx < My * Kz; idx += blockDim.x) {
         const int ky = idx / Kz, k = idx - ky * Kz;
-        A2[k * ly + ky] = W[((size_t)x * My + ky) * Kz + k];
+        const Cx<R> v = W[((size_t)x * My + ky) * Kz + k];
+        A2[k * ly + ky] = dy ? cmul(v, dy[ky]) : v;
     }
     __syncthreads();
     // B2: inverse y; only rows y < ny are used
@@ -435,14 +562,18 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
         const int ya = 2 * c, yb = ya + 1;
         const bool lo = k < Kz;
         const int kk = lo ? k : Mz - k;
-        const Cx<R> A = res2[kk * ly + ya];
-        const Cx<R> B = yb < ny ? res2[kk * ly + yb] : cx<R>(0, 0);
+        Cx<R> A = res2[kk * ly + ya];
+        Cx<R> B = yb < ny ? res2[kk * ly + yb] : cx<R>(0, 0);
+        if (dz) {
+            A = cmul(A, dz[kk]);
+            B = cmul(B, dz[kk]);
+        }
         A1[c * lz + k] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
     }
     __syncthreads();
     const Cx<R>* res = fft_lines<R, true>(A1, B1, lz, ncz, rz, twz);
     const double norm = st->phi_norm, denom = st->phi_denom;
-    const R fscale = (R)st->phi_scalef;  // (float)(norm / denom), computed once by the mesh finalize
+    const R fscale = (R)st->phi_scalef * mul;  // (float)(norm / denom), computed once by the mesh finalize
     for (int idx = threadIdx.x; idx < ncz * nz; idx += blockDim.x) {
         const int c = idx / nz, z = idx - c * nz;
         const int ya = 2 * c, yb = ya + 1;
@@ -452,19 +583,33 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
             phi[((size_t)x * ny + ya) * nz + z] = (R)(((double)v.x * norm) / denom);
             if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = (R)(((double)v.y * norm) / denom);
         } else {
-            phi[((size_t)x * ny + ya) * nz + z] = v.x * fscale;
-            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = v.y * fscale;
+            const bool zx = zero_axis == 0 && x == nx - 1, zz = zero_axis == 2 && z == nz - 1;
+            const bool za = zx || zz || (zero_axis == 1 && ya == ny - 1);
+            const bool zb = zx || zz || (zero_axis == 1 && yb == ny - 1);
+            phi[((size_t)x * ny + ya) * nz + z] = za ? (R)0 : v.x * fscale;
+            if (yb < ny) phi[((size_t)x * ny + yb) * nz + z] = zb ? (R)0 : v.y * fscale;
         }
     }
 }
 
+// blockIdx.y: the output (0 the potential; with spectral fields 1 Ex, 2 Ey, 3 Ez)
 template <typename R>
 __global__ void __launch_bounds__(PLANE_THREADS) k_yz_inv(const Cx<R>* __restrict__ W, R* __restrict__ phi, int ny,
                                                           int nz, int My, int Kz, RadixPlan rz, RadixPlan ry,
                                                           const Cx<R>* __restrict__ twz,
-                                                          const Cx<R>* __restrict__ twy, const ScState* st) {
+                                                          const Cx<R>* __restrict__ twy, const ScState* st,
+                                                          Spec<R> sp) {
     pdl_wait();
-    yz_inv_body<R>(W, phi, ny, nz, My, Kz, rz, ry, twz, twy, st, (int)blockIdx.x);
+    const int f = (int)blockIdx.y;
+    const Cx<R>* src;
+    R* out;
+    const Cx<R>* dz;
+    R mul;
+    Spec<R> spp = sp;
+    spp.W3 = nullptr;  // the plane pass applies D(ky) itself
+    inv_out<R>(spp, st, f, W, phi, src, out, dz, mul);
+    yz_inv_body<R>(src, out, ny, nz, My, Kz, rz, ry, twz, twy, st, (int)blockIdx.x, f == 2 ? sp.dy : nullptr, dz,
+                   mul, f - 1, (int)gridDim.x);
 }
 
 static int optin_smem();
@@ -479,11 +624,29 @@ static int optin_smem() {
     return v;
 }
 
+// the spectral-field pointers of a plan's workspace (W2 == nullptr: none)
+template <typename R>
+static Spec<R> spec_of(const Plan& p, const Layout& L, char* ws, bool fields) {
+    Spec<R> sp = {};
+    if (!(fields && p.spectral && sizeof(R) == 4)) return sp;
+    sp.W2 = reinterpret_cast<Cx<R>*>(ws + L.W2);
+    sp.W3 = reinterpret_cast<Cx<R>*>(ws + L.W3);
+    sp.dx = reinterpret_cast<const Cx<R>*>(ws + L.dt_x);
+    sp.dy = reinterpret_cast<const Cx<R>*>(ws + L.dt_y);
+    sp.dz = reinterpret_cast<const Cx<R>*>(ws + L.dt_z);
+    sp.ex = reinterpret_cast<R*>(ws + L.ex);
+    sp.ey = reinterpret_cast<R*>(ws + L.ey);
+    sp.ez = reinterpret_cast<R*>(ws + L.ez);
+    return sp;
+}
+
 template <typename R>
 static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid, R* phi, const long long* qfix,
-                              cudaStream_t s, int part) {
+                              cudaStream_t s, int part, bool fields) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int Kz = p.Mz / 2 + 1, Ky = p.My / 2 + 1;
+    const Spec<R> sp = spec_of<R>(p, L, ws, fields);
+    const int nbuf = sp.W2 ? 3 : 2;  // line buffers of the x pass and the y inverse
     Cx<R>* W = reinterpret_cast<Cx<R>*>(ws + L.W);
     const R* G = reinterpret_cast<const R*>(ws + L.green);
     const Cx<R>* twx = reinterpret_cast<const Cx<R>*>(ws + L.tw_x);
@@ -493,9 +656,12 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     const int NC = z_lines_per_block(p.Mz);
     const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
     dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
-    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
+    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx, nbuf);
+    const int tkyi = strided_cols<R>(p.My, nbuf);  // the y inverse
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
+    const size_t smyi = sizeof(Cx<R>) * (size_t)(p.My + nbuf * tkyi * fft_ls(p.My));
     dim3 gy((Kz + tky - 1) / tky, p.nx);
+    dim3 gyi((Kz + tkyi - 1) / tkyi, p.nx, sp.W2 ? 2 : 1);
     static const int optin = optin_smem();
     const bool plane = plane_fits<R>(p, optin);
     const size_t smp = plane_smem<R>(p);
@@ -506,22 +672,24 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
         if ((e = set_smem(k_zfwd<R>, smz))) return e;
         launch(k_zfwd<R>, gz, FFT_THREADS, smz, s, qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
         if ((e = set_smem(k_ypass<R, false>, smy))) return e;
-        launch(k_ypass<R, false>, gy, FFT_THREADS, smy, s, W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+        launch(k_ypass<R, false>, gy, FFT_THREADS, smy, s, W, p.ny, p.My, Kz, p.ry, twy, tky, st, Spec<R>{});
     }
     if (part == CONV_FORWARD) return cudaGetLastError();
-    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + nbuf * tkx * fft_ls(p.Mx));
     dim3 gx((Kz + tkx - 1) / tkx, p.My);
     if ((e = set_smem(k_xconv<R>, smx))) return e;
-    launch(k_xconv<R>, gx, FFT_THREADS, smx, s, W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st);
+    launch(k_xconv<R>, gx, FFT_THREADS, smx, s, W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st, sp);
+    const int nout = sp.W2 ? 4 : 1;  // the potential, then Ex, Ey, Ez
     if (plane) {
         if ((e = set_smem(k_yz_inv<R>, smp))) return e;
-        launch(k_yz_inv<R>, p.nx, PLANE_THREADS, smp, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy, st);
+        launch(k_yz_inv<R>, dim3(p.nx, nout), PLANE_THREADS, smp, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy,
+               st, sp);
         return cudaGetLastError();
     }
-    if ((e = set_smem(k_ypass<R, true>, smy))) return e;
-    launch(k_ypass<R, true>, gy, FFT_THREADS, smy, s, W, p.ny, p.My, Kz, p.ry, twy, tky, st);
+    if ((e = set_smem(k_ypass<R, true>, smyi))) return e;
+    launch(k_ypass<R, true>, gyi, FFT_THREADS, smyi, s, W, p.ny, p.My, Kz, p.ry, twy, tkyi, st, sp);
     if ((e = set_smem(k_zinv<R>, smz))) return e;
-    launch(k_zinv<R>, gz, FFT_THREADS, smz, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
+    launch(k_zinv<R>, dim3(gz.x, gz.y, nout), FFT_THREADS, smz, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st, sp);
     return cudaGetLastError();
 }
 
@@ -530,13 +698,15 @@ static cudaError_t prepare_fft_t(const Plan& p) {
     cudaError_t e;
     const int NC = z_lines_per_block(p.Mz);
     const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
-    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx);
+    const int nbuf = (p.spectral && sizeof(R) == 4) ? 3 : 2;
+    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx, nbuf), tkyi = strided_cols<R>(p.My, nbuf);
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
-    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
+    const size_t smyi = sizeof(Cx<R>) * (size_t)(p.My + nbuf * tkyi * fft_ls(p.My));
+    const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + nbuf * tkx * fft_ls(p.Mx));
     if ((e = set_smem(k_zfwd<R>, smz))) return e;
     if ((e = set_smem(k_ypass<R, false>, smy))) return e;
     if ((e = set_smem(k_xconv<R>, smx))) return e;
-    if ((e = set_smem(k_ypass<R, true>, smy))) return e;
+    if ((e = set_smem(k_ypass<R, true>, smyi))) return e;
     if ((e = set_smem(k_zinv<R>, smz))) return e;
     if (plane_fits<R>(p, optin_smem())) {
         if ((e = set_smem(k_zy_fwd<R>, plane_smem<R>(p)))) return e;
@@ -550,12 +720,12 @@ cudaError_t prepare_fft_kernels(const Plan& p) {
 }
 
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in, void* phi_out,
-                            cudaStream_t s, const long long* qfix, int part) {
+                            cudaStream_t s, const long long* qfix, int part, bool fields) {
     if (p.prec == SC_FP64)
         return convolve_t<double>(p, L, ws, static_cast<double*>(const_cast<void*>(qgrid_in)),
-                                  static_cast<double*>(phi_out), nullptr, s, part);
+                                  static_cast<double*>(phi_out), nullptr, s, part, false);
     return convolve_t<float>(p, L, ws, static_cast<float*>(const_cast<void*>(qgrid_in)), static_cast<float*>(phi_out),
-                             qfix, s, part);
+                             qfix, s, part, fields);
 }
 
 template <typename R>
@@ -563,7 +733,12 @@ static cudaError_t field_t(const Plan& p, const Layout& L, char* ws, cudaStream_
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int bt = p.nz < 256 ? ((p.nz + 31) / 32) * 32 : 256;
     const dim3 grid(p.ny, p.nx);
-    if (sizeof(R) == 4)
+    if (sizeof(R) == 4 && p.spectral)
+        launch(k_field_octs_spectral, grid, bt, 0, s, reinterpret_cast<const float*>(ws + L.ex),
+               reinterpret_cast<const float*>(ws + L.ey), reinterpret_cast<const float*>(ws + L.ez),
+               reinterpret_cast<float*>(ws + L.exq), reinterpret_cast<float*>(ws + L.eyq),
+               reinterpret_cast<float*>(ws + L.ezq), p.nx, p.ny, p.nz, st);
+    else if (sizeof(R) == 4)
         launch(k_field_octs, grid, bt, 0, s, reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
                                          reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq),
                                          p.nx, p.ny, p.nz, st);

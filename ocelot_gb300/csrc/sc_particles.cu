@@ -2042,7 +2042,9 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
             }
         }
         // the buffer refilled here is read STAGES - 1 iterations on, after
-        // the barriers of the iterations between
+        // the barriers of the iterations between; with two buffers that is
+        // the next iteration, so a barrier publishes the lead's s_tile first
+        if constexpr (STAGES < 3) __syncthreads();
     }
     if (lead) {
         if (failed) {
@@ -2063,7 +2065,14 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
     X(2, 256, 3, 1, 4)       \
     X(3, 256, 2, 1, 5)       \
     X(4, 128, 4, 1, 8)       \
-    X(5, 256, 4, 1, 3)
+    X(5, 256, 4, 1, 3)       \
+    X(6, 512, 3, 1, 2)       \
+    X(7, 1024, 3, 1, 1)      \
+    X(8, 256, 3, 1, 5)
+
+// the default: 256-particle tiles, one particle per thread, 4 blocks per SM
+// (measured fastest from 1M particles up on 48^3 to 128x128x256 meshes)
+constexpr int kDefaultKickVariant = 2;
 
 template <int TILE, int STAGES, int PPT, int MINB>
 __global__ void __launch_bounds__(KickTiling<TILE, STAGES, PPT>::threads, MINB)
@@ -2173,7 +2182,7 @@ __global__ void __launch_bounds__(KickTiling<TILE, STAGES, PPT>::threads, MINB)
     const float* oy = reinterpret_cast<const float*>(B.ws + B.L.eyq);
     const float* oz = reinterpret_cast<const float*>(B.ws + B.L.ezq);
     if (kick_group(B.rp, B.kp.ld) >= 2) kick32_tma_body<TILE, STAGES, PPT>(B.rp, ox, oy, oz, B.kp, st, vb);
-    else if (PPT == 2) kick32_body<1>(B.rp, ox, oy, oz, B.kp, st, vb);  // 256 threads: the direct-access loop
+    else kick32_body<1>(B.rp, ox, oy, oz, B.kp, st, vb);  // rows without 16-byte alignment: the direct-access loop
 }
 
 // the compiled kick tilings, indexed by a plan's kick_variant
@@ -2192,7 +2201,10 @@ static const KickVariant kKickVariants[] = {
 #undef SC_KV
 };
 constexpr int kNumKickVariants = (int)(sizeof(kKickVariants) / sizeof(kKickVariants[0]));
+static_assert(KickTiling<256, 3, 1>::threads == PT, "the default kick tiling has PT threads");
 static_assert(kNumKickVariants == SC_KICK_NVARIANTS, "SC_KICK_NVARIANTS must count SC_KICK_VARIANTS");
+
+int default_kick_variant() { return kDefaultKickVariant; }
 
 int kick_variant_info(int v, int* tile, int* stages, int* ppt, int* minb) {
     if (v < 0 || v >= kNumKickVariants) return 0;
@@ -2212,8 +2224,9 @@ cudaError_t launch_batch_particles(BatchPartKernel k, const BatchBeam* beams, co
         case BP_EXTENT: launch(kb_extent32, blocks, PT, EX_SMEM, s, beams, start, nb); break;
         case BP_KEYS: launch(kb_keys32, blocks, PT, 0, s, beams, start, nb); break;
         case BP_KICK: {
-            // the batch's particle blocks are sized for 256 threads (BS_PART): the tilings of 256 threads
-            const KickVariant& v = kKickVariants[0];
+            // the batch's particle blocks (BS_PART) are launched with the
+            // 256-thread tiling that is the plans' default
+            const KickVariant& v = kKickVariants[kDefaultKickVariant];
             launch(v.batch_fn, blocks, v.threads, v.smem, s, beams, start, nb);
             break;
         }

@@ -32,7 +32,7 @@ from .physics_proc import PhysProc
 _PREC = {"fp64": N.SC_FP64, "fp32": N.SC_FP32}
 
 
-def plan_mode(precision: str, deposit: str = "fixed", igf: str = "hybrid") -> int:
+def plan_mode(precision: str, deposit: str = "fixed", igf: str = "hybrid", fields: str = "difference") -> int:
     """Mode bits of a plan (include/ocelot_sc.h): the FP32 form's options."""
     if precision not in _PREC:
         raise ValueError(f"precision must be one of {sorted(_PREC)}, not {precision!r}")
@@ -40,12 +40,16 @@ def plan_mode(precision: str, deposit: str = "fixed", igf: str = "hybrid") -> in
         raise ValueError(f"deposit must be 'fixed' or 'sorted', not {deposit!r}")
     if igf not in ("hybrid", "exact"):
         raise ValueError(f"igf must be 'hybrid' or 'exact', not {igf!r}")
+    if fields not in ("difference", "spectral"):
+        raise ValueError(f"fields must be 'difference' or 'spectral', not {fields!r}")
     mode = _PREC[precision]
     if precision == "fp32":
         if deposit == "sorted":
             mode |= N.SC_FP32_SORTED_DEPOSIT
         if igf == "exact":
             mode |= N.SC_FP32_EXACT_IGF
+        if fields == "spectral":
+            mode |= N.SC_FP32_SPECTRAL_FIELDS
     return mode
 
 
@@ -209,7 +213,12 @@ class SpaceCharge(PhysProc):
     accumulation, default; "sorted": radix sort + Kahan segment sums) and
     ``igf`` ("hybrid": FP64 8-corner IGF near the origin, multipole form
     beyond 5 cell widths, default; "exact": FP64 8-corner IGF everywhere),
-    and ``device``.
+    ``fields`` ("difference": forward differences of the FP32 potential,
+    default; "spectral": the same differences taken in Fourier space before
+    the inverse transforms, whose rounding is relative to the field and not
+    to the potential -- for beams whose field differences are small against
+    the potential, at the cost of three more inverse transforms) and
+    ``device``.
     """
 
     def __init__(self, step=1, **kwargs):
@@ -225,7 +234,8 @@ class SpaceCharge(PhysProc):
         self.precision = kwargs.get("precision", "fp64")
         self.deposit = kwargs.get("deposit", "fixed")
         self.igf = kwargs.get("igf", "hybrid")
-        plan_mode(self.precision, self.deposit, self.igf)  # validates
+        self.fields = kwargs.get("fields", "difference")
+        plan_mode(self.precision, self.deposit, self.igf, self.fields)  # validates
         self.device = kwargs.get("device", None)
         self._engines = {}
 
@@ -238,7 +248,7 @@ class SpaceCharge(PhysProc):
 
     def engine(self, shape=None) -> Engine:
         shape = tuple(int(v) for v in (self.nmesh_xyz if shape is None else shape))
-        mode = plan_mode(self.precision, self.deposit, self.igf)
+        mode = plan_mode(self.precision, self.deposit, self.igf, self.fields)
         key = (shape, mode, str(self.device))
         eng = self._engines.get(key)
         if eng is None:

@@ -34,7 +34,8 @@ from ocelot_gb300 import SpaceCharge  # noqa: E402
 
 Q = 1e-9
 BUNCHES = [(1e-3, 1e-3, 1e-3), (50e-6, 50e-6, 25e-3)]
-FORMS = [dict(precision="fp64"), dict(precision="fp32", igf="hybrid"), dict(precision="fp32", igf="exact")]
+FORMS = [dict(precision="fp64"), dict(precision="fp32", igf="hybrid"), dict(precision="fp32", igf="exact"),
+         dict(precision="fp32", fields="spectral")]
 
 
 def _slack(form):
