@@ -342,7 +342,7 @@ int sc_kick_launches(const sc_plan* plan);
  *     particle (SC_REGION_FIELD), for error measurements; the FP32 form then
  *     runs its direct-access kick loop (same arithmetic, same particles). */
 #define SC_PARAM_RECORD_FIELD 1
-#define SC_KICK_NVARIANTS 9
+#define SC_KICK_NVARIANTS 14
 int sc_plan_set_param(sc_plan* plan, int param, int value);
 int sc_plan_get_param(const sc_plan* plan, int param, int* value);
 /* Tile (particles), tile buffers, particles per thread and blocks per SM of a

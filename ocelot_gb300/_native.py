@@ -32,7 +32,7 @@ SC_NSTAGES = 11
 # launch-shape parameters of a plan (sc_plan_set_param)
 SC_PARAM_KICK_VARIANT = 0
 SC_PARAM_RECORD_FIELD = 1
-SC_KICK_NVARIANTS = 9
+SC_KICK_NVARIANTS = 14
 
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
 SC_WAIT_FRAME = 0

@@ -425,6 +425,20 @@ __device__ __forceinline__ void bulk_wait_read() {
 }
 // every bulk group has completed
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// Per-thread asynchronous copies global -> shared (cp.async): 8 bytes, both
+// addresses 8-byte aligned; src_bytes 0 fills the 8 bytes with zeros.  A
+// thread's copies form groups (commit) and wait_group<N> waits until at most
+// N of the calling thread's newest groups are still in flight -- a wait on
+// the thread's own copies only, which complete like ordinary loads.
+__device__ __forceinline__ void async_copy8(void* dst_smem, const void* src, unsigned src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst_smem)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 // orders this thread's shared-memory writes before later async-proxy reads
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 

@@ -1832,18 +1832,20 @@ __device__ __forceinline__ float oct_sample(const float* __restrict__ O, const A
 // coordinates to FP32 accuracy.)  The conversions are branch-free inline
 // forms (d2f_kick, f2d_exact): with range-checked forms and out-of-line
 // fallbacks the kick kernel, at its 80-register limit, ran 15% slower.
+// The kick of one particle as six FP32 increments of its MAD coordinates
+// (x, x', y, y', tau, delta), from the coordinates rounded to FP32 (f).
 // rec != nullptr (the record-field mode): the three field samples, the
 // trilinear gathers of Ex, Ey, Ez at the particle before the gamma0 factor
 // (sc.py:201-204), are stored at rec[0], rec[nX], rec[2 nX].
-__device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp,
-                                         float* rec = nullptr) {
+__device__ __forceinline__ void kick_inc(const float (&f)[6], const Kick32C& C, const KickParams& kp,
+                                         float (&inc)[6], float* rec = nullptr) {
     float px, py, pz, E;
-    mom32(d2f_kick(r[1]), d2f_kick(r[3]), d2f_kick(r[5]), kp, px, py, pz, E);
+    mom32(f[1], f[3], f[5], kp, px, py, pz, E);
     // lab position, rotated and scaled to the grid
-    const float tau = d2f_kick(r[4]);
+    const float tau = f[4];
     const float iE = rcpf(E);
     float l[3];
-    lab32(d2f_kick(r[0]), d2f_kick(r[2]), tau, px, py, pz, E, kp, l);
+    lab32(f[0], f[2], tau, px, py, pz, E, kp, l);
     float X[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -1880,15 +1882,41 @@ __device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const
     const float dtau = tau * fz * iE * rcpf(pzn);
     const float iEE = iE * iEn;
     // new MAD coordinates as increments (coord_transform.py:16-54)
-    const float dx = fmaf(tau * fmaf(dpx, E, -px * dE), iEE, pxn * iEn * dtau);
-    const float dy = fmaf(tau * fmaf(dpy, E, -py * dE), iEE, pyn * iEn * dtau);
-    // the only FP64 arithmetic: six additions into the float64 coordinates
-    r[0] += f2d_exact(dx);
-    r[1] += f2d_exact(dpx * C.ipref);
-    r[2] += f2d_exact(dy);
-    r[3] += f2d_exact(dpy * C.ipref);
-    r[4] += f2d_exact(dtau);
-    r[5] += f2d_exact(dE * C.ipref);
+    inc[0] = fmaf(tau * fmaf(dpx, E, -px * dE), iEE, pxn * iEn * dtau);
+    inc[1] = dpx * C.ipref;
+    inc[2] = fmaf(tau * fmaf(dpy, E, -py * dE), iEE, pyn * iEn * dtau);
+    inc[3] = dpy * C.ipref;
+    inc[4] = dtau;
+    inc[5] = dE * C.ipref;
+}
+
+// FP32 gather + kick of one particle, r = its six float64 coordinates,
+// updated in place.  The momenta, the rotated grid coordinates and the kick
+// are recomputed from r in FP32 with fused multiply-adds and the hardware's
+// approximate reciprocal and square root, so the kick reads nothing per
+// particle but rparticles.  (The NGP keys, which must equal the FP64 form's,
+// are decided by the keys kernel alone; the gather only needs the grid
+// coordinates to FP32 accuracy.)  The conversions are branch-free inline
+// forms (d2f_kick, f2d_exact): with range-checked forms and out-of-line
+// fallbacks the kick kernel, at its 80-register limit, ran 15% slower.  The
+// only FP64 arithmetic is the six additions into the float64 coordinates.
+__device__ __forceinline__ void kick_one(double (&r)[6], const Kick32C& C, const KickParams& kp,
+                                         float* rec = nullptr) {
+    float f[6], inc[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[k] = d2f_kick(r[k]);
+    kick_inc(f, C, kp, inc, rec);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r[k] += f2d_exact(inc[k]);
+}
+
+// one double from shared memory, read where it stands in the program (not
+// merged with an earlier read of the same word, so it holds no register
+// across the code between)
+__device__ __forceinline__ double ld_shared_f64(const double* p) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(smem_u32(p)));
+    return v;
 }
 
 // Gather + kick with direct row accesses: each thread takes G consecutive
@@ -1998,26 +2026,25 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
         const bool ok = mbar_wait(&bar[s], (unsigned)((t / STAGES) & 1), kp.wait_limit[2]);
         double* B = buf + s * 6 * TILE;
         const int j = PPT * threadIdx.x;
-        if (PPT == 2 && j + 1 < staged) {  // both particles staged: 16-byte shared accesses
-            double r[2][6];
+        if (PPT == 2 && j + 1 < staged) {  // both particles staged
+            // the FP32 coordinates for the kicks; the float64 values are read
+            // again for the additions, so they hold no registers meanwhile
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const double2 v = *reinterpret_cast<const double2*>(B + k * TILE + j);
-                r[0][k] = v.x;
-                r[1][k] = v.y;
+            for (int w = 0; w < 2; ++w) {
+                float f[6], inc[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) f[k] = d2f_kick(ld_shared_f64(B + k * TILE + j + w));
+                kick_inc(f, C, kp, inc);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) B[k * TILE + j + w] = ld_shared_f64(B + k * TILE + j + w) + f2d_exact(inc[k]);
             }
-            kick_one(r[0], C, kp);
-            kick_one(r[1], C, kp);
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                *reinterpret_cast<double2*>(B + k * TILE + j) = make_double2(r[0][k], r[1][k]);
         } else if (PPT == 1 && j < staged) {
-            double r[6];
+            float f[6], inc[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) r[k] = B[k * TILE + j];
-            kick_one(r, C, kp);
+            for (int k = 0; k < 6; ++k) f[k] = d2f_kick(ld_shared_f64(B + k * TILE + j));
+            kick_inc(f, C, kp, inc);
 #pragma unroll
-            for (int k = 0; k < 6; ++k) B[k * TILE + j] = r[k];
+            for (int k = 0; k < 6; ++k) B[k * TILE + j] = ld_shared_f64(B + k * TILE + j) + f2d_exact(inc[k]);
         } else if (j < cnt && ok) {  // the odd last particle of the beam (j == staged): read and written directly
             double r[6];
             for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i0 + j];
@@ -2056,6 +2083,84 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
     }
 }
 
+// Gather + kick without block barriers: each thread streams its particles
+// through a private ring of STAGES slots in shared memory (the six doubles of
+// one particle per slot, [STAGES][6][threads] so that a warp's lanes touch
+// consecutive words) with per-thread asynchronous copies, and waits only for
+// its own copies -- so a warp whose gathers return late holds up no other
+// warp.  Work goes in chunks of 32 consecutive particles (one per lane) that
+// warps take in turn: a warp's first chunk is its index in the grid, each
+// further one is claimed from the kick's counter when its copies are issued,
+// STAGES - 1 chunks ahead of the one being kicked.  Results are stored
+// directly (each warp writes 256 contiguous bytes per row).  Any row stride
+// works (the copies are 8 bytes).  Every particle's arithmetic is kick_one,
+// so this gives the same bits as every other tiling.
+template <int STAGES>
+__device__ __forceinline__ void kick32_async_body(double* __restrict__ rp, const float* __restrict__ ox,
+                                                  const float* __restrict__ oy, const float* __restrict__ oz,
+                                                  const KickParams& kp, ScState* st, VBlk vb,
+                                                  float* __restrict__ rec = nullptr) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    if (st->status != SC_OK) return;  // read by every thread; the frame set it before this launch
+    double* ring = reinterpret_cast<double*>(smraw);  // [STAGES][6][blockDim.x]
+    const int nt = (int)blockDim.x, lane = (int)(threadIdx.x & 31);
+    const int64_t n = kp.n, ld = kp.ld;
+    const int64_t nchunk = (n + 31) / 32;
+    const int64_t wpb = nt / 32;
+    const int64_t first = (int64_t)vb.x * wpb + (threadIdx.x >> 5), nwarps = (int64_t)vb.nx * wpb;
+    auto claim = [&]() -> int64_t {
+        unsigned c = 0;
+        if (lane == 0) c = atomicAdd(&st->kick_next, 1u);
+        return nwarps + (int64_t)__shfl_sync(FULL, c, 0);
+    };
+    auto issue = [&](int s, int64_t c) {  // this lane's particle of chunk c into slot s
+        const int64_t i = c * 32 + lane;
+        if (c < nchunk && i < n) {
+            double* slot = ring + (size_t)s * 6 * nt + threadIdx.x;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) async_copy8(slot + k * nt, rp + k * ld + i, 8u);
+        }
+        async_commit();  // one group per slot, empty or not, so that the group count stays in step
+    };
+    const Kick32C C = kick32_const(st, kp, ox, oy, oz);
+    int64_t chunk[STAGES];
+    bool more = true;  // the last claim was a chunk (the same in every lane of the warp)
+#pragma unroll
+    for (int s = 0; s < STAGES; ++s) {
+        chunk[s] = !more ? nchunk : (s == 0 ? first : claim());
+        more = chunk[s] < nchunk;
+        issue(s, chunk[s]);
+    }
+    for (int64_t t = 0;; ++t) {
+        const int s = (int)(t % STAGES);
+        int64_t c = 0;
+#pragma unroll
+        for (int u = 0; u < STAGES; ++u)
+            if (u == s) c = chunk[u];
+        if (c >= nchunk) break;
+        async_wait<STAGES - 1>();  // this thread's copies of slot s have landed
+        const int64_t i = c * 32 + lane;
+        if (i < n) {
+            // the coordinates in FP32 for the kick; the float64 values are read
+            // again for the additions, so they hold no registers meanwhile
+            const double* slot = ring + (size_t)s * 6 * nt + threadIdx.x;
+            float f[6], inc[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) f[k] = d2f_kick(ld_shared_f64(slot + k * nt));
+            kick_inc(f, C, kp, inc, rec ? rec + i : nullptr);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) rp[k * ld + i] = ld_shared_f64(slot + k * nt) + f2d_exact(inc[k]);
+        }
+        const int64_t nc = more ? claim() : nchunk;
+        more = nc < nchunk;
+#pragma unroll
+        for (int u = 0; u < STAGES; ++u)
+            if (u == s) chunk[u] = nc;
+        issue(s, nc);
+    }
+    async_wait<0>();
+}
+
 // The kick's tilings: (tile, tile buffers, particles per thread, blocks per
 // SM the kernel is compiled for).  Variant 0 is the default; a plan's
 // kick_variant selects another (autotuned per mesh and particle count).
@@ -2069,6 +2174,13 @@ __device__ __forceinline__ void kick32_tma_body(double* __restrict__ rp, const f
     X(6, 512, 3, 1, 2)       \
     X(7, 1024, 3, 1, 1)      \
     X(8, 256, 3, 1, 5)
+// the barrier-free tilings (kick32_async_body, 256 threads): (slots per thread, blocks per SM)
+#define SC_KICK_ASYNC_VARIANTS(X) \
+    X(9, 3, 5)                    \
+    X(10, 4, 4)                   \
+    X(11, 2, 6)                   \
+    X(12, 6, 3)                   \
+    X(13, 3, 4)
 
 // the default: 256-particle tiles, one particle per thread, 4 blocks per SM
 // (measured fastest from 1M particles up on 48^3 to 128x128x256 meshes)
@@ -2080,6 +2192,14 @@ __global__ void __launch_bounds__(KickTiling<TILE, STAGES, PPT>::threads, MINB)
                  const float* __restrict__ oz, KickParams kp, ScState* st) {
     pdl_wait();
     kick32_tma_body<TILE, STAGES, PPT>(rp, ox, oy, oz, kp, st, hw_vblk());
+}
+
+template <int STAGES, int MINB>
+__global__ void __launch_bounds__(PT, MINB)
+    k_kick32_async(double* __restrict__ rp, const float* __restrict__ ox, const float* __restrict__ oy,
+                   const float* __restrict__ oz, KickParams kp, ScState* st) {
+    pdl_wait();
+    kick32_async_body<STAGES>(rp, ox, oy, oz, kp, st, hw_vblk());
 }
 
 constexpr int KICK_MIN_BLOCKS = 3;  // blocks per SM of the direct-access kick kernels
@@ -2170,6 +2290,19 @@ __global__ void __launch_bounds__(PT, 4) kb_keys32(const BatchBeam* __restrict__
     else keys32_body<false>(X, keys, B.rp, B.q, qfix, B.kp, st, vb);
 }
 
+template <int STAGES, int MINB>
+__global__ void __launch_bounds__(PT, MINB) kb_kick32_async(const BatchBeam* __restrict__ beams,
+                                                            const int* __restrict__ start, int nb) {
+    pdl_wait();
+    const int b = batch_beam(start, nb);
+    const BatchBeam& B = beams[b];
+    const VBlk vb = batch_vblk(start, b, B.gx[BS_PART], 1);
+    ScState* st = reinterpret_cast<ScState*>(B.ws + B.L.state);
+    kick32_async_body<STAGES>(B.rp, reinterpret_cast<const float*>(B.ws + B.L.exq),
+                              reinterpret_cast<const float*>(B.ws + B.L.eyq),
+                              reinterpret_cast<const float*>(B.ws + B.L.ezq), B.kp, st, vb);
+}
+
 template <int TILE, int STAGES, int PPT, int MINB>
 __global__ void __launch_bounds__(KickTiling<TILE, STAGES, PPT>::threads, MINB)
     kb_kick32(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
@@ -2191,14 +2324,20 @@ using KickBatchFn = void (*)(const BatchBeam*, const int*, int);
 struct KickVariant {
     KickFn fn;
     KickBatchFn batch_fn;
-    int tile, stages, ppt, minb, threads;
+    int tile, stages, ppt, minb, threads;  // tile 32: a barrier-free tiling (chunks of 32 per warp)
     size_t smem;
+    bool any_rows;                         // runs on any row stride (else 16-byte aligned rows, even stride)
 };
 static const KickVariant kKickVariants[] = {
-#define SC_KV(i, T, S, P, M) \
-    {k_kick32_tma<T, S, P, M>, kb_kick32<T, S, P, M>, T, S, P, M, KickTiling<T, S, P>::threads, KickTiling<T, S, P>::smem},
+#define SC_KV(i, T, S, P, M)                                                                                       \
+    {k_kick32_tma<T, S, P, M>, kb_kick32<T, S, P, M>, T, S, P, M, KickTiling<T, S, P>::threads,                  \
+     KickTiling<T, S, P>::smem, false},
     SC_KICK_VARIANTS(SC_KV)
 #undef SC_KV
+#define SC_KA(i, S, M) \
+    {k_kick32_async<S, M>, kb_kick32_async<S, M>, 32, S, 1, M, PT, (size_t)S * 6 * PT * sizeof(double), true},
+    SC_KICK_ASYNC_VARIANTS(SC_KA)
+#undef SC_KA
 };
 constexpr int kNumKickVariants = (int)(sizeof(kKickVariants) / sizeof(kKickVariants[0]));
 static_assert(KickTiling<256, 3, 1>::threads == PT, "the default kick tiling has PT threads");
@@ -2360,14 +2499,16 @@ cudaError_t launch_gather_kick(const Plan& p, const Layout& L, char* ws, const K
         const int g = kick_group(rp, kp.ld);
         // one wave of resident blocks, each looping over its tiles or groups
         const KickVariant& v = kKickVariants[p.kick_variant >= 0 && p.kick_variant < kNumKickVariants ? p.kick_variant : 0];
-        const int minb = g >= 2 ? v.minb : KICK_MIN_BLOCKS;
-        const int64_t units = g >= 2 ? (kp.n + v.tile - 1) / v.tile : (kp.n + PT - 1) / PT;
+        const bool tiled = g >= 2 || v.any_rows;
+        const int minb = tiled ? v.minb : KICK_MIN_BLOCKS;
+        const int per_block = v.any_rows ? v.threads : v.tile;  // particles per block per round
+        const int64_t units = tiled ? (kp.n + per_block - 1) / per_block : (kp.n + PT - 1) / PT;
         const int64_t kb = units < (int64_t)p.sm_count * minb ? units : (int64_t)p.sm_count * minb;
         const int nbk = (int)(kb > 0 ? kb : 1);
         ScState* stw = reinterpret_cast<ScState*>(ws + L.state);
         if (p.record_field)  // the direct-access loop, storing the field samples in the X rows
             launch(k_kick32<1, true>, nbk, PT, 0, s, rp, ox, oy, oz, kp, st, reinterpret_cast<float*>(ws + L.X));
-        else if (g >= 2) launch(v.fn, nbk, v.threads, v.smem, s, rp, ox, oy, oz, kp, stw);
+        else if (tiled) launch(v.fn, nbk, v.threads, v.smem, s, rp, ox, oy, oz, kp, stw);
         else launch(k_kick32<1, false>, nbk, PT, 0, s, rp, ox, oy, oz, kp, st, nullptr);
     }
     return cudaGetLastError();
