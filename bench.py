@@ -127,7 +127,7 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def time_form(precision, n, steps, warmup, dev, flush, fields="difference"):
+def time_form(precision, n, steps, warmup, dev, flush, fields="spectral"):
     """Device-resident kicks; per-kick CUDA events; per-stage events from the library."""
     import torch
     from ocelot_gb300 import SpaceCharge
@@ -428,6 +428,16 @@ def time_batched(steps, warmup, dev):
         b.synchronize()
         ms.append(a.elapsed_time(b))
     batch.check()
+    # stage split of the batched kick (events between the launches: separate kicks)
+    batch.profile(True)
+    stage_ms = {}
+    for _ in range(3):
+        batch.kick()
+        for k, v in batch.profile_read().items():
+            stage_ms.setdefault(k, []).append(v)
+    batch.profile(False)
+    stage_ms = {k: sum(v) / len(v) for k, v in stage_ms.items()}
+    batch.check()
     # the same beams, one plain kick each, on one stream (same plans and workspaces)
     seq_ms = []
     for it in range(warmup + steps):
@@ -450,7 +460,7 @@ def time_batched(steps, warmup, dev):
                     "E 5-500 MeV, Q 20-500 pC, sigma_x and sigma_tau log-uniform 20-500 um; one 0.1 m kick "
                     "per beam per step (FP32 form); 15 launches per step recorded as one CUDA graph",
         "beams": len(specs), "particles": ntot, "value": ntot / (t * 1e-3), "unit": "particle-kicks/s",
-        "ms_per_step": t, "launches_per_step": 15,
+        "ms_per_step": t, "launches_per_step": 15, "stages_ms": stage_ms,
         "sequential": {"value": ntot / (ts * 1e-3), "ms_per_step": ts, "launches_per_step": 15 * len(specs),
                        "how": "one sc_kick per beam, one stream, same plans and workspaces"},
         "batched_over_sequential": ts / t,
@@ -508,7 +518,8 @@ def time_serving(dev, rates=SERVE_RATES, jobs=SERVE_JOBS):
 
 def headline_config(n, ws):
     """The workload of the headline line (the same dict in both arms)."""
-    return {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step (FP32 form)",
+    return {"workload": "2M particles, 64^3 mesh, 130 MeV, 1 nC, one 0.1 m kick per step (FP32 form, spectral "
+                        "fields)",
             "n_particles": n, "mesh": MESH, "form": "fp32",
             "l2": "flushed between kicks (256 MB write, then 256 MB read)", "parallelism": f"replicas x{ws}"}
 
@@ -689,8 +700,8 @@ def main():
         kick32, stages32, launches32 = time_form("fp32", n, args.steps, args.warmup, dev, flush)
         barrier()
     kick64, stages64, _ = ([], {}, 0) if args.no_fp64 else time_form("fp64", n, args.steps, 3, dev, flush)
-    kicksp, stagessp, _ = ([], {}, 0) if args.kick_only else time_form("fp32", n, args.steps, 3, dev, flush,
-                                                                     fields="spectral")
+    kickdf, stagesdf, _ = ([], {}, 0) if args.kick_only else time_form("fp32", n, args.steps, 3, dev, flush,
+                                                                     fields="difference")
     e2e_dt, h2d, d2h = (math.nan, 0, 0) if args.kick_only else time_e2e("fp32", n, args.steps, args.warmup, dev)
     e2e_page_dt = math.nan if args.kick_only else time_e2e("fp32", n, args.steps, args.warmup, dev, pinned=False)[0]
     e2e64_dt = math.nan if (args.kick_only or args.no_fp64) else time_e2e("fp64", n, args.steps, args.warmup, dev)[0]
@@ -702,12 +713,13 @@ def main():
         for cfg in (CONFIG1, CONFIG3):
             configs[cfg["key"]] = time_config(cfg, 3, 1, dev, flush, cpu_threads)
         configs["config3"]["fp32_errors_vs_fp64"] = form_errors(CONFIG3, dev, fp32_mode={"fields": "spectral"})
-        configs["config3"]["fp32_difference_fields_errors_vs_fp64"] = form_errors(CONFIG3, dev)
+        configs["config3"]["fp32_difference_fields_errors_vs_fp64"] = form_errors(CONFIG3, dev,
+                                                                                   fp32_mode={"fields": "difference"})
     batched = None if args.no_batch else time_batched(args.steps, args.warmup, dev)
     serving = None if args.no_serve else time_serving(dev)
     head_cfg = {"n": n, "mesh": MESH, "E": E_GEV, "dz": DZ, "charge": CHARGE, "beam": "gauss"}
-    errors = None if args.kick_only else form_errors(head_cfg, dev)
-    errors_sp = None if args.kick_only else form_errors(head_cfg, dev, fp32_mode={"fields": "spectral"})
+    errors = None if args.kick_only else form_errors(head_cfg, dev, fp32_mode={"fields": "spectral"})
+    errors_df = None if args.kick_only else form_errors(head_cfg, dev, fp32_mode={"fields": "difference"})
     barrier()
 
     t32 = sum(kick32) / 1e3
@@ -749,12 +761,13 @@ def main():
                                     "d2h_bytes_per_step": d2h, "host_memory": "pinned"}
                                    if e2e64_dt == e2e64_dt else None)} if kick64 else None),
             "fp32_over_fp64": (statistics.mean(kick64) / statistics.mean(kick32)) if kick64 else None,
-            "fp32_spectral_form": ({"value": n * args.steps / (sum(kicksp) / 1e3),
-                                    "ms_per_step": statistics.mean(kicksp), "stages_ms": stagessp,
-                                    "errors_vs_fp64": errors_sp,
-                                    "over_fp64": (statistics.mean(kick64) / statistics.mean(kicksp)) if kick64 else None,
-                                    "what": "the FP32 form with the field differences taken in Fourier space "
-                                            "(fields='spectral')"} if kicksp else None),
+            "fp32_difference_form": ({"value": n * args.steps / (sum(kickdf) / 1e3),
+                                      "ms_per_step": statistics.mean(kickdf), "stages_ms": stagesdf,
+                                      "errors_vs_fp64": errors_df,
+                                      "over_fp64": (statistics.mean(kick64) / statistics.mean(kickdf)) if kick64 else None,
+                                      "what": "the FP32 form with the reference's differences of the FP32 potential "
+                                              "(fields='difference'); the headline form takes them in Fourier space"}
+                                     if kickdf else None),
             "fp32_kick_rel_rms_err_vs_fp64": errors["kick"] if errors else None,
             "fp32_errors_vs_fp64": errors,
             "stages_ms": stages32,

@@ -160,6 +160,12 @@ int sc_batch_set(sc_batch* batch, const sc_beam* beams, int nbeams, void* stream
 int sc_kick_batched(sc_batch* batch, void* stream);
 /* Kernels launched by the last sc_kick_batched (0 before the first). */
 int sc_batch_launches(const sc_batch* batch);
+/* Stage timing of batched kicks, as sc_profile_enable / sc_profile_read of a
+ * plan (the same SC_NSTAGES stages, summed over the beams of each launch);
+ * the events sit between the launches, so kicks timed this way run a little
+ * slower.  No counterpart in the reference. */
+int sc_batch_profile_enable(sc_batch* batch, int enable);
+int sc_batch_profile_read(sc_batch* batch, float* ms /* [SC_NSTAGES] */);
 /* rparticles <- R . rparticles + B for every beam of the table that was set
  * with a map (sc_beam.tmap), in one launch: the transport before the kick of
  * a tracking step (TransferMap.mul_p_array, transfer_map.py:40-50), with the

@@ -87,6 +87,8 @@ SIGNATURES = {
     "sc_batch_set": (C.c_int, [vp, C.POINTER(ScBeam), C.c_int, vp]),
     "sc_kick_batched": (C.c_int, [vp, vp]),
     "sc_batch_launches": (C.c_int, [vp]),
+    "sc_batch_profile_enable": (C.c_int, [vp, C.c_int]),
+    "sc_batch_profile_read": (C.c_int, [vp, C.POINTER(C.c_float)]),
     "sc_tmap_batched": (C.c_int, [vp, vp]),
     "sc_profile_enable": (C.c_int, [vp, C.c_int]),
     "sc_profile_read": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]),

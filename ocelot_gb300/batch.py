@@ -29,16 +29,17 @@ class BeamBatch:
     ``commit()`` uploads the work table; ``kick()`` kicks every beam
     (asynchronous, current stream); ``graph()`` records one batched kick as
     a CUDA graph to replay.  ``igf="exact"`` uses the FP64 8-corner IGF on
-    the whole octant instead of the hybrid table.
+    the whole octant instead of the hybrid table; ``fields`` as in
+    ``SpaceCharge`` (spectral by default).
     """
 
-    def __init__(self, device=None, igf: str = "hybrid", max_beams: int = 1024):
+    def __init__(self, device=None, igf: str = "hybrid", max_beams: int = 1024, fields: str = "spectral"):
         import torch
         if not torch.cuda.is_available():
             raise N.NativeLibraryError("ocelot_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = N.lib()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-        self.mode = plan_mode("fp32", "fixed", igf)
+        self.mode = plan_mode("fp32", "fixed", igf, fields)
         self.max_beams = int(max_beams)
         h = C.c_void_p()
         with torch.cuda.device(self.device):
@@ -126,6 +127,17 @@ class BeamBatch:
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_tmap_batched(self.handle,
                                              C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
+
+    def profile(self, enable: bool = True):
+        """Stage events between the batched launches (read with profile_read)."""
+        N.check(self.lib.sc_batch_profile_enable(self.handle, 1 if enable else 0))
+
+    def profile_read(self):
+        """{stage: ms} of the last batched kick (synchronous)."""
+        ms = (C.c_float * N.SC_NSTAGES)()
+        N.check(self.lib.sc_batch_profile_read(self.handle, ms))
+        names = [self.lib.sc_profile_stage_name(i).decode() for i in range(N.SC_NSTAGES)]
+        return dict(zip(names, [float(v) for v in ms]))
 
     @property
     def launches(self) -> int:

@@ -742,6 +742,8 @@ struct sc_batch {
     cudaStream_t side;
     cudaEvent_t fork, join;
     int last_launches;
+    bool profiling;
+    cudaEvent_t ev[NEV];     // as a plan's: main stream 0..9, side stream 10..13
 };
 
 int sc_batch_create(sc_batch** out, int max_beams) {
@@ -775,6 +777,8 @@ int sc_batch_create(sc_batch** out, int max_beams) {
 
 void sc_batch_destroy(sc_batch* b) {
     if (!b) return;
+    if (b->profiling)
+        for (int i = 0; i < NEV; ++i) cudaEventDestroy(b->ev[i]);
     if (b->side) {
         cudaStreamSynchronize(b->side);
         cudaStreamDestroy(b->side);
@@ -798,9 +802,8 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
     for (int i = 0; i < nbeams; ++i) {
         const sc_beam& m = beams[i];
         if (!m.plan) return fail(SC_ERR_ARG, "beam %d: plan is NULL", i);
-        if (m.plan->p.prec != SC_FP32 || m.plan->p.sorted_deposit || m.plan->p.spectral)
-            return fail(SC_ERR_UNSUPPORTED,
-                        "beam %d: batched kicks need SC_FP32 plans with the fixed-point deposit and difference fields", i);
+        if (m.plan->p.prec != SC_FP32 || m.plan->p.sorted_deposit)
+            return fail(SC_ERR_UNSUPPORTED, "beam %d: batched kicks need SC_FP32 plans with the fixed-point deposit", i);
         if (m.zstep == 0 && !m.tmap) continue;  // nothing to do for this beam
         if (m.n < 1 || m.n > 0x7fffffffLL) return fail(SC_ERR_ARG, "beam %d: n=%lld", i, (long long)m.n);
         if (!m.rparticles || !m.q) return fail(SC_ERR_ARG, "beam %d: rparticles or q is NULL", i);
@@ -900,35 +903,85 @@ int sc_kick_batched(sc_batch* b, void* stream) {
     const int stride = b->max_beams + 1;
     auto row = [&](int st) { return start + st * stride; };
     const int nb = b->nb;
+    auto bmark = [&](int i, cudaStream_t st) {
+        if (b->profiling) cudaEventRecord(b->ev[i], st);
+    };
+    bmark(0, s);
     SC_CUDA(launch_batch_particles(BP_FRAME, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched frame");
+    bmark(1, s);
     SC_CUDA(launch_batch_particles(BP_EXTENT, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched extent");
+    bmark(2, s);
     SC_CUDA(cudaEventRecord(b->fork, s), "cudaEventRecord");
     SC_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0), "cudaStreamWaitEvent");
+    bmark(10, b->side);
     SC_CUDA(launch_batch_igf(beams, row(BS_IGF_C), row(BS_IGF_D), nb, b->blocks[BS_IGF_C], b->blocks[BS_IGF_D],
                              b->side),
             "batched igf");
+    bmark(11, b->side);
     const int gb[3] = {b->blocks[BS_GREEN_Z], b->blocks[BS_GREEN_Y], b->blocks[BS_GREEN_X]};
     SC_CUDA(launch_batch_green(beams, row(BS_GREEN_Z), row(BS_GREEN_Y), row(BS_GREEN_X), nb, gb, b->green_smem,
                                b->side),
             "batched green spectrum");
+    bmark(12, b->side);
     SC_CUDA(cudaEventRecord(b->join, b->side), "cudaEventRecord");
     SC_CUDA(launch_batch_particles(BP_KEYS, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched keys");
-    const int fb[3] = {b->blocks[BS_FFT_Z], b->blocks[BS_FFT_Y], b->blocks[BS_FFT_X]};
-    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), nb, fb, b->fft_smem, s,
+    bmark(3, s);
+    bmark(4, s);
+    bmark(5, s);
+    const int fb[5] = {b->blocks[BS_FFT_Z], b->blocks[BS_FFT_Y], b->blocks[BS_FFT_X], b->blocks[BS_FFT_YI],
+                       b->blocks[BS_FFT_ZI]};
+    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), row(BS_FFT_YI), row(BS_FFT_ZI),
+                                  nb, fb, b->fft_smem, s,
                                   CONV_FORWARD),
             "batched convolve");
+    bmark(13, s);
     SC_CUDA(cudaStreamWaitEvent(s, b->join, 0), "cudaStreamWaitEvent");
-    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), nb, fb, b->fft_smem, s,
-                                  CONV_REST),
+    bmark(6, s);
+    SC_CUDA(launch_batch_convolve(beams, row(BS_FFT_Z), row(BS_FFT_Y), row(BS_FFT_X), row(BS_FFT_YI), row(BS_FFT_ZI),
+                                  nb, fb, b->fft_smem, s, CONV_REST),
             "batched convolve");
+    bmark(7, s);
     SC_CUDA(launch_batch_field(beams, row(BS_FIELD), nb, b->blocks[BS_FIELD], s), "batched field");
+    bmark(8, s);
     SC_CUDA(launch_batch_particles(BP_KICK, beams, row(BS_PART), nb, b->blocks[BS_PART], s), "batched kick");
+    bmark(9, s);
     // frame, extent, igf 2, green 3, keys, convolve 5, field, kick
     b->last_launches = 1 + 1 + 2 + 3 + 1 + 5 + 1 + 1;
     return SC_OK;
 }
 
 int sc_batch_launches(const sc_batch* b) { return b ? b->last_launches : 0; }
+
+int sc_batch_profile_enable(sc_batch* b, int enable) {
+    if (!b) return fail(SC_ERR_ARG, "batch is NULL");
+    if (enable && !b->profiling) {
+        for (int i = 0; i < NEV; ++i) {
+            const cudaError_t e = cudaEventCreate(&b->ev[i]);
+            if (e) {
+                for (int j = 0; j < i; ++j) cudaEventDestroy(b->ev[j]);
+                return cuda_fail(e, "cudaEventCreate");
+            }
+        }
+        b->profiling = true;
+    } else if (!enable && b->profiling) {
+        for (int i = 0; i < NEV; ++i) cudaEventDestroy(b->ev[i]);
+        b->profiling = false;
+    }
+    return SC_OK;
+}
+
+int sc_batch_profile_read(sc_batch* b, float* ms) {
+    if (!b || !ms) return fail(SC_ERR_ARG, "bad arguments");
+    if (!b->profiling) return fail(SC_ERR_ARG, "profiling is not enabled");
+    SC_CUDA(cudaEventSynchronize(b->ev[9]), "cudaEventSynchronize");
+    static const int a[SC_NSTAGES] = {0, 1, 2, 3, 4, 10, 11, 13, 6, 7, 8};
+    static const int e[SC_NSTAGES] = {1, 2, 3, 4, 5, 11, 12, 6, 7, 8, 9};
+    for (int i = 0; i < SC_NSTAGES; ++i) SC_CUDA(cudaEventElapsedTime(&ms[i], b->ev[a[i]], b->ev[e[i]]), "cudaEventElapsedTime");
+    float fwd = 0.f;
+    SC_CUDA(cudaEventElapsedTime(&fwd, b->ev[5], b->ev[13]), "cudaEventElapsedTime");
+    ms[8] += fwd;
+    return SC_OK;
+}
 
 int sc_tmap_batched(sc_batch* b, void* stream) {
     if (!b) return fail(SC_ERR_ARG, "batch is NULL");

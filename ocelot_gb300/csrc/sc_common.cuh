@@ -270,9 +270,11 @@ enum BatchStage {
     BS_GREEN_Z,    // spectrum S1
     BS_GREEN_Y,    // spectrum S2
     BS_GREEN_X,    // spectrum S3
-    BS_FFT_Z,      // F1 and B1
-    BS_FFT_Y,      // F2 and B2
+    BS_FFT_Z,      // F1
+    BS_FFT_Y,      // F2
     BS_FFT_X,      // F3 (x forward, Green multiply, x inverse)
+    BS_FFT_YI,     // B2 (with spectral fields: two groups of blocks, W and the x-differenced W2)
+    BS_FFT_ZI,     // B1 (with spectral fields: four groups, the potential and Ex, Ey, Ez)
     BS_FIELD,      // field quads
     BS_TMAP,       // transport map (sc_tmap_batched): also the beams without a kick this step
     BS_COUNT
@@ -317,8 +319,9 @@ cudaError_t launch_batch_igf(const BatchBeam* beams, const int* start_c, const i
                              int blocks_d, cudaStream_t s);
 cudaError_t launch_batch_green(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
                                const int blocks[3], const size_t smem[3], cudaStream_t s);
-cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
-                                  const int blocks[3], const size_t smem[3], cudaStream_t s, int part = CONV_ALL);
+cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx,
+                                  const int* syi, const int* szi, int nb,
+                                  const int blocks[5], const size_t smem[3], cudaStream_t s, int part = CONV_ALL);
 cudaError_t launch_batch_field(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
 cudaError_t launch_batch_tmap(const BatchBeam* beams, const int* start, int nb, int blocks, cudaStream_t s);
 // host-side tiling of one beam (sets the tiling fields and grids of B)

@@ -408,12 +408,12 @@ __global__ void k_field_octs(const float* __restrict__ phi, float* __restrict__ 
 __device__ __forceinline__ float at_or0(const float* __restrict__ F, int i, int j, int k, int nx, int ny, int nz) {
     return (i < nx && j < ny && k < nz) ? F[((size_t)i * ny + j) * nz + k] : 0.f;
 }
-__global__ void k_field_octs_spectral(const float* __restrict__ ex, const float* __restrict__ ey,
-                                      const float* __restrict__ ez, float* __restrict__ ox, float* __restrict__ oy,
-                                      float* __restrict__ oz, int nx, int ny, int nz, const ScState* st) {
-    pdl_wait();
+__device__ __forceinline__ void field_octs_spectral_body(const float* __restrict__ ex, const float* __restrict__ ey,
+                                                         const float* __restrict__ ez, float* __restrict__ ox,
+                                                         float* __restrict__ oy, float* __restrict__ oz, int nx,
+                                                         int ny, int nz, const ScState* st, VBlk vb) {
     if (st->status) return;
-    const int j = blockIdx.x, i = blockIdx.y;
+    const int j = vb.x, i = vb.y;
     const float* const in[3] = {ex, ey, ez};
     float* const out[3] = {ox, oy, oz};
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {
@@ -430,6 +430,12 @@ __global__ void k_field_octs_spectral(const float* __restrict__ ex, const float*
             st_oct(out[d] + 8 * c, o);
         }
     }
+}
+__global__ void k_field_octs_spectral(const float* __restrict__ ex, const float* __restrict__ ey,
+                                      const float* __restrict__ ez, float* __restrict__ ox, float* __restrict__ oy,
+                                      float* __restrict__ oz, int nx, int ny, int nz, const ScState* st) {
+    pdl_wait();
+    field_octs_spectral_body(ex, ey, ez, ox, oy, oz, nx, ny, nz, st, hw_vblk());
 }
 
 
@@ -626,7 +632,7 @@ static int optin_smem() {
 
 // the spectral-field pointers of a plan's workspace (W2 == nullptr: none)
 template <typename R>
-static Spec<R> spec_of(const Plan& p, const Layout& L, char* ws, bool fields) {
+__host__ __device__ __forceinline__ Spec<R> spec_of(const Plan& p, const Layout& L, char* ws, bool fields) {
     Spec<R> sp = {};
     if (!(fields && p.spectral && sizeof(R) == 4)) return sp;
     sp.W2 = reinterpret_cast<Cx<R>*>(ws + L.W2);
@@ -775,81 +781,123 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_zfwd(const BatchBeam* __restri
                      reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.fft_nc, st, vb);
 }
 
-template <bool INV>
-__global__ void __launch_bounds__(FFT_THREADS) kb_ypass(const BatchBeam* __restrict__ beams,
-                                                        const int* __restrict__ start, int nb) {
+// forward y pass
+__global__ void __launch_bounds__(FFT_THREADS) kb_yfwd(const BatchBeam* __restrict__ beams,
+                                                       const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_FFT_Y)
-    ypass_body<float, INV>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry,
-                           reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.fft_tky, st, vb);
+    ypass_body<float, false>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry,
+                             reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.fft_tky, st, vb);
+}
+
+// inverse y pass: block group 0 takes W (and, with spectral fields, W x D(ky)
+// into W3), group 1 the x-differenced W2 (as k_ypass's blockIdx.z)
+__global__ void __launch_bounds__(FFT_THREADS) kb_yinv(const BatchBeam* __restrict__ beams,
+                                                       const int* __restrict__ start, int nb) {
+    pdl_wait();
+    BATCH_BEAM(BS_FFT_YI)
+    const Spec<float> sp = spec_of<float>(p, L, ws, true);
+    const int f = vb.y / p.nx;
+    const VBlk v = {vb.x, vb.y - f * p.nx, vb.nx, p.nx};
+    const Cx<float>* tw = reinterpret_cast<const Cx<float>*>(ws + L.tw_y);
+    if (f == 0)
+        ypass_body<float, true>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry, tw,
+                                B.fft_tky, st, v, sp.W3, sp.dy);
+    else
+        ypass_body<float, true>(sp.W2, p.ny, p.My, p.Mz / 2 + 1, p.ry, tw, B.fft_tky, st, v);
 }
 
 __global__ void __launch_bounds__(FFT_THREADS) kb_xconv(const BatchBeam* __restrict__ beams,
                                                         const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_FFT_X)
+    const Spec<float> sp = spec_of<float>(p, L, ws, true);
     xconv_body<float>(reinterpret_cast<Cx<float>*>(ws + L.W), reinterpret_cast<const float*>(ws + L.green), p.nx,
                       p.My, p.Mz / 2 + 1, p.My / 2 + 1, p.rx, reinterpret_cast<const Cx<float>*>(ws + L.tw_x),
-                      B.fft_tkx, st, vb);
+                      B.fft_tkx, st, vb, sp.W2, sp.dx);
 }
 
+// inverse z pass: block group f writes output f (the potential; with spectral
+// fields also Ex, Ey, Ez), as k_zinv's blockIdx.z
 __global__ void __launch_bounds__(FFT_THREADS) kb_zinv(const BatchBeam* __restrict__ beams,
                                                        const int* __restrict__ start, int nb) {
     pdl_wait();
-    BATCH_BEAM(BS_FFT_Z)
-    zinv_body<float>(reinterpret_cast<const Cx<float>*>(ws + L.W), reinterpret_cast<float*>(ws + L.phi), p.ny, p.nz,
-                     p.My, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z), B.fft_nc, st, vb);
+    BATCH_BEAM(BS_FFT_ZI)
+    const Spec<float> sp = spec_of<float>(p, L, ws, true);
+    const int f = vb.y / p.nx;
+    const VBlk v = {vb.x, vb.y - f * p.nx, vb.nx, p.nx};
+    const Cx<float>* src;
+    float* out;
+    const Cx<float>* dz;
+    float mul;
+    inv_out<float>(sp, st, f, reinterpret_cast<const Cx<float>*>(ws + L.W), reinterpret_cast<float*>(ws + L.phi), src,
+                   out, dz, mul);
+    zinv_body<float>(src, out, p.ny, p.nz, p.My, p.Mz / 2 + 1, p.rz, reinterpret_cast<const Cx<float>*>(ws + L.tw_z),
+                     B.fft_nc, st, v, dz, mul, f - 1, p.nx);
 }
 
 __global__ void kb_field_octs(const BatchBeam* __restrict__ beams, const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_FIELD)
-    field_octs_body(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
-                    reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq), p.nx, p.ny, p.nz,
-                     st, vb);
+    if (p.spectral)
+        field_octs_spectral_body(reinterpret_cast<const float*>(ws + L.ex), reinterpret_cast<const float*>(ws + L.ey),
+                                 reinterpret_cast<const float*>(ws + L.ez), reinterpret_cast<float*>(ws + L.exq),
+                                 reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq), p.nx, p.ny,
+                                 p.nz, st, vb);
+    else
+        field_octs_body(reinterpret_cast<const float*>(ws + L.phi), reinterpret_cast<float*>(ws + L.exq),
+                        reinterpret_cast<float*>(ws + L.eyq), reinterpret_cast<float*>(ws + L.ezq), p.nx, p.ny, p.nz,
+                        st, vb);
 }
 #undef BATCH_BEAM
 
 void batch_fft_tiling(BatchBeam& B, size_t smem[3]) {
     const Plan& p = B.p;
     const int Kz = p.Mz / 2 + 1;
+    const int nbuf = p.spectral ? 3 : 2;  // line buffers of the x pass and the y passes
     B.fft_nc = z_lines_per_block(p.Mz);
-    B.fft_tky = strided_cols<float>(p.My);
-    B.fft_tkx = strided_cols<float>(p.Mx);
+    B.fft_tky = strided_cols<float>(p.My, nbuf);
+    B.fft_tkx = strided_cols<float>(p.Mx, nbuf);
     B.gx[BS_FFT_Z] = (p.ny + 2 * B.fft_nc - 1) / (2 * B.fft_nc);
     B.gy[BS_FFT_Z] = p.nx;
     B.gx[BS_FFT_Y] = (Kz + B.fft_tky - 1) / B.fft_tky;
     B.gy[BS_FFT_Y] = p.nx;
     B.gx[BS_FFT_X] = (Kz + B.fft_tkx - 1) / B.fft_tkx;
     B.gy[BS_FFT_X] = p.My;
+    B.gx[BS_FFT_YI] = B.gx[BS_FFT_Y];
+    B.gy[BS_FFT_YI] = p.nx * (p.spectral ? 2 : 1);
+    B.gx[BS_FFT_ZI] = B.gx[BS_FFT_Z];
+    B.gy[BS_FFT_ZI] = p.nx * (p.spectral ? 4 : 1);
     B.gx[BS_FIELD] = p.ny;
     B.gy[BS_FIELD] = p.nx;
     smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.fft_nc * fft_ls(p.Mz));
-    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.fft_tky * fft_ls(p.My));
-    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.fft_tkx * fft_ls(p.Mx));
+    smem[1] = sizeof(Cx<float>) * (size_t)(p.My + nbuf * B.fft_tky * fft_ls(p.My));
+    smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + nbuf * B.fft_tkx * fft_ls(p.Mx));
 }
 
 cudaError_t prepare_batch_fft() {
     cudaError_t e;
     const size_t big = 48 * 1024 + 1;
     if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_zfwd), big))) return e;
-    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_ypass<false>), big))) return e;
-    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_ypass<true>), big))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_yfwd), big))) return e;
+    if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_yinv), big))) return e;
     if ((e = smem_opt_in(reinterpret_cast<const void*>(kb_xconv), big))) return e;
     return smem_opt_in(reinterpret_cast<const void*>(kb_zinv), big);
 }
 
-cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx, int nb,
-                                  const int blocks[3], const size_t smem[3], cudaStream_t s, int part) {
+// blocks: the five passes' block counts (z, y, x forward; y, z inverse)
+cudaError_t launch_batch_convolve(const BatchBeam* beams, const int* sz, const int* sy, const int* sx,
+                                  const int* syi, const int* szi, int nb, const int blocks[5], const size_t smem[3],
+                                  cudaStream_t s, int part) {
     if (nb <= 0) return cudaSuccess;
     if (part != CONV_REST) {
         launch(kb_zfwd, blocks[0], FFT_THREADS, smem[0], s, beams, sz, nb);
-        launch(kb_ypass<false>, blocks[1], FFT_THREADS, smem[1], s, beams, sy, nb);
+        launch(kb_yfwd, blocks[1], FFT_THREADS, smem[1], s, beams, sy, nb);
     }
     if (part == CONV_FORWARD) return cudaGetLastError();
     launch(kb_xconv, blocks[2], FFT_THREADS, smem[2], s, beams, sx, nb);
-    launch(kb_ypass<true>, blocks[1], FFT_THREADS, smem[1], s, beams, sy, nb);
-    launch(kb_zinv, blocks[0], FFT_THREADS, smem[0], s, beams, sz, nb);
+    launch(kb_yinv, blocks[3], FFT_THREADS, smem[1], s, beams, syi, nb);
+    launch(kb_zinv, blocks[4], FFT_THREADS, smem[0], s, beams, szi, nb);
     return cudaGetLastError();
 }
 

@@ -1801,18 +1801,21 @@ struct AxisW {
     float t;
     bool ok;
 };
+// The base cell is clamped into [0, n-2] whether or not the sample is valid,
+// so that the oct load below is always in bounds and needs no branch.
 __device__ __forceinline__ AxisW axis_w(float c, int n) {
     AxisW a;
     a.ok = c >= 0.f && c <= (float)(n - 1);
     int i = (int)c;
-    a.i = i > n - 2 ? n - 2 : i;
+    i = i > n - 2 ? n - 2 : i;
+    a.i = i < 0 ? 0 : i;
     a.t = c - (float)a.i;
     return a;
 }
-// one staggered field component from its octs at (ax, ay, az)
+// one staggered field component from its octs at (ax, ay, az); outside the
+// mesh the (in-bounds) load is made and its sample replaced by 0
 __device__ __forceinline__ float oct_sample(const float* __restrict__ O, const AxisW& ax, const AxisW& ay,
                                             const AxisW& az, int ny, int nz) {
-    if (!(ax.ok && ay.ok && az.ok)) return 0.f;
     const float* p = O + 8 * ((ax.i * ny + ay.i) * nz + az.i);  // < 2^31: meshes have at most 256^3 cells
     float o[8];
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -1820,7 +1823,8 @@ __device__ __forceinline__ float oct_sample(const float* __restrict__ O, const A
         : "l"(p));
     const float y0 = lerpf(lerpf(o[0], o[1], az.t), lerpf(o[2], o[3], az.t), ay.t);
     const float y1 = lerpf(lerpf(o[4], o[5], az.t), lerpf(o[6], o[7], az.t), ay.t);
-    return lerpf(y0, y1, ax.t);
+    const float v = lerpf(y0, y1, ax.t);
+    return (ax.ok && ay.ok && az.ok) ? v : 0.f;
 }
 
 // FP32 gather + kick of one particle, r = its six float64 coordinates,
@@ -2107,11 +2111,21 @@ __device__ __forceinline__ void kick32_async_body(double* __restrict__ rp, const
     const int64_t n = kp.n, ld = kp.ld;
     const int64_t nchunk = (n + 31) / 32;
     const int64_t wpb = nt / 32;
-    const int64_t first = (int64_t)vb.x * wpb + (threadIdx.x >> 5), nwarps = (int64_t)vb.nx * wpb;
+    // chunks are handed out in units of CLAIM consecutive chunks: one atomic
+    // per unit; a warp's first unit is its index in the grid
+    constexpr int CLAIM = 4;
+    const int64_t nwarps = (int64_t)vb.nx * wpb;
+    int64_t unit = (int64_t)vb.x * wpb + (threadIdx.x >> 5);
+    int in_unit = 0;
     auto claim = [&]() -> int64_t {
-        unsigned c = 0;
-        if (lane == 0) c = atomicAdd(&st->kick_next, 1u);
-        return nwarps + (int64_t)__shfl_sync(FULL, c, 0);
+        if (in_unit == CLAIM) {
+            unsigned c = 0;
+            if (lane == 0) c = atomicAdd(&st->kick_next, 1u);
+            unit = nwarps + (int64_t)__shfl_sync(FULL, c, 0);
+            in_unit = 0;
+        }
+        const int64_t c = unit * CLAIM + in_unit++;
+        return c < nchunk ? c : nchunk;
     };
     auto issue = [&](int s, int64_t c) {  // this lane's particle of chunk c into slot s
         const int64_t i = c * 32 + lane;
@@ -2127,7 +2141,7 @@ __device__ __forceinline__ void kick32_async_body(double* __restrict__ rp, const
     bool more = true;  // the last claim was a chunk (the same in every lane of the warp)
 #pragma unroll
     for (int s = 0; s < STAGES; ++s) {
-        chunk[s] = !more ? nchunk : (s == 0 ? first : claim());
+        chunk[s] = !more ? nchunk : claim();
         more = chunk[s] < nchunk;
         issue(s, chunk[s]);
     }

@@ -10,9 +10,9 @@ Two forms (constructor keyword ``precision``):
 
 * ``"fp64"`` (default, the plain form): FP64 end to end; reproduces the
   reference's ``apply`` to ~1e-10 relative on ``rparticles``.
-* ``"fp32"`` (the precision form): FP32 deposit, FFT convolution and
-  gather, FP64 Green's-function table and FP64 accumulation of the kick
-  into ``rparticles``.
+* ``"fp32"`` (the precision form): FP32 deposit, FFT convolution (field
+  differences in Fourier space) and gather, FP64 Green's-function table and
+  FP64 accumulation of the kick into ``rparticles``.
 
 ``apply(p_array, zstep)`` accepts Ocelot's host ``ParticleArray`` (numpy
 arrays; copied to the GPU and back each call, like the reference mutating
@@ -32,7 +32,7 @@ from .physics_proc import PhysProc
 _PREC = {"fp64": N.SC_FP64, "fp32": N.SC_FP32}
 
 
-def plan_mode(precision: str, deposit: str = "fixed", igf: str = "hybrid", fields: str = "difference") -> int:
+def plan_mode(precision: str, deposit: str = "fixed", igf: str = "hybrid", fields: str = "spectral") -> int:
     """Mode bits of a plan (include/ocelot_sc.h): the FP32 form's options."""
     if precision not in _PREC:
         raise ValueError(f"precision must be one of {sorted(_PREC)}, not {precision!r}")
@@ -213,12 +213,13 @@ class SpaceCharge(PhysProc):
     accumulation, default; "sorted": radix sort + Kahan segment sums) and
     ``igf`` ("hybrid": FP64 8-corner IGF near the origin, multipole form
     beyond 5 cell widths, default; "exact": FP64 8-corner IGF everywhere),
-    ``fields`` ("difference": forward differences of the FP32 potential,
-    default; "spectral": the same differences taken in Fourier space before
-    the inverse transforms, whose rounding is relative to the field and not
-    to the potential -- for beams whose field differences are small against
-    the potential, at the cost of three more inverse transforms) and
-    ``device``.
+    ``fields`` ("spectral", default: the forward differences of the
+    potential (sc.py:195-200) taken in Fourier space before the inverse
+    transforms, so that their FP32 rounding is relative to the field and not
+    to the potential, which is hundreds of times larger than the difference
+    of neighbouring cells -- ~30x smaller kick errors for ~2% more time on the
+    2M / 64^3 beam; "difference": the reference's differences of the FP32
+    potential) and ``device``.
     """
 
     def __init__(self, step=1, **kwargs):
@@ -234,7 +235,7 @@ class SpaceCharge(PhysProc):
         self.precision = kwargs.get("precision", "fp64")
         self.deposit = kwargs.get("deposit", "fixed")
         self.igf = kwargs.get("igf", "hybrid")
-        self.fields = kwargs.get("fields", "difference")
+        self.fields = kwargs.get("fields", "spectral")
         plan_mode(self.precision, self.deposit, self.igf, self.fields)  # validates
         self.device = kwargs.get("device", None)
         self._engines = {}

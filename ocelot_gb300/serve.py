@@ -106,7 +106,8 @@ class Server:
     ahead of the host at most.
     """
 
-    def __init__(self, device=None, hbm_budget=None, max_active: int = 64, inflight: int = 2, igf: str = "hybrid"):
+    def __init__(self, device=None, hbm_budget=None, max_active: int = 64, inflight: int = 2, igf: str = "hybrid",
+                 fields: str = "spectral"):
         import torch
         self.torch = torch
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -116,8 +117,8 @@ class Server:
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.inflight = max(1, int(inflight))
-        self.mode = plan_mode("fp32", "fixed", igf)
-        self.batch = BeamBatch(self.device, igf=igf, max_beams=self.max_active)
+        self.mode = plan_mode("fp32", "fixed", igf, fields)
+        self.batch = BeamBatch(self.device, igf=igf, max_beams=self.max_active, fields=fields)
         self.stream = torch.cuda.Stream(self.device)
         self.copy_stream = torch.cuda.Stream(self.device)
         self.pending = collections.deque()

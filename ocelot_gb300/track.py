@@ -463,7 +463,8 @@ class DeviceTrack:
         from .sc import Engine, plan_mode
         keys = {}
         for p, _, _ in processes:
-            key = (tuple(int(v) for v in p.nmesh_xyz), p.precision, plan_mode(p.precision, p.deposit, p.igf))
+            key = (tuple(int(v) for v in p.nmesh_xyz), p.precision,
+                   plan_mode(p.precision, p.deposit, p.igf, getattr(p, "fields", "spectral")))
             if key not in keys:
                 keys[key] = len(self.engines)
                 self.engines.append(Engine(key[0], key[1], self.dev, key[2]))

@@ -46,17 +46,17 @@ def _dev(rp, q, odd_stride=False):
     return buf[:, :n], torch.from_numpy(q).to(DEV)
 
 
-def _alone(rp, q, spec, kicks=1, odd_stride=False):
+def _alone(rp, q, spec, kicks=1, odd_stride=False, fields="spectral"):
     d_rp, d_q = _dev(rp, q, odd_stride)
-    sc = SpaceCharge(nmesh_xyz=spec[1], precision="fp32")
+    sc = SpaceCharge(nmesh_xyz=spec[1], precision="fp32", fields=fields)
     for _ in range(kicks):
         sc.apply_device(d_rp, d_q, spec[2], spec[6])
     sc.check()
     return d_rp.cpu().numpy()
 
 
-def _batch(beams, kicks=1, graph=False, odd=()):
-    b = BeamBatch(DEV)
+def _batch(beams, kicks=1, graph=False, odd=(), fields="spectral"):
+    b = BeamBatch(DEV, fields=fields)
     tensors = []
     for i, (rp, q, spec) in enumerate(beams):
         d_rp, d_q = _dev(rp, q, i in odd)
@@ -74,14 +74,15 @@ def _batch(beams, kicks=1, graph=False, odd=()):
     return b, [t[0].cpu().numpy() for t in tensors]
 
 
-@pytest.mark.parametrize("kicks,graph", [(1, False), (3, False), (3, True)])
-def test_batched_equals_alone(kicks, graph):
+@pytest.mark.parametrize("kicks,graph,fields", [(1, False, "spectral"), (3, False, "spectral"), (3, True, "spectral"),
+                                                (2, False, "difference"), (2, True, "difference")])
+def test_batched_equals_alone(kicks, graph, fields):
     beams = [(*_beam(i, s), s) for i, s in enumerate(SPECS)]
-    b, outs = _batch(beams, kicks, graph)
+    b, outs = _batch(beams, kicks, graph, fields=fields)
     b.check()
     assert b.launches == 15
     for (rp, q, spec), out in zip(beams, outs):
-        ref = _alone(rp, q, spec, kicks)
+        ref = _alone(rp, q, spec, kicks, fields=fields)
         assert np.array_equal(out, ref), spec
         assert not np.array_equal(out, rp)
 
