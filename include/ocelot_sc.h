@@ -76,6 +76,8 @@ int sc_read_status(const sc_plan* plan, void* ws, void* stream);
  * (sc.py:168), the field grids Ex/Ey/Ez (sc.py:195-200), all [nx][ny][nz];
  * the cell keys (sc.py:192) as uint32[n].  Grids are double for an SC_FP64
  * plan and float for SC_FP32.  Offsets do not depend on n except for keys.
+ * A kick of an SC_FP32_SPECTRAL_FIELDS plan leaves the potential out (its
+ * field octs do not need it) unless SC_PARAM_RECORD_FIELD is set.
  * SC_REGION_STATUS is the int that sc_read_status returns (the last kick's
  * status) and SC_REGION_FIRST_ERROR an int holding the first non-OK status of
  * any earlier kick since sc_workspace_init: a device-resident loop of many

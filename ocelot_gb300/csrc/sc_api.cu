@@ -611,7 +611,10 @@ int sc_kick(sc_plan* plan, void* ws_v, size_t ws_bytes, double* rp, int64_t ld, 
     mark(plan, 13, s);
     SC_CUDA(cudaStreamWaitEvent(s, plan->join, 0), "cudaStreamWaitEvent");  // join
     mark(plan, 6, s);
-    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s, qfix, CONV_REST, true), "convolve");
+    // the kick's field octs do not read the potential: with spectral fields it
+    // is produced only for the record-field mode
+    SC_CUDA(launch_convolve(p, L, ws, ws + L.qgrid, ws + L.phi, s, qfix, CONV_REST, true, p.record_field != 0),
+            "convolve");
     mark(plan, 7, s);
     SC_CUDA(launch_field_grids(p, L, ws, s), "field grids");
     mark(plan, 8, s);

@@ -228,7 +228,7 @@ cudaError_t launch_green_spectrum(const Plan& p, const Layout& L, char* ws, cuda
 enum ConvPart { CONV_ALL = 0, CONV_FORWARD = 1, CONV_REST = 2 };
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in,
                             void* phi_out, cudaStream_t s, const long long* qfix = nullptr, int part = CONV_ALL,
-                            bool fields = false);
+                            bool fields = false, bool want_phi = true);
 cudaError_t launch_field_grids(const Plan& p, const Layout& L, char* ws, cudaStream_t s);
 // kernels launch_convolve(CONV_ALL) launches for this plan
 int convolve_launches(const Plan& p);

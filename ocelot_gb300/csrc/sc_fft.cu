@@ -62,6 +62,7 @@ struct Spec {
     R* ex;                           // field grids [nx][ny][nz], zero on their last plane
     R* ey;
     R* ez;
+    int f0;                          // first output of the inverse passes: 0 with the potential, 1 without
 };
 template <typename R>
 __device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
@@ -321,7 +322,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zinv(const Cx<R>* __restrict__ 
                                                       const Cx<R>* __restrict__ twg, int NC,
                                                       const ScState* st, Spec<R> sp) {
     pdl_wait();
-    const int f = (int)blockIdx.z;
+    const int f = (int)blockIdx.z + sp.f0;
     const Cx<R>* src;
     R* out;
     const Cx<R>* dz;
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(PLANE_THREADS) k_yz_inv(const Cx<R>* __restric
                                                           const Cx<R>* __restrict__ twy, const ScState* st,
                                                           Spec<R> sp) {
     pdl_wait();
-    const int f = (int)blockIdx.y;
+    const int f = (int)blockIdx.y + sp.f0;
     const Cx<R>* src;
     R* out;
     const Cx<R>* dz;
@@ -631,10 +632,14 @@ static int optin_smem() {
 }
 
 // the spectral-field pointers of a plan's workspace (W2 == nullptr: none)
+// want_phi: the inverse passes also produce the potential (the kick's field
+// octs do not read it; an inspection or the record-field mode does)
 template <typename R>
-__host__ __device__ __forceinline__ Spec<R> spec_of(const Plan& p, const Layout& L, char* ws, bool fields) {
+__host__ __device__ __forceinline__ Spec<R> spec_of(const Plan& p, const Layout& L, char* ws, bool fields,
+                                                    bool want_phi = true) {
     Spec<R> sp = {};
     if (!(fields && p.spectral && sizeof(R) == 4)) return sp;
+    sp.f0 = want_phi ? 0 : 1;
     sp.W2 = reinterpret_cast<Cx<R>*>(ws + L.W2);
     sp.W3 = reinterpret_cast<Cx<R>*>(ws + L.W3);
     sp.dx = reinterpret_cast<const Cx<R>*>(ws + L.dt_x);
@@ -648,10 +653,10 @@ __host__ __device__ __forceinline__ Spec<R> spec_of(const Plan& p, const Layout&
 
 template <typename R>
 static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid, R* phi, const long long* qfix,
-                              cudaStream_t s, int part, bool fields) {
+                              cudaStream_t s, int part, bool fields, bool want_phi) {
     const ScState* st = reinterpret_cast<const ScState*>(ws + L.state);
     const int Kz = p.Mz / 2 + 1, Ky = p.My / 2 + 1;
-    const Spec<R> sp = spec_of<R>(p, L, ws, fields);
+    const Spec<R> sp = spec_of<R>(p, L, ws, fields, want_phi);
     const int nbuf = sp.W2 ? 3 : 2;  // line buffers of the x pass and the y inverse
     Cx<R>* W = reinterpret_cast<Cx<R>*>(ws + L.W);
     const R* G = reinterpret_cast<const R*>(ws + L.green);
@@ -685,7 +690,7 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     dim3 gx((Kz + tkx - 1) / tkx, p.My);
     if ((e = set_smem(k_xconv<R>, smx))) return e;
     launch(k_xconv<R>, gx, FFT_THREADS, smx, s, W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st, sp);
-    const int nout = sp.W2 ? 4 : 1;  // the potential, then Ex, Ey, Ez
+    const int nout = sp.W2 ? 4 - sp.f0 : 1;  // [the potential,] Ex, Ey, Ez
     if (plane) {
         if ((e = set_smem(k_yz_inv<R>, smp))) return e;
         launch(k_yz_inv<R>, dim3(p.nx, nout), PLANE_THREADS, smp, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy,
@@ -726,12 +731,12 @@ cudaError_t prepare_fft_kernels(const Plan& p) {
 }
 
 cudaError_t launch_convolve(const Plan& p, const Layout& L, char* ws, const void* qgrid_in, void* phi_out,
-                            cudaStream_t s, const long long* qfix, int part, bool fields) {
+                            cudaStream_t s, const long long* qfix, int part, bool fields, bool want_phi) {
     if (p.prec == SC_FP64)
         return convolve_t<double>(p, L, ws, static_cast<double*>(const_cast<void*>(qgrid_in)),
-                                  static_cast<double*>(phi_out), nullptr, s, part, false);
+                                  static_cast<double*>(phi_out), nullptr, s, part, false, true);
     return convolve_t<float>(p, L, ws, static_cast<float*>(const_cast<void*>(qgrid_in)), static_cast<float*>(phi_out),
-                             qfix, s, part, fields);
+                             qfix, s, part, fields, want_phi);
 }
 
 template <typename R>
@@ -823,9 +828,9 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_zinv(const BatchBeam* __restri
                                                        const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_FFT_ZI)
-    const Spec<float> sp = spec_of<float>(p, L, ws, true);
-    const int f = vb.y / p.nx;
-    const VBlk v = {vb.x, vb.y - f * p.nx, vb.nx, p.nx};
+    const Spec<float> sp = spec_of<float>(p, L, ws, true, false);
+    const int f = vb.y / p.nx + sp.f0;
+    const VBlk v = {vb.x, vb.y - (f - sp.f0) * p.nx, vb.nx, p.nx};
     const Cx<float>* src;
     float* out;
     const Cx<float>* dz;
@@ -867,7 +872,7 @@ void batch_fft_tiling(BatchBeam& B, size_t smem[3]) {
     B.gx[BS_FFT_YI] = B.gx[BS_FFT_Y];
     B.gy[BS_FFT_YI] = p.nx * (p.spectral ? 2 : 1);
     B.gx[BS_FFT_ZI] = B.gx[BS_FFT_Z];
-    B.gy[BS_FFT_ZI] = p.nx * (p.spectral ? 4 : 1);
+    B.gy[BS_FFT_ZI] = p.nx * (p.spectral ? 3 : 1);  // spectral fields: Ex, Ey, Ez (no potential)
     B.gx[BS_FIELD] = p.ny;
     B.gy[BS_FIELD] = p.nx;
     smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.fft_nc * fft_ls(p.Mz));
