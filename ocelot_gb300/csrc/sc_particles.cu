@@ -1059,13 +1059,33 @@ __global__ void __launch_bounds__(PT) k_extent64(const double* __restrict__ xp, 
     if (arrive_last(&st->done_extent, gridDim.x)) mesh_finalize(part, gridDim.x, kp, st, -1.0);
 }
 
-// Rotated position (z scaled by gamma0) of particle i to ~1e-11 of a cell:
-// each lab coordinate is its FP64 MAD value plus a small correction computed
-// in FP32 (x - (px/E) tau, and z = -tau + tau (1 - pz/E) with
-// 1 - pz/E = (m^2 + pT^2) / ((E + pz) E), free of cancellation), rotated in
-// FP64.  No FP64 division or square root.
+// Rotated position (z scaled by gamma0) of particle i with the FP64 form's
+// operations, for the few particles whose FP32 position is too close to a
+// cell face or to the extent to decide.  (Forming only the lab position's
+// corrections in FP32 is not enough: at a few MeV the correction of z is a
+// sizeable fraction of a cell, and its FP32 rounding of ~1e-8 cells put a
+// particle 1.4e-8 cells from a face in the neighbouring cell.)  The result
+// equals the FP64 form's position up to the rounding of the frame (T, gamma0),
+// so the keys agree except for a particle within ~1e-14 cells of a face.
 __device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t ld, int64_t i, const KickParams& kp,
                                          const double (&T)[3][3], double g0, double v[3]) {
+    // the FP64 form's operations: xxstg_2_xp_mad, the BLAS-order rotation
+    // and the gamma0 product (k_frame64, k_extent64)
+    double r[6], xp[6];
+    for (int k = 0; k < 6; ++k) r[k] = rp[k * ld + i];
+    mad_to_cart64(r, kp, xp);
+    for (int j = 0; j < 3; ++j) v[j] = dot3_blas(xp[0], xp[1], xp[2], T[0][j], T[1][j], T[2][j]);
+    v[2] = __dmul_rn(v[2], g0);
+}
+// A cheaper estimate of the same position, to ~1e-8 of a cell at a few MeV
+// (~1e-11 at 100 MeV): each lab coordinate is its FP64 MAD value plus a small
+// correction computed in FP32 (x - (px/E) tau, and z = -tau + tau (1 - pz/E)
+// with 1 - pz/E = (m^2 + pT^2) / ((E + pz) E), free of cancellation), rotated
+// in FP64.  Only for the near-face particles of a keys block beyond the
+// KEYS_FINE that its list takes, inside the particle loop, where the FP64
+// transform's registers would slow every particle.
+__device__ __forceinline__ void xyz_fine32(const double* __restrict__ rp, int64_t ld, int64_t i,
+                                           const KickParams& kp, const double (&T)[3][3], double g0, double v[3]) {
     const double x = rp[i], y = rp[2 * ld + i], tau = rp[4 * ld + i];
     float px, py, pz, E;
     mom32(d2f(rp[ld + i]), d2f(rp[3 * ld + i]), d2f(rp[5 * ld + i]), kp, px, py, pz, E);
@@ -1080,7 +1100,7 @@ __device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t 
 
 // FP32 extent.  Pass 1 computes the rotated positions in FP32, stores them and
 // reduces FP32 extremes and charge moments.  Pass 2 re-walks the block's
-// particles and evaluates to ~1e-11 of a cell (xyz_fine) every particle whose
+// particles and evaluates in FP64 (xyz_fine) every particle whose
 // FP32 coordinate lies within a rounding margin of the block's FP32 extreme:
 // the FP64 extreme of the block is among them, so the mesh step equals the
 // FP64 form's.
@@ -1528,12 +1548,16 @@ __device__ __forceinline__ long long to_fixed(double q, int S) {
     return (b >> 63) ? -(long long)v : (long long)v;
 }
 
-constexpr int KEYS_FINE = 256;
+constexpr int KEYS_FINE = 1024;
 
 // FP32 grid coordinates with an explicit rounding margin; a particle whose
-// coordinate lies within the margin of a cell face is recomputed to ~1e-11 of
-// a cell (xyz_fine), so its key equals the FP64 form's key unless it lies
-// within ~1e-11 of the face.
+// coordinate lies within the margin of a cell face is recomputed with the
+// FP64 form's operations (xyz_fine, then X / step - X_off as k_keys64), so
+// its key equals the FP64 form's key unless it lies within the rounding of
+// the frame (~1e-14 cells) of the face.  A block lists up to KEYS_FINE such
+// particles (about 0.4% of a beam's particles are near a face; a block holds
+// a few thousand); beyond that, in degenerate beams only, the rest take the
+// cheaper estimate xyz_fine32.
 // rp == nullptr (el_field entry) keeps the FP32 result.
 // qfix != nullptr: the deposit -- each charge, in units of 2^-S, is added to
 // its cell with a 64-bit integer atomic.  Integer addition is exact and
@@ -1594,10 +1618,10 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
             double xv[3];
-            xyz_fine(rp, ld, i, kp, T, st->gamma0, xv);
+            xyz_fine32(rp, ld, i, kp, T, st->gamma0, xv);
             double e[3];
-            for (int j = 0; j < 3; ++j) {
-                e[j] = fma(xv[j], st->isteps[j], -st->xoff[j]);
+            for (int j = 0; j < 3; ++j) {  // the FP64 form's grid coordinate (k_keys64)
+                e[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
                 g[j] = (float)e[j];
             }
             bad |= !key_of(floor(e[0]) + 1, floor(e[1]) + 1, floor(e[2]) + 1, kp, key);
@@ -1629,7 +1653,7 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
         double xv[3];
         xyz_fine(rp, ld, i, kp, T, st->gamma0, xv);
         double g[3];
-        for (int j = 0; j < 3; ++j) g[j] = fma(xv[j], st->isteps[j], -st->xoff[j]);
+        for (int j = 0; j < 3; ++j) g[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
         uint32_t key;
         bad |= !key_of(floor(g[0]) + 1, floor(g[1]) + 1, floor(g[2]) + 1, kp, key);
         keys[i] = key;
