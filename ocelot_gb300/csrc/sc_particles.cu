@@ -1084,19 +1084,32 @@ __device__ __forceinline__ void xyz_fine(const double* __restrict__ rp, int64_t 
 // in FP64.  Only for the near-face particles of a keys block beyond the
 // KEYS_FINE that its list takes, inside the particle loop, where the FP64
 // transform's registers would slow every particle.
+// err (optional): a bound on |v - xyz_fine| per axis -- 2^-18 of each FP32
+// correction (a few roundings of ~2^-24 each, the approximate reciprocals'
+// ~2^-22, and margin) carried through the rotation.
 __device__ __forceinline__ void xyz_fine32(const double* __restrict__ rp, int64_t ld, int64_t i,
-                                           const KickParams& kp, const double (&T)[3][3], double g0, double v[3]) {
+                                           const KickParams& kp, const double (&T)[3][3], double g0, double v[3],
+                                           double* err = nullptr) {
     const double x = rp[i], y = rp[2 * ld + i], tau = rp[4 * ld + i];
     float px, py, pz, E;
     mom32(d2f(rp[ld + i]), d2f(rp[3 * ld + i]), d2f(rp[5 * ld + i]), kp, px, py, pz, E);
     const float tf = d2f(tau), iE = rcpf(E);
-    const double l0 = x - f2d(px * iE * tf);
-    const double l1 = y - f2d(py * iE * tf);
+    const float c0 = px * iE * tf, c1 = py * iE * tf;
+    const double l0 = x - f2d(c0);
+    const double l1 = y - f2d(c1);
     const float k = (kp.m2_f + fmaf(px, px, py * py)) * rcpf((E + pz) * E);
-    const double l2 = -tau + f2d(tf * k);
+    const float c2 = tf * k;
+    const double l2 = -tau + f2d(c2);
     for (int j = 0; j < 3; ++j) v[j] = fma(l2, T[2][j], fma(l1, T[1][j], l0 * T[0][j]));
     v[2] *= g0;
+    if (err) {
+        const double e0 = fabs((double)c0), e1 = fabs((double)c1), e2 = fabs((double)c2);
+        for (int j = 0; j < 3; ++j)
+            err[j] = ldexp(fma(e2, fabs(T[2][j]), fma(e1, fabs(T[1][j]), e0 * fabs(T[0][j]))), -18) *
+                     (j == 2 ? g0 : 1.0);
+    }
 }
+
 
 // FP32 extent.  Pass 1 computes the rotated positions in FP32, stores them and
 // reduces FP32 extremes and charge moments.  Pass 2 re-walks the block's
@@ -1548,16 +1561,42 @@ __device__ __forceinline__ long long to_fixed(double q, int S) {
     return (b >> 63) ? -(long long)v : (long long)v;
 }
 
+// NGP key of a near-face particle, equal to the FP64 form's: the grid
+// coordinate from the cheap estimate when every axis is farther from a face
+// than the estimate's error bound (plus 1e-12 cells for the FP64 roundings),
+// else from the FP64 form's operations.  Returns false outside the mesh.
+__device__ __forceinline__ bool key_fine(const double* __restrict__ rp, int64_t ld, int64_t i, const KickParams& kp,
+                                         const ScState* st, uint32_t& key, float (&gf)[3]) {
+    double T[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
+    double xv[3], err[3], g[3];
+    xyz_fine32(rp, ld, i, kp, T, st->gamma0, xv, err);
+    bool sure = true;
+    for (int j = 0; j < 3; ++j) {  // the FP64 form's grid coordinate (k_keys64)
+        g[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
+        const double d = fabs(g[j] - rint(g[j]));
+        sure &= d > fma(err[j], st->isteps[j], 1e-12);
+    }
+    if (!sure) {
+        xyz_fine(rp, ld, i, kp, T, st->gamma0, xv);
+        for (int j = 0; j < 3; ++j) g[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
+    }
+    for (int j = 0; j < 3; ++j) gf[j] = (float)g[j];
+    return key_of(floor(g[0]) + 1, floor(g[1]) + 1, floor(g[2]) + 1, kp, key);
+}
+
 constexpr int KEYS_FINE = 1024;
 
 // FP32 grid coordinates with an explicit rounding margin; a particle whose
 // coordinate lies within the margin of a cell face is recomputed with the
 // FP64 form's operations (xyz_fine, then X / step - X_off as k_keys64), so
 // its key equals the FP64 form's key unless it lies within the rounding of
-// the frame (~1e-14 cells) of the face.  A block lists up to KEYS_FINE such
-// particles (about 0.4% of a beam's particles are near a face; a block holds
-// a few thousand); beyond that, in degenerate beams only, the rest take the
-// cheaper estimate xyz_fine32.
+// the frame (~1e-14 cells) of the face (key_fine: the cheap estimate
+// xyz_fine32 decides unless it lies within its error bound of a face).  A
+// block lists up to KEYS_FINE such particles (about 0.4% of a beam's
+// particles are near a face; a block holds a few thousand); beyond that, in
+// degenerate beams only, the rest take the cheap estimate alone.
 // rp == nullptr (el_field entry) keeps the FP32 result.
 // qfix != nullptr: the deposit -- each charge, in units of 2^-S, is added to
 // its cell with a 64-bit integer atomic.  Integer addition is exact and
@@ -1647,15 +1686,9 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
     const int nf = s_nfine < KEYS_FINE ? s_nfine : KEYS_FINE;
     for (int e = threadIdx.x; e < nf; e += blockDim.x) {
         const int64_t i = s_fine[e];
-        double T[3][3];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
-        double xv[3];
-        xyz_fine(rp, ld, i, kp, T, st->gamma0, xv);
-        double g[3];
-        for (int j = 0; j < 3; ++j) g[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
         uint32_t key;
-        bad |= !key_of(floor(g[0]) + 1, floor(g[1]) + 1, floor(g[2]) + 1, kp, key);
+        float gf[3];
+        bad |= !key_fine(rp, ld, i, kp, st, key, gf);
         keys[i] = key;
         if (qfix && SC_IDX_OK(st, 13, key, (long long)kp.nx * kp.ny * kp.nz))
             atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
