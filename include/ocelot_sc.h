@@ -350,6 +350,13 @@ int sc_kick_launches(const sc_plan* plan);
  *     particle (SC_REGION_FIELD), for error measurements; the FP32 form then
  *     runs its direct-access kick loop (same arithmetic, same particles). */
 #define SC_PARAM_RECORD_FIELD 1
+/*   SC_PARAM_FFT_PLANE_FWD / SC_PARAM_FFT_PLANE_INV: 1 (default) runs the z
+ *     and y transforms of one x plane in one block where the plane fits
+ *     shared memory (one launch per direction, 64 blocks on a 64^3 mesh); 0
+ *     runs them as separate passes of many smaller blocks.  The lines go
+ *     through the same transform code either way: identical results. */
+#define SC_PARAM_FFT_PLANE_FWD 2
+#define SC_PARAM_FFT_PLANE_INV 3
 #define SC_KICK_NVARIANTS 14
 int sc_plan_set_param(sc_plan* plan, int param, int value);
 int sc_plan_get_param(const sc_plan* plan, int param, int* value);

@@ -32,6 +32,8 @@ SC_NSTAGES = 11
 # launch-shape parameters of a plan (sc_plan_set_param)
 SC_PARAM_KICK_VARIANT = 0
 SC_PARAM_RECORD_FIELD = 1
+SC_PARAM_FFT_PLANE_FWD = 2
+SC_PARAM_FFT_PLANE_INV = 3
 SC_KICK_NVARIANTS = 14
 
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds

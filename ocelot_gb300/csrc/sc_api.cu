@@ -343,6 +343,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     p.part_blocks = p.sm_count * 4;
     for (int k = 0; k < 3; ++k) p.wait_limit[k] = MBAR_WAIT_LIMIT;
     p.kick_variant = default_kick_variant();
+    p.fft_plane_fwd = p.fft_plane_inv = 1;
     // everything that is not a stream operation happens here, so that kicks
     // can be recorded in a CUDA graph
     SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
@@ -441,6 +442,11 @@ int sc_plan_set_param(sc_plan* plan, int param, int value) {
             if (value != 0 && value != 1) return fail(SC_ERR_ARG, "record field must be 0 or 1");
             plan->p.record_field = value;
             return SC_OK;
+        case SC_PARAM_FFT_PLANE_FWD:
+        case SC_PARAM_FFT_PLANE_INV:
+            if (value != 0 && value != 1) return fail(SC_ERR_ARG, "FFT plane parameter must be 0 or 1");
+            (param == SC_PARAM_FFT_PLANE_FWD ? plan->p.fft_plane_fwd : plan->p.fft_plane_inv) = value;
+            return SC_OK;
         default: return fail(SC_ERR_ARG, "unknown plan parameter %d", param);
     }
 }
@@ -450,6 +456,8 @@ int sc_plan_get_param(const sc_plan* plan, int param, int* value) {
     switch (param) {
         case SC_PARAM_KICK_VARIANT: *value = plan->p.kick_variant; return SC_OK;
         case SC_PARAM_RECORD_FIELD: *value = plan->p.record_field; return SC_OK;
+        case SC_PARAM_FFT_PLANE_FWD: *value = plan->p.fft_plane_fwd; return SC_OK;
+        case SC_PARAM_FFT_PLANE_INV: *value = plan->p.fft_plane_inv; return SC_OK;
         default: return fail(SC_ERR_ARG, "unknown plan parameter %d", param);
     }
 }

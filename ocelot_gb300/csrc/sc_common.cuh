@@ -169,6 +169,8 @@ struct Plan {
     unsigned wait_limit[3];  // KickParams::wait_limit of this plan's kicks
     int kick_variant;        // tiling of the FP32 gather + kick (sc_particles.cu, SC_KICK_VARIANTS)
     int record_field;        // the kick also stores the field at each particle (SC_REGION_FIELD)
+    int fft_plane_fwd;       // 1: plane-fused z + y forward passes where the plane fits, 0: separate passes
+    int fft_plane_inv;       // 1: plane-fused y + z inverse passes where the plane fits, 0: separate passes
 };
 // tile, tile buffers, particles per thread and blocks per SM of kick variant v (0 if v is out of range)
 int kick_variant_info(int v, int* tile, int* stages, int* ppt, int* minb);

@@ -620,9 +620,14 @@ __global__ void __launch_bounds__(PLANE_THREADS) k_yz_inv(const Cx<R>* __restric
 }
 
 static int optin_smem();
+// the plane-fused passes are used where the plane fits shared memory and the
+// plan's parameters (SC_PARAM_FFT_PLANE_FWD / _INV) allow them
+static bool plane_ok(const Plan& p) {
+    return p.prec == SC_FP64 ? plane_fits<double>(p, optin_smem()) : plane_fits<float>(p, optin_smem());
+}
 int convolve_launches(const Plan& p) {
-    const bool plane = p.prec == SC_FP64 ? plane_fits<double>(p, optin_smem()) : plane_fits<float>(p, optin_smem());
-    return plane ? 3 : 5;
+    const bool plane = plane_ok(p);
+    return (plane && p.fft_plane_fwd ? 1 : 2) + 1 + (plane && p.fft_plane_inv ? 1 : 2);
 }
 
 static int optin_smem() {
@@ -675,8 +680,9 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     dim3 gyi((Kz + tkyi - 1) / tkyi, p.nx, sp.W2 ? 2 : 1);
     static const int optin = optin_smem();
     const bool plane = plane_fits<R>(p, optin);
+    const bool plane_fwd = plane && p.fft_plane_fwd, plane_inv = plane && p.fft_plane_inv;
     const size_t smp = plane_smem<R>(p);
-    if (plane && part != CONV_REST) {
+    if (plane_fwd && part != CONV_REST) {
         if ((e = set_smem(k_zy_fwd<R>, smp))) return e;
         launch(k_zy_fwd<R>, p.nx, PLANE_THREADS, smp, s, qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy, st);
     } else if (part != CONV_REST) {
@@ -691,7 +697,7 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     if ((e = set_smem(k_xconv<R>, smx))) return e;
     launch(k_xconv<R>, gx, FFT_THREADS, smx, s, W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st, sp);
     const int nout = sp.W2 ? 4 - sp.f0 : 1;  // [the potential,] Ex, Ey, Ez
-    if (plane) {
+    if (plane_inv) {
         if ((e = set_smem(k_yz_inv<R>, smp))) return e;
         launch(k_yz_inv<R>, dim3(p.nx, nout), PLANE_THREADS, smp, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, p.ry, twz, twy,
                st, sp);

@@ -27,10 +27,12 @@ TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_ta
 
 # parameter -> candidate values (the plan's launch-shape knobs)
 def candidates():
-    return {N.SC_PARAM_KICK_VARIANT: list(range(N.SC_KICK_NVARIANTS))}
+    return {N.SC_PARAM_KICK_VARIANT: list(range(N.SC_KICK_NVARIANTS)),
+            N.SC_PARAM_FFT_PLANE_FWD: [1, 0], N.SC_PARAM_FFT_PLANE_INV: [1, 0]}
 
 
-PARAM_NAMES = {N.SC_PARAM_KICK_VARIANT: "kick_variant"}
+PARAM_NAMES = {N.SC_PARAM_KICK_VARIANT: "kick_variant", N.SC_PARAM_FFT_PLANE_FWD: "fft_plane_fwd",
+               N.SC_PARAM_FFT_PLANE_INV: "fft_plane_inv"}
 _NAME_TO_PARAM = {v: k for k, v in PARAM_NAMES.items()}
 
 _lock = threading.Lock()

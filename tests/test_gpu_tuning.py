@@ -59,3 +59,26 @@ def test_bad_variant_is_refused():
     eng = Engine((16, 16, 16), "fp32", DEV, tuned=False)
     with pytest.raises(ValueError, match=r"\[sc error 1\]"):
         eng.set_param(N.SC_PARAM_KICK_VARIANT, N.SC_KICK_NVARIANTS)
+
+
+@pytest.mark.parametrize("precision,fields", [("fp32", "spectral"), ("fp32", "difference"), ("fp64", "difference")])
+def test_fft_plane_parameters_give_the_same_bits(precision, fields):
+    """Plane-fused or separate FFT passes, forward and inverse: the same lines
+    through the same transform code, so the kick is bit-identical."""
+    from ocelot_gb300.sc import plan_mode
+    n, mesh = 100_001, (48, 48, 48)
+    rp, q = sc_oracle.gaussian_beam(n, 23, charge=1e-9)
+    r0 = torch.from_numpy(rp).to(DEV)
+    dq = torch.from_numpy(q).to(DEV)
+    d = torch.zeros((6, n + 1), dtype=torch.float64, device=DEV)[:, :n]
+    eng = Engine(mesh, precision, DEV, plan_mode(precision, fields=fields), tuned=False)
+    outs = []
+    for fwd, inv in ((1, 1), (0, 1), (1, 0), (0, 0)):
+        eng.set_param(N.SC_PARAM_FFT_PLANE_FWD, fwd)
+        eng.set_param(N.SC_PARAM_FFT_PLANE_INV, inv)
+        d.copy_(r0)
+        eng.kick(d, dq, n, 0.130, 0.1)
+        eng.check_status()
+        outs.append(d.cpu().numpy())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
