@@ -54,17 +54,32 @@ PhysConst phys_const() {
     return c;
 }
 
+// The smallest length 2^k or 3 * 2^k (8 .. 512) that holds the linear
+// convolution of n cells (M >= 2n - 1): 96 cells take 192 rather than 256.
 int choose_fft_length(int n) {
     const int need = 2 * n - 1;
+    int best = 0;
     for (int L = 8; L <= 512; L *= 2)
-        if (L >= need) return L;
-    return 0;
+        if (L >= need) {
+            best = L;
+            break;
+        }
+    for (int L = 12; L <= 384; L *= 2)
+        if (L >= need) {
+            if (!best || L < best) best = L;
+            break;
+        }
+    return best;
 }
 
 bool make_radix_plan(int L, RadixPlan* p) {
     p->L = L;
     p->nst = 0;
     int rem = L;
+    if (rem % 3 == 0) {  // one radix-3 stage first (as plan_radix)
+        p->r[p->nst++] = 3;
+        rem /= 3;
+    }
     while (rem % 8 == 0 && rem > 1) {
         if (p->nst >= MAX_STAGES) return false;
         p->r[p->nst++] = 8;

@@ -1,4 +1,4 @@
-// Batched mixed-radix (2/4/8) Stockham FFT of lines held in shared memory.
+// Batched mixed-radix (3/2/4/8) Stockham FFT of lines held in shared memory.
 //
 // The lines of one thread block live in shared memory, line l at a + l*ls,
 // elements contiguous.  Each stage reads radix-r butterfly inputs with stride
@@ -27,6 +27,19 @@ __device__ __forceinline__ void dft4(C& a0, C& a1, C& a2, C& a3) {
     a2 = csub(t0, t2);
     a1 = cadd(t1, t3);
     a3 = csub(t1, t3);
+}
+
+// 3-point DFT: y_k = sum_t a_t w^(t k), w = exp(-2 pi i / 3) (forward) or its
+// conjugate (inverse): y0 = a + (b + c), y1,2 = a - (b + c)/2 -/+ i (sqrt(3)/2)(b - c)
+template <typename R, bool INV>
+__device__ __forceinline__ void dft3(Cx<R>& a, Cx<R>& b, Cx<R>& c) {
+    const R s = INV ? (R)-0.86602540378443864676 : (R)0.86602540378443864676;
+    const Cx<R> t = cadd(b, c), d = csub(b, c);
+    const Cx<R> m = cx<R>(a.x - (R)0.5 * t.x, a.y - (R)0.5 * t.y);
+    const Cx<R> r = cx<R>(s * d.y, -s * d.x);  // -i s d
+    a = cadd(a, t);
+    b = cadd(m, r);
+    c = csub(m, r);
 }
 
 template <typename R, bool INV>
@@ -75,6 +88,7 @@ __device__ __forceinline__ void stockham_stage(const Cx<R>* __restrict__ a, Cx<R
             }
         }
         if (RAD == 2) dft2<Cx<R>, INV>(v[0], v[1]);
+        else if (RAD == 3) dft3<R, INV>(v[0], v[1], v[2]);
         else if (RAD == 4) dft4<Cx<R>, INV>(v[0], v[1], v[2], v[3]);
         else dft8<R, INV>(v);
         const int out = (j - k) * RAD + k;
@@ -85,11 +99,17 @@ __device__ __forceinline__ void stockham_stage(const Cx<R>* __restrict__ a, Cx<R
 
 // The same stages with the line length known at compile time: the radix of
 // each stage, the butterfly count and the twiddle stride are constants, so
-// the index arithmetic reduces to shifts and masks.  The plan is the greedy
-// one of make_radix_plan (radix 8 while it divides, then 4, then 2) and the
-// arithmetic is that of stockham_stage, so results are identical.
+// the index arithmetic reduces to shifts, masks and multiplications.  The
+// plan is the one of make_radix_plan (for lengths 3 * 2^k one radix-3 stage,
+// then radix 8 while it divides, then 4, then 2) and the arithmetic is that
+// of stockham_stage, so results are identical.
 constexpr int plan_radix(int L, int s) {
     int rem = L, st = 0;
+    if (rem % 3 == 0) {
+        if (st == s) return 3;
+        rem /= 3;
+        ++st;
+    }
     while (rem % 8 == 0 && rem > 1) {
         if (st == s) return 8;
         rem /= 8;
@@ -139,6 +159,7 @@ __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx
             }
         }
         if (RAD == 2) dft2<Cx<R>, INV>(v[0], v[1]);
+        else if (RAD == 3) dft3<R, INV>(v[0], v[1], v[2]);
         else if (RAD == 4) dft4<Cx<R>, INV>(v[0], v[1], v[2], v[3]);
         else dft8<R, INV>(v);
         const int out = (j - k) * RAD + k;
@@ -167,7 +188,13 @@ template <typename R, bool INV>
 __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan& rp, const Cx<R>* tw) {
     switch (rp.L) {  // the padded lengths of meshes up to 256 per axis
         case 8: return fft_stages_c<R, INV, 8, 0, 1>(a, b, ls, nl, tw);
+        case 12: return fft_stages_c<R, INV, 12, 0, 1>(a, b, ls, nl, tw);
         case 16: return fft_stages_c<R, INV, 16, 0, 1>(a, b, ls, nl, tw);
+        case 24: return fft_stages_c<R, INV, 24, 0, 1>(a, b, ls, nl, tw);
+        case 48: return fft_stages_c<R, INV, 48, 0, 1>(a, b, ls, nl, tw);
+        case 96: return fft_stages_c<R, INV, 96, 0, 1>(a, b, ls, nl, tw);
+        case 192: return fft_stages_c<R, INV, 192, 0, 1>(a, b, ls, nl, tw);
+        case 384: return fft_stages_c<R, INV, 384, 0, 1>(a, b, ls, nl, tw);
         case 32: return fft_stages_c<R, INV, 32, 0, 1>(a, b, ls, nl, tw);
         case 64: return fft_stages_c<R, INV, 64, 0, 1>(a, b, ls, nl, tw);
         case 128: return fft_stages_c<R, INV, 128, 0, 1>(a, b, ls, nl, tw);
@@ -180,6 +207,7 @@ __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan&
         const int r = rp.r[s];
         if (r == 8) stockham_stage<R, INV, 8>(a, b, rp.L, ls, nl, Ns, tw);
         else if (r == 4) stockham_stage<R, INV, 4>(a, b, rp.L, ls, nl, Ns, tw);
+        else if (r == 3) stockham_stage<R, INV, 3>(a, b, rp.L, ls, nl, Ns, tw);
         else stockham_stage<R, INV, 2>(a, b, rp.L, ls, nl, Ns, tw);
         __syncthreads();
         Cx<R>* t = a;

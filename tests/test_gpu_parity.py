@@ -437,3 +437,25 @@ def test_tmap_matches_oracle():
     d = torch.from_numpy(rp).to(DEV)
     tmap_apply(R, B, d)
     assert np.abs(d.cpu().numpy() - ref).max() <= 1e-15 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("mesh", [[24, 40, 48], [96, 12, 20], [48, 48, 48]])
+def test_radix3_lengths_match_the_oracle(mesh):
+    """Meshes whose padded FFT length is 3 * 2^k (48 for 24, 96 for 48, 192 for
+    96 cells): the potential within 1e-12 (FP64) and 1e-6 (FP32) of the
+    oracle's (numpy FFTs of 2N-1), and an FP64 kick within 1e-10."""
+    rng = np.random.default_rng(5)
+    q = rng.random(mesh) * 1e-15
+    steps = (3e-6, 4e-6, 1e-3)
+    ref = sc_oracle.potential(q, steps)
+    for prec, tol in (("fp64", 1e-12), ("fp32", 1e-6)):
+        sc = SpaceCharge(nmesh_xyz=mesh, precision=prec)
+        assert rel(sc.potential(q, steps), ref) < tol, prec
+    assert SpaceCharge(nmesh_xyz=mesh).engine().fft_shape() == tuple(
+        {12: 24, 20: 48, 24: 48, 40: 96, 48: 96, 96: 192}[m] for m in mesh)
+    rp, q2 = sc_oracle.gaussian_beam(30_000, 7)
+    out = rp.copy()
+    sc_oracle.sc_apply(out, q2, 0.130, 0.1, mesh)
+    pa = make_pa(rp, q2, 0.130)
+    SpaceCharge(nmesh_xyz=mesh).apply(pa, 0.1)
+    assert rel_rows(pa.rparticles, out) < 1e-10
