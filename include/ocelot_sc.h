@@ -357,7 +357,7 @@ int sc_kick_launches(const sc_plan* plan);
  *     through the same transform code either way: identical results. */
 #define SC_PARAM_FFT_PLANE_FWD 2
 #define SC_PARAM_FFT_PLANE_INV 3
-#define SC_KICK_NVARIANTS 14
+#define SC_KICK_NVARIANTS 16
 int sc_plan_set_param(sc_plan* plan, int param, int value);
 int sc_plan_get_param(const sc_plan* plan, int param, int* value);
 /* Tile (particles), tile buffers, particles per thread and blocks per SM of a

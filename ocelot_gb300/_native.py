@@ -34,7 +34,7 @@ SC_PARAM_KICK_VARIANT = 0
 SC_PARAM_RECORD_FIELD = 1
 SC_PARAM_FFT_PLANE_FWD = 2
 SC_PARAM_FFT_PLANE_INV = 3
-SC_KICK_NVARIANTS = 14
+SC_KICK_NVARIANTS = 16
 
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
 SC_WAIT_FRAME = 0

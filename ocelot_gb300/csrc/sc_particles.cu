@@ -2252,6 +2252,10 @@ __device__ __forceinline__ void kick32_async_body(double* __restrict__ rp, const
     X(11, 2, 6)                   \
     X(12, 6, 3)                   \
     X(13, 3, 4)
+// more bulk-copy tilings (indices after the barrier-free ones)
+#define SC_KICK_VARIANTS_B(X) \
+    X(14, 256, 3, 1, 6)       \
+    X(15, 256, 2, 1, 6)
 
 // the default: 256-particle tiles, one particle per thread, 4 blocks per SM
 // (measured fastest from 1M particles up on 48^3 to 128x128x256 meshes)
@@ -2404,11 +2408,12 @@ static const KickVariant kKickVariants[] = {
     {k_kick32_tma<T, S, P, M>, kb_kick32<T, S, P, M>, T, S, P, M, KickTiling<T, S, P>::threads,                  \
      KickTiling<T, S, P>::smem, false},
     SC_KICK_VARIANTS(SC_KV)
-#undef SC_KV
 #define SC_KA(i, S, M) \
     {k_kick32_async<S, M>, kb_kick32_async<S, M>, 32, S, 1, M, PT, (size_t)S * 6 * PT * sizeof(double), true},
     SC_KICK_ASYNC_VARIANTS(SC_KA)
 #undef SC_KA
+    SC_KICK_VARIANTS_B(SC_KV)
+#undef SC_KV
 };
 constexpr int kNumKickVariants = (int)(sizeof(kKickVariants) / sizeof(kKickVariants[0]));
 static_assert(KickTiling<256, 3, 1>::threads == PT, "the default kick tiling has PT threads");

@@ -4,8 +4,8 @@ The plan's launch-shape parameters (``sc_plan_set_param``) change how the
 work is cut into blocks and tiles, never the arithmetic: every candidate must
 give bit-identical particles, and the tuner checks that before it times
 anything.  For one (form, mesh, N) it kicks a seeded Gaussian beam on the
-GPU with each candidate, times the kicks with CUDA events (L2 flushed before
-each), and keeps the fastest.  Results go to a small JSON table -- by
+GPU with each candidate, times the stages the candidate changes with the
+library's stage events (L2 flushed before each kick), and keeps the fastest.  Results go to a small JSON table -- by
 default ``tuning_table.json`` beside this module, or the file named by
 ``OCELOT_SC_TUNING`` -- that ``Engine`` reads: before a kick of N particles
 it applies the entry of its form and mesh whose particle count is nearest to
@@ -33,6 +33,11 @@ def candidates():
 
 PARAM_NAMES = {N.SC_PARAM_KICK_VARIANT: "kick_variant", N.SC_PARAM_FFT_PLANE_FWD: "fft_plane_fwd",
                N.SC_PARAM_FFT_PLANE_INV: "fft_plane_inv"}
+# the stages (sc_profile_read) each parameter changes: a candidate is timed by
+# the sum of these stage times, which a few-microsecond difference does not
+# drown in the rest of the kick
+PARAM_STAGES = {N.SC_PARAM_KICK_VARIANT: ("kick",), N.SC_PARAM_FFT_PLANE_FWD: ("convolve", "join_wait"),
+                N.SC_PARAM_FFT_PLANE_INV: ("convolve", "field")}
 _NAME_TO_PARAM = {v: k for k, v in PARAM_NAMES.items()}
 
 _lock = threading.Lock()
@@ -105,8 +110,9 @@ def _beam(n: int, device, seed: int = 1):
 def tune(shape, n: int, precision: str = "fp32", device=None, energy_gev: float = 0.130, zstep: float = 0.1,
          reps: int = 5, warmup: int = 2, save: bool = False, path: str | None = None) -> dict:
     """Time every candidate of every parameter (one parameter at a time, the
-    others at their current best) on a seeded beam of n particles; returns
-    {"params": best, "us": {param name: {value: us per kick}}, "identical": True}.
+    others at their current best) on a seeded beam of n particles, by the
+    stages the parameter changes (library stage events); returns
+    {"params": best, "us": {param name: {value: us of those stages}}, "identical": True}.
     Raises if a candidate changes a single bit of the result."""
     import torch
     from .sc import Engine
@@ -118,7 +124,7 @@ def tune(shape, n: int, precision: str = "fp32", device=None, energy_gev: float 
     flush_w = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def kick_once():
+    def kick_once(stages=None):
         rp.copy_(rp0)
         flush_w.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -126,7 +132,10 @@ def tune(shape, n: int, precision: str = "fp32", device=None, energy_gev: float 
         eng.kick(rp, q, n, energy_gev, zstep)
         b.record(stream)
         b.synchronize()
-        return a.elapsed_time(b) * 1e3
+        if stages is None:
+            return a.elapsed_time(b) * 1e3
+        ms, _ = eng.profile_read()
+        return sum(ms[k] for k in stages) * 1e3
 
     best = {p: eng.get_param(p) for p in candidates()}
     ref = None
@@ -142,7 +151,9 @@ def tune(shape, n: int, precision: str = "fp32", device=None, energy_gev: float 
                 ref = rp.clone()
             elif not torch.equal(rp, ref):
                 raise RuntimeError(f"{PARAM_NAMES[p]}={v} changed the kick's result: launch shapes must not")
-            us[v] = min(kick_once() for _ in range(reps))
+            eng.profile(True)
+            us[v] = min(kick_once(PARAM_STAGES[p]) for _ in range(reps))
+            eng.profile(False)
             eng.check_status()
         best[p] = min(us, key=us.get)
         eng.set_param(p, best[p])
