@@ -143,8 +143,8 @@ Layout make_layout(const Plan& p, int64_t n) {
     L.sort_q = take(rs * ns);
     L.sort_tmp_k = take(4 * ns);
     L.sort_tmp_v = take(4 * ns);
-    const size_t sb = (ns + 4095) / 4096;
-    L.sort_hist = take(p.sorted_deposit ? 4 * 512 * (sb ? sb : 1) : 0);
+    const size_t sb = ns ? (size_t)sort_blocks((int64_t)ns) : 1;
+    L.sort_hist = take(p.sorted_deposit ? 4 * 512 * sb : 0);
     L.sort_tot = take(p.sorted_deposit ? 4 * 512 : 0);
     L.total = o;
     return L;
@@ -736,7 +736,7 @@ int sc_sort_keys(const uint32_t* keys_in, int64_t n, int key_bits, uint32_t* key
     if (!ws || ws_bytes < need) return fail(SC_ERR_WORKSPACE, "sort workspace needs %zu bytes", need);
     char* w = static_cast<char*>(ws);
     const size_t a = align_up(4 * (size_t)n);
-    const size_t nb = (size_t)((n + 4095) / 4096);
+    const size_t nb = (size_t)sort_blocks(n);
     uint32_t* tk = reinterpret_cast<uint32_t*>(w);
     uint32_t* tv = reinterpret_cast<uint32_t*>(w + a);
     uint32_t* hist = reinterpret_cast<uint32_t*>(w + 2 * a);

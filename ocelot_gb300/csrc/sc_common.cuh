@@ -204,6 +204,7 @@ cudaError_t launch_gather_xyz(const Plan& p, const Layout& L, char* ws, const Ki
 
 // sort + deposit (sc_sort.cu)
 size_t sort_scratch_bytes(int64_t n, int key_bits);
+int sort_blocks(int64_t n);  // blocks of a sort of n keys (rows of its digit histogram)
 int sort_passes(int key_bits);
 // With q_src set, the last pass writes q_src[index] (as double or float) into
 // q_out instead of the permutation.

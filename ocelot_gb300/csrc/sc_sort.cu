@@ -13,9 +13,9 @@
 // depend on scheduling, so it is the same alone and in a batch.
 //
 // Each radix pass is three launches with no inter-block waiting:
-//   hist     per-block digit histogram of a 4096-key tile -> hist[digit][block]
+//   hist     per-block digit histogram of a tile of 256, 1024 or 4096 keys -> hist[digit][block]
 //   rowscan  one warp per digit: exclusive scan along the blocks, digit totals
-//   scatter  per block: digit bases from the totals, then 16 rounds of 256 keys,
+//   scatter  per block: digit bases from the totals, then 1, 4 or 16 rounds of 256 keys,
 //            ranking equal digits within a warp by __match_any_sync and across
 //            warps by a per-digit prefix in shared memory (stable order:
 //            round, warp, lane = particle order)
@@ -24,23 +24,22 @@
 namespace ocsc {
 
 constexpr int RT = 256;
-constexpr int RITEMS = 16;
-constexpr int RTILE = RT * RITEMS;
+constexpr int RITEMS = 16;  // rounds of RT keys per block at most (large sorts)
 constexpr int RWARPS = RT / 32;
 constexpr int RMAXBITS = 9;
 constexpr int RBINS = 1 << RMAXBITS;  // 512 digits at most
 constexpr unsigned FULLM = 0xffffffffu;
 
 __global__ void __launch_bounds__(RT) k_rhist(const uint32_t* __restrict__ keys, int64_t n, int shift, int bins,
-                                              uint32_t* __restrict__ hist) {
+                                              uint32_t* __restrict__ hist, int items) {
     pdl_wait();
     __shared__ uint32_t h[RBINS];
     for (int d = threadIdx.x; d < RBINS; d += RT) h[d] = 0;
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * RTILE;
+    const int64_t base = (int64_t)blockIdx.x * RT * items;
     const uint32_t mask = (uint32_t)bins - 1;
 #pragma unroll 4
-    for (int it = 0; it < RITEMS; ++it) {
+    for (int it = 0; it < items; ++it) {
         const int64_t i = base + it * RT + threadIdx.x;
         if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1u);
     }
@@ -74,7 +73,7 @@ __global__ void __launch_bounds__(RT) k_rscatter(const uint32_t* __restrict__ ki
                                                  int64_t n, int shift, int bins, const uint32_t* __restrict__ hist,
                                                  const uint32_t* __restrict__ tot, uint32_t* __restrict__ kout,
                                                  uint32_t* __restrict__ vout, const double* __restrict__ qsrc,
-                                                 void* __restrict__ qout, int qfloat) {
+                                                 void* __restrict__ qout, int qfloat, int items) {
     pdl_wait();
     __shared__ uint32_t base[RBINS];
     __shared__ uint32_t wc[RWARPS][RBINS];
@@ -99,8 +98,8 @@ __global__ void __launch_bounds__(RT) k_rscatter(const uint32_t* __restrict__ ki
     __syncthreads();
     const uint32_t lt = (1u << lane) - 1u;
     const uint32_t mask = (uint32_t)bins - 1;
-    const int64_t tile = (int64_t)blockIdx.x * RTILE;
-    for (int r = 0; r < RITEMS; ++r) {
+    const int64_t tile = (int64_t)blockIdx.x * RT * items;
+    for (int r = 0; r < items; ++r) {
         const int64_t i = tile + (int64_t)r * RT + tid;
         const bool valid = i < n;
         const uint32_t key = valid ? kin[i] : 0u;
@@ -140,7 +139,16 @@ __global__ void __launch_bounds__(RT) k_rscatter(const uint32_t* __restrict__ ki
     }
 }
 
-static int sort_blocks(int64_t n) { return (int)((n + RTILE - 1) / RTILE); }
+// Rounds of RT keys per block: every round pays a clear and a scan of the
+// digit table behind four barriers whatever its size, so small sorts take
+// one or four rounds per block (more blocks in parallel) and large ones 16
+// (fewer digit-table rows for the scans).  The stable order, and so the
+// result, does not depend on the tiling.
+static int sort_items(int64_t n) { return n <= (1 << 18) ? 1 : (n <= (1 << 20) ? 4 : RITEMS); }
+int sort_blocks(int64_t n) {
+    const int64_t t = (int64_t)RT * sort_items(n);
+    return (int)((n + t - 1) / t);
+}
 
 int sort_passes(int key_bits) { return key_bits <= 0 ? 1 : (key_bits + RMAXBITS - 1) / RMAXBITS; }
 
@@ -154,7 +162,7 @@ cudaError_t launch_sort(const uint32_t* keys_in, int64_t n, int key_bits, uint32
                         uint32_t* tmp_k, uint32_t* tmp_v, uint32_t* hist, uint32_t* tot, cudaStream_t s,
                         const double* q_src, void* q_out, bool q_float) {
     if (n <= 0) return cudaSuccess;
-    const int nb = sort_blocks(n);
+    const int nb = sort_blocks(n), items = sort_items(n);
     const int passes = sort_passes(key_bits);
     const int width = key_bits <= 0 ? 1 : (key_bits + passes - 1) / passes;  // <= RMAXBITS
     const uint32_t* sk = keys_in;
@@ -167,11 +175,11 @@ cudaError_t launch_sort(const uint32_t* keys_in, int64_t n, int key_bits, uint32
         const int bins = 1 << dbits;
         uint32_t* dk = to_out ? keys_out : tmp_k;
         uint32_t* dv = to_out ? perm_out : tmp_v;
-        launch(k_rhist, nb, RT, 0, s, sk, n, shift, bins, hist);
+        launch(k_rhist, nb, RT, 0, s, sk, n, shift, bins, hist, items);
         launch(k_rrowscan, (bins * 32 + 255) / 256, 256, 0, s, hist, nb, bins, tot);
         const bool last = p == passes - 1;
         launch(k_rscatter, nb, RT, 0, s, sk, sv, n, shift, bins, hist, tot, dk, dv, last ? q_src : nullptr,
-                                     last ? q_out : nullptr, q_float ? 1 : 0);
+                                     last ? q_out : nullptr, q_float ? 1 : 0, items);
         sk = dk;
         sv = dv;
         to_out = !to_out;
