@@ -1110,26 +1110,10 @@ __device__ __forceinline__ void xyz_fine32(const double* __restrict__ rp, int64_
     }
 }
 
-// A candidate extreme of the extent pass: the FP32-corrected estimate when
-// its error bound is below 1e-10 of the cell (cell[j] ~ the mesh step from
-// the block's FP32 extent) -- at 100 MeV and above, where the correction of
-// the lab position is small -- else the FP64 form's operations: at a few MeV
-// the estimate is off by ~1e-8 cells, enough to move the mesh step and with
-// it the key of a particle that close to a face.
-__device__ __forceinline__ void extent_pos(const double* __restrict__ rp, int64_t ld, int64_t i, const KickParams& kp,
-                                           const double (&T)[3][3], double g0, const float (&cell)[3], double v[3]) {
-    double err[3];
-    xyz_fine32(rp, ld, i, kp, T, g0, v, err);
-    bool ok = true;
-    for (int j = 0; j < 3; ++j) ok &= err[j] < 1e-10 * (double)cell[j];
-    if (!ok) xyz_fine(rp, ld, i, kp, T, g0, v);
-}
-
-
 
 // FP32 extent.  Pass 1 computes the rotated positions in FP32, stores them and
 // reduces FP32 extremes and charge moments.  Pass 2 re-walks the block's
-// particles and evaluates in FP64 (extent_pos) every particle whose
+// particles and evaluates in FP64 (xyz_fine) every particle whose
 // FP32 coordinate lies within a rounding margin of the block's FP32 extreme:
 // the FP64 extreme of the block is among them, so the mesh step equals the
 // FP64 form's.
@@ -1197,11 +1181,9 @@ __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, con
             emax[j] = ord64(-INFINITY);
         }
     __syncthreads();
-    float tol[3], cell[3];
-    for (int j = 0; j < 3; ++j) {  // 2^-18 of the coordinate scale: 64x the FP32 rounding bound of v
+    float tol[3];
+    for (int j = 0; j < 3; ++j)  // 2^-18 of the coordinate scale: 64x the FP32 rounding bound of v
         tol[j] = ldexpf(fmaxf(fabsf(bmin[j]), fabsf(bmax[j])) + (bmax[j] - bmin[j]), -18);
-        cell[j] = (bmax[j] - bmin[j]) / (float)((j == 0 ? kp.nx : j == 1 ? kp.ny : kp.nz) - 3);
-    }
     if (ok) {
         double Td[3][3];
         for (int a = 0; a < 3; ++a)
@@ -1219,7 +1201,7 @@ __device__ __forceinline__ void extent32_body(const double* __restrict__ rp, con
             }
             if (cand) {
                 double v[3];
-                extent_pos(rp, ld, i, kp, Td, g0d, cell, v);
+                xyz_fine(rp, ld, i, kp, Td, g0d, v);
                 for (int j = 0; j < 3; ++j) {
                     if (X[j * nX + i] <= bmin[j] + tol[j]) atomicMin(&emin[j], ord64(v[j]));
                     if (X[j * nX + i] >= bmax[j] - tol[j]) atomicMax(&emax[j], ord64(v[j]));
@@ -1363,11 +1345,10 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
             emax[j] = ord64(-INFINITY);
         }
     __syncthreads();
-    float tol[3], cell[3];
+    float tol[3];
     bool mine = false;
     for (int j = 0; j < 3; ++j) {  // 2^-18 of the coordinate scale: 64x the FP32 rounding bound of v
         tol[j] = ldexpf(fmaxf(fabsf(bmin[j]), fabsf(bmax[j])) + (bmax[j] - bmin[j]), -18);
-        cell[j] = (bmax[j] - bmin[j]) / (float)((j == 0 ? kp.nx : j == 1 ? kp.ny : kp.nz) - 3);
         mine |= (my_mn[j] <= bmin[j] + tol[j]) || (my_mx[j] >= bmax[j] - tol[j]);
     }
     if (ok && streamed && mine) {
@@ -1406,7 +1387,7 @@ __device__ __forceinline__ void extent32_tma_body(const double* __restrict__ rp,
                 sides &= ~(63ull << (6 * p));
                 const int64_t i = Tl.start(t0 + p / 2) + 2 * threadIdx.x + (p & 1);
                 double v[3];
-                extent_pos(rp, ld, i, kp, Td, g0d, cell, v);
+                xyz_fine(rp, ld, i, kp, Td, g0d, v);
                 for (int j = 0; j < 3; ++j) {
                     if (sd & (1u << j)) atomicMin(&emin[j], ord64(v[j]));
                     if (sd & (8u << j)) atomicMax(&emax[j], ord64(v[j]));
