@@ -127,14 +127,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def time_form(precision, n, steps, warmup, dev, flush, fields="spectral"):
+def time_form(precision, n, steps, warmup, dev, flush, fields="spectral", mesh=MESH):
     """Device-resident kicks; per-kick CUDA events; per-stage events from the library."""
     import torch
     from ocelot_gb300 import SpaceCharge
     rp, q = beam(n)
     d_rp = torch.from_numpy(rp).to(dev)
     d_q = torch.from_numpy(q).to(dev)
-    sc = SpaceCharge(nmesh_xyz=MESH, precision=precision, device=dev, fields=fields)
+    sc = SpaceCharge(nmesh_xyz=mesh, precision=precision, device=dev, fields=fields)
     eng = sc.engine()
     eng.ensure(n)
     stream = torch.cuda.current_stream(dev)
@@ -647,11 +647,24 @@ def main():
                     help="time the FP32 kick alone (no other leg): the small case for profiling")
     ap.add_argument("--transport", type=int, default=0, metavar="N",
                     help="time the tracking transport kernels (slice forms, moments) on N particles and exit")
+    ap.add_argument("--profile-form", choices=["fp32", "fp64"], default=None,
+                    help="time kicks of one form alone on --n particles and a --mesh^3 mesh, print one line and exit "
+                         "(the small cases of the profiles)")
+    ap.add_argument("--mesh", type=int, default=64)
     ap.add_argument("--tune", action="store_true",
                     help="autotune the launch shapes on the benchmark meshes and particle counts, print the "
                          "timings (and store them in the tuning table with --tune-save) and exit")
     ap.add_argument("--tune-save", action="store_true")
     args = ap.parse_args()
+    if args.profile_form:
+        import torch
+        dev = torch.device("cuda", 0)
+        flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+        kick, stages, launches = time_form(args.profile_form, args.n, args.steps, max(args.warmup, 3), dev,
+                                           flush_buf.zero_, mesh=[args.mesh] * 3)
+        print(json.dumps({"form": args.profile_form, "n": args.n, "mesh": [args.mesh] * 3, "ms_per_kick": kick,
+                          "stages_ms": stages, "launches": launches}), flush=True)
+        return
     if args.tune:
         from ocelot_gb300 import tuning
         cases = [((64, 64, 64), 2_000_000), ((64, 64, 64), 200_000), ((63, 63, 63), 200_000),
