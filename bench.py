@@ -5,16 +5,32 @@ uncorrelated 6D Gaussian beam (sigma_x = sigma_y = 50 um, sigma_x' = sigma_y'
 = 1e-5, sigma_tau = 100 um, sigma_delta = 1e-4), 130 MeV, 1 nC split equally,
 one kick of dz = 0.1 m per step.  Synthetic data, no dataset involved.
 
-A step is one kick.  ``value`` is particle-kicks/s of the FP32 form (the
-headline) with the particles resident in HBM, timed with CUDA events around
-each kick; L2 (129 MB, larger than the 112 MB of particles and charges) is
-flushed between timed kicks by writing a 256 MB buffer and then reading
-another 256 MB buffer (the read writes the flush's dirty lines back to HBM
-before the kick starts, so the kick does not pay for them).  The FP64 form is
-timed the same way and reported beside it.  ``e2e`` is the same metric through
-``SpaceCharge.apply`` on a host ``ParticleArray`` in pinned memory: the
-host->device copy of rparticles and q_array and the device->host copy of
-rparticles are inside the timed region of every step.
+A step is one kick.  ``value`` is particle-kicks/s of the FP32 form (spectral
+fields, the library's default; the headline) with the particles resident in
+HBM, timed with CUDA events around each kick; L2 (129 MB, larger than the
+112 MB of particles and charges) is flushed between timed kicks by writing a
+256 MB buffer and then reading another 256 MB buffer (the read writes the
+flush's dirty lines back to HBM before the kick starts, so the kick does not
+pay for them).  Timed the same way and reported beside it: the FP32 form with
+the reference's difference fields and the FP64 form, each with its stage
+times; the errors of phi, of E at the particles (recorded by the kick itself)
+and of the momentum kicks of both FP32 forms against the FP64 form.  ``e2e``
+is the same metric through ``SpaceCharge.apply`` on a host ``ParticleArray``
+in pinned memory: the host->device copy of rparticles and q_array and the
+device->host copy of rparticles are inside the timed region of every step;
+``e2e_pageable`` the same with pageable numpy arrays, and ``e2e_roofline``
+the step's copies at the measured host-link bandwidth against the e2e step.
+``config1`` (the plain FP64 form: 200k particles, 63^3, 10 kicks per step)
+and ``config3`` (the FP32 stress workload: 10M particles at 6.5 MeV on
+128x128x256, 20 kicks per step) are timed with their rooflines, CPU baselines
+and errors; ``batched`` (96 uneven beams, one graph-replayed batched kick per
+step, with its stage times) and ``serving`` (Poisson-arriving FODO tracking
+jobs, latency percentiles) complete the line.
+
+Modes that print their own line and exit: --kick-only (the FP32 kick alone),
+--profile-form fp32|fp64 with --n and --mesh (one form's kicks on a chosen
+size: the small cases of the ncu captures), --transport N (the tracking
+kernels), --tune [--tune-save] (the autotuner on this GPU).
 
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/sc_oracle.py: numpy, scipy.ndimage and scipy.fft on all host cores)
