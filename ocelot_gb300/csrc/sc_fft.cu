@@ -69,6 +69,62 @@ __device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
     return cx<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// Stage the charge of NC complex z lines into the line buffer a (line c at
+// a + c * lz): the real part of line c is row y0 + 2c of plane x, the
+// imaginary part row y0 + 2c + 1, zero-padded from nz to Mz.  With qfix the
+// charge arrives as the 64-bit fixed-point grid, is scaled to R and is also
+// stored in q.  U elements per thread per round: all their loads are issued
+// before any of them is converted or stored, one memory round trip per round.
+// code, code + 1: the index-check codes of the two rows
+template <typename R>
+__device__ __forceinline__ void stage_charge_lines(R* __restrict__ q, const long long* __restrict__ qfix,
+                                                   Cx<R>* __restrict__ a, int lz, int x, int y0, int NC, int ny,
+                                                   int nz, int Mz, const ScState* st, long long ncell, int code) {
+    constexpr int U = 4;
+    const float ufix = qfix ? st->qfix_inv : 0.f;
+    for (DivWalk w(threadIdx.x, blockDim.x, Mz); w.q < NC;) {
+        int cs[U], zs[U];
+        bool oka[U], okb[U];
+        size_t ia[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            cs[u] = w.q;
+            zs[u] = w.r;
+            w.next();
+            const int ya = y0 + 2 * cs[u], yb = ya + 1;
+            const bool in = cs[u] < NC && zs[u] < nz;
+            ia[u] = ((size_t)x * ny + ya) * nz + zs[u];
+            oka[u] = in && ya < ny && SC_IDX_OK(st, code, ia[u], ncell);
+            okb[u] = in && yb < ny && SC_IDX_OK(st, code + 1, ia[u] + nz, ncell);
+        }
+        R re[U], im[U];
+        if (qfix) {
+            long long fa[U], fb[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                fa[u] = oka[u] ? qfix[ia[u]] : 0;
+                fb[u] = okb[u] ? qfix[ia[u] + nz] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                re[u] = (R)(__ll2float_rn(fa[u]) * ufix);
+                im[u] = (R)(__ll2float_rn(fb[u]) * ufix);
+                if (oka[u]) q[ia[u]] = re[u];
+                if (okb[u]) q[ia[u] + nz] = im[u];
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                re[u] = oka[u] ? q[ia[u]] : (R)0;
+                im[u] = okb[u] ? q[ia[u] + nz] : (R)0;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (cs[u] < NC) a[cs[u] * lz + zs[u]] = cx<R>(re[u], im[u]);
+    }
+}
+
 // qfix != nullptr: the charge arrives as the 64-bit fixed-point grid of the
 // FP32 form's exact deposit; it is scaled to R here and also stored in q
 // (the charge grid an inspection reads back)
@@ -86,29 +142,11 @@ __device__ __forceinline__ void zfwd_body(R* __restrict__ q, const long long* __
     load_twiddles<R>(tw, twg, Mz);
     const int x = vb.y;
     const int y0 = vb.x * 2 * NC;
-    for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
-        const int c = idx / Mz, z = idx - c * Mz;
-        const int ya = y0 + 2 * c, yb = ya + 1;
-        R re = 0, im = 0;
-        if (z < nz) {
-            const size_t ia = ((size_t)x * ny + ya) * nz + z, ib = ia + nz;
-            [[maybe_unused]] const long long ncell = (long long)vb.ny * ny * nz;
-            if ((ya < ny && !SC_IDX_OK(st, 21, ia, ncell)) || (yb < ny && !SC_IDX_OK(st, 22, ib, ncell))) continue;
-            if (qfix) {
-                const float u = st->qfix_inv;
-                if (ya < ny) { re = (R)(__ll2float_rn(qfix[ia]) * u); q[ia] = re; }
-                if (yb < ny) { im = (R)(__ll2float_rn(qfix[ib]) * u); q[ib] = im; }
-            } else {
-                if (ya < ny) re = q[ia];
-                if (yb < ny) im = q[ib];
-            }
-        }
-        a[c * lz + z] = cx<R>(re, im);
-    }
+    stage_charge_lines<R>(q, qfix, a, lz, x, y0, NC, ny, nz, Mz, st, (long long)vb.ny * ny * nz, 21);
     __syncthreads();
     Cx<R>* res = fft_lines<R, false>(a, b, lz, NC, rz, tw);
-    for (int idx = threadIdx.x; idx < NC * Kz; idx += blockDim.x) {
-        const int c = idx / Kz, k = idx - c * Kz;
+    for (DivWalk w(threadIdx.x, blockDim.x, Kz); w.q < NC; w.next()) {
+        const int c = w.q, k = w.r;
         const int ya = y0 + 2 * c, yb = ya + 1;
         const Cx<R> Z = res[c * lz + k];
         const Cx<R> Zm = res[c * lz + (k == 0 ? 0 : Mz - k)];
@@ -129,10 +167,12 @@ __global__ void __launch_bounds__(FFT_THREADS) k_zfwd(R* __restrict__ q, const l
 }
 
 // strided pass along y: forward (rows < ny in, all My out) or inverse (all in, rows < ny out),
-// in place on W.  W3 != nullptr (inverse, spectral fields): the block also
+// in place on W.  The columns are the nx * Kz lines (x, kz), flattened as
+// x * Kz + kz; block vb.x takes TK consecutive ones (a block may straddle two
+// x planes).  W3 != nullptr (inverse, spectral fields): the block also
 // transforms its columns of W multiplied by D(ky) into W3 (a third line buffer)
 template <typename R, bool INV>
-__device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My, int Kz, const RadixPlan& ry,
+__device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int nx, int ny, int My, int Kz, const RadixPlan& ry,
                                            const Cx<R>* __restrict__ twg, int TK, const ScState* st, VBlk vb,
                                            Cx<R>* __restrict__ W3 = nullptr, const Cx<R>* __restrict__ dy = nullptr) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -143,47 +183,61 @@ __device__ __forceinline__ void ypass_body(Cx<R>* __restrict__ W, int ny, int My
     Cx<R>* b = a + TK * ls;
     Cx<R>* c = b + TK * ls;
     load_twiddles<R>(tw, twg, My);
-    const int x = vb.y;
-    const int k0 = vb.x * TK;
+    const ColMap cm(TK);
+    const int col = vb.x * TK + cm.kk;
+    const bool live = col < nx * Kz;
+    const int x = col / Kz, k = col - x * Kz;
+    const size_t base = ((size_t)x * My) * Kz + k;  // element y of the column at base + y * Kz
     const int nin = INV ? My : ny;
-    for (int idx = threadIdx.x; idx < My * TK; idx += blockDim.x) {
-        const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
-        Cx<R> v = cx<R>(0, 0);
-        if (y < nin && k < Kz) v = W[((size_t)x * My + y) * Kz + k];
-        a[kk * ls + y] = v;
-        if (W3) c[kk * ls + y] = cmul(v, dy[y]);
+    Cx<R>* la = a + cm.kk * ls;
+    Cx<R>* lc = c + cm.kk * ls;
+    constexpr int U = 8;  // rows per round: their loads are issued together
+    for (int y0 = cm.r0; y0 < My; y0 += U * cm.rs) {
+        Cx<R> v[U], d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int y = y0 + u * cm.rs;
+            v[u] = (y < nin && live) ? W[base + (size_t)y * Kz] : cx<R>(0, 0);
+            d[u] = (W3 && y < My) ? dy[y] : cx<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int y = y0 + u * cm.rs;
+            if (y < My) {
+                la[y] = v[u];
+                if (W3) lc[y] = cmul(v[u], d[u]);
+            }
+        }
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, INV>(a, b, ls, TK, ry, tw);
     const int nout = INV ? ny : My;
-    for (int idx = threadIdx.x; idx < nout * TK; idx += blockDim.x) {
-        const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
-        if (k < Kz) W[((size_t)x * My + y) * Kz + k] = res[kk * ls + y];
-    }
+    if (live)
+        for (int y = cm.r0; y < nout; y += cm.rs) W[base + (size_t)y * Kz] = res[cm.kk * ls + y];
     if (W3) {
         __syncthreads();  // a and b are free
         Cx<R>* res3 = fft_lines<R, INV>(c, a, ls, TK, ry, tw);
-        for (int idx = threadIdx.x; idx < nout * TK; idx += blockDim.x) {
-            const int y = idx / TK, kk = idx - y * TK, k = k0 + kk;
-            if (k < Kz) W3[((size_t)x * My + y) * Kz + k] = res3[kk * ls + y];
-        }
+        if (live)
+            for (int y = cm.r0; y < nout; y += cm.rs) W3[base + (size_t)y * Kz] = res3[cm.kk * ls + y];
     }
 }
 
-// blockIdx.z = 0: W (and, with spectral fields, W x D(ky) into W3);
-// blockIdx.z = 1 (inverse, spectral fields): the x-differenced grid W2 in place
+// blockIdx.y = 0: W (and, with spectral fields, W x D(ky) into W3);
+// blockIdx.y = 1 (inverse, spectral fields): the x-differenced grid W2 in place
 template <typename R, bool INV>
-__global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int ny, int My, int Kz,
+__global__ void __launch_bounds__(FFT_THREADS) k_ypass(Cx<R>* __restrict__ W, int nx, int ny, int My, int Kz,
                                                        RadixPlan ry, const Cx<R>* __restrict__ twg,
                                                        int TK, const ScState* st, Spec<R> sp) {
     pdl_wait();
-    if (blockIdx.z == 0) ypass_body<R, INV>(W, ny, My, Kz, ry, twg, TK, st, hw_vblk(), sp.W3, sp.dy);
-    else ypass_body<R, INV>(sp.W2, ny, My, Kz, ry, twg, TK, st, hw_vblk());
+    if (blockIdx.y == 0) ypass_body<R, INV>(W, nx, ny, My, Kz, ry, twg, TK, st, hw_vblk(), sp.W3, sp.dy);
+    else ypass_body<R, INV>(sp.W2, nx, ny, My, Kz, ry, twg, TK, st, hw_vblk());
 }
 
-// x pass: forward FFT of the nx non-zero planes, Green multiply, inverse FFT, keep x < nx
-// W2 != nullptr (spectral fields): the product times D(kx) goes through its
-// own inverse transform (a third line buffer) into W2
+// x pass: forward FFT of the nx non-zero planes, Green multiply, inverse FFT, keep x < nx.
+// The columns are the My * Kz lines (ky, kz), flattened as ky * Kz + kz (the
+// element x of a column at x * My * Kz + column); block vb.x takes TK
+// consecutive ones.  W2 != nullptr (spectral fields): the product times D(kx)
+// goes through its own inverse transform (a third line buffer) into W2
 template <typename R>
 __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __restrict__ G, int nx, int My, int Kz,
                                            int Ky, const RadixPlan& rx, const Cx<R>* __restrict__ twg, int TK,
@@ -198,41 +252,63 @@ __device__ __forceinline__ void xconv_body(Cx<R>* __restrict__ W, const R* __res
     Cx<R>* b = a + TK * ls;
     Cx<R>* c = b + TK * ls;
     load_twiddles<R>(tw, twg, Mx);
-    const int ky = vb.y;
+    const ColMap cm(TK);
+    const int col = vb.x * TK + cm.kk;
+    const int ncol = My * Kz;
+    const bool live = col < ncol;
+    const int ky = col / Kz, k = col - ky * Kz;
     const int gy = ky <= My - ky ? ky : My - ky;
-    const int k0 = vb.x * TK;
-    for (int idx = threadIdx.x; idx < Mx * TK; idx += blockDim.x) {
-        const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
-        Cx<R> v = cx<R>(0, 0);
-        if (x < nx && k < Kz) v = W[((size_t)x * My + ky) * Kz + k];
-        a[kk * ls + x] = v;
+    const int gk = gy * Kz + k;  // the column's Green entry at gx * Ky * Kz + gk
+    const int KyKz = Ky * Kz;
+    Cx<R>* la = a + cm.kk * ls;
+    constexpr int U = 8;  // rows per round: their loads are issued together
+    for (int x0 = cm.r0; x0 < Mx; x0 += U * cm.rs) {
+        Cx<R> v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int x = x0 + u * cm.rs;
+            v[u] = (x < nx && live) ? W[(size_t)x * ncol + col] : cx<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (x0 + u * cm.rs < Mx) la[x0 + u * cm.rs] = v[u];
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, false>(a, b, ls, TK, rx, tw);
-    for (int idx = threadIdx.x; idx < Mx * TK; idx += blockDim.x) {
-        const int kx = idx / TK, kk = idx - kx * TK, k = k0 + kk;
-        const int gx = kx <= Mx - kx ? kx : Mx - kx;
-        const long long gi = ((long long)gx * Ky + gy) * Kz + k;
-        const R g = (k < Kz && SC_IDX_OK(st, 23, gi, (long long)(rx.L / 2 + 1) * Ky * Kz)) ? G[gi] : (R)0;
-        Cx<R> v = res[kk * ls + kx];
-        v.x *= g;
-        v.y *= g;
-        res[kk * ls + kx] = v;
-        if (W2) c[kk * ls + kx] = cmul(v, dx[kx]);
+    Cx<R>* lr = res + cm.kk * ls;
+    Cx<R>* lc = c + cm.kk * ls;
+    for (int x0 = cm.r0; x0 < Mx; x0 += U * cm.rs) {
+        R g[U];
+        Cx<R> d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int kx = x0 + u * cm.rs;
+            const int gx = kx <= Mx - kx ? kx : Mx - kx;
+            const long long gi = (long long)gx * KyKz + gk;
+            g[u] = (kx < Mx && live && SC_IDX_OK(st, 23, gi, (long long)(rx.L / 2 + 1) * KyKz)) ? G[gi] : (R)0;
+            d[u] = (W2 && kx < Mx) ? dx[kx] : cx<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int kx = x0 + u * cm.rs;
+            if (kx < Mx) {
+                Cx<R> v = lr[kx];
+                v.x *= g[u];
+                v.y *= g[u];
+                lr[kx] = v;
+                if (W2) lc[kx] = cmul(v, d[u]);
+            }
+        }
     }
     __syncthreads();
     Cx<R>* res2 = fft_lines<R, true>(res, res == a ? b : a, ls, TK, rx, tw);
-    for (int idx = threadIdx.x; idx < nx * TK; idx += blockDim.x) {
-        const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
-        if (k < Kz) W[((size_t)x * My + ky) * Kz + k] = res2[kk * ls + x];
-    }
+    if (live)
+        for (int x = cm.r0; x < nx; x += cm.rs) W[(size_t)x * ncol + col] = res2[cm.kk * ls + x];
     if (W2) {
         __syncthreads();  // a and b are free
         Cx<R>* res3 = fft_lines<R, true>(c, a, ls, TK, rx, tw);
-        for (int idx = threadIdx.x; idx < nx * TK; idx += blockDim.x) {
-            const int x = idx / TK, kk = idx - x * TK, k = k0 + kk;
-            if (k < Kz) W2[((size_t)x * My + ky) * Kz + k] = res3[kk * ls + x];
-        }
+        if (live)
+            for (int x = cm.r0; x < nx; x += cm.rs) W2[(size_t)x * ncol + col] = res3[cm.kk * ls + x];
     }
 }
 
@@ -278,27 +354,40 @@ __device__ __forceinline__ void zinv_body(const Cx<R>* __restrict__ W, R* __rest
     load_twiddles<R>(tw, twg, Mz);
     const int x = vb.y;
     const int y0 = vb.x * 2 * NC;
-    for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
-        const int c = idx / Mz, k = idx - c * Mz;
-        const int ya = y0 + 2 * c, yb = ya + 1;
-        const bool lo = k < Kz;
-        const int kk = lo ? k : Mz - k;
-        Cx<R> A = cx<R>(0, 0), B = cx<R>(0, 0);
-        if (ya < ny) A = W[((size_t)x * My + ya) * Kz + kk];
-        if (yb < ny) B = W[((size_t)x * My + yb) * Kz + kk];
-        if (dz) {
-            A = cmul(A, dz[kk]);
-            B = cmul(B, dz[kk]);
+    constexpr int U = 4;  // elements per thread per round, their loads issued together
+    for (DivWalk w(threadIdx.x, blockDim.x, Mz); w.q < NC;) {
+        int cs[U], ks[U];
+        Cx<R> A[U], B[U], d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            cs[u] = w.q;
+            ks[u] = w.r;
+            w.next();
+            const int ya = y0 + 2 * cs[u], yb = ya + 1;
+            const bool in = cs[u] < NC;
+            const int kk = ks[u] < Kz ? ks[u] : Mz - ks[u];
+            A[u] = (in && ya < ny) ? W[((size_t)x * My + ya) * Kz + kk] : cx<R>(0, 0);
+            B[u] = (in && yb < ny) ? W[((size_t)x * My + yb) * Kz + kk] : cx<R>(0, 0);
+            d[u] = (dz && in) ? dz[kk] : cx<R>(0, 0);
         }
-        // Z = A + iB, Hermitian-extended above Mz/2
-        a[c * lz + k] = lo ? cx<R>(A.x - B.y, A.y + B.x) : cx<R>(A.x + B.y, B.x - A.y);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (cs[u] >= NC) continue;
+            Cx<R> Au = A[u], Bu = B[u];
+            if (dz) {
+                Au = cmul(Au, d[u]);
+                Bu = cmul(Bu, d[u]);
+            }
+            // Z = A + iB, Hermitian-extended above Mz/2
+            a[cs[u] * lz + ks[u]] = ks[u] < Kz ? cx<R>(Au.x - Bu.y, Au.y + Bu.x) : cx<R>(Au.x + Bu.y, Bu.x - Au.y);
+        }
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, true>(a, b, lz, NC, rz, tw);
     const double norm = st->phi_norm, denom = st->phi_denom;
     const R fscale = (R)st->phi_scalef * mul;  // (float)(norm / denom), computed once by the mesh finalize
-    for (int idx = threadIdx.x; idx < NC * nz; idx += blockDim.x) {
-        const int c = idx / nz, z = idx - c * nz;
+    for (DivWalk w(threadIdx.x, blockDim.x, nz); w.q < NC; w.next()) {
+        const int c = w.q, z = w.r;
         const int ya = y0 + 2 * c, yb = ya + 1;
         const Cx<R> v = res[c * lz + z];
         if (sizeof(R) == 8) {
@@ -481,31 +570,13 @@ __device__ __forceinline__ void zy_fwd_body(R* __restrict__ q, const long long* 
     load_twiddles<R>(twz, twzg, Mz);
     load_twiddles<R>(twy, twyg, My);
     // F1: two charge rows per complex line (as k_zfwd)
-    for (int idx = threadIdx.x; idx < ncz * Mz; idx += blockDim.x) {
-        const int c = idx / Mz, z = idx - c * Mz;
-        const int ya = 2 * c, yb = ya + 1;
-        R re = 0, im = 0;
-        if (z < nz) {
-            const size_t ia = ((size_t)x * ny + ya) * nz + z, ib = ia + nz;
-            [[maybe_unused]] const long long ncell = (long long)nx * ny * nz;
-            if ((ya < ny && !SC_IDX_OK(st, 25, ia, ncell)) || (yb < ny && !SC_IDX_OK(st, 26, ib, ncell))) continue;
-            if (qfix) {
-                const float u = st->qfix_inv;
-                if (ya < ny) { re = (R)(__ll2float_rn(qfix[ia]) * u); q[ia] = re; }
-                if (yb < ny) { im = (R)(__ll2float_rn(qfix[ib]) * u); q[ib] = im; }
-            } else {
-                if (ya < ny) re = q[ia];
-                if (yb < ny) im = q[ib];
-            }
-        }
-        A1[c * lz + z] = cx<R>(re, im);
-    }
+    stage_charge_lines<R>(q, qfix, A1, lz, x, 0, ncz, ny, nz, Mz, st, (long long)nx * ny * nz, 25);
     __syncthreads();
     const Cx<R>* res1 = fft_lines<R, false>(A1, B1, lz, ncz, rz, twz);
     // unpack the two real lines into the y lines (column kz, row y); rows
     // ny..My-1 are the zero padding of F2
-    for (int idx = threadIdx.x; idx < ncz * Kz; idx += blockDim.x) {
-        const int c = idx / Kz, k = idx - c * Kz;
+    for (DivWalk w(threadIdx.x, blockDim.x, Kz); w.q < ncz; w.next()) {
+        const int c = w.q, k = w.r;
         const int ya = 2 * c, yb = ya + 1;
         const Cx<R> Z = res1[c * lz + k];
         const Cx<R> Zm = res1[c * lz + (k == 0 ? 0 : Mz - k)];
@@ -513,16 +584,11 @@ __device__ __forceinline__ void zy_fwd_body(R* __restrict__ q, const long long* 
         A2[k * ly + ya] = cx<R>((Z.x + Zm.x) * h, (Z.y - Zm.y) * h);
         if (yb < ny) A2[k * ly + yb] = cx<R>((Z.y + Zm.y) * h, (Zm.x - Z.x) * h);
     }
-    for (int idx = threadIdx.x; idx < Kz * (My - ny); idx += blockDim.x) {
-        const int k = idx / (My - ny), r = idx - k * (My - ny);
-        A2[k * ly + ny + r] = cx<R>(0, 0);
-    }
+    for (DivWalk w(threadIdx.x, blockDim.x, Kz); w.q < My - ny; w.next()) A2[w.r * ly + ny + w.q] = cx<R>(0, 0);
     __syncthreads();
     const Cx<R>* res2 = fft_lines<R, false>(A2, B2, ly, Kz, ry, twy);
-    for (int idx = threadIdx.x; idx < My * Kz; idx += blockDim.x) {
-        const int ky = idx / Kz, k = idx - ky * Kz;
-        W[((size_t)x * My + ky) * Kz + k] = res2[k * ly + ky];
-    }
+    Cx<R>* Wx = W + (size_t)x * My * Kz;  // the plane: row ky, column k at ky * Kz + k
+    for (DivWalk w(threadIdx.x, blockDim.x, Kz); w.q < My; w.next()) Wx[w.q * Kz + w.r] = res2[w.r * ly + w.q];
 }
 
 template <typename R>
@@ -553,10 +619,23 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
     Cx<R>* B2 = A2 + Kz * ly;
     load_twiddles<R>(twz, twzg, Mz);
     load_twiddles<R>(twy, twyg, My);
-    for (int idx = threadIdx.x; idx < My * Kz; idx += blockDim.x) {
-        const int ky = idx / Kz, k = idx - ky * Kz;
-        const Cx<R> v = W[((size_t)x * My + ky) * Kz + k];
-        A2[k * ly + ky] = dy ? cmul(v, dy[ky]) : v;
+    const Cx<R>* Wx = W + (size_t)x * My * Kz;
+    constexpr int U = 4;  // elements per thread per round, their loads issued together
+    for (DivWalk w(threadIdx.x, blockDim.x, Kz); w.q < My;) {
+        int ys[U], ks[U];
+        Cx<R> v[U], d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            ys[u] = w.q;
+            ks[u] = w.r;
+            w.next();
+            const bool in = ys[u] < My;
+            v[u] = in ? Wx[ys[u] * Kz + ks[u]] : cx<R>(0, 0);
+            d[u] = (dy && in) ? dy[ys[u]] : cx<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (ys[u] < My) A2[ks[u] * ly + ys[u]] = dy ? cmul(v[u], d[u]) : v[u];
     }
     __syncthreads();
     // B2: inverse y; only rows y < ny are used
@@ -564,8 +643,8 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
     Cx<R>* A1 = res2 == B2 ? A2 : B2;
     Cx<R>* B1 = A1 + ncz * lz;
     // B1: two output rows per complex line, Hermitian-extended (as k_zinv)
-    for (int idx = threadIdx.x; idx < ncz * Mz; idx += blockDim.x) {
-        const int c = idx / Mz, k = idx - c * Mz;
+    for (DivWalk w(threadIdx.x, blockDim.x, Mz); w.q < ncz; w.next()) {
+        const int c = w.q, k = w.r;
         const int ya = 2 * c, yb = ya + 1;
         const bool lo = k < Kz;
         const int kk = lo ? k : Mz - k;
@@ -581,8 +660,8 @@ __device__ __forceinline__ void yz_inv_body(const Cx<R>* __restrict__ W, R* __re
     const Cx<R>* res = fft_lines<R, true>(A1, B1, lz, ncz, rz, twz);
     const double norm = st->phi_norm, denom = st->phi_denom;
     const R fscale = (R)st->phi_scalef * mul;  // (float)(norm / denom), computed once by the mesh finalize
-    for (int idx = threadIdx.x; idx < ncz * nz; idx += blockDim.x) {
-        const int c = idx / nz, z = idx - c * nz;
+    for (DivWalk w(threadIdx.x, blockDim.x, nz); w.q < ncz; w.next()) {
+        const int c = w.q, z = w.r;
         const int ya = 2 * c, yb = ya + 1;
         const Cx<R> v = res[c * lz + z];
         if (sizeof(R) == 8) {
@@ -676,8 +755,9 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     const int tkyi = strided_cols<R>(p.My, nbuf);  // the y inverse
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
     const size_t smyi = sizeof(Cx<R>) * (size_t)(p.My + nbuf * tkyi * fft_ls(p.My));
-    dim3 gy((Kz + tky - 1) / tky, p.nx);
-    dim3 gyi((Kz + tkyi - 1) / tkyi, p.nx, sp.W2 ? 2 : 1);
+    const int ycols = p.nx * Kz;  // the y passes' columns (x, kz)
+    dim3 gy((ycols + tky - 1) / tky);
+    dim3 gyi((ycols + tkyi - 1) / tkyi, sp.W2 ? 2 : 1);
     static const int optin = optin_smem();
     const bool plane = plane_fits<R>(p, optin);
     const bool plane_fwd = plane && p.fft_plane_fwd, plane_inv = plane && p.fft_plane_inv;
@@ -689,11 +769,11 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
         if ((e = set_smem(k_zfwd<R>, smz))) return e;
         launch(k_zfwd<R>, gz, FFT_THREADS, smz, s, qgrid, qfix, W, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st);
         if ((e = set_smem(k_ypass<R, false>, smy))) return e;
-        launch(k_ypass<R, false>, gy, FFT_THREADS, smy, s, W, p.ny, p.My, Kz, p.ry, twy, tky, st, Spec<R>{});
+        launch(k_ypass<R, false>, gy, FFT_THREADS, smy, s, W, p.nx, p.ny, p.My, Kz, p.ry, twy, tky, st, Spec<R>{});
     }
     if (part == CONV_FORWARD) return cudaGetLastError();
     const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + nbuf * tkx * fft_ls(p.Mx));
-    dim3 gx((Kz + tkx - 1) / tkx, p.My);
+    dim3 gx((p.My * Kz + tkx - 1) / tkx);  // the x pass's columns (ky, kz)
     if ((e = set_smem(k_xconv<R>, smx))) return e;
     launch(k_xconv<R>, gx, FFT_THREADS, smx, s, W, G, p.nx, p.My, Kz, Ky, p.rx, twx, tkx, st, sp);
     const int nout = sp.W2 ? 4 - sp.f0 : 1;  // [the potential,] Ex, Ey, Ez
@@ -704,7 +784,7 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
         return cudaGetLastError();
     }
     if ((e = set_smem(k_ypass<R, true>, smyi))) return e;
-    launch(k_ypass<R, true>, gyi, FFT_THREADS, smyi, s, W, p.ny, p.My, Kz, p.ry, twy, tkyi, st, sp);
+    launch(k_ypass<R, true>, gyi, FFT_THREADS, smyi, s, W, p.nx, p.ny, p.My, Kz, p.ry, twy, tkyi, st, sp);
     if ((e = set_smem(k_zinv<R>, smz))) return e;
     launch(k_zinv<R>, dim3(gz.x, gz.y, nout), FFT_THREADS, smz, s, W, phi, p.ny, p.nz, p.My, Kz, p.rz, twz, NC, st, sp);
     return cudaGetLastError();
@@ -797,25 +877,23 @@ __global__ void __launch_bounds__(FFT_THREADS) kb_yfwd(const BatchBeam* __restri
                                                        const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_FFT_Y)
-    ypass_body<float, false>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry,
+    ypass_body<float, false>(reinterpret_cast<Cx<float>*>(ws + L.W), p.nx, p.ny, p.My, p.Mz / 2 + 1, p.ry,
                              reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.fft_tky, st, vb);
 }
 
-// inverse y pass: block group 0 takes W (and, with spectral fields, W x D(ky)
-// into W3), group 1 the x-differenced W2 (as k_ypass's blockIdx.z)
+// inverse y pass: block row 0 takes W (and, with spectral fields, W x D(ky)
+// into W3), row 1 the x-differenced W2 (as k_ypass's blockIdx.y)
 __global__ void __launch_bounds__(FFT_THREADS) kb_yinv(const BatchBeam* __restrict__ beams,
                                                        const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_FFT_YI)
     const Spec<float> sp = spec_of<float>(p, L, ws, true);
-    const int f = vb.y / p.nx;
-    const VBlk v = {vb.x, vb.y - f * p.nx, vb.nx, p.nx};
     const Cx<float>* tw = reinterpret_cast<const Cx<float>*>(ws + L.tw_y);
-    if (f == 0)
-        ypass_body<float, true>(reinterpret_cast<Cx<float>*>(ws + L.W), p.ny, p.My, p.Mz / 2 + 1, p.ry, tw,
-                                B.fft_tky, st, v, sp.W3, sp.dy);
+    if (vb.y == 0)
+        ypass_body<float, true>(reinterpret_cast<Cx<float>*>(ws + L.W), p.nx, p.ny, p.My, p.Mz / 2 + 1, p.ry, tw,
+                                B.fft_tky, st, vb, sp.W3, sp.dy);
     else
-        ypass_body<float, true>(sp.W2, p.ny, p.My, p.Mz / 2 + 1, p.ry, tw, B.fft_tky, st, v);
+        ypass_body<float, true>(sp.W2, p.nx, p.ny, p.My, p.Mz / 2 + 1, p.ry, tw, B.fft_tky, st, vb);
 }
 
 __global__ void __launch_bounds__(FFT_THREADS) kb_xconv(const BatchBeam* __restrict__ beams,
@@ -871,12 +949,12 @@ void batch_fft_tiling(BatchBeam& B, size_t smem[3]) {
     B.fft_tkx = strided_cols<float>(p.Mx, nbuf);
     B.gx[BS_FFT_Z] = (p.ny + 2 * B.fft_nc - 1) / (2 * B.fft_nc);
     B.gy[BS_FFT_Z] = p.nx;
-    B.gx[BS_FFT_Y] = (Kz + B.fft_tky - 1) / B.fft_tky;
-    B.gy[BS_FFT_Y] = p.nx;
-    B.gx[BS_FFT_X] = (Kz + B.fft_tkx - 1) / B.fft_tkx;
-    B.gy[BS_FFT_X] = p.My;
+    B.gx[BS_FFT_Y] = (p.nx * Kz + B.fft_tky - 1) / B.fft_tky;  // columns (x, kz)
+    B.gy[BS_FFT_Y] = 1;
+    B.gx[BS_FFT_X] = (p.My * Kz + B.fft_tkx - 1) / B.fft_tkx;  // columns (ky, kz)
+    B.gy[BS_FFT_X] = 1;
     B.gx[BS_FFT_YI] = B.gx[BS_FFT_Y];
-    B.gy[BS_FFT_YI] = p.nx * (p.spectral ? 2 : 1);
+    B.gy[BS_FFT_YI] = p.spectral ? 2 : 1;
     B.gx[BS_FFT_ZI] = B.gx[BS_FFT_Z];
     B.gy[BS_FFT_ZI] = p.nx * (p.spectral ? 3 : 1);  // spectral fields: Ex, Ey, Ez (no potential)
     B.gx[BS_FIELD] = p.ny;

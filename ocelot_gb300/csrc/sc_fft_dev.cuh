@@ -223,4 +223,38 @@ __device__ __forceinline__ void load_twiddles(Cx<R>* dst, const Cx<R>* src, int 
     for (int i = threadIdx.x; i < L; i += blockDim.x) dst[i] = src[i];
 }
 
+// Quotient and remainder of i = start, start + step, start + 2 step, ... by d,
+// carried from one to the next: two divisions per thread instead of one per
+// element in the line-staging loops (d is a run-time line length).
+struct DivWalk {
+    int q, r, dq, dr, d;
+    __device__ __forceinline__ DivWalk(int start, int step, int d_) : d(d_) {
+        q = start / d;
+        r = start - q * d;
+        dq = step / d;
+        dr = step - dq * d;
+    }
+    __device__ __forceinline__ void next() {
+        q += dq;
+        r += dr;
+        if (r >= d) {
+            r -= d;
+            ++q;
+        }
+    }
+};
+
+// Columns of a strided pass: the block's TK columns (TK a power of two) are
+// consecutive entries of a flattened column index, thread t takes column
+// t mod TK and rows t / TK, t / TK + blockDim / TK, ...; no division per element.
+struct ColMap {
+    int kk, r0, rs;
+    __device__ __forceinline__ explicit ColMap(int TK) {
+        const int lg = 31 - __clz(TK);
+        kk = threadIdx.x & (TK - 1);
+        r0 = threadIdx.x >> lg;
+        rs = blockDim.x >> lg;
+    }
+};
+
 }  // namespace ocsc
