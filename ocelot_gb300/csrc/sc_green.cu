@@ -203,21 +203,30 @@ __device__ __forceinline__ void green_z_body(const R* __restrict__ k1, R* __rest
     Cx<R>* B = A + NC * lz;
     load_twiddles<R>(tw, twg, Mz);
     const int x = vb.y, y0 = vb.x * 2 * NC;
-    for (int idx = threadIdx.x; idx < NC * Mz; idx += blockDim.x) {
-        const int c = idx / Mz, z = idx - c * Mz;
-        const int ya = y0 + 2 * c, yb = ya + 1;
-        const int zs = even_src(z, nz, Mz);
-        R re = 0, im = 0;
-        if (zs >= 0 && SC_IDX_OK(st, 33, ((long long)x * ny + (ya < ny ? ya : 0)) * nz + zs, (long long)vb.ny * ny * nz)) {
-            if (ya < ny) re = k1[((size_t)x * ny + ya) * nz + zs];
-            if (yb < ny) im = k1[((size_t)x * ny + yb) * nz + zs];
+    constexpr int U = 4;  // elements per thread per round, their loads issued together
+    for (DivWalk w(threadIdx.x, blockDim.x, Mz); w.q < NC;) {
+        int cs[U], zz[U];
+        R re[U], im[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            cs[u] = w.q;
+            zz[u] = w.r;
+            w.next();
+            const int ya = y0 + 2 * cs[u], yb = ya + 1;
+            const int zs = cs[u] < NC ? even_src(zz[u], nz, Mz) : -1;
+            const bool ok = zs >= 0 && SC_IDX_OK(st, 33, ((long long)x * ny + (ya < ny ? ya : 0)) * nz + zs,
+                                                 (long long)vb.ny * ny * nz);
+            re[u] = (ok && ya < ny) ? k1[((size_t)x * ny + ya) * nz + zs] : (R)0;
+            im[u] = (ok && yb < ny) ? k1[((size_t)x * ny + yb) * nz + zs] : (R)0;
         }
-        A[c * lz + z] = cx<R>(re, im);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (cs[u] < NC) A[cs[u] * lz + zz[u]] = cx<R>(re[u], im[u]);
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, false>(A, B, lz, NC, rz, tw);
-    for (int idx = threadIdx.x; idx < NC * Kz; idx += blockDim.x) {
-        const int c = idx / Kz, k = idx - c * Kz;
+    for (DivWalk w(threadIdx.x, blockDim.x, Kz); w.q < NC; w.next()) {
+        const int c = w.q, k = w.r;
         const int ya = y0 + 2 * c, yb = ya + 1;
         const Cx<R> v = res[c * lz + k];
         if (!SC_IDX_OK(st, 35, ((long long)x * ny + (yb < ny ? yb : ya)) * Kz + k, (long long)vb.ny * ny * Kz)) continue;
@@ -235,11 +244,14 @@ __global__ void __launch_bounds__(GT) k_green_z(const R* __restrict__ k1, R* __r
 }
 
 // S2/S3: strided passes over columns kz (paired), line axis of length n -> M,
-// input rows in[(o*nin + l)*Kz + kz], output rows out[(o*nout + kl)*Kz + kz]
+// input rows in[(o*nin + l)*Kz + kz], output rows out[(o*nout + kl)*Kz + kz].
+// The complex lines are the column pairs (2 pr, 2 pr + 1) of every outer index
+// o < nouter, flattened as o * P + pr (P = ceil(Kz / 2)); block vb.x takes GTK
+// consecutive ones, thread t the line t mod GTK (GTK a power of two).
 template <typename R>
 __device__ __forceinline__ void green_strided_body(const R* __restrict__ in, R* __restrict__ out, int n,
                                                    int nin_stride, int nout, int Kz, int outer_in_stride,
-                                                   int outer_out_stride, const RadixPlan& rp,
+                                                   int outer_out_stride, int nouter, const RadixPlan& rp,
                                                    const Cx<R>* __restrict__ twg, int GTK, const IgfArgs& a,
                                                    const ScState* st, VBlk vb) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -249,41 +261,48 @@ __device__ __forceinline__ void green_strided_body(const R* __restrict__ in, R* 
     Cx<R>* A = tw + M;
     Cx<R>* B = A + GTK * ls;
     load_twiddles<R>(tw, twg, M);
-    const int o = vb.y;
-    const int k0 = vb.x * 2 * GTK;
+    const ColMap cm(GTK);
+    const int P = (Kz + 1) / 2;
+    const int f = vb.x * GTK + cm.kk;
+    const bool live = f < nouter * P;
+    const int o = f / P, pr = f - o * P;
+    const int ka = 2 * pr, kb = ka + 1;
     const R* src = in + (size_t)o * outer_in_stride;
     R* dst = out + (size_t)o * outer_out_stride;
-    for (int idx = threadIdx.x; idx < M * GTK; idx += blockDim.x) {
-        const int l = idx / GTK, kk = idx - l * GTK;
-        const int ka = k0 + 2 * kk, kb = ka + 1;
-        const int ls_ = even_src(l, n, M);
-        R re = 0, im = 0;
-        if (ls_ >= 0) {
-            if (ka < Kz) re = src[(size_t)ls_ * nin_stride + ka];
-            if (kb < Kz) im = src[(size_t)ls_ * nin_stride + kb];
+    Cx<R>* la = A + cm.kk * ls;
+    constexpr int U = 8;  // rows per round: their loads are issued together
+    for (int l0 = cm.r0; l0 < M; l0 += U * cm.rs) {
+        R re[U], im[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int l = l0 + u * cm.rs;
+            const int lsrc = (live && l < M) ? even_src(l, n, M) : -1;
+            re[u] = (lsrc >= 0 && ka < Kz) ? src[(size_t)lsrc * nin_stride + ka] : (R)0;
+            im[u] = (lsrc >= 0 && kb < Kz) ? src[(size_t)lsrc * nin_stride + kb] : (R)0;
         }
-        A[kk * ls + l] = cx<R>(re, im);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (l0 + u * cm.rs < M) la[l0 + u * cm.rs] = cx<R>(re[u], im[u]);
     }
     __syncthreads();
     Cx<R>* res = fft_lines<R, false>(A, B, ls, GTK, rp, tw);
-    for (int idx = threadIdx.x; idx < nout * GTK; idx += blockDim.x) {
-        const int l = idx / GTK, kk = idx - l * GTK;
-        const int ka = k0 + 2 * kk, kb = ka + 1;
-        const Cx<R> v = res[kk * ls + l];
-        if (ka < Kz) dst[(size_t)l * nin_stride + ka] = v.x;
-        if (kb < Kz) dst[(size_t)l * nin_stride + kb] = v.y;
-    }
+    if (live)
+        for (int l = cm.r0; l < nout; l += cm.rs) {
+            const Cx<R> v = res[cm.kk * ls + l];
+            if (ka < Kz) dst[(size_t)l * nin_stride + ka] = v.x;
+            if (kb < Kz) dst[(size_t)l * nin_stride + kb] = v.y;
+        }
 }
 
 template <typename R>
 __global__ void __launch_bounds__(GT) k_green_strided(const R* __restrict__ in, R* __restrict__ out, int n,
                                                       int nin_stride, int nout, int Kz, int outer_in_stride,
-                                                      int outer_out_stride, RadixPlan rp,
+                                                      int outer_out_stride, int nouter, RadixPlan rp,
                                                       const Cx<R>* __restrict__ twg, int GTK, IgfArgs a,
                                                       const ScState* st) {
     pdl_wait();
-    green_strided_body<R>(in, out, n, nin_stride, nout, Kz, outer_in_stride, outer_out_stride, rp, twg, GTK, a, st,
-                          hw_vblk());
+    green_strided_body<R>(in, out, n, nin_stride, nout, Kz, outer_in_stride, outer_out_stride, nouter, rp, twg, GTK,
+                          a, st, hw_vblk());
 }
 
 
@@ -361,11 +380,13 @@ static cudaError_t spectrum_t(const Plan& p, const Layout& L, char* ws, cudaStre
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
     const size_t smx = sizeof(Cx<R>) * (size_t)(p.Mx + 2 * tkx * fft_ls(p.Mx));
     if ((e = set_smem(k_green_strided<R>, smx > smy ? smx : smy))) return e;
-    dim3 gy((Kz + 2 * tky - 1) / (2 * tky), p.nx);
-    launch(k_green_strided<R>, gy, GT, smy, s, s1, s2, p.ny, Kz, Ky, Kz, p.ny * Kz, Ky * Kz, p.ry, twy, tky, a, st);
+    const int P = (Kz + 1) / 2;  // column pairs per outer index
+    dim3 gy((p.nx * P + tky - 1) / tky);
+    launch(k_green_strided<R>, gy, GT, smy, s, s1, s2, p.ny, Kz, Ky, Kz, p.ny * Kz, Ky * Kz, p.nx, p.ry, twy, tky, a,
+           st);
     // S3 along x: for each ky, rows x < nx of S2[.][ky] -> rows kx < Kx of G[.][ky]
-    dim3 gx((Kz + 2 * tkx - 1) / (2 * tkx), Ky);
-    launch(k_green_strided<R>, gx, GT, smx, s, s2, g, p.nx, Ky * Kz, Kx, Kz, Kz, Kz, p.rx, twx, tkx, a, st);
+    dim3 gx((Ky * P + tkx - 1) / tkx);
+    launch(k_green_strided<R>, gx, GT, smx, s, s2, g, p.nx, Ky * Kz, Kx, Kz, Kz, Kz, Ky, p.rx, twx, tkx, a, st);
     return cudaGetLastError();
 }
 
@@ -447,11 +468,11 @@ __global__ void __launch_bounds__(GT) kb_green_strided(const BatchBeam* __restri
     if (AXIS == 1)
         green_strided_body<float>(reinterpret_cast<const float*>(ws + L.green_s1),
                                   reinterpret_cast<float*>(ws + L.green_s2), p.ny, Kz, Ky, Kz, p.ny * Kz, Ky * Kz,
-                                  p.ry, reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.green_tky,
+                                  p.nx, p.ry, reinterpret_cast<const Cx<float>*>(ws + L.tw_y), B.green_tky,
                                   batch_igf_args(p, 0), st, vb);
     else
         green_strided_body<float>(reinterpret_cast<const float*>(ws + L.green_s2),
-                                  reinterpret_cast<float*>(ws + L.green), p.nx, Ky * Kz, Kx, Kz, Kz, Kz, p.rx,
+                                  reinterpret_cast<float*>(ws + L.green), p.nx, Ky * Kz, Kx, Kz, Kz, Kz, Ky, p.rx,
                                   reinterpret_cast<const Cx<float>*>(ws + L.tw_x), B.green_tkx, batch_igf_args(p, 0),
                                   st, vb);
 }
@@ -477,10 +498,11 @@ void batch_green_tiling(BatchBeam& B, size_t smem[3]) {
     B.gy[BS_IGF_D] = 1;
     B.gx[BS_GREEN_Z] = (p.ny + 2 * B.green_nc - 1) / (2 * B.green_nc);
     B.gy[BS_GREEN_Z] = p.nx;
-    B.gx[BS_GREEN_Y] = (Kz + 2 * B.green_tky - 1) / (2 * B.green_tky);
-    B.gy[BS_GREEN_Y] = p.nx;
-    B.gx[BS_GREEN_X] = (Kz + 2 * B.green_tkx - 1) / (2 * B.green_tkx);
-    B.gy[BS_GREEN_X] = Ky;
+    const int P = (Kz + 1) / 2;  // column pairs per outer index
+    B.gx[BS_GREEN_Y] = (p.nx * P + B.green_tky - 1) / B.green_tky;
+    B.gy[BS_GREEN_Y] = 1;
+    B.gx[BS_GREEN_X] = (Ky * P + B.green_tkx - 1) / B.green_tkx;
+    B.gy[BS_GREEN_X] = 1;
     smem[0] = sizeof(Cx<float>) * (size_t)(p.Mz + 2 * B.green_nc * fft_ls(p.Mz));
     smem[1] = sizeof(Cx<float>) * (size_t)(p.My + 2 * B.green_tky * fft_ls(p.My));
     smem[2] = sizeof(Cx<float>) * (size_t)(p.Mx + 2 * B.green_tkx * fft_ls(p.Mx));

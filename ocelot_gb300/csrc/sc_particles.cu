@@ -1622,63 +1622,97 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
     const float ig0 = st->ig0f, g0 = st->g0f;
     const int S = st->qfix_shift;
     bool bad = false;
-    PAIR_LOOP_BEGIN(n)
-    float v[3][2];
-    for (int j = 0; j < 3; ++j) ld_rowf(X + j * nX, i0_, pair_, v[j][0], v[j][1]);
-    double qq[2] = {0.0, 0.0};
-    if (qfix) ld_row(q, i0_, pair_, qq[0], qq[1]);
-    uint32_t key2[2] = {0u, 0u};
-    float g2[3][2];
-    for (int w = 0; w < W_; ++w) {
-        const int64_t i = i0_ + w;
-        const float v0 = v[0][w], v1 = v[1][w], v2 = v[2][w];
-        const float nrm = sqrtf_fast(fmaf(v0, v0, fmaf(v1, v1, (v2 * ig0) * (v2 * ig0))));  // |lab position|
-        float g[3] = {grid32(v0, is[0], of[0]), grid32(v1, is[1], of[1]), grid32(v2, is[2], of[2])};
-        bool amb = false;
-        for (int j = 0; j < 3; ++j) {
-            const float scale = (j == 2 ? nrm * g0 : nrm) * is[j] + fabsf(of[j]) + 1.0f;
-            // 16 units in the last place of the scale: 2x the error bound of g
-            // (FP32 position with approximate momenta, product, difference)
-            const float tol = ldexpf(scale, -19);
-            const float f = g[j] - floorf(g[j]);
-            amb |= !(f >= tol && f <= 1.0f - tol);
-        }
-        uint32_t key = 0u;
-        bool deferred = false;
-        if (amb && rp) {
-            const int slot = atomicAdd(&s_nfine, 1);
-            if (slot < KEYS_FINE) {
-                s_fine[slot] = (uint32_t)i;  // n < 2^31
-                deferred = true;
+    // the pair loop of PAIR_LOOP_BEGIN, KG pairs per thread per round: the
+    // loads of all KG pairs are issued before the first is processed, so a
+    // thread keeps KG times the bytes in flight
+    constexpr int KG = 2;
+    const int64_t npair_ = VEC ? n / 2 : n;
+    const int64_t ntot_ = npair_ + ((VEC && (n & 1)) ? 1 : 0);
+    const int64_t pstride_ = (int64_t)vb.nx * blockDim.x;
+    for (int64_t pg_ = vb.x * (int64_t)blockDim.x + threadIdx.x; pg_ < ntot_; pg_ += KG * pstride_) {
+        unsigned slow = 0u;  // bit 2u + w: particle w of pair u takes the estimate after the round
+        float vg[KG][3][2];
+        double qg[KG][2];
+#pragma unroll
+        for (int u = 0; u < KG; ++u) {
+            const int64_t p_ = pg_ + u * pstride_;
+            const bool pair_ = VEC && p_ < npair_;
+            const int64_t i0_ = pair_ ? 2 * p_ : (VEC ? n - 1 : p_);
+            qg[u][0] = qg[u][1] = 0.0;
+            if (p_ < ntot_) {
+                for (int j = 0; j < 3; ++j) ld_rowf(X + j * nX, i0_, pair_, vg[u][j][0], vg[u][j][1]);
+                if (qfix) ld_row(q, i0_, pair_, qg[u][0], qg[u][1]);
             }
         }
-        if (amb && rp && !deferred) {
+#pragma unroll
+        for (int u = 0; u < KG; ++u) {
+            const int64_t p_ = pg_ + u * pstride_;
+            if (p_ >= ntot_) break;
+            const bool pair_ = VEC && p_ < npair_;
+            const int64_t i0_ = pair_ ? 2 * p_ : (VEC ? n - 1 : p_);
+            const int W_ = pair_ ? 2 : 1;
+            float (&v)[3][2] = vg[u];
+            double (&qq)[2] = qg[u];
+            uint32_t key2[2] = {0u, 0u};
+            float g2[3][2];
+            for (int w = 0; w < W_; ++w) {
+                const int64_t i = i0_ + w;
+                const float v0 = v[0][w], v1 = v[1][w], v2 = v[2][w];
+                const float nrm = sqrtf_fast(fmaf(v0, v0, fmaf(v1, v1, (v2 * ig0) * (v2 * ig0))));  // |lab position|
+                float g[3] = {grid32(v0, is[0], of[0]), grid32(v1, is[1], of[1]), grid32(v2, is[2], of[2])};
+                bool amb = false;
+                for (int j = 0; j < 3; ++j) {
+                    const float scale = (j == 2 ? nrm * g0 : nrm) * is[j] + fabsf(of[j]) + 1.0f;
+                    // 16 units in the last place of the scale: 2x the error bound of g
+                    // (FP32 position with approximate momenta, product, difference)
+                    const float tol = ldexpf(scale, -19);
+                    const float f = g[j] - floorf(g[j]);
+                    amb |= !(f >= tol && f <= 1.0f - tol);
+                }
+                uint32_t key = 0u;
+                bool deferred = false;
+                if (amb && rp) {
+                    const int slot = atomicAdd(&s_nfine, 1);
+                    if (slot < KEYS_FINE) s_fine[slot] = (uint32_t)i;  // n < 2^31
+                    else slow |= 1u << (2 * u + w);                    // the list is full: after this round
+                    deferred = true;
+                }
+                if (!deferred) {
+                    bad |= !key_of_f(floorf(g[0]) + 1.f, floorf(g[1]) + 1.f, floorf(g[2]) + 1.f, kp, key);
+                    if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
+                        atomicAdd(qfix + key, (unsigned long long)to_fixed(qq[w], S));
+                }
+                key2[w] = key;
+                for (int j = 0; j < 3; ++j) g2[j][w] = g[j];
+            }
+            if (pair_) *reinterpret_cast<uint2*>(keys + i0_) = make_uint2(key2[0], key2[1]);
+            else keys[i0_] = key2[0];
+            // the el_field entry gathers at the stored grid coordinates; the kick
+            // recomputes them from rparticles
+            if (!rp)
+                for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
+        }
+        // near-face particles beyond the block's list (degenerate beams only):
+        // the FP32-corrected estimate alone, out of the unrolled loop
+        while (slow) {
+            const int bit = __ffs(slow) - 1;
+            slow &= slow - 1;
+            const int64_t p_ = pg_ + (bit >> 1) * pstride_;
+            const int64_t i = (VEC && p_ < npair_ ? 2 * p_ : (VEC ? n - 1 : p_)) + (bit & 1);
             double T[3][3];
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
-            double xv[3];
+            double xv[3], e[3];
             xyz_fine32(rp, ld, i, kp, T, st->gamma0, xv);
-            double e[3];
-            for (int j = 0; j < 3; ++j) {  // the FP64 form's grid coordinate (k_keys64)
+            for (int j = 0; j < 3; ++j)  // the FP64 form's grid coordinate (k_keys64)
                 e[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
-                g[j] = (float)e[j];
-            }
+            uint32_t key = 0u;
             bad |= !key_of(floor(e[0]) + 1, floor(e[1]) + 1, floor(e[2]) + 1, kp, key);
-        } else {
-            bad |= !key_of_f(floorf(g[0]) + 1.f, floorf(g[1]) + 1.f, floorf(g[2]) + 1.f, kp, key);
+            keys[i] = key;
+            if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
+                atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
         }
-        if (qfix && !deferred && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
-            atomicAdd(qfix + key, (unsigned long long)to_fixed(qq[w], S));
-        key2[w] = key;
-        for (int j = 0; j < 3; ++j) g2[j][w] = g[j];
     }
-    if (pair_) *reinterpret_cast<uint2*>(keys + i0_) = make_uint2(key2[0], key2[1]);
-    else keys[i0_] = key2[0];
-    // the el_field entry gathers at the stored grid coordinates; the kick
-    // recomputes them from rparticles
-    if (!rp)
-        for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
-    PAIR_LOOP_END
     // the listed particles: key from the FP64 coordinates and the deposit;
     // one per thread, so the block waits for one slow FP64 evaluation
     // instead of each warp stalling on its own
