@@ -95,6 +95,12 @@ int sc_read_status(const sc_plan* plan, void* ws, void* stream);
  * before the gamma0 factor (sc.py:201-204) -- as 3 rows of nX = n rounded up
  * to a multiple of 4 (double for SC_FP64, float for SC_FP32). */
 #define SC_REGION_FIELD 8
+/* SC_REGION_IGF: the cell integrals of the Green's function of the last
+ * call, [nx][ny][nz] in the plan's precision (FP32 form: the hybrid table of
+ * 8-corner FP64 differences near the origin, the line form across and the
+ * multipole form beyond; the table is rebuilt only when the mesh step
+ * changes). */
+#define SC_REGION_IGF 9
 int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t* offset, int64_t* bytes);
 
 /* ---- the kick ---------------------------------------------------------- */
@@ -357,6 +363,14 @@ int sc_kick_launches(const sc_plan* plan);
  *     through the same transform code either way: identical results. */
 #define SC_PARAM_FFT_PLANE_FWD 2
 #define SC_PARAM_FFT_PLANE_INV 3
+/*   SC_PARAM_FFT_COLS_X / SC_PARAM_FFT_COLS_Y: lines (columns of the work
+ *     grid) per block of the x pass and of the separate y passes: 2, 4, 8 or
+ *     16, or 0 (default) for as many as fit, up to 16.  Fewer columns per
+ *     block take less shared memory, so more blocks share an SM.  The lines
+ *     are independent: identical results.  A batched kick also caps them so
+ *     that four blocks share an SM. */
+#define SC_PARAM_FFT_COLS_X 4
+#define SC_PARAM_FFT_COLS_Y 5
 #define SC_KICK_NVARIANTS 16
 int sc_plan_set_param(sc_plan* plan, int param, int value);
 int sc_plan_get_param(const sc_plan* plan, int param, int* value);

@@ -34,6 +34,8 @@ SC_PARAM_KICK_VARIANT = 0
 SC_PARAM_RECORD_FIELD = 1
 SC_PARAM_FFT_PLANE_FWD = 2
 SC_PARAM_FFT_PLANE_INV = 3
+SC_PARAM_FFT_COLS_X = 4
+SC_PARAM_FFT_COLS_Y = 5
 SC_KICK_NVARIANTS = 16
 
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
@@ -41,7 +43,8 @@ SC_WAIT_FRAME = 0
 SC_WAIT_EXTENT = 1
 SC_WAIT_KICK = 2
 
-REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7, "field": 8}
+REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7, "field": 8,
+           "igf": 9}
 
 ERROR_TEXT = {
     SC_ERR_DEGENERATE: "degenerate beam: zero or non-finite extent or total charge (mesh step would be 0)",

@@ -75,6 +75,7 @@ class BeamBatch:
         if engine is None:
             engine = Engine(tuple(int(v) for v in nmesh_xyz), "fp32", self.device, self.mode)
         engine.ensure(n)
+        engine.apply_tuning(n)  # the beam's FFT tiling in the batched passes
         self.beams.append((engine, rparticles, q_array, float(energy_gev), float(zstep), tmap))
         self._table = None
         return len(self.beams) - 1

@@ -359,6 +359,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     for (int k = 0; k < 3; ++k) p.wait_limit[k] = MBAR_WAIT_LIMIT;
     p.kick_variant = default_kick_variant();
     p.fft_plane_fwd = p.fft_plane_inv = 1;
+    p.fft_cols_x = p.fft_cols_y = 0;
     // everything that is not a stream operation happens here, so that kicks
     // can be recorded in a CUDA graph
     SC_CUDA(prepare_fft_kernels(p), "kernel attributes");
@@ -462,6 +463,12 @@ int sc_plan_set_param(sc_plan* plan, int param, int value) {
             if (value != 0 && value != 1) return fail(SC_ERR_ARG, "FFT plane parameter must be 0 or 1");
             (param == SC_PARAM_FFT_PLANE_FWD ? plan->p.fft_plane_fwd : plan->p.fft_plane_inv) = value;
             return SC_OK;
+        case SC_PARAM_FFT_COLS_X:
+        case SC_PARAM_FFT_COLS_Y:
+            if (value != 0 && value != 2 && value != 4 && value != 8 && value != 16)
+                return fail(SC_ERR_ARG, "FFT columns per block must be 0, 2, 4, 8 or 16");
+            (param == SC_PARAM_FFT_COLS_X ? plan->p.fft_cols_x : plan->p.fft_cols_y) = value;
+            return SC_OK;
         default: return fail(SC_ERR_ARG, "unknown plan parameter %d", param);
     }
 }
@@ -473,6 +480,8 @@ int sc_plan_get_param(const sc_plan* plan, int param, int* value) {
         case SC_PARAM_RECORD_FIELD: *value = plan->p.record_field; return SC_OK;
         case SC_PARAM_FFT_PLANE_FWD: *value = plan->p.fft_plane_fwd; return SC_OK;
         case SC_PARAM_FFT_PLANE_INV: *value = plan->p.fft_plane_inv; return SC_OK;
+        case SC_PARAM_FFT_COLS_X: *value = plan->p.fft_cols_x; return SC_OK;
+        case SC_PARAM_FFT_COLS_Y: *value = plan->p.fft_cols_y; return SC_OK;
         default: return fail(SC_ERR_ARG, "unknown plan parameter %d", param);
     }
 }
@@ -539,6 +548,7 @@ int sc_workspace_region(const sc_plan* plan, int64_t n_max, int region, int64_t*
             *offset = (int64_t)(L.state + offsetof(ScState, first_error));
             *bytes = (int64_t)sizeof(int);
             break;
+        case SC_REGION_IGF: *offset = (int64_t)L.igf_k1; *bytes = (int64_t)(rs * ncell); break;
         default: return fail(SC_ERR_ARG, "unknown region %d", region);
     }
     return SC_OK;

@@ -67,6 +67,10 @@ struct ScState {
     // near box of the hybrid Green's function (cells with all indices below
     // it use the FP64 8-corner formula)
     int igf_box[3];
+    // cells long along z (hz the largest step): the transverse near box of
+    // the line form (igf_line_of)
+    int igf_line;
+    int igf_tbox[2];
     unsigned int done_frame;     // blocks finished, for the last-block reductions
     unsigned int done_extent;
     unsigned int kick_next;      // tiles claimed by the gather + kick (reset by the frame finalize)
@@ -84,6 +88,23 @@ constexpr int WS_MAGIC = 0x5c6b0e11;
 // integral is within 5e-8 of the exact integral (checked against an
 // extended-precision IGF).  Written into the state once per kick by the
 // kernel that sets the mesh step.
+// Cells long along z (hz >= hx, hy; every relativistic beam whose bunch is
+// not much shorter than it is wide): the near box along z keeps its
+// ceil(5 hz / hz) + 1 = 6 cells, but across it only the cells within
+// ceil(5 ht / h) + 1 of the axis (ht = max(hx, hy)) need the 8-corner
+// formula.  The cells of the first six z planes farther out are at least
+// 5 ht from the z axis, where the line form of the cell integral (exact
+// along z, Gauss-Legendre across) is within FP32 rounding of the exact
+// integral (igf_line in sc_green.cu).  axis 0 or 1; FP32 arithmetic with a
+// relative margin of 2^-20 (the box is at most one cell larger than exact).
+__device__ __forceinline__ bool igf_line_of(const double (&h)[3]) { return h[2] >= h[0] && h[2] >= h[1]; }
+__device__ __forceinline__ int igf_tbox_of(const double (&h)[3], int axis, int n) {
+    const float ht = (float)fmax(h[0], h[1]);
+    const float v = 5.0f * ht / (float)h[axis] * (1.0f + 0x1p-20f);
+    const int b = v >= (float)n ? n : (int)ceilf(v) + 1;
+    return b > n ? n : b;
+}
+
 __device__ __forceinline__ void igf_box_of(const double (&h)[3], int nx, int ny, int nz, int (&b)[3]) {
     const double hm = fmax(h[0], fmax(h[1], h[2]));
     const int n[3] = {nx, ny, nz};
@@ -171,6 +192,8 @@ struct Plan {
     int record_field;        // the kick also stores the field at each particle (SC_REGION_FIELD)
     int fft_plane_fwd;       // 1: plane-fused z + y forward passes where the plane fits, 0: separate passes
     int fft_plane_inv;       // 1: plane-fused y + z inverse passes where the plane fits, 0: separate passes
+    int fft_cols_x;          // columns per block of the x pass (0: as many as fit, up to 16)
+    int fft_cols_y;          // columns per block of the separate y passes (0: as many as fit, up to 16)
 };
 // tile, tile buffers, particles per thread and blocks per SM of kick variant v (0 if v is out of range)
 int kick_variant_info(int v, int* tile, int* stages, int* ppt, int* minb);

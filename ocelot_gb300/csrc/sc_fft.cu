@@ -39,6 +39,14 @@ static inline int strided_cols(int M, int nbuf = 2) {
     while (tk > 2 && sizeof(Cx<R>) * (size_t)(M + nbuf * tk * fft_ls(M)) > 200 * 1024) tk /= 2;
     return tk;
 }
+// the plan's columns per block (SC_PARAM_FFT_COLS_X / _Y; 0: strided_cols),
+// never more than fit.  The columns are independent lines, so the grouping
+// changes no result.
+template <typename R>
+static inline int pass_cols(int want, int M, int nbuf = 2) {
+    const int fit = strided_cols<R>(M, nbuf);
+    return (want > 0 && want < fit) ? want : fit;
+}
 
 // Spectral fields (FP32 with SC_FP32_SPECTRAL_FIELDS).  The field grids are
 // forward differences of the potential, Ex[i] = (phi[i] - phi[i+1]) / hx
@@ -751,8 +759,8 @@ static cudaError_t convolve_t(const Plan& p, const Layout& L, char* ws, R* qgrid
     const int NC = z_lines_per_block(p.Mz);
     const size_t smz = sizeof(Cx<R>) * (size_t)(p.Mz + 2 * NC * fft_ls(p.Mz));
     dim3 gz((p.ny + 2 * NC - 1) / (2 * NC), p.nx);
-    const int tky = strided_cols<R>(p.My), tkx = strided_cols<R>(p.Mx, nbuf);
-    const int tkyi = strided_cols<R>(p.My, nbuf);  // the y inverse
+    const int tky = pass_cols<R>(p.fft_cols_y, p.My), tkx = pass_cols<R>(p.fft_cols_x, p.Mx, nbuf);
+    const int tkyi = pass_cols<R>(p.fft_cols_y, p.My, nbuf);  // the y inverse
     const size_t smy = sizeof(Cx<R>) * (size_t)(p.My + 2 * tky * fft_ls(p.My));
     const size_t smyi = sizeof(Cx<R>) * (size_t)(p.My + nbuf * tkyi * fft_ls(p.My));
     const int ycols = p.nx * Kz;  // the y passes' columns (x, kz)
@@ -940,13 +948,23 @@ __global__ void kb_field_octs(const BatchBeam* __restrict__ beams, const int* __
 }
 #undef BATCH_BEAM
 
+// A batched launch gives every block the largest dynamic shared memory of
+// its beams, so one beam with long lines would set the occupancy of all the
+// others: the batch caps each beam's strided-pass blocks at what lets four
+// blocks share an SM (228 KB per SM, 1 KB reserved per block).
+constexpr size_t BATCH_FFT_SMEM = 233472 / 4 - 1024;
+static int batch_cols(int tk, int M, int nbuf) {
+    while (tk > 2 && sizeof(Cx<float>) * (size_t)(M + nbuf * tk * fft_ls(M)) > BATCH_FFT_SMEM) tk /= 2;
+    return tk;
+}
+
 void batch_fft_tiling(BatchBeam& B, size_t smem[3]) {
     const Plan& p = B.p;
     const int Kz = p.Mz / 2 + 1;
     const int nbuf = p.spectral ? 3 : 2;  // line buffers of the x pass and the y passes
     B.fft_nc = z_lines_per_block(p.Mz);
-    B.fft_tky = strided_cols<float>(p.My, nbuf);
-    B.fft_tkx = strided_cols<float>(p.Mx, nbuf);
+    B.fft_tky = batch_cols(pass_cols<float>(p.fft_cols_y, p.My, nbuf), p.My, nbuf);
+    B.fft_tkx = batch_cols(pass_cols<float>(p.fft_cols_x, p.Mx, nbuf), p.Mx, nbuf);
     B.gx[BS_FFT_Z] = (p.ny + 2 * B.fft_nc - 1) / (2 * B.fft_nc);
     B.gy[BS_FFT_Z] = p.nx;
     B.gx[BS_FFT_Y] = (p.nx * Kz + B.fft_tky - 1) / B.fft_tky;  // columns (x, kz)

@@ -46,11 +46,13 @@ __device__ __forceinline__ void igf_spacing(const ScState* st, const IgfArgs& a,
 
 // Near box of the hybrid table (igf_box_of in sc_common.cuh): computed once
 // per kick with the mesh step and kept in the state; the full octant when
-// the table is exact
+// the table is exact.  Cells long along z take the transverse box of the
+// line form (igf_tbox_of).
 __device__ __forceinline__ void igf_box(const ScState* st, int nx, int ny, int nz, int hybrid, int b[3]) {
     if (!hybrid) { b[0] = nx; b[1] = ny; b[2] = nz; return; }
-    b[0] = st->igf_box[0];
-    b[1] = st->igf_box[1];
+    const bool line = st->igf_line;
+    b[0] = line ? st->igf_tbox[0] : st->igf_box[0];
+    b[1] = line ? st->igf_tbox[1] : st->igf_box[1];
     b[2] = st->igf_box[2];
 }
 
@@ -65,10 +67,88 @@ __device__ __forceinline__ double igf_point(double x, double y, double z) {
     return __dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(t1, t2), t3), t4), t5), t6);
 }
 
+// Line form of the integral of 1/r over the cell centred at (X, Y, Z >= 0)
+// with half-widths (a, b, c), for cells at least 5 max(2a, 2b) from the z
+// axis: exact along z,
+//   L(rho) = asinh((Z + c) / rho) - asinh((Z - c) / rho),
+// and the 3 x 3 Gauss-Legendre product rule across the cell (the transverse
+// integrand is smooth there: the rule's error is below 1e-10 relative).  L is
+// formed without cancellation: for Z > c as log1p(r - 1) of the ratio
+// r = (u + su) / (v + sv), u, v = (Z +- c) / rho, su, sv = sqrt(1 + u^2),
+// sqrt(1 + v^2), with
+//   r - 1 = (2c / rho) (1 + (u + v) / (su + sv)) / (v + sv);
+// for Z <= c as asinh(u) + asinh(-v).  Every term is positive, so the FP32
+// result is within a few roundings (2e-7 relative, checked against a
+// 40-digit evaluation of the 8-corner formula) of the exact integral.
+__device__ __forceinline__ float line_L(float r2, float Z, float c) {
+    const float irho = 1.0f / sqrtf(r2);
+    const float u = (Z + c) * irho, v = (Z - c) * irho;
+    if (!(v > 0.0f)) return asinhf(u) + asinhf(-v);
+    const float su = sqrtf(1.0f + u * u), sv = sqrtf(1.0f + v * v);
+    return log1pf((2.0f * c * irho) * (1.0f + (u + v) / (su + sv)) / (v + sv));
+}
+__device__ __forceinline__ float cell_line(float X, float Y, float Z, float a, float b, float c) {
+    const float t[3] = {-0.77459666924148337704f, 0.0f, 0.77459666924148337704f};  // +-sqrt(3/5), 0
+    const float w[3] = {0.55555555555555555556f, 0.88888888888888888889f, 0.55555555555555555556f};
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float x = X + a * t[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float y = Y + b * t[j];
+            s = s + (w[i] * w[j]) * line_L(x * x + y * y, Z, c);
+        }
+    }
+    return a * b * s;
+}
+
+// One of the six terms of igf_point (term 0..5: t1..t6), with the same
+// operations, so that their sum in igf_point's order is its result bit for
+// bit.  Terms 0, 2, 4 take an arctangent, 1, 3, 5 a logarithm.
+__device__ __forceinline__ double igf_term(double x, double y, double z, int term) {
+    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    switch (term) {
+        case 0: return __dmul_rn(__dmul_rn(__dmul_rn(-x, x), 0.5), atan(__ddiv_rn(__dmul_rn(y, z), __dmul_rn(x, r))));
+        case 1: return __dmul_rn(__dmul_rn(y, z), log(__dadd_rn(x, r)));
+        case 2: return __dmul_rn(__dmul_rn(__dmul_rn(y, y), 0.5), atan(__ddiv_rn(__dmul_rn(z, x), __dmul_rn(y, r))));
+        case 3: return __dmul_rn(__dmul_rn(z, x), log(__dadd_rn(y, r)));
+        case 4: return __dmul_rn(__dmul_rn(__dmul_rn(z, z), 0.5), atan(__ddiv_rn(__dmul_rn(x, y), __dmul_rn(z, r))));
+        default: return __dmul_rn(__dmul_rn(x, y), log(__dadd_rn(z, r)));
+    }
+}
+
+// corner c of a box with corner strides (cy1 * cz1, cz1, 1): its coordinates
+__device__ __forceinline__ void igf_corner_xyz(unsigned c, int cy1, int cz1, double hx, double hy, double hz,
+                                               double& x, double& y, double& z) {
+    const unsigned t = c / (unsigned)cz1;
+    const int k = (int)(c - t * (unsigned)cz1);
+    const int i = (int)(t / (unsigned)cy1);
+    const int j = (int)(t - (unsigned)i * cy1);
+    x = __dsub_rn(__dmul_rn(hx, (double)i), __dmul_rn(hx, 0.5));
+    y = __dsub_rn(__dmul_rn(hy, (double)j), __dmul_rn(hy, 0.5));
+    z = __dsub_rn(__dmul_rn(hz, (double)k), __dmul_rn(hz, 0.5));
+}
+
+constexpr int IGF_THREADS = 256;
+constexpr int IGF_SPLIT = IGF_THREADS / 6;  // corners per block per round in the split form
+
 // IG on the corners of the near box (the whole octant when not hybrid),
-// stored with the box's corner strides
-__device__ __forceinline__ void igf_corners_body(double* __restrict__ ig, int nx, int ny, int nz, const IgfArgs& a,
-                                                 const ScState* st, VBlk vb) {
+// stored with the box's corner strides.
+// The whole octant (the exact table): one thread per corner, bound by the
+// FP64 pipe.  The near box of the hybrid table has a few hundred corners, so
+// the time is the latency of one igf_point -- on this GPU's narrow FP64 pipe
+// some 20 us of dependent arithmetic through three arctangents and three
+// logarithms.  There each corner's six terms go to six threads (the
+// arctangents in one half of the block, the logarithms in the other, so no
+// warp runs both) and a seventh sums them in igf_point's order through shared
+// memory: the same bits in a third of the time.  For cells long along z the
+// line-form cells of the table (k1) are computed by the other blocks of the
+// same launch meanwhile; blocks [0, bc) take the corners.
+template <typename R>
+__device__ __forceinline__ void igf_corners_body(double* __restrict__ ig, R* __restrict__ k1, int nx, int ny, int nz,
+                                                 const IgfArgs& a, const ScState* st, VBlk vb) {
+    __shared__ double terms[6 * IGF_SPLIT];
     if (igf_skip(st, a)) return;
     double hx, hy, hz;
     igf_spacing(st, a, hx, hy, hz);
@@ -77,22 +157,71 @@ __device__ __forceinline__ void igf_corners_body(double* __restrict__ ig, int nx
     const int cx1 = b[0] + 1, cy1 = b[1] + 1, cz1 = b[2] + 1;
     // 32-bit index arithmetic: a mesh has fewer than 2^31 corners
     const unsigned total = (unsigned)cx1 * cy1 * cz1;
-    for (unsigned c = vb.x * blockDim.x + threadIdx.x; c < total; c += vb.nx * blockDim.x) {
-        const unsigned t = c / (unsigned)cz1;
-        const int k = (int)(c - t * (unsigned)cz1);
-        const int i = (int)(t / (unsigned)cy1);
-        const int j = (int)(t - (unsigned)i * cy1);
-        const double x = __dsub_rn(__dmul_rn(hx, (double)i), __dmul_rn(hx, 0.5));
-        const double y = __dsub_rn(__dmul_rn(hy, (double)j), __dmul_rn(hy, 0.5));
-        const double z = __dsub_rn(__dmul_rn(hz, (double)k), __dmul_rn(hz, 0.5));
-        if (!SC_IDX_OK(st, 31, c, (long long)(nx + 1) * (ny + 1) * (nz + 1))) continue;
-        ig[c] = igf_point(x, y, z);
+    const long long all = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+    if (!a.hybrid) {
+        for (unsigned c = vb.x * blockDim.x + threadIdx.x; c < total; c += vb.nx * blockDim.x) {
+            double x, y, z;
+            igf_corner_xyz(c, cy1, cz1, hx, hy, hz, x, y, z);
+            if (!SC_IDX_OK(st, 31, c, all)) continue;
+            ig[c] = igf_point(x, y, z);
+        }
+        return;
+    }
+    const bool line = st->igf_line;
+    const int nblk = vb.nx;
+    int bc = nblk;  // blocks on the corners
+    if (line && nblk > 1) {
+        const int want = (int)((total + IGF_SPLIT - 1) / IGF_SPLIT);
+        bc = want < nblk - 1 ? want : nblk - 1;
+    }
+    if (vb.x < bc) {
+        // term m of corner e of the round: thread (m % 2) * 3 * IGF_SPLIT + (m / 2) * IGF_SPLIT + e
+        const int tid = threadIdx.x;
+        const int half = tid / (3 * IGF_SPLIT), rem = tid - half * 3 * IGF_SPLIT;
+        const int m = 2 * (rem / IGF_SPLIT) + half, e = rem % IGF_SPLIT;  // m: 0,2,4 atan; 1,3,5 log
+        for (unsigned c0 = vb.x * IGF_SPLIT; c0 < total; c0 += bc * IGF_SPLIT) {
+            const unsigned c = c0 + e;
+            if (tid < 6 * IGF_SPLIT && c < total) {
+                double x, y, z;
+                igf_corner_xyz(c, cy1, cz1, hx, hy, hz, x, y, z);
+                terms[m * IGF_SPLIT + e] = igf_term(x, y, z, m);
+            }
+            __syncthreads();
+            if (tid < IGF_SPLIT && c0 + tid < total && SC_IDX_OK(st, 31, c0 + tid, all)) {
+                const double* t = terms + tid;
+                ig[c0 + tid] = __dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(t[0], t[IGF_SPLIT]), t[2 * IGF_SPLIT]),
+                                                             t[3 * IGF_SPLIT]),
+                                                   t[4 * IGF_SPLIT]),
+                                         t[5 * IGF_SPLIT]);
+            }
+            __syncthreads();
+        }
+    }
+    if (line && (vb.x >= bc || nblk == 1)) {
+        // the line-form cells: k below the near box, (i, j) outside it
+        const float hxf = a.use_state ? st->stepsf[0] : (float)hx;
+        const float hyf = a.use_state ? st->stepsf[1] : (float)hy;
+        const float hzf = a.use_state ? st->stepsf[2] : (float)hz;
+        const int lb = nblk == 1 ? 0 : vb.x - bc, nlb = nblk == 1 ? 1 : nblk - bc;
+        const unsigned ncl = (unsigned)nx * ny * b[2];
+        for (unsigned c = lb * blockDim.x + threadIdx.x; c < ncl; c += nlb * blockDim.x) {
+            const unsigned t = c / (unsigned)b[2];
+            const int k = (int)(c - t * (unsigned)b[2]);
+            const int i = (int)(t / (unsigned)ny);
+            const int j = (int)(t - (unsigned)i * ny);
+            if (i < b[0] && j < b[1]) continue;
+            const unsigned o = ((unsigned)i * ny + j) * nz + k;
+            if (!SC_IDX_OK(st, 35, o, (long long)nx * ny * nz)) continue;
+            k1[o] = (R)cell_line((float)i * hxf, (float)j * hyf, (float)k * hzf, 0.5f * hxf, 0.5f * hyf, 0.5f * hzf);
+        }
     }
 }
 
-__global__ void k_igf_corners(double* __restrict__ ig, int nx, int ny, int nz, IgfArgs a, const ScState* st) {
+template <typename R>
+__global__ void __launch_bounds__(IGF_THREADS) k_igf_corners(double* __restrict__ ig, R* __restrict__ k1, int nx,
+                                                             int ny, int nz, IgfArgs a, const ScState* st) {
     pdl_wait();
-    igf_corners_body(ig, nx, ny, nz, a, st, hw_vblk());
+    igf_corners_body<R>(ig, k1, nx, ny, nz, a, st, hw_vblk());
 }
 
 // 4th-order multipole form of the integral of 1/r over the cell centred at
@@ -119,7 +248,8 @@ __device__ __forceinline__ float cell_multipole(float X, float Y, float Z, float
 }
 
 // cell integrals: the 8-corner difference of IG inside the near box (FP64),
-// the multipole form outside it (FP32 form only); written as R
+// the multipole form outside it (FP32 form only; for cells long along z the
+// corners kernel has written the line-form cells); written as R
 template <typename R>
 __device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* __restrict__ k1, int nx, int ny,
                                               int nz, const IgfArgs& a, const ScState* st, VBlk vb) {
@@ -141,6 +271,7 @@ __device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* 
         hzf = (float)hz;
     }
     const float a2 = 0.25f * hxf * hxf, b2 = 0.25f * hyf * hyf, c2 = 0.25f * hzf * hzf, V = hxf * hyf * hzf;
+    const bool line = a.hybrid && st->igf_line;
     const unsigned total = (unsigned)nx * ny * nz;
     const unsigned sy = bx[2] + 1, sx = (unsigned)(bx[1] + 1) * (bx[2] + 1);
     for (unsigned c = vb.x * blockDim.x + threadIdx.x; c < total; c += vb.nx * blockDim.x) {
@@ -159,6 +290,8 @@ __device__ __forceinline__ void igf_diff_body(const double* __restrict__ ig, R* 
             v = __dadd_rn(v, ig[o + sx]);
             v = __dsub_rn(v, ig[o]);
             k1[c] = (R)v;
+        } else if (line && k < bx[2]) {
+            continue;  // the line form, written by the corners kernel
         } else {
             if (!SC_IDX_OK(st, 34, c, total)) continue;
             k1[c] = (R)cell_multipole((float)i * hxf, (float)j * hyf, (float)k * hzf, a2, b2, c2, V);
@@ -322,7 +455,8 @@ cudaError_t launch_igf_h(const Plan& p, const Layout& L, char* ws, double* kern_
     a.hybrid = 0;
     double* ig = reinterpret_cast<double*>(ws + L.igf_ig);
     const size_t nc = (size_t)(p.nx + 1) * (p.ny + 1) * (p.nz + 1);
-    launch(k_igf_corners, grid_for(nc, p.sm_count), 256, 0, s, ig, p.nx, p.ny, p.nz, a, st);
+    launch(k_igf_corners<double>, grid_for(nc, p.sm_count), IGF_THREADS, 0, s, ig, (double*)nullptr, p.nx, p.ny,
+           p.nz, a, st);
     const size_t nk = (size_t)p.nx * p.ny * p.nz;
     launch(k_igf_diff<double>, grid_for(nk, p.sm_count), 256, 0, s, ig, kern_out, p.nx, p.ny, p.nz, a, st);
     return cudaGetLastError();
@@ -341,8 +475,13 @@ cudaError_t launch_igf(const Plan& p, const Layout& L, char* ws, cudaStream_t s)
     // registers left over hold the blocks of the concurrent particle kernels
     size_t gb = (nc + 255) / 256;
     if (gb > (size_t)p.sm_count) gb = (size_t)p.sm_count;
-    launch(k_igf_corners, (int)gb, 256, 0, s, ig, p.nx, p.ny, p.nz, a, st);
     const size_t nk = (size_t)p.nx * p.ny * p.nz;
+    if (p.prec == SC_FP64)
+        launch(k_igf_corners<double>, (int)gb, IGF_THREADS, 0, s, ig, reinterpret_cast<double*>(ws + L.igf_k1), p.nx,
+               p.ny, p.nz, a, st);
+    else
+        launch(k_igf_corners<float>, (int)gb, IGF_THREADS, 0, s, ig, reinterpret_cast<float*>(ws + L.igf_k1), p.nx,
+               p.ny, p.nz, a, st);
     if (p.prec == SC_FP64)
         launch(k_igf_diff<double>, grid_for(nk, p.sm_count), 256, 0, s, ig, reinterpret_cast<double*>(ws + L.igf_k1), p.nx,
                                                                      p.ny, p.nz, a, st);
@@ -438,7 +577,8 @@ __global__ void __launch_bounds__(256) kb_igf_corners(const BatchBeam* __restric
                                                       const int* __restrict__ start, int nb) {
     pdl_wait();
     BATCH_BEAM(BS_IGF_C)
-    igf_corners_body(reinterpret_cast<double*>(ws + L.igf_ig), p.nx, p.ny, p.nz, batch_igf_args(p, 1), st, vb);
+    igf_corners_body<float>(reinterpret_cast<double*>(ws + L.igf_ig), reinterpret_cast<float*>(ws + L.igf_k1), p.nx,
+                            p.ny, p.nz, batch_igf_args(p, 1), st, vb);
 }
 
 __global__ void __launch_bounds__(256) kb_igf_diff(const BatchBeam* __restrict__ beams,
@@ -612,7 +752,8 @@ extern "C" int sc_sym_kernel_static(int nx, int ny, int nz, double hx, double hy
     a.use_state = 0;
     a.force = 1;
     a.hybrid = 0;
-    launch(k_igf_corners, grid_for((size_t)corners, sms), 256, 0, s, ig, nx, ny, nz, a, st);
+    launch(k_igf_corners<double>, grid_for((size_t)corners, sms), IGF_THREADS, 0, s, ig, (double*)nullptr, nx, ny, nz,
+           a, st);
     launch(k_igf_diff<double>, grid_for((size_t)nx * ny * nz, sms), 256, 0, s, ig, kern, nx, ny, nz, a, st);
     e = cudaGetLastError();
     if (e != cudaSuccess) return sc_report(SC_ERR_CUDA, "sc_sym_kernel_static: %s", cudaGetErrorString(e));

@@ -746,6 +746,8 @@ __device__ void mesh_finish(const double (&mn)[3], const double (&mx)[3], const 
         st->istepsf[k] = (float)istepk;
         st->xofff[k] = (float)xoffk;
         st->igf_box[k] = bk;
+        if (k < 2) st->igf_tbox[k] = igf_tbox_of(steps, k, nm[k]);
+        if (k == 2) st->igf_line = igf_line_of(steps);
     }
     if (lane == 1) st->phi_norm = kp.phi_norm;
     if (lane == 2) {
@@ -1462,6 +1464,9 @@ __global__ void k_set_mesh(ScState* st, double hx, double hy, double hz, KickPar
     st->phi_norm = kp.phi_norm;
     const double h[3] = {hx, hy, hz};
     igf_box_of(h, kp.nx, kp.ny, kp.nz, st->igf_box);
+    st->igf_line = igf_line_of(h);
+    st->igf_tbox[0] = igf_tbox_of(h, 0, kp.nx);
+    st->igf_tbox[1] = igf_tbox_of(h, 1, kp.ny);
     const bool same = hx == st->igf_h[0] && hy == st->igf_h[1] && hz == st->igf_h[2];
     st->igf_rebuild = same ? 0 : 1;
     st->igf_h[0] = hx;

@@ -130,11 +130,7 @@ class Engine:
         """Launch one kick on the current stream (asynchronous)."""
         torch = _torch()
         self.ensure(n)
-        if self.tuned and self._tuned_n != n:
-            from . import tuning
-            for param, value in tuning.lookup(self.precision, self.shape, n).items():
-                self.set_param(param, value)
-            self._tuned_n = n
+        self.apply_tuning(n)
         ld = rp.stride(0)
         if rp.stride(1) != 1:
             raise ValueError("rparticles rows must be contiguous")
@@ -176,6 +172,16 @@ class Engine:
         N.check(self.lib.sc_profile_read(self.plan, ms, C.byref(nl)))
         names = [self.lib.sc_profile_stage_name(i).decode() for i in range(N.SC_NSTAGES)]
         return dict(zip(names, [float(v) for v in ms])), nl.value
+
+    def apply_tuning(self, n: int):
+        """Launch shapes of the tuning table's entry for this form, mesh and
+        particle count (nothing unless the engine is tuned); results do not
+        change."""
+        if self.tuned and self._tuned_n != n:
+            from . import tuning
+            for param, value in tuning.lookup(self.precision, self.shape, n).items():
+                self.set_param(param, value)
+            self._tuned_n = n
 
     def set_param(self, param: int, value: int):
         """A launch-shape parameter of the plan (N.SC_PARAM_*); results do not change."""

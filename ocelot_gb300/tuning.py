@@ -28,16 +28,20 @@ TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_ta
 # parameter -> candidate values (the plan's launch-shape knobs)
 def candidates():
     return {N.SC_PARAM_KICK_VARIANT: list(range(N.SC_KICK_NVARIANTS)),
-            N.SC_PARAM_FFT_PLANE_FWD: [1, 0], N.SC_PARAM_FFT_PLANE_INV: [1, 0]}
+            N.SC_PARAM_FFT_PLANE_FWD: [1, 0], N.SC_PARAM_FFT_PLANE_INV: [1, 0],
+            N.SC_PARAM_FFT_COLS_X: [0, 8, 4], N.SC_PARAM_FFT_COLS_Y: [0, 8, 4]}
 
 
 PARAM_NAMES = {N.SC_PARAM_KICK_VARIANT: "kick_variant", N.SC_PARAM_FFT_PLANE_FWD: "fft_plane_fwd",
-               N.SC_PARAM_FFT_PLANE_INV: "fft_plane_inv"}
+               N.SC_PARAM_FFT_PLANE_INV: "fft_plane_inv", N.SC_PARAM_FFT_COLS_X: "fft_cols_x",
+               N.SC_PARAM_FFT_COLS_Y: "fft_cols_y"}
 # the stages (sc_profile_read) each parameter changes: a candidate is timed by
 # the sum of these stage times, which a few-microsecond difference does not
 # drown in the rest of the kick
 PARAM_STAGES = {N.SC_PARAM_KICK_VARIANT: ("kick",), N.SC_PARAM_FFT_PLANE_FWD: ("convolve", "join_wait"),
-                N.SC_PARAM_FFT_PLANE_INV: ("convolve", "field")}
+                N.SC_PARAM_FFT_PLANE_INV: ("convolve", "field"),
+                N.SC_PARAM_FFT_COLS_X: ("convolve", "join_wait", "field"),
+                N.SC_PARAM_FFT_COLS_Y: ("convolve", "join_wait", "field")}
 _NAME_TO_PARAM = {v: k for k, v in PARAM_NAMES.items()}
 
 _lock = threading.Lock()

@@ -53,7 +53,7 @@ def test_tuner_picks_an_identical_variant_and_records_it(tmp_path):
     assert 0 <= v < N.SC_KICK_NVARIANTS
     assert set(res["us"]["kick_variant"]) == {str(i) for i in range(N.SC_KICK_NVARIANTS)}
     assert tuning.lookup("fp32", (32, 32, 32), 200_000, path)[N.SC_PARAM_KICK_VARIANT] == v
-    assert set(res["params"]) == {"kick_variant", "fft_plane_fwd", "fft_plane_inv"}
+    assert set(res["params"]) == {"kick_variant", "fft_plane_fwd", "fft_plane_inv", "fft_cols_x", "fft_cols_y"}
 
 
 def test_bad_variant_is_refused():
@@ -83,3 +83,32 @@ def test_fft_plane_parameters_give_the_same_bits(precision, fields):
         outs.append(d.cpu().numpy())
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+@pytest.mark.parametrize("precision,fields,mesh", [("fp32", "spectral", (48, 48, 48)), ("fp32", "difference", (96, 96, 96)),
+                                                   ("fp64", "difference", (48, 48, 48))])
+def test_fft_columns_per_block_give_the_same_bits(precision, fields, mesh):
+    """Columns per block of the x pass and of the separate y passes group
+    independent lines into blocks: every choice gives the same bits."""
+    from ocelot_gb300.sc import plan_mode
+    n = 100_001
+    rp, q = sc_oracle.gaussian_beam(n, 29, charge=1e-9)
+    r0 = torch.from_numpy(rp).to(DEV)
+    dq = torch.from_numpy(q).to(DEV)
+    d = torch.zeros((6, n + 1), dtype=torch.float64, device=DEV)[:, :n]
+    eng = Engine(mesh, precision, DEV, plan_mode(precision, fields=fields), tuned=False)
+    eng.set_param(N.SC_PARAM_FFT_PLANE_FWD, 0)  # the separate y pass forward too
+    eng.set_param(N.SC_PARAM_FFT_PLANE_INV, 0)
+    outs = []
+    for cx, cy in ((0, 0), (16, 4), (2, 16), (8, 8), (4, 2)):
+        eng.set_param(N.SC_PARAM_FFT_COLS_X, cx)
+        eng.set_param(N.SC_PARAM_FFT_COLS_Y, cy)
+        assert (eng.get_param(N.SC_PARAM_FFT_COLS_X), eng.get_param(N.SC_PARAM_FFT_COLS_Y)) == (cx, cy)
+        d.copy_(r0)
+        eng.kick(d, dq, n, 0.130, 0.1)
+        eng.check_status()
+        outs.append(d.cpu().numpy())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    with pytest.raises(ValueError, match=r"\[sc error 1\]"):
+        eng.set_param(N.SC_PARAM_FFT_COLS_X, 3)
