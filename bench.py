@@ -416,13 +416,14 @@ def device_beam(spec, dev):
     return buf[:, :n], q
 
 
-def time_batched(steps, warmup, dev):
+def time_batched(steps, warmup, dev, nbeams=96):
     """The 96-beam workload kicked by sc_kick_batched (one launch per stage,
     recorded once as a CUDA graph and replayed), against the same beams
-    kicked one sc_kick after another on one stream."""
+    kicked one sc_kick after another on one stream.  nbeams < 96: the first
+    nbeams beams of the same draw (the small case of the batch's profiles)."""
     import torch
     from ocelot_gb300.batch import BeamBatch
-    specs = batch_specs()
+    specs = batch_specs()[:nbeams]
     batch = BeamBatch(dev)
     beams = []
     for sp in specs:
@@ -667,6 +668,8 @@ def main():
                     help="time kicks of one form alone on --n particles and a --mesh^3 mesh, print one line and exit "
                          "(the small cases of the profiles)")
     ap.add_argument("--mesh", type=int, default=64)
+    ap.add_argument("--batch-only", type=int, default=0, metavar="BEAMS",
+                    help="time the batched leg alone on the first BEAMS beams of its draw, print one line and exit")
     ap.add_argument("--tune", action="store_true",
                     help="autotune the launch shapes on the benchmark meshes and particle counts, print the "
                          "timings (and store them in the tuning table with --tune-save) and exit")
@@ -680,6 +683,11 @@ def main():
                                            flush_buf.zero_, mesh=[args.mesh] * 3)
         print(json.dumps({"form": args.profile_form, "n": args.n, "mesh": [args.mesh] * 3, "ms_per_kick": kick,
                           "stages_ms": stages, "launches": launches}), flush=True)
+        return
+    if args.batch_only:
+        import torch
+        dev = torch.device("cuda", 0)
+        print(json.dumps(time_batched(args.steps, max(args.warmup, 3), dev, args.batch_only)), flush=True)
         return
     if args.tune:
         from ocelot_gb300 import tuning

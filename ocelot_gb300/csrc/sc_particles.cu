@@ -1553,6 +1553,15 @@ __device__ __forceinline__ bool key_of_f(float fx, float fy, float fz, const Kic
 }
 
 // q * 2^S rounded to an integer, on the integer pipes (|q| 2^S < 2^62)
+// One charge into the fixed-point grid: a reduction without a return value
+// (red), so the thread does not wait for the L2 round trip of the atomic.
+// (atomicAdd with its result unused compiles to an atom that returns it,
+// and the next use of its register waits for the reply.)  Integer addition
+// in any order gives the same grid.
+__device__ __forceinline__ void deposit_fixed(unsigned long long* p, long long v) {
+    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(p), "l"((unsigned long long)v) : "memory");
+}
+
 __device__ __forceinline__ long long to_fixed(double q, int S) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(q);
     const int e = (int)((b >> 52) & 0x7ff);
@@ -1685,7 +1694,7 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
                 if (!deferred) {
                     bad |= !key_of_f(floorf(g[0]) + 1.f, floorf(g[1]) + 1.f, floorf(g[2]) + 1.f, kp, key);
                     if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
-                        atomicAdd(qfix + key, (unsigned long long)to_fixed(qq[w], S));
+                        deposit_fixed(qfix + key, to_fixed(qq[w], S));
                 }
                 key2[w] = key;
                 for (int j = 0; j < 3; ++j) g2[j][w] = g[j];
@@ -1715,7 +1724,7 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
             bad |= !key_of(floor(e[0]) + 1, floor(e[1]) + 1, floor(e[2]) + 1, kp, key);
             keys[i] = key;
             if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
-                atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
+                deposit_fixed(qfix + key, to_fixed(q[i], S));
         }
     }
     // the listed particles: key from the FP64 coordinates and the deposit;
@@ -1730,7 +1739,7 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
         bad |= !key_fine(rp, ld, i, kp, st, key, gf);
         keys[i] = key;
         if (qfix && SC_IDX_OK(st, 13, key, (long long)kp.nx * kp.ny * kp.nz))
-            atomicAdd(qfix + key, (unsigned long long)to_fixed(q[i], S));
+            deposit_fixed(qfix + key, to_fixed(q[i], S));
     }
     if (bad) atomicCAS(&st->status, SC_OK, SC_ERR_NONFINITE);
 }
