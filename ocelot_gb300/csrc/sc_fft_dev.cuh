@@ -1,4 +1,5 @@
-// Batched mixed-radix (3/2/4/8) Stockham FFT of lines held in shared memory.
+// Batched FFTs of lines held in shared memory: mixed-radix (3/2/4/8)
+// Stockham passes, and for the common FP32 lengths the two-step form below.
 //
 // The lines of one thread block live in shared memory, line l at a + l*ls,
 // elements contiguous.  Each stage reads radix-r butterfly inputs with stride
@@ -168,6 +169,173 @@ __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx
     }
 }
 
+// ---------------------------------------------------------------------------
+// Two-step FFT (FP32 lines of length L = P * Q).  With n = Q n1 + n2 and
+// k = k1 + P k2,
+//   X[k1 + P k2] = sum_n2 w_Q^(n2 k2) w_L^(n2 k1) sum_n1 w_P^(n1 k1) x[Q n1 + n2].
+// Step 1, one work item per (line, n2): the P-point DFT over n1 in registers,
+// the twiddle w_L^(n2 k1), each k1 stored in row k1 of a table with rows of
+// Q + 1.  Step 2, one item per (line, k1): the Q-point DFT over n2 in
+// registers, stored in natural order.  Every butterfly stays in registers:
+// one shared-memory round trip and one barrier per step against one per
+// radix stage of the Stockham passes, and about half their instructions
+// (measured alone on this GPU: 1.8x the Stockham rate at L = 128, 2x at 256).
+// Work items run line-fastest (LF) when a power-of-two count of 16 or more
+// lines share the block: the lanes of a half-warp then hold 16 lines at the
+// same offset, which the odd line stride puts on distinct banks.  The
+// twiddles come as tw2[k1 * Q + n2] = w_L^(n2 k1) (load_twiddles lays the
+// table out so for these lengths).
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R fmar(R a, R b, R c) {
+    if constexpr (sizeof(R) == 4) return fmaf(a, b, c);
+    else return fma(a, b, c);
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> cmulc(Cx<R> v, R wr, R wi) {  // v * (wr + i wi), constant factor
+    return cx<R>(fmar<R>(v.x, wr, -(v.y * wi)), fmar<R>(v.x, wi, v.y * wr));
+}
+
+// 16-point DFT, natural order in and out: two 8-point DFTs of the even and
+// odd elements, the odd ones times w16^k
+template <typename R, bool INV>
+__device__ __forceinline__ void dft16(Cx<R>* v) {
+    Cx<R> e[8], o[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        e[i] = v[2 * i];
+        o[i] = v[2 * i + 1];
+    }
+    dft8<R, INV>(e);
+    dft8<R, INV>(o);
+    const R c1 = (R)0.92387953251128675613, s1 = (R)0.38268343236508977173, h = (R)0.70710678118654752440;
+    const R sg = INV ? (R)1 : (R)-1;  // w16^k = cos(2 pi k / 16) + i sg sin(2 pi k / 16)
+    o[1] = cmulc<R>(o[1], c1, sg * s1);
+    o[2] = cx<R>((o[2].x - sg * o[2].y) * h, (o[2].y + sg * o[2].x) * h);
+    o[3] = cmulc<R>(o[3], s1, sg * c1);
+    o[4] = INV ? cmul_pi(o[4]) : cmul_mi(o[4]);
+    o[5] = cmulc<R>(o[5], -s1, sg * c1);
+    o[6] = cx<R>((-o[6].x - sg * o[6].y) * h, (-o[6].y + sg * o[6].x) * h);
+    o[7] = cmulc<R>(o[7], -c1, sg * s1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = cadd(e[k], o[k]);
+        v[k + 8] = csub(e[k], o[k]);
+    }
+}
+
+// 12-point DFT, natural order: n = 4 n1 + n2, k = k1 + 3 k2; four 3-point
+// DFTs, the twiddles w12^(n2 k1), three 4-point DFTs
+template <typename R, bool INV>
+__device__ __forceinline__ void dft12(Cx<R>* v) {
+    Cx<R> y[4][3];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+        Cx<R> a = v[n2], b = v[4 + n2], c = v[8 + n2];
+        dft3<R, INV>(a, b, c);
+        y[n2][0] = a;
+        y[n2][1] = b;
+        y[n2][2] = c;
+    }
+    const R r3 = (R)0.86602540378443864676, hf = (R)0.5;
+    const R sg = INV ? (R)1 : (R)-1;
+    y[1][1] = cmulc<R>(y[1][1], r3, sg * hf);             // w12^1
+    y[1][2] = cmulc<R>(y[1][2], hf, sg * r3);             // w12^2
+    y[2][1] = cmulc<R>(y[2][1], hf, sg * r3);             // w12^2
+    y[2][2] = cmulc<R>(y[2][2], -hf, sg * r3);            // w12^4
+    y[3][1] = INV ? cmul_pi(y[3][1]) : cmul_mi(y[3][1]);  // w12^3
+    y[3][2] = cx<R>(-y[3][2].x, -y[3][2].y);              // w12^6
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+        Cx<R> a0 = y[0][k1], a1 = y[1][k1], a2 = y[2][k1], a3 = y[3][k1];
+        dft4<Cx<R>, INV>(a0, a1, a2, a3);
+        v[k1] = a0;
+        v[k1 + 3] = a1;
+        v[k1 + 6] = a2;
+        v[k1 + 9] = a3;
+    }
+}
+
+template <typename R, bool INV, int P>
+__device__ __forceinline__ void dft_reg(Cx<R>* v) {
+    if constexpr (P == 8) dft8<R, INV>(v);
+    else if constexpr (P == 12) dft12<R, INV>(v);
+    else if constexpr (P == 16) dft16<R, INV>(v);
+    else static_assert(P == 8 || P == 12 || P == 16, "register DFT sizes 8, 12, 16");
+}
+
+// v * w (forward) or v * conj(w) (inverse), with fused multiply-adds
+template <typename R, bool INV>
+__device__ __forceinline__ Cx<R> twmul(Cx<R> v, Cx<R> w) {
+    if (INV) return cx<R>(fmar<R>(v.x, w.x, v.y * w.y), fmar<R>(v.y, w.x, -(v.x * w.y)));
+    return cx<R>(fmar<R>(v.x, w.x, -(v.y * w.y)), fmar<R>(v.x, w.y, v.y * w.x));
+}
+
+// Q of the factorisation L = P * Q of the two-step lengths (FP32); 0: the
+// Stockham passes.  Measured in whole kicks on this GPU: the two-step passes
+// are faster where the passes are bound by the SMs' issue rate (meshes of
+// 96 to 128 cells per axis padded to 192 and 256, and batches), the Stockham
+// passes where one wave of blocks makes them latency-bound (64-cell axes
+// padded to 128: 0.228 against 0.221 ms per 2M / 64^3 kick).
+__host__ __device__ constexpr int two_step_q(int L) {
+    return L == 96 ? 12 : (L == 192 ? 16 : (L == 256 ? 16 : 0));
+}
+
+// ls >= fft_ls(L) >= P (Q + 1); a holds the input, b is scratch; the result
+// is returned in a.  LF: nl is a power of two, lg its log2.  Called by every
+// thread of the block; ends with a barrier.
+template <typename R, bool INV, int L, bool LF>
+__device__ __forceinline__ Cx<R>* fft_two_step(Cx<R>* a, Cx<R>* b, int ls, int nl, int lg, const Cx<R>* tw2) {
+    constexpr int Q = two_step_q(L), P = L / Q;
+    static_assert(Q > 0 && P * Q == L && P * (Q + 1) <= fft_ls(L), "two-step factorisation");
+    for (int idx = threadIdx.x; idx < nl * Q; idx += blockDim.x) {
+        int line, n2;
+        if (LF) {
+            n2 = idx >> lg;
+            line = idx & (nl - 1);
+        } else {
+            line = idx / Q;
+            n2 = idx - line * Q;
+        }
+        const Cx<R>* src = a + line * ls + n2;
+        Cx<R> v[P];
+#pragma unroll
+        for (int n1 = 0; n1 < P; ++n1) v[n1] = src[n1 * Q];
+        dft_reg<R, INV, P>(v);
+        Cx<R>* dst = b + line * ls + n2;
+        dst[0] = v[0];
+#pragma unroll
+        for (int k1 = 1; k1 < P; ++k1) dst[k1 * (Q + 1)] = twmul<R, INV>(v[k1], tw2[k1 * Q + n2]);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nl * P; idx += blockDim.x) {
+        int line, k1;
+        if (LF) {
+            k1 = idx >> lg;
+            line = idx & (nl - 1);
+        } else {
+            line = idx / P;
+            k1 = idx - line * P;
+        }
+        const Cx<R>* src = b + line * ls + k1 * (Q + 1);
+        Cx<R> u[Q];
+#pragma unroll
+        for (int n2 = 0; n2 < Q; ++n2) u[n2] = src[n2];
+        dft_reg<R, INV, Q>(u);
+        Cx<R>* dst = a + line * ls + k1;
+#pragma unroll
+        for (int k2 = 0; k2 < Q; ++k2) dst[k2 * P] = u[k2];
+    }
+    __syncthreads();
+    return a;
+}
+
+template <typename R, bool INV, int L>
+__device__ __forceinline__ Cx<R>* fft_two_step_any(Cx<R>* a, Cx<R>* b, int ls, int nl, const Cx<R>* tw2) {
+    if (nl >= 16 && (nl & (nl - 1)) == 0) return fft_two_step<R, INV, L, true>(a, b, ls, nl, 31 - __clz(nl), tw2);
+    return fft_two_step<R, INV, L, false>(a, b, ls, nl, 0, tw2);
+}
+
 // ls must be at least fft_ls(L)
 template <typename R, bool INV, int L, int S, int NS>
 __device__ __forceinline__ Cx<R>* fft_stages_c(Cx<R>* a, Cx<R>* b, int ls, int nl, const Cx<R>* tw) {
@@ -186,6 +354,14 @@ __device__ __forceinline__ Cx<R>* fft_stages_c(Cx<R>* a, Cx<R>* b, int ls, int n
 // every thread of the block; ends with a barrier.
 template <typename R, bool INV>
 __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan& rp, const Cx<R>* tw) {
+    if constexpr (sizeof(R) == 4) {  // FP32: two register steps (tw laid out by load_twiddles)
+        switch (rp.L) {
+            case 96: return fft_two_step_any<R, INV, 96>(a, b, ls, nl, tw);
+            case 192: return fft_two_step_any<R, INV, 192>(a, b, ls, nl, tw);
+            case 256: return fft_two_step_any<R, INV, 256>(a, b, ls, nl, tw);
+            default: break;
+        }
+    }
     switch (rp.L) {  // the padded lengths of meshes up to 256 per axis
         case 8: return fft_stages_c<R, INV, 8, 0, 1>(a, b, ls, nl, tw);
         case 12: return fft_stages_c<R, INV, 12, 0, 1>(a, b, ls, nl, tw);
@@ -218,8 +394,21 @@ __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan&
     return a;
 }
 
+// The twiddle table of fft_lines in shared memory, from src[m] = w_L^m:
+// the same table for the Stockham passes, tw2[k1 * Q + n2] = w_L^(n2 k1)
+// for the two-step lengths of FP32
 template <typename R>
 __device__ __forceinline__ void load_twiddles(Cx<R>* dst, const Cx<R>* src, int L) {
+    if constexpr (sizeof(R) == 4) {
+        const int Q = two_step_q(L);
+        if (Q) {
+            for (int i = threadIdx.x; i < L; i += blockDim.x) {
+                const int k1 = i / Q, n2 = i - k1 * Q;
+                dst[i] = src[k1 * n2];
+            }
+            return;
+        }
+    }
     for (int i = threadIdx.x; i < L; i += blockDim.x) dst[i] = src[i];
 }
 
