@@ -667,7 +667,7 @@ def main():
     ap.add_argument("--profile-form", choices=["fp32", "fp64"], default=None,
                     help="time kicks of one form alone on --n particles and a --mesh^3 mesh, print one line and exit "
                          "(the small cases of the profiles)")
-    ap.add_argument("--mesh", type=int, default=64)
+    ap.add_argument("--mesh", default="64", help="mesh cells per axis, or nx,ny,nz")
     ap.add_argument("--batch-only", type=int, default=0, metavar="BEAMS",
                     help="time the batched leg alone on the first BEAMS beams of its draw, print one line and exit")
     ap.add_argument("--tune", action="store_true",
@@ -675,13 +675,17 @@ def main():
                          "timings (and store them in the tuning table with --tune-save) and exit")
     ap.add_argument("--tune-save", action="store_true")
     args = ap.parse_args()
+    mesh = [int(v) for v in str(args.mesh).split(",")]
+    mesh = mesh * 3 if len(mesh) == 1 else mesh
+    if len(mesh) != 3:
+        ap.error("--mesh takes one size or nx,ny,nz")
     if args.profile_form:
         import torch
         dev = torch.device("cuda", 0)
         flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
         kick, stages, launches = time_form(args.profile_form, args.n, args.steps, max(args.warmup, 3), dev,
-                                           flush_buf.zero_, mesh=[args.mesh] * 3)
-        print(json.dumps({"form": args.profile_form, "n": args.n, "mesh": [args.mesh] * 3, "ms_per_kick": kick,
+                                           flush_buf.zero_, mesh=mesh)
+        print(json.dumps({"form": args.profile_form, "n": args.n, "mesh": mesh, "ms_per_kick": kick,
                           "stages_ms": stages, "launches": launches}), flush=True)
         return
     if args.batch_only:
