@@ -371,7 +371,7 @@ int sc_kick_launches(const sc_plan* plan);
  *     that four blocks share an SM. */
 #define SC_PARAM_FFT_COLS_X 4
 #define SC_PARAM_FFT_COLS_Y 5
-#define SC_KICK_NVARIANTS 16
+#define SC_KICK_NVARIANTS 21
 int sc_plan_set_param(sc_plan* plan, int param, int value);
 int sc_plan_get_param(const sc_plan* plan, int param, int* value);
 /* Tile (particles), tile buffers, particles per thread and blocks per SM of a

@@ -36,7 +36,7 @@ SC_PARAM_FFT_PLANE_FWD = 2
 SC_PARAM_FFT_PLANE_INV = 3
 SC_PARAM_FFT_COLS_X = 4
 SC_PARAM_FFT_COLS_Y = 5
-SC_KICK_NVARIANTS = 16
+SC_KICK_NVARIANTS = 21
 
 # the kernels whose bulk-copy waits sc_plan_set_wait_limit bounds
 SC_WAIT_FRAME = 0

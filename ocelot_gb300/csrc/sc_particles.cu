@@ -2303,11 +2303,21 @@ __device__ __forceinline__ void kick32_async_body(double* __restrict__ rp, const
 // more bulk-copy tilings (indices after the barrier-free ones)
 #define SC_KICK_VARIANTS_B(X) \
     X(14, 256, 3, 1, 6)       \
-    X(15, 256, 2, 1, 6)
+    X(15, 256, 2, 1, 6)       \
+    X(16, 128, 4, 1, 6)       \
+    X(17, 128, 3, 1, 6)       \
+    X(18, 128, 6, 1, 6)       \
+    X(19, 64, 4, 1, 12)       \
+    X(20, 64, 6, 1, 12)
 
-// the default: 256-particle tiles, one particle per thread, 4 blocks per SM
-// (measured fastest from 1M particles up on 48^3 to 128x128x256 meshes)
-constexpr int kDefaultKickVariant = 2;
+// the default: 128-particle tiles of one particle per thread, four tile
+// buffers, six blocks of 128 threads per SM (the same 80 registers as the
+// 256-particle tilings): measured fastest on 48^3 to 128x128x256 meshes from
+// 200k particles up -- the half-size tiles halve the tail of the kernel (a
+// block's last tile) and a slow warp holds four warps at the barrier instead
+// of eight (2M / 64^3: 57.3 -> 55.2 us; 10M / 128x128x256: 303 -> 279 us
+// with the 3-buffer form)
+constexpr int kDefaultKickVariant = 16;
 constexpr int kBatchKickVariant = 13;  // the batched kick's tiling (launch_batch_particles)
 
 template <int TILE, int STAGES, int PPT, int MINB>
@@ -2465,7 +2475,7 @@ static const KickVariant kKickVariants[] = {
 #undef SC_KV
 };
 constexpr int kNumKickVariants = (int)(sizeof(kKickVariants) / sizeof(kKickVariants[0]));
-static_assert(KickTiling<256, 3, 1>::threads == PT, "the default kick tiling has PT threads");
+static_assert(KickTiling<256, 3, 1>::threads == PT, "the 256-particle, one-per-thread tilings have PT threads");
 static_assert(kNumKickVariants == SC_KICK_NVARIANTS, "SC_KICK_NVARIANTS must count SC_KICK_VARIANTS");
 
 int default_kick_variant() { return kDefaultKickVariant; }
