@@ -67,10 +67,10 @@ SEED = 2024
 B_PER_PARTICLE = 104
 B_KICK_KERNEL_PER_PARTICLE = 96  # gather+kick: rparticles read + write
 # DRAM traffic of one k_kick32_tma launch per particle, from the ncu capture
-# summarised in profiles/k_kick32_tma_4M_64cube.txt (200.38 MB read + 133.11 MB
+# summarised in profiles/k_kick32_tma_4M_64cube.txt (200.39 MB read + 132.49 MB
 # written at 4M particles); traffic grows with the particles, so it is scaled
 # to the bench's n
-KICK_TRAFFIC_PER_PARTICLE = (200.38e6 + 133.11e6) / 4e6
+KICK_TRAFFIC_PER_PARTICLE = (200.39e6 + 132.49e6) / 4e6
 
 
 def log(*a):
