@@ -200,11 +200,14 @@ __global__ void k_cell_bounds(const uint32_t* __restrict__ sk, int64_t n, uint32
     }
 }
 
-// One warp per cell sums the cell's run of charges, which the last radix pass
-// carried into sorted (cell, particle) order.  FP64: a strictly sequential
-// left fold in particle order, np.bincount's summation (sc.py:193), bit for
-// bit.  FP32: lane-strided Kahan sums combined by a fixed shuffle tree with
-// error-free (two-sum) additions.  Empty cells get 0, so no memset of the grid.
+// The cell's run of charges, which the last radix pass carried into sorted
+// (cell, particle) order, summed into the cell.  FP64: one thread per cell, a
+// strictly sequential left fold in particle order from 0 -- np.bincount's
+// summation (sc.py:193), bit for bit.  (One warp per cell with every lane
+// folding the same shuffled values spent 32 lanes of this GPU's narrow FP64
+// pipe per addition: 370 us per 2M particles.)  FP32: one warp per cell,
+// lane-strided Kahan sums combined by a fixed shuffle tree with error-free
+// (two-sum) additions.  Empty cells get 0, so no memset of the grid.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = __fadd_rn(a, b);
     const float bb = __fsub_rn(s, a);
@@ -217,20 +220,27 @@ __global__ void __launch_bounds__(256) k_deposit_cells(const R* __restrict__ sq,
                                                        R* __restrict__ qgrid, const ScState* st) {
     pdl_wait();
     if (st->status) return;
+    if constexpr (sizeof(R) == 8) {
+        const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell; c += nt) {
+            const uint32_t b = start[c], e = end[c];
+            double sum = 0.0;
+            uint32_t k = b;
+            for (; k + 4 <= e; k += 4) {  // four loads in flight, the additions in order
+                const double v0 = sq[k], v1 = sq[k + 1], v2 = sq[k + 2], v3 = sq[k + 3];
+                sum = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(sum, v0), v1), v2), v3);
+            }
+            for (; k < e; ++k) sum = __dadd_rn(sum, (double)sq[k]);
+            qgrid[c] = (R)sum;
+        }
+        return;
+    }
     const int lane = threadIdx.x & 31;
     const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t c = w0; c < ncell; c += nw) {
         const uint32_t b = start[c], e = end[c];
-        if (sizeof(R) == 8) {
-            double sum = 0.0;
-            for (uint32_t k = b; k < e; k += 32) {
-                const double v = (k + lane < e) ? (double)sq[k + lane] : 0.0;
-                const int m = (int)min(32u, e - k);
-                for (int l = 0; l < m; ++l) sum = __dadd_rn(sum, __shfl_sync(0xffffffffu, v, l));
-            }
-            if (lane == 0) qgrid[c] = (R)sum;
-        } else {
+        {
             float sum = 0.f, comp = 0.f;
             for (uint32_t k = b + lane; k < e; k += 32) {
                 const float y = __fsub_rn((float)sq[k], comp);
@@ -265,7 +275,9 @@ cudaError_t launch_deposit(const Plan& p, const Layout& L, char* ws, const doubl
     uint32_t* cs = reinterpret_cast<uint32_t*>(ws + L.cell_start);
     uint32_t* ce = reinterpret_cast<uint32_t*>(ws + L.cell_end);
     launch(k_cell_bounds, (int)b, 256, 0, s, sk, n, cs, ce, st);
-    const int cb = p.sm_count * 8;
+    const int cb = p.prec == SC_FP64 ? (int)((ncell + 255) / 256 < (int64_t)p.sm_count * 16 ? (ncell + 255) / 256
+                                                                                            : (int64_t)p.sm_count * 16)
+                                     : p.sm_count * 8;
     if (p.prec == SC_FP64)
         launch(k_deposit_cells<double>, cb, 256, 0, s, reinterpret_cast<const double*>(ws + L.sort_q), cs, ce, ncell,
                                                    reinterpret_cast<double*>(ws + L.qgrid), st);
