@@ -1707,18 +1707,21 @@ __device__ __forceinline__ void keys32_body(float* __restrict__ X, uint32_t* __r
                 for (int j = 0; j < 3; ++j) st_rowf(X + j * nX, i0_, pair_, g2[j][0], g2[j][1]);
         }
         // near-face particles beyond the block's list (degenerate beams only):
-        // evaluated here, out of the unrolled loop, with the same exact key as
-        // the listed ones -- so every key is the FP64 form's whatever the
-        // blocks, and the kick does not depend on how the particles are cut
-        // into blocks (a solo kick and a batch cut them differently)
+        // the FP32-corrected estimate alone, out of the unrolled loop
         while (slow) {
             const int bit = __ffs(slow) - 1;
             slow &= slow - 1;
             const int64_t p_ = pg_ + (bit >> 1) * pstride_;
             const int64_t i = (VEC && p_ < npair_ ? 2 * p_ : (VEC ? n - 1 : p_)) + (bit & 1);
+            double T[3][3];
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) T[a][b] = st->T[a][b];
+            double xv[3], e[3];
+            xyz_fine32(rp, ld, i, kp, T, st->gamma0, xv);
+            for (int j = 0; j < 3; ++j)  // the FP64 form's grid coordinate (k_keys64)
+                e[j] = __dsub_rn(div_checked(xv[j], st->steps[j], st->isteps[j]), st->xoff[j]);
             uint32_t key = 0u;
-            float gf[3];
-            bad |= !key_fine(rp, ld, i, kp, st, key, gf);
+            bad |= !key_of(floor(e[0]) + 1, floor(e[1]) + 1, floor(e[2]) + 1, kp, key);
             keys[i] = key;
             if (qfix && SC_IDX_OK(st, 11, key, (long long)kp.nx * kp.ny * kp.nz))
                 deposit_fixed(qfix + key, to_fixed(q[i], S));
@@ -2594,9 +2597,6 @@ cudaError_t launch_set_mesh(const Plan& p, const Layout& L, char* ws, const Kick
 cudaError_t launch_keys(const Plan& p, const Layout& L, char* ws, const KickParams& kp, const double* rp,
                         const double* q, cudaStream_t s, bool qfix_zeroed) {
     ScState* st = reinterpret_cast<ScState*>(ws + L.state);
-    // three blocks per SM: a fourth (the kernel's registers allow it) starves
-    // the Green's-function branch on the second stream (2M / 64^3: keys 34 ->
-    // 44 us, the kick 0.214 -> 0.228 ms)
     const int nb = particle_blocks(p, kp.n);
     uint32_t* keys = reinterpret_cast<uint32_t*>(ws + L.keys);
     if (p.prec == SC_FP64)
