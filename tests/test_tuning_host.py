@@ -36,3 +36,11 @@ def test_committed_table_holds_valid_parameters():
                 assert name in tuning.PARAM_NAMES.values()
                 if name == "kick_variant":
                     assert 0 <= v < N.SC_KICK_NVARIANTS
+                elif name in ("fft_plane_fwd", "fft_plane_inv"):
+                    assert v in (0, 1)
+                elif name in ("fft_cols_x", "fft_cols_y"):
+                    assert v in (0, 2, 4, 8, 16)
+            # every candidate the tuner timed is recorded with its time
+            for name, times in e.get("us", {}).items():
+                assert name in tuning.PARAM_NAMES.values()
+                assert str(e["params"][name]) in times
