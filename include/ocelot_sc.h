@@ -159,12 +159,22 @@ int sc_batch_create(sc_batch** out, int max_beams);
 void sc_batch_destroy(sc_batch* batch);
 /* Validates the beams and uploads the work table with an asynchronous copy
  * on `stream`.  Waits (on the host) only for the copy of the previous call.
- * Not allowed during stream capture. */
+ * Not allowed during stream capture.  On any error the batch keeps the table
+ * it had.  Once a kick or transport of this batch has been recorded in a CUDA
+ * graph, the graph's launches (number of beams, blocks per stage, shared
+ * memory) are fixed: a table of another shape -- other particle counts or
+ * meshes, a beam more or less, a kick length set to zero -- is refused with
+ * SC_ERR_ARG, and those beams are kicked with a new batch.  Tables of the same
+ * shape (new kick lengths, energies, maps, buffers) are accepted. */
 int sc_batch_set(sc_batch* batch, const sc_beam* beams, int nbeams, void* stream);
 /* Kicks every beam of the table currently set (stream-ordered after the
  * upload).  Capturable in a CUDA graph; a replay kicks the beams of the
- * table resident at replay time.  Device errors latch in each beam's
- * workspace (sc_read_status). */
+ * table resident at replay time (of the shape recorded, see sc_batch_set).
+ * Fails with SC_ERR_WORKSPACE, launching nothing, when a beam's plan had its
+ * workspace initialised again (sc_workspace_init) after sc_batch_set: set the
+ * table again.  A graph recorded before that still holds the old workspace;
+ * set the table again before replaying it.  Device errors latch in each
+ * beam's workspace (sc_read_status). */
 int sc_kick_batched(sc_batch* batch, void* stream);
 /* Kernels launched by the last sc_kick_batched (0 before the first). */
 int sc_batch_launches(const sc_batch* batch);

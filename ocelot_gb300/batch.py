@@ -31,6 +31,11 @@ class BeamBatch:
     a CUDA graph to replay.  ``igf="exact"`` uses the FP64 8-corner IGF on
     the whole octant instead of the hybrid table; ``fields`` as in
     ``SpaceCharge`` (spectral by default).
+
+    The table holds each beam's workspace: when an engine's workspace is
+    allocated anew (a solo kick of more particles grew it), ``kick()``,
+    ``transport()`` and a graph's ``replay()`` upload the table again first.
+    After ``graph()`` the batch's launch shape is fixed (see ``graph``).
     """
 
     def __init__(self, device=None, igf: str = "hybrid", max_beams: int = 1024, fields: str = "spectral"):
@@ -48,6 +53,7 @@ class BeamBatch:
         self.beams = []      # (engine, rp, q, E, zstep, tmap or None)
         self._table = None
         self._maps = None
+        self._ws = None      # the workspaces the uploaded table holds
 
     def __del__(self):
         try:
@@ -110,12 +116,20 @@ class BeamBatch:
             N.check(self.lib.sc_batch_set(self.handle, arr, len(self.beams),
                                           C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
         self._table, self._maps = arr, maps   # copied by sc_batch_set; kept for inspection
+        self._ws = self._workspaces()
+
+    def _workspaces(self):
+        return [(e.ws.data_ptr(), e.ws.numel()) if e.ws is not None else None for e, *_ in self.beams]
+
+    def _refresh(self):
+        """Upload the table if it changed or a beam's workspace was allocated anew."""
+        if self._table is None or self._ws != self._workspaces():
+            self.commit()
 
     def kick(self):
         """Kick every beam once (asynchronous on the current stream)."""
         import torch
-        if self._table is None:
-            self.commit()
+        self._refresh()
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_kick_batched(self.handle,
                                              C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
@@ -123,8 +137,7 @@ class BeamBatch:
     def transport(self):
         """Apply every beam's transport map (one launch, current stream)."""
         import torch
-        if self._table is None:
-            self.commit()
+        self._refresh()
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_tmap_batched(self.handle,
                                              C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)))
@@ -145,18 +158,37 @@ class BeamBatch:
         return int(self.lib.sc_batch_launches(self.handle))
 
     def graph(self, stream=None):
-        """Record one batched kick as a CUDA graph (``.replay()`` kicks again)."""
+        """Record one batched kick as a CUDA graph; ``.replay()`` kicks the
+        beams of the table current at replay time.
+
+        The recorded launches fix the batch's shape: afterwards ``commit()``
+        accepts new kick lengths, energies and maps for the same beams, but
+        raises for other particle counts or meshes, an added or removed beam,
+        or a kick length set to zero (kick those beams with a new batch)."""
         import torch
-        if self._table is None:
-            self.commit()
+        self._refresh()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.device(self.device):
             torch.cuda.synchronize(self.device)
             with torch.cuda.graph(g, stream=stream):
                 self.kick()
-        return g
+        return BatchGraph(self, g)
 
     def check(self):
         """Wait for the GPU and raise if any beam latched an error."""
         for e, *_ in self.beams:
             e.check_status()
+
+
+class BatchGraph:
+    """A batched kick recorded as a CUDA graph (``BeamBatch.graph``)."""
+
+    def __init__(self, batch: BeamBatch, graph):
+        self.batch = batch
+        self.graph = graph
+
+    def replay(self):
+        """Kick the beams of the batch's current table again (current
+        stream); the table is uploaded first if it changed since."""
+        self.batch._refresh()
+        self.graph.replay()

@@ -10,6 +10,7 @@
 #include <new>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "sc_common.cuh"
 
@@ -765,8 +766,19 @@ int sc_tmap_apply(const double* R, const double* B, double* rp, int64_t ld, int6
     return SC_OK;
 }
 
+// what sc_batch_set saw of a kicked beam's workspace: a kick of the table
+// checks it again, so that a workspace initialised anew since (a grown
+// workspace, the old one freed) fails instead of being written
+struct BatchWs {
+    const sc_plan* plan;  // NULL for a transport-only beam
+    const void* ws;
+    size_t ws_bytes;
+    int index;            // the beam's index in the caller's array
+};
+
 struct sc_batch {
     int max_beams;
+    BatchWs* ws_seen;        // [max_beams], host
     char* h_buf;             // pinned: BatchBeam[max_beams], then int start[BS_COUNT][max_beams + 1]
     char* d_buf;             // device copy
     size_t beams_bytes, start_bytes;
@@ -779,8 +791,18 @@ struct sc_batch {
     cudaEvent_t fork, join;
     int last_launches;
     bool profiling;
+    bool captured;           // a stream capture has recorded this batch's launches
     cudaEvent_t ev[NEV];     // as a plan's: main stream 0..9, side stream 10..13
 };
+
+// A kick or transport recorded in a CUDA graph fixes the batch's launch shape
+// (see sc_batch_set).
+static int note_capture(sc_batch* b, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SC_CUDA(cudaStreamIsCapturing(s, &cs), "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone) b->captured = true;
+    return SC_OK;
+}
 
 int sc_batch_create(sc_batch** out, int max_beams) {
     if (!out) return fail(SC_ERR_ARG, "batch pointer is NULL");
@@ -793,6 +815,11 @@ int sc_batch_create(sc_batch** out, int max_beams) {
     if (!b) return fail(SC_ERR_ARG, "out of host memory");
     memset(b, 0, sizeof *b);
     b->max_beams = max_beams;
+    b->ws_seen = new (std::nothrow) BatchWs[max_beams];
+    if (!b->ws_seen) {
+        delete b;
+        return fail(SC_ERR_ARG, "out of host memory");
+    }
     b->beams_bytes = align_up(sizeof(BatchBeam) * (size_t)max_beams);
     b->start_bytes = sizeof(int) * (size_t)BS_COUNT * (max_beams + 1);
     cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&b->h_buf), b->beams_bytes + b->start_bytes);
@@ -824,6 +851,7 @@ void sc_batch_destroy(sc_batch* b) {
     if (b->join) cudaEventDestroy(b->join);
     if (b->d_buf) cudaFree(b->d_buf);
     if (b->h_buf) cudaFreeHost(b->h_buf);
+    delete[] b->ws_seen;
     delete b;
 }
 
@@ -863,13 +891,19 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
     BatchBeam* hb = reinterpret_cast<BatchBeam*>(b->h_buf);
     int* hs = reinterpret_cast<int*>(b->h_buf + b->beams_bytes);
     const int stride = b->max_beams + 1;
+    // the new table's launch shape goes into locals: the batch keeps its
+    // current table and shape until every check below has passed
     int nb = 0;
-    for (int k = 0; k < 3; ++k) b->fft_smem[k] = b->green_smem[k] = 0;
+    int blocks[BS_COUNT];
+    size_t fsm[3] = {0, 0, 0}, gsm[3] = {0, 0, 0};
+    std::vector<BatchWs> wsv;
+    wsv.reserve(nbeams);
     for (int i = 0; i < nbeams; ++i) {
         const sc_beam& m = beams[i];
         if (m.zstep == 0 && !m.tmap) continue;
         BatchBeam& B = hb[nb];
         memset(&B, 0, sizeof B);
+        wsv.push_back(BatchWs{m.zstep == 0 ? nullptr : m.plan, m.ws, m.ws_bytes, i});
         const Plan& p = m.plan->p;
         B.rp = m.rparticles;
         B.q = m.q;
@@ -899,8 +933,8 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
         batch_fft_tiling(B, fs);
         batch_green_tiling(B, gs);
         for (int k = 0; k < 3; ++k) {
-            b->fft_smem[k] = fs[k] > b->fft_smem[k] ? fs[k] : b->fft_smem[k];
-            b->green_smem[k] = gs[k] > b->green_smem[k] ? gs[k] : b->green_smem[k];
+            fsm[k] = fs[k] > fsm[k] ? fs[k] : fsm[k];
+            gsm[k] = gs[k] > gsm[k] ? gs[k] : gsm[k];
         }
         B.gx[BS_PART] = batch_particle_blocks(p, m.n);
         B.gy[BS_PART] = 1;
@@ -914,8 +948,24 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
             if (acc > 0x7fffffffLL) return fail(SC_ERR_UNSUPPORTED, "batch needs more than 2^31 blocks in a stage");
             hs[st * stride + i + 1] = (int)acc;
         }
-        b->blocks[st] = (int)acc;
+        blocks[st] = (int)acc;
     }
+    if (b->captured) {
+        // a captured graph replays the launches it recorded -- beam count,
+        // blocks per stage, dynamic shared memory -- over whatever table is
+        // resident: only a table of that shape may replace the current one
+        bool same = nb == b->nb;
+        for (int st = 0; st < BS_COUNT; ++st) same = same && blocks[st] == b->blocks[st];
+        for (int k = 0; k < 3; ++k) same = same && fsm[k] <= b->fft_smem[k] && gsm[k] <= b->green_smem[k];
+        if (!same)
+            return fail(SC_ERR_ARG,
+                        "a CUDA graph recorded this batch's launches for another table shape (number of beams, "
+                        "blocks per stage, shared memory): kick these beams with a new batch");
+    } else {
+        for (int k = 0; k < 3; ++k) b->fft_smem[k] = fsm[k], b->green_smem[k] = gsm[k];
+    }
+    for (int st = 0; st < BS_COUNT; ++st) b->blocks[st] = blocks[st];
+    for (int i = 0; i < nb; ++i) b->ws_seen[i] = wsv[i];
     b->nb = nb;
     cudaStream_t s = (cudaStream_t)stream;
     if (nb) {
@@ -929,11 +979,24 @@ int sc_batch_set(sc_batch* b, const sc_beam* beams, int nbeams, void* stream) {
     return SC_OK;
 }
 
+static int check_batch_ws(const sc_batch* b) {
+    for (int i = 0; i < b->nb; ++i) {
+        const BatchWs& w = b->ws_seen[i];
+        if (w.plan && (w.plan->ws_ready != w.ws || w.plan->ws_ready_bytes != w.ws_bytes))
+            return fail(SC_ERR_WORKSPACE,
+                        "beam %d: its plan's workspace was initialised again after sc_batch_set (set the table again)",
+                        w.index);
+    }
+    return SC_OK;
+}
+
 int sc_kick_batched(sc_batch* b, void* stream) {
     if (!b) return fail(SC_ERR_ARG, "batch is NULL");
     b->last_launches = 0;
     if (b->nb == 0) return SC_OK;
+    if (int r = check_batch_ws(b)) return r;
     cudaStream_t s = (cudaStream_t)stream;
+    if (int r = note_capture(b, s)) return r;
     const BatchBeam* beams = reinterpret_cast<const BatchBeam*>(b->d_buf);
     const int* start = reinterpret_cast<const int*>(b->d_buf + b->beams_bytes);
     const int stride = b->max_beams + 1;
@@ -1022,6 +1085,7 @@ int sc_batch_profile_read(sc_batch* b, float* ms) {
 int sc_tmap_batched(sc_batch* b, void* stream) {
     if (!b) return fail(SC_ERR_ARG, "batch is NULL");
     if (b->nb == 0) return SC_OK;
+    if (int r = note_capture(b, (cudaStream_t)stream)) return r;
     const BatchBeam* beams = reinterpret_cast<const BatchBeam*>(b->d_buf);
     const int* start = reinterpret_cast<const int*>(b->d_buf + b->beams_bytes);
     SC_CUDA(launch_batch_tmap(beams, start + BS_TMAP * (b->max_beams + 1), b->nb, b->blocks[BS_TMAP],

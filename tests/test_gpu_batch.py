@@ -187,3 +187,58 @@ def test_zero_step_beam_with_a_map_is_transported():
     sc.apply_device(e0, eq0, good[2][2], good[2][6])
     sc.check()
     assert np.array_equal(d0.cpu().numpy(), e0.cpu().numpy())
+
+
+def test_workspace_allocated_anew_after_commit():
+    """A beam's engine whose workspace grows after the table was uploaded (a
+    solo kick of more particles) no longer matches the table: the C entry
+    point refuses to kick with the old workspace, and BeamBatch uploads the
+    table again before its next kick, whose result equals the solo kick."""
+    import ctypes as C
+    from ocelot_gb300 import _native as N
+    from ocelot_gb300.sc import Engine
+    spec = SPECS[2]
+    rp, q = _beam(2, spec)
+    d_rp, d_q = _dev(rp, q)
+    eng = Engine(tuple(spec[1]), "fp32", DEV)
+    b = BeamBatch(DEV)
+    b.add(d_rp, d_q, spec[2], spec[1], spec[6], engine=eng)
+    b.commit()
+    old = eng.ws.data_ptr()
+    eng.ensure(4 * eng.cap)
+    assert eng.ws.data_ptr() != old
+    stream = C.c_void_p(torch.cuda.current_stream(DEV).cuda_stream)
+    assert b.lib.sc_kick_batched(b.handle, stream) == N.SC_ERR_WORKSPACE
+    assert b.launches == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(d_rp.cpu().numpy(), rp)          # nothing ran
+    b.kick()
+    torch.cuda.synchronize()
+    b.check()
+    assert np.array_equal(d_rp.cpu().numpy(), _alone(rp, q, spec))
+
+
+def test_graph_fixes_the_table_shape():
+    """After a kick is recorded as a graph, a table of another shape (a beam's
+    kick length set to zero removes it from the kick stages) is refused;
+    a table of the same shape with other kick lengths is accepted, and a
+    replay kicks with the new lengths."""
+    beams = [(*_beam(i, s), s) for i, s in enumerate(SPECS[:3])]
+    b = BeamBatch(DEV)
+    tensors = []
+    for rp, q, spec in beams:
+        d_rp, d_q = _dev(rp, q)
+        tensors.append(d_rp)
+        b.add(d_rp, d_q, spec[2], spec[1], spec[6])
+    g = b.graph()
+    b.set_step(1, 0.0)
+    with pytest.raises(ValueError, match=r"\[sc error 1\]"):
+        b.commit()
+    half = [s[:6] + (s[6] / 2,) for _, _, s in beams]
+    for i, s in enumerate(half):
+        b.set_step(i, s[6])
+    g.replay()
+    torch.cuda.synchronize()
+    b.check()
+    for (rp, q, _), s, t in zip(beams, half, tensors):
+        assert np.array_equal(t.cpu().numpy(), _alone(rp, q, s))
