@@ -24,12 +24,14 @@ from __future__ import annotations
 
 import collections
 import dataclasses
+import math
 import time
 
 import numpy as np
 
 from . import _native as N
 from .batch import BeamBatch
+from .globals import m_e_GeV
 from .sc import Engine, plan_mode
 from .track import _lattice_sequence, step_maps
 
@@ -79,6 +81,39 @@ def device_gaussian(spec: BeamSpec, device):
                                spec.sigma_p)):
         buf[row].normal_(0.0, float(sig), generator=g)
     return buf[:, :n], torch.full((n,), spec.charge / n, dtype=torch.float64, device=device)
+
+
+def validate_request(request: Request):
+    """Check a request before it is queued and return its step list.
+
+    Everything a job needs is checked here, on the host, so that no admitted
+    job can fail a later tick for all the jobs batched with it: the beam's
+    shape (rparticles (6, N), q_array of N entries, N >= 1) and energy (above
+    the electron's rest energy, as the kick's gamma needs), the mesh (three
+    dimensions >= 4), and the step list -- the transport map and kick length
+    of every step, which depend only on the line and the energy -- so that a
+    line without steps (a zero-length section) is refused instead of being
+    admitted as a job that never finishes."""
+    b = request.beam
+    if isinstance(b, BeamSpec):
+        n, E = int(b.n), float(b.energy_gev)
+    else:
+        shape = np.shape(b.rparticles)
+        if len(shape) != 2 or shape[0] != 6:
+            raise ValueError(f"rparticles must have shape (6, N), not {shape}")
+        n, E = int(shape[1]), float(b.E)
+        if np.size(b.q_array) != n:
+            raise ValueError(f"q_array has {np.size(b.q_array)} entries for {n} particles")
+    if n < 1:
+        raise ValueError("zero-size array: the space-charge kick needs at least one particle")
+    if not (math.isfinite(E) and E > m_e_GeV):
+        raise ValueError(f"beam energy {E} GeV: must be finite and above the electron rest energy")
+    if len(request.nmesh) != 3 or min(int(v) for v in request.nmesh) < 4:
+        raise ValueError(f"nmesh {request.nmesh}: three dimensions >= 4 needed")
+    steps = step_maps(_lattice_sequence(request.elements), E, request.unit_step, int(request.sc_step))
+    if not steps:
+        raise ValueError("the lattice section has no tracking steps (zero length): nothing to track")
+    return steps
 
 
 class _Job:
@@ -136,21 +171,9 @@ class Server:
     # ---- requests ---------------------------------------------------------
     def submit(self, request: Request, t_arrive: float | None = None) -> int:
         """Queue a request; returns its job id.  ``t_arrive``: its arrival
-        time (time.perf_counter()), now by default."""
-        b = request.beam
-        n = int(b.n) if isinstance(b, BeamSpec) else int(np.shape(b.rparticles)[1])
-        if n < 1:
-            raise ValueError("zero-size array: the space-charge kick needs at least one particle")
-        if len(request.nmesh) != 3 or min(int(v) for v in request.nmesh) < 4:
-            raise ValueError(f"nmesh {request.nmesh}: three dimensions >= 4 needed")
-        # the step list (transport map and kick length of every step) depends
-        # only on the line and the beam energy: built here, so that a line
-        # without steps (a zero-length section) is refused instead of being
-        # admitted as a job that never finishes
-        E = float(b.energy_gev) if isinstance(b, BeamSpec) else float(b.E)
-        steps = step_maps(_lattice_sequence(request.elements), E, request.unit_step, int(request.sc_step))
-        if not steps:
-            raise ValueError("the lattice section has no tracking steps (zero length): nothing to track")
+        time (time.perf_counter()), now by default.  Raises ValueError for a
+        request that ``validate_request`` refuses."""
+        steps = validate_request(request)
         jid = self._next_id
         self._next_id += 1
         job = _Job(jid, request, time.perf_counter() if t_arrive is None else t_arrive)

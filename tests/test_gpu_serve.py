@@ -131,3 +131,16 @@ def test_line_without_steps_is_refused():
     jid = srv.submit(_req(*JOBS[0], cells=1))
     srv.drain(timeout_s=60.0)
     assert srv.result(jid).shape == (6, JOBS[0][0])
+
+
+def test_request_refused_at_submit_leaves_the_server_idle():
+    # validate_request runs at submit: a beam whose q_array does not match its
+    # particles never reaches the batched kernels
+    srv = S.Server(DEV)
+    pa = ParticleArray(64)
+    pa.rparticles[:] = np.random.default_rng(3).standard_normal((6, 64)) * 1e-4
+    pa.q_array = np.full(32, 1e-12)
+    pa.E = 0.13
+    with pytest.raises(ValueError, match="q_array has"):
+        srv.submit(S.Request(pa, S.fodo(1), (15, 15, 15)))
+    assert not srv.busy()
