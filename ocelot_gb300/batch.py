@@ -18,7 +18,7 @@ import ctypes as C
 import math
 
 from . import _native as N
-from .sc import Engine, plan_mode
+from .sc import Engine, check_beam_tensors, cuda_device, plan_mode
 
 
 class BeamBatch:
@@ -43,7 +43,7 @@ class BeamBatch:
         if not torch.cuda.is_available():
             raise N.NativeLibraryError("ocelot_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = N.lib()
-        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.device = cuda_device(device)
         self.mode = plan_mode("fp32", "fixed", igf, fields)
         self.max_beams = int(max_beams)
         h = C.c_void_p()
@@ -78,6 +78,7 @@ class BeamBatch:
         n = int(rparticles.shape[1])
         if n == 0:
             raise ValueError("zero-size array: the space-charge kick needs at least one particle")
+        check_beam_tensors(rparticles, q_array, n, self.device)
         if engine is None:
             engine = Engine(tuple(int(v) for v in nmesh_xyz), "fp32", self.device, self.mode)
         engine.ensure(n)

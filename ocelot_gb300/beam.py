@@ -55,6 +55,13 @@ class DeviceParticleArray:
         self.s = float(s)
         if not (isinstance(rparticles, torch.Tensor) and rparticles.is_cuda and rparticles.dtype == torch.float64):
             raise TypeError("rparticles must be a CUDA float64 tensor")
+        if rparticles.dim() != 2 or rparticles.shape[0] != 6:
+            raise ValueError(f"rparticles must have shape (6, N), not {tuple(rparticles.shape)}")
+        if not (isinstance(q_array, torch.Tensor) and q_array.dtype == torch.float64 and
+                q_array.device == rparticles.device and q_array.dim() == 1 and
+                q_array.numel() == rparticles.shape[1]):
+            raise ValueError(f"q_array must be a float64 vector of {rparticles.shape[1]} charges on "
+                             f"{rparticles.device}")
 
     @classmethod
     def from_host(cls, p_array, device=None, pinned_staging=True):

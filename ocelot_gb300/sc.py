@@ -58,6 +58,34 @@ def _torch():
     return torch
 
 
+def cuda_device(device=None):
+    """``device`` as a CUDA device with its index ("cuda" is the current device)."""
+    torch = _torch()
+    d = torch.device(device) if device is not None else torch.device("cuda")
+    if d.type != "cuda":
+        raise ValueError(f"{d}: the kick runs on a CUDA device")
+    return d if d.index is not None else torch.device("cuda", torch.cuda.current_device())
+
+
+def check_beam_tensors(rp, q, n: int, device):
+    """The kernels read n particles of rparticles [6, >= n] (contiguous rows)
+    and n charges from q: both float64 tensors on ``device``.  Raises before
+    anything is launched when that does not hold."""
+    torch = _torch()
+    if not (isinstance(rp, torch.Tensor) and isinstance(q, torch.Tensor)):
+        raise TypeError("rparticles and q_array must be torch tensors")
+    if rp.dtype != torch.float64 or q.dtype != torch.float64:
+        raise TypeError(f"rparticles and q_array must be float64, not {rp.dtype} / {q.dtype}")
+    if rp.device != device or q.device != device:
+        raise ValueError(f"rparticles ({rp.device}) and q_array ({q.device}) must be on {device}")
+    if rp.dim() != 2 or rp.shape[0] != 6 or rp.shape[1] < n:
+        raise ValueError(f"rparticles must have shape (6, N) with N >= {n}, not {tuple(rp.shape)}")
+    if rp.stride(1) != 1:
+        raise ValueError("rparticles rows must be contiguous")
+    if q.dim() != 1 or q.numel() < n or not q.is_contiguous():
+        raise ValueError(f"q_array must be a contiguous vector of {n} charges, not {tuple(q.shape)}")
+
+
 def _ptr(t) -> C.c_void_p:
     return C.c_void_p(t.data_ptr())
 
@@ -75,7 +103,7 @@ class Engine:
         if not torch.cuda.is_available():
             raise N.NativeLibraryError("ocelot_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = N.lib()
-        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.device = cuda_device(device)
         self.shape = tuple(int(v) for v in shape)
         self.precision = precision
         self.mode = plan_mode(precision) if mode is None else int(mode)
@@ -129,11 +157,10 @@ class Engine:
     def kick(self, rp, q, n: int, energy_gev: float, zstep: float, mesh_scale=math.nan, mesh_shift=math.nan):
         """Launch one kick on the current stream (asynchronous)."""
         torch = _torch()
+        check_beam_tensors(rp, q, n, self.device)
         self.ensure(n)
         self.apply_tuning(n)
         ld = rp.stride(0)
-        if rp.stride(1) != 1:
-            raise ValueError("rparticles rows must be contiguous")
         with torch.cuda.device(self.device):
             N.check(self.lib.sc_kick(self.plan, _ptr(self.ws), self.ws.numel(), _ptr(rp), ld, _ptr(q), n,
                                      float(energy_gev), float(zstep), float(mesh_scale), float(mesh_shift),

@@ -32,7 +32,7 @@ import numpy as np
 from . import _native as N
 from .batch import BeamBatch
 from .globals import m_e_GeV
-from .sc import Engine, plan_mode
+from .sc import Engine, cuda_device, plan_mode
 from .track import _lattice_sequence, step_maps
 
 
@@ -145,7 +145,7 @@ class Server:
                  fields: str = "spectral"):
         import torch
         self.torch = torch
-        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.device = cuda_device(device)
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info(self.device)
             hbm_budget = int(free * 0.8)

@@ -119,8 +119,8 @@ def tune(shape, n: int, precision: str = "fp32", device=None, energy_gev: float 
     {"params": best, "us": {param name: {value: us of those stages}}, "identical": True}.
     Raises if a candidate changes a single bit of the result."""
     import torch
-    from .sc import Engine
-    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    from .sc import Engine, cuda_device
+    dev = cuda_device(device)
     eng = Engine(tuple(int(v) for v in shape), precision, dev, tuned=False)
     eng.ensure(n)
     rp0, q = _beam(n, dev)

@@ -408,6 +408,18 @@ def test_degenerate_beam_raises_and_leaves_particles(n):
     assert np.all(pa.rparticles == 0)
 
 
+def test_short_charge_vector_is_refused_before_any_launch():
+    rp, q = sc_oracle.gaussian_beam(1000, 6)
+    d_rp = torch.from_numpy(rp).to(DEV)
+    sc = SpaceCharge(nmesh_xyz=[15, 15, 15], precision="fp32", device="cuda")
+    with pytest.raises(ValueError, match="q_array"):
+        sc.apply_device(d_rp, torch.from_numpy(q[:999]).to(DEV), 0.130, 0.1)
+    with pytest.raises(ValueError, match="must be on"):
+        sc.apply_device(d_rp, torch.from_numpy(q), 0.130, 0.1)
+    sc.check()
+    assert np.array_equal(d_rp.cpu().numpy(), rp)
+
+
 def test_nonfinite_particle_raises():
     rp, q = sc_oracle.gaussian_beam(1000, 6)
     rp[0, 17] = np.nan
