@@ -46,6 +46,7 @@ extern "C" {
 #define SC_ERR_NONFINITE 5   /* non-finite particle coordinate or momentum (device) */
 #define SC_ERR_UNSUPPORTED 6 /* grid too large for the FFT plan */
 #define SC_ERR_TIMEOUT 7     /* a device-side wait gave up after its iteration limit */
+#define SC_ERR_OOM 8         /* host or device memory for the library's own buffers could not be allocated */
 
 typedef struct sc_plan sc_plan; /* opaque, host-side only */
 

@@ -12,6 +12,8 @@ import threading
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "lib", "libocelot_sc.so")
 
+SC_ABI_VERSION = 1
+
 SC_FP64 = 0
 SC_FP32 = 1
 SC_FP32_SORTED_DEPOSIT = 0x10
@@ -26,6 +28,7 @@ SC_ERR_DEGENERATE = 4
 SC_ERR_NONFINITE = 5
 SC_ERR_UNSUPPORTED = 6
 SC_ERR_TIMEOUT = 7
+SC_ERR_OOM = 8
 
 SC_NSTAGES = 11
 
@@ -42,6 +45,21 @@ SC_KICK_NVARIANTS = 21
 SC_WAIT_FRAME = 0
 SC_WAIT_EXTENT = 1
 SC_WAIT_KICK = 2
+
+# largest mesh (in corners) of the workspace-free sc_sym_kernel_static
+SC_SYM_KERNEL_STATIC_MAX_CORNERS = 524288
+
+# transport records: doubles per packed second-order map (R[36], B[6], the
+# combined coefficients Tc[6][21]) and the slice kinds of sc_slices_apply
+SC_MAP2_DOUBLES = 36 + 6 + 6 * 21
+SC_SLICE_MAP = 0
+SC_SLICE_CAVITY = 1
+SC_SLICE_MAP_PLANAR = 2
+SC_SLICE_MAP_DRIFT = 3
+SC_SLICE_MAP_LINEAR = 4
+
+# doubles per set of beam moments written by sc_moments
+SC_MOMENTS = 21
 
 REGIONS = {"qgrid": 0, "phi": 1, "ex": 2, "ey": 3, "ez": 4, "keys": 5, "status": 6, "first_error": 7, "field": 8,
            "igf": 9}
@@ -153,4 +171,6 @@ def check(code: int) -> None:
         msg = last_error()
         if code in (SC_ERR_ARG, SC_ERR_DEGENERATE, SC_ERR_NONFINITE, SC_ERR_UNSUPPORTED):
             raise ValueError(f"[sc error {code}] {msg}")
+        if code == SC_ERR_OOM:
+            raise MemoryError(f"[sc error {code}] {msg}")
         raise ScError(code, msg)

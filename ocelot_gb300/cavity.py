@@ -23,14 +23,15 @@ from __future__ import annotations
 
 import numpy as np
 
+from . import _native as N
 from .globals import m_e_GeV, speed_of_light
 
-MAP2_DOUBLES = 36 + 6 + 6 * 21
-SLICE_MAP = 0      # SC_SLICE_MAP
-SLICE_CAVITY = 1   # SC_SLICE_CAVITY
-SLICE_MAP_PLANAR = 2   # SC_SLICE_MAP_PLANAR
-SLICE_MAP_DRIFT = 3    # SC_SLICE_MAP_DRIFT
-SLICE_MAP_LINEAR = 4   # SC_SLICE_MAP_LINEAR
+MAP2_DOUBLES = N.SC_MAP2_DOUBLES
+SLICE_MAP = N.SC_SLICE_MAP
+SLICE_CAVITY = N.SC_SLICE_CAVITY
+SLICE_MAP_PLANAR = N.SC_SLICE_MAP_PLANAR
+SLICE_MAP_DRIFT = N.SC_SLICE_MAP_DRIFT
+SLICE_MAP_LINEAR = N.SC_SLICE_MAP_LINEAR
 
 
 def _pair(j, k):

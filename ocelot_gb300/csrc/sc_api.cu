@@ -261,7 +261,8 @@ int sc_report(int code, const char* fmt, ...) {
 }  // namespace ocsc
 
 static int cuda_fail(cudaError_t e, const char* where) {
-    return fail(SC_ERR_CUDA, "%s: %s (%s)", where, cudaGetErrorString(e), cudaGetErrorName(e));
+    return fail(e == cudaErrorMemoryAllocation ? SC_ERR_OOM : SC_ERR_CUDA, "%s: %s (%s)", where,
+                cudaGetErrorString(e), cudaGetErrorName(e));
 }
 
 #define SC_CUDA(call, where)                          \
@@ -367,7 +368,7 @@ int sc_plan_create(sc_plan** out, int nx, int ny, int nz, int mode) {
     SC_CUDA(prepare_green_kernels(p), "kernel attributes");
     SC_CUDA(prepare_particle_kernels(), "kernel attributes");
     sc_plan* h = new (std::nothrow) sc_plan;
-    if (!h) return fail(SC_ERR_ARG, "out of host memory");
+    if (!h) return fail(SC_ERR_OOM, "out of host memory");
     h->p = p;
     h->ws_ready = nullptr;
     h->ws_ready_bytes = 0;
@@ -812,13 +813,13 @@ int sc_batch_create(sc_batch** out, int max_beams) {
     SC_CUDA(prepare_batch_green(), "kernel attributes");
     SC_CUDA(prepare_particle_kernels(), "kernel attributes");
     sc_batch* b = new (std::nothrow) sc_batch;
-    if (!b) return fail(SC_ERR_ARG, "out of host memory");
+    if (!b) return fail(SC_ERR_OOM, "out of host memory");
     memset(b, 0, sizeof *b);
     b->max_beams = max_beams;
     b->ws_seen = new (std::nothrow) BatchWs[max_beams];
     if (!b->ws_seen) {
         delete b;
-        return fail(SC_ERR_ARG, "out of host memory");
+        return fail(SC_ERR_OOM, "out of host memory");
     }
     b->beams_bytes = align_up(sizeof(BatchBeam) * (size_t)max_beams);
     b->start_bytes = sizeof(int) * (size_t)BS_COUNT * (max_beams + 1);
@@ -832,7 +833,7 @@ int sc_batch_create(sc_batch** out, int max_beams) {
     if (!e) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
     if (e) {
         sc_batch_destroy(b);
-        return fail(SC_ERR_CUDA, "sc_batch_create: %s", cudaGetErrorString(e));
+        return cuda_fail(e, "sc_batch_create");
     }
     *out = b;
     return SC_OK;

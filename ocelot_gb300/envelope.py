@@ -15,9 +15,10 @@ from __future__ import annotations
 
 import numpy as np
 
+from . import _native as N
 from .globals import m_e_GeV
 
-MOMENTS = 21  # SC_MOMENTS: count, tau mean/std (bounds), 6 means, 12 central moments
+MOMENTS = N.SC_MOMENTS  # count, tau mean/std (bounds), 6 means, 12 central moments
 _MEANS = ("x", "y", "px", "py", "tau", "p")
 _SECOND = ("xx", "xpx", "pxpx", "yy", "ypy", "pypy", "tautau", "xy", "pxpy", "xpy", "ypx", "pp")
 _S4 = np.array([[0, 0, 1, 0], [0, 0, 0, 1], [-1, 0, 0, 0], [0, -1, 0, 0]], dtype=np.float64)

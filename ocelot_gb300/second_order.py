@@ -31,7 +31,7 @@ import numpy as np
 from . import _native as N
 from .globals import m_e_GeV
 
-MAP2_DOUBLES = 36 + 6 + 6 * 21  # R[36], B[6], then Tc[6][21] (the C ABI's SC_MAP2_DOUBLES)
+MAP2_DOUBLES = N.SC_MAP2_DOUBLES  # R[36], B[6], then Tc[6][21]
 
 
 def _cs(k2: float, L: float):

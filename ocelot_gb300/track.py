@@ -499,7 +499,7 @@ class DeviceTrack:
             self._step_dz = [st.dz for st in slices]
             table = np.concatenate([st.table for st in slices]) if slices else np.zeros((0, 1))
             if table.shape[0] == 0:
-                table = np.zeros((1, 168))
+                table = np.zeros((1, N.SC_MAP2_DOUBLES))
             kinds = np.concatenate([st.kinds for st in slices]) if slices else np.zeros(0, np.int32)
             first = np.cumsum([0] + [st.table.shape[0] for st in slices]).astype(np.int32)
             self.first = torch.from_numpy(first).to(self.dev)

@@ -36,6 +36,24 @@ def test_header_declares_the_api():
         assert must in names
 
 
+def test_header_constants_match_the_bindings():
+    """Every integer constant the header defines (modes, status codes,
+    parameters, regions, limits) has the same value in the Python bindings."""
+    from ocelot_gb300 import _native
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    defs = dict(re.findall(r"^#define\s+(SC_\w+)\s+(0x[0-9a-fA-F]+|\d+)\s*$", text, flags=re.M))
+    assert len(defs) > 20
+    regions = {k: int(v, 0) for k, v in defs.items() if k.startswith("SC_REGION_")}
+    for name, value in defs.items():
+        if name.startswith("SC_REGION_"):
+            continue
+        assert hasattr(_native, name), f"{name} is not in the bindings"
+        assert getattr(_native, name) == int(value, 0), name
+    assert sorted(_native.REGIONS.values()) == sorted(regions.values())
+    assert len({v for k, v in defs.items() if k.startswith("SC_ERR_")}) == \
+        len([k for k in defs if k.startswith("SC_ERR_")])       # distinct status codes
+
+
 def test_library_exports_every_declared_symbol(native):
     lib = native.lib()
     names = _declared()
@@ -44,7 +62,7 @@ def test_library_exports_every_declared_symbol(native):
         assert hasattr(lib, name), name
         assert name in native.SIGNATURES, f"{name} has no ctypes signature"
     assert set(native.SIGNATURES) == set(names)
-    assert lib.sc_abi_version() == 1
+    assert lib.sc_abi_version() == native.SC_ABI_VERSION
 
 
 def test_library_argument_checks_without_gpu(native):
