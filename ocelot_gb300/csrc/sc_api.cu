@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "sc_common.cuh"
+#include "sc_fft_dev.cuh"
 
 namespace ocsc {
 
@@ -173,10 +174,18 @@ __global__ void k_init_ws(ScState* st, Cx<R>* tx, int Mx, Cx<R>* ty, int My, Cx<
         st->igf_h[0] = st->igf_h[1] = st->igf_h[2] = NAN;
         st->ws_magic = WS_MAGIC;
     }
+    // w_M^m, laid out as fft_lines reads it: entry i holds m = i for the
+    // two-step lengths, the stage table's m for the Stockham lengths (entries
+    // past its M - R0 hold w_M^i, unused)
     double s, c;
-    if (i < Mx) { sincospi(2.0 * i / Mx, &s, &c); tx[i] = cx<R>((R)c, (R)-s); }
-    if (i < My) { sincospi(2.0 * i / My, &s, &c); ty[i] = cx<R>((R)c, (R)-s); }
-    if (i < Mz) { sincospi(2.0 * i / Mz, &s, &c); tz[i] = cx<R>((R)c, (R)-s); }
+    auto entry = [&](int M) {
+        const int m = (uses_two_step<R>(M) || i >= M - next_radix(M)) ? i : stage_tw_exponent(M, i);
+        sincospi(2.0 * m / M, &s, &c);
+        return cx<R>((R)c, (R)-s);
+    };
+    if (i < Mx) tx[i] = entry(Mx);
+    if (i < My) ty[i] = entry(My);
+    if (i < Mz) tz[i] = entry(Mz);
     if (dx) {
         if (i < Mx) dx[i] = diff_factor<R>(i, Mx);
         if (i < My) dy[i] = diff_factor<R>(i, My);

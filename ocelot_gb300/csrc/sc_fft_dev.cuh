@@ -5,8 +5,9 @@
 // elements contiguous.  Each stage reads radix-r butterfly inputs with stride
 // L/r, applies the twiddles w^(t*k), does the r-point DFT in registers and
 // writes the outputs in autosorted (Stockham) order into the other buffer, so
-// no bit reversal is needed.  Twiddles come from a per-block copy of
-// tw[m] = exp(-2*pi*i*m/L) in shared memory; the inverse uses their
+// no bit reversal is needed.  Twiddles come from a per-block table in
+// shared memory built from tw[m] = exp(-2*pi*i*m/L) (load_twiddles: one block
+// of entries per stage, read by consecutive lanes); the inverse uses their
 // conjugates and leaves the 1/L normalisation to the caller.
 #pragma once
 #include "sc_common.cuh"
@@ -65,11 +66,12 @@ __device__ __forceinline__ void dft8(Cx<R>* v) {
     v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
 }
 
+// tw: the stage twiddle table of load_twiddles; the stage's block starts at
+// Ns - (the first stage's radix)
 template <typename R, bool INV, int RAD>
 __device__ __forceinline__ void stockham_stage(const Cx<R>* __restrict__ a, Cx<R>* __restrict__ b,
-                                               int L, int ls, int nl, int Ns, const Cx<R>* tw) {
+                                               int L, int ls, int nl, int Ns, const Cx<R>* tw, int tw_off) {
     const int nb = L / RAD;
-    const int step = L / (Ns * RAD);
     const int total = nb * nl;
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
         const int line = idx / nb;
@@ -83,7 +85,7 @@ __device__ __forceinline__ void stockham_stage(const Cx<R>* __restrict__ a, Cx<R
         if (Ns > 1) {
 #pragma unroll
             for (int t = 1; t < RAD; ++t) {
-                Cx<R> w = tw[t * k * step];
+                Cx<R> w = tw[tw_off + (t - 1) * Ns + k];
                 if (INV) w.y = -w.y;
                 v[t] = cmul(v[t], w);
             }
@@ -129,18 +131,29 @@ constexpr int plan_radix(int L, int s) {
     return 0;
 }
 
-// Intermediate stages keep element i of a line at i + i/8: the Stockham
-// output index of the early stages strides by RAD elements per thread, which
-// in the plain layout puts 8 or more threads of a warp on the same bank; with
-// one pad element per 8 the strides spread over all banks.  The first stage
-// reads and the last one writes the plain layout the kernels load and store.
-__device__ __forceinline__ int fft_pad(int i) { return i + (i >> 3); }
+// Intermediate stages keep element i of a line at a padded position: the
+// Stockham output index of the early stages strides by RAD elements per
+// thread, which in the plain layout puts 8 or more threads of a warp on the
+// same bank.  One pad element per 16 (lines of 128 points and more) spreads
+// those strides over all banks and keeps the 16 lanes of a half-warp that
+// read consecutive elements on 16 distinct bank pairs; with one pad per 8 the
+// half-warp's 16 elements spanned 17 slots and its first and last lane met on
+// one bank (a shared-memory model of the stages: 11% fewer wavefronts at 128
+// points, 10% at 512).  Shorter lines keep one pad per 8, which is as good or
+// better there.  The first stage reads and the last one writes the plain
+// layout the kernels load and store; the padded line fits in fft_ls(L).
+template <int L>
+__device__ __forceinline__ int fft_pad(int i) {
+    return L >= 128 ? i + (i >> 4) : i + (i >> 3);
+}
 
+// tw: the stage twiddle table of load_twiddles (this stage's block at
+// NS - plan_radix(L, 0), entry (t - 1) NS + k = w_L^(t k L / (NS RAD)))
 template <typename R, bool INV, int RAD, int L, int NS, bool PIN, bool POUT>
 __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx<R>* __restrict__ b, int ls,
                                                  int nl, const Cx<R>* tw) {
     constexpr int nb = L / RAD;
-    constexpr int step = L / (NS * RAD);
+    constexpr int tw_off = NS - plan_radix(L, 0);
     const int total = nb * nl;
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
         const int line = idx / nb;
@@ -150,11 +163,11 @@ __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx
         Cx<R>* dst = b + line * ls;
         Cx<R> v[RAD];
 #pragma unroll
-        for (int t = 0; t < RAD; ++t) v[t] = src[PIN ? fft_pad(j + t * nb) : j + t * nb];
+        for (int t = 0; t < RAD; ++t) v[t] = src[PIN ? fft_pad<L>(j + t * nb) : j + t * nb];
         if (NS > 1) {
 #pragma unroll
             for (int t = 1; t < RAD; ++t) {
-                Cx<R> w = tw[t * k * step];
+                Cx<R> w = tw[tw_off + (t - 1) * NS + k];
                 if (INV) w.y = -w.y;
                 v[t] = cmul(v[t], w);
             }
@@ -165,7 +178,7 @@ __device__ __forceinline__ void stockham_stage_c(const Cx<R>* __restrict__ a, Cx
         else dft8<R, INV>(v);
         const int out = (j - k) * RAD + k;
 #pragma unroll
-        for (int t = 0; t < RAD; ++t) dst[POUT ? fft_pad(out + t * NS) : out + t * NS] = v[t];
+        for (int t = 0; t < RAD; ++t) dst[POUT ? fft_pad<L>(out + t * NS) : out + t * NS] = v[t];
     }
 }
 
@@ -380,11 +393,11 @@ __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan&
     }
     int Ns = 1;
     for (int s = 0; s < rp.nst; ++s) {
-        const int r = rp.r[s];
-        if (r == 8) stockham_stage<R, INV, 8>(a, b, rp.L, ls, nl, Ns, tw);
-        else if (r == 4) stockham_stage<R, INV, 4>(a, b, rp.L, ls, nl, Ns, tw);
-        else if (r == 3) stockham_stage<R, INV, 3>(a, b, rp.L, ls, nl, Ns, tw);
-        else stockham_stage<R, INV, 2>(a, b, rp.L, ls, nl, Ns, tw);
+        const int r = rp.r[s], off = Ns - rp.r[0];
+        if (r == 8) stockham_stage<R, INV, 8>(a, b, rp.L, ls, nl, Ns, tw, off);
+        else if (r == 4) stockham_stage<R, INV, 4>(a, b, rp.L, ls, nl, Ns, tw, off);
+        else if (r == 3) stockham_stage<R, INV, 3>(a, b, rp.L, ls, nl, Ns, tw, off);
+        else stockham_stage<R, INV, 2>(a, b, rp.L, ls, nl, Ns, tw, off);
         __syncthreads();
         Cx<R>* t = a;
         a = b;
@@ -394,9 +407,45 @@ __device__ Cx<R>* fft_lines(Cx<R>* a, Cx<R>* b, int ls, int nl, const RadixPlan&
     return a;
 }
 
-// The twiddle table of fft_lines in shared memory, from src[m] = w_L^m:
-// the same table for the Stockham passes, tw2[k1 * Q + n2] = w_L^(n2 k1)
-// for the two-step lengths of FP32
+// the radix of the next Stockham stage of a line with rem points left to
+// split (the order of plan_radix / make_radix_plan: a 3 first, then 8s, a 4,
+// a 2)
+__host__ __device__ inline int next_radix(int rem) {
+    return rem % 3 == 0 ? 3 : (rem % 8 == 0 ? 8 : (rem % 4 == 0 ? 4 : 2));
+}
+
+// The Stockham stage twiddle table: one block per stage after the first, in
+// stage order -- the stage of NS points per butterfly group and radix RAD
+// holds w_L^(t k L / (NS RAD)) at (t - 1) NS + k for t = 1 .. RAD - 1, k < NS,
+// and starts at NS - R0 (R0 the first radix; L - R0 entries in all) -- so that
+// lanes with consecutive k read consecutive entries (read from a table of
+// w_L^m by m = t k L / (NS RAD), the 512-point stages put up to 8 lanes on one
+// bank).  stage_tw_exponent gives the m of entry i < L - R0; the workspace's
+// twiddle tables are laid out this way once, when it is initialised.
+__host__ __device__ inline int stage_tw_exponent(int L, int i) {
+    const int r0 = next_radix(L);
+    const int g = i + r0;   // the stage of entry i: NS <= g < NS * RAD
+    int ns = r0, rem = L / r0, r = next_radix(rem);
+    while (ns * r <= g) {
+        ns *= r;
+        rem /= r;
+        r = next_radix(rem);
+    }
+    const int rel = g - ns, t = rel / ns + 1, k = rel - (t - 1) * ns;
+    return t * k * (L / (ns * r));
+}
+
+// Whether a line length of this precision takes the two-step form (its
+// twiddle table then stays w_L^m in the workspace, the stage table otherwise).
+template <typename R>
+__host__ __device__ constexpr bool uses_two_step(int L) {
+    return sizeof(R) == 4 && two_step_q(L) != 0;
+}
+
+// The twiddle table of fft_lines in shared memory (room for L entries) from
+// the workspace's table src: for the two-step lengths of FP32 src[m] = w_L^m
+// and tw2[k1 * Q + n2] = w_L^(n2 k1) is formed here; for the Stockham lengths
+// src already holds the stage table and is copied.
 template <typename R>
 __device__ __forceinline__ void load_twiddles(Cx<R>* dst, const Cx<R>* src, int L) {
     if constexpr (sizeof(R) == 4) {
