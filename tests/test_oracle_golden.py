@@ -49,14 +49,42 @@ def test_oracle_bit_identical_to_reference(path):
 def test_oracle_pinned_to_reference_track_golden():
     """test_track_with_sp: 10k particles, 194 kicks, SecondTM transport.
 
-    The pin itself is made by tests/golden/make_golden.py, which needs the
-    reference checkout; this test checks the recorded outcome.
+    The record tests/golden/make_golden.py wrote when it ran the oracle's
+    kicks inside the reference's own track() (which needs the reference
+    checkout); test_oracle_retracks_the_reference_regression_line recomputes
+    the line here without it.
     """
     s = json.load(open(os.path.join(GOLDEN, "track_pin.json")))
     assert s["n_kicks"] > 100 and s["n_particles"] == 10000
     for k, v in s["oracle_vs_golden_max_abs"].items():
         assert v <= s["tolerance_abs"], (k, v)
     assert s["oracle_pinned"]
+
+
+def test_oracle_retracks_the_reference_regression_line():
+    """test_track_with_sp's line (16 cavities, SecondTM, SpaceCharge with step
+    1 up to the second cavity and step 5 after it; 10k particles, 193 kicks at
+    63^3) tracked again here: the Navigator's schedule and the slice maps on
+    the host (numpy), every kick by the oracle.  The particles must end within
+    the reference test's own tolerance (1e-12 absolute, space_charge_test.py:65)
+    of the reference's own track() of the same beam."""
+    from test_cavity_host import LINE, line_elements, line_procs
+
+    from ocelot_gb300 import cavity as CV
+    from ocelot_gb300 import track as T
+    seq, procs = line_elements(), line_procs()
+    steps = T.navigator_steps([e.l for e in seq], procs, 0.02)
+    slices, _, _ = T.step_slices(seq, float(LINE["E_start"]), steps, order=2)
+    X = np.array(LINE["rp_start"], dtype=np.float64)
+    kicks = 0
+    for st in slices:
+        if len(st.kinds):
+            X = CV.apply_records_numpy(st.table, st.kinds, X)
+        for _, E, zstep in st.kicks:
+            sc_oracle.sc_apply(X, LINE["q"], E, zstep, [63, 63, 63])
+            kicks += 1
+    assert kicks == 193
+    assert np.abs(X - LINE["rp_end"]).max() <= 1e-12
 
 
 def test_track_kick_fixture_replays_on_oracle():
