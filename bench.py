@@ -243,16 +243,17 @@ def host_link(dev, h2d_bytes, d2h_bytes):
 
 # Configurations of the metric timed beside the headline (each a sequence of
 # kicks on a seeded synthetic beam; a step is the whole sequence)
-CONFIG1 = {"key": "config1", "form": "fp64", "n": 200_000, "mesh": [63, 63, 63], "E": 0.130, "charge": 250e-12,
-           "dz": 0.1, "kicks": 10, "beam": "gauss",
-           "workload": "plain FP64 form: 200k particles, 6D Gaussian (sigma_x = sigma_y = 50 um, sigma_x' = "
-                       "sigma_y' = 1e-5, sigma_tau = 100 um, sigma_delta = 1e-4), 130 MeV, 250 pC, 63^3 mesh, "
-                       "10 kicks of 0.1 m"}
-CONFIG3 = {"key": "config3", "form": "fp32", "fields": "spectral", "n": 10_000_000, "mesh": [128, 128, 256],
-           "E": 0.0065, "charge": 500e-12, "dz": 0.05, "kicks": 20, "beam": "flat",
-           "workload": "low-energy stress case, FP32 form with spectral fields: 10M particles at 6.5 MeV, 500 pC, "
-                       "flat-top tau of 2 mm with 100 um Gaussian edges, chirp delta += -10 tau, transverse "
-                       "Gaussian 200 um with a 1 mrad x-tau tilt, 128x128x256 mesh, 20 kicks of 0.05 m"}
+PLAIN_200K_63 = {"key": "config1", "form": "fp64", "n": 200_000, "mesh": [63, 63, 63], "E": 0.130,
+                 "charge": 250e-12, "dz": 0.1, "kicks": 10, "beam": "gauss",
+                 "workload": "plain FP64 form: 200k particles, 6D Gaussian (sigma_x = sigma_y = 50 um, "
+                             "sigma_x' = sigma_y' = 1e-5, sigma_tau = 100 um, sigma_delta = 1e-4), 130 MeV, "
+                             "250 pC, 63^3 mesh, 10 kicks of 0.1 m"}
+STRESS_10M_128X128X256 = {
+    "key": "config3", "form": "fp32", "fields": "spectral", "n": 10_000_000, "mesh": [128, 128, 256],
+    "E": 0.0065, "charge": 500e-12, "dz": 0.05, "kicks": 20, "beam": "flat",
+    "workload": "low-energy stress case, FP32 form with spectral fields: 10M particles at 6.5 MeV, 500 pC, "
+                "flat-top tau of 2 mm with 100 um Gaussian edges, chirp delta += -10 tau, transverse "
+                "Gaussian 200 um with a 1 mrad x-tau tilt, 128x128x256 mesh, 20 kicks of 0.05 m"}
 
 
 def config_beam(cfg, seed=SEED):
@@ -660,7 +661,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip timing the FP64 form")
     ap.add_argument("--no-batch", action="store_true", help="skip the 96-beam batched leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
-    ap.add_argument("--no-configs", action="store_true", help="skip the config 1 and config 3 legs")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the plain 200k / 63^3 FP64 and the 10M / 128x128x256 FP32 legs")
     ap.add_argument("--kick-only", action="store_true",
                     help="time the FP32 kick alone (no other leg): the small case for profiling")
     ap.add_argument("--transport", type=int, default=0, metavar="N",
@@ -752,10 +754,11 @@ def main():
     cpu_threads = None if (args.no_cpu or rank != 0) else threads
     configs = {}
     if not args.no_configs:
-        for cfg in (CONFIG1, CONFIG3):
+        for cfg in (PLAIN_200K_63, STRESS_10M_128X128X256):
             configs[cfg["key"]] = time_config(cfg, 3, 1, dev, flush, cpu_threads)
-        configs["config3"]["fp32_errors_vs_fp64"] = form_errors(CONFIG3, dev, fp32_mode={"fields": "spectral"})
-        configs["config3"]["fp32_difference_fields_errors_vs_fp64"] = form_errors(CONFIG3, dev,
+        configs["config3"]["fp32_errors_vs_fp64"] = form_errors(STRESS_10M_128X128X256, dev,
+                                                                 fp32_mode={"fields": "spectral"})
+        configs["config3"]["fp32_difference_fields_errors_vs_fp64"] = form_errors(STRESS_10M_128X128X256, dev,
                                                                                    fp32_mode={"fields": "difference"})
     batched = None if args.no_batch else time_batched(args.steps, args.warmup, dev)
     serving = None if args.no_serve else time_serving(dev)

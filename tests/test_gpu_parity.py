@@ -149,7 +149,7 @@ def test_reference_regression_kicks_at_reference_tolerance():
         assert np.abs(pa.rparticles - d[f"k{j}_rp_out"]).max() <= 1e-12
 
 
-def test_config1_ten_kicks_vs_oracle():
+def test_plain_200k_63cube_ten_kicks_vs_oracle():
     """200k particles, 63^3, 130 MeV, 250 pC, 10 kicks of 0.1 m: <= 1e-10 per row."""
     rp, q = sc_oracle.gaussian_beam(200_000, 11, charge=250e-12)
     ref = rp.copy()
