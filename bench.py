@@ -303,6 +303,27 @@ def form_errors(cfg, dev, seed=SEED + 1, fp32_mode=None):
     return res
 
 
+def padded_length(n: int) -> int:
+    """The FFT length the library pads a mesh axis of n cells to: the smallest
+    2^k or 3 * 2^k (8 .. 512) holding the linear convolution (>= 2n - 1)."""
+    fits = [L for L in [8 << k for k in range(7)] + [12 << k for k in range(6)] if L >= 2 * n - 1]
+    return min(fits) if fits else 0
+
+
+def fp64_work_per_kick(mesh):
+    """Algorithmic FP64 work of one kick of the plain form, counted by the
+    reference's operations: its potential is three complex 3D FFTs of the
+    padded grid (sc.py:135-168), 5 M log2 M flops each, and its Green's function
+    evaluates 3 arctangents, 3 logarithms and a square root per corner of the
+    (nx+1)(ny+1)(nz+1) lattice (sc.py:109-133).  The library's passes do less
+    than the FFT count (real-to-half-complex transforms, lines that are all
+    padding skipped), so the count is not a rate to hold against the FP64 peak."""
+    M = math.prod(padded_length(int(v)) for v in mesh)
+    return {"fft_flops_reference_count": 3 * 5 * M * math.log2(M),
+            "padded_grid": [padded_length(int(v)) for v in mesh],
+            "igf_transcendentals": 7 * math.prod(int(v) + 1 for v in mesh)}
+
+
 def time_config(cfg, steps, warmup, dev, flush, cpu_threads=None):
     """A configuration's kick sequence, device-resident: every step restores
     the initial beam (outside the timed region), flushes L2 and times the
@@ -354,9 +375,13 @@ def time_config(cfg, steps, warmup, dev, flush, cpu_threads=None):
            "value": n * cfg["kicks"] / t, "unit": "particle-kicks/s", "ms_per_step": t * 1e3,
            "ms_per_kick": t * 1e3 / cfg["kicks"], "gpu_launches": launches, "stages_ms_one_kick": stages,
            "l2": "flushed before each step; the kicks of a step run back to back",
-           "roofline": {"bound": "hbm" if cfg["form"] == "fp32" else "fp64 pipe (see DESIGN)",
+           "roofline": {"bound": "hbm" if cfg["form"] == "fp32" else
+                        "fp64 pipe: every FP64-form kernel with arithmetic keeps it 65-85% busy (ncu); the bytes "
+                        "below are far from the HBM bound",
                         "algorithmic_bytes_per_kick": b_kick, "achieved": achieved, "unit": "GB/s",
                         "peak": peak, "frac": achieved / peak, "peak_kind": peak_kind_text(kind)}}
+    if cfg["form"] == "fp64":
+        out["fp64_work_per_kick"] = fp64_work_per_kick(mesh)
     if cpu_threads:
         from oracle import sc_oracle
         rp_c, q_c = config_beam(cfg)
